@@ -1,0 +1,248 @@
+/*
+ * rxg.h -- C ABI of the GB300-native RXMesh hot path (librxg.so).
+ *
+ * Plain pointers and sizes only.  Every call returns an rxg_status; nothing
+ * exits or aborts.  `stream` is a cudaStream_t passed as void* (NULL = the
+ * legacy default stream).  Unless a function says otherwise, array arguments
+ * may live in device memory or in host memory (pageable or pinned); host
+ * arrays are staged through library-owned device buffers inside the call and
+ * the call returns after the result has landed in the host array.
+ *
+ * Element numbering.  A mesh keeps two numberings for vertices, edges and
+ * faces:
+ *   - input ids: the caller's vertex ids, face ids in input order, and edge
+ *     ids in first-appearance order over faces, (v0,v1),(v1,v2),(v2,v0) per
+ *     face, exactly as RXMesh numbers its global edges
+ *     (include/rxmesh/rxmesh.cpp:518-620);
+ *   - linear ids: patch-ordered ids, owned elements of patch 0 first, then
+ *     patch 1, ... (RXMesh's linear_id, include/rxmesh/context.h:299-331).
+ * Queries and per-element arrays passed to kernels use linear ids; the
+ * rxg_mesh_*_map calls give the permutations and rxg_permute applies them.
+ */
+#ifndef RXG_H
+#define RXG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int rxg_status;
+enum {
+    RXG_OK                 = 0,
+    RXG_ERR_INVALID        = 1, /* bad argument, out-of-range index, size mismatch */
+    RXG_ERR_NOMEM          = 2, /* host or device allocation failed */
+    RXG_ERR_CUDA           = 3, /* a CUDA runtime call failed (message: rxg_last_error) */
+    RXG_ERR_NONMANIFOLD    = 4, /* operation needs an edge- and vertex-manifold mesh */
+    RXG_ERR_PATCH_LIMIT    = 5, /* a patch exceeds the 16-bit local-index limits */
+    RXG_ERR_NOT_CONVERGED  = 6, /* iterative solver hit max_iter (outputs still valid) */
+    RXG_ERR_DEVICE_TIMEOUT = 7, /* a bounded device-side wait gave up */
+    RXG_ERR_UNSUPPORTED    = 8,
+    RXG_ERR_NO_DEVICE      = 9
+};
+
+/* Query operations (RXMesh Op, include/rxmesh/types.h) */
+enum {
+    RXG_OP_VV = 0, /* vertex -> adjacent vertices   (CSR over vertices) */
+    RXG_OP_VE = 1, /* vertex -> incident edges      (CSR over vertices) */
+    RXG_OP_VF = 2, /* vertex -> incident faces      (CSR over vertices) */
+    RXG_OP_FV = 3, /* face   -> 3 vertices          (dense nf x 3)      */
+    RXG_OP_EV = 4  /* edge   -> 2 vertices          (dense ne x 2)      */
+};
+
+enum { RXG_ELEM_VERTEX = 0, RXG_ELEM_EDGE = 1, RXG_ELEM_FACE = 2 };
+enum { RXG_F32 = 0, RXG_F64 = 1 };
+enum { RXG_NORMAL_MAX = 0, RXG_NORMAL_AREA = 1 };
+
+typedef struct rxg_mesh rxg_mesh;
+
+typedef struct rxg_mesh_info {
+    int64_t num_vertices, num_edges, num_faces;
+    int64_t num_patches;
+    int64_t max_valence;
+    int32_t is_closed;          /* every edge has two faces */
+    int32_t is_edge_manifold;   /* no edge has more than two faces */
+    int32_t patch_faces;        /* requested faces per patch */
+    int32_t max_local_vertices; /* largest patch, owned + ribbon */
+    int32_t max_local_edges;
+    int32_t max_local_faces;
+    int64_t ribbon_vertices;    /* sum over patches of not-owned local vertices */
+    int64_t ribbon_faces;
+    int64_t device_bytes;       /* device memory held by the mesh topology */
+} rxg_mesh_info;
+
+/* Status name and the last error message of the calling thread. */
+const char* rxg_status_string(rxg_status s);
+const char* rxg_last_error(void);
+
+/*
+ * Build a static mesh from a triangle list (host arrays).  fv: nf*3 vertex
+ * ids in [0, nv).  Faces are partitioned into patches of at most patch_faces
+ * faces (RXMeshStatic(fv, patcher_file, patch_size), rxmesh_static.h:61-100;
+ * build pipeline rxmesh.cpp:86-225).  Topology is uploaded to the current
+ * CUDA device.
+ */
+rxg_status rxg_mesh_create(const int32_t* fv, int64_t nf, int64_t nv,
+                           int32_t patch_faces, rxg_mesh** out);
+void       rxg_mesh_destroy(rxg_mesh* m);
+
+/* rxg_mesh_create with flags.  RXG_MESH_HOST_ONLY builds the patches on the
+ * host and uploads nothing (for inspecting a partition without a GPU; such a
+ * mesh can only be passed to the rxg_mesh_* introspection calls). */
+enum { RXG_MESH_HOST_ONLY = 1 };
+rxg_status rxg_mesh_create_ex(const int32_t* fv, int64_t nf, int64_t nv,
+                              int32_t patch_faces, int32_t flags, rxg_mesh** out);
+
+/*
+ * Patch layout for inspection: hdr receives num_patches records of 16 int32
+ * {nVo,nVl,nEo,nEl,nFo,nFl, v_base,e_base,f_base, vv_base,vf_base,
+ *  ev_off,fe_off,rv_off,re_off,rf_off}; arena receives *words uint32 words
+ * (EV as u16 pairs, FE as u16 (edge<<1|dir) triples, ribbon -> linear id
+ * tables).  Either may be NULL; *words is always set.  Counterpart of
+ * RXMesh's PatchInfo (include/rxmesh/patch_info.h:24-92).
+ */
+rxg_status rxg_mesh_patches(const rxg_mesh* m, int32_t* hdr, uint32_t* arena,
+                            int64_t* words);
+rxg_status rxg_mesh_get_info(const rxg_mesh* m, rxg_mesh_info* info);
+
+/* lin_to_input (host, n_elem ints): input id of each linear id
+ * (RXMeshStatic::map_to_global, rxmesh_static.h:874-905). */
+rxg_status rxg_mesh_linear_to_input(const rxg_mesh* m, int32_t elem,
+                                    int32_t* lin_to_input);
+/* Input-numbered edge list (host, ne*2), RXMesh's m_edges_map order. */
+rxg_status rxg_mesh_input_edges(const rxg_mesh* m, int32_t* ev);
+
+/*
+ * Gather/scatter between input and linear order for per-element arrays of
+ * `ncomp` components of `dtype` (RXG_F32/RXG_F64).  to_linear=1: dst[lin] =
+ * src[input(lin)], else dst[input(lin)] = src[lin].  Device arrays only.
+ * Replaces Attribute construction from / export to input order
+ * (rxmesh_static.h:608-793, attribute.h:326-390).
+ */
+rxg_status rxg_permute(const rxg_mesh* m, int32_t elem, int32_t to_linear,
+                       int32_t dtype, int32_t ncomp, const void* src, void* dst,
+                       void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Queries (Query<blockThreads>::dispatch, query.h:21-75;               */
+/* RXMeshStatic::for_each<Op>, rxmesh_static.h:524-566)                 */
+/* ------------------------------------------------------------------ */
+
+/* Sizes of a query's output: rows (V, V, V, F, E) and values (2E, 2E, 3F, 3F, 2E). */
+rxg_status rxg_query_size(const rxg_mesh* m, int32_t op, int64_t* n_rows,
+                          int64_t* n_values);
+
+/*
+ * Materialise a query for every owned element, in linear ids.  For VV/VE/VF,
+ * offsets has n_rows+1 entries (CSR, row = linear vertex id); for FV/EV
+ * offsets may be NULL (fixed 3 or 2 entries per row).  Order inside a row is
+ * unspecified (RXMesh compares rows as sets, tests/RXMesh_test/rxmesh_test.h:347-440).
+ */
+rxg_status rxg_query(const rxg_mesh* m, int32_t op, int32_t* offsets,
+                     int32_t* values, void* stream);
+
+/*
+ * Oriented VV (Query::dispatch<Op::VV>(..., oriented=true),
+ * rxmesh_queries.cuh:376-499): each row lists the one-ring in the rotational
+ * order of the incident faces.  A boundary vertex's row starts and ends at
+ * its two boundary neighbours and gets boundary[v]=1 (boundary may be NULL).
+ * Needs a manifold mesh.
+ */
+rxg_status rxg_query_oriented_vv(const rxg_mesh* m, int32_t* offsets,
+                                 int32_t* values, int8_t* boundary,
+                                 void* stream);
+
+/*
+ * Per-vertex normals in linear order, FP32.  weighting RXG_NORMAL_MAX:
+ * sum over faces of n_f/(|e_a|^2+|e_b|^2) (compute_vertex_normal,
+ * apps/VertexNormal/vertex_normal_kernel.cuh:10-43); RXG_NORMAL_AREA: sum of
+ * the unnormalised face normals.  xyz, out: nv*3 floats, linear order.
+ */
+rxg_status rxg_vertex_normals(const rxg_mesh* m, int32_t weighting,
+                              const float* xyz, float* out, void* stream);
+
+/*
+ * Synchronise `stream`, then read and clear the device error word that
+ * bounded device-side waits set instead of hanging (RXG_ERR_DEVICE_TIMEOUT,
+ * RXG_ERR_NONMANIFOLD).  No reference counterpart: RXMesh device code uses
+ * assert (e.g. kernels/rxmesh_queries.cuh:60-95).
+ */
+rxg_status rxg_device_check(void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Cotangent Laplacian, SpMV, CG/PCG, implicit MCF                      */
+/* ------------------------------------------------------------------ */
+
+/* CSR matrix in linear vertex order, diagonal first in each row
+ * (SparseMatrix<T>(rx, Op::VV), sparse_matrix.h:77-78,133-241). */
+typedef struct rxg_csr {
+    int64_t  n;       /* rows = cols */
+    int64_t  nnz;
+    int32_t* row_ptr; /* device, n+1 */
+    int32_t* col;     /* device, nnz */
+    void*    val;     /* device, nnz of dtype */
+    int32_t  dtype;   /* RXG_F32 or RXG_F64 */
+} rxg_csr;
+
+/* Number of rows and non-zeros of the mesh's VV+diagonal pattern. */
+rxg_status rxg_mcf_pattern_size(const rxg_mesh* m, int64_t* n, int64_t* nnz);
+
+/*
+ * Assemble the implicit-MCF system of mcf_A_setup / mcf_B_setup
+ * (apps/MCF/mcf_kernels.cuh:302-426, cotangent weights of
+ * geometry_util.cuh:107-206): A = 2M + dt*L, B = 2M x.  xyz: nv*3 FP64,
+ * linear order, device.  A must have row_ptr/col/val of the pattern size
+ * (they are filled); B: nv*3 of A.dtype (may be NULL).  dtype RXG_F32
+ * computes weights in FP32, except for triangles with an angle below 1e-3
+ * rad, which are computed in FP64.
+ */
+rxg_status rxg_mcf_assemble(const rxg_mesh* m, double dt, const double* xyz,
+                            rxg_csr* A, void* B, void* stream);
+
+/* Y = A X for nc right-hand sides (row-major n x nc, nc <= 4), dtype of A.
+ * (SparseMatrix::multiply, sparse_matrix.h:1173-1263) */
+rxg_status rxg_spmm(const rxg_csr* A, int32_t nc, const void* X, void* Y,
+                    void* stream);
+
+typedef struct rxg_solver_opts {
+    int32_t max_iter;
+    double  abs_tol;  /* on delta = |r|^2 (CG) or r.z (PCG) */
+    double  rel_tol;  /* on delta / delta_0 */
+    int32_t precond;  /* 0 = CG, 1 = Jacobi PCG */
+} rxg_solver_opts;
+
+typedef struct rxg_solver_stats {
+    int32_t iters;      /* completed iterations (CGSolver::iter_taken) */
+    int32_t converged;
+    double  start_res;  /* delta_0 */
+    double  final_res;  /* final delta */
+} rxg_solver_stats;
+
+/*
+ * Solve A X = B (nc columns as one long vector), X in/out as the initial
+ * guess.  CGSolver / PCGSolver::pre_solve+solve (cg_solver.h:37-125,
+ * pcg_solver.h:34-144, iterative_solver.h:52-58).  All scalars stay on the
+ * device; the host reads only the final statistics.  Device arrays only.
+ */
+rxg_status rxg_cg_solve(const rxg_csr* A, int32_t nc, const void* B, void* X,
+                        const rxg_solver_opts* opts, rxg_solver_stats* stats,
+                        void* stream);
+
+/*
+ * One or more implicit MCF steps in place on xyz (nv*3 FP64, linear order,
+ * device or host).  precision RXG_F64: the plain path (FP64 assembly, FP64
+ * PCG).  RXG_F32: FP32 assembly and FP32 PCG inside an iterative-refinement
+ * loop whose residual is recomputed in FP64.  Stops when the FP64 relative
+ * residual |B - A x| / |B - A x_start| < tol (or max_iter PCG iterations).
+ * stats (may be NULL) receives the totals of the last step.
+ * (mcf(), apps/MCF/mcf.cu:93-134, run_cg apps/MCF/mcf_cg.h:12-129)
+ */
+rxg_status rxg_mcf_step(const rxg_mesh* m, double dt, int32_t nsteps,
+                        int32_t precision, double tol, int32_t max_iter,
+                        double* xyz, rxg_solver_stats* stats, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RXG_H */

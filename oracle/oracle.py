@@ -1,0 +1,231 @@
+"""ctypes wrapper over oracle/_build/liboracle.so (the CPU restatement).
+
+TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's CPU
+legs are the only users.  Every function documents the reference routine it
+restates in rxg_oracle.c.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_REF = None
+
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+i8p = np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+I64 = ctypes.c_int64
+
+
+def build():
+    """Compile the oracle (and oracle/_ref when the reference tree exists)."""
+    subprocess.check_call(["make", "-s", "-C", _HERE], stdout=subprocess.DEVNULL)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "_build", "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = ctypes.CDLL(path)
+        L.orc_build_edges.restype = I64
+        L.orc_build_edges.argtypes = [I64, i32p, i32p, i32p]
+        L.orc_vv_ve.argtypes = [I64, I64, i32p, ctypes.c_int, i64p, i32p]
+        L.orc_vf.argtypes = [I64, I64, i32p, i64p, i32p]
+        L.orc_vertex_normals.argtypes = [I64, I64, i32p, f64p, ctypes.c_int, f64p]
+        L.orc_oriented_vv.restype = ctypes.c_int
+        L.orc_oriented_vv.argtypes = [I64, i32p, i64p, i32p, i64p, i32p, i8p]
+        L.orc_mcf_assemble.argtypes = [I64, i64p, i32p, i8p, f64p, ctypes.c_double,
+                                       i64p, i32p, f64p, f64p]
+        L.orc_cg.restype = ctypes.c_int
+        L.orc_cg.argtypes = [I64, ctypes.c_int, i64p, i32p, f64p, f64p, f64p,
+                             ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                             ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                             ctypes.POINTER(ctypes.c_double)]
+        L.orc_spmm.argtypes = [I64, ctypes.c_int, i64p, i32p, f64p, f64p, f64p]
+        L.orc_rest_frame.argtypes = [I64, i32p, f64p, f64p, f64p]
+        L.orc_arap_face.restype = ctypes.c_double
+        L.orc_arap_face.argtypes = [f64p, f64p, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_arap_assemble.restype = ctypes.c_double
+        L.orc_arap_assemble.argtypes = [I64, I64, i32p, f64p, f64p, f64p, i64p, i32p,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_partial_voronoi_area.restype = ctypes.c_double
+        L.orc_partial_voronoi_area.argtypes = [f64p, f64p, f64p]
+        L.orc_half_cot.restype = ctypes.c_double
+        L.orc_half_cot.argtypes = [f64p, f64p, f64p]
+        _LIB = L
+    return _LIB
+
+
+def ref_lib():
+    """The reference's own vertex_normal_ref compiled from its source, or None."""
+    global _REF
+    if _REF is None:
+        path = os.path.join(_HERE, "_ref", "libref_normals.so")
+        if not os.path.exists(path):
+            return None
+        try:
+            R = ctypes.CDLL(path)
+        except OSError:
+            return None
+        R.ref_vertex_normal_f32.argtypes = [I64, I64, i32p, f32p, f32p]
+        R.ref_vertex_normal_f64.argtypes = [I64, I64, i32p, f64p, f64p]
+        _REF = R
+    return _REF
+
+
+def _fv(fv):
+    return np.ascontiguousarray(fv, dtype=np.int32).reshape(-1)
+
+
+def edges(fv):
+    """Reference edge numbering (rxmesh.cpp:518-620). Returns (ev[ne,2], fe[nf,3])."""
+    f = _fv(fv)
+    nf = f.size // 3
+    ev = np.empty(6 * nf, np.int32)
+    fe = np.empty(3 * nf, np.int32)
+    ne = lib().orc_build_edges(nf, f, ev, fe)
+    if ne < 0:
+        raise MemoryError("oracle edge map")
+    return ev[: 2 * ne].reshape(-1, 2).copy(), fe.reshape(-1, 3)
+
+
+def vv(nv, ev, want_edges=False):
+    """Sorted VV (or VE) rows as CSR (off int64[nv+1], val int32)."""
+    e = np.ascontiguousarray(ev, np.int32).reshape(-1)
+    off = np.empty(nv + 1, np.int64)
+    val = np.empty(e.size, np.int32)
+    lib().orc_vv_ve(nv, e.size // 2, e, int(want_edges), off, val)
+    return off, val
+
+
+def vf(nv, fv):
+    """Sorted VF rows as CSR."""
+    f = _fv(fv)
+    off = np.empty(nv + 1, np.int64)
+    val = np.empty(f.size, np.int32)
+    lib().orc_vf(nv, f.size // 3, f, off, val)
+    return off, val
+
+
+def vertex_normals(fv, xyz, weighting=0):
+    """weighting 0 = Max weights (vertex_normal_ref.h), 1 = area weights."""
+    f = _fv(fv)
+    x = np.ascontiguousarray(xyz, np.float64).reshape(-1)
+    out = np.empty_like(x)
+    lib().orc_vertex_normals(x.size // 3, f.size // 3, f, x, int(weighting), out)
+    return out.reshape(-1, 3)
+
+
+def ref_vertex_normals(fv, xyz, dtype=np.float32):
+    """Run the reference's own vertex_normal_ref, if compiled here."""
+    R = ref_lib()
+    if R is None:
+        return None
+    f = _fv(fv)
+    x = np.ascontiguousarray(xyz, dtype).reshape(-1)
+    out = np.empty_like(x)
+    fn = R.ref_vertex_normal_f32 if dtype == np.float32 else R.ref_vertex_normal_f64
+    fn(x.size // 3, f.size // 3, f, x, out)
+    return out.reshape(-1, 3)
+
+
+def oriented_vv(nv, fv):
+    """Oriented one-ring CSR + boundary flags (rxmesh_queries.cuh:376-499)."""
+    f = _fv(fv)
+    voff, vval = vf(nv, f)
+    off = np.empty(nv + 1, np.int64)
+    val = np.empty(2 * f.size, np.int32)  # 2E <= 6F (open meshes have 2E > 3F)
+    bnd = np.empty(nv, np.int8)
+    rc = lib().orc_oriented_vv(nv, f, voff, vval, off, val, bnd)
+    if rc != 0:
+        raise ValueError("non-manifold vertex fan")
+    return off, val[: off[-1]].copy(), bnd
+
+
+def mcf_system(fv, xyz, dt, ring=None):
+    """(row_ptr, col, val, B) of the MCF system (mcf_kernels.cuh:302-426)."""
+    x = np.ascontiguousarray(xyz, np.float64).reshape(-1)
+    nv = x.size // 3
+    if ring is None:
+        ring = oriented_vv(nv, fv)
+    off, rv, bnd = ring
+    nnz = int(off[-1]) + nv
+    rp = np.empty(nv + 1, np.int64)
+    col = np.empty(nnz, np.int32)
+    val = np.empty(nnz, np.float64)
+    B = np.empty(3 * nv, np.float64)
+    lib().orc_mcf_assemble(nv, off, np.ascontiguousarray(rv, np.int32), bnd, x,
+                           float(dt), rp, col, val, B)
+    return rp, col, val, B.reshape(-1, 3)
+
+
+def cg(rp, col, val, B, X0, max_iter=1000, abs_tol=1e-6, rel_tol=0.0, precond=False):
+    """CGSolver/PCGSolver recurrence (cg_solver.h:37-125, pcg_solver.h:34-144).
+
+    Returns (X, iters, start_res, final_res, converged)."""
+    Bm = np.ascontiguousarray(B, np.float64)
+    nc = Bm.shape[1] if Bm.ndim == 2 else 1
+    n = rp.size - 1
+    X = np.ascontiguousarray(X0, np.float64).reshape(-1).copy()
+    it = ctypes.c_int(0)
+    r0 = ctypes.c_double(0)
+    r1 = ctypes.c_double(0)
+    conv = lib().orc_cg(n, nc, np.ascontiguousarray(rp, np.int64), np.ascontiguousarray(col, np.int32),
+                        np.ascontiguousarray(val, np.float64), Bm.reshape(-1), X, int(max_iter),
+                        float(abs_tol), float(rel_tol), int(bool(precond)),
+                        ctypes.byref(it), ctypes.byref(r0), ctypes.byref(r1))
+    return X.reshape(Bm.shape), it.value, r0.value, r1.value, bool(conv)
+
+
+def spmm(rp, col, val, X):
+    Xm = np.ascontiguousarray(X, np.float64)
+    nc = Xm.shape[1] if Xm.ndim == 2 else 1
+    Y = np.empty_like(Xm).reshape(-1)
+    lib().orc_spmm(rp.size - 1, nc, np.ascontiguousarray(rp, np.int64),
+                   np.ascontiguousarray(col, np.int32), np.ascontiguousarray(val, np.float64),
+                   Xm.reshape(-1), Y)
+    return Y.reshape(Xm.shape)
+
+
+def rest_frame(fv, xyz_rest):
+    """Per-face Mr^{-1} (nf,2,2) and rest area (param.cu:113-141)."""
+    f = _fv(fv)
+    x = np.ascontiguousarray(xyz_rest, np.float64).reshape(-1)
+    nf = f.size // 3
+    minv = np.empty(4 * nf, np.float64)
+    area = np.empty(nf, np.float64)
+    lib().orc_rest_frame(nf, f, x, minv, area)
+    return minv.reshape(nf, 2, 2), area
+
+
+def arap_face(x9, minv, area, want_hess=True):
+    x = np.ascontiguousarray(x9, np.float64).reshape(9)
+    m = np.ascontiguousarray(minv, np.float64).reshape(4)
+    g = np.empty(9, np.float64)
+    H = np.empty(81, np.float64)
+    E = lib().orc_arap_face(x, m, float(area), g.ctypes.data, H.ctypes.data if want_hess else None)
+    return E, g, H.reshape(9, 9)
+
+
+def arap_assemble(fv, x, minv, area, rp, col, want_hess=True):
+    """Total energy, per-face energy, gradient (nv,3), Hessian blocks (nnz,3,3)."""
+    f = _fv(fv)
+    xx = np.ascontiguousarray(x, np.float64).reshape(-1)
+    nv = xx.size // 3
+    nf = f.size // 3
+    fe = np.empty(nf, np.float64)
+    g = np.empty(3 * nv, np.float64)
+    nnz = int(rp[-1])
+    H = np.empty(9 * nnz, np.float64) if want_hess else None
+    E = lib().orc_arap_assemble(nv, nf, f, xx, np.ascontiguousarray(minv, np.float64).reshape(-1),
+                                np.ascontiguousarray(area, np.float64), np.ascontiguousarray(rp, np.int64),
+                                np.ascontiguousarray(col, np.int32), fe.ctypes.data, g.ctypes.data,
+                                H.ctypes.data if want_hess else None)
+    return E, fe, g.reshape(nv, 3), (H.reshape(nnz, 3, 3) if want_hess else None)

@@ -1,0 +1,202 @@
+"""rxmesh_gb300: GB300-native RXMesh hot path (host-side mirror of the reference API).
+
+Names follow the reference: RXMeshStatic (include/rxmesh/rxmesh_static.h),
+Op (include/rxmesh/types.h), SparseMatrix (matrix/sparse_matrix.h), CGSolver /
+PCGSolver (matrix/cg_solver.h, pcg_solver.h).  All compute goes through the C
+ABI of librxg.so (include/rxg.h); device memory and streams come from torch.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import RXGError, check
+
+__all__ = ["Op", "RXMeshStatic", "SparseMatrix", "CGSolver", "PCGSolver", "RXGError",
+           "device_check"]
+
+
+class Op:
+    """Query operations (RXMesh's Op enum, include/rxmesh/types.h)."""
+    VV, VE, VF, FV, EV = 0, 1, 2, 3, 4
+    NAMES = {"VV": 0, "VE": 1, "VF": 2, "FV": 3, "EV": 4}
+
+
+_ELEM = {"v": 0, "vertex": 0, "e": 1, "edge": 1, "f": 2, "face": 2}
+_DT = {torch.float32: 0, torch.float64: 1}
+
+
+def _stream(stream=None):
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def device_check(stream=None):
+    """Sync and read the device error word (rxg_device_check)."""
+    L = _lib.load()
+    check(L.rxg_device_check(_stream(stream)))
+
+
+class RXMeshStatic:
+    """Static triangle mesh split into patches (RXMeshStatic, rxmesh_static.h:61-100).
+
+    fv: (nf, 3) int array of input vertex ids.  patch_size: faces per patch.
+    The patch topology lives on the current CUDA device unless host_only.
+    """
+
+    def __init__(self, fv, num_vertices=None, patch_size=512, host_only=False):
+        L = _lib.load()
+        f = np.ascontiguousarray(fv, dtype=np.int32).reshape(-1, 3)
+        nv = int(f.max()) + 1 if num_vertices is None else int(num_vertices)
+        self._fv = f
+        h = ctypes.c_void_p()
+        check(L.rxg_mesh_create_ex(f.ctypes.data, f.shape[0], nv, int(patch_size),
+                                   1 if host_only else 0, ctypes.byref(h)))
+        self._h = h
+        self._L = L
+        self.host_only = host_only
+        info = _lib.MeshInfo()
+        check(L.rxg_mesh_get_info(h, ctypes.byref(info)))
+        self.info = {k: getattr(info, k) for k, _ in info._fields_}
+        self._maps = {}
+        self._dmaps = {}
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._L.rxg_mesh_destroy(h)
+            self._h = None
+
+    # ---- sizes (get_num_vertices & co., rxmesh.h) ---------------------
+    def get_num_vertices(self):
+        return self.info["num_vertices"]
+
+    def get_num_edges(self):
+        return self.info["num_edges"]
+
+    def get_num_faces(self):
+        return self.info["num_faces"]
+
+    def get_num_patches(self):
+        return self.info["num_patches"]
+
+    def is_closed(self):
+        return bool(self.info["is_closed"])
+
+    def is_edge_manifold(self):
+        return bool(self.info["is_edge_manifold"])
+
+    def _n(self, elem):
+        return (self.get_num_vertices(), self.get_num_edges(), self.get_num_faces())[elem]
+
+    # ---- numbering ------------------------------------------------------
+    def linear_to_input(self, elem="v"):
+        """Input id of every linear id (map_to_global, rxmesh_static.h:874-905)."""
+        e = _ELEM[elem]
+        if e not in self._maps:
+            out = np.empty(self._n(e), np.int32)
+            check(self._L.rxg_mesh_linear_to_input(self._h, e, out.ctypes.data))
+            self._maps[e] = out
+        return self._maps[e]
+
+    def input_to_linear(self, elem="v"):
+        m = self.linear_to_input(elem)
+        inv = np.empty_like(m)
+        inv[m] = np.arange(m.size, dtype=np.int32)
+        return inv
+
+    def input_edges(self):
+        """(ne, 2) edge list in RXMesh's global edge order (rxmesh.cpp:518-620)."""
+        out = np.empty(2 * self.get_num_edges(), np.int32)
+        check(self._L.rxg_mesh_input_edges(self._h, out.ctypes.data))
+        return out.reshape(-1, 2)
+
+    def patches(self):
+        """(headers (np, 16) int32, arena uint32) of the patch layout."""
+        words = ctypes.c_int64()
+        check(self._L.rxg_mesh_patches(self._h, None, None, ctypes.byref(words)))
+        hdr = np.empty((self.get_num_patches(), 16), np.int32)
+        arena = np.empty(words.value, np.uint32)
+        check(self._L.rxg_mesh_patches(self._h, hdr.ctypes.data, arena.ctypes.data,
+                                       ctypes.byref(words)))
+        return hdr, arena
+
+    def to_linear(self, t, elem="v", stream=None):
+        """Device tensor in input order -> new device tensor in linear order."""
+        return self._permute(t, elem, 1, stream)
+
+    def to_input(self, t, elem="v", stream=None):
+        """Device tensor in linear order -> new device tensor in input order."""
+        return self._permute(t, elem, 0, stream)
+
+    def _permute(self, t, elem, to_linear, stream):
+        e = _ELEM[elem]
+        t = t.contiguous()
+        if t.shape[0] != self._n(e) or t.dtype not in _DT or not t.is_cuda:
+            raise ValueError("expected a CUDA float32/float64 tensor with %d rows" % self._n(e))
+        out = torch.empty_like(t)
+        ncomp = t.numel() // max(1, t.shape[0])
+        check(self._L.rxg_permute(self._h, e, to_linear, _DT[t.dtype], ncomp, _ptr(t), _ptr(out),
+                                  _stream(stream)))
+        return out
+
+    # ---- queries (Query::dispatch / for_each<Op>) -------------------------
+    def query_size(self, op):
+        rows, vals = ctypes.c_int64(), ctypes.c_int64()
+        check(self._L.rxg_query_size(self._h, int(op), ctypes.byref(rows), ctypes.byref(vals)))
+        return rows.value, vals.value
+
+    def query(self, op, stream=None, offsets=None, values=None):
+        """Materialise query `op` for all owned elements, in linear ids.
+
+        Returns (offsets, values) int32 CUDA tensors; offsets is None for FV/EV
+        (3 or 2 values per row)."""
+        op = Op.NAMES.get(op, op) if isinstance(op, str) else int(op)
+        rows, nval = self.query_size(op)
+        dev = torch.device("cuda", torch.cuda.current_device())
+        csr = op <= Op.VF
+        if csr and offsets is None:
+            offsets = torch.empty(rows + 1, dtype=torch.int32, device=dev)
+        if values is None:
+            values = torch.empty(nval, dtype=torch.int32, device=dev)
+        check(self._L.rxg_query(self._h, op, _ptr(offsets) if csr else None, _ptr(values),
+                                _stream(stream)))
+        return (offsets if csr else None), values
+
+    def query_host(self, op, offsets, values):
+        """Same as query() into host numpy arrays (copies inside the call)."""
+        check(self._L.rxg_query(self._h, int(op),
+                                offsets.ctypes.data if offsets is not None else None,
+                                values.ctypes.data, None))
+        return offsets, values
+
+    def query_oriented_vv(self, stream=None):
+        """Oriented one-ring (rxmesh_queries.cuh:376-499): (offsets, values, boundary)."""
+        nv = self.get_num_vertices()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        off = torch.empty(nv + 1, dtype=torch.int32, device=dev)
+        val = torch.empty(2 * self.get_num_edges(), dtype=torch.int32, device=dev)
+        bnd = torch.empty(nv, dtype=torch.int8, device=dev)
+        check(self._L.rxg_query_oriented_vv(self._h, _ptr(off), _ptr(val), _ptr(bnd),
+                                            _stream(stream)))
+        return off, val, bnd
+
+    def vertex_normals(self, xyz, weighting="max", stream=None, out=None):
+        """Vertex normals (linear order, FP32) of linear-order positions xyz (nv, 3)."""
+        w = {"max": 0, "area": 1}[weighting] if isinstance(weighting, str) else int(weighting)
+        xyz = xyz.contiguous()
+        if xyz.dtype != torch.float32 or not xyz.is_cuda or xyz.numel() != 3 * self.get_num_vertices():
+            raise ValueError("xyz must be a CUDA float32 tensor of shape (nv, 3)")
+        if out is None:
+            out = torch.empty_like(xyz)
+        check(self._L.rxg_vertex_normals(self._h, w, _ptr(xyz), _ptr(out), _stream(stream)))
+        return out
+
+
+from ._solvers import SparseMatrix, CGSolver, PCGSolver, mcf_step  # noqa: E402

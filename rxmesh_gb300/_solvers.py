@@ -1,0 +1,147 @@
+"""SparseMatrix / CGSolver / PCGSolver / mcf_step over the C ABI.
+
+Mirrors include/rxmesh/matrix/sparse_matrix.h (SparseMatrix<T>(rx, Op::VV)),
+matrix/cg_solver.h and matrix/pcg_solver.h; mcf_step mirrors the MCF app's
+run_cg (apps/MCF/mcf_cg.h:12-129).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, RXGError
+
+_DT = {torch.float32: 0, torch.float64: 1}
+
+
+def _stream(stream=None):
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class SparseMatrix:
+    """CSR matrix in linear vertex order, diagonal first (SparseMatrix<T>, sparse_matrix.h:77)."""
+
+    def __init__(self, rx=None, dtype=torch.float64, row_ptr=None, col=None, val=None):
+        self._L = _lib.load()
+        if rx is not None:
+            n, nnz = ctypes.c_int64(), ctypes.c_int64()
+            check(self._L.rxg_mcf_pattern_size(rx._h, ctypes.byref(n), ctypes.byref(nnz)))
+            dev = torch.device("cuda", torch.cuda.current_device())
+            self.row_ptr = torch.zeros(n.value + 1, dtype=torch.int32, device=dev)
+            self.col = torch.zeros(nnz.value, dtype=torch.int32, device=dev)
+            self.val = torch.zeros(nnz.value, dtype=dtype, device=dev)
+        else:
+            self.row_ptr, self.col, self.val = row_ptr.contiguous(), col.contiguous(), val.contiguous()
+        self.rx = rx
+
+    @property
+    def dtype(self):
+        return self.val.dtype
+
+    def rows(self):
+        return self.row_ptr.numel() - 1
+
+    def cols(self):
+        return self.rows()
+
+    def csr(self):
+        c = _lib.CSR()
+        c.n = self.rows()
+        c.nnz = self.col.numel()
+        c.row_ptr = self.row_ptr.data_ptr()
+        c.col = self.col.data_ptr()
+        c.val = self.val.data_ptr()
+        c.dtype = _DT[self.val.dtype]
+        return c
+
+    def multiply(self, X, Y=None, stream=None):
+        """Y = A X (sparse_matrix.h:1173-1263); X is (n, nc) of the matrix dtype."""
+        X = X.contiguous()
+        nc = 1 if X.dim() == 1 else X.shape[1]
+        if Y is None:
+            Y = torch.empty_like(X)
+        c = self.csr()
+        check(self._L.rxg_spmm(ctypes.byref(c), nc, _ptr(X), _ptr(Y), _stream(stream)))
+        return Y
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        n = self.rows()
+        return sp.csr_matrix((self.val.cpu().numpy(), self.col.cpu().numpy(),
+                              self.row_ptr.cpu().numpy()), shape=(n, n))
+
+
+def mcf_assemble(rx, xyz_lin, dt, dtype=torch.float64, stream=None):
+    """(A, B) of the MCF system (mcf_A_setup / mcf_B_setup) at linear positions xyz_lin."""
+    A = SparseMatrix(rx, dtype)
+    B = torch.empty((rx.get_num_vertices(), 3), dtype=dtype, device=A.val.device)
+    c = A.csr()
+    x = xyz_lin.to(torch.float64).contiguous()
+    check(A._L.rxg_mcf_assemble(rx._h, float(dt), _ptr(x), ctypes.byref(c), _ptr(B), _stream(stream)))
+    return A, B
+
+
+class CGSolver:
+    """CGSolver(A, unknown_dim, max_iter, abs_tol, rel_tol) (cg_solver.h:17-35)."""
+    PRECOND = 0
+
+    def __init__(self, A, unknown_dim, max_iter, abs_tol=1e-6, rel_tol=0.0):
+        self.A, self.nc = A, int(unknown_dim)
+        self.max_iter, self.abs_tol, self.rel_tol = int(max_iter), float(abs_tol), float(rel_tol)
+        self._stats = _lib.SolverStats()
+        self._L = _lib.load()
+
+    def pre_solve(self, B, X, stream=None):
+        # the residual set-up runs inside solve() (same kernel launch)
+        return None
+
+    def solve(self, B, X, stream=None):
+        o = _lib.SolverOpts(self.max_iter, self.abs_tol, self.rel_tol, self.PRECOND)
+        c = self.A.csr()
+        st = self._L.rxg_cg_solve(ctypes.byref(c), self.nc, _ptr(B.contiguous()), _ptr(X),
+                                  ctypes.byref(o), ctypes.byref(self._stats), _stream(stream))
+        if st not in (0, 6):
+            check(st)
+        return X
+
+    def iter_taken(self):
+        return self._stats.iters
+
+    def start_residual(self):
+        return self._stats.start_res
+
+    def final_residual(self):
+        return self._stats.final_res
+
+    def converged(self):
+        return bool(self._stats.converged)
+
+
+class PCGSolver(CGSolver):
+    """Jacobi-preconditioned CG (pcg_solver.h:14-213)."""
+    PRECOND = 1
+
+
+def mcf_step(rx, xyz_lin, dt, nsteps=1, precision="f64", tol=1e-6, max_iter=5000, stream=None):
+    """Implicit MCF steps in place on xyz_lin ((nv,3) float64 CUDA tensor, linear order).
+
+    Returns the solver stats dict of the last step."""
+    L = _lib.load()
+    if xyz_lin.dtype != torch.float64 or not xyz_lin.is_contiguous():
+        raise ValueError("xyz_lin must be a contiguous float64 tensor")
+    prec = {"f64": 1, "f32": 0, "mixed": 0}[precision]
+    st = _lib.SolverStats()
+    ptr = xyz_lin.data_ptr() if xyz_lin.is_cuda else xyz_lin.numpy().ctypes.data
+    rc = L.rxg_mcf_step(rx._h, float(dt), int(nsteps), prec, float(tol), int(max_iter),
+                        ctypes.c_void_p(ptr), ctypes.byref(st), _stream(stream))
+    if rc not in (0, 6):
+        check(rc)
+    return {"iters": st.iters, "converged": bool(st.converged), "start_res": st.start_res,
+            "final_res": st.final_res}

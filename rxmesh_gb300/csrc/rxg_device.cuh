@@ -1,0 +1,156 @@
+// Device helpers shared by the kernels: TMA bulk copies into shared memory
+// with an mbarrier, bounded waits that report through an error word instead
+// of hanging, and block-wide scans/reductions.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rxg_internal.h"
+
+namespace rxg {
+
+// error codes OR-ed into the device error word
+enum : int {
+    DEVERR_MBAR_TIMEOUT   = 1,
+    DEVERR_GRID_TIMEOUT   = 2,
+    DEVERR_SMEM_OVERFLOW  = 4,
+    DEVERR_NONMANIFOLD    = 8,
+};
+
+// spin limit of every bounded wait; try_wait itself suspends for a
+// hardware-defined interval per attempt, so this bounds a wait to well
+// under a second on a healthy GPU while never hanging a faulty one.
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+    // make the initialised barrier visible to the async (TMA) proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// global -> shared bulk copy (TMA, non-tensor).  dst, src 16-byte aligned,
+// bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait on phase `parity` of an mbarrier.  On timeout the error word
+// gets DEVERR_MBAR_TIMEOUT, then the thread waits once more (bounded) for
+// the copies still in flight and returns false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err)
+{
+    for (uint32_t i = 0; i < kWaitLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    if (err) atomicOr(err, DEVERR_MBAR_TIMEOUT);
+    for (uint32_t i = 0; i < kWaitLimit; ++i)
+        if (mbar_try_wait(bar, parity)) break;
+    return false;
+}
+
+// bytes of a slice of `words` 32-bit words padded to 16 bytes
+__host__ __device__ __forceinline__ uint32_t pad16_bytes(int32_t words)
+{
+    return (uint32_t)(((words + 3) & ~3) * 4);
+}
+
+__host__ __device__ __forceinline__ int32_t pad4i(int32_t n) { return (n + 3) & ~3; }
+
+// Exclusive scan of s[0..n) in place, returns the total.  256-thread blocks.
+// Each thread scans a contiguous chunk, warps combine chunk totals with
+// shuffles, and warp totals go through shared memory.  Deterministic.
+template <int BT>
+__device__ __forceinline__ int32_t block_exclusive_scan(int32_t* s, int32_t n, int32_t* s_warp)
+{
+    const int tid   = threadIdx.x;
+    const int chunk = (n + BT - 1) / BT;
+    const int beg   = min(n, tid * chunk), end = min(n, beg + chunk);
+    int32_t   sum   = 0;
+    for (int i = beg; i < end; ++i) sum += s[i];
+    // inclusive warp scan of per-thread sums
+    int32_t x = sum;
+    const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int32_t w = lane < BT / 32 ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < BT / 32) s_warp[lane] = w;  // inclusive warp totals
+    }
+    __syncthreads();
+    int32_t run   = x - sum + (warp > 0 ? s_warp[warp - 1] : 0);
+    int32_t total = s_warp[BT / 32 - 1];
+    for (int i = beg; i < end; ++i) {
+        int32_t v = s[i];
+        s[i]      = run;
+        run += v;
+    }
+    __syncthreads();
+    return total;
+}
+
+// Copy n ints from shared (sbuf holds element g - gbase at sbuf[shift + ...],
+// shift = gbase & 3) to global dst[gbase .. gbase+n) with 16-byte stores in
+// the aligned middle and scalar stores at the ragged ends.
+template <int BT>
+__device__ __forceinline__ void store_ints_aligned(int32_t* __restrict__ dst, int64_t gbase,
+                                                   const int32_t* sbuf, int32_t n)
+{
+    const int64_t g_end   = gbase + n;
+    const int64_t g0      = (gbase + 3) & ~int64_t(3);
+    const int64_t g1      = g_end & ~int64_t(3);
+    const int64_t sbase   = gbase & ~int64_t(3);  // sbuf[j] <-> global sbase + j
+    if (g0 >= g1) {
+        for (int64_t g = gbase + threadIdx.x; g < g_end; g += BT) dst[g] = sbuf[g - sbase];
+        return;
+    }
+    for (int64_t g = gbase + threadIdx.x; g < g0; g += BT) dst[g] = sbuf[g - sbase];
+    for (int64_t g = g1 + threadIdx.x; g < g_end; g += BT) dst[g] = sbuf[g - sbase];
+    const int32_t nv4 = (int32_t)((g1 - g0) >> 2);
+    const int4*   s4  = reinterpret_cast<const int4*>(sbuf + (g0 - sbase));
+    int4*         d4  = reinterpret_cast<int4*>(dst + g0);
+    for (int32_t i = threadIdx.x; i < nv4; i += BT) d4[i] = s4[i];
+}
+
+}  // namespace rxg

@@ -1,0 +1,106 @@
+// Internal structures shared by the translation units of librxg.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/rxg.h"
+
+namespace rxg {
+
+// Per-patch header, one per CTA of a patch-parallel kernel.  Local ids are
+// 16-bit: owned elements first, then ribbon (not-owned) elements.
+struct PatchHdr
+{
+    int32_t nVo, nVl;  // owned / local vertices
+    int32_t nEo, nEl;  // owned / local edges
+    int32_t nFo, nFl;  // owned / local faces
+    int32_t v_base;    // linear id of owned vertex 0
+    int32_t e_base;
+    int32_t f_base;
+    int32_t vv_base;   // first VV/VE value of this patch's owned rows
+    int32_t vf_base;   // first VF value of this patch's owned rows
+    int32_t ev_off;    // arena word offsets (16-byte aligned slices)
+    int32_t fe_off;
+    int32_t rv_off;    // ribbon vertex -> linear id
+    int32_t re_off;    // ribbon edge   -> linear id
+    int32_t rf_off;    // ribbon face   -> linear id
+};
+static_assert(sizeof(PatchHdr) == 64, "PatchHdr is one 64-byte line");
+
+// Device-resident topology (owned by Mesh).
+struct DeviceTopo
+{
+    PatchHdr* hdr   = nullptr;
+    uint32_t* arena = nullptr;  // words: ev (u16 pairs), fe (u16 triples), ribbon tables
+    int64_t   arena_words = 0;
+    // permutations, linear -> input (device copies for rxg_permute)
+    int32_t* v_l2i = nullptr;
+    int32_t* e_l2i = nullptr;
+    int32_t* f_l2i = nullptr;
+    // face -> 3 linear vertex ids (face linear order), used by per-face kernels
+    int32_t* fv_lin = nullptr;
+};
+
+struct Mesh
+{
+    int64_t nv = 0, ne = 0, nf = 0;
+    int32_t patch_faces = 0;
+    int32_t num_patches = 0;
+    int32_t device      = 0;
+    bool    closed = true, edge_manifold = true;
+    int64_t max_valence = 0;
+    int32_t max_vl = 0, max_el = 0, max_fl = 0, max_vo = 0, max_eo = 0, max_fo = 0;
+    int64_t ribbon_v = 0, ribbon_f = 0;
+
+    std::vector<int32_t> ev_in;  // input edge list (ne*2)
+    std::vector<int32_t> v_l2i, e_l2i, f_l2i;
+    std::vector<int32_t> v_i2l, e_i2l, f_i2l;
+    std::vector<PatchHdr> hdr;
+    std::vector<uint32_t> arena;
+
+    DeviceTopo d;
+
+    // lazily built device structures (guarded by the mesh's own mutex)
+    void* lazy = nullptr;
+
+    int64_t device_bytes = 0;
+};
+
+// thread-local error message
+void        set_error(const char* fmt, ...);
+rxg_status  cuda_status(cudaError_t e, const char* what);
+
+#define RXG_CUDA_TRY(call)                                   \
+    do {                                                     \
+        cudaError_t _e = (call);                             \
+        if (_e != cudaSuccess) return cuda_status(_e, #call); \
+    } while (0)
+
+// Host/device pointer classification: true when p is device-accessible
+// memory allocated by CUDA (device or managed).  Host memory (pageable,
+// pinned or registered) returns false.
+bool is_device_ptr(const void* p);
+
+// Lazily allocated per-mesh device scratch and the oriented ring.
+struct Lazy;
+Lazy* lazy_of(const Mesh* m);
+void  lazy_free(Mesh* m);
+
+// Query kernels entry (rxg_query.cu)
+rxg_status launch_query(const Mesh* m, int op, int32_t* d_off, int32_t* d_val,
+                        cudaStream_t s);
+
+// device error word (bounded waits)
+int* device_error_word();
+rxg_status check_device_error(cudaStream_t s);
+
+}  // namespace rxg
+
+struct rxg_mesh
+{
+    rxg::Mesh m;
+};

@@ -1,0 +1,537 @@
+// Patch-parallel query kernels: VV, VE, VF, FV, EV and vertex normals.
+//
+// One CTA per patch (RXMesh's launch shape, rxmesh_static.inl:443-496).  The
+// CTA stages its patch's EV / FE slices and ribbon tables into shared memory
+// with TMA bulk copies (cp.async.bulk + mbarrier), builds the vertex-centred
+// transposes there (the counting sort of block_mat_transpose,
+// kernels/rxmesh_queries.cuh:17-107), resolves not-owned elements through the
+// dense ribbon table (in place of the LP hashtable lookup of
+// iterator.cuh:117-143) and writes its owned rows as one contiguous chunk of
+// the global CSR with 16-byte stores.
+#include <algorithm>
+#include <cstdio>
+
+#include "rxg_device.cuh"
+
+namespace rxg {
+
+constexpr int kQT = 256;  // threads per query CTA
+
+__device__ int g_err_word;
+
+int* device_error_word()
+{
+    static int* p = nullptr;
+    if (!p) cudaGetSymbolAddress((void**)&p, g_err_word);
+    return p;
+}
+
+rxg_status check_device_error(cudaStream_t s)
+{
+    int* d = device_error_word();
+    int  h = 0;
+    RXG_CUDA_TRY(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RXG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h) {
+        int zero = 0;
+        cudaMemcpy(d, &zero, sizeof(int), cudaMemcpyHostToDevice);
+        if (h & DEVERR_MBAR_TIMEOUT) {
+            set_error("a bounded mbarrier wait timed out on the device (code %d)", h);
+            return RXG_ERR_DEVICE_TIMEOUT;
+        }
+        if (h & DEVERR_GRID_TIMEOUT) {
+            set_error("a bounded grid barrier timed out on the device (code %d)", h);
+            return RXG_ERR_DEVICE_TIMEOUT;
+        }
+        if (h & DEVERR_NONMANIFOLD) {
+            set_error("a vertex fan is not a disk or half-disk (non-manifold vertex)");
+            return RXG_ERR_NONMANIFOLD;
+        }
+        set_error("device error word %d", h);
+        return RXG_ERR_CUDA;
+    }
+    return RXG_OK;
+}
+
+// ---------------------------------------------------------------------
+// staging
+// ---------------------------------------------------------------------
+
+struct Slice
+{
+    const uint32_t* src;
+    uint32_t        bytes;
+};
+
+// thread 0 arms the barrier and issues up to 4 bulk copies; everybody waits.
+// Shared destinations must be 16-byte aligned.
+template <int N>
+__device__ __forceinline__ bool stage(uint64_t* bar, uint32_t* const (&dst)[N],
+                                      const Slice (&sl)[N], int* err)
+{
+    if (threadIdx.x == 0) {
+        uint32_t total = 0;
+#pragma unroll
+        for (int i = 0; i < N; ++i) total += sl[i].bytes;
+        mbar_arrive_expect_tx(bar, total);
+#pragma unroll
+        for (int i = 0; i < N; ++i)
+            if (sl[i].bytes) bulk_g2s(dst[i], sl[i].src, sl[i].bytes, bar);
+    }
+    return mbar_wait_bounded(bar, 0, err);
+}
+
+__device__ __forceinline__ PatchHdr load_hdr(const PatchHdr* __restrict__ hdrs)
+{
+    const int4* p = reinterpret_cast<const int4*>(hdrs + blockIdx.x);
+    PatchHdr    h;
+    int4*       q = reinterpret_cast<int4*>(&h);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) q[i] = __ldg(p + i);
+    return h;
+}
+
+__device__ __forceinline__ uint32_t fe_words(int32_t nF) { return (uint32_t)((3 * nF + 1) / 2); }
+
+// vertex k (0..2) of local face f from FE (edge<<1|dir) and EV (a | b<<16)
+__device__ __forceinline__ uint32_t face_vertex(const uint16_t* s_fe, const uint32_t* s_ev, int f,
+                                                int k)
+{
+    uint32_t fe = s_fe[3 * f + k];
+    uint32_t ev = s_ev[fe >> 1];
+    return (fe & 1u) ? (ev >> 16) : (ev & 0xffffu);
+}
+
+// ---------------------------------------------------------------------
+// VV / VE  (OP 0 / 1) and VF (OP 2): vertex-centred transposes
+// ---------------------------------------------------------------------
+
+template <int OP>
+__global__ void __launch_bounds__(kQT) k_query_vertex(const PatchHdr* __restrict__ hdrs,
+                                                      const uint32_t* __restrict__ arena,
+                                                      int32_t* __restrict__ out_off,
+                                                      int32_t* __restrict__ out_val, int* err)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ uint64_t bar;
+    __shared__ int32_t  s_warp[kQT / 32];
+
+    const PatchHdr h   = load_hdr(hdrs);
+    const int32_t  nVo = h.nVo;
+    const int32_t  nRib = OP == 0 ? h.nVl - h.nVo : (OP == 1 ? h.nEl - h.nEo : h.nFl - h.nFo);
+    const int32_t  ribOff = OP == 0 ? h.rv_off : (OP == 1 ? h.re_off : h.rf_off);
+
+    // shared layout (all 16-byte aligned)
+    uint32_t* s_ev  = smem;
+    uint32_t* s_fe  = s_ev + pad4i(h.nEl);
+    uint32_t* s_rib = s_fe + (OP == 2 ? pad4i((int32_t)fe_words(h.nFl)) : 0);
+    int32_t*  s_cnt = reinterpret_cast<int32_t*>(s_rib + pad4i(nRib));
+    int32_t*  s_out = s_cnt + pad4i(nVo + 1);
+
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    for (int i = threadIdx.x; i <= nVo; i += kQT) s_cnt[i] = 0;
+    __syncthreads();
+
+    bool ok;
+    if (OP == 2) {
+        uint32_t* const dst[3] = {s_ev, s_fe, s_rib};
+        const Slice     sl[3]  = {{arena + h.ev_off, pad16_bytes(h.nEl)},
+                                  {arena + h.fe_off, pad16_bytes((int32_t)fe_words(h.nFl))},
+                                  {arena + ribOff, pad16_bytes(nRib)}};
+        ok = stage(&bar, dst, sl, err);
+    } else {
+        uint32_t* const dst[2] = {s_ev, s_rib};
+        const Slice     sl[2]  = {{arena + h.ev_off, pad16_bytes(h.nEl)},
+                                  {arena + ribOff, pad16_bytes(nRib)}};
+        ok = stage(&bar, dst, sl, err);
+    }
+    if (!ok) return;
+
+    const uint16_t* fe16 = reinterpret_cast<const uint16_t*>(s_fe);
+
+    // 1. count owned-vertex incidences
+    if (OP == 2) {
+        for (int i = threadIdx.x; i < 3 * h.nFl; i += kQT) {
+            uint32_t v = face_vertex(fe16, s_ev, i / 3, i % 3);
+            if ((int32_t)v < nVo) atomicAdd(&s_cnt[v], 1);
+        }
+    } else {
+        for (int e = threadIdx.x; e < h.nEl; e += kQT) {
+            uint32_t ev = s_ev[e];
+            uint32_t a = ev & 0xffffu, b = ev >> 16;
+            if ((int32_t)a < nVo) atomicAdd(&s_cnt[a], 1);
+            if ((int32_t)b < nVo) atomicAdd(&s_cnt[b], 1);
+        }
+    }
+    __syncthreads();
+
+    // 2. exclusive scan -> row offsets of the patch's owned rows
+    const int32_t total = block_exclusive_scan<kQT>(s_cnt, nVo + 1, s_warp);
+    const int32_t vbase = OP == 2 ? h.vf_base : h.vv_base;
+    for (int v = threadIdx.x; v <= nVo; v += kQT) out_off[h.v_base + v] = vbase + s_cnt[v];
+    __syncthreads();
+
+    // 3. scatter values (linear ids) into the staged chunk
+    int32_t* sbuf = s_out + (vbase & 3);  // element g lives at s_out[g - (vbase & ~3)]
+    if (OP == 2) {
+        for (int i = threadIdx.x; i < 3 * h.nFl; i += kQT) {
+            int      f = i / 3;
+            uint32_t v = face_vertex(fe16, s_ev, f, i % 3);
+            if ((int32_t)v < nVo) {
+                int32_t pos = atomicAdd(&s_cnt[v], 1);
+                sbuf[pos]   = f < h.nFo ? h.f_base + f : (int32_t)s_rib[f - h.nFo];
+            }
+        }
+    } else {
+        for (int e = threadIdx.x; e < h.nEl; e += kQT) {
+            uint32_t ev = s_ev[e];
+            uint32_t a = ev & 0xffffu, b = ev >> 16;
+            int32_t  val_a, val_b;
+            if (OP == 0) {
+                val_a = (int32_t)b < nVo ? h.v_base + (int32_t)b : (int32_t)s_rib[b - nVo];
+                val_b = (int32_t)a < nVo ? h.v_base + (int32_t)a : (int32_t)s_rib[a - nVo];
+            } else {
+                val_a = val_b = e < h.nEo ? h.e_base + e : (int32_t)s_rib[e - h.nEo];
+            }
+            if ((int32_t)a < nVo) sbuf[atomicAdd(&s_cnt[a], 1)] = val_a;
+            if ((int32_t)b < nVo) sbuf[atomicAdd(&s_cnt[b], 1)] = val_b;
+        }
+    }
+    __syncthreads();
+
+    // 4. contiguous, vectorised write-out of the chunk
+    store_ints_aligned<kQT>(out_val, vbase, s_out, total);
+}
+
+// ---------------------------------------------------------------------
+// FV (OP 3) and EV (OP 4): owned-element rows, one output word per thread
+// ---------------------------------------------------------------------
+
+template <int OP>
+__global__ void __launch_bounds__(kQT) k_query_elem(const PatchHdr* __restrict__ hdrs,
+                                                    const uint32_t* __restrict__ arena,
+                                                    int32_t* __restrict__ out_val, int* err)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ uint64_t bar;
+
+    const PatchHdr h   = load_hdr(hdrs);
+    const int32_t  nVo = h.nVo;
+    const int32_t  nVr = h.nVl - h.nVo;
+    // FV needs every local edge an owned face uses, i.e. the whole EV slice;
+    // EV needs only the owned prefix.
+    const int32_t ev_words = OP == 3 ? h.nEl : h.nEo;
+    const int32_t fe_w     = OP == 3 ? (int32_t)fe_words(h.nFo) : 0;
+
+    uint32_t* s_ev = smem;
+    uint32_t* s_fe = s_ev + pad4i(ev_words);
+    uint32_t* s_rv = s_fe + pad4i(fe_w);
+
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    uint32_t* const dst[3] = {s_ev, s_fe, s_rv};
+    const Slice     sl[3]  = {{arena + h.ev_off, pad16_bytes(ev_words)},
+                              {arena + h.fe_off, pad16_bytes(fe_w)},
+                              {arena + h.rv_off, pad16_bytes(nVr)}};
+    if (!stage(&bar, dst, sl, err)) return;
+
+    const uint16_t* fe16 = reinterpret_cast<const uint16_t*>(s_fe);
+    if (OP == 3) {
+        const int32_t n    = 3 * h.nFo;
+        int32_t*      base = out_val + 3 * (int64_t)h.f_base;
+        for (int i = threadIdx.x; i < n; i += kQT) {
+            uint32_t v = face_vertex(fe16, s_ev, i / 3, i % 3);
+            base[i]    = (int32_t)v < nVo ? h.v_base + (int32_t)v : (int32_t)s_rv[v - nVo];
+        }
+    } else {
+        const int32_t n    = 2 * h.nEo;
+        int32_t*      base = out_val + 2 * (int64_t)h.e_base;
+        for (int i = threadIdx.x; i < n; i += kQT) {
+            uint32_t ev = s_ev[i >> 1];
+            uint32_t v  = (i & 1) ? (ev >> 16) : (ev & 0xffffu);
+            base[i]     = (int32_t)v < nVo ? h.v_base + (int32_t)v : (int32_t)s_rv[v - nVo];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// Vertex normals (OP 5): per patch, every local face (owned + ribbon)
+// contributes to the patch's owned vertices in shared memory, so owned
+// normals are written once, with no global atomics and no zero-fill pass.
+// Formula of compute_vertex_normal (apps/VertexNormal/vertex_normal_kernel.cuh:10-43).
+// ---------------------------------------------------------------------
+
+template <int W>
+__global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restrict__ hdrs,
+                                                        const uint32_t* __restrict__ arena,
+                                                        const float* __restrict__ xyz,
+                                                        float* __restrict__ out, int* err)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ uint64_t bar;
+
+    const PatchHdr h   = load_hdr(hdrs);
+    const int32_t  nVo = h.nVo, nVr = h.nVl - h.nVo;
+    uint32_t* s_ev  = smem;
+    uint32_t* s_fe  = s_ev + pad4i(h.nEl);
+    uint32_t* s_rv  = s_fe + pad4i((int32_t)fe_words(h.nFl));
+    float*    s_pos = reinterpret_cast<float*>(s_rv + pad4i(nVr));
+    float*    s_acc = s_pos + pad4i(3 * h.nVl);
+
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    for (int i = threadIdx.x; i < 3 * nVo; i += kQT) {
+        s_acc[i] = 0.f;
+        s_pos[i] = __ldg(xyz + 3 * (int64_t)h.v_base + i);
+    }
+    __syncthreads();
+    uint32_t* const dst[3] = {s_ev, s_fe, s_rv};
+    const Slice     sl[3]  = {{arena + h.ev_off, pad16_bytes(h.nEl)},
+                              {arena + h.fe_off, pad16_bytes((int32_t)fe_words(h.nFl))},
+                              {arena + h.rv_off, pad16_bytes(nVr)}};
+    if (!stage(&bar, dst, sl, err)) return;
+    for (int i = threadIdx.x; i < 3 * nVr; i += kQT)
+        s_pos[3 * nVo + i] = __ldg(xyz + 3 * (int64_t)s_rv[i / 3] + (i % 3));
+    __syncthreads();
+
+    const uint16_t* fe16 = reinterpret_cast<const uint16_t*>(s_fe);
+    for (int f = threadIdx.x; f < h.nFl; f += kQT) {
+        uint32_t v[3];
+        float3   c[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            v[k] = face_vertex(fe16, s_ev, f, k);
+            c[k] = make_float3(s_pos[3 * v[k]], s_pos[3 * v[k] + 1], s_pos[3 * v[k] + 2]);
+        }
+        if ((int32_t)v[0] >= nVo && (int32_t)v[1] >= nVo && (int32_t)v[2] >= nVo) continue;
+        const float3 u = make_float3(c[1].x - c[0].x, c[1].y - c[0].y, c[1].z - c[0].z);
+        const float3 w = make_float3(c[2].x - c[0].x, c[2].y - c[0].y, c[2].z - c[0].z);
+        const float  n[3] = {u.y * w.z - w.y * u.z, u.z * w.x - w.z * u.x, u.x * w.y - w.x * u.y};
+        float        l[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float3 a = c[k], b = c[(k + 1) % 3];
+            const float  dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+            l[k]            = dx * dx + dy * dy + dz * dz;
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if ((int32_t)v[k] >= nVo) continue;
+            const float d = W == RXG_NORMAL_MAX ? (l[k] + l[(k + 2) % 3]) : 1.f;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+                atomicAdd(&s_acc[3 * v[k] + i], W == RXG_NORMAL_MAX ? n[i] / d : n[i]);
+        }
+    }
+    __syncthreads();
+    float* o = out + 3 * (int64_t)h.v_base;
+    for (int i = threadIdx.x; i < 3 * nVo; i += kQT) o[i] = s_acc[i];
+}
+
+// ---------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------
+
+// dynamic shared memory (bytes) of one patch for a kernel kind
+static size_t smem_words(const PatchHdr& h, int kind)
+{
+    const int32_t nVr = h.nVl - h.nVo, nEr = h.nEl - h.nEo, nFr = h.nFl - h.nFo;
+    const int32_t few = pad4i((3 * h.nFl + 1) / 2);
+    switch (kind) {
+        case RXG_OP_VV:
+        case RXG_OP_VE:
+            return pad4i(h.nEl) + pad4i(kind == RXG_OP_VV ? nVr : nEr) + pad4i(h.nVo + 1) +
+                   2 * h.nEl + 4;
+        case RXG_OP_VF:
+            return pad4i(h.nEl) + few + pad4i(nFr) + pad4i(h.nVo + 1) + 3 * h.nFl + 4;
+        case RXG_OP_FV: return pad4i(h.nEl) + pad4i((3 * h.nFo + 1) / 2) + pad4i(nVr);
+        case RXG_OP_EV: return pad4i(h.nEo) + pad4i(nVr);
+        default:  // normals
+            return pad4i(h.nEl) + few + pad4i(nVr) + pad4i(3 * h.nVl) + 3 * h.nVo;
+    }
+}
+
+size_t query_smem_bytes(const Mesh* m, int kind)
+{
+    size_t w = 0;
+    for (const PatchHdr& h : m->hdr) w = std::max(w, smem_words(h, kind));
+    return w * 4;
+}
+
+template <typename K>
+static rxg_status launch_patch_kernel(K kern, const Mesh* m, size_t smem, cudaStream_t s,
+                                      const char* name)
+{
+    (void)kern;
+    if (smem > 227 * 1024) {
+        set_error("%s: a patch needs %zu bytes of shared memory (> 227 KB); use smaller patches",
+                  name, smem);
+        return RXG_ERR_PATCH_LIMIT;
+    }
+    return RXG_OK;
+}
+
+template <typename F, typename... Args>
+static rxg_status launch(F* kern, const Mesh* m, size_t smem, cudaStream_t s, const char* name,
+                         Args... args)
+{
+    rxg_status st = launch_patch_kernel(kern, m, smem, s, name);
+    if (st) return st;
+    if (smem > 48 * 1024)
+        RXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+    kern<<<m->num_patches, kQT, smem, s>>>(args...);
+    RXG_CUDA_TRY(cudaGetLastError());
+    return RXG_OK;
+}
+
+rxg_status launch_query(const Mesh* m, int op, int32_t* d_off, int32_t* d_val, cudaStream_t s)
+{
+    const size_t smem = query_smem_bytes(m, op);
+    int*         err  = device_error_word();
+    switch (op) {
+        case RXG_OP_VV:
+            return launch(k_query_vertex<0>, m, smem, s, "VV", (const PatchHdr*)m->d.hdr,
+                          (const uint32_t*)m->d.arena, d_off, d_val, err);
+        case RXG_OP_VE:
+            return launch(k_query_vertex<1>, m, smem, s, "VE", (const PatchHdr*)m->d.hdr,
+                          (const uint32_t*)m->d.arena, d_off, d_val, err);
+        case RXG_OP_VF:
+            return launch(k_query_vertex<2>, m, smem, s, "VF", (const PatchHdr*)m->d.hdr,
+                          (const uint32_t*)m->d.arena, d_off, d_val, err);
+        case RXG_OP_FV:
+            return launch(k_query_elem<3>, m, smem, s, "FV", (const PatchHdr*)m->d.hdr,
+                          (const uint32_t*)m->d.arena, d_val, err);
+        case RXG_OP_EV:
+            return launch(k_query_elem<4>, m, smem, s, "EV", (const PatchHdr*)m->d.hdr,
+                          (const uint32_t*)m->d.arena, d_val, err);
+    }
+    set_error("rxg_query: unknown op %d", op);
+    return RXG_ERR_INVALID;
+}
+
+rxg_status launch_normals(const Mesh* m, int weighting, const float* xyz, float* out,
+                          cudaStream_t s)
+{
+    const size_t smem = query_smem_bytes(m, 5);
+    int*         err  = device_error_word();
+    if (weighting == RXG_NORMAL_MAX)
+        return launch(k_vertex_normals<RXG_NORMAL_MAX>, m, smem, s, "normals",
+                      (const PatchHdr*)m->d.hdr, (const uint32_t*)m->d.arena, xyz, out, err);
+    return launch(k_vertex_normals<RXG_NORMAL_AREA>, m, smem, s, "normals",
+                  (const PatchHdr*)m->d.hdr, (const uint32_t*)m->d.arena, xyz, out, err);
+}
+
+// scratch helper: device copy of a possibly-host array
+struct Staged
+{
+    void*        d    = nullptr;
+    bool         owns = false;
+    cudaStream_t s    = nullptr;
+    ~Staged()
+    {
+        if (owns) cudaFreeAsync(d, s);
+    }
+};
+
+static rxg_status stage_out(void* user, size_t bytes, cudaStream_t s, Staged& st)
+{
+    st.s = s;
+    if (user == nullptr || is_device_ptr(user)) {
+        st.d = user;
+        return RXG_OK;
+    }
+    RXG_CUDA_TRY(cudaMallocAsync(&st.d, bytes ? bytes : 16, s));
+    st.owns = true;
+    return RXG_OK;
+}
+
+static rxg_status stage_in(const void* user, size_t bytes, cudaStream_t s, Staged& st)
+{
+    st.s = s;
+    if (user == nullptr || is_device_ptr(user)) {
+        st.d = const_cast<void*>(user);
+        return RXG_OK;
+    }
+    RXG_CUDA_TRY(cudaMallocAsync(&st.d, bytes ? bytes : 16, s));
+    st.owns = true;
+    RXG_CUDA_TRY(cudaMemcpyAsync(st.d, user, bytes, cudaMemcpyHostToDevice, s));
+    return RXG_OK;
+}
+
+static rxg_status finish_out(void* user, const Staged& st, size_t bytes, cudaStream_t s)
+{
+    if (!st.owns) return RXG_OK;
+    RXG_CUDA_TRY(cudaMemcpyAsync(user, st.d, bytes, cudaMemcpyDeviceToHost, s));
+    return RXG_OK;
+}
+
+}  // namespace rxg
+
+using namespace rxg;
+
+extern "C" {
+
+rxg_status rxg_query_size(const rxg_mesh* h, int32_t op, int64_t* n_rows, int64_t* n_values)
+{
+    if (!h || !n_rows || !n_values) {
+        set_error("rxg_query_size: NULL argument");
+        return RXG_ERR_INVALID;
+    }
+    const Mesh& M = h->m;
+    switch (op) {
+        case RXG_OP_VV:
+        case RXG_OP_VE: *n_rows = M.nv; *n_values = 2 * M.ne; return RXG_OK;
+        case RXG_OP_VF: *n_rows = M.nv; *n_values = 3 * M.nf; return RXG_OK;
+        case RXG_OP_FV: *n_rows = M.nf; *n_values = 3 * M.nf; return RXG_OK;
+        case RXG_OP_EV: *n_rows = M.ne; *n_values = 2 * M.ne; return RXG_OK;
+    }
+    set_error("rxg_query_size: unknown op %d", op);
+    return RXG_ERR_INVALID;
+}
+
+rxg_status rxg_query(const rxg_mesh* h, int32_t op, int32_t* offsets, int32_t* values,
+                     void* stream)
+{
+    int64_t rows, nval;
+    rxg_status st = rxg_query_size(h, op, &rows, &nval);
+    if (st) return st;
+    const bool csr = op <= RXG_OP_VF;
+    if (!values || (csr && !offsets)) {
+        set_error("rxg_query: values%s must not be NULL", csr ? " and offsets" : "");
+        return RXG_ERR_INVALID;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    Staged       so, sv;
+    const size_t off_bytes = csr ? (size_t)(rows + 1) * 4 : 0, val_bytes = (size_t)nval * 4;
+    if ((st = stage_out(csr ? offsets : nullptr, off_bytes, s, so))) return st;
+    if ((st = stage_out(values, val_bytes, s, sv))) return st;
+    if ((st = launch_query(&h->m, op, (int32_t*)so.d, (int32_t*)sv.d, s))) return st;
+    if (csr && (st = finish_out(offsets, so, off_bytes, s))) return st;
+    if ((st = finish_out(values, sv, val_bytes, s))) return st;
+    if (so.owns || sv.owns) RXG_CUDA_TRY(cudaStreamSynchronize(s));
+    return RXG_OK;
+}
+
+rxg_status rxg_vertex_normals(const rxg_mesh* h, int32_t weighting, const float* xyz, float* out,
+                              void* stream)
+{
+    if (!h || !xyz || !out || (weighting != RXG_NORMAL_MAX && weighting != RXG_NORMAL_AREA)) {
+        set_error("rxg_vertex_normals: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    cudaStream_t s     = (cudaStream_t)stream;
+    const size_t bytes = (size_t)h->m.nv * 12;
+    Staged       si, so;
+    rxg_status   st;
+    if ((st = stage_in(xyz, bytes, s, si))) return st;
+    if ((st = stage_out(out, bytes, s, so))) return st;
+    if ((st = launch_normals(&h->m, weighting, (const float*)si.d, (float*)so.d, s))) return st;
+    if ((st = finish_out(out, so, bytes, s))) return st;
+    if (si.owns || so.owns) RXG_CUDA_TRY(cudaStreamSynchronize(s));
+    return RXG_OK;
+}
+
+// Syncs `stream`, reads and clears the device error word set by bounded waits.
+rxg_status rxg_device_check(void* stream) { return check_device_error((cudaStream_t)stream); }
+
+}  // extern "C"

@@ -1,0 +1,119 @@
+"""CPU tests of librxg.so: exports, host-side mesh build and patch layout.
+
+No compute kernel runs here; the patch arena is decoded on the CPU and the
+queries it encodes are compared bit-exactly with the oracle."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden, sorted_rows
+from rxmesh_gb300 import meshgen
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "rxg.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return set(re.findall(r"\b(rxg_[a-z0-9_]+)\s*\(", txt))
+
+
+def test_library_exports_every_declared_symbol():
+    from rxmesh_gb300 import _lib
+    import ctypes
+    L = ctypes.CDLL(_lib.load().__dict__["_name"])
+    missing = [s for s in sorted(header_symbols()) if not hasattr(L, s)]
+    assert not missing, missing
+    assert header_symbols() <= set(_lib.SIGNATURES), "bindings lag the header"
+
+
+def test_invalid_arguments_return_status():
+    import ctypes
+    from rxmesh_gb300 import _lib
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    bad = np.array([[0, 1, 5]], np.int32)
+    assert L.rxg_mesh_create_ex(bad.ctypes.data, 1, 3, 64, 1, ctypes.byref(h)) == 1
+    assert b"outside" in L.rxg_last_error()
+    rep = np.array([[0, 1, 1]], np.int32)
+    assert L.rxg_mesh_create_ex(rep.ctypes.data, 1, 3, 64, 1, ctypes.byref(h)) == 1
+    ok = np.array([[0, 1, 2]], np.int32)
+    assert L.rxg_mesh_create_ex(ok.ctypes.data, 1, 3, 8, 1, ctypes.byref(h)) == 1  # patch too small
+    assert L.rxg_status_string(6) == b"RXG_ERR_NOT_CONVERGED"
+
+
+def decode(rx):
+    """Per-patch decoding of the arena into linear-id queries (CPU)."""
+    hdr, arena = rx.patches()
+    nv, ne, nf = rx.get_num_vertices(), rx.get_num_edges(), rx.get_num_faces()
+    vv = [None] * nv
+    ve = [None] * nv
+    vf = [None] * nv
+    fvq = np.full((nf, 3), -1, np.int64)
+    evq = np.full((ne, 2), -1, np.int64)
+    for h in hdr:
+        nVo, nVl, nEo, nEl, nFo, nFl, vb, eb, fb, vvb, vfb, evo, feo, rvo, reo, rfo = h.tolist()
+        ev = arena[evo:evo + nEl]
+        a, b = (ev & 0xFFFF).astype(np.int64), (ev >> 16).astype(np.int64)
+        fe = arena[feo:feo + (3 * nFl + 1) // 2 + 4].view(np.uint16)[:3 * nFl].reshape(-1, 3).astype(np.int64)
+        rv = arena[rvo:rvo + nVl - nVo].astype(np.int64)
+        re_ = arena[reo:reo + nEl - nEo].astype(np.int64)
+        rf = arena[rfo:rfo + nFl - nFo].astype(np.int64)
+        linv = lambda l: np.where(l < nVo, vb + l, rv[np.maximum(l - nVo, 0)] if rv.size else 0)
+        line = lambda l: np.where(l < nEo, eb + l, re_[np.maximum(l - nEo, 0)] if re_.size else 0)
+        linf = lambda l: np.where(l < nFo, fb + l, rf[np.maximum(l - nFo, 0)] if rf.size else 0)
+        fvl = np.where(fe & 1, b[fe >> 1], a[fe >> 1])
+        for v in range(nVo):
+            m1, m2 = a == v, b == v
+            vv[vb + v] = sorted(linv(np.concatenate([b[m1], a[m2]])).tolist())
+            ve[vb + v] = sorted(line(np.concatenate([np.nonzero(m1)[0], np.nonzero(m2)[0]])).tolist())
+            vf[vb + v] = sorted(linf(np.nonzero((fvl == v).any(1))[0]).tolist())
+        if nFo:
+            fvq[fb:fb + nFo] = linv(fvl[:nFo])
+        if nEo:
+            evq[eb:eb + nEo] = np.stack([linv(a[:nEo]), linv(b[:nEo])], 1)
+    return vv, ve, vf, fvq, evq
+
+
+MESHES = {
+    "torus": lambda: meshgen.torus(24, 16)[::-1],
+    "icosphere": lambda: meshgen.icosphere(3)[::-1],
+    "plane": lambda: meshgen.plane(13, 9)[::-1],
+    "bunnyhead": lambda: (golden("bunnyhead")["fv"], golden("bunnyhead")["xyz"]),
+}
+
+
+@pytest.mark.parametrize("name", list(MESHES))
+@pytest.mark.parametrize("patch", [32, 512])
+def test_patch_layout_encodes_exact_queries(oracle, name, patch):
+    from rxmesh_gb300 import RXMeshStatic
+    fv, x = MESHES[name]()
+    nv = len(x)
+    rx = RXMeshStatic(fv, nv, patch_size=patch, host_only=True)
+    assert rx.get_num_faces() == len(fv) and rx.get_num_vertices() == nv
+    ev_ref, _ = oracle.edges(fv)
+    assert np.array_equal(rx.input_edges(), ev_ref)  # reference edge numbering
+    vl, el, fl = rx.linear_to_input("v"), rx.linear_to_input("e"), rx.linear_to_input("f")
+    for m, n in ((vl, nv), (el, len(ev_ref)), (fl, len(fv))):
+        assert np.array_equal(np.sort(m), np.arange(n))
+    hdr, _ = rx.patches()
+    assert (hdr[:, 4] <= patch).all()
+    vv, ve, vf, fvq, evq = decode(rx)
+    off, val = oracle.vv(nv, ev_ref)
+    want = sorted_rows(off, val)
+    got = [None] * nv
+    for lin in range(nv):
+        got[vl[lin]] = tuple(sorted(vl[np.array(vv[lin], np.int64)].tolist()))
+    assert got == want
+    off, val = oracle.vv(nv, ev_ref, want_edges=True)
+    want = sorted_rows(off, val)
+    for lin in range(nv):
+        got[vl[lin]] = tuple(sorted(el[np.array(ve[lin], np.int64)].tolist()))
+    assert got == want
+    off, val = oracle.vf(nv, fv)
+    want = sorted_rows(off, val)
+    for lin in range(nv):
+        got[vl[lin]] = tuple(sorted(fl[np.array(vf[lin], np.int64)].tolist()))
+    assert got == want
+    assert np.array_equal(vl[fvq][np.argsort(fl)], np.asarray(fv))  # FV in input vertex order
+    assert np.array_equal(vl[evq][np.argsort(el)], ev_ref)          # EV as first encountered
