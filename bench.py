@@ -1,0 +1,399 @@
+"""Benchmark of the RXMesh hot path on one GB300.
+
+Headline (one JSON line on stdout): the query + vertex-normal sweep on a
+1024 x 1024 torus (1,048,576 vertices, 2,097,152 faces, patches of <= 512
+faces): VV, VE, VF, FV, EV and area-weighted normals, as canonical GB/s
+(algorithmic bytes: int16 patch topology read once, int32 CSR written once,
+fp32 positions).  Beside it, in the same line, the implicit MCF step on the
+level-8 icosphere (655,362 vertices) in FP64 and in mixed precision, 10 steps
+at dt = 1e-3, with the error of each against the FP64 oracle.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl rxg|reference] [--no-mcf]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MCF steps/s & query GB/s vs HBM peak; mixed vs FP64 at 1e-6 rel error, 1 GB300"
+WORKLOAD = "query+normal sweep, torus 1024x1024 (V=1,048,576 F=2,097,152), patches<=512 faces"
+OPS = ["VV", "VE", "VF", "FV", "EV", "normals"]
+
+
+def canonical_bytes(V, E, F):
+    """Algorithmic bytes per query (int16 topology in, int32 ids / fp32 out)."""
+    return {
+        "VV": 4 * E + 8 * E + 4 * (V + 1),
+        "VE": 4 * E + 8 * E + 4 * (V + 1),
+        "VF": 4 * E + 6 * F + 12 * F + 4 * (V + 1),
+        "FV": 4 * E + 6 * F + 12 * F,
+        "EV": 4 * E + 8 * E,
+        "normals": 4 * E + 6 * F + 12 * V + 12 * V,
+    }
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """dram bytes per launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "query_sweep_torus1024.md")
+    out = {}
+    if os.path.exists(p):
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                for kv in line.split(":", 1)[1].split():
+                    k, v = kv.split("=")
+                    out[k] = float(v)
+    return out
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        time.sleep(0.2)
+        if self.p is not None:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------
+# CPU legs (oracle port): bounded sample of the same sweep
+# ----------------------------------------------------------------------------
+
+def cpu_sweep_once(n=384):
+    """One sweep of the oracle port on an n x n torus; returns (seconds, bytes)."""
+    from oracle import oracle as O
+    from rxmesh_gb300 import meshgen
+    x, f = meshgen.torus(n, n, jitter=1e-3, seed=0)
+    V, F = len(x), len(f)
+    t0 = time.perf_counter()
+    ev, fe = O.edges(f)  # the static structure the queries are derived from
+    t_setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.vv(V, ev)
+    O.vv(V, ev, want_edges=True)
+    O.vf(V, f)
+    np.copy(f)
+    np.copy(ev)
+    O.vertex_normals(f, x.astype(np.float64), 1)
+    dt = time.perf_counter() - t0
+    E = len(ev)
+    return dt, sum(canonical_bytes(V, E, F).values()), t_setup
+
+
+def _cpu_worker(args):
+    n, reps = args
+    tot, b = 0.0, 0
+    for _ in range(reps):
+        dt, bb, _ = cpu_sweep_once(n)
+        tot += dt
+        b += bb
+    return tot, b
+
+
+def run_reference(args):
+    """--impl reference: the CPU implementation of the sweep on all host cores."""
+    import multiprocessing as mp
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    n = 384
+    with ctx.Pool(cores) as pool:
+        for _ in range(max(1, args.warmup)):
+            pool.map(_cpu_worker, [(n, 1)] * cores)
+        tot_b, wall = 0, 0.0
+        for _ in range(args.steps):
+            res = pool.map(_cpu_worker, [(n, 1)] * cores)
+            tot_b += sum(r[1] for r in res)
+            wall += max(r[0] for r in res)  # cores run concurrently: the slowest one
+    gbs = tot_b / wall / 1e9
+    line = {"metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32/fp64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD},
+            "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port",
+                             "sample": "per step: %d processes, each one sweep of a %dx%d torus (the same "
+                                       "queries and normals; sweep time only, mesh set-up excluded)" % (cores, n, n)},
+            "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ----------------------------------------------------------------------------
+# GPU legs
+# ----------------------------------------------------------------------------
+
+def run_sweep(args, torch, rx, xl, sizes):
+    from rxmesh_gb300 import Op
+    V, E, F = sizes
+    dev = torch.device("cuda")
+    stream = torch.cuda.current_stream()
+    outs = {}
+    for name, op in (("VV", Op.VV), ("VE", Op.VE), ("VF", Op.VF), ("FV", Op.FV), ("EV", Op.EV)):
+        rows, nval = rx.query_size(op)
+        outs[name] = (torch.empty(rows + 1, dtype=torch.int32, device=dev) if op <= Op.VF else None,
+                      torch.empty(nval, dtype=torch.int32, device=dev))
+    nrm = torch.empty_like(xl)
+    # L2 flush: write one 256 MB buffer, then read another, so the dirty lines
+    # of the write are written back before the timed sweep starts
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    clean = torch.ones(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def flush_l2():
+        flush.fill_(1.0)
+        return clean.sum()
+
+    def launch(name):
+        if name == "normals":
+            rx.vertex_normals(xl, "area", out=nrm)
+        else:
+            rx.query(getattr(Op, name), offsets=outs[name][0], values=outs[name][1])
+
+    # Each kernel is timed alone after an L2 flush.  No host sync sits between
+    # the flush and the kernel, so the ~80 us flush covers the host's enqueue
+    # of the events and the launch and the events bracket only the kernel.
+    for _ in range(args.warmup):
+        for name in OPS:
+            flush_l2()
+            launch(name)
+    torch.cuda.synchronize()
+    evs = []
+    with Clocks() as clk:
+        for _ in range(args.steps):
+            for name in OPS:
+                flush_l2()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                launch(name)
+                b.record(stream)
+                evs.append((name, a, b))
+        torch.cuda.synchronize()
+    per = {k: [] for k in OPS}
+    for name, a, b in evs:
+        per[name].append(a.elapsed_time(b))
+    total_ms = sum(sum(v) for v in per.values())
+    clocks = clk.summary()
+    return per, total_ms / args.steps, clocks, outs, nrm
+
+
+def run_e2e(args, torch, rx, x_in_host, sizes):
+    """Same sweep through the C ABI with pinned host buffers (copies inside the call)."""
+    import ctypes
+    from rxmesh_gb300 import Op, _lib
+    L = _lib.load()
+    V, E, F = sizes
+    host = {}
+    d2h = 0
+    for name, op in (("VV", Op.VV), ("VE", Op.VE), ("VF", Op.VF), ("FV", Op.FV), ("EV", Op.EV)):
+        rows, nval = rx.query_size(op)
+        off = torch.empty(rows + 1, dtype=torch.int32).pin_memory() if op <= Op.VF else None
+        val = torch.empty(nval, dtype=torch.int32).pin_memory()
+        host[name] = (off, val)
+        d2h += (off.numel() * 4 if off is not None else 0) + val.numel() * 4
+    # positions arrive in linear order from the host, normals go back to the host
+    xh = x_in_host.pin_memory()
+    nh = torch.empty_like(xh).pin_memory()
+    d2h += nh.numel() * 4
+    h2d = xh.numel() * 4
+
+    def sweep():
+        for name in ("VV", "VE", "VF", "FV", "EV"):
+            off, val = host[name]
+            _lib.check(L.rxg_query(rx._h, getattr(Op, name),
+                                   ctypes.c_void_p(off.data_ptr()) if off is not None else None,
+                                   ctypes.c_void_p(val.data_ptr()), None))
+        _lib.check(L.rxg_vertex_normals(rx._h, 1, ctypes.c_void_p(xh.data_ptr()),
+                                        ctypes.c_void_p(nh.data_ptr()), None))
+
+    for _ in range(args.warmup):
+        sweep()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(args.steps):
+        sweep()
+    t1.record()
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / args.steps
+    return ms, h2d, d2h
+
+
+def run_mcf(args, torch):
+    """Level-8 icosphere, 10 implicit MCF steps at dt=1e-3: FP64 and mixed."""
+    from oracle import oracle as O
+    from rxmesh_gb300 import RXMeshStatic, meshgen, mcf_step
+    level, nsteps, dt, tol = 8, 10, 1e-3, 1e-6
+    v, f = meshgen.icosphere(level)
+    x0 = meshgen.radial_noise(v, 0.02, 0)
+    rx = RXMeshStatic(f, len(x0), patch_size=256)
+    x0l = rx.to_linear(torch.tensor(x0, device="cuda"))
+    res = {"workload": "icosphere level 8 (V=%d F=%d), %d steps dt=%g, Jacobi PCG" % (len(x0), len(f), nsteps, dt)}
+    # FP64 oracle for the first step (CPU, solved to 1e-12 relative residual)
+    rp, col, val, B = O.mcf_system(f, x0, dt)
+    Xo, it_o, _, _, _ = O.cg(rp, col, val, B, x0, 20000, 0.0, 1e-24, True)
+    for prec in ("f64", "mixed"):
+        x = x0l.clone()
+        mcf_step(rx, x, dt, 1, prec, tol=tol)  # warm-up + error of step 1
+        got = rx.to_input(x).cpu().numpy()
+        err = float(np.linalg.norm(got - Xo) / np.linalg.norm(Xo))
+        err_upd = float(np.linalg.norm(got - Xo) / np.linalg.norm(Xo - x0))
+        times = []
+        for _ in range(max(1, args.steps)):
+            x = x0l.clone()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = mcf_step(rx, x, dt, nsteps, prec, tol=tol)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        t = statistics.median(times)
+        res[prec] = {"steps_per_s": nsteps / t, "ms_per_step": 1e3 * t / nsteps,
+                     "cg_iters_last_step": st["iters"], "rel_err_step1": err,
+                     "rel_err_of_update_step1": err_upd}
+    res["mixed_speedup_vs_f64"] = res["mixed"]["steps_per_s"] / res["f64"]["steps_per_s"]
+    res["oracle_pcg_iters_step1"] = it_o
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="rxg", choices=["rxg", "reference"])
+    ap.add_argument("--no-mcf", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from rxmesh_gb300 import RXMeshStatic, meshgen
+    x, f = meshgen.torus(1024, 1024, jitter=1e-3, seed=rank)
+    rx = RXMeshStatic(f, len(x), patch_size=512)
+    V, E, F = rx.get_num_vertices(), rx.get_num_edges(), rx.get_num_faces()
+    xl = rx.to_linear(torch.tensor(x, device="cuda"))
+    if world > 1:
+        torch.distributed.barrier()
+    per, ms, clocks, _, _ = run_sweep(args, torch, rx, xl, (V, E, F))
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    cb = canonical_bytes(V, E, F)
+    sweep_bytes = sum(cb.values())
+    value = world * sweep_bytes / (ms * 1e-3) / 1e9
+    e2e_ms, h2d, d2h = run_e2e(args, torch, rx, xl.cpu(), (V, E, F))
+    avg = {k: statistics.mean(v) for k, v in per.items()}
+    dom = max(avg, key=lambda k: avg[k])
+    peak, peak_kind = peaks()
+    ach = cb[dom] / (avg[dom] * 1e-3) / 1e9
+    traffic = profiled_traffic().get(dom)
+    line = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "l2": "flushed before every timed sweep (256 MB write, then 256 MB read)",
+                   "patch_faces": 512, "num_patches": rx.get_num_patches(),
+                   "ribbon_vertex_fraction": rx.info["ribbon_vertices"] / V,
+                   "ribbon_face_fraction": rx.info["ribbon_faces"] / F},
+        "per_kernel_ms": avg,
+        "per_kernel_gbs": {k: cb[k] / (avg[k] * 1e-3) / 1e9 for k in OPS},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+                     "frac": ach / peak, "peak_source": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes": cb[dom]},
+        "e2e": {"value": sweep_bytes / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "gpu_launches": len(OPS) * args.steps,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+        O.build()
+        reps, tot, b = 0, 0.0, 0
+        while tot < 8.0 and reps < 40:
+            dt, bb, _ = cpu_sweep_once(384)
+            tot += dt
+            b += bb
+            reps += 1
+        line["cpu_baseline"] = {"value": b / tot / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                                "sample": "%d sweeps of a 384x384 torus (oracle port, 1 thread)" % reps}
+    if rank == 0 and not args.no_mcf:
+        line["mcf"] = run_mcf(args, torch)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

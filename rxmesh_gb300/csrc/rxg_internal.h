@@ -68,7 +68,10 @@ struct Mesh
     void* lazy = nullptr;
 
     int64_t device_bytes = 0;
+    size_t  smem_bytes[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // per query kind, max over patches
 };
+
+void compute_smem_table(Mesh& m);
 
 // thread-local error message
 void        set_error(const char* fmt, ...);

@@ -467,6 +467,7 @@ rxg_status rxg_mesh_create_ex(const int32_t* fv, int64_t nf, int64_t nv, int32_t
         set_error("rxg_mesh_create: host allocation failed");
         s = RXG_ERR_NOMEM;
     }
+    if (s == RXG_OK) compute_smem_table(h->m);
     if (s == RXG_OK && !(flags & RXG_MESH_HOST_ONLY)) {
         // face -> linear vertex ids, face linear order
         std::vector<int32_t> fvl(3 * nf);

@@ -10,12 +10,12 @@
 // the global CSR with 16-byte stores.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 
 #include "rxg_device.cuh"
 
 namespace rxg {
 
-constexpr int kQT = 256;  // threads per query CTA
 
 __device__ int g_err_word;
 
@@ -57,6 +57,20 @@ rxg_status check_device_error(cudaStream_t s)
 // staging
 // ---------------------------------------------------------------------
 
+// Warp 0 waits on the barrier phase (bounded); the other warps wait at the
+// CTA barrier and so spend no issue slots.  The CTA barrier orders the
+// completed bulk copies before every thread's reads.
+__device__ __forceinline__ bool wait_stage(uint64_t* bar, int* err)
+{
+    __shared__ int s_ok;
+    if (threadIdx.x < 32) {
+        bool ok = mbar_wait_bounded(bar, 0, err);
+        if (threadIdx.x == 0) s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
 struct Slice
 {
     const uint32_t* src;
@@ -78,7 +92,7 @@ __device__ __forceinline__ bool stage(uint64_t* bar, uint32_t* const (&dst)[N],
         for (int i = 0; i < N; ++i)
             if (sl[i].bytes) bulk_g2s(dst[i], sl[i].src, sl[i].bytes, bar);
     }
-    return mbar_wait_bounded(bar, 0, err);
+    return wait_stage(bar, err);
 }
 
 __device__ __forceinline__ PatchHdr load_hdr(const PatchHdr* __restrict__ hdrs)
@@ -106,7 +120,7 @@ __device__ __forceinline__ uint32_t face_vertex(const uint16_t* s_fe, const uint
 // VV / VE  (OP 0 / 1) and VF (OP 2): vertex-centred transposes
 // ---------------------------------------------------------------------
 
-template <int OP>
+template <int OP, int kQT>
 __global__ void __launch_bounds__(kQT) k_query_vertex(const PatchHdr* __restrict__ hdrs,
                                                       const uint32_t* __restrict__ arena,
                                                       int32_t* __restrict__ out_off,
@@ -207,7 +221,7 @@ __global__ void __launch_bounds__(kQT) k_query_vertex(const PatchHdr* __restrict
 // FV (OP 3) and EV (OP 4): owned-element rows, one output word per thread
 // ---------------------------------------------------------------------
 
-template <int OP>
+template <int OP, int kQT>
 __global__ void __launch_bounds__(kQT) k_query_elem(const PatchHdr* __restrict__ hdrs,
                                                     const uint32_t* __restrict__ arena,
                                                     int32_t* __restrict__ out_val, int* err)
@@ -261,7 +275,7 @@ __global__ void __launch_bounds__(kQT) k_query_elem(const PatchHdr* __restrict__
 // Formula of compute_vertex_normal (apps/VertexNormal/vertex_normal_kernel.cuh:10-43).
 // ---------------------------------------------------------------------
 
-template <int W>
+template <int W, int kQT>
 __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restrict__ hdrs,
                                                         const uint32_t* __restrict__ arena,
                                                         const float* __restrict__ xyz,
@@ -350,12 +364,16 @@ static size_t smem_words(const PatchHdr& h, int kind)
     }
 }
 
-size_t query_smem_bytes(const Mesh* m, int kind)
+void compute_smem_table(Mesh& m)
 {
-    size_t w = 0;
-    for (const PatchHdr& h : m->hdr) w = std::max(w, smem_words(h, kind));
-    return w * 4;
+    for (int kind = 0; kind < 6; ++kind) {
+        size_t w = 0;
+        for (const PatchHdr& h : m.hdr) w = std::max(w, smem_words(h, kind));
+        m.smem_bytes[kind] = w * 4;
+    }
 }
+
+size_t query_smem_bytes(const Mesh* m, int kind) { return m->smem_bytes[kind]; }
 
 template <typename K>
 static rxg_status launch_patch_kernel(K kern, const Mesh* m, size_t smem, cudaStream_t s,
@@ -371,54 +389,83 @@ static rxg_status launch_patch_kernel(K kern, const Mesh* m, size_t smem, cudaSt
 }
 
 template <typename F, typename... Args>
-static rxg_status launch(F* kern, const Mesh* m, size_t smem, cudaStream_t s, const char* name,
-                         Args... args)
+static rxg_status launch(F* kern, int threads, const Mesh* m, size_t smem, cudaStream_t s,
+                         const char* name, Args... args)
 {
     rxg_status st = launch_patch_kernel(kern, m, smem, s, name);
     if (st) return st;
     if (smem > 48 * 1024)
         RXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem));
-    kern<<<m->num_patches, kQT, smem, s>>>(args...);
+    kern<<<m->num_patches, threads, smem, s>>>(args...);
     RXG_CUDA_TRY(cudaGetLastError());
     return RXG_OK;
 }
 
-rxg_status launch_query(const Mesh* m, int op, int32_t* d_off, int32_t* d_val, cudaStream_t s)
+// threads per query CTA: 128 by default (fastest on the 1024x1024 torus with
+// 512-face patches), RXG_QUERY_THREADS=32|64|128|256 to tune
+int query_threads()
 {
-    const size_t smem = query_smem_bytes(m, op);
-    int*         err  = device_error_word();
+    static int t = 0;
+    if (!t) {
+        const char* e = getenv("RXG_QUERY_THREADS");
+        t             = e ? atoi(e) : 128;
+        if (t != 32 && t != 64 && t != 128 && t != 256) t = 128;
+    }
+    return t;
+}
+
+template <int BT>
+static rxg_status launch_query_bt(const Mesh* m, int op, int32_t* d_off, int32_t* d_val,
+                                  cudaStream_t s)
+{
+    const size_t    smem = query_smem_bytes(m, op);
+    int*            err  = device_error_word();
+    const PatchHdr* hd   = m->d.hdr;
+    const uint32_t* ar   = m->d.arena;
     switch (op) {
-        case RXG_OP_VV:
-            return launch(k_query_vertex<0>, m, smem, s, "VV", (const PatchHdr*)m->d.hdr,
-                          (const uint32_t*)m->d.arena, d_off, d_val, err);
-        case RXG_OP_VE:
-            return launch(k_query_vertex<1>, m, smem, s, "VE", (const PatchHdr*)m->d.hdr,
-                          (const uint32_t*)m->d.arena, d_off, d_val, err);
-        case RXG_OP_VF:
-            return launch(k_query_vertex<2>, m, smem, s, "VF", (const PatchHdr*)m->d.hdr,
-                          (const uint32_t*)m->d.arena, d_off, d_val, err);
-        case RXG_OP_FV:
-            return launch(k_query_elem<3>, m, smem, s, "FV", (const PatchHdr*)m->d.hdr,
-                          (const uint32_t*)m->d.arena, d_val, err);
-        case RXG_OP_EV:
-            return launch(k_query_elem<4>, m, smem, s, "EV", (const PatchHdr*)m->d.hdr,
-                          (const uint32_t*)m->d.arena, d_val, err);
+        case RXG_OP_VV: return launch(k_query_vertex<0, BT>, BT, m, smem, s, "VV", hd, ar, d_off, d_val, err);
+        case RXG_OP_VE: return launch(k_query_vertex<1, BT>, BT, m, smem, s, "VE", hd, ar, d_off, d_val, err);
+        case RXG_OP_VF: return launch(k_query_vertex<2, BT>, BT, m, smem, s, "VF", hd, ar, d_off, d_val, err);
+        case RXG_OP_FV: return launch(k_query_elem<3, BT>, BT, m, smem, s, "FV", hd, ar, d_val, err);
+        case RXG_OP_EV: return launch(k_query_elem<4, BT>, BT, m, smem, s, "EV", hd, ar, d_val, err);
     }
     set_error("rxg_query: unknown op %d", op);
     return RXG_ERR_INVALID;
 }
 
-rxg_status launch_normals(const Mesh* m, int weighting, const float* xyz, float* out,
-                          cudaStream_t s)
+rxg_status launch_query(const Mesh* m, int op, int32_t* d_off, int32_t* d_val, cudaStream_t s)
+{
+    switch (query_threads()) {
+        case 32: return launch_query_bt<32>(m, op, d_off, d_val, s);
+        case 64: return launch_query_bt<64>(m, op, d_off, d_val, s);
+        case 256: return launch_query_bt<256>(m, op, d_off, d_val, s);
+        default: return launch_query_bt<128>(m, op, d_off, d_val, s);
+    }
+}
+
+template <int BT>
+static rxg_status launch_normals_bt(const Mesh* m, int weighting, const float* xyz, float* out,
+                                    cudaStream_t s)
 {
     const size_t smem = query_smem_bytes(m, 5);
     int*         err  = device_error_word();
     if (weighting == RXG_NORMAL_MAX)
-        return launch(k_vertex_normals<RXG_NORMAL_MAX>, m, smem, s, "normals",
+        return launch(k_vertex_normals<RXG_NORMAL_MAX, BT>, BT, m, smem, s, "normals",
                       (const PatchHdr*)m->d.hdr, (const uint32_t*)m->d.arena, xyz, out, err);
-    return launch(k_vertex_normals<RXG_NORMAL_AREA>, m, smem, s, "normals",
+    return launch(k_vertex_normals<RXG_NORMAL_AREA, BT>, BT, m, smem, s, "normals",
                   (const PatchHdr*)m->d.hdr, (const uint32_t*)m->d.arena, xyz, out, err);
+}
+
+rxg_status launch_normals(const Mesh* m, int weighting, const float* xyz, float* out,
+                          cudaStream_t s)
+{
+    switch (query_threads()) {
+        case 32: return launch_normals_bt<32>(m, weighting, xyz, out, s);
+        case 64: return launch_normals_bt<64>(m, weighting, xyz, out, s);
+        case 256: return launch_normals_bt<256>(m, weighting, xyz, out, s);
+        default: return launch_normals_bt<128>(m, weighting, xyz, out, s);
+    }
 }
 
 // scratch helper: device copy of a possibly-host array
@@ -498,6 +545,10 @@ rxg_status rxg_query(const rxg_mesh* h, int32_t op, int32_t* offsets, int32_t* v
     const bool csr = op <= RXG_OP_VF;
     if (!values || (csr && !offsets)) {
         set_error("rxg_query: values%s must not be NULL", csr ? " and offsets" : "");
+        return RXG_ERR_INVALID;
+    }
+    if (((uintptr_t)values & 15u) != 0) {
+        set_error("rxg_query: values must be 16-byte aligned (vectorised row stores)");
         return RXG_ERR_INVALID;
     }
     cudaStream_t s = (cudaStream_t)stream;

@@ -23,7 +23,9 @@ def to_input_csr(rx, A):
     return sp.csr_matrix((S.data, (vl[S.row], vl[S.col])), shape=(n, n))
 
 
-@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 2e-6)])
+# FP64 assembly: 1e-12 of the row diagonal; FP32 weights (FP64 only for
+# triangles with an angle below 1e-3 rad): 1e-5 of the row diagonal.
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-12), (torch.float32, 1e-5)])
 @pytest.mark.parametrize("kind", ["sphere", "plane", "bunnyhead"])
 def test_mcf_assembly_matches_oracle(oracle, dtype, tol, kind):
     import scipy.sparse as sp
@@ -44,10 +46,12 @@ def test_mcf_assembly_matches_oracle(oracle, dtype, tol, kind):
     rp, col, val, Bo = oracle.mcf_system(f, x, 0.01)
     Ao = sp.csr_matrix((val, col, rp), shape=Ag.shape)
     assert Ag.nnz == Ao.nnz
-    scale = abs(Ao).max()
-    assert abs(Ag - Ao).max() <= tol * scale
+    diag = Ao.diagonal()
+    D = abs(Ag - Ao).tocsr()
+    row_err = np.array([D[i].max() if D[i].nnz else 0.0 for i in range(D.shape[0])])
+    assert (row_err <= tol * diag).all(), (row_err / diag).max()
     Bg = rx.to_input(B.to(torch.float64)).cpu().numpy()
-    assert np.abs(Bg - Bo).max() <= tol * np.abs(Bo).max()
+    assert (np.abs(Bg - Bo).max(1) <= tol * np.abs(Bo).max(1) + 1e-300).all()
 
 
 def test_spmm_matches_oracle(oracle):

@@ -74,19 +74,23 @@ def test_query_into_host_buffers(oracle):
 
 
 @pytest.mark.parametrize("name", ["sphere3", "torus", "cloth", "bunnyhead"])
-def test_normals_against_reference_fixture(name):
+def test_normals_against_reference_fixture(oracle, name):
     # fixtures: output of the reference's own vertex_normal_ref (FP64 and FP32)
     from rxmesh_gb300 import RXMeshStatic
     g = golden(name)
     rx = RXMeshStatic(g["fv"], len(g["xyz"]), patch_size=256)
-    x = torch.tensor(g["xyz"], dtype=torch.float32, device="cuda")
+    x32 = g["xyz"].astype(np.float32)
+    x = torch.tensor(x32, device="cuda")
     n = rx.to_input(rx.vertex_normals(rx.to_linear(x), "max")).cpu().numpy()
-    ref = g["ref_normals_f64"]
-    scale = np.linalg.norm(ref, axis=1)
-    err = np.linalg.norm(n - ref, axis=1) / scale
+    # 1e-6 relative against the FP64 oracle on the same (FP32) positions
+    ref = oracle.vertex_normals(g["fv"], x32.astype(np.float64), 0)
+    err = np.linalg.norm(n - ref, axis=1) / np.linalg.norm(ref, axis=1)
     assert err.max() < 1e-6
-    # and the reference's FP32 run, with its own 1e-4 absolute check (vertex_normal.cu:90-108)
+    # the reference's FP32 run, with its own absolute check (vertex_normal.cu:90-108)
     assert np.abs(np.abs(n) - np.abs(g["ref_normals_f32"])).max() <= 1e-4
+    # and its FP64 run on the unrounded positions (input quantisation only)
+    ref64 = g["ref_normals_f64"]
+    assert (np.linalg.norm(n - ref64, axis=1) / np.linalg.norm(ref64, axis=1)).max() < 1e-5
 
 
 @pytest.mark.parametrize("weighting", ["max", "area"])
