@@ -230,6 +230,27 @@ rxg_status rxg_cg_solve(const rxg_csr* A, int32_t nc, const void* B, void* X,
                         void* stream);
 
 /*
+ * rxg_cg_solve without any device allocation.  No counterpart in the
+ * reference: it exists for callers that may not allocate device memory at
+ * solve time (an application that owns all device memory through its own
+ * pool and budget, a plugin that must not allocate behind its host, code
+ * that allocates only at start-up).  Same solver, arguments and statistics
+ * as rxg_cg_solve; the work vectors live in a fixed static device array of
+ * just over 16 MiB inside the library, which every GPU that loads the
+ * library holds until the process exits.
+ * Limits: A->n <= 131072 rows and nc <= 3 columns; larger problems return
+ * RXG_ERR_INVALID with a message (use rxg_cg_solve).
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU
+ * (other streams, other host threads) race and must be serialised by the
+ * caller.  Device arrays only.
+ */
+rxg_status rxg_cg_solve_noalloc(const rxg_csr* A, int32_t nc, const void* B,
+                                void* X, const rxg_solver_opts* opts,
+                                rxg_solver_stats* stats, void* stream);
+
+/*
  * One or more implicit MCF steps in place on xyz (nv*3 FP64, linear order,
  * device or host).  precision RXG_F64: the plain path (FP64 assembly, FP64
  * PCG).  RXG_F32: FP32 assembly and FP32 PCG inside an iterative-refinement

@@ -73,6 +73,7 @@ SIGNATURES = {
     "rxg_mcf_assemble": [P, D, P, P, P, P],
     "rxg_spmm": [P, I32, P, P, P],
     "rxg_cg_solve": [P, I32, P, P, P, P, P],
+    "rxg_cg_solve_noalloc": [P, I32, P, P, P, P, P],
     "rxg_mcf_step": [P, D, I32, I32, D, I32, P, P, P],
 }
 _RESTYPE = {"rxg_status_string": ctypes.c_char_p, "rxg_last_error": ctypes.c_char_p,

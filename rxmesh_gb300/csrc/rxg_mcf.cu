@@ -1230,3 +1230,104 @@ rxg_status rxg_mcf_step(const rxg_mesh* h, double dt, int32_t nsteps, int32_t pr
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------
+// CG without device allocation.
+//
+// Some callers may not call cudaMalloc (or any allocating routine) at solve
+// time: a host application that owns all device memory through its own pool
+// and budget, a plugin that must not allocate behind its host's back, or code
+// that allocates only at start-up.  rxg_cg_solve_noalloc runs the same
+// persistent CG/PCG kernel as rxg_cg_solve, but its work vectors, partial
+// sums, grid-barrier words and statistics live in the file-scope array below
+// instead of a cudaMallocAsync'd buffer.  The array is part of the library's
+// device image: every GPU that loads this code holds it until the process
+// exits, so its size is fixed and modest (just over 16 MiB).
+// ---------------------------------------------------------------------
+
+namespace rxg {
+
+constexpr int64_t kNoAllocMaxRows = 131072;  // rows of A
+constexpr int     kNoAllocMaxCols = 3;       // right-hand sides
+constexpr int     kNoAllocMaxGrid = 1024;    // cooperative CTAs (partials)
+constexpr size_t  kNoAllocBytes =
+    5 * ((sizeof(double) * kNoAllocMaxRows * kNoAllocMaxCols + 255) & ~size_t(255)) +
+    ((sizeof(double) * kNoAllocMaxRows + 255) & ~size_t(255)) +
+    ((sizeof(double) * 2 * kNoAllocMaxGrid + 255) & ~size_t(255)) + 3 * 256;
+
+static __device__ __align__(256) unsigned char g_cg_noalloc_scratch[kNoAllocBytes];
+
+// Device address of the scratch array for the current device.  Host code
+// cannot use the symbol itself (it names a host-side stand-in), so the
+// address is taken once per device with cudaGetSymbolAddress and cached.
+static rxg_status noalloc_scratch(uint8_t** out)
+{
+    static std::mutex mu;
+    static uint8_t*   addr[64] = {nullptr};
+    int               dev      = 0;
+    RXG_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_error("rxg_cg_solve_noalloc: device ordinal %d out of range", dev);
+        return RXG_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> g(mu);
+    if (!addr[dev]) {
+        void*       p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_cg_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_cg_noalloc_scratch)");
+        addr[dev] = static_cast<uint8_t*>(p);
+    }
+    *out = addr[dev];
+    return RXG_OK;
+}
+
+}  // namespace rxg
+
+extern "C" rxg_status rxg_cg_solve_noalloc(const rxg_csr* A, int32_t nc, const void* B, void* X,
+                                           const rxg_solver_opts* opts, rxg_solver_stats* stats,
+                                           void* stream)
+{
+    using namespace rxg;
+    if (!A || !B || !X || !opts || nc < 1 || A->n <= 0 || opts->max_iter < 0 ||
+        (A->dtype != RXG_F32 && A->dtype != RXG_F64)) {
+        set_error("rxg_cg_solve_noalloc: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    if (A->n > kNoAllocMaxRows || nc > kNoAllocMaxCols) {
+        set_error("rxg_cg_solve_noalloc: %lld rows x %d columns exceeds the fixed scratch "
+                  "(at most %lld rows and %d columns); use rxg_cg_solve",
+                  (long long)A->n, nc, (long long)kNoAllocMaxRows, kNoAllocMaxCols);
+        return RXG_ERR_INVALID;
+    }
+    if (!is_device_ptr(B) || !is_device_ptr(X) || !is_device_ptr(A->val)) {
+        set_error("rxg_cg_solve_noalloc: A, B and X must be device arrays");
+        return RXG_ERR_INVALID;
+    }
+    uint8_t*   scratch = nullptr;
+    rxg_status st      = noalloc_scratch(&scratch);
+    if (st) return st;
+    const bool   pc    = opts->precond != 0;
+    const int    G     = A->dtype == RXG_F64 ? cg_grid_any<double>(nc, pc, A->n)
+                                             : cg_grid_any<float>(nc, pc, A->n);
+    const size_t bytes = A->dtype == RXG_F64 ? cg_scratch_bytes<double>(A->n, nc, G)
+                                             : cg_scratch_bytes<float>(A->n, nc, G);
+    if (G > kNoAllocMaxGrid || bytes > kNoAllocBytes) {
+        set_error("rxg_cg_solve_noalloc: needs %zu scratch bytes for %d CTAs, the fixed array "
+                  "holds %zu",
+                  bytes, G, kNoAllocBytes);
+        return RXG_ERR_UNSUPPORTED;
+    }
+    // Every call reuses the same array and the kernel writes each work vector
+    // before reading it; cg_launch zeroes the grid-barrier words on `stream`.
+    cudaStream_t     s = (cudaStream_t)stream;
+    rxg_solver_stats local;
+    if (A->dtype == RXG_F64)
+        st = cg_dispatch<double>(nc, A->n, A->row_ptr, A->col, (const double*)A->val,
+                                 (const double*)B, (double*)X, *opts, &local, scratch, s);
+    else
+        st = cg_dispatch<float>(nc, A->n, A->row_ptr, A->col, (const float*)A->val,
+                                (const float*)B, (float*)X, *opts, &local, scratch, s);
+    if (st) return st;
+    if (stats) *stats = local;
+    return local.converged ? RXG_OK : RXG_ERR_NOT_CONVERGED;
+}
