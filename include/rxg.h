@@ -89,8 +89,11 @@ void       rxg_mesh_destroy(rxg_mesh* m);
 
 /* rxg_mesh_create with flags.  RXG_MESH_HOST_ONLY builds the patches on the
  * host and uploads nothing (for inspecting a partition without a GPU; such a
- * mesh can only be passed to the rxg_mesh_* introspection calls). */
-enum { RXG_MESH_HOST_ONLY = 1 };
+ * mesh can only be passed to the rxg_mesh_* introspection calls).
+ * RXG_MESH_SPLIT_COMPONENTS never lets a patch span two connected
+ * components, so each component's elements get contiguous linear ids in
+ * input order of components (used to pack many meshes into one). */
+enum { RXG_MESH_HOST_ONLY = 1, RXG_MESH_SPLIT_COMPONENTS = 2 };
 rxg_status rxg_mesh_create_ex(const int32_t* fv, int64_t nf, int64_t nv,
                               int32_t patch_faces, int32_t flags, rxg_mesh** out);
 
@@ -252,16 +255,118 @@ rxg_status rxg_cg_solve_noalloc(const rxg_csr* A, int32_t nc, const void* B,
 
 /*
  * One or more implicit MCF steps in place on xyz (nv*3 FP64, linear order,
- * device or host).  precision RXG_F64: the plain path (FP64 assembly, FP64
- * PCG).  RXG_F32: FP32 assembly and FP32 PCG inside an iterative-refinement
- * loop whose residual is recomputed in FP64.  Stops when the FP64 relative
- * residual |B - A x| / |B - A x_start| < tol (or max_iter PCG iterations).
+ * device or host).  precision RXG_F64: the plain path (FP64 assembly and the
+ * reference's Jacobi-PCG recurrence in FP64).  RXG_F32: FP32 assembly (FP64
+ * for triangles with an angle below 1e-3 rad) and FP32 Jacobi-PCG inner
+ * solves inside an iterative-refinement loop whose residual B - A x is
+ * accumulated in FP64.  Both stop when the Jacobi-weighted residual
+ * r.D^-1 r has fallen by tol^2 from its value at the step's start (the PCG
+ * measure of pcg_solver.h:34-144), or after max_iter PCG iterations.
  * stats (may be NULL) receives the totals of the last step.
  * (mcf(), apps/MCF/mcf.cu:93-134, run_cg apps/MCF/mcf_cg.h:12-129)
  */
 rxg_status rxg_mcf_step(const rxg_mesh* m, double dt, int32_t nsteps,
                         int32_t precision, double tol, int32_t max_iter,
                         double* xyz, rxg_solver_stats* stats, void* stream);
+
+/*
+ * Adjoint of one plain (FP64) implicit MCF step x_out = A(x_in)^{-1} B(x_in):
+ * given g_out = dl/dx_out, writes g_in = dl/dx_in, including the dependence
+ * of the cotangent weights and Voronoi areas on x_in.  One extra Jacobi-PCG
+ * solve with the same matrix (A is symmetric) to relative residual tol.
+ * All arrays nv*3 FP64, linear order, device.  No counterpart in the
+ * reference (its MCF is not differentiable); the forward it inverts is
+ * mcf_A_setup / mcf_B_setup (apps/MCF/mcf_kernels.cuh:302-426).
+ */
+rxg_status rxg_mcf_step_backward(const rxg_mesh* m, double dt,
+                                 const double* x_in, const double* x_out,
+                                 const double* g_out, double* g_in, double tol,
+                                 int32_t max_iter, rxg_solver_stats* stats,
+                                 void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Batched MCF: many meshes in one persistent launch                    */
+/* ------------------------------------------------------------------ */
+
+typedef struct rxg_batch rxg_batch;
+
+/*
+ * Pack nmesh triangle meshes into one batch (host arrays).  fv holds the
+ * meshes' faces one after another, each with vertex ids local to its mesh;
+ * nf[m] / nv[m] are the face / vertex counts of mesh m.  Internally one mesh
+ * whose patches never span two meshes (RXMeshStatic packing several meshes,
+ * include/rxmesh/rxmesh_static.cu:66-160).  Every mesh must be manifold and
+ * use all of its vertices.
+ */
+rxg_status rxg_batch_create(int32_t nmesh, const int32_t* fv, const int64_t* nf,
+                            const int64_t* nv, int32_t patch_faces,
+                            rxg_batch** out);
+void       rxg_batch_destroy(rxg_batch* b);
+/* The union mesh (for queries and numbering); owned by the batch. */
+rxg_status rxg_batch_mesh(const rxg_batch* b, const rxg_mesh** mesh);
+
+/*
+ * nsteps mixed-precision implicit MCF steps (as rxg_mcf_step with
+ * RXG_F32) on every mesh of the batch, in place on xyz (device, sum(nv)*3
+ * FP64, meshes one after another in their input order).  One persistent
+ * launch: each CTA takes a mesh (largest first) and runs its whole flow.
+ * The first call on a batch allocates its work arrays; later calls
+ * allocate nothing and do not synchronise, so they can be captured in a
+ * CUDA graph.  No counterpart in the reference (one mesh per launch there).
+ */
+rxg_status rxg_batch_mcf(rxg_batch* b, double dt, int32_t nsteps, double tol,
+                         int32_t max_iter, double* xyz, void* stream);
+
+/* Per-mesh PCG iterations and convergence flags of the last rxg_batch_mcf
+ * (host arrays of nmesh ints, either may be NULL; synchronises). */
+rxg_status rxg_batch_stats(const rxg_batch* b, int32_t* iters, int32_t* converged);
+
+/*
+ * Autotuner: times rxg_batch_mcf on a copy of xyz for CTA sizes 256/512/1024
+ * and 1-8 CTAs per SM (within occupancy) and keeps the fastest for later
+ * calls.  xyz is not modified.
+ */
+rxg_status rxg_batch_autotune(rxg_batch* b, double dt, int32_t nsteps, double tol,
+                              int32_t max_iter, const double* xyz, int32_t* threads,
+                              int32_t* blocks_per_sm, float* best_ms, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Per-face ARAP energy, gradient, Hessian (DiffScalarProblem path)     */
+/* ------------------------------------------------------------------ */
+
+/* 3x3-block CSR over the [diagonal, one-ring] pattern of rxg_mcf_pattern_size
+ * (HessianSparseMatrix<T,3>, diff/hessian_sparse_matrix.h:16-137); val holds
+ * nnzb row-major 3x3 blocks. */
+typedef struct rxg_bcsr {
+    int64_t  n;       /* block rows */
+    int64_t  nnzb;    /* blocks */
+    int32_t* row_ptr; /* device, n+1 */
+    int32_t* col;     /* device, nnzb */
+    void*    val;     /* device, 9*nnzb of dtype */
+    int32_t  dtype;
+} rxg_bcsr;
+
+/*
+ * Flat rest frame per face from rest positions (FP64, nv*3, linear order):
+ * rest receives Mr^{-1} (row-major 2x2, nf*4 of dtype, face linear order),
+ * Mr built as apps/Param/param.cu:113-141 does.  Device arrays.
+ */
+rxg_status rxg_arap_rest(const rxg_mesh* m, const double* xyz_rest,
+                         int32_t dtype, void* rest, void* stream);
+
+/*
+ * Per-face ARAP energy E_f = A_f ||J_f - R(J_f)||_F^2, J_f = [b-a, c-a] Mr^{-1},
+ * R the polar factor, A_f the rest area; its gradient and exact Hessian
+ * (DiffScalarProblem::eval_terms / grad / hess / get_current_loss,
+ * diff/diff_scalar_problem.h:310-363; per-element kernel
+ * diff/diff_query_kernel.cuh:199-322).  x: nv*3 of dtype (linear order);
+ * energy: total (device or host double, may be NULL); face_E (nf, may be
+ * NULL); grad (nv*3, may be NULL, overwritten); hess (may be NULL; row_ptr,
+ * col and val are overwritten).  Needs a manifold mesh.
+ */
+rxg_status rxg_arap_eval(const rxg_mesh* m, int32_t dtype, const void* x,
+                         const void* rest, double* energy, void* face_E,
+                         void* grad, rxg_bcsr* hess, void* stream);
 
 #ifdef __cplusplus
 }

@@ -14,6 +14,7 @@ from . import _lib
 from ._lib import RXGError, check
 
 __all__ = ["Op", "RXMeshStatic", "SparseMatrix", "CGSolver", "PCGSolver", "RXGError",
+           "DiffScalarProblem", "BlockSparseMatrix", "mcf_step", "MeshBatch",
            "device_check"]
 
 
@@ -199,4 +200,6 @@ class RXMeshStatic:
         return out
 
 
-from ._solvers import SparseMatrix, CGSolver, PCGSolver, mcf_step  # noqa: E402
+from ._solvers import SparseMatrix, CGSolver, PCGSolver, mcf_step, MeshBatch  # noqa: E402
+from ._diff import (DiffScalarProblem, BlockSparseMatrix, ArapEnergy, MCFFlow,  # noqa: E402
+                    arap_energy, mcf_flow, mcf_step_backward)

@@ -1,0 +1,169 @@
+"""DiffScalarProblem mirror for the per-face ARAP term, and the torch autograd
+bindings of the differentiable path.
+
+DiffScalarProblem (include/rxmesh/diff/diff_scalar_problem.h:27-401) takes
+user lambdas; lambdas cannot cross the C ABI, so the one energy of this path
+(per-face ARAP against a flat rest frame) is a fixed term here:
+`DiffScalarProblem(rx).add_arap_term(rest_xyz)` then `eval_terms(x)`.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+from ._lib import check
+
+_DT = {torch.float32: 0, torch.float64: 1}
+
+
+def _stream(stream=None):
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class BlockSparseMatrix:
+    """3x3-block CSR over the [diagonal, one-ring] pattern (HessianSparseMatrix)."""
+
+    def __init__(self, n, nnzb, dtype, device):
+        self.row_ptr = torch.zeros(n + 1, dtype=torch.int32, device=device)
+        self.col = torch.zeros(nnzb, dtype=torch.int32, device=device)
+        self.val = torch.zeros(nnzb, 3, 3, dtype=dtype, device=device)
+
+    def bcsr(self):
+        b = _lib.BCSR()
+        b.n = self.row_ptr.numel() - 1
+        b.nnzb = self.col.numel()
+        b.row_ptr = self.row_ptr.data_ptr()
+        b.col = self.col.data_ptr()
+        b.val = self.val.data_ptr()
+        b.dtype = _DT[self.val.dtype]
+        return b
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        n = self.row_ptr.numel() - 1
+        return sp.bsr_matrix((self.val.cpu().numpy(), self.col.cpu().numpy(),
+                              self.row_ptr.cpu().numpy()), shape=(3 * n, 3 * n))
+
+
+class DiffScalarProblem:
+    """Energy / gradient / Hessian assembly driver (DiffScalarProblem<T,3,VertexHandle,true>)."""
+
+    def __init__(self, rx, dtype=torch.float64, assemble_hessian=True):
+        self.rx = rx
+        self.dtype = dtype
+        self.assemble_hessian = assemble_hessian
+        self._L = _lib.load()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        n, nnz = ctypes.c_int64(), ctypes.c_int64()
+        check(self._L.rxg_mcf_pattern_size(rx._h, ctypes.byref(n), ctypes.byref(nnz)))
+        self.grad = torch.zeros(n.value, 3, dtype=dtype, device=dev)
+        self.face_energy = torch.zeros(rx.get_num_faces(), dtype=dtype, device=dev)
+        self.hess = BlockSparseMatrix(n.value, nnz.value, dtype, dev) if assemble_hessian else None
+        self.rest = None
+        self._loss = None
+
+    def add_arap_term(self, rest_xyz_lin):
+        """Per-face ARAP term against the flat rest frame of rest_xyz_lin (nv,3, linear order)."""
+        xr = rest_xyz_lin.to(torch.float64).contiguous()
+        self.rest = torch.empty(self.rx.get_num_faces(), 4, dtype=self.dtype, device=xr.device)
+        check(self._L.rxg_arap_rest(self.rx._h, _p(xr), _DT[self.dtype], _p(self.rest), _stream()))
+        return self
+
+    def eval_terms(self, x_lin, with_hessian=None, stream=None):
+        """Energy, gradient (and Hessian) at x_lin (nv,3, linear order)."""
+        if self.rest is None:
+            raise RuntimeError("add_arap_term() first")
+        x = x_lin.to(self.dtype).contiguous()
+        h = self.assemble_hessian if with_hessian is None else with_hessian
+        e = torch.zeros(1, dtype=torch.float64, device=x.device)
+        b = self.hess.bcsr() if (h and self.hess is not None) else None
+        check(self._L.rxg_arap_eval(self.rx._h, _DT[self.dtype], _p(x), _p(self.rest), _p(e),
+                                    _p(self.face_energy), _p(self.grad),
+                                    ctypes.byref(b) if b is not None else None, _stream(stream)))
+        self._loss = e
+        return e
+
+    def get_current_loss(self):
+        return float(self._loss.item())
+
+
+def mcf_step_backward(rx, x_in, x_out, g_out, dt, tol=1e-12, max_iter=20000, stream=None):
+    """dl/dx_in of one plain implicit MCF step, given dl/dx_out (rxg_mcf_step_backward)."""
+    L = _lib.load()
+    g_in = torch.empty_like(x_in)
+    st = _lib.SolverStats()
+    rc = L.rxg_mcf_step_backward(rx._h, float(dt), _p(x_in.contiguous()), _p(x_out.contiguous()),
+                                 _p(g_out.contiguous()), _p(g_in), float(tol), int(max_iter),
+                                 ctypes.byref(st), _stream(stream))
+    if rc not in (0, 6):
+        check(rc)
+    return g_in
+
+
+class ArapEnergy(torch.autograd.Function):
+    """E = sum_f A_f ||J_f - R(J_f)||^2 at linear-order positions x (problem from DiffScalarProblem)."""
+
+    @staticmethod
+    def forward(ctx, x_lin, problem):
+        e = problem.eval_terms(x_lin, with_hessian=False)
+        ctx.save_for_backward(problem.grad.clone().to(x_lin.dtype))
+        return e.to(x_lin.dtype).reshape(())
+
+    @staticmethod
+    def backward(ctx, go):
+        (g,) = ctx.saved_tensors
+        return go * g, None
+
+
+class MCFFlow(torch.autograd.Function):
+    """nsteps plain implicit MCF steps from x0 (linear order, FP64), differentiable in x0.
+
+    The backward recomputes the flow segment by segment from positions saved
+    every `checkpoint_every` steps (memory O(nsteps/k + k) states) and runs
+    rxg_mcf_step_backward through each step in reverse."""
+
+    @staticmethod
+    def forward(ctx, x0_lin, rx, dt, nsteps, checkpoint_every=5, tol=1e-12, max_iter=20000):
+        from ._solvers import mcf_step
+        x = x0_lin.detach().to(torch.float64).contiguous().clone()
+        ckpts = [x.clone()]
+        for t in range(nsteps):
+            mcf_step(rx, x, dt, 1, "f64", tol=tol, max_iter=max_iter)
+            if (t + 1) % checkpoint_every == 0 and t + 1 < nsteps:
+                ckpts.append(x.clone())
+        ctx.rx, ctx.dt, ctx.nsteps, ctx.k = rx, dt, nsteps, checkpoint_every
+        ctx.tol, ctx.max_iter = tol, max_iter
+        ctx.save_for_backward(*ckpts)
+        return x
+
+    @staticmethod
+    def backward(ctx, g):
+        from ._solvers import mcf_step
+        ckpts = ctx.saved_tensors
+        g = g.to(torch.float64).contiguous()
+        k, n = ctx.k, ctx.nsteps
+        for seg in reversed(range(len(ckpts))):
+            start = seg * k
+            end = min(start + k, n)
+            states = [ckpts[seg]]
+            for _ in range(start, end):
+                x = states[-1].clone()
+                mcf_step(ctx.rx, x, ctx.dt, 1, "f64", tol=ctx.tol, max_iter=ctx.max_iter)
+                states.append(x)
+            for t in reversed(range(end - start)):
+                g = mcf_step_backward(ctx.rx, states[t], states[t + 1], g, ctx.dt, ctx.tol, ctx.max_iter)
+        return g, None, None, None, None, None, None
+
+
+def mcf_flow(x0_lin, rx, dt, nsteps, checkpoint_every=5, tol=1e-12, max_iter=20000):
+    return MCFFlow.apply(x0_lin, rx, dt, nsteps, checkpoint_every, tol, max_iter)
+
+
+def arap_energy(x_lin, problem):
+    return ArapEnergy.apply(x_lin, problem)

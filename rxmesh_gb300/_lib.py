@@ -37,6 +37,11 @@ class CSR(ctypes.Structure):
                 ("col", ctypes.c_void_p), ("val", ctypes.c_void_p), ("dtype", ctypes.c_int32)]
 
 
+class BCSR(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("nnzb", ctypes.c_int64), ("row_ptr", ctypes.c_void_p),
+                ("col", ctypes.c_void_p), ("val", ctypes.c_void_p), ("dtype", ctypes.c_int32)]
+
+
 class SolverOpts(ctypes.Structure):
     _fields_ = [("max_iter", ctypes.c_int32), ("abs_tol", ctypes.c_double),
                 ("rel_tol", ctypes.c_double), ("precond", ctypes.c_int32)]
@@ -75,9 +80,18 @@ SIGNATURES = {
     "rxg_cg_solve": [P, I32, P, P, P, P, P],
     "rxg_cg_solve_noalloc": [P, I32, P, P, P, P, P],
     "rxg_mcf_step": [P, D, I32, I32, D, I32, P, P, P],
+    "rxg_mcf_step_backward": [P, D, P, P, P, P, D, I32, P, P],
+    "rxg_arap_rest": [P, P, I32, P, P],
+    "rxg_batch_create": [I32, P, P, P, I32, P],
+    "rxg_batch_destroy": [P],
+    "rxg_batch_mesh": [P, P],
+    "rxg_batch_mcf": [P, D, I32, D, I32, P, P],
+    "rxg_batch_stats": [P, P, P],
+    "rxg_batch_autotune": [P, D, I32, D, I32, P, P, P, P, P],
+    "rxg_arap_eval": [P, I32, P, P, P, P, P, P, P],
 }
 _RESTYPE = {"rxg_status_string": ctypes.c_char_p, "rxg_last_error": ctypes.c_char_p,
-            "rxg_mesh_destroy": None}
+            "rxg_mesh_destroy": None, "rxg_batch_destroy": None}
 
 
 def lib_path():

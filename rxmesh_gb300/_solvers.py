@@ -145,3 +145,58 @@ def mcf_step(rx, xyz_lin, dt, nsteps=1, precision="f64", tol=1e-6, max_iter=5000
         check(rc)
     return {"iters": st.iters, "converged": bool(st.converged), "start_res": st.start_res,
             "final_res": st.final_res}
+
+
+class MeshBatch:
+    """Many meshes packed for one-launch batched MCF (rxg_batch_*).
+
+    meshes: list of (fv, nv) with vertex ids local to each mesh.  Positions
+    are passed as one (sum nv, 3) float64 CUDA tensor, meshes one after
+    another in their input order."""
+
+    def __init__(self, meshes, patch_size=256):
+        import numpy as np
+        self._L = _lib.load()
+        fvs = [np.ascontiguousarray(f, np.int32).reshape(-1, 3) for f, _ in meshes]
+        nf = np.array([len(f) for f in fvs], np.int64)
+        nv = np.array([int(v) for _, v in meshes], np.int64)
+        allf = np.ascontiguousarray(np.concatenate(fvs), np.int32)
+        h = ctypes.c_void_p()
+        check(self._L.rxg_batch_create(len(fvs), allf.ctypes.data, nf.ctypes.data, nv.ctypes.data,
+                                       int(patch_size), ctypes.byref(h)))
+        self._h = h
+        self.nmesh = len(fvs)
+        self.nv = nv
+        self.nf = nf
+        self.voff = np.concatenate([[0], np.cumsum(nv)])
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._L.rxg_batch_destroy(h)
+            self._h = None
+
+    def mcf(self, xyz, dt, nsteps=1, tol=1e-6, max_iter=5000, stream=None):
+        """Mixed-precision implicit MCF on every mesh, in place on xyz."""
+        if xyz.dtype != torch.float64 or not xyz.is_cuda or not xyz.is_contiguous():
+            raise ValueError("xyz must be a contiguous float64 CUDA tensor")
+        check(self._L.rxg_batch_mcf(self._h, float(dt), int(nsteps), float(tol), int(max_iter),
+                                    _ptr(xyz), _stream(stream)))
+        return xyz
+
+    def stats(self):
+        import numpy as np
+        it = np.empty(self.nmesh, np.int32)
+        cv = np.empty(self.nmesh, np.int32)
+        check(self._L.rxg_batch_stats(self._h, it.ctypes.data, cv.ctypes.data))
+        return it, cv.astype(bool)
+
+    def autotune(self, xyz, dt, nsteps=1, tol=1e-6, max_iter=5000, stream=None):
+        """Pick the fastest CTA size / CTAs per SM for this batch (xyz untouched)."""
+        t = ctypes.c_int32()
+        b = ctypes.c_int32()
+        ms = ctypes.c_float()
+        check(self._L.rxg_batch_autotune(self._h, float(dt), int(nsteps), float(tol), int(max_iter),
+                                         _ptr(xyz), ctypes.byref(t), ctypes.byref(b), ctypes.byref(ms),
+                                         _stream(stream)))
+        return t.value, b.value, ms.value

@@ -1,0 +1,414 @@
+// Per-face ARAP energy, gradient and 3x3-block Hessian (the DiffScalarProblem
+// path: diff/diff_scalar_problem.h:310-321, diff/diff_query_kernel.cuh:199-322,
+// diff/hessian_sparse_matrix.h:16-137), written analytically instead of with
+// forward-mode AD.
+//
+// Energy of face f with rest frame Mr (param.cu:113-141) and deformed edge
+// matrix M = [b-a, c-a] (3x2): J = M Mr^{-1} = [j1 j2],
+//   E_f = A_f * ||J - R(J)||_F^2 = A_f * (s - 2 sqrt(s + 2d) + 2),
+//   s = |j1|^2 + |j2|^2 = s1^2 + s2^2,  d = |j1 x j2| = s1 s2,
+// with R(J) the polar factor and s1, s2 the singular values of J.
+//
+// Assembly is a vertex-centred gather: each vertex walks the faces of its
+// oriented fan, recomputes their 6x6 Hessians in J-space and writes its own
+// block row [diag, ring...] once, so no atomics are needed and the result
+// is deterministic.
+#include <algorithm>
+#include <cfloat>
+
+#include "rxg_device.cuh"
+#include "rxg_lazy.h"
+
+namespace rxg {
+
+template <typename T>
+struct FaceDeriv
+{
+    T E;
+    T gE[6];     // dE/du, u = [j1; j2]
+    T Hu[6][6];  // d2E/du2
+    T d[3][2];   // u_k = sum_v d[v][k] x_v
+};
+
+template <typename T>
+__device__ __forceinline__ void cross3(const T* a, const T* b, T* c)
+{
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+template <typename T, bool HESS>
+__device__ __forceinline__ void arap_face(const T* x9, const T* mi, T A, FaceDeriv<T>& o)
+{
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        o.d[1][k] = mi[k];
+        o.d[2][k] = mi[2 + k];
+        o.d[0][k] = -(o.d[1][k] + o.d[2][k]);
+    }
+    T u[6];
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            u[3 * k + c] = o.d[0][k] * x9[c] + o.d[1][k] * x9[3 + c] + o.d[2][k] * x9[6 + c];
+    const T* j1 = u;
+    const T* j2 = u + 3;
+    const T  s  = j1[0] * j1[0] + j1[1] * j1[1] + j1[2] * j1[2] + j2[0] * j2[0] + j2[1] * j2[1] +
+               j2[2] * j2[2];
+    T w[3];
+    cross3(j1, j2, w);
+    const T d  = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    const T q  = s + T(2) * d;
+    const T sq = sqrt(q);
+    {
+        // Energy without cancellation near the rest state: with M = J^T J - I
+        // and mu its eigenvalues (sigma^2 - 1), (sigma - 1)^2 equals
+        // mu^2 / (sqrt(1 + mu) + 1)^2.  (s - 2 sqrt(q) + 2 loses every digit
+        // of a small strain in FP32.)
+        const T m00 = fma(j1[0], j1[0], fma(j1[1], j1[1], fma(j1[2], j1[2], T(-1))));
+        const T m11 = fma(j2[0], j2[0], fma(j2[1], j2[1], fma(j2[2], j2[2], T(-1))));
+        const T m01 = j1[0] * j2[0] + j1[1] * j2[1] + j1[2] * j2[2];
+        const T hm  = T(0.5) * (m00 + m11);
+        const T dm  = T(0.5) * (m00 - m11);
+        const T r   = sqrt(dm * dm + m01 * m01);
+        const T det = m00 * m11 - m01 * m01;
+        T       mu1, mu2;
+        if (hm >= T(0)) {
+            mu1 = hm + r;
+            mu2 = mu1 != T(0) ? det / mu1 : T(0);
+        } else {
+            mu2 = hm - r;
+            mu1 = det / mu2;
+        }
+        auto f = [](T mu) {
+            const T den = sqrt(max(T(0), T(1) + mu)) + T(1);
+            return (mu / den) * (mu / den);
+        };
+        o.E = A * (f(mu1) + f(mu2));
+    }
+    // W = dw/du = [ -[j2]x , [j1]x ]
+    T W[3][6];
+    {
+        const T cj2[3][3] = {{0, -j2[2], j2[1]}, {j2[2], 0, -j2[0]}, {-j2[1], j2[0], 0}};
+        const T cj1[3][3] = {{0, -j1[2], j1[1]}, {j1[2], 0, -j1[0]}, {-j1[1], j1[0], 0}};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                W[i][j]     = -cj2[i][j];
+                W[i][j + 3] = cj1[i][j];
+            }
+    }
+    T wh[3] = {0, 0, 0};
+    if (d > T(0)) {
+        wh[0] = w[0] / d;
+        wh[1] = w[1] / d;
+        wh[2] = w[2] / d;
+    }
+    T gq[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        const T gd = W[0][i] * wh[0] + W[1][i] * wh[1] + W[2][i] * wh[2];
+        gq[i]      = T(2) * u[i] + T(2) * gd;
+        o.gE[i]    = A * (T(2) * u[i] - gq[i] / sq);
+    }
+    if (!HESS) return;
+    // Hd = W^T P W + [[0, -[wh]x], [[wh]x, 0]],  P = (I - wh wh^T) / d
+    T PW[3][6];
+    if (d > T(0)) {
+        const T id = T(1) / d;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int b = 0; b < 6; ++b) {
+                const T ww = wh[0] * W[0][b] + wh[1] * W[1][b] + wh[2] * W[2][b];
+                PW[i][b]   = (W[i][b] - wh[i] * ww) * id;
+            }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int b = 0; b < 6; ++b) PW[i][b] = T(0);
+    }
+    const T cw[3][3] = {{0, -wh[2], wh[1]}, {wh[2], 0, -wh[0]}, {-wh[1], wh[0], 0}};
+    const T isq = T(1) / sq, c3 = T(1) / (T(2) * q * sq);
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+#pragma unroll
+        for (int b = a; b < 6; ++b) {
+            T hd = W[0][a] * PW[0][b] + W[1][a] * PW[1][b] + W[2][a] * PW[2][b];
+            if (a < 3 && b >= 3) hd += -cw[a][b - 3];
+            const T hs = a == b ? T(2) : T(0);
+            const T h  = A * (hs - (hs + T(2) * hd) * isq + gq[a] * gq[b] * c3);
+            o.Hu[a][b] = h;
+            o.Hu[b][a] = h;
+        }
+}
+
+// d[l][k] with a run-time l, by selects (keeps d in registers)
+template <typename T>
+__device__ __forceinline__ T dsel(const FaceDeriv<T>& o, int l, int k)
+{
+    return l == 0 ? o.d[0][k] : (l == 1 ? o.d[1][k] : o.d[2][k]);
+}
+
+// out (3x3 row-major) += d[vi] x d[vj] contraction of Hu
+template <typename T>
+__device__ __forceinline__ void block_of(const FaceDeriv<T>& o, int vi, int vj, T* out)
+{
+    const T a0 = dsel(o, vi, 0), a1 = dsel(o, vi, 1), b0 = dsel(o, vj, 0), b1 = dsel(o, vj, 1);
+#pragma unroll
+    for (int ci = 0; ci < 3; ++ci)
+#pragma unroll
+        for (int cj = 0; cj < 3; ++cj)
+            out[3 * ci + cj] += a0 * (b0 * o.Hu[ci][cj] + b1 * o.Hu[ci][3 + cj]) +
+                                a1 * (b0 * o.Hu[3 + ci][cj] + b1 * o.Hu[3 + ci][3 + cj]);
+}
+
+// rest frame of param.cu:113-141 -> Mr^{-1} (row-major 2x2) per face
+template <typename T>
+__global__ void k_arap_rest(int64_t nf, const int32_t* __restrict__ fv, const double* __restrict__ xr,
+                            T* __restrict__ minv)
+{
+    for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nf;
+         f += (int64_t)gridDim.x * blockDim.x) {
+        const double* a = xr + 3 * (int64_t)fv[3 * f];
+        const double* b = xr + 3 * (int64_t)fv[3 * f + 1];
+        const double* c = xr + 3 * (int64_t)fv[3 * f + 2];
+        const double  e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+        const double  e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+        double        n[3], t[3];
+        cross3(e1, e2, n);
+        const double l1    = sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+        const double b1[3] = {e1[0] / l1, e1[1] / l1, e1[2] / l1};
+        cross3(n, b1, t);
+        const double lt    = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+        const double b2[3] = {t[0] / lt, t[1] / lt, t[2] / lt};
+        const double m00 = e1[0] * b1[0] + e1[1] * b1[1] + e1[2] * b1[2];
+        const double m01 = e2[0] * b1[0] + e2[1] * b1[1] + e2[2] * b1[2];
+        const double m11 = e2[0] * b2[0] + e2[1] * b2[1] + e2[2] * b2[2];
+        const double det = m00 * m11;
+        minv[4 * f + 0]  = (T)(m11 / det);
+        minv[4 * f + 1]  = (T)(-m01 / det);
+        minv[4 * f + 2]  = (T)0;
+        minv[4 * f + 3]  = (T)(m00 / det);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void load_face(const int32_t* __restrict__ fv, const T* __restrict__ x,
+                                          const T* __restrict__ minv, int32_t f, int32_t v[3],
+                                          T x9[9], T mi[4], T& area)
+{
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        v[k] = __ldg(fv + 3 * (int64_t)f + k);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) x9[3 * k + c] = x[3 * (int64_t)v[k] + c];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) mi[k] = __ldg(minv + 4 * (int64_t)f + k);
+    area = T(0.5) / (mi[0] * mi[3] - mi[1] * mi[2]);
+}
+
+__device__ __forceinline__ int local_index(const int32_t v[3], int32_t p)
+{
+    return v[0] == p ? 0 : (v[1] == p ? 1 : 2);
+}
+
+template <int BT>
+__device__ __forceinline__ double block_sum_d(double v, double* s_red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_red[warp] = v;
+    __syncthreads();
+    double t = 0;
+    if (warp == 0) {
+        t = lane < BT / 32 ? s_red[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    return t;  // valid in thread 0
+}
+
+// One thread per vertex p: gradient row, Hessian block row [diag, ring...],
+// and (for faces whose first vertex is p) the face energy.
+template <typename T, bool HESS>
+__global__ void __launch_bounds__(128) k_arap_vertex(
+    int64_t nv, const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ ring_off,
+    const int32_t* __restrict__ ring, const int32_t* __restrict__ ring_face,
+    const int8_t* __restrict__ bnd, const int32_t* __restrict__ fv, const T* __restrict__ x,
+    const T* __restrict__ minv, T* __restrict__ face_E, T* __restrict__ grad, T* __restrict__ hval,
+    double* __restrict__ part)
+{
+    __shared__ double s_red[128 / 32];
+    double            esum = 0;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nv;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t  ro = ring_off[p];
+        const int32_t  k  = ring_off[p + 1] - ro;
+        const int32_t  nf = bnd[p] ? k - 1 : k;
+        const int32_t  rp = row_ptr[p];
+        T              g[3] = {0, 0, 0}, D[9], carry[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) D[i] = carry[i] = T(0);
+        for (int32_t i = 0; i < nf; ++i) {
+            const int32_t f = ring_face[ro + i];
+            int32_t       v[3];
+            T             x9[9], mi[4], area;
+            load_face(fv, x, minv, f, v, x9, mi, area);
+            FaceDeriv<T> o;
+            arap_face<T, HESS>(x9, mi, area, o);
+            const int lp = local_index(v, (int32_t)p);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) g[c] += dsel(o, lp, 0) * o.gE[c] + dsel(o, lp, 1) * o.gE[3 + c];
+            if (lp == 0) {
+                if (face_E) face_E[f] = o.E;
+                esum += (double)o.E;
+            }
+            if (HESS) {
+                const int li = local_index(v, ring[ro + i]);
+                const int lj = local_index(v, ring[ro + (i + 1 < k ? i + 1 : 0)]);
+                block_of(o, lp, lp, D);
+                T bi[9];
+#pragma unroll
+                for (int t = 0; t < 9; ++t) bi[t] = carry[t];
+                block_of(o, lp, li, bi);
+                T* slot = hval + 9 * (int64_t)(rp + 1 + i);
+#pragma unroll
+                for (int t = 0; t < 9; ++t) {
+                    slot[t]  = bi[t];
+                    carry[t] = T(0);
+                }
+                block_of(o, lp, lj, carry);
+            }
+        }
+        if (HESS) {
+            if (k > 0) {
+                // interior: the last face also touches ring[0]; boundary: the
+                // last neighbour has only the face before it
+                T* slot = hval + 9 * (int64_t)(rp + 1 + (bnd[p] ? k - 1 : 0));
+                if (bnd[p]) {
+#pragma unroll
+                    for (int t = 0; t < 9; ++t) slot[t] = carry[t];
+                } else {
+#pragma unroll
+                    for (int t = 0; t < 9; ++t) slot[t] += carry[t];
+                }
+            }
+            T* dslot = hval + 9 * (int64_t)rp;
+#pragma unroll
+            for (int t = 0; t < 9; ++t) dslot[t] = D[t];
+        }
+        if (grad) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) grad[3 * p + c] = g[c];
+        }
+    }
+    const double t = block_sum_d<128>(esum, s_red);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void k_sum_partials(const double* __restrict__ part, int n, double* __restrict__ out)
+{
+    double v = 0;
+    for (int i = threadIdx.x; i < n; i += 32) v += part[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) out[0] = v;
+}
+
+}  // namespace rxg
+
+using namespace rxg;
+
+extern "C" {
+
+rxg_status rxg_arap_rest(const rxg_mesh* h, const double* xyz_rest, int32_t dtype, void* rest,
+                         void* stream)
+{
+    if (!h || !xyz_rest || !rest || (dtype != RXG_F32 && dtype != RXG_F64)) {
+        set_error("rxg_arap_rest: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    if (!is_device_ptr(xyz_rest) || !is_device_ptr(rest)) {
+        set_error("rxg_arap_rest: xyz_rest and rest must be device arrays");
+        return RXG_ERR_INVALID;
+    }
+    const Mesh&  M = h->m;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int    g = grid_for_items(M.nf);
+    if (dtype == RXG_F64)
+        k_arap_rest<double><<<g, 256, 0, s>>>(M.nf, M.d.fv_lin, xyz_rest, (double*)rest);
+    else
+        k_arap_rest<float><<<g, 256, 0, s>>>(M.nf, M.d.fv_lin, xyz_rest, (float*)rest);
+    RXG_CUDA_TRY(cudaGetLastError());
+    return RXG_OK;
+}
+
+rxg_status rxg_arap_eval(const rxg_mesh* h, int32_t dtype, const void* x, const void* rest,
+                         double* energy, void* face_E, void* grad, rxg_bcsr* hess, void* stream)
+{
+    if (!h || !x || !rest || (dtype != RXG_F32 && dtype != RXG_F64)) {
+        set_error("rxg_arap_eval: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    if (hess && (!hess->row_ptr || !hess->col || !hess->val || hess->dtype != dtype)) {
+        set_error("rxg_arap_eval: hess needs row_ptr, col, val of the same dtype");
+        return RXG_ERR_INVALID;
+    }
+    if (!is_device_ptr(x) || !is_device_ptr(rest) || (grad && !is_device_ptr(grad)) ||
+        (face_E && !is_device_ptr(face_E)) || (hess && !is_device_ptr(hess->val))) {
+        set_error("rxg_arap_eval: x, rest, grad, face_E and hess must be device arrays");
+        return RXG_ERR_INVALID;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    Lazy*        z;
+    rxg_status   st = ensure_pattern(&h->m, s, &z);
+    if (st) return st;
+    const int64_t nv = h->m.nv;
+    if (hess) {
+        hess->n   = nv;
+        hess->nnzb = z->nnz;
+        RXG_CUDA_TRY(cudaMemcpyAsync(hess->row_ptr, z->row_ptr, 4 * (nv + 1), cudaMemcpyDeviceToDevice, s));
+        RXG_CUDA_TRY(cudaMemcpyAsync(hess->col, z->col, 4 * z->nnz, cudaMemcpyDeviceToDevice, s));
+    }
+    const int G = std::min<int>(grid_for_items(nv) * 2, 152 * 16);
+    double*   part;
+    RXG_CUDA_TRY(cudaMallocAsync((void**)&part, sizeof(double) * (G + 1), s));
+#define RXG_ARAP_LAUNCH(T, H)                                                                      \
+    k_arap_vertex<T, H><<<G, 128, 0, s>>>(nv, z->row_ptr, z->ring_off, z->ring, z->ring_face,       \
+                                          z->bnd, h->m.d.fv_lin, (const T*)x, (const T*)rest,       \
+                                          (T*)face_E, (T*)grad, hess ? (T*)hess->val : nullptr, part)
+    if (dtype == RXG_F64) {
+        if (hess)
+            RXG_ARAP_LAUNCH(double, true);
+        else
+            RXG_ARAP_LAUNCH(double, false);
+    } else {
+        if (hess)
+            RXG_ARAP_LAUNCH(float, true);
+        else
+            RXG_ARAP_LAUNCH(float, false);
+    }
+#undef RXG_ARAP_LAUNCH
+    k_sum_partials<<<1, 32, 0, s>>>(part, G, part + G);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && energy) {
+        if (is_device_ptr(energy))
+            e = cudaMemcpyAsync(energy, part + G, sizeof(double), cudaMemcpyDeviceToDevice, s);
+        else {
+            e = cudaMemcpyAsync(energy, part + G, sizeof(double), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        }
+    }
+    cudaFreeAsync(part, s);
+    if (e != cudaSuccess) return cuda_status(e, "rxg_arap_eval");
+    return RXG_OK;
+}
+
+}  // extern "C"

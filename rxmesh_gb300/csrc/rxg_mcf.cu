@@ -3,9 +3,13 @@
 // FP64 iterative refinement).
 #include <algorithm>
 #include <cfloat>
+#include <cstdio>
+#include <cstdlib>
 #include <mutex>
 
 #include "rxg_device.cuh"
+#include "rxg_lazy.h"
+#include "rxg_mcf_common.cuh"
 
 namespace rxg {
 
@@ -16,21 +20,6 @@ size_t query_smem_bytes(const Mesh* m, int kind);
 // ---------------------------------------------------------------------
 // per-mesh lazily built structures
 // ---------------------------------------------------------------------
-
-struct Lazy
-{
-    std::mutex mu;
-    bool       ring_ready = false;
-    int32_t*   ring_off   = nullptr;  // nv+1, linear ids
-    int32_t*   ring       = nullptr;  // 2*ne
-    int8_t*    bnd        = nullptr;  // nv
-    int32_t*   row_ptr    = nullptr;  // nv+1  (= ring_off + p)
-    int32_t*   col        = nullptr;  // nnz   (diagonal first, then the ring)
-    int64_t    nnz        = 0;
-    // MCF step scratch (sized for this mesh)
-    void*   buf      = nullptr;
-    size_t  buf_size = 0;
-};
 
 static std::mutex g_lazy_mu;
 
@@ -49,6 +38,7 @@ void lazy_free(Mesh* m)
     cudaFree(z->ring_off);
     cudaFree(z->ring);
     cudaFree(z->bnd);
+    cudaFree(z->ring_face);
     cudaFree(z->row_ptr);
     cudaFree(z->col);
     cudaFree(z->buf);
@@ -82,6 +72,8 @@ static int grid_for(int64_t work, int threads = 256)
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 32));
 }
 
+int grid_for_items(int64_t work) { return grid_for(work); }
+
 // ---------------------------------------------------------------------
 // Oriented VV: per patch, VF transpose in shared memory, then one thread per
 // owned vertex walks its fan (face (p,a,b) is followed by the face whose
@@ -101,7 +93,8 @@ __global__ void __launch_bounds__(kQT2) k_oriented_vv(const PatchHdr* __restrict
                                                       const uint32_t* __restrict__ arena,
                                                       int32_t* __restrict__ out_off,
                                                       int32_t* __restrict__ out_val,
-                                                      int8_t* __restrict__ out_bnd, int* err)
+                                                      int8_t* __restrict__ out_bnd,
+                                                      int32_t* __restrict__ out_rface, int* err)
 {
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ uint64_t bar;
@@ -118,7 +111,8 @@ __global__ void __launch_bounds__(kQT2) k_oriented_vv(const PatchHdr* __restrict
     uint32_t* s_ev   = smem;
     uint32_t* s_fe   = s_ev + pad4i(h.nEl);
     uint32_t* s_rv   = s_fe + few;
-    int32_t*  s_fcnt = reinterpret_cast<int32_t*>(s_rv + pad4i(nVr));  // VF offsets
+    uint32_t* s_rf   = s_rv + pad4i(nVr);
+    int32_t*  s_fcnt = reinterpret_cast<int32_t*>(s_rf + pad4i(h.nFl - h.nFo));  // VF offsets
     int32_t*  s_ecnt = s_fcnt + pad4i(nVo + 1);                           // valences
     int32_t*  s_vf   = s_ecnt + pad4i(nVo + 1);                           // VF values (local)
 
@@ -130,10 +124,12 @@ __global__ void __launch_bounds__(kQT2) k_oriented_vv(const PatchHdr* __restrict
     __syncthreads();
     if (threadIdx.x == 0) {
         const uint32_t b0 = pad16_bytes(h.nEl), b1 = (uint32_t)few * 4, b2 = pad16_bytes(nVr);
-        mbar_arrive_expect_tx(&bar, b0 + b1 + b2);
+        const uint32_t b3 = pad16_bytes(h.nFl - h.nFo);
+        mbar_arrive_expect_tx(&bar, b0 + b1 + b2 + b3);
         if (b0) bulk_g2s(s_ev, arena + h.ev_off, b0, &bar);
         if (b1) bulk_g2s(s_fe, arena + h.fe_off, b1, &bar);
         if (b2) bulk_g2s(s_rv, arena + h.rv_off, b2, &bar);
+        if (b3) bulk_g2s(s_rf, arena + h.rf_off, b3, &bar);
     }
     if (!mbar_wait_bounded(&bar, 0, err)) return;
     const uint16_t* fe16 = reinterpret_cast<const uint16_t*>(s_fe);
@@ -166,10 +162,12 @@ __global__ void __launch_bounds__(kQT2) k_oriented_vv(const PatchHdr* __restrict
     auto lin = [&](uint32_t l) -> int32_t {
         return (int32_t)l < nVo ? h.v_base + (int32_t)l : (int32_t)s_rv[l - nVo];
     };
+    auto linf = [&](int f) -> int32_t { return f < h.nFo ? h.f_base + f : (int32_t)s_rf[f - h.nFo]; };
     for (int v = threadIdx.x; v < nVo; v += kQT2) {
         const int32_t beg = v == 0 ? 0 : s_fcnt[v - 1], end = s_fcnt[v], k = end - beg;
         const int32_t obeg = h.vv_base + s_ecnt[v], olen = s_ecnt[v + 1] - s_ecnt[v];
         int32_t*      o    = out_val + obeg;
+        int32_t*      of   = out_rface ? out_rface + obeg : nullptr;  // face after ring[i]
         if (k == 0) {
             out_bnd[h.v_base + v] = 0;
             continue;
@@ -218,6 +216,7 @@ __global__ void __launch_bounds__(kQT2) k_oriented_vv(const PatchHdr* __restrict
         while (true) {
             ++nvis;
             ab(cur, a, b);
+            if (of && pos - 1 < olen) of[pos - 1] = linf(s_vf[beg + cur]);
             int nxt = -1;
             for (int t = 0; t < k; ++t) {
                 uint32_t a2, b2;
@@ -229,7 +228,10 @@ __global__ void __launch_bounds__(kQT2) k_oriented_vv(const PatchHdr* __restrict
             }
             if (nxt < 0 || nxt == start) {
                 if (is_b) {
-                    if (pos < olen) o[pos] = lin(b);
+                    if (pos < olen) {
+                        o[pos] = lin(b);
+                        if (of) of[pos] = -1;  // no face after the last boundary neighbour
+                    }
                     ++pos;
                 }
                 break;
@@ -263,130 +265,6 @@ __global__ void k_pattern(int64_t nv, const int32_t* __restrict__ ring_off,
 }
 
 // ---------------------------------------------------------------------
-// cotangent weights and Voronoi areas (include/rxmesh/geometry_util.cuh)
-// ---------------------------------------------------------------------
-
-template <typename T>
-struct V3
-{
-    T x, y, z;
-};
-template <typename T>
-__device__ __forceinline__ V3<T> sub(V3<T> a, V3<T> b)
-{
-    return {a.x - b.x, a.y - b.y, a.z - b.z};
-}
-template <typename T>
-__device__ __forceinline__ T dot(V3<T> a, V3<T> b)
-{
-    return a.x * b.x + a.y * b.y + a.z * b.z;
-}
-template <typename T>
-__device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b)
-{
-    // glm::cross component order
-    return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
-}
-template <typename T>
-__device__ __forceinline__ T tri_area(V3<T> p0, V3<T> p1, V3<T> p2)
-{
-    V3<T> c = cross(sub(p1, p0), sub(p2, p0));
-    return T(0.5) * sqrt(dot(c, c));
-}
-template <typename T>
-__device__ __forceinline__ T clamp_cot(T v)
-{
-    const T bound = T(19.1);
-    return v < -bound ? -bound : (v > bound ? bound : v);
-}
-template <typename T>
-__device__ __forceinline__ T tmin();
-template <>
-__device__ __forceinline__ float tmin<float>()
-{
-    return FLT_MIN;
-}
-template <>
-__device__ __forceinline__ double tmin<double>()
-{
-    return DBL_MIN;
-}
-
-// partial_weight of edge_cotan_weight (geometry_util.cuh:173-206)
-template <typename T>
-__device__ __forceinline__ T half_cot(V3<T> p, V3<T> r, V3<T> v)
-{
-    const T A = tri_area(p, r, v);
-    if (A > tmin<T>()) return clamp_cot(dot(sub(p, v), sub(r, v)) / A);
-    return T(0);
-}
-
-// partial_voronoi_area (geometry_util.cuh:117-167)
-template <typename T>
-__device__ __forceinline__ T voronoi(V3<T> p, V3<T> q, V3<T> r)
-{
-    const V3<T> pq = sub(q, p), qr = sub(r, q), pr = sub(r, p);
-    const T     A  = tri_area(p, q, r);
-    if (A <= tmin<T>()) return T(-1);
-    const T dp = dot(pq, pr), dq = -dot(qr, pq), dr = dot(qr, pr);
-    if (dp < T(0)) return T(0.25) * A;
-    if (dq < T(0) || dr < T(0)) return T(0.125) * A;
-    return T(0.125) * (dot(pr, pr) * clamp_cot(dq / A) + dot(pq, pq) * clamp_cot(dr / A));
-}
-
-__device__ __forceinline__ V3<float> tof(V3<double> a)
-{
-    return {(float)a.x, (float)a.y, (float)a.z};
-}
-
-// true when a triangle has an angle below 1e-3 rad: sin^2 of its smallest
-// angle, |cross|^2 / (product of the two largest squared edge lengths)
-__device__ __forceinline__ bool near_degenerate(V3<float> a, V3<float> b, V3<float> c)
-{
-    const V3<float> ab = sub(b, a), ac = sub(c, a), bc = sub(c, b);
-    const V3<float> cr = cross(ab, ac);
-    const float     l0 = dot(ab, ab), l1 = dot(ac, ac), l2 = dot(bc, bc);
-    const float     mn = fminf(l0, fminf(l1, l2));
-    const float     big = (l0 * l1 * l2) / fmaxf(mn, FLT_MIN);
-    return dot(cr, cr) < 1e-6f * big;
-}
-
-// weight and area evaluators: exact type T, or FP32 with an FP64 redo of
-// near-degenerate triangles (the mixed path)
-template <typename T>
-struct Geo
-{
-    __device__ static T hc(V3<double> p, V3<double> r, V3<double> v)
-    {
-        return half_cot<T>({(T)p.x, (T)p.y, (T)p.z}, {(T)r.x, (T)r.y, (T)r.z}, {(T)v.x, (T)v.y, (T)v.z});
-    }
-    __device__ static T va(V3<double> p, V3<double> q, V3<double> r)
-    {
-        return voronoi<T>({(T)p.x, (T)p.y, (T)p.z}, {(T)q.x, (T)q.y, (T)q.z}, {(T)r.x, (T)r.y, (T)r.z});
-    }
-};
-struct GeoMixed
-{
-    __device__ static float hc(V3<double> p, V3<double> r, V3<double> v)
-    {
-        const V3<float> pf = tof(p), rf = tof(r), vf = tof(v);
-        if (near_degenerate(pf, rf, vf)) return (float)half_cot<double>(p, r, v);
-        return half_cot<float>(pf, rf, vf);
-    }
-    __device__ static float va(V3<double> p, V3<double> q, V3<double> r)
-    {
-        const V3<float> pf = tof(p), qf = tof(q), rf = tof(r);
-        if (near_degenerate(pf, qf, rf)) return (float)voronoi<double>(p, q, r);
-        return voronoi<float>(pf, qf, rf);
-    }
-};
-
-__device__ __forceinline__ V3<double> ld3(const double* __restrict__ x, int32_t i)
-{
-    return {__ldg(x + 3 * (int64_t)i), __ldg(x + 3 * (int64_t)i + 1), __ldg(x + 3 * (int64_t)i + 2)};
-}
-
-// ---------------------------------------------------------------------
 // MCF system (mcf_A_setup / mcf_B_setup, apps/MCF/mcf_kernels.cuh:302-426).
 // One thread per vertex walks its oriented ring with a rolling window of
 // three positions; the row is [diag, ring...] so no column search is done.
@@ -394,12 +272,57 @@ __device__ __forceinline__ V3<double> ld3(const double* __restrict__ x, int32_t 
 // rows use only the fan's real triangles.
 // ---------------------------------------------------------------------
 
-template <typename T, typename G, typename TB>
+// output policies of the assembly kernel: CSR values + n x 3 B, or packed
+// entries + 4-wide B
+template <typename T, typename TB>
+struct CsrOut
+{
+    T*  val;
+    TB* B;
+    __device__ void entry(int32_t idx, int32_t, T v) const { val[idx] = v; }
+    __device__ void diag_full(int64_t, TB) const {}
+    __device__ void rhs(int64_t p, TB x, TB y, TB z) const
+    {
+        if (B) {
+            B[3 * p + 0] = x;
+            B[3 * p + 1] = y;
+            B[3 * p + 2] = z;
+        }
+    }
+};
+template <typename T, typename TB>
+struct PackedOut
+{
+    Ent<T>* ent;
+    R4<TB>* B;
+    TB*     diag;  // optional: the diagonal in TB before rounding to T
+    __device__ void entry(int32_t idx, int32_t c, T v) const
+    {
+        Ent<T> e;
+        e.col    = c;
+        e.val    = v;
+        ent[idx] = e;
+    }
+    __device__ void diag_full(int64_t p, TB d) const
+    {
+        if (diag) diag[p] = d;
+    }
+    __device__ void rhs(int64_t p, TB x, TB y, TB z) const
+    {
+        R4<TB> b;
+        b.x  = x;
+        b.y  = y;
+        b.z  = z;
+        b.w  = TB(0);
+        B[p] = b;
+    }
+};
+
+template <typename T, typename G, typename TB, typename Out>
 __global__ void __launch_bounds__(256) k_mcf_assemble(int64_t nv, const int32_t* __restrict__ row_ptr,
                                                       const int32_t* __restrict__ col,
                                                       const int8_t* __restrict__ bnd,
-                                                      const double* __restrict__ xyz, T dt,
-                                                      T* __restrict__ val, TB* __restrict__ B)
+                                                      const double* __restrict__ xyz, T dt, Out out)
 {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nv;
          p += (int64_t)gridDim.x * blockDim.x) {
@@ -408,7 +331,10 @@ __global__ void __launch_bounds__(256) k_mcf_assemble(int64_t nv, const int32_t*
         const int32_t* rg  = col + rp + 1;
         const bool    wrap = bnd[p] == 0;
         const V3<double> P = ld3(xyz, (int32_t)p);
-        T                area = T(0), sumw = T(0);
+        // row sums accumulate in TB (FP64 on the MCF paths): the diagonal is
+        // 2*area + sum of the T-rounded weights, so the Laplacian part keeps
+        // exactly zero row sums when the FP64 residual uses it
+        TB area = TB(0), sumw = TB(0);
         if (k > 0) {
             V3<double> Q = ld3(xyz, rg[k - 1]), R = ld3(xyz, rg[0]);
             for (int32_t i = 0; i < k; ++i) {
@@ -418,23 +344,21 @@ __global__ void __launch_bounds__(256) k_mcf_assemble(int64_t nv, const int32_t*
                 if (has_q) w += G::hc(P, R, Q);
                 if (has_s) w += G::hc(P, R, S);
                 w = (w >= T(0) ? w : T(0)) * dt;
-                sumw += w;
-                val[rp + 1 + i] = -w;
+                sumw += (TB)w;
+                out.entry(rp + 1 + i, rg[i], -w);
                 if (has_q) {
                     const T a = G::va(P, Q, R);
-                    area += a > T(0) ? a : T(0);
+                    area += a > T(0) ? (TB)a : TB(0);
                 }
                 Q = R;
                 R = S;
             }
         }
-        const T vw  = T(0.5) / area;
-        val[rp]     = T(1) / vw + sumw;
-        if (B) {
-            B[3 * p + 0] = (TB)P.x / (TB)vw;
-            B[3 * p + 1] = (TB)P.y / (TB)vw;
-            B[3 * p + 2] = (TB)P.z / (TB)vw;
-        }
+        const TB vw = TB(0.5) / area;
+        const TB dg = TB(1) / vw + sumw;
+        out.entry(rp, (int32_t)p, (T)dg);
+        out.diag_full(p, dg);
+        out.rhs(p, (TB)P.x / vw, (TB)P.y / vw, (TB)P.z / vw);
     }
 }
 
@@ -468,88 +392,12 @@ __global__ void __launch_bounds__(256) k_spmm(int64_t n, const int32_t* __restri
 // ---------------------------------------------------------------------
 // Persistent CG / Jacobi-PCG (CGSolver / PCGSolver, cg_solver.h:37-125,
 // pcg_solver.h:34-144).  One cooperative launch runs the whole solve; the
-// grid synchronises twice per iteration through a bounded barrier and every
-// block reduces the per-block partial dot products itself in a fixed order,
-// so all blocks take the same (deterministic) alpha, beta and stop decision
-// without a host round trip.  The search-direction update p = z + beta p is
-// fused into the next SpMM (double-buffered p).
+// grid synchronises twice per iteration, each time through a bounded barrier
+// that also sums the per-block partial dot products in a fixed order, so all
+// blocks take the same (deterministic) alpha, beta and stop decision without
+// a host round trip.  The search-direction update p = z + beta p needs no
+// barrier of its own: S = A p is carried as A z + beta S.
 // ---------------------------------------------------------------------
-
-// bar[0] arrivals, bar[1] generation, bar[2] abort
-__device__ __forceinline__ bool grid_sync(unsigned* bar, unsigned nblocks, int* err, int* s_ok)
-{
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned* vgen = bar + 1;
-        volatile unsigned* vab  = bar + 2;
-        const unsigned     g    = *vgen;
-        int                ok   = 1;
-        __threadfence();
-        const unsigned a = atomicAdd(bar, 1u);
-        if (a == nblocks - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            uint32_t i = 0;
-            while (*vgen == g) {
-                if (*vab) {
-                    ok = 0;
-                    break;
-                }
-                if (++i > kWaitLimit) {
-                    atomicOr(err, DEVERR_GRID_TIMEOUT);
-                    atomicExch(bar + 2, 1u);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        *s_ok = ok;
-    }
-    __syncthreads();
-    return *s_ok != 0;
-}
-
-// block sum of a double, result valid in every thread
-template <int BT>
-__device__ __forceinline__ double block_sum(double v, double* s_red)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) s_red[warp] = v;
-    __syncthreads();
-    double t = 0;
-    if (warp == 0) {
-        t = lane < BT / 32 ? s_red[lane] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) s_red[BT / 32] = t;
-    }
-    __syncthreads();
-    return s_red[BT / 32];
-}
-
-// sum of the grid's partials in a fixed order (identical in every block)
-template <int BT>
-__device__ __forceinline__ double grid_partials_sum(const double* part, int G, double* s_red)
-{
-    double v = 0;
-    if (threadIdx.x < 32) {
-        for (int i = threadIdx.x; i < G; i += 32) v += *((volatile const double*)(part + i));
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (threadIdx.x == 0) s_red[BT / 32 + 1] = v;
-    }
-    __syncthreads();
-    double r = s_red[BT / 32 + 1];
-    __syncthreads();
-    return r;
-}
 
 template <typename T>
 struct CGArgs
@@ -575,9 +423,120 @@ struct CGArgs
     int*           err;
 };
 
-constexpr int kCGT = 256;
+// Grid-wide sum of one double per block, fused with the grid barrier.
+// Thread 0 of every block posts its block's value and arrives on a counter
+// that only ever grows (reduction k ends at arrival G*(k+1)); the last block
+// to arrive sums all posts in a fixed order, so every run and every block
+// sees the same value, and publishes it in slot[k & 1], a 64-bit word that
+// reads all-ones (a NaN) until then.  Before publishing it re-arms the other
+// slot for reduction k+1, which no block can still be reading.  The other
+// blocks poll that one word: one round trip instead of a flag and a value.
+// The wait is bounded: on timeout the error word and an abort flag are set
+// and false is returned.  bar[0] arrivals, bar[2] abort, bar[4..7] slots
+// (16-byte aligned); the host sets bar[0..3] to 0 and the slots to all-ones.
+__device__ __forceinline__ bool grid_reduce(double v, double* part, unsigned* bar, unsigned G,
+                                            unsigned k, int* err, double* s_red, int* s_ok,
+                                            double* out)
+{
+    unsigned long long* slot = reinterpret_cast<unsigned long long*>(bar + 4);
+    const unsigned long long kNotYet = ~0ull;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const unsigned lane = threadIdx.x;
+        unsigned       last = 0;
+        if (lane == 0) {
+            part[blockIdx.x] = v;
+            __threadfence();
+            last = (atomicAdd(bar, 1u) % G) == G - 1 ? 1u : 0u;
+        }
+        last       = __shfl_sync(0xffffffffu, last, 0);
+        int    ok  = 1;
+        double sum = 0;
+        if (last) {
+            __threadfence();
+            double acc = 0;
+#pragma unroll 4
+            for (unsigned i = lane; i < G; i += 32) acc += __ldcg(part + i);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            sum = acc;
+            if (lane == 0) {
+                *((volatile unsigned long long*)(slot + ((k + 1) & 1))) = kNotYet;
+                __threadfence();
+                *((volatile unsigned long long*)(slot + (k & 1))) =
+                    (unsigned long long)__double_as_longlong(acc);
+            }
+        } else if (lane == 0) {
+            volatile unsigned* vab = bar + 2;
+            uint32_t           it  = 0;
+            while (true) {
+                const unsigned long long w = *((volatile unsigned long long*)(slot + (k & 1)));
+                if (w != kNotYet) {
+                    sum = __longlong_as_double((long long)w);
+                    break;
+                }
+                if (*vab) {
+                    ok = 0;
+                    break;
+                }
+                if (++it > kWaitLimit) {
+                    atomicOr(err, DEVERR_GRID_TIMEOUT);
+                    atomicExch(bar + 2, 1u);
+                    ok = 0;
+                    break;
+                }
+            }
+            __threadfence();
+        }
+        if (lane == 0) {
+            s_red[0] = sum;
+            *s_ok    = ok;
+        }
+    }
+    __syncthreads();
+    *out          = s_red[0];
+    const bool ok = *s_ok != 0;
+    __syncthreads();
+    return ok;
+}
 
-template <typename T, int NC, bool PC>
+// host side of the barrier state: counter and abort to 0, slots to all-ones
+static cudaError_t reset_grid_reduce(unsigned* bar, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(bar, 0, 16, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(bar + 4, 0xFF, 32, s);  // up to two value slots
+    return e;
+}
+
+// acc = sum_j A_ij x_j over row i, eight non-zeros per round so that all
+// column/value loads and then all gathers of a round are in flight together
+// (rows of the MCF matrix have about seven entries).  Padding lanes read
+// row i itself with weight zero.  diag (may be null) receives A_ii.
+template <typename T, int NC>
+__device__ __forceinline__ void row_spmv(const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                         const T* __restrict__ val, int64_t i, const T* x, T* acc,
+                                         T* diag)
+{
+    const int32_t b = __ldg(rp + i), e = __ldg(rp + i + 1);
+    for (int32_t j0 = b; j0 < e; j0 += 8) {
+        int32_t cj[8];
+        T       v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const bool ok = j0 + u < e;
+            cj[u]         = ok ? __ldg(col + j0 + u) : (int32_t)i;
+            v[u]          = ok ? __ldg(val + j0 + u) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (diag && j0 + u < e && cj[u] == i) *diag = v[u];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) acc[c] += v[u] * x[(int64_t)cj[u] * NC + c];
+        }
+    }
+}
+
+template <typename T, int NC, bool PC, int kCGT>
 __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
 {
     __shared__ double s_red[kCGT / 32 + 2];
@@ -587,45 +546,39 @@ __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
     const int64_t  r0    = blockIdx.x * chunk;
     const int64_t  r1    = min(a.n, r0 + chunk);
     T* const       src   = PC ? a.Z : a.R;  // vector the direction is built from
+    unsigned       kred  = 0;               // reductions done so far
+    // Per-thread partial dot products stay in T over the thread's few rows;
+    // the block and grid reductions are in FP64.
 
     // ---- pre_solve: S = A X, R = B - S, Z = D^-1 R, delta = R.Z (or R.R)
-    double part = 0;
+    T tpart = T(0);
     for (int64_t i = r0 + threadIdx.x; i < r1; i += kCGT) {
-        const int32_t b = __ldg(a.rp + i), e = __ldg(a.rp + i + 1);
-        T             acc[NC];
+        T acc[NC];
 #pragma unroll
         for (int c = 0; c < NC; ++c) acc[c] = T(0);
         T diag = T(0);
-        for (int32_t j = b; j < e; ++j) {
-            const int32_t cj = __ldg(a.col + j);
-            const T       v  = __ldg(a.val + j);
-            if (cj == i) diag = v;
-#pragma unroll
-            for (int c = 0; c < NC; ++c) acc[c] += v * a.X[(int64_t)cj * NC + c];
-        }
+        row_spmv<T, NC>(a.rp, a.col, a.val, i, a.X, acc, &diag);
         const T di = T(1) / (diag + (sizeof(T) == 4 ? (T)FLT_EPSILON : (T)DBL_EPSILON));
         if (PC) a.dinv[i] = di;
-        T tp = T(0);
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
-            const T r = a.B[i * NC + c] - acc[c];
+            const T r       = a.B[i * NC + c] - acc[c];
             a.R[i * NC + c] = r;
             if (PC) {
                 const T z       = di * r;
                 a.Z[i * NC + c] = z;
-                tp += r * z;
+                tpart += r * z;
             } else {
-                tp += r * r;
+                tpart += r * r;
             }
         }
-        part += (double)tp;
     }
-    part = block_sum<kCGT>(part, s_red);
-    if (threadIdx.x == 0) a.part[blockIdx.x] = part;
-    if (!grid_sync(a.bar, G, a.err, &s_ok)) return;
-    const double delta0 = grid_partials_sum<kCGT>(a.part, G, s_red);
-    double       delta  = delta0;
-    auto conv = [&](double d) { return d < a.abs_tol || d / delta0 < a.rel_tol; };
+    double delta0;
+    if (!grid_reduce(block_sum<kCGT>((double)tpart, s_red), a.part, a.bar, G, kred++, a.err, s_red,
+                     &s_ok, &delta0))
+        return;
+    double delta = delta0;
+    auto   conv  = [&](double d) { return d < a.abs_tol || d / delta0 < a.rel_tol; };
     if (conv(delta0)) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             a.dstat[0] = delta0;
@@ -635,68 +588,57 @@ __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
         }
         return;
     }
-    double beta = 0;
-    int    it   = 0;
-    bool   done = false;
+    double   beta = 0;
+    int      it   = 0;
+    bool     done = false;
+    T* const P    = a.P0;
     while (it < a.max_iter) {
-        T* const Pold = (it & 1) ? a.P1 : a.P0;
-        T* const Pnew = (it & 1) ? a.P0 : a.P1;
-        const T  bt   = (T)beta;
-        // ---- phase A: p = src + beta p_old (fused), S = A p, part = S.p
-        part = 0;
+        const T bt = (T)beta;
+        // ---- phase A: S = A src + beta S (= A p by linearity), p = src + beta p,
+        //      S.p.  Only own rows of S and p are read back, so the p update
+        //      needs neither extra work per non-zero nor another barrier.
+        tpart = T(0);
         for (int64_t i = r0 + threadIdx.x; i < r1; i += kCGT) {
-            const int32_t b = __ldg(a.rp + i), e = __ldg(a.rp + i + 1);
-            T             acc[NC];
+            T acc[NC];
 #pragma unroll
             for (int c = 0; c < NC; ++c) acc[c] = T(0);
-            for (int32_t j = b; j < e; ++j) {
-                const int64_t cj = (int64_t)__ldg(a.col + j) * NC;
-                const T       v  = __ldg(a.val + j);
-#pragma unroll
-                for (int c = 0; c < NC; ++c) {
-                    const T pj = it == 0 ? src[cj + c] : src[cj + c] + bt * Pold[cj + c];
-                    acc[c] += v * pj;
-                }
-            }
-            T tp = T(0);
+            row_spmv<T, NC>(a.rp, a.col, a.val, i, src, acc, (T*)nullptr);
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
-                const T pi = it == 0 ? src[i * NC + c] : src[i * NC + c] + bt * Pold[i * NC + c];
-                Pnew[i * NC + c] = pi;
-                a.S[i * NC + c]  = acc[c];
-                tp += acc[c] * pi;
+                const T si = it == 0 ? acc[c] : acc[c] + bt * a.S[i * NC + c];
+                const T pi = it == 0 ? src[i * NC + c] : src[i * NC + c] + bt * P[i * NC + c];
+                P[i * NC + c]   = pi;
+                a.S[i * NC + c] = si;
+                tpart += si * pi;
             }
-            part += (double)tp;
         }
-        part = block_sum<kCGT>(part, s_red);
-        if (threadIdx.x == 0) a.part[G + blockIdx.x] = part;
-        if (!grid_sync(a.bar, G, a.err, &s_ok)) return;
-        const double alpha = delta / grid_partials_sum<kCGT>(a.part + G, G, s_red);
-        const T      al    = (T)alpha;
+        double sp;
+        if (!grid_reduce(block_sum<kCGT>((double)tpart, s_red), a.part, a.bar, G, kred++, a.err,
+                         s_red, &s_ok, &sp))
+            return;
+        const T al = (T)(delta / sp);
         // ---- phase B: X += alpha p, R -= alpha S, Z = D^-1 R, delta' = R.Z
-        part = 0;
+        tpart = T(0);
         for (int64_t i = r0 + threadIdx.x; i < r1; i += kCGT) {
             const T di = PC ? a.dinv[i] : T(1);
-            T       tp = T(0);
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
-                a.X[i * NC + c] += al * Pnew[i * NC + c];
-                const T r = a.R[i * NC + c] - al * a.S[i * NC + c];
+                a.X[i * NC + c] += al * P[i * NC + c];
+                const T r       = a.R[i * NC + c] - al * a.S[i * NC + c];
                 a.R[i * NC + c] = r;
                 if (PC) {
                     const T z       = di * r;
                     a.Z[i * NC + c] = z;
-                    tp += r * z;
+                    tpart += r * z;
                 } else {
-                    tp += r * r;
+                    tpart += r * r;
                 }
             }
-            part += (double)tp;
         }
-        part = block_sum<kCGT>(part, s_red);
-        if (threadIdx.x == 0) a.part[blockIdx.x] = part;
-        if (!grid_sync(a.bar, G, a.err, &s_ok)) return;
-        const double dn = grid_partials_sum<kCGT>(a.part, G, s_red);
+        double dn;
+        if (!grid_reduce(block_sum<kCGT>((double)tpart, s_red), a.part, a.bar, G, kred++, a.err,
+                         s_red, &s_ok, &dn))
+            return;
         if (conv(dn)) {
             delta = dn;
             done  = true;
@@ -730,19 +672,43 @@ static int num_sms()
     return sms;
 }
 
-template <typename T, int NC, bool PC>
-static int cg_grid(int64_t n)
+// CTA size of the persistent CG kernel: RXG_CG_THREADS=256|512|1024 (default 512)
+static int cg_threads()
+{
+    static int t = 0;
+    if (!t) {
+        const char* e = getenv("RXG_CG_THREADS");
+        t             = e ? atoi(e) : 512;
+        if (t != 256 && t != 512 && t != 1024) t = 512;
+    }
+    return t;
+}
+
+template <typename T, int NC, bool PC, int BT>
+static int cg_grid_bt(int64_t n)
 {
     static int per_sm = -1;
     if (per_sm < 0) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<T, NC, PC>, kCGT, 0) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<T, NC, PC, BT>, BT, 0) !=
             cudaSuccess)
             per_sm = 1;
-        per_sm = std::max(1, std::min(per_sm, 4));
+        int cap = 4;
+        if (const char* e = getenv("RXG_CG_BLOCKS_PER_SM")) cap = std::max(1, atoi(e));
+        per_sm = std::max(1, std::min(per_sm, cap));
     }
     int64_t g = (int64_t)num_sms() * per_sm;
     g         = std::min<int64_t>(g, std::max<int64_t>(1, (n + 31) / 32));
     return (int)g;
+}
+
+template <typename T, int NC, bool PC>
+static int cg_grid(int64_t n)
+{
+    switch (cg_threads()) {
+        case 256: return cg_grid_bt<T, NC, PC, 256>(n);
+        case 1024: return cg_grid_bt<T, NC, PC, 1024>(n);
+        default: return cg_grid_bt<T, NC, PC, 512>(n);
+    }
 }
 
 static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
@@ -783,10 +749,12 @@ static rxg_status cg_launch(int64_t n, const int32_t* rp, const int32_t* col, co
     a.abs_tol  = o.abs_tol;
     a.rel_tol  = o.rel_tol;
     a.err      = device_error_word();
-    RXG_CUDA_TRY(cudaMemsetAsync(a.bar, 0, 256, s));
+    RXG_CUDA_TRY(reset_grid_reduce(a.bar, s));
     void* args[] = {&a};
-    RXG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_cg<T, NC, PC>, dim3(G), dim3(kCGT),
-                                             args, 0, s));
+    const void* kern = cg_threads() == 256    ? (const void*)k_cg<T, NC, PC, 256>
+                       : cg_threads() == 1024 ? (const void*)k_cg<T, NC, PC, 1024>
+                                              : (const void*)k_cg<T, NC, PC, 512>;
+    RXG_CUDA_TRY(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(cg_threads()), args, 0, s));
     if (st) {
         double ds[2];
         int    is[2];
@@ -871,14 +839,14 @@ static size_t oriented_smem_bytes(const Mesh* m)
     size_t w = 0;
     for (const PatchHdr& h : m->hdr) {
         const size_t few = pad4i((3 * h.nFl + 1) / 2);
-        w = std::max(w, (size_t)pad4i(h.nEl) + few + pad4i(h.nVl - h.nVo) + 2 * pad4i(h.nVo + 1) +
-                            3 * (size_t)h.nFl);
+        w = std::max(w, (size_t)pad4i(h.nEl) + few + pad4i(h.nVl - h.nVo) + pad4i(h.nFl - h.nFo) +
+                            2 * pad4i(h.nVo + 1) + 3 * (size_t)h.nFl);
     }
     return w * 4;
 }
 
 static rxg_status launch_oriented(const Mesh* m, int32_t* off, int32_t* val, int8_t* bnd,
-                                  cudaStream_t s)
+                                  int32_t* rface, cudaStream_t s)
 {
     const size_t smem = oriented_smem_bytes(m);
     if (smem > 227 * 1024) {
@@ -888,13 +856,13 @@ static rxg_status launch_oriented(const Mesh* m, int32_t* off, int32_t* val, int
     if (smem > 48 * 1024)
         RXG_CUDA_TRY(cudaFuncSetAttribute(k_oriented_vv, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem));
-    k_oriented_vv<<<m->num_patches, kQT2, smem, s>>>(m->d.hdr, m->d.arena, off, val, bnd,
+    k_oriented_vv<<<m->num_patches, kQT2, smem, s>>>(m->d.hdr, m->d.arena, off, val, bnd, rface,
                                                       device_error_word());
     RXG_CUDA_TRY(cudaGetLastError());
     return RXG_OK;
 }
 
-static rxg_status ensure_pattern(const Mesh* m, cudaStream_t s, Lazy** out)
+rxg_status ensure_pattern(const Mesh* m, cudaStream_t s, Lazy** out)
 {
     Lazy* z = lazy_of(m);
     std::lock_guard<std::mutex> g(z->mu);
@@ -911,7 +879,8 @@ static rxg_status ensure_pattern(const Mesh* m, cudaStream_t s, Lazy** out)
     RXG_CUDA_TRY(cudaMalloc(&z->bnd, std::max<int64_t>(16, nv)));
     RXG_CUDA_TRY(cudaMalloc(&z->row_ptr, 4 * (nv + 1)));
     RXG_CUDA_TRY(cudaMalloc(&z->col, 4 * z->nnz));
-    rxg_status st = launch_oriented(m, z->ring_off, z->ring, z->bnd, s);
+    RXG_CUDA_TRY(cudaMalloc(&z->ring_face, 4 * std::max<int64_t>(1, 2 * ne)));
+    rxg_status st = launch_oriented(m, z->ring_off, z->ring, z->bnd, z->ring_face, s);
     if (st) return st;
     k_pattern<<<grid_for(nv + 1), 256, 0, s>>>(nv, z->ring_off, z->ring, z->row_ptr, z->col);
     RXG_CUDA_TRY(cudaGetLastError());
@@ -922,43 +891,684 @@ static rxg_status ensure_pattern(const Mesh* m, cudaStream_t s, Lazy** out)
 }
 
 // ---------------------------------------------------------------------
-// mixed-precision helpers
+// Persistent Jacobi-PCG on the packed MCF layout: the same iteration as
+// k_cg (fused barrier-reductions, S carried as A z + beta S) on 4-wide row
+// vectors and (column, value) entries, so a row, a neighbour or a non-zero
+// is one wide access.  Used by the MCF step for both precisions.
 // ---------------------------------------------------------------------
 
-// x += d ; returns nothing
-__global__ void k_add_correction(int64_t m, double* __restrict__ x, const float* __restrict__ d)
+template <typename T>
+struct CGMArgs
 {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
-         i += (int64_t)gridDim.x * blockDim.x)
-        x[i] += (double)d[i];
+    int64_t        n;
+    const int32_t* rp;
+    const Ent<T>*  ent;
+    const R4<T>*   B;
+    R4<T>*         X;
+    R4<T>*         R;
+    R4<T>*         P;
+    R4<T>*         S;
+    R4<T>*         Z;
+    T*             dinv;
+    double*        part;
+    unsigned*      bar;
+    double*        dstat;
+    int*           istat;
+    int            max_iter;
+    double         abs_tol, rel_tol;
+    int*           err;
+};
+
+template <typename T, int kBT>
+__global__ void __launch_bounds__(kBT) k_cgm(CGMArgs<T> a)
+{
+    __shared__ double s_red[kBT / 32 + 2];
+    __shared__ int    s_ok;
+    const unsigned G     = gridDim.x;
+    const int64_t  chunk = (a.n + G - 1) / G;
+    const int64_t  r0    = blockIdx.x * chunk;
+    const int64_t  r1    = min(a.n, r0 + chunk);
+    unsigned       kred  = 0;
+    const T        eps   = sizeof(T) == 4 ? (T)FLT_EPSILON : (T)DBL_EPSILON;
+
+    // ---- pre_solve: R = B - A X, Z = D^-1 R, delta = R.Z
+    T tpart = T(0);
+    for (int64_t i = r0 + threadIdx.x; i < r1; i += kBT) {
+        T ax = 0, ay = 0, az = 0, diag = 0;
+        row_spmv4<T>(a.rp, a.ent, i, a.X, ax, ay, az, &diag);
+        const T     di = T(1) / (diag + eps);
+        const R4<T> b  = a.B[i];
+        R4<T>       r, z;
+        r.x = b.x - ax, r.y = b.y - ay, r.z = b.z - az, r.w = T(0);
+        z.x = di * r.x, z.y = di * r.y, z.z = di * r.z, z.w = T(0);
+        a.dinv[i] = di;
+        a.R[i]    = r;
+        a.Z[i]    = z;
+        tpart += r.x * z.x + r.y * z.y + r.z * z.z;
+    }
+    double delta0;
+    if (!grid_reduce(block_sum<kBT>((double)tpart, s_red), a.part, a.bar, G, kred++, a.err, s_red,
+                     &s_ok, &delta0))
+        return;
+    double delta = delta0;
+    auto   conv  = [&](double d) { return d < a.abs_tol || d / delta0 < a.rel_tol; };
+    double beta  = 0;
+    int    it    = 0;
+    bool   done  = conv(delta0);
+    while (!done && it < a.max_iter) {
+        const T bt = (T)beta;
+        // ---- phase A: S = A z + beta S, p = z + beta p, S.p
+        tpart = T(0);
+        for (int64_t i = r0 + threadIdx.x; i < r1; i += kBT) {
+            T ax = 0, ay = 0, az = 0;
+            row_spmv4<T>(a.rp, a.ent, i, a.Z, ax, ay, az, (T*)nullptr);
+            const R4<T> zi = a.Z[i];
+            R4<T>       si, pi;
+            if (it == 0) {
+                si.x = ax, si.y = ay, si.z = az;
+                pi = zi;
+            } else {
+                const R4<T> so = a.S[i], po = a.P[i];
+                si.x = ax + bt * so.x, si.y = ay + bt * so.y, si.z = az + bt * so.z;
+                pi.x = zi.x + bt * po.x, pi.y = zi.y + bt * po.y, pi.z = zi.z + bt * po.z;
+            }
+            si.w = pi.w = T(0);
+            a.S[i] = si;
+            a.P[i] = pi;
+            tpart += si.x * pi.x + si.y * pi.y + si.z * pi.z;
+        }
+        double sp;
+        if (!grid_reduce(block_sum<kBT>((double)tpart, s_red), a.part, a.bar, G, kred++, a.err,
+                         s_red, &s_ok, &sp))
+            return;
+        const T al = (T)(delta / sp);
+        // ---- phase B: X += alpha p, R -= alpha S, Z = D^-1 R, R.Z
+        tpart = T(0);
+        for (int64_t i = r0 + threadIdx.x; i < r1; i += kBT) {
+            const T     di = a.dinv[i];
+            R4<T>       x  = a.X[i], r = a.R[i];
+            const R4<T> pi = a.P[i], si = a.S[i];
+            x.x += al * pi.x, x.y += al * pi.y, x.z += al * pi.z;
+            r.x -= al * si.x, r.y -= al * si.y, r.z -= al * si.z;
+            R4<T> z;
+            z.x = di * r.x, z.y = di * r.y, z.z = di * r.z, z.w = T(0);
+            a.X[i] = x;
+            a.R[i] = r;
+            a.Z[i] = z;
+            tpart += r.x * z.x + r.y * z.y + r.z * z.z;
+        }
+        double dn;
+        if (!grid_reduce(block_sum<kBT>((double)tpart, s_red), a.part, a.bar, G, kred++, a.err,
+                         s_red, &s_ok, &dn))
+            return;
+        if (conv(dn)) {
+            delta = dn;
+            done  = true;
+            break;
+        }
+        beta  = dn / delta;
+        delta = dn;
+        ++it;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.dstat[0] = delta0;
+        a.dstat[1] = delta;
+        a.istat[0] = it;
+        a.istat[1] = done ? 1 : 0;
+    }
 }
 
-// r = B - A x in FP64 with FP32 matrix entries; r32 = (float) r; per-block |r|^2
-__global__ void __launch_bounds__(256) k_resid_mixed(int64_t n, const int32_t* __restrict__ rp,
-                                                     const int32_t* __restrict__ col,
-                                                     const float* __restrict__ val,
-                                                     const double* __restrict__ x,
-                                                     const double* __restrict__ B,
-                                                     float* __restrict__ r32,
-                                                     double* __restrict__ part)
+// ---------------------------------------------------------------------
+// Pipelined Jacobi-PCG (Ghysels & Vanroose 2014, "Hiding global
+// synchronization latency in the preconditioned conjugate gradient
+// algorithm") for the FP32 inner solves of the mixed MCF step.  With the
+// Jacobi preconditioner M = D^-1 applied elementwise, u = M r, m = M w and
+// q = M s are never stored, and every iteration is ONE pass over the rows:
+//   n = A (M w_old)             gathered from the other w buffer
+//   z = n + beta z,  s = w + beta s,  p = M r + beta p
+//   x += alpha p,  r -= alpha s,  w_new = w_old - alpha z
+//   gamma' = r . M r,  delta' = w_new . M r
+// followed by ONE grid reduction of (gamma', delta').  alpha, beta come from
+// the previous reduction: beta = gamma / gamma_prev,
+// alpha = gamma / (delta - beta gamma / alpha_prev).  w is double-buffered
+// (neighbours read the old one) and carries dinv in its fourth lane.
+// The stopping rule is the PCG one on gamma = r . M r.
+// ---------------------------------------------------------------------
+
+template <typename T>
+struct PipeArgs
+{
+    int64_t        n;
+    const int32_t* rp;
+    const Ent<T>*  ent;
+    const R4<T>*   B;
+    R4<T>*         X;
+    R4<T>*         R;   // w lane: dinv
+    R4<T>*         W0;  // w lane: dinv
+    R4<T>*         W1;
+    R4<T>*         Z;
+    R4<T>*         S;
+    R4<T>*         P;
+    double*        part;  // 2 * G
+    unsigned*      bar;
+    double*        dstat;
+    int*           istat;
+    int            max_iter;
+    double         abs_tol, rel_tol;
+    int*           err;
+};
+
+// two-value version of grid_reduce (gamma and delta in one barrier); the
+// second value uses part[G..2G) and slot pair bar[8..11]
+__device__ __forceinline__ bool grid_reduce2v(double v0, double v1, double* part, unsigned* bar,
+                                              unsigned G, unsigned k, int* err, double* s_red,
+                                              int* s_ok, double* o0, double* o1)
+{
+    unsigned long long* slot = reinterpret_cast<unsigned long long*>(bar + 4);  // [2] v0, [2] v1
+    const unsigned long long kNotYet = ~0ull;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const unsigned lane = threadIdx.x;
+        unsigned       last = 0;
+        if (lane == 0) {
+            part[blockIdx.x]     = v0;
+            part[G + blockIdx.x] = v1;
+            __threadfence();
+            last = (atomicAdd(bar, 1u) % G) == G - 1 ? 1u : 0u;
+        }
+        last      = __shfl_sync(0xffffffffu, last, 0);
+        int    ok = 1;
+        double s0 = 0, s1 = 0;
+        if (last) {
+            __threadfence();
+            double a0 = 0, a1 = 0;
+#pragma unroll 4
+            for (unsigned i = lane; i < G; i += 32) {
+                a0 += __ldcg(part + i);
+                a1 += __ldcg(part + G + i);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+                a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+            }
+            s0 = a0, s1 = a1;
+            if (lane == 0) {
+                // v1 first: pollers read v0's slot last (published last)
+                *((volatile unsigned long long*)(slot + 2 + ((k + 1) & 1))) = kNotYet;
+                *((volatile unsigned long long*)(slot + ((k + 1) & 1)))     = kNotYet;
+                __threadfence();
+                *((volatile unsigned long long*)(slot + 2 + (k & 1))) =
+                    (unsigned long long)__double_as_longlong(a1);
+                __threadfence();
+                *((volatile unsigned long long*)(slot + (k & 1))) =
+                    (unsigned long long)__double_as_longlong(a0);
+            }
+        } else if (lane == 0) {
+            volatile unsigned* vab = bar + 2;
+            uint32_t           it  = 0;
+            while (true) {
+                const unsigned long long w = *((volatile unsigned long long*)(slot + (k & 1)));
+                if (w != kNotYet) {
+                    s0 = __longlong_as_double((long long)w);
+                    break;
+                }
+                if (*vab) {
+                    ok = 0;
+                    break;
+                }
+                if (++it > kWaitLimit) {
+                    atomicOr(err, DEVERR_GRID_TIMEOUT);
+                    atomicExch(bar + 2, 1u);
+                    ok = 0;
+                    break;
+                }
+            }
+            __threadfence();
+            s1 = __longlong_as_double(
+                (long long)*((volatile unsigned long long*)(slot + 2 + (k & 1))));
+        }
+        if (lane == 0) {
+            s_red[0] = s0;
+            s_red[1] = s1;
+            *s_ok    = ok;
+        }
+    }
+    __syncthreads();
+    *o0           = s_red[0];
+    *o1           = s_red[1];
+    const bool ok = *s_ok != 0;
+    __syncthreads();
+    return ok;
+}
+
+// acc = sum_j A_ij (dinv_j v_j) with dinv_j in lane w of v_j
+template <typename T>
+__device__ __forceinline__ void row_spmv_scaled(const int32_t* __restrict__ rp,
+                                                const Ent<T>* __restrict__ ent, int64_t i,
+                                                const R4<T>* v, T& ax, T& ay, T& az)
+{
+    const int32_t b = __ldg(rp + i), e = __ldg(rp + i + 1);
+    for (int32_t j0 = b; j0 < e; j0 += 8) {
+        Ent<T> q[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (j0 + u < e) {
+                q[u] = ent[j0 + u];
+            } else {
+                q[u].col = (int32_t)i;
+                q[u].val = T(0);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const R4<T> xv = v[q[u].col];
+            const T     c  = q[u].val * xv.w;
+            ax += c * xv.x;
+            ay += c * xv.y;
+            az += c * xv.z;
+        }
+    }
+}
+
+template <typename T, int kBT>
+__global__ void __launch_bounds__(kBT) k_pcg_pipe(PipeArgs<T> a)
+{
+    __shared__ double s_red[kBT / 32 + 2];
+    __shared__ int    s_ok;
+    const unsigned G     = gridDim.x;
+    const int64_t  chunk = (a.n + G - 1) / G;
+    const int64_t  r0    = blockIdx.x * chunk;
+    const int64_t  r1    = min(a.n, r0 + chunk);
+    unsigned       kred  = 0;
+    const T        eps   = sizeof(T) == 4 ? (T)FLT_EPSILON : (T)DBL_EPSILON;
+
+    // ---- r = B - A X (dinv into lane w), then barrier
+    for (int64_t i = r0 + threadIdx.x; i < r1; i += kBT) {
+        T ax = 0, ay = 0, az = 0, diag = 0;
+        row_spmv4<T>(a.rp, a.ent, i, a.X, ax, ay, az, &diag);
+        const R4<T> b = a.B[i];
+        R4<T>       r;
+        r.x = b.x - ax, r.y = b.y - ay, r.z = b.z - az, r.w = T(1) / (diag + eps);
+        a.R[i] = r;
+    }
+    double d0, d1;
+    if (!grid_reduce2v(0.0, 0.0, a.part, a.bar, G, kred++, a.err, s_red, &s_ok, &d0, &d1)) return;
+    // ---- w = A M r; gamma = r.Mr, delta = w.Mr
+    T tg = T(0), td = T(0);
+    for (int64_t i = r0 + threadIdx.x; i < r1; i += kBT) {
+        T ax = 0, ay = 0, az = 0;
+        row_spmv_scaled<T>(a.rp, a.ent, i, a.R, ax, ay, az);
+        const R4<T> r = a.R[i];
+        R4<T>       w;
+        w.x = ax, w.y = ay, w.z = az, w.w = r.w;
+        a.W0[i]    = w;
+        const T ux = r.w * r.x, uy = r.w * r.y, uz = r.w * r.z;
+        tg += r.x * ux + r.y * uy + r.z * uz;
+        td += w.x * ux + w.y * uy + w.z * uz;
+    }
+    double gamma, delta;
+    if (!grid_reduce2v(block_sum<kBT>((double)tg, s_red), block_sum<kBT>((double)td, s_red), a.part,
+                       a.bar, G, kred++, a.err, s_red, &s_ok, &gamma, &delta))
+        return;
+    const double gamma0 = gamma;
+    auto   conv  = [&](double g) { return g < a.abs_tol || g / gamma0 < a.rel_tol; };
+    double alpha_prev = 1.0, gamma_prev = 1.0;
+    int    it   = 0;
+    bool   done = conv(gamma0);
+    // stagnation guard: in FP32 the recursive residual of the pipelined
+    // recurrences can stall above a tight target; the caller's FP64
+    // refinement restarts from a fresh residual instead
+    double best = gamma0;
+    int    best_it = 0;
+    while (!done && it < a.max_iter) {
+        double alpha, beta;
+        if (it == 0) {
+            beta  = 0.0;
+            alpha = gamma / delta;
+        } else {
+            beta  = gamma / gamma_prev;
+            alpha = gamma / (delta - beta * gamma / alpha_prev);
+        }
+        const T     al = (T)alpha, bt = (T)beta;
+        R4<T>*      Wo = (it & 1) ? a.W1 : a.W0;
+        R4<T>*      Wn = (it & 1) ? a.W0 : a.W1;
+        tg = T(0), td = T(0);
+        for (int64_t i = r0 + threadIdx.x; i < r1; i += kBT) {
+            T nx = 0, ny = 0, nz = 0;
+            row_spmv_scaled<T>(a.rp, a.ent, i, Wo, nx, ny, nz);
+            const R4<T> w = Wo[i];
+            R4<T>       r = a.R[i], x = a.X[i], z, s, p;
+            const T     di = r.w;
+            if (it == 0) {
+                z.x = nx, z.y = ny, z.z = nz;
+                s.x = w.x, s.y = w.y, s.z = w.z;
+                p.x = di * r.x, p.y = di * r.y, p.z = di * r.z;
+            } else {
+                const R4<T> zo = a.Z[i], so = a.S[i], po = a.P[i];
+                z.x = nx + bt * zo.x, z.y = ny + bt * zo.y, z.z = nz + bt * zo.z;
+                s.x = w.x + bt * so.x, s.y = w.y + bt * so.y, s.z = w.z + bt * so.z;
+                p.x = di * r.x + bt * po.x, p.y = di * r.y + bt * po.y, p.z = di * r.z + bt * po.z;
+            }
+            z.w = s.w = p.w = T(0);
+            x.x += al * p.x, x.y += al * p.y, x.z += al * p.z;
+            r.x -= al * s.x, r.y -= al * s.y, r.z -= al * s.z;
+            R4<T> wn;
+            wn.x = w.x - al * z.x, wn.y = w.y - al * z.y, wn.z = w.z - al * z.z, wn.w = di;
+            a.Z[i] = z;
+            a.S[i] = s;
+            a.P[i] = p;
+            a.X[i] = x;
+            a.R[i] = r;
+            Wn[i]  = wn;
+            const T ux = di * r.x, uy = di * r.y, uz = di * r.z;
+            tg += r.x * ux + r.y * uy + r.z * uz;
+            td += wn.x * ux + wn.y * uy + wn.z * uz;
+        }
+        double gn, dn;
+        if (!grid_reduce2v(block_sum<kBT>((double)tg, s_red), block_sum<kBT>((double)td, s_red),
+                           a.part, a.bar, G, kred++, a.err, s_red, &s_ok, &gn, &dn))
+            return;
+        alpha_prev = alpha;
+        gamma_prev = gamma;
+        gamma      = gn;
+        delta      = dn;
+        ++it;
+        done = conv(gn);
+        if (gn < 0.25 * best) {
+            best    = gn;
+            best_it = it;
+        } else if (it - best_it > 40) {
+            break;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.dstat[0] = gamma0;
+        a.dstat[1] = gamma;
+        a.istat[0] = it;
+        a.istat[1] = done ? 1 : 0;
+    }
+}
+
+// CTA size of the packed MCF solver: RXG_MCF_CG_THREADS=256|512|1024 (default 1024)
+static int cgm_threads()
+{
+    static int t = 0;
+    if (!t) {
+        const char* e = getenv("RXG_MCF_CG_THREADS");
+        t             = e ? atoi(e) : 1024;
+        if (t != 256 && t != 512 && t != 1024) t = 1024;
+    }
+    return t;
+}
+
+template <typename T, int BT>
+static int cgm_grid_bt(int64_t n)
+{
+    static int per_sm = -1;
+    if (per_sm < 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgm<T, BT>, BT, 0) != cudaSuccess)
+            per_sm = 1;
+        per_sm = std::max(1, std::min(per_sm, 2048 / BT));
+    }
+    int64_t g = (int64_t)num_sms() * per_sm;
+    return (int)std::min<int64_t>(g, std::max<int64_t>(1, (n + 31) / 32));
+}
+
+template <typename T>
+static int cgm_grid(int64_t n)
+{
+    switch (cgm_threads()) {
+        case 256: return cgm_grid_bt<T, 256>(n);
+        case 512: return cgm_grid_bt<T, 512>(n);
+        default: return cgm_grid_bt<T, 1024>(n);
+    }
+}
+
+template <typename T>
+static size_t cgm_scratch_bytes(int64_t n, int G)
+{
+    return 4 * align256(sizeof(R4<T>) * n) + align256(sizeof(T) * n) +
+           align256(sizeof(double) * G) + 3 * 256;
+}
+
+template <typename T>
+static rxg_status cgm_launch(int64_t n, const int32_t* rp, const Ent<T>* ent, const R4<T>* B,
+                             R4<T>* X, const rxg_solver_opts& o, rxg_solver_stats* st,
+                             uint8_t* scratch, cudaStream_t s)
+{
+    const int    G  = cgm_grid<T>(n);
+    const size_t vb = align256(sizeof(R4<T>) * n);
+    CGMArgs<T>   a;
+    uint8_t*     q = scratch;
+    a.n   = n;
+    a.rp  = rp;
+    a.ent = ent;
+    a.B   = B;
+    a.X   = X;
+    a.R = (R4<T>*)q, q += vb;
+    a.P = (R4<T>*)q, q += vb;
+    a.S = (R4<T>*)q, q += vb;
+    a.Z = (R4<T>*)q, q += vb;
+    a.dinv  = (T*)q, q += align256(sizeof(T) * n);
+    a.part  = (double*)q, q += align256(sizeof(double) * G);
+    a.bar   = (unsigned*)q, q += 256;
+    a.dstat = (double*)q, q += 256;
+    a.istat = (int*)q, q += 256;
+    a.max_iter = o.max_iter;
+    a.abs_tol  = o.abs_tol;
+    a.rel_tol  = o.rel_tol;
+    a.err      = device_error_word();
+    RXG_CUDA_TRY(reset_grid_reduce(a.bar, s));
+    void*       args[] = {&a};
+    const void* kern   = cgm_threads() == 256   ? (const void*)k_cgm<T, 256>
+                         : cgm_threads() == 512 ? (const void*)k_cgm<T, 512>
+                                                : (const void*)k_cgm<T, 1024>;
+    RXG_CUDA_TRY(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(cgm_threads()), args, 0, s));
+    double ds[2];
+    int    is[2];
+    RXG_CUDA_TRY(cudaMemcpyAsync(ds, a.dstat, sizeof(ds), cudaMemcpyDeviceToHost, s));
+    RXG_CUDA_TRY(cudaMemcpyAsync(is, a.istat, sizeof(is), cudaMemcpyDeviceToHost, s));
+    RXG_CUDA_TRY(cudaStreamSynchronize(s));
+    rxg_status e = check_device_error(s);
+    if (e) return e;
+    st->start_res = ds[0];
+    st->final_res = ds[1];
+    st->iters     = is[0];
+    st->converged = is[1];
+    return RXG_OK;
+}
+
+template <typename T>
+static size_t pipe_scratch_bytes(int64_t n, int G)
+{
+    return 6 * align256(sizeof(R4<T>) * n) + align256(sizeof(double) * 2 * G) + 3 * 256;
+}
+
+template <typename T, int BT>
+static int pipe_grid_bt(int64_t n)
+{
+    static int per_sm = -1;
+    if (per_sm < 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_pipe<T, BT>, BT, 0) !=
+            cudaSuccess)
+            per_sm = 1;
+        per_sm = std::max(1, std::min(per_sm, 2048 / BT));
+    }
+    int64_t g = (int64_t)num_sms() * per_sm;
+    return (int)std::min<int64_t>(g, std::max<int64_t>(1, (n + 31) / 32));
+}
+
+// CTA size of the pipelined solver: RXG_MCF_PIPE_THREADS=256|512|1024 (default
+// 512: at 1024 threads the 64-register cap makes it spill)
+static int pipe_threads()
+{
+    static int t = 0;
+    if (!t) {
+        const char* e = getenv("RXG_MCF_PIPE_THREADS");
+        t             = e ? atoi(e) : 512;
+        if (t != 256 && t != 512 && t != 1024) t = 512;
+    }
+    return t;
+}
+
+template <typename T>
+static int pipe_grid(int64_t n)
+{
+    switch (pipe_threads()) {
+        case 256: return pipe_grid_bt<T, 256>(n);
+        case 512: return pipe_grid_bt<T, 512>(n);
+        default: return pipe_grid_bt<T, 1024>(n);
+    }
+}
+
+template <typename T>
+static rxg_status pipe_launch(int64_t n, const int32_t* rp, const Ent<T>* ent, const R4<T>* B,
+                              R4<T>* X, const rxg_solver_opts& o, rxg_solver_stats* st,
+                              uint8_t* scratch, cudaStream_t s)
+{
+    const int    G  = pipe_grid<T>(n);
+    const size_t vb = align256(sizeof(R4<T>) * n);
+    PipeArgs<T>  a;
+    uint8_t*     q = scratch;
+    a.n   = n;
+    a.rp  = rp;
+    a.ent = ent;
+    a.B   = B;
+    a.X   = X;
+    a.R  = (R4<T>*)q, q += vb;
+    a.W0 = (R4<T>*)q, q += vb;
+    a.W1 = (R4<T>*)q, q += vb;
+    a.Z  = (R4<T>*)q, q += vb;
+    a.S  = (R4<T>*)q, q += vb;
+    a.P  = (R4<T>*)q, q += vb;
+    a.part  = (double*)q, q += align256(sizeof(double) * 2 * G);
+    a.bar   = (unsigned*)q, q += 256;
+    a.dstat = (double*)q, q += 256;
+    a.istat = (int*)q, q += 256;
+    a.max_iter = o.max_iter;
+    a.abs_tol  = o.abs_tol;
+    a.rel_tol  = o.rel_tol;
+    a.err      = device_error_word();
+    RXG_CUDA_TRY(reset_grid_reduce(a.bar, s));
+    void*       args[] = {&a};
+    const void* kern   = pipe_threads() == 256   ? (const void*)k_pcg_pipe<T, 256>
+                         : pipe_threads() == 512 ? (const void*)k_pcg_pipe<T, 512>
+                                                 : (const void*)k_pcg_pipe<T, 1024>;
+    RXG_CUDA_TRY(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(pipe_threads()), args, 0, s));
+    double ds[2];
+    int    is[2];
+    RXG_CUDA_TRY(cudaMemcpyAsync(ds, a.dstat, sizeof(ds), cudaMemcpyDeviceToHost, s));
+    RXG_CUDA_TRY(cudaMemcpyAsync(is, a.istat, sizeof(is), cudaMemcpyDeviceToHost, s));
+    RXG_CUDA_TRY(cudaStreamSynchronize(s));
+    rxg_status e = check_device_error(s);
+    if (e) return e;
+    st->start_res = ds[0];
+    st->final_res = ds[1];
+    st->iters     = is[0];
+    st->converged = is[1];
+    return RXG_OK;
+}
+
+// RXG_MCF_VERBOSE=1 prints one line per refinement sweep to stderr
+static bool mcf_verbose()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("RXG_MCF_VERBOSE");
+        v             = (e && e[0] == '1') ? 1 : 0;
+    }
+    return v == 1;
+}
+
+// Inner solver of the mixed MCF step: the standard PCG recurrence (k_cgm);
+// RXG_MCF_PIPELINED=1 selects the pipelined one (one grid barrier per
+// iteration, but its FP32 recursive residual can stall over many flow
+// steps, which costs more refinement sweeps than the barrier saves).
+static bool mixed_pipelined()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("RXG_MCF_PIPELINED");
+        v             = (e && e[0] == '1') ? 1 : 0;
+    }
+    return v == 1;
+}
+
+// positions n x 3 (caller layout) <-> 4-wide
+__global__ void k_pack3(int64_t n, const double* __restrict__ x, R4<double>* __restrict__ y)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        R4<double> v;
+        v.x = x[3 * i], v.y = x[3 * i + 1], v.z = x[3 * i + 2], v.w = 0.0;
+        y[i] = v;
+    }
+}
+__global__ void k_unpack3(int64_t n, const R4<double>* __restrict__ y, double* __restrict__ x)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const R4<double> v = y[i];
+        x[3 * i] = v.x, x[3 * i + 1] = v.y, x[3 * i + 2] = v.z;
+    }
+}
+
+// x += d (FP64 += FP32 correction)
+__global__ void k_add_correction4(int64_t n, R4<double>* __restrict__ x, const R4<float>* __restrict__ d)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        R4<double>      v = x[i];
+        const R4<float> c = d[i];
+        v.x += (double)c.x, v.y += (double)c.y, v.z += (double)c.z;
+        x[i] = v;
+    }
+}
+
+// r = B - A x accumulated in FP64 from the FP32 off-diagonal entries and the
+// FP64 diagonal (2*area + the sum of the FP32 weights); r32 = (float) r;
+// per-block r . D^-1 r (the Jacobi-weighted norm the plain PCG stops on)
+__global__ void __launch_bounds__(256) k_resid_mixed4(int64_t n, const int32_t* __restrict__ rp,
+                                                      const Ent<float>* __restrict__ ent,
+                                                      const double* __restrict__ diag,
+                                                      const R4<double>* __restrict__ x,
+                                                      const R4<double>* __restrict__ B,
+                                                      R4<float>* __restrict__ r32,
+                                                      double* __restrict__ part)
 {
     __shared__ double s_red[256 / 32 + 2];
     double            acc2 = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        double a0 = 0, a1 = 0, a2 = 0;
-        for (int32_t j = rp[i]; j < rp[i + 1]; ++j) {
-            const double  v = (double)val[j];
-            const int64_t c = 3 * (int64_t)col[j];
-            a0 += v * x[c];
-            a1 += v * x[c + 1];
-            a2 += v * x[c + 2];
+        const R4<double> xi = x[i];
+        const double     d  = diag[i];
+        double           a0 = d * xi.x, a1 = d * xi.y, a2 = d * xi.z;
+        const int32_t    e  = rp[i + 1];
+        for (int32_t j0 = rp[i] + 1; j0 < e; j0 += 8) {
+            Ent<float> q[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (j0 + u < e) {
+                    q[u] = ent[j0 + u];
+                } else {
+                    q[u].col = (int32_t)i;
+                    q[u].val = 0.f;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const double     v  = (double)q[u].val;
+                const R4<double> xv = x[q[u].col];
+                a0 += v * xv.x, a1 += v * xv.y, a2 += v * xv.z;
+            }
         }
-        const double e0 = B[3 * i] - a0, e1 = B[3 * i + 1] - a1, e2 = B[3 * i + 2] - a2;
-        r32[3 * i]     = (float)e0;
-        r32[3 * i + 1] = (float)e1;
-        r32[3 * i + 2] = (float)e2;
-        acc2 += e0 * e0 + e1 * e1 + e2 * e2;
+        const R4<double> b  = B[i];
+        const double     e0 = b.x - a0, e1 = b.y - a1, e2 = b.z - a2;
+        R4<float>        r;
+        r.x = (float)e0, r.y = (float)e1, r.z = (float)e2, r.w = 0.f;
+        r32[i] = r;
+        acc2 += (e0 * e0 + e1 * e1 + e2 * e2) / d;
     }
     acc2 = block_sum<256>(acc2, s_red);
     if (threadIdx.x == 0) part[blockIdx.x] = acc2;
@@ -1025,7 +1635,7 @@ rxg_status rxg_query_oriented_vv(const rxg_mesh* h, int32_t* offsets, int32_t* v
     }
     int8_t* b = boundary;
     if (!b) RXG_CUDA_TRY(cudaMallocAsync((void**)&b, std::max<int64_t>(16, h->m.nv), S_(stream)));
-    rxg_status st = launch_oriented(&h->m, offsets, values, b, S_(stream));
+    rxg_status st = launch_oriented(&h->m, offsets, values, b, nullptr, S_(stream));
     if (!boundary) cudaFreeAsync(b, S_(stream));
     if (st) return st;
     return check_device_error(S_(stream));
@@ -1066,10 +1676,10 @@ rxg_status rxg_mcf_assemble(const rxg_mesh* h, double dt, const double* xyz, rxg
     const int g = grid_for(nv);
     if (A->dtype == RXG_F64)
         k_mcf_assemble<double, Geo<double>, double><<<g, 256, 0, s>>>(
-            nv, z->row_ptr, z->col, z->bnd, xyz, dt, (double*)A->val, (double*)B);
+            nv, z->row_ptr, z->col, z->bnd, xyz, dt, CsrOut<double, double>{(double*)A->val, (double*)B});
     else
         k_mcf_assemble<float, GeoMixed, float><<<g, 256, 0, s>>>(
-            nv, z->row_ptr, z->col, z->bnd, xyz, (float)dt, (float*)A->val, (float*)B);
+            nv, z->row_ptr, z->col, z->bnd, xyz, (float)dt, CsrOut<float, float>{(float*)A->val, (float*)B});
     RXG_CUDA_TRY(cudaGetLastError());
     return RXG_OK;
 }
@@ -1147,77 +1757,98 @@ rxg_status rxg_mcf_step(const rxg_mesh* h, double dt, int32_t nsteps, int32_t pr
     rxg_status   st = ensure_pattern(&h->m, s, &z);
     if (st) return st;
     const int64_t n = h->m.nv, nnz = z->nnz;
-    const int     Gd = cg_grid_any<double>(3, true, n), Gf = cg_grid_any<float>(3, true, n);
     const int     Gr = grid_for(n);
-    const size_t  plain = align256(8 * nnz) + align256(24 * n) + cg_scratch_bytes<double>(n, 3, Gd);
-    const size_t  mixed = align256(4 * nnz) + align256(24 * n) + 2 * align256(12 * n) +
-                         align256(8 * Gr) + cg_scratch_bytes<float>(n, 3, Gf);
+    // buffers: X4 (FP64 positions), B4 (FP64 RHS), packed A, then per precision
+    const size_t x4b = align256(sizeof(R4<double>) * n);
+    const size_t plain = 2 * x4b + align256(sizeof(Ent<double>) * nnz) +
+                         cgm_scratch_bytes<double>(n, cgm_grid<double>(n));
+    const size_t mixed = 2 * x4b + align256(sizeof(Ent<float>) * nnz) +
+                         2 * align256(sizeof(R4<float>) * n) + align256(8 * Gr) + align256(8 * n) +
+                         std::max(cgm_scratch_bytes<float>(n, cgm_grid<float>(n)),
+                                  pipe_scratch_bytes<float>(n, pipe_grid<float>(n)));
     {
         std::lock_guard<std::mutex> g(z->mu);
         if ((st = mcf_buffers(z, std::max(plain, mixed), s))) return st;
     }
     // positions: device, or staged from host
-    double* X         = xyz;
-    bool    staged    = false;
+    double* X      = xyz;
+    bool    staged = false;
     if (!is_device_ptr(xyz)) {
         RXG_CUDA_TRY(cudaMallocAsync((void**)&X, 24 * n, s));
         RXG_CUDA_TRY(cudaMemcpyAsync(X, xyz, 24 * n, cudaMemcpyHostToDevice, s));
         staged = true;
     }
-    uint8_t*         q    = (uint8_t*)z->buf;
+    uint8_t*    q  = (uint8_t*)z->buf;
+    R4<double>* X4 = (R4<double>*)q;
+    R4<double>* B4 = (R4<double>*)(q + x4b);
+    uint8_t*    p  = q + 2 * x4b;
     rxg_solver_stats last = {0, 1, 0.0, 0.0};
     const int        ga   = grid_for(n);
+    k_pack3<<<ga, 256, 0, s>>>(n, X, X4);
     for (int step = 0; step < nsteps && st == RXG_OK; ++step) {
+        // the assembly reads the caller-layout positions of this step
+        if (step > 0) k_unpack3<<<ga, 256, 0, s>>>(n, X4, X);
         if (precision == RXG_F64) {
-            double*  val = (double*)q;
-            double*  B   = (double*)(q + align256(8 * nnz));
-            uint8_t* scr = q + align256(8 * nnz) + align256(24 * n);
+            Ent<double>* ent = (Ent<double>*)p;
+            uint8_t*     scr = p + align256(sizeof(Ent<double>) * nnz);
             k_mcf_assemble<double, Geo<double>, double><<<ga, 256, 0, s>>>(
-                n, z->row_ptr, z->col, z->bnd, X, dt, val, B);
+                n, z->row_ptr, z->col, z->bnd, X, dt, PackedOut<double, double>{ent, B4, nullptr});
             RXG_CUDA_TRY(cudaGetLastError());
             rxg_solver_opts o = {max_iter, 0.0, tol * tol, 1};
-            st = cg_dispatch<double>(3, n, z->row_ptr, z->col, val, B, X, o, &last, scr, s);
+            st = cgm_launch<double>(n, z->row_ptr, ent, B4, X4, o, &last, scr, s);
         } else {
-            float*   val  = (float*)q;
-            uint8_t* p    = q + align256(4 * nnz);
-            double*  B    = (double*)p;
-            p += align256(24 * n);
-            float* r32 = (float*)p;
-            p += align256(12 * n);
-            float* d32 = (float*)p;
-            p += align256(12 * n);
-            double* part = (double*)p;
-            p += align256(8 * Gr);
-            uint8_t* scr = p;
-            k_mcf_assemble<float, GeoMixed, double><<<ga, 256, 0, s>>>(n, z->row_ptr, z->col, z->bnd,
-                                                                       X, (float)dt, val, B);
+            Ent<float>* ent = (Ent<float>*)p;
+            uint8_t*    w   = p + align256(sizeof(Ent<float>) * nnz);
+            R4<float>*  r32 = (R4<float>*)w;
+            w += align256(sizeof(R4<float>) * n);
+            R4<float>* d32 = (R4<float>*)w;
+            w += align256(sizeof(R4<float>) * n);
+            double* part = (double*)w;
+            w += align256(8 * Gr);
+            double* D64 = (double*)w;
+            w += align256(8 * n);
+            uint8_t* scr = w;
+            k_mcf_assemble<float, GeoMixed, double><<<ga, 256, 0, s>>>(
+                n, z->row_ptr, z->col, z->bnd, X, (float)dt, PackedOut<float, double>{ent, B4, D64});
             RXG_CUDA_TRY(cudaGetLastError());
-            k_resid_mixed<<<Gr, 256, 0, s>>>(n, z->row_ptr, z->col, val, X, B, r32, part);
+            k_resid_mixed4<<<Gr, 256, 0, s>>>(n, z->row_ptr, ent, D64, X4, B4, r32, part);
             double rr0;
             if ((st = reduce_partials(part, Gr, s, &rr0))) break;
-            double rr = rr0;
+            double rr       = rr0;
             int    total_it = 0;
-            bool   conv = rr0 == 0.0;
+            bool   conv     = rr0 == 0.0;
             for (int sweep = 0; sweep < 16 && !conv && total_it < max_iter; ++sweep) {
                 // solve only as far as this sweep needs, but not below FP32's reach
                 const double need  = tol * std::sqrt(rr0 / rr);
                 const double inner = std::max(1e-4, 0.3 * need);
-                RXG_CUDA_TRY(cudaMemsetAsync(d32, 0, 12 * n, s));
+                RXG_CUDA_TRY(cudaMemsetAsync(d32, 0, sizeof(R4<float>) * n, s));
                 rxg_solver_opts  o = {max_iter - total_it, 0.0, inner * inner, 1};
                 rxg_solver_stats si;
-                st = cg_dispatch<float>(3, n, z->row_ptr, z->col, val, r32, d32, o, &si, scr, s);
+                st = mixed_pipelined()
+                         ? pipe_launch<float>(n, z->row_ptr, ent, r32, d32, o, &si, scr, s)
+                         : cgm_launch<float>(n, z->row_ptr, ent, r32, d32, o, &si, scr, s);
                 if (st) break;
                 total_it += si.iters + 1;
-                k_add_correction<<<grid_for(3 * n), 256, 0, s>>>(3 * n, X, d32);
-                k_resid_mixed<<<Gr, 256, 0, s>>>(n, z->row_ptr, z->col, val, X, B, r32, part);
+                k_add_correction4<<<ga, 256, 0, s>>>(n, X4, d32);
+                k_resid_mixed4<<<Gr, 256, 0, s>>>(n, z->row_ptr, ent, D64, X4, B4, r32, part);
                 if ((st = reduce_partials(part, Gr, s, &rr))) break;
                 conv = rr < tol * tol * rr0;
+                if (mcf_verbose())
+                    fprintf(stderr, "rxg mcf mixed: sweep %d inner_tol %.3g iters %d conv %d "
+                                    "gamma %.3g -> %.3g |r|^2/|r0|^2 %.3g\n",
+                            sweep, inner, si.iters, si.converged, si.start_res, si.final_res,
+                            rr / rr0);
             }
             last.iters     = total_it;
             last.converged = conv ? 1 : 0;
             last.start_res = rr0;
             last.final_res = rr;
         }
+    }
+    if (st == RXG_OK) {
+        k_unpack3<<<ga, 256, 0, s>>>(n, X4, X);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) st = cuda_status(e, "rxg_mcf_step");
     }
     if (st == RXG_OK && staged) {
         RXG_CUDA_TRY(cudaMemcpyAsync(xyz, X, 24 * n, cudaMemcpyDeviceToHost, s));
@@ -1328,6 +1959,223 @@ extern "C" rxg_status rxg_cg_solve_noalloc(const rxg_csr* A, int32_t nc, const v
         st = cg_dispatch<float>(nc, A->n, A->row_ptr, A->col, (const float*)A->val,
                                 (const float*)B, (float*)X, *opts, &local, scratch, s);
     if (st) return st;
+    if (stats) *stats = local;
+    return local.converged ? RXG_OK : RXG_ERR_NOT_CONVERGED;
+}
+
+// ---------------------------------------------------------------------
+// Adjoint of one implicit MCF step.
+//
+// Forward: A(x) x1 = B(x), A = 2 diag(area) + dt L(w), B = 2 diag(area) x
+// (mcf_A_setup / mcf_B_setup).  For a loss l with gbar = dl/dx1:
+//   lambda = A^{-T} gbar = A^{-1} gbar          (A is symmetric: one more PCG)
+//   dl/dA_ij = -lambda_i . x1_j,  dl/dB_i = lambda_i
+// and with row p's area a_p and weights w_pr:
+//   dl/da_p  = 2 lambda_p . (x_p - x1_p)
+//   dl/dw_pr = dt lambda_p . (x1_r - x1_p)      (times the max(w,0) gate)
+//   dl/dx_p += 2 a_p lambda_p                   (B's explicit x)
+// The weight and area derivatives come from forward-mode duals run through
+// the same half_cot / voronoi code as the assembly, so clamps and obtuse
+// branches are differentiated exactly as evaluated.
+// ---------------------------------------------------------------------
+
+namespace rxg {
+
+struct Dual9
+{
+    double v;
+    double d[9];
+    __device__ Dual9() : v(0)
+    {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) d[i] = 0;
+    }
+    __device__ Dual9(double x) : v(x)
+    {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) d[i] = 0;
+    }
+};
+__device__ __forceinline__ Dual9 operator+(const Dual9& a, const Dual9& b)
+{
+    Dual9 r(a.v + b.v);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) r.d[i] = a.d[i] + b.d[i];
+    return r;
+}
+__device__ __forceinline__ Dual9 operator-(const Dual9& a, const Dual9& b)
+{
+    Dual9 r(a.v - b.v);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) r.d[i] = a.d[i] - b.d[i];
+    return r;
+}
+__device__ __forceinline__ Dual9 operator-(const Dual9& a)
+{
+    Dual9 r(-a.v);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) r.d[i] = -a.d[i];
+    return r;
+}
+__device__ __forceinline__ Dual9 operator*(const Dual9& a, const Dual9& b)
+{
+    Dual9 r(a.v * b.v);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+    return r;
+}
+__device__ __forceinline__ Dual9 operator/(const Dual9& a, const Dual9& b)
+{
+    const double iv = 1.0 / b.v;
+    Dual9        r(a.v * iv);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * iv;
+    return r;
+}
+__device__ __forceinline__ Dual9& operator+=(Dual9& a, const Dual9& b) { return a = a + b; }
+__device__ __forceinline__ Dual9 sqrt(const Dual9& a)
+{
+    const double s = ::sqrt(a.v);
+    Dual9        r(s);
+    const double h = s > 0 ? 0.5 / s : 0.0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) r.d[i] = a.d[i] * h;
+    return r;
+}
+__device__ __forceinline__ bool operator<(const Dual9& a, const Dual9& b) { return a.v < b.v; }
+__device__ __forceinline__ bool operator>(const Dual9& a, const Dual9& b) { return a.v > b.v; }
+__device__ __forceinline__ bool operator<=(const Dual9& a, const Dual9& b) { return a.v <= b.v; }
+__device__ __forceinline__ bool operator>=(const Dual9& a, const Dual9& b) { return a.v >= b.v; }
+template <>
+__device__ __forceinline__ Dual9 tmin<Dual9>()
+{
+    return Dual9(DBL_MIN);
+}
+
+// seeded dual vertex: tangent slots 3*slot .. 3*slot+2
+__device__ __forceinline__ V3<Dual9> seed3(V3<double> a, int slot)
+{
+    V3<Dual9> r{Dual9(a.x), Dual9(a.y), Dual9(a.z)};
+    r.x.d[3 * slot]     = 1.0;
+    r.y.d[3 * slot + 1] = 1.0;
+    r.z.d[3 * slot + 2] = 1.0;
+    return r;
+}
+
+__device__ __forceinline__ void scatter3(double* __restrict__ g, int32_t v, const Dual9& f, int slot,
+                                         double c)
+{
+    atomicAdd(g + 3 * (int64_t)v + 0, c * f.d[3 * slot + 0]);
+    atomicAdd(g + 3 * (int64_t)v + 1, c * f.d[3 * slot + 1]);
+    atomicAdd(g + 3 * (int64_t)v + 2, c * f.d[3 * slot + 2]);
+}
+
+// g_in must be zero on entry
+__global__ void __launch_bounds__(128) k_mcf_backward(int64_t nv, const int32_t* __restrict__ row_ptr,
+                                                      const int32_t* __restrict__ col,
+                                                      const int8_t* __restrict__ bnd,
+                                                      const double* __restrict__ x,
+                                                      const double* __restrict__ x1,
+                                                      const double* __restrict__ lam, double dt,
+                                                      double* __restrict__ g_in)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nv;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t    rp   = row_ptr[p];
+        const int32_t    k    = row_ptr[p + 1] - rp - 1;
+        const int32_t*   rg   = col + rp + 1;
+        const bool       wrap = bnd[p] == 0;
+        const V3<double> P    = ld3(x, (int32_t)p);
+        const V3<double> L    = ld3(lam, (int32_t)p);
+        const V3<double> Y    = ld3(x1, (int32_t)p);
+        const double     ap   = 2.0 * (L.x * (P.x - Y.x) + L.y * (P.y - Y.y) + L.z * (P.z - Y.z));
+        double           area = 0.0;
+        for (int32_t i = 0; i < k; ++i) {
+            const int32_t    r = rg[i], q = rg[(i + k - 1) % k], s = rg[(i + 1) % k];
+            const bool       has_q = wrap || i > 0, has_s = wrap || i < k - 1;
+            const V3<double> R = ld3(x, r), Q = ld3(x, q), S = ld3(x, s);
+            double           w = 0;
+            if (has_q) w += half_cot<double>(P, R, Q);
+            if (has_s) w += half_cot<double>(P, R, S);
+            const V3<double> Yr = ld3(x1, r);
+            const double beta = dt * (L.x * (Yr.x - Y.x) + L.y * (Yr.y - Y.y) + L.z * (Yr.z - Y.z));
+            if (w >= 0.0 && beta != 0.0) {
+                if (has_q) {
+                    const Dual9 h = half_cot<Dual9>(seed3(P, 0), seed3(R, 1), seed3(Q, 2));
+                    scatter3(g_in, (int32_t)p, h, 0, beta);
+                    scatter3(g_in, r, h, 1, beta);
+                    scatter3(g_in, q, h, 2, beta);
+                }
+                if (has_s) {
+                    const Dual9 h = half_cot<Dual9>(seed3(P, 0), seed3(R, 1), seed3(S, 2));
+                    scatter3(g_in, (int32_t)p, h, 0, beta);
+                    scatter3(g_in, r, h, 1, beta);
+                    scatter3(g_in, s, h, 2, beta);
+                }
+            }
+            if (has_q) {
+                const Dual9 a = voronoi<Dual9>(seed3(P, 0), seed3(Q, 1), seed3(R, 2));
+                if (a.v > 0.0) {
+                    area += a.v;
+                    if (ap != 0.0) {
+                        scatter3(g_in, (int32_t)p, a, 0, ap);
+                        scatter3(g_in, q, a, 1, ap);
+                        scatter3(g_in, r, a, 2, ap);
+                    }
+                }
+            }
+        }
+        atomicAdd(g_in + 3 * p + 0, 2.0 * area * L.x);
+        atomicAdd(g_in + 3 * p + 1, 2.0 * area * L.y);
+        atomicAdd(g_in + 3 * p + 2, 2.0 * area * L.z);
+    }
+}
+
+}  // namespace rxg
+
+extern "C" rxg_status rxg_mcf_step_backward(const rxg_mesh* h, double dt, const double* x_in,
+                                            const double* x_out, const double* g_out,
+                                            double* g_in, double tol, int32_t max_iter,
+                                            rxg_solver_stats* stats, void* stream)
+{
+    using namespace rxg;
+    if (!h || !x_in || !x_out || !g_out || !g_in || !(tol > 0) || max_iter <= 0) {
+        set_error("rxg_mcf_step_backward: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    if (!is_device_ptr(x_in) || !is_device_ptr(x_out) || !is_device_ptr(g_out) || !is_device_ptr(g_in)) {
+        set_error("rxg_mcf_step_backward: all arrays must be device arrays");
+        return RXG_ERR_INVALID;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    Lazy*        z;
+    rxg_status   st = ensure_pattern(&h->m, s, &z);
+    if (st) return st;
+    const int64_t n = h->m.nv, nnz = z->nnz;
+    const int     Gd = cg_grid_any<double>(3, true, n);
+    const size_t  need = align256(8 * nnz) + 2 * align256(24 * n) + cg_scratch_bytes<double>(n, 3, Gd);
+    {
+        std::lock_guard<std::mutex> g(z->mu);
+        if ((st = mcf_buffers(z, need, s))) return st;
+    }
+    uint8_t* q   = (uint8_t*)z->buf;
+    double*  val = (double*)q;
+    double*  B   = (double*)(q + align256(8 * nnz));
+    double*  lam = (double*)(q + align256(8 * nnz) + align256(24 * n));
+    uint8_t* scr = q + align256(8 * nnz) + 2 * align256(24 * n);
+    const int ga = grid_for(n);
+    k_mcf_assemble<double, Geo<double>, double><<<ga, 256, 0, s>>>(n, z->row_ptr, z->col, z->bnd,
+                                                                  x_in, dt, CsrOut<double, double>{val, B});
+    RXG_CUDA_TRY(cudaGetLastError());
+    RXG_CUDA_TRY(cudaMemsetAsync(lam, 0, 24 * n, s));
+    rxg_solver_opts  o = {max_iter, 0.0, tol * tol, 1};
+    rxg_solver_stats local;
+    st = cg_dispatch<double>(3, n, z->row_ptr, z->col, val, g_out, lam, o, &local, scr, s);
+    if (st) return st;
+    RXG_CUDA_TRY(cudaMemsetAsync(g_in, 0, 24 * n, s));
+    k_mcf_backward<<<grid_for(n, 128), 128, 0, s>>>(n, z->row_ptr, z->col, z->bnd, x_in, x_out, lam,
+                                                     dt, g_in);
+    RXG_CUDA_TRY(cudaGetLastError());
     if (stats) *stats = local;
     return local.converged ? RXG_OK : RXG_ERR_NOT_CONVERGED;
 }

@@ -79,7 +79,8 @@ inline int32_t pad4(int32_t words) { return (words + 3) & ~3; }
 
 }  // namespace
 
-static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv, int32_t P)
+static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv, int32_t P,
+                             bool split_components)
 {
     M.nf          = nf;
     M.nv          = nv;
@@ -154,7 +155,10 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
         cnt          = 1;
         while (cnt < P) {
             if (qh == qt) {
-                if (cnt >= P / 2) break;
+                // a component is exhausted: close the patch, or keep filling it
+                // from the next unassigned face (never across components when
+                // split_components asks each component to keep its own patches)
+                if (split_components || cnt >= P / 2) break;
                 while (seed < nf && fpatch[seed] >= 0) ++seed;
                 if (seed >= nf) break;
                 fpatch[seed] = p;
@@ -462,7 +466,7 @@ rxg_status rxg_mesh_create_ex(const int32_t* fv, int64_t nf, int64_t nv, int32_t
     }
     rxg_status s;
     try {
-        s = build_host(h->m, fv, nf, nv, patch_faces);
+        s = build_host(h->m, fv, nf, nv, patch_faces, (flags & RXG_MESH_SPLIT_COMPONENTS) != 0);
     } catch (const std::bad_alloc&) {
         set_error("rxg_mesh_create: host allocation failed");
         s = RXG_ERR_NOMEM;

@@ -1,0 +1,103 @@
+"""GPU parity of the per-face ARAP energy, gradient and block Hessian."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+from rxmesh_gb300 import meshgen
+
+pytestmark = pytest.mark.gpu
+
+
+def cloth(n=24, seed=4):
+    """create_plane grid, flat rest shape, corners displaced (the cloth workload, small)."""
+    x0, f = meshgen.plane(n, n, 1.0 / (n - 1))
+    rng = np.random.default_rng(seed)
+    x = x0.copy()
+    corners = [0, n - 1, n * (n - 1), n * n - 1]
+    x[corners] += rng.uniform(-0.2, 0.2, size=(4, 3))
+    x += 0.01 * rng.normal(size=x.shape)  # generic interior state
+    return x0, x, f
+
+
+def oracle_ref(oracle, f, x0, x, rx, prob):
+    minv, area = oracle.rest_frame(f, x0)
+    rp = prob.hess.row_ptr.cpu().numpy().astype(np.int64)
+    vl = rx.linear_to_input("v")
+    col_in = vl[prob.hess.col.cpu().numpy()]
+    # oracle assembles on the GPU's block pattern, expressed in input ids
+    il = rx.input_to_linear("v")
+    rows = np.repeat(np.arange(len(vl)), np.diff(rp))
+    order = []
+    rp_in = np.zeros(len(vl) + 1, np.int64)
+    for p in range(len(vl)):
+        lin = il[p]
+        order.append(np.arange(rp[lin], rp[lin + 1]))
+        rp_in[p + 1] = rp_in[p] + rp[lin + 1] - rp[lin]
+    order = np.concatenate(order)
+    E, fE, g, H = oracle.arap_assemble(f, x, minv, area, rp_in, col_in[order].astype(np.int32))
+    Hlin = np.empty_like(H)
+    Hlin[order] = H
+    return E, fE, g, Hlin, minv
+
+
+@pytest.mark.parametrize("dtype,rtol", [(torch.float64, 1e-11), (torch.float32, 2e-4)])
+@pytest.mark.parametrize("kind", ["cloth", "bunnyhead", "sphere"])
+def test_arap_matches_oracle(oracle, dtype, rtol, kind):
+    from rxmesh_gb300 import DiffScalarProblem, RXMeshStatic
+    if kind == "cloth":
+        x0, x, f = cloth()
+    elif kind == "bunnyhead":
+        g = golden("bunnyhead")
+        x0, f = g["xyz"], g["fv"]
+        x = x0 + 0.002 * np.random.default_rng(1).normal(size=x0.shape)
+    else:
+        v, f = meshgen.icosphere(3)
+        x0 = v
+        x = meshgen.radial_noise(v, 0.05, 2)
+    rx = RXMeshStatic(f, len(x0), patch_size=128)
+    dev = "cuda"
+    x0l = rx.to_linear(torch.tensor(x0, device=dev))
+    xl = rx.to_linear(torch.tensor(x, device=dev))
+    prob = DiffScalarProblem(rx, dtype).add_arap_term(x0l)
+    prob.eval_terms(xl)
+    E, fE, g, H, minv = oracle_ref(oracle, f, x0, x, rx, prob)
+    # rest frames
+    fl = rx.linear_to_input("f")
+    assert np.abs(prob.rest.double().cpu().numpy() - minv[fl].reshape(-1, 4)).max() <= rtol * np.abs(minv).max()
+    assert abs(prob.get_current_loss() - E) <= rtol * abs(E) + 1e-300
+    fe = prob.face_energy.double().cpu().numpy()
+    assert np.abs(fe - fE[fl]).max() <= rtol * np.abs(fE).max()
+    gg = rx.to_input(prob.grad).double().cpu().numpy()
+    assert np.abs(gg - g).max() <= rtol * np.abs(g).max()
+    Hg = prob.hess.val.double().cpu().numpy()
+    assert np.abs(Hg - H).max() <= rtol * np.abs(H).max()
+
+
+def test_arap_gradient_central_differences():
+    # FP64 central differences h = 1e-6 on random directions
+    from rxmesh_gb300 import DiffScalarProblem, RXMeshStatic
+    x0, x, f = cloth(12, seed=9)
+    rx = RXMeshStatic(f, len(x0), patch_size=64)
+    x0l = rx.to_linear(torch.tensor(x0, device="cuda"))
+    xl = rx.to_linear(torch.tensor(x, device="cuda"))
+    prob = DiffScalarProblem(rx, torch.float64).add_arap_term(x0l)
+    prob.eval_terms(xl)
+    g = prob.grad.clone()
+    Hs = prob.hess.to_scipy()
+    rng = np.random.default_rng(0)
+    h = 1e-6
+    for _ in range(16):
+        d = torch.tensor(rng.normal(size=x.shape), device="cuda")
+        ep = prob.eval_terms(xl + h * d, with_hessian=False).item()
+        em = prob.eval_terms(xl - h * d, with_hessian=False).item()
+        fd = (ep - em) / (2 * h)
+        an = (g * d).sum().item()
+        assert abs(fd - an) <= 1e-5 * max(1.0, abs(an))
+        prob.eval_terms(xl + h * d, with_hessian=False)
+        gp = prob.grad.clone()
+        prob.eval_terms(xl - h * d, with_hessian=False)
+        gm = prob.grad.clone()
+        fdg = ((gp - gm) / (2 * h)).cpu().numpy().ravel()
+        hd = Hs @ d.cpu().numpy().ravel()
+        assert np.abs(fdg - hd).max() <= 1e-5 * max(1.0, np.abs(hd).max())
