@@ -435,11 +435,20 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-arap", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--only", choices=["sweep", "mcf", "arap", "batch"],
+                    help="run one workload and print only its results (for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
 
     import torch
+    if args.only and args.only != "sweep":
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        fn = {"mcf": run_mcf, "arap": run_arap, "batch": run_batch}[args.only]
+        print(json.dumps({"only": args.only, args.only: fn(args, torch)}))
+        return
+    if args.only == "sweep":
+        args.no_mcf = args.no_arap = args.no_batch = args.no_cpu = True
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
