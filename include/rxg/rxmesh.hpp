@@ -1,0 +1,561 @@
+// rxg/rxmesh.hpp -- C++ host facade over the C ABI of librxg.so (rxg.h).
+//
+// Keeps the names and argument meaning of RXMesh's host API for the hot path
+// so that C++ callers switch with few edits:
+//   RXMeshStatic            include/rxmesh/rxmesh_static.h:61-112
+//   Op                      include/rxmesh/types.h
+//   DenseMatrix<T>          include/rxmesh/matrix/dense_matrix.h (device
+//                           storage; row-major here, ColMajor by default there)
+//   SparseMatrix<T>         include/rxmesh/matrix/sparse_matrix.h:77
+//   CGSolver / PCGSolver    include/rxmesh/matrix/cg_solver.h:17-130,
+//                           matrix/pcg_solver.h:14-213
+//   DiffScalarProblem       include/rxmesh/diff/diff_scalar_problem.h:310-321
+//                           (ARAP term only)
+// Every call goes through librxg.so; errors throw rxg::Error carrying the
+// rxg_status and rxg_last_error().  Header only; needs the CUDA runtime.
+#ifndef RXG_RXMESH_HPP
+#define RXG_RXMESH_HPP
+
+#include <cuda_runtime_api.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../rxg.h"
+
+namespace rxg {
+
+class Error : public std::runtime_error
+{
+   public:
+    Error(rxg_status s, const std::string& what) : std::runtime_error(what), status(s) {}
+    rxg_status status;
+};
+
+inline void check(rxg_status s)
+{
+    if (s != RXG_OK)
+        throw Error(s, std::string(rxg_status_string(s)) + ": " + rxg_last_error());
+}
+
+inline void check_cuda(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess)
+        throw Error(RXG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Query operations (RXMesh's Op)
+enum class Op : int32_t {
+    VV = RXG_OP_VV,
+    VE = RXG_OP_VE,
+    VF = RXG_OP_VF,
+    FV = RXG_OP_FV,
+    EV = RXG_OP_EV
+};
+
+// where a buffer lives (RXMesh's locationT)
+enum locationT : uint32_t { LOCATION_NONE = 0, HOST = 1, DEVICE = 2, LOCATION_ALL = 3 };
+
+template <typename T>
+struct dtype_of;
+template <>
+struct dtype_of<float>
+{
+    static constexpr int32_t value = RXG_F32;
+};
+template <>
+struct dtype_of<double>
+{
+    static constexpr int32_t value = RXG_F64;
+};
+
+// Owning device array.
+template <typename T>
+class DeviceArray
+{
+   public:
+    DeviceArray() = default;
+    explicit DeviceArray(size_t n) { resize(n); }
+    DeviceArray(const DeviceArray&)            = delete;
+    DeviceArray& operator=(const DeviceArray&) = delete;
+    DeviceArray(DeviceArray&& o) noexcept : m_ptr(o.m_ptr), m_n(o.m_n)
+    {
+        o.m_ptr = nullptr;
+        o.m_n   = 0;
+    }
+    DeviceArray& operator=(DeviceArray&& o) noexcept
+    {
+        std::swap(m_ptr, o.m_ptr);
+        std::swap(m_n, o.m_n);
+        return *this;
+    }
+    ~DeviceArray()
+    {
+        if (m_ptr) cudaFree(m_ptr);
+    }
+    void resize(size_t n)
+    {
+        if (m_ptr) cudaFree(m_ptr);
+        m_ptr = nullptr;
+        m_n   = n;
+        if (n) check_cuda(cudaMalloc(reinterpret_cast<void**>(&m_ptr), n * sizeof(T)), "cudaMalloc");
+    }
+    T*       data() { return m_ptr; }
+    const T* data() const { return m_ptr; }
+    size_t   size() const { return m_n; }
+
+    void upload(const T* h, size_t n, cudaStream_t s = nullptr)
+    {
+        if (n != m_n) resize(n);
+        if (n) check_cuda(cudaMemcpyAsync(m_ptr, h, n * sizeof(T), cudaMemcpyHostToDevice, s),
+                          "cudaMemcpyAsync");
+        check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    }
+    std::vector<T> to_host(cudaStream_t s = nullptr) const
+    {
+        std::vector<T> h(m_n);
+        if (m_n)
+            check_cuda(cudaMemcpyAsync(h.data(), m_ptr, m_n * sizeof(T), cudaMemcpyDeviceToHost, s),
+                       "cudaMemcpyAsync");
+        check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        return h;
+    }
+    void fill_zero(cudaStream_t s = nullptr)
+    {
+        if (m_n) check_cuda(cudaMemsetAsync(m_ptr, 0, m_n * sizeof(T), s), "cudaMemsetAsync");
+    }
+
+   private:
+    T*     m_ptr = nullptr;
+    size_t m_n   = 0;
+};
+
+// rows x cols dense matrix in device memory, row-major (one row per mesh
+// element, as every rxg call expects).
+template <typename T>
+class DenseMatrix
+{
+   public:
+    DenseMatrix() = default;
+    DenseMatrix(int64_t rows, int64_t cols, locationT where = DEVICE)
+        : m_rows(rows), m_cols(cols), m_d((size_t)(rows * cols))
+    {
+        (void)where;
+        m_d.fill_zero();
+        check_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
+    }
+    int64_t  rows() const { return m_rows; }
+    int64_t  cols() const { return m_cols; }
+    T*       data(locationT = DEVICE) { return m_d.data(); }
+    const T* data(locationT = DEVICE) const { return m_d.data(); }
+    void     reset(T v, locationT = DEVICE, cudaStream_t s = nullptr)
+    {
+        if (v == T(0)) {
+            m_d.fill_zero(s);
+            return;
+        }
+        std::vector<T> h(m_d.size(), v);
+        m_d.upload(h.data(), h.size(), s);
+    }
+    void from_host(const std::vector<T>& h, cudaStream_t s = nullptr)
+    {
+        if ((int64_t)h.size() != m_rows * m_cols) throw Error(RXG_ERR_INVALID, "size mismatch");
+        m_d.upload(h.data(), h.size(), s);
+    }
+    std::vector<T> to_host(cudaStream_t s = nullptr) const { return m_d.to_host(s); }
+
+   private:
+    int64_t        m_rows = 0, m_cols = 0;
+    DeviceArray<T> m_d;
+};
+
+// CSR adjacency of a query: offsets (rows+1, absent for FV/EV) and values,
+// both in device memory, in linear ids.
+struct QueryResult
+{
+    int64_t              rows = 0;
+    DeviceArray<int32_t> offsets;
+    DeviceArray<int32_t> values;
+};
+
+// Static triangle mesh split into patches of at most patch_size faces.
+class RXMeshStatic
+{
+   public:
+    // fv: one {v0, v1, v2} per face, input vertex ids (rxmesh_static.h:87-92).
+    // patcher_file is accepted for signature parity and must be empty: the
+    // partition is always recomputed (a BFS partitioner, deterministic).
+    explicit RXMeshStatic(std::vector<std::vector<uint32_t>>& fv,
+                          const std::string                   patcher_file = "",
+                          const uint32_t                      patch_size   = 512,
+                          bool                                host_only    = false)
+    {
+        if (!patcher_file.empty())
+            throw Error(RXG_ERR_UNSUPPORTED, "patcher files are not supported");
+        std::vector<int32_t> flat;
+        flat.reserve(3 * fv.size());
+        int64_t nv = 0;
+        for (const auto& f : fv) {
+            if (f.size() != 3) throw Error(RXG_ERR_INVALID, "only triangle faces are supported");
+            for (uint32_t v : f) {
+                flat.push_back((int32_t)v);
+                nv = std::max<int64_t>(nv, (int64_t)v + 1);
+            }
+        }
+        rxg_mesh* m = nullptr;
+        check(rxg_mesh_create_ex(flat.data(), (int64_t)fv.size(), nv, (int32_t)patch_size,
+                                 host_only ? RXG_MESH_HOST_ONLY : 0, &m));
+        m_mesh.reset(m);
+        check(rxg_mesh_get_info(m, &m_info));
+    }
+    RXMeshStatic(const RXMeshStatic&)            = delete;
+    RXMeshStatic& operator=(const RXMeshStatic&) = delete;
+
+    uint32_t get_num_vertices() const { return (uint32_t)m_info.num_vertices; }
+    uint32_t get_num_edges() const { return (uint32_t)m_info.num_edges; }
+    uint32_t get_num_faces() const { return (uint32_t)m_info.num_faces; }
+    uint32_t get_num_patches() const { return (uint32_t)m_info.num_patches; }
+    uint32_t get_patch_size() const { return (uint32_t)m_info.patch_faces; }
+    uint32_t get_input_max_valence() const { return (uint32_t)m_info.max_valence; }
+    bool     is_closed() const { return m_info.is_closed != 0; }
+    bool     is_edge_manifold() const { return m_info.is_edge_manifold != 0; }
+    const rxg_mesh_info& info() const { return m_info; }
+    const rxg_mesh*      handle() const { return m_mesh.get(); }
+
+    // input id of every linear id (map_to_global, rxmesh_static.h:874-905)
+    std::vector<int32_t> linear_to_input(int32_t elem = RXG_ELEM_VERTEX) const
+    {
+        const int64_t n = elem == RXG_ELEM_VERTEX ? m_info.num_vertices
+                          : elem == RXG_ELEM_EDGE ? m_info.num_edges
+                                                  : m_info.num_faces;
+        std::vector<int32_t> out((size_t)n);
+        check(rxg_mesh_linear_to_input(handle(), elem, out.data()));
+        return out;
+    }
+
+    // Vertex coordinates in input order (add_vertex_coordinates,
+    // rxmesh_static.h:110-112); kept on the device in linear order, FP64.
+    void add_vertex_coordinates(const std::vector<std::vector<double>>& vertices,
+                                cudaStream_t                            s = nullptr)
+    {
+        if ((int64_t)vertices.size() != m_info.num_vertices)
+            throw Error(RXG_ERR_INVALID, "one coordinate triple per vertex expected");
+        const std::vector<int32_t> l2i = linear_to_input(RXG_ELEM_VERTEX);
+        std::vector<double>        h(3 * vertices.size());
+        for (size_t l = 0; l < l2i.size(); ++l)
+            for (int c = 0; c < 3; ++c) h[3 * l + c] = vertices[(size_t)l2i[l]].at(c);
+        m_xyz = DenseMatrix<double>(m_info.num_vertices, 3);
+        m_xyz.from_host(h, s);
+    }
+    DenseMatrix<double>&       get_input_vertex_coordinates() { return m_xyz; }
+    const DenseMatrix<double>& get_input_vertex_coordinates() const { return m_xyz; }
+
+    // for_each<op> materialising every owned element's adjacency
+    // (Query::dispatch, query.h:21-75), CSR in linear ids.
+    QueryResult query(Op op, cudaStream_t s = nullptr) const
+    {
+        QueryResult r;
+        int64_t     nval = 0;
+        check(rxg_query_size(handle(), (int32_t)op, &r.rows, &nval));
+        const bool csr = op == Op::VV || op == Op::VE || op == Op::VF;
+        if (csr) r.offsets.resize((size_t)r.rows + 1);
+        r.values.resize((size_t)nval);
+        check(rxg_query(handle(), (int32_t)op, csr ? r.offsets.data() : nullptr, r.values.data(), s));
+        return r;
+    }
+
+    // oriented one-ring (rxmesh_queries.cuh:376-499): offsets, values, boundary flag
+    void query_oriented_vv(DeviceArray<int32_t>& off, DeviceArray<int32_t>& val,
+                           DeviceArray<int8_t>& bnd, cudaStream_t s = nullptr) const
+    {
+        off.resize((size_t)m_info.num_vertices + 1);
+        val.resize((size_t)(2 * m_info.num_edges));
+        bnd.resize((size_t)m_info.num_vertices);
+        check(rxg_query_oriented_vv(handle(), off.data(), val.data(), bnd.data(), s));
+    }
+
+    // vertex normals of linear-order FP32 positions (compute_vertex_normal,
+    // apps/VertexNormal/vertex_normal_kernel.cuh)
+    void compute_vertex_normal(const DenseMatrix<float>& xyz, DenseMatrix<float>& out,
+                               int32_t weighting = RXG_NORMAL_MAX, cudaStream_t s = nullptr) const
+    {
+        check(rxg_vertex_normals(handle(), weighting, xyz.data(), out.data(), s));
+    }
+
+   private:
+    struct Del
+    {
+        void operator()(rxg_mesh* m) const { rxg_mesh_destroy(m); }
+    };
+    std::unique_ptr<rxg_mesh, Del> m_mesh;
+    rxg_mesh_info                  m_info{};
+    DenseMatrix<double>            m_xyz;
+};
+
+// CSR over linear vertex ids with the [diagonal, one-ring] pattern of the
+// mesh (SparseMatrix<T>(rx), sparse_matrix.h:77).
+template <typename T>
+class SparseMatrix
+{
+   public:
+    explicit SparseMatrix(const RXMeshStatic& rx)
+    {
+        int64_t n = 0, nnz = 0;
+        check(rxg_mcf_pattern_size(rx.handle(), &n, &nnz));
+        m_n = n;
+        m_row_ptr.resize((size_t)n + 1);
+        m_col.resize((size_t)nnz);
+        m_val.resize((size_t)nnz);
+        m_row_ptr.fill_zero();
+        m_col.fill_zero();
+        m_val.fill_zero();
+        check_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
+    }
+    int64_t rows() const { return m_n; }
+    int64_t cols() const { return m_n; }
+    int64_t non_zeros() const { return (int64_t)m_col.size(); }
+    rxg_csr csr()
+    {
+        rxg_csr c;
+        c.n       = m_n;
+        c.nnz     = (int64_t)m_col.size();
+        c.row_ptr = m_row_ptr.data();
+        c.col     = m_col.data();
+        c.val     = m_val.data();
+        c.dtype   = dtype_of<T>::value;
+        return c;
+    }
+    // Y = A X (sparse_matrix.h:1173-1263)
+    void multiply(const DenseMatrix<T>& X, DenseMatrix<T>& Y, cudaStream_t s = nullptr)
+    {
+        rxg_csr c = csr();
+        check(rxg_spmm(&c, (int32_t)X.cols(), X.data(), Y.data(), s));
+    }
+    DeviceArray<int32_t>& row_ptr() { return m_row_ptr; }
+    DeviceArray<int32_t>& col_idx() { return m_col; }
+    DeviceArray<T>&       values() { return m_val; }
+
+   private:
+    int64_t              m_n = 0;
+    DeviceArray<int32_t> m_row_ptr, m_col;
+    DeviceArray<T>       m_val;
+};
+
+// (A, B) of the implicit MCF system at linear-order positions xyz
+// (mcf_A_setup / mcf_B_setup, apps/MCF/mcf_kernels.cuh:302-426)
+template <typename T>
+inline void mcf_assemble(const RXMeshStatic& rx, double dt, const DenseMatrix<double>& xyz,
+                         SparseMatrix<T>& A, DenseMatrix<T>& B, cudaStream_t s = nullptr)
+{
+    rxg_csr c = A.csr();
+    check(rxg_mcf_assemble(rx.handle(), dt, xyz.data(), &c, B.data(), s));
+}
+
+// CG (cg_solver.h:17-130); PCG adds the Jacobi preconditioner
+// (pcg_solver.h:14-213).  pre_solve is folded into solve, which runs the whole
+// solve in one device launch.
+template <typename T>
+struct CGSolver
+{
+    CGSolver(SparseMatrix<T>& sys, int unknown_dim, int max_iter, T abs_tol = 1e-6, T rel_tol = 0.0)
+        : A(&sys), m_nc(unknown_dim), m_max_iter(max_iter), m_abs_tol(abs_tol), m_rel_tol(rel_tol)
+    {
+    }
+    virtual ~CGSolver() = default;
+    virtual void pre_solve(const DenseMatrix<T>&, DenseMatrix<T>&, cudaStream_t = nullptr) {}
+    virtual void solve(const DenseMatrix<T>& B, DenseMatrix<T>& X, cudaStream_t s = nullptr)
+    {
+        rxg_solver_opts o;
+        o.max_iter   = m_max_iter;
+        o.abs_tol    = (double)m_abs_tol;
+        o.rel_tol    = (double)m_rel_tol;
+        o.precond    = precond();
+        rxg_csr    c = A->csr();
+        rxg_status st = rxg_cg_solve(&c, m_nc, B.data(), X.data(), &o, &m_stats, s);
+        if (st != RXG_ERR_NOT_CONVERGED) check(st);
+    }
+    virtual std::string name() { return "CG"; }
+    int                 iter_taken() const { return m_stats.iters; }
+    T                   start_residual() const { return (T)m_stats.start_res; }
+    T                   final_residual() const { return (T)m_stats.final_res; }
+    bool                converged() const { return m_stats.converged != 0; }
+
+   protected:
+    virtual int32_t  precond() const { return 0; }
+    SparseMatrix<T>* A;
+    int              m_nc, m_max_iter;
+    T                m_abs_tol, m_rel_tol;
+    rxg_solver_stats m_stats{};
+};
+
+template <typename T>
+struct PCGSolver : public CGSolver<T>
+{
+    using CGSolver<T>::CGSolver;
+    std::string name() override { return "PCG"; }
+
+   protected:
+    int32_t precond() const override { return 1; }
+};
+
+// nsteps implicit MCF steps in place on linear-order FP64 positions
+// (run_cg of apps/MCF/mcf_cg.h:12-129); precision RXG_F64 (plain) or
+// RXG_F32 (FP32 inner solves with FP64 refinement).
+inline rxg_solver_stats mcf_step(const RXMeshStatic& rx, DenseMatrix<double>& xyz, double dt,
+                                 int32_t nsteps = 1, int32_t precision = RXG_F64,
+                                 double tol = 1e-6, int32_t max_iter = 5000,
+                                 cudaStream_t s = nullptr)
+{
+    rxg_solver_stats st{};
+    rxg_status       r =
+        rxg_mcf_step(rx.handle(), dt, nsteps, precision, tol, max_iter, xyz.data(), &st, s);
+    if (r != RXG_ERR_NOT_CONVERGED) check(r);
+    return st;
+}
+
+// dl/dx_in of one plain implicit MCF step given dl/dx_out (adjoint solve
+// with the same matrix); FP64, linear order.
+inline rxg_solver_stats mcf_step_backward(const RXMeshStatic& rx, double dt,
+                                          const DenseMatrix<double>& x_in,
+                                          const DenseMatrix<double>& x_out,
+                                          const DenseMatrix<double>& g_out,
+                                          DenseMatrix<double>& g_in, double tol = 1e-12,
+                                          int32_t max_iter = 20000, cudaStream_t s = nullptr)
+{
+    rxg_solver_stats st{};
+    rxg_status       r = rxg_mcf_step_backward(rx.handle(), dt, x_in.data(), x_out.data(),
+                                               g_out.data(), g_in.data(), tol, max_iter, &st, s);
+    if (r != RXG_ERR_NOT_CONVERGED) check(r);
+    return st;
+}
+
+// 3x3-block CSR over the [diagonal, one-ring] pattern (HessianSparseMatrix,
+// diff/hessian_sparse_matrix.h:16-137)
+template <typename T>
+class BlockSparseMatrix
+{
+   public:
+    BlockSparseMatrix(int64_t n, int64_t nnzb) : m_n(n), m_row_ptr(n + 1), m_col(nnzb), m_val(9 * nnzb)
+    {
+    }
+    rxg_bcsr bcsr()
+    {
+        rxg_bcsr b;
+        b.n       = m_n;
+        b.nnzb    = (int64_t)m_col.size();
+        b.row_ptr = m_row_ptr.data();
+        b.col     = m_col.data();
+        b.val     = m_val.data();
+        b.dtype   = dtype_of<T>::value;
+        return b;
+    }
+    int64_t               rows() const { return m_n; }
+    int64_t               non_zero_blocks() const { return (int64_t)m_col.size(); }
+    DeviceArray<int32_t>& row_ptr() { return m_row_ptr; }
+    DeviceArray<int32_t>& col_idx() { return m_col; }
+    DeviceArray<T>&       values() { return m_val; }
+
+   private:
+    int64_t              m_n;
+    DeviceArray<int32_t> m_row_ptr, m_col;
+    DeviceArray<T>       m_val;
+};
+
+// Energy / gradient / Hessian driver for the per-face ARAP term
+// (DiffScalarProblem<T, 3, VertexHandle, true>, diff_scalar_problem.h:27-401;
+// the reference takes a user lambda per face, which a C ABI cannot carry, so
+// the term is fixed: add_arap_term(rest positions)).
+template <typename T>
+class DiffScalarProblem
+{
+   public:
+    explicit DiffScalarProblem(const RXMeshStatic& rx, bool assemble_hessian = true) : m_rx(&rx)
+    {
+        int64_t n = 0, nnz = 0;
+        check(rxg_mcf_pattern_size(rx.handle(), &n, &nnz));
+        grad = DenseMatrix<T>(n, 3);
+        face_energy.resize(rx.get_num_faces());
+        if (assemble_hessian) hess.reset(new BlockSparseMatrix<T>(n, nnz));
+    }
+    // rest: linear-order FP64 positions of the flat rest shape
+    void add_arap_term(const DenseMatrix<double>& rest, cudaStream_t s = nullptr)
+    {
+        m_rest.resize(4 * (size_t)m_rx->get_num_faces());
+        check(rxg_arap_rest(m_rx->handle(), rest.data(), dtype_of<T>::value, m_rest.data(), s));
+    }
+    // evaluate at linear-order positions x (eval_terms, diff_scalar_problem.h:310-321)
+    void eval_terms(const DenseMatrix<T>& x, cudaStream_t s = nullptr)
+    {
+        if (!m_rest.size()) throw Error(RXG_ERR_INVALID, "add_arap_term() first");
+        rxg_bcsr  b  = hess ? hess->bcsr() : rxg_bcsr{};
+        check(rxg_arap_eval(m_rx->handle(), dtype_of<T>::value, x.data(), m_rest.data(), &m_loss,
+                            face_energy.data(), grad.data(), hess ? &b : nullptr, s));
+    }
+    T get_current_loss() const { return (T)m_loss; }
+
+    DenseMatrix<T>                        grad;
+    DeviceArray<T>                        face_energy;
+    std::unique_ptr<BlockSparseMatrix<T>> hess;
+
+   private:
+    const RXMeshStatic* m_rx;
+    DeviceArray<T>      m_rest;
+    double              m_loss = 0.0;
+};
+
+// Many meshes of uneven size, mixed-precision implicit MCF in one persistent
+// launch (graph-captured after the first call).
+class MeshBatch
+{
+   public:
+    // meshes: (fv, nv) per mesh, vertex ids local to the mesh
+    MeshBatch(const std::vector<std::pair<std::vector<int32_t>, int64_t>>& meshes,
+              int32_t                                                     patch_faces = 256)
+    {
+        std::vector<int32_t> fv;
+        std::vector<int64_t> nf, nv;
+        for (const auto& m : meshes) {
+            fv.insert(fv.end(), m.first.begin(), m.first.end());
+            nf.push_back((int64_t)m.first.size() / 3);
+            nv.push_back(m.second);
+            m_total_vertices += m.second;
+        }
+        rxg_batch* b = nullptr;
+        check(rxg_batch_create((int32_t)meshes.size(), fv.data(), nf.data(), nv.data(), patch_faces,
+                               &b));
+        m_b.reset(b);
+        m_n = (int32_t)meshes.size();
+    }
+    // xyz: all meshes' FP64 positions one after another, in input order
+    void mcf(DenseMatrix<double>& xyz, double dt, int32_t nsteps = 1, double tol = 1e-6,
+             int32_t max_iter = 5000, cudaStream_t s = nullptr)
+    {
+        check(rxg_batch_mcf(m_b.get(), dt, nsteps, tol, max_iter, xyz.data(), s));
+    }
+    void stats(std::vector<int32_t>& iters, std::vector<int32_t>& converged) const
+    {
+        iters.resize((size_t)m_n);
+        converged.resize((size_t)m_n);
+        check(rxg_batch_stats(m_b.get(), iters.data(), converged.data()));
+    }
+    int32_t num_meshes() const { return m_n; }
+    int64_t num_vertices() const { return m_total_vertices; }
+
+   private:
+    struct Del
+    {
+        void operator()(rxg_batch* b) const { rxg_batch_destroy(b); }
+    };
+    std::unique_ptr<rxg_batch, Del> m_b;
+    int32_t                         m_n              = 0;
+    int64_t                         m_total_vertices = 0;
+};
+
+}  // namespace rxg
+
+#endif  // RXG_RXMESH_HPP

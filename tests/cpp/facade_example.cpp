@@ -1,0 +1,212 @@
+// C++ use of the rxg facade (include/rxg/rxmesh.hpp), written the way an
+// RXMesh application drives the same path: build an RXMeshStatic, run
+// queries, assemble the MCF system, solve it with PCGSolver, take MCF steps,
+// evaluate the ARAP term, and run a small batch.
+//
+//   facade_example host   -- mesh build and numbering only (no GPU needed)
+//   facade_example gpu    -- the whole path on the current GPU
+// Prints "OK" and exits 0 when every check passes; prints the failing check
+// and exits 1 otherwise.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <set>
+#include <vector>
+
+#include "rxg/rxmesh.hpp"
+
+using namespace rxg;
+
+#define REQUIRE(c)                                                 \
+    do {                                                           \
+        if (!(c)) {                                                \
+            std::printf("FAILED: %s (line %d)\n", #c, __LINE__);   \
+            return 1;                                              \
+        }                                                          \
+    } while (0)
+
+// closed torus on an n x m (u, v) grid, two triangles per cell
+static void torus(int n, int m, std::vector<std::vector<uint32_t>>& fv,
+                  std::vector<std::vector<double>>& xyz)
+{
+    const double R = 1.0, r = 0.3, pi = 3.14159265358979323846;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < m; ++j) {
+            const double u = 2 * pi * i / n, v = 2 * pi * j / m;
+            xyz.push_back({(R + r * std::cos(v)) * std::cos(u), (R + r * std::cos(v)) * std::sin(u),
+                           r * std::sin(v)});
+            const uint32_t a = i * m + j, b = ((i + 1) % n) * m + j, c = ((i + 1) % n) * m + (j + 1) % m,
+                           d = i * m + (j + 1) % m;
+            fv.push_back({a, b, c});
+            fv.push_back({a, c, d});
+        }
+}
+
+// open k x k grid in the plane z = 0, spacing 1
+static void grid(int k, std::vector<int32_t>& fv, std::vector<double>& xyz)
+{
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < k; ++j) {
+            xyz.push_back(j);
+            xyz.push_back(i);
+            xyz.push_back(0.0);
+        }
+    for (int i = 0; i + 1 < k; ++i)
+        for (int j = 0; j + 1 < k; ++j) {
+            const int a = i * k + j, b = a + 1, c = a + k + 1, d = a + k;
+            const int t[6] = {a, b, c, a, c, d};
+            fv.insert(fv.end(), t, t + 6);
+        }
+}
+
+static int host_checks()
+{
+    std::vector<std::vector<uint32_t>> fv;
+    std::vector<std::vector<double>>   xyz;
+    torus(48, 32, fv, xyz);
+    RXMeshStatic rx(fv, "", 128, /*host_only=*/true);
+    REQUIRE(rx.get_num_vertices() == 48 * 32);
+    REQUIRE(rx.get_num_faces() == 2 * 48 * 32);
+    REQUIRE(rx.get_num_edges() == 3 * 48 * 32);
+    REQUIRE(rx.is_closed() && rx.is_edge_manifold());
+    REQUIRE(rx.get_num_patches() >= 24);
+    const std::vector<int32_t> l2i = rx.linear_to_input(RXG_ELEM_VERTEX);
+    std::set<int32_t>          seen(l2i.begin(), l2i.end());
+    REQUIRE(seen.size() == l2i.size() && *seen.begin() == 0);
+    bool threw = false;
+    try {
+        std::vector<std::vector<uint32_t>> bad = {{0, 1}};
+        RXMeshStatic                       r2(bad, "", 128, true);
+    } catch (const Error& e) {
+        threw = e.status == RXG_ERR_INVALID;
+    }
+    REQUIRE(threw);
+    return 0;
+}
+
+static int gpu_checks()
+{
+    std::vector<std::vector<uint32_t>> fv;
+    std::vector<std::vector<double>>   xyz;
+    torus(96, 64, fv, xyz);
+    RXMeshStatic rx(fv);
+    rx.add_vertex_coordinates(xyz);
+    const uint32_t nv = rx.get_num_vertices();
+    const std::vector<int32_t> vl2i = rx.linear_to_input(RXG_ELEM_VERTEX);
+
+    // VV: every torus vertex has valence 6 and adjacency is symmetric
+    QueryResult                vv  = rx.query(Op::VV);
+    const std::vector<int32_t> off = vv.offsets.to_host(), val = vv.values.to_host();
+    REQUIRE((int64_t)off.size() == nv + 1);
+    std::set<std::pair<int32_t, int32_t>> adj;
+    for (uint32_t v = 0; v < nv; ++v) {
+        REQUIRE(off[v + 1] - off[v] == 6);
+        for (int32_t k = off[v]; k < off[v + 1]; ++k) adj.insert({(int32_t)v, val[k]});
+    }
+    for (const auto& e : adj) REQUIRE(adj.count({e.second, e.first}) == 1);
+
+    // FV maps back to the input faces (up to rotation)
+    QueryResult                fvq  = rx.query(Op::FV);
+    const std::vector<int32_t> fval = fvq.values.to_host();
+    const std::vector<int32_t> fl2i = rx.linear_to_input(RXG_ELEM_FACE);
+    for (size_t f = 0; f < fl2i.size(); ++f) {
+        const auto& in = fv[(size_t)fl2i[f]];
+        int         a = vl2i[fval[3 * f]], b = vl2i[fval[3 * f + 1]], c = vl2i[fval[3 * f + 2]];
+        bool        same = false;
+        for (int r = 0; r < 3; ++r) {
+            same |= (int)in[r] == a && (int)in[(r + 1) % 3] == b && (int)in[(r + 2) % 3] == c;
+        }
+        REQUIRE(same);
+    }
+
+    // MCF system + Jacobi PCG: |A X - B| / |B| small
+    const double        dt = 1e-3;
+    SparseMatrix<double> A(rx);
+    DenseMatrix<double>  B(nv, 3), X(nv, 3), AX(nv, 3);
+    mcf_assemble(rx, dt, rx.get_input_vertex_coordinates(), A, B);
+    PCGSolver<double> solver(A, 3, 2000, 1e-20, 0.0);
+    solver.pre_solve(B, X);
+    solver.solve(B, X);
+    REQUIRE(solver.iter_taken() > 0 && solver.converged());
+    A.multiply(X, AX);
+    const std::vector<double> hb = B.to_host(), hax = AX.to_host();
+    double                    num = 0, den = 0;
+    for (size_t i = 0; i < hb.size(); ++i) {
+        num += (hax[i] - hb[i]) * (hax[i] - hb[i]);
+        den += hb[i] * hb[i];
+    }
+    REQUIRE(std::sqrt(num / den) < 1e-8);
+
+    // mcf_step: plain FP64 against mixed precision
+    DenseMatrix<double> x64(nv, 3), x32(nv, 3);
+    const std::vector<double> x0 = rx.get_input_vertex_coordinates().to_host();
+    x64.from_host(x0);
+    x32.from_host(x0);
+    mcf_step(rx, x64, dt, 3, RXG_F64, 1e-8);
+    mcf_step(rx, x32, dt, 3, RXG_F32, 1e-8);
+    const std::vector<double> h64 = x64.to_host(), h32 = x32.to_host();
+    num = den = 0;
+    for (size_t i = 0; i < h64.size(); ++i) {
+        num += (h64[i] - h32[i]) * (h64[i] - h32[i]);
+        den += h64[i] * h64[i];
+    }
+    REQUIRE(std::sqrt(num / den) < 1e-6);
+
+    // ARAP: zero energy and gradient at rest, positive after a stretch
+    std::vector<int32_t> gfv;
+    std::vector<double>  gx;
+    grid(24, gfv, gx);
+    std::vector<std::vector<uint32_t>> gf;
+    for (size_t t = 0; t < gfv.size(); t += 3)
+        gf.push_back({(uint32_t)gfv[t], (uint32_t)gfv[t + 1], (uint32_t)gfv[t + 2]});
+    RXMeshStatic gr(gf);
+    std::vector<std::vector<double>> gxyz;
+    for (size_t i = 0; i < gx.size(); i += 3) gxyz.push_back({gx[i], gx[i + 1], gx[i + 2]});
+    gr.add_vertex_coordinates(gxyz);
+    DiffScalarProblem<double> prob(gr);
+    prob.add_arap_term(gr.get_input_vertex_coordinates());
+    prob.eval_terms(gr.get_input_vertex_coordinates());
+    REQUIRE(std::fabs(prob.get_current_loss()) < 1e-12);
+    const std::vector<double> g0 = prob.grad.to_host();
+    for (double g : g0) REQUIRE(std::fabs(g) < 1e-10);
+    std::vector<double> stretched = gr.get_input_vertex_coordinates().to_host();
+    for (size_t i = 0; i < stretched.size(); i += 3) stretched[i] *= 1.1;
+    DenseMatrix<double> xs(gr.get_num_vertices(), 3);
+    xs.from_host(stretched);
+    prob.eval_terms(xs);
+    REQUIRE(prob.get_current_loss() > 1e-3);
+    REQUIRE(prob.hess && prob.hess->non_zero_blocks() > 0);
+
+    // batch: two meshes, one launch
+    std::vector<int32_t> t1;
+    for (const auto& f : fv)
+        for (uint32_t v : f) t1.push_back((int32_t)v);
+    std::vector<std::pair<std::vector<int32_t>, int64_t>> meshes = {{t1, (int64_t)nv},
+                                                                    {gfv, (int64_t)gxyz.size()}};
+    MeshBatch batch(meshes);
+    std::vector<double> bx;
+    for (const auto& p : xyz) bx.insert(bx.end(), p.begin(), p.end());
+    bx.insert(bx.end(), gx.begin(), gx.end());
+    DenseMatrix<double> dbx((int64_t)bx.size() / 3, 3);
+    dbx.from_host(bx);
+    batch.mcf(dbx, dt, 2, 1e-6);
+    std::vector<int32_t> iters, conv;
+    batch.stats(iters, conv);
+    REQUIRE(iters.size() == 2 && conv[0] && conv[1]);
+    return 0;
+}
+
+int main(int argc, char** argv)
+{
+    const bool gpu = argc > 1 && std::strcmp(argv[1], "gpu") == 0;
+    try {
+        const int rc = gpu ? gpu_checks() : host_checks();
+        if (rc) return rc;
+    } catch (const Error& e) {
+        std::printf("FAILED: exception %s\n", e.what());
+        return 1;
+    }
+    std::printf("OK\n");
+    return 0;
+}
