@@ -17,6 +17,7 @@
 #include <numeric>
 #include <vector>
 
+#include "rxg_gridsum.cuh"
 #include "rxg_lazy.h"
 #include "rxg_mcf_common.cuh"
 
@@ -150,11 +151,22 @@ __device__ __forceinline__ double residual(int64_t v0, int64_t v1, const BatchAr
     return block_sum<BT>(part, s_red);
 }
 
+// scalar state of a CTA's inner PCG: the FP64 recurrence is touched by
+// thread 0 only; every thread reads the FP32 step sizes and the flag
+struct BatchPCG
+{
+    double delta0, delta;
+    int    it;
+    float  al, bt;
+    int    done;
+};
+
 // block-level Jacobi-PCG for A D = R (R is overwritten as the residual);
-// returns the iterations completed
+// returns the iterations completed.  Dot products: FP32 per thread and
+// warp, FP64 per CTA (rxg_gridsum.cuh).
 template <int BT>
 __device__ int inner_pcg(int64_t v0, int64_t v1, const BatchArgs& a, double rel2, int max_it,
-                         double* s_red)
+                         RedSmem& red, BatchPCG& c)
 {
     float tp = 0.f;
     for (int64_t i = v0 + threadIdx.x; i < v1; i += BT) {
@@ -169,12 +181,13 @@ __device__ int inner_pcg(int64_t v0, int64_t v1, const BatchArgs& a, double rel2
         a.D[i] = zero;
         tp += r.x * z.x + r.y * z.y + r.z * z.z;
     }
-    double       delta  = block_sum<BT>((double)tp, s_red);
-    const double delta0 = delta;
-    int          it     = 0;
-    if (!(delta0 > 0)) return 0;
-    while (it < max_it) {
-        // S = A P, P.S   (block_sum's barriers order P before the gathers)
+    block_sum_post<BT>(tp, red, [&](double t) {
+        c.delta0 = c.delta = t;
+        c.it               = 0;
+        c.done             = !(t > 0) || max_it <= 0;
+    });
+    while (!c.done) {
+        // S = A P, P.S   (the block barriers order P before the gathers)
         tp = 0.f;
         for (int64_t i = v0 + threadIdx.x; i < v1; i += BT) {
             float ax = 0, ay = 0, az = 0;
@@ -185,7 +198,8 @@ __device__ int inner_pcg(int64_t v0, int64_t v1, const BatchArgs& a, double rel2
             const R4<float> p = a.P[i];
             tp += s.x * p.x + s.y * p.y + s.z * p.z;
         }
-        const float al = (float)(delta / block_sum<BT>((double)tp, s_red));
+        block_sum_post<BT>(tp, red, [&](double sp) { c.al = (float)(c.delta / sp); });
+        const float al = c.al;
         tp             = 0.f;
         for (int64_t i = v0 + threadIdx.x; i < v1; i += BT) {
             const float     di = a.dinv[i];
@@ -199,10 +213,18 @@ __device__ int inner_pcg(int64_t v0, int64_t v1, const BatchArgs& a, double rel2
             a.Z[i] = z;
             tp += r.x * z.x + r.y * z.y + r.z * z.z;
         }
-        const double dn = block_sum<BT>((double)tp, s_red);
-        if (dn < rel2 * delta0) break;
-        const float bt = (float)(dn / delta);
-        delta          = dn;
+        block_sum_post<BT>(tp, red, [&](double dn) {
+            if (dn < rel2 * c.delta0) {
+                c.done = 1;
+                return;
+            }
+            c.bt    = (float)(dn / c.delta);
+            c.delta = dn;
+            ++c.it;
+            c.done = c.it >= max_it;
+        });
+        if (c.done) break;
+        const float bt = c.bt;
         for (int64_t i = v0 + threadIdx.x; i < v1; i += BT) {
             const R4<float> z = a.Z[i];
             R4<float>       p = a.P[i];
@@ -210,16 +232,17 @@ __device__ int inner_pcg(int64_t v0, int64_t v1, const BatchArgs& a, double rel2
             a.P[i] = p;
         }
         __syncthreads();
-        ++it;
     }
-    return it;
+    return c.it;
 }
 
 template <int BT>
 __global__ void __launch_bounds__(BT) k_mcf_batch(BatchArgs a)
 {
-    __shared__ int    s_job;
-    __shared__ double s_red[BT / 32 + 2];
+    __shared__ int      s_job;
+    __shared__ double   s_red[BT / 32 + 2];
+    __shared__ RedSmem  red;
+    __shared__ BatchPCG pcg;
     while (true) {
         if (threadIdx.x == 0) s_job = atomicAdd(a.queue, 1);
         __syncthreads();
@@ -239,7 +262,7 @@ __global__ void __launch_bounds__(BT) k_mcf_batch(BatchArgs a)
             for (int sweep = 0; sweep < 16 && !conv && total_it < a.max_iter; ++sweep) {
                 const double need  = a.tol * sqrt(rr0 / rr);
                 const double inner = fmax(1e-4, 0.3 * need);
-                total_it += inner_pcg<BT>(v0, v1, a, inner * inner, a.max_iter - total_it, s_red) + 1;
+                total_it += inner_pcg<BT>(v0, v1, a, inner * inner, a.max_iter - total_it, red, pcg) + 1;
                 for (int64_t i = v0 + threadIdx.x; i < v1; i += BT) {
                     R4<double>      x = a.X[i];
                     const R4<float> d = a.D[i];

@@ -153,4 +153,65 @@ __device__ __forceinline__ void store_ints_aligned(int32_t* __restrict__ dst, in
     for (int32_t i = threadIdx.x; i < nv4; i += BT) d4[i] = s4[i];
 }
 
+// Write n values to global dst[gbase .. gbase+n) from 16-bit local ids in
+// shared memory (sbuf[j] <-> global (gbase & ~3) + j), each mapped to its
+// 32-bit id by map(): 8-byte shared loads and 16-byte global stores in the
+// aligned middle, scalar accesses at the ragged ends.  sbuf 8-byte aligned.
+template <int BT, typename Map>
+__device__ __forceinline__ void store_u16_mapped(int32_t* __restrict__ dst, int64_t gbase,
+                                                 const uint16_t* sbuf, int32_t n, const Map& map)
+{
+    const int64_t g_end = gbase + n;
+    const int64_t g0    = (gbase + 3) & ~int64_t(3);
+    const int64_t g1    = g_end & ~int64_t(3);
+    const int64_t sbase = gbase & ~int64_t(3);
+    if (g0 >= g1) {
+        for (int64_t g = gbase + threadIdx.x; g < g_end; g += BT) dst[g] = map(sbuf[g - sbase]);
+        return;
+    }
+    for (int64_t g = gbase + threadIdx.x; g < g0; g += BT) dst[g] = map(sbuf[g - sbase]);
+    for (int64_t g = g1 + threadIdx.x; g < g_end; g += BT) dst[g] = map(sbuf[g - sbase]);
+    const int32_t nv4 = (int32_t)((g1 - g0) >> 2);
+    const uint2*  s4  = reinterpret_cast<const uint2*>(sbuf + (g0 - sbase));
+    int4*         d4  = reinterpret_cast<int4*>(dst + g0);
+    for (int32_t i = threadIdx.x; i < nv4; i += BT) {
+        const uint2 w = s4[i];
+        int4        o;
+        o.x   = map(w.x & 0xffffu);
+        o.y   = map(w.x >> 16);
+        o.z   = map(w.y & 0xffffu);
+        o.w   = map(w.y >> 16);
+        d4[i] = o;
+    }
+}
+
+// Bounded wait on phase `parity` of an mbarrier that suspends the thread
+// between attempts (try_wait with a time hint), so a waiting warp issues
+// almost nothing.  Same error reporting as mbar_wait_bounded.
+__device__ __forceinline__ bool mbar_try_wait_hint(uint64_t* bar, uint32_t parity, uint32_t ns)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(ns)
+        : "memory");
+    return ok != 0;
+}
+
+constexpr uint32_t kHintNs         = 20000;  // 20 us per attempt
+constexpr uint32_t kHintedAttempts = 25000;  // ~0.5 s in all
+
+__device__ __forceinline__ bool mbar_wait_hinted(uint64_t* bar, uint32_t parity, int* err)
+{
+    for (uint32_t i = 0; i < kHintedAttempts; ++i)
+        if (mbar_try_wait_hint(bar, parity, kHintNs)) return true;
+    if (err) atomicOr(err, DEVERR_MBAR_TIMEOUT);
+    for (uint32_t i = 0; i < kHintedAttempts; ++i)
+        if (mbar_try_wait_hint(bar, parity, kHintNs)) break;
+    return false;
+}
+
 }  // namespace rxg

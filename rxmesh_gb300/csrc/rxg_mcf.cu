@@ -9,6 +9,7 @@
 
 #include "rxg_device.cuh"
 #include "rxg_lazy.h"
+#include "rxg_gridsum.cuh"
 #include "rxg_mcf_common.cuh"
 
 namespace rxg {
@@ -42,6 +43,7 @@ void lazy_free(Mesh* m)
     cudaFree(z->row_ptr);
     cudaFree(z->col);
     cudaFree(z->buf);
+    cudaFree(z->d_oc_bounds);
     delete z;
     m->lazy = nullptr;
 }
@@ -536,64 +538,82 @@ __device__ __forceinline__ void row_spmv(const int32_t* __restrict__ rp, const i
     }
 }
 
+// scalar recurrence of k_cgm, in shared memory, touched by thread 0 only
+struct CGMScalars
+{
+    double delta0, delta, beta;
+    int    it;
+    bool   conv;
+};
+
+// per-thread partial -> grid sum: FP32 partials reduce in FP32 per warp,
+// FP64 ones are staged and summed by warp 0 (rxg_gridsum.cuh)
+template <int BT, typename Post>
+__device__ __forceinline__ bool cgm_sum(float v, double*, GridSum& g, RedSmem& r, Post post)
+{
+    return grid_sum<BT>(v, g, r, post);
+}
+template <int BT, typename Post>
+__device__ __forceinline__ bool cgm_sum(double v, double* s_part, GridSum& g, RedSmem& r, Post post)
+{
+    return grid_sum_staged<BT>(v, s_part, g, r, post);
+}
+
 template <typename T, int NC, bool PC, int kCGT>
 __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
 {
-    __shared__ double s_red[kCGT / 32 + 2];
-    __shared__ int    s_ok;
-    const unsigned G     = gridDim.x;
-    const int64_t  chunk = (a.n + G - 1) / G;
-    const int64_t  r0    = blockIdx.x * chunk;
-    const int64_t  r1    = min(a.n, r0 + chunk);
-    T* const       src   = PC ? a.Z : a.R;  // vector the direction is built from
-    unsigned       kred  = 0;               // reductions done so far
+    __shared__ RedSmem    red;
+    __shared__ double     s_part[sizeof(T) == 8 ? kCGT : 1];
+    __shared__ CGMScalars c;
+    __shared__ T          s_al, s_bt;
+    __shared__ int        s_first, s_done;
+    const int64_t chunk = (a.n + gridDim.x - 1) / gridDim.x;
+    const int64_t r0    = blockIdx.x * chunk;
+    const int64_t r1    = min(a.n, r0 + chunk);
+    T* const      src   = PC ? a.Z : a.R;  // vector the direction is built from
+    GridSum       g{a.bar, a.part, a.err, gridDim.x, 0u};
+    auto          conv = [&](double d) { return d < a.abs_tol || d / c.delta0 < a.rel_tol; };
     // Per-thread partial dot products stay in T over the thread's few rows;
-    // the block and grid reductions are in FP64.
+    // the block and grid reductions are in FP64, and the scalar recurrence
+    // runs on thread 0 (rxg_gridsum.cuh).
 
     // ---- pre_solve: S = A X, R = B - S, Z = D^-1 R, delta = R.Z (or R.R)
     T tpart = T(0);
     for (int64_t i = r0 + threadIdx.x; i < r1; i += kCGT) {
         T acc[NC];
 #pragma unroll
-        for (int c = 0; c < NC; ++c) acc[c] = T(0);
+        for (int k = 0; k < NC; ++k) acc[k] = T(0);
         T diag = T(0);
         row_spmv<T, NC>(a.rp, a.col, a.val, i, a.X, acc, &diag);
         const T di = T(1) / (diag + (sizeof(T) == 4 ? (T)FLT_EPSILON : (T)DBL_EPSILON));
         if (PC) a.dinv[i] = di;
 #pragma unroll
-        for (int c = 0; c < NC; ++c) {
-            const T r       = a.B[i * NC + c] - acc[c];
-            a.R[i * NC + c] = r;
+        for (int k = 0; k < NC; ++k) {
+            const T r       = a.B[i * NC + k] - acc[k];
+            a.R[i * NC + k] = r;
             if (PC) {
                 const T z       = di * r;
-                a.Z[i * NC + c] = z;
+                a.Z[i * NC + k] = z;
                 tpart += r * z;
             } else {
                 tpart += r * r;
             }
         }
     }
-    double delta0;
-    if (!grid_reduce(block_sum<kCGT>((double)tpart, s_red), a.part, a.bar, G, kred++, a.err, s_red,
-                     &s_ok, &delta0))
+    if (!cgm_sum<kCGT>(tpart, s_part, g, red, [&](double t) {
+            c.delta0 = c.delta = t;
+            c.beta             = 0.0;
+            c.it               = 0;
+            c.conv             = conv(t);
+            s_bt               = T(0);
+            s_first            = 1;
+            s_done             = c.conv || a.max_iter <= 0;
+        }))
         return;
-    double delta = delta0;
-    auto   conv  = [&](double d) { return d < a.abs_tol || d / delta0 < a.rel_tol; };
-    if (conv(delta0)) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            a.dstat[0] = delta0;
-            a.dstat[1] = delta0;
-            a.istat[0] = 0;
-            a.istat[1] = 1;
-        }
-        return;
-    }
-    double   beta = 0;
-    int      it   = 0;
-    bool     done = false;
-    T* const P    = a.P0;
-    while (it < a.max_iter) {
-        const T bt = (T)beta;
+    T* const P = a.P0;
+    while (!s_done) {
+        const T    bt    = s_bt;
+        const bool first = s_first != 0;
         // ---- phase A: S = A src + beta S (= A p by linearity), p = src + beta p,
         //      S.p.  Only own rows of S and p are read back, so the p update
         //      needs neither extra work per non-zero nor another barrier.
@@ -601,58 +621,58 @@ __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
         for (int64_t i = r0 + threadIdx.x; i < r1; i += kCGT) {
             T acc[NC];
 #pragma unroll
-            for (int c = 0; c < NC; ++c) acc[c] = T(0);
+            for (int k = 0; k < NC; ++k) acc[k] = T(0);
             row_spmv<T, NC>(a.rp, a.col, a.val, i, src, acc, (T*)nullptr);
 #pragma unroll
-            for (int c = 0; c < NC; ++c) {
-                const T si = it == 0 ? acc[c] : acc[c] + bt * a.S[i * NC + c];
-                const T pi = it == 0 ? src[i * NC + c] : src[i * NC + c] + bt * P[i * NC + c];
-                P[i * NC + c]   = pi;
-                a.S[i * NC + c] = si;
+            for (int k = 0; k < NC; ++k) {
+                const T si = first ? acc[k] : acc[k] + bt * a.S[i * NC + k];
+                const T pi = first ? src[i * NC + k] : src[i * NC + k] + bt * P[i * NC + k];
+                P[i * NC + k]   = pi;
+                a.S[i * NC + k] = si;
                 tpart += si * pi;
             }
         }
-        double sp;
-        if (!grid_reduce(block_sum<kCGT>((double)tpart, s_red), a.part, a.bar, G, kred++, a.err,
-                         s_red, &s_ok, &sp))
-            return;
-        const T al = (T)(delta / sp);
+        if (!cgm_sum<kCGT>(tpart, s_part, g, red, [&](double sp) { s_al = (T)(c.delta / sp); })) return;
+        const T al = s_al;
         // ---- phase B: X += alpha p, R -= alpha S, Z = D^-1 R, delta' = R.Z
         tpart = T(0);
         for (int64_t i = r0 + threadIdx.x; i < r1; i += kCGT) {
             const T di = PC ? a.dinv[i] : T(1);
 #pragma unroll
-            for (int c = 0; c < NC; ++c) {
-                a.X[i * NC + c] += al * P[i * NC + c];
-                const T r       = a.R[i * NC + c] - al * a.S[i * NC + c];
-                a.R[i * NC + c] = r;
+            for (int k = 0; k < NC; ++k) {
+                a.X[i * NC + k] += al * P[i * NC + k];
+                const T r       = a.R[i * NC + k] - al * a.S[i * NC + k];
+                a.R[i * NC + k] = r;
                 if (PC) {
                     const T z       = di * r;
-                    a.Z[i * NC + c] = z;
+                    a.Z[i * NC + k] = z;
                     tpart += r * z;
                 } else {
                     tpart += r * r;
                 }
             }
         }
-        double dn;
-        if (!grid_reduce(block_sum<kCGT>((double)tpart, s_red), a.part, a.bar, G, kred++, a.err,
-                         s_red, &s_ok, &dn))
+        if (!cgm_sum<kCGT>(tpart, s_part, g, red, [&](double dn) {
+                if (conv(dn)) {
+                    c.delta = dn;
+                    c.conv  = true;
+                    s_done  = 1;
+                    return;
+                }
+                c.beta  = dn / c.delta;
+                c.delta = dn;
+                ++c.it;
+                s_bt    = (T)c.beta;
+                s_first = 0;
+                s_done  = c.it >= a.max_iter;
+            }))
             return;
-        if (conv(dn)) {
-            delta = dn;
-            done  = true;
-            break;
-        }
-        beta  = dn / delta;
-        delta = dn;
-        ++it;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.dstat[0] = delta0;
-        a.dstat[1] = delta;
-        a.istat[0] = it;
-        a.istat[1] = done ? 1 : 0;
+        a.dstat[0] = c.delta0;
+        a.dstat[1] = c.delta;
+        a.istat[0] = c.it;
+        a.istat[1] = c.conv ? 1 : 0;
     }
 }
 
@@ -922,14 +942,17 @@ struct CGMArgs
 template <typename T, int kBT>
 __global__ void __launch_bounds__(kBT) k_cgm(CGMArgs<T> a)
 {
-    __shared__ double s_red[kBT / 32 + 2];
-    __shared__ int    s_ok;
-    const unsigned G     = gridDim.x;
-    const int64_t  chunk = (a.n + G - 1) / G;
-    const int64_t  r0    = blockIdx.x * chunk;
-    const int64_t  r1    = min(a.n, r0 + chunk);
-    unsigned       kred  = 0;
-    const T        eps   = sizeof(T) == 4 ? (T)FLT_EPSILON : (T)DBL_EPSILON;
+    __shared__ RedSmem    red;
+    __shared__ double     s_part[sizeof(T) == 8 ? kBT : 1];
+    __shared__ CGMScalars c;
+    __shared__ T          s_al, s_bt;
+    __shared__ int        s_first, s_done;
+    const int64_t chunk = (a.n + gridDim.x - 1) / gridDim.x;
+    const int64_t r0    = blockIdx.x * chunk;
+    const int64_t r1    = min(a.n, r0 + chunk);
+    const T       eps   = sizeof(T) == 4 ? (T)FLT_EPSILON : (T)DBL_EPSILON;
+    GridSum       g{a.bar, a.part, a.err, gridDim.x, 0u};
+    auto          conv = [&](double d) { return d < a.abs_tol || d / c.delta0 < a.rel_tol; };
 
     // ---- pre_solve: R = B - A X, Z = D^-1 R, delta = R.Z
     T tpart = T(0);
@@ -946,17 +969,19 @@ __global__ void __launch_bounds__(kBT) k_cgm(CGMArgs<T> a)
         a.Z[i]    = z;
         tpart += r.x * z.x + r.y * z.y + r.z * z.z;
     }
-    double delta0;
-    if (!grid_reduce(block_sum<kBT>((double)tpart, s_red), a.part, a.bar, G, kred++, a.err, s_red,
-                     &s_ok, &delta0))
+    if (!cgm_sum<kBT>(tpart, s_part, g, red, [&](double t) {
+            c.delta0 = c.delta = t;
+            c.beta             = 0.0;
+            c.it               = 0;
+            c.conv             = conv(t);
+            s_bt               = T(0);
+            s_first            = 1;
+            s_done             = c.conv || a.max_iter <= 0;
+        }))
         return;
-    double delta = delta0;
-    auto   conv  = [&](double d) { return d < a.abs_tol || d / delta0 < a.rel_tol; };
-    double beta  = 0;
-    int    it    = 0;
-    bool   done  = conv(delta0);
-    while (!done && it < a.max_iter) {
-        const T bt = (T)beta;
+    while (!s_done) {
+        const T    bt    = s_bt;
+        const bool first = s_first != 0;
         // ---- phase A: S = A z + beta S, p = z + beta p, S.p
         tpart = T(0);
         for (int64_t i = r0 + threadIdx.x; i < r1; i += kBT) {
@@ -964,7 +989,7 @@ __global__ void __launch_bounds__(kBT) k_cgm(CGMArgs<T> a)
             row_spmv4<T>(a.rp, a.ent, i, a.Z, ax, ay, az, (T*)nullptr);
             const R4<T> zi = a.Z[i];
             R4<T>       si, pi;
-            if (it == 0) {
+            if (first) {
                 si.x = ax, si.y = ay, si.z = az;
                 pi = zi;
             } else {
@@ -977,11 +1002,8 @@ __global__ void __launch_bounds__(kBT) k_cgm(CGMArgs<T> a)
             a.P[i] = pi;
             tpart += si.x * pi.x + si.y * pi.y + si.z * pi.z;
         }
-        double sp;
-        if (!grid_reduce(block_sum<kBT>((double)tpart, s_red), a.part, a.bar, G, kred++, a.err,
-                         s_red, &s_ok, &sp))
-            return;
-        const T al = (T)(delta / sp);
+        if (!cgm_sum<kBT>(tpart, s_part, g, red, [&](double sp) { s_al = (T)(c.delta / sp); })) return;
+        const T al = s_al;
         // ---- phase B: X += alpha p, R -= alpha S, Z = D^-1 R, R.Z
         tpart = T(0);
         for (int64_t i = r0 + threadIdx.x; i < r1; i += kBT) {
@@ -997,24 +1019,27 @@ __global__ void __launch_bounds__(kBT) k_cgm(CGMArgs<T> a)
             a.Z[i] = z;
             tpart += r.x * z.x + r.y * z.y + r.z * z.z;
         }
-        double dn;
-        if (!grid_reduce(block_sum<kBT>((double)tpart, s_red), a.part, a.bar, G, kred++, a.err,
-                         s_red, &s_ok, &dn))
+        if (!cgm_sum<kBT>(tpart, s_part, g, red, [&](double dn) {
+                if (conv(dn)) {
+                    c.delta = dn;
+                    c.conv  = true;
+                    s_done  = 1;
+                    return;
+                }
+                c.beta  = dn / c.delta;
+                c.delta = dn;
+                ++c.it;
+                s_bt    = (T)c.beta;
+                s_first = 0;
+                s_done  = c.it >= a.max_iter;
+            }))
             return;
-        if (conv(dn)) {
-            delta = dn;
-            done  = true;
-            break;
-        }
-        beta  = dn / delta;
-        delta = dn;
-        ++it;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.dstat[0] = delta0;
-        a.dstat[1] = delta;
-        a.istat[0] = it;
-        a.istat[1] = done ? 1 : 0;
+        a.dstat[0] = c.delta0;
+        a.dstat[1] = c.delta;
+        a.istat[0] = c.it;
+        a.istat[1] = c.conv ? 1 : 0;
     }
 }
 
@@ -1329,7 +1354,7 @@ template <typename T>
 static size_t cgm_scratch_bytes(int64_t n, int G)
 {
     return 4 * align256(sizeof(R4<T>) * n) + align256(sizeof(T) * n) +
-           align256(sizeof(double) * G) + 3 * 256;
+           align256(sizeof(double) * 2 * G) + 3 * 256;
 }
 
 template <typename T>
@@ -1351,7 +1376,7 @@ static rxg_status cgm_launch(int64_t n, const int32_t* rp, const Ent<T>* ent, co
     a.S = (R4<T>*)q, q += vb;
     a.Z = (R4<T>*)q, q += vb;
     a.dinv  = (T*)q, q += align256(sizeof(T) * n);
-    a.part  = (double*)q, q += align256(sizeof(double) * G);
+    a.part  = (double*)q, q += align256(sizeof(double) * 2 * G);
     a.bar   = (unsigned*)q, q += 256;
     a.dstat = (double*)q, q += 256;
     a.istat = (int*)q, q += 256;
@@ -1762,10 +1787,12 @@ rxg_status rxg_mcf_step(const rxg_mesh* h, double dt, int32_t nsteps, int32_t pr
     const size_t x4b = align256(sizeof(R4<double>) * n);
     const size_t plain = 2 * x4b + align256(sizeof(Ent<double>) * nnz) +
                          cgm_scratch_bytes<double>(n, cgm_grid<double>(n));
+    const int64_t max_row = h->m.max_valence + 1;  // diagonal + one-ring
     const size_t mixed = 2 * x4b + align256(sizeof(Ent<float>) * nnz) +
                          2 * align256(sizeof(R4<float>) * n) + align256(8 * Gr) + align256(8 * n) +
-                         std::max(cgm_scratch_bytes<float>(n, cgm_grid<float>(n)),
-                                  pipe_scratch_bytes<float>(n, pipe_grid<float>(n)));
+                         std::max({cgm_scratch_bytes<float>(n, cgm_grid<float>(n)),
+                                   pipe_scratch_bytes<float>(n, pipe_grid<float>(n)),
+                                   mcf_onchip_scratch_bytes(n, max_row)});
     {
         std::lock_guard<std::mutex> g(z->mu);
         if ((st = mcf_buffers(z, std::max(plain, mixed), s))) return st;
@@ -1782,8 +1809,9 @@ rxg_status rxg_mcf_step(const rxg_mesh* h, double dt, int32_t nsteps, int32_t pr
     R4<double>* X4 = (R4<double>*)q;
     R4<double>* B4 = (R4<double>*)(q + x4b);
     uint8_t*    p  = q + 2 * x4b;
-    rxg_solver_stats last = {0, 1, 0.0, 0.0};
-    const int        ga   = grid_for(n);
+    rxg_solver_stats last   = {0, 1, 0.0, 0.0};
+    const int        ga     = grid_for(n);
+    const bool       onchip = precision == RXG_F32 && !mixed_pipelined() && mcf_onchip_fits(n, max_row);
     k_pack3<<<ga, 256, 0, s>>>(n, X, X4);
     for (int step = 0; step < nsteps && st == RXG_OK; ++step) {
         // the assembly reads the caller-layout positions of this step
@@ -1811,6 +1839,12 @@ rxg_status rxg_mcf_step(const rxg_mesh* h, double dt, int32_t nsteps, int32_t pr
             k_mcf_assemble<float, GeoMixed, double><<<ga, 256, 0, s>>>(
                 n, z->row_ptr, z->col, z->bnd, X, (float)dt, PackedOut<float, double>{ent, B4, D64});
             RXG_CUDA_TRY(cudaGetLastError());
+            if (onchip) {
+                // whole refinement in one launch; statistics read after the last step
+                st = mcf_onchip_solve(z, n, max_row, ent, D64, B4, X4, r32, scr, tol, max_iter, s);
+                if (st == RXG_OK && step == nsteps - 1) st = mcf_onchip_stats(scr, &last, s);
+                continue;
+            }
             k_resid_mixed4<<<Gr, 256, 0, s>>>(n, z->row_ptr, ent, D64, X4, B4, r32, part);
             double rr0;
             if ((st = reduce_partials(part, Gr, s, &rr0))) break;
