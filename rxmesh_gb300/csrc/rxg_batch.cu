@@ -3,23 +3,64 @@
 // The meshes are packed into one union mesh whose patches never span two
 // components (RXG_MESH_SPLIT_COMPONENTS), so every mesh owns one contiguous
 // range of linear vertex ids (the reference packs several meshes into one
-// RXMeshStatic the same way, rxmesh_static.cu:66-160).  One CTA takes one
-// mesh from a work queue (largest first) and runs that mesh's whole
-// mixed-precision flow on its own: FP32 cotangent assembly (FP64 for
-// near-degenerate triangles), FP64 residual, FP32 Jacobi-PCG refinement
-// sweeps, all steps -- synchronising only with __syncthreads, so there are no
-// grid barriers and no host round trips, and the call can be captured in a
-// CUDA graph.
+// RXMeshStatic the same way, rxmesh_static.cu:66-160).
+//
+// Scheduling.  A mesh is a job for a gang of k CTAs, k = ceil(rows / tile),
+// so a 65 K-vertex grid is solved by 16 SMs while a 162-vertex sphere gets one
+// CTA.  The host builds a gang schedule once per (CTA shape, tile): jobs in
+// longest-first order each take the k CTAs that become free first (list
+// scheduling), and every CTA walks its own jobs in the order of their planned
+// start.  All CTAs share that one order, so a CTA can wait for the other
+// members of its gang without a deadlock; the launch is cooperative, so all
+// of them are resident.  A gang synchronises through its own ticket counter
+// (rxg_gridsum.cuh protocol with the gang's size), a one-CTA job only with
+// __syncthreads.
+//
+// Per job, all flow steps run inside the launch: FP32 cotangent assembly (FP64
+// for near-degenerate triangles and near-right Voronoi corners), FP64
+// residual, and one FP32 Jacobi-PCG per step with FP64 residual replacement
+// (the mixed solver of rxg_onchip.cu, here on global vectors).  No host round
+// trips, so the call can be captured in a CUDA graph.  rxg_batch_autotune
+// times the CTA size, CTAs per SM and the tile on the caller's batch.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <mutex>
 #include <numeric>
+#include <queue>
 #include <vector>
 
 #include "rxg_gridsum.cuh"
 #include "rxg_lazy.h"
 #include "rxg_mcf_common.cuh"
+
+namespace rxg {
+
+// one gang schedule (device arrays), built for a grid of G CTAs
+struct GangPlan
+{
+    int      G = 0, bt = 0, bps = 0, tile = 0, kmax = 1, njobs = 0;
+    int32_t* d_job_mesh  = nullptr;  // per job: mesh
+    int32_t* d_job_k     = nullptr;  // per job: CTAs in its gang
+    int32_t* d_cta_off   = nullptr;  // G+1: CTA b walks entries [off[b], off[b+1])
+    int32_t* d_cta_job   = nullptr;  // per entry: job
+    int32_t* d_cta_rank  = nullptr;  // per entry: rank of the CTA in the job's gang
+    unsigned* d_bar      = nullptr;  // 4 words per job (ticket, abort)
+    double*   d_part     = nullptr;  // 2 * kmax per job
+    void free_all()
+    {
+        cudaFree(d_job_mesh);
+        cudaFree(d_job_k);
+        cudaFree(d_cta_off);
+        cudaFree(d_cta_job);
+        cudaFree(d_cta_rank);
+        cudaFree(d_bar);
+        cudaFree(d_part);
+        *this = GangPlan();
+    }
+};
+
+}  // namespace rxg
 
 struct rxg_batch
 {
@@ -27,16 +68,16 @@ struct rxg_batch
     int32_t              nmesh = 0;
     std::vector<int64_t> voff, foff;       // input offsets per mesh (nmesh+1)
     std::vector<int32_t> vstart, vcount;   // linear vertex range per mesh
-    int32_t*             d_order  = nullptr;
     int32_t*             d_vstart = nullptr;
     int32_t*             d_vcount = nullptr;
-    int32_t*             d_queue  = nullptr;
     int32_t*             d_iters  = nullptr;
     int32_t*             d_conv   = nullptr;
     void*                buf      = nullptr;
     size_t               buf_size = 0;
     int32_t              threads  = 512;
-    int32_t              blocks_per_sm = 2;
+    int32_t              blocks_per_sm = 1;
+    int32_t              tile          = 4096;
+    rxg::GangPlan        plan;
     std::mutex           mu;
 };
 
@@ -44,18 +85,23 @@ namespace rxg {
 
 struct BatchArgs
 {
-    int32_t           nmesh;
-    const int32_t*    order;
     const int32_t*    vstart;
     const int32_t*    vcount;
-    int32_t*          queue;
+    const int32_t*    job_mesh;
+    const int32_t*    job_k;
+    const int32_t*    cta_off;
+    const int32_t*    cta_job;
+    const int32_t*    cta_rank;
+    unsigned*         bar;
+    double*           part;
+    int               kmax;
     const int32_t*    row_ptr;
     const int32_t*    col;
     const int8_t*     bnd;
-    Ent<float>*       ent;
+    int64_t           n;     // rows of the union (ELL slot stride)
+    Ent<float>*       ent;   // CSR entries (W = 0) or slot-major ELL of width W
     R4<double>*       X;
     R4<double>*       B;
-    R4<float>*        R;
     R4<float>*        P;
     R4<float>*        S;
     R4<float>*        Z;
@@ -68,6 +114,7 @@ struct BatchArgs
     int32_t           max_iter;
     int32_t*          iters;
     int32_t*          conv;
+    int*              err;
 };
 
 __device__ __forceinline__ V3<double> pos4(const R4<double>* X, int32_t i)
@@ -78,6 +125,14 @@ __device__ __forceinline__ V3<double> pos4(const R4<double>* X, int32_t i)
 
 // one row of the MCF system (mcf_A_setup / mcf_B_setup), FP32 weights with
 // FP64 for near-degenerate triangles, positions from the packed FP64 state
+// entry u of row p: CSR position row_ptr[p] + u, or ELL slot u
+template <int W>
+__device__ __forceinline__ int64_t ent_at(const BatchArgs& a, int64_t p, int32_t rp, int u)
+{
+    return W ? u * a.n + p : (int64_t)rp + u;
+}
+
+template <int W>
 __device__ __forceinline__ void assemble_row(int64_t p, const BatchArgs& a)
 {
     const int32_t    rp   = a.row_ptr[p];
@@ -99,7 +154,7 @@ __device__ __forceinline__ void assemble_row(int64_t p, const BatchArgs& a)
             Ent<float> e;
             e.col              = rg[i];
             e.val              = -w;
-            a.ent[rp + 1 + i]  = e;
+            a.ent[ent_at<W>(a, p, rp, 1 + i)] = e;
             if (has_q) {
                 const float ar = GeoMixed::va(P, Q, R);
                 area += ar > 0.f ? (double)ar : 0.0;
@@ -109,33 +164,41 @@ __device__ __forceinline__ void assemble_row(int64_t p, const BatchArgs& a)
         }
     }
     const double vw = 0.5 / area;
-    const double dg = 1.0 / vw + sumw;
+    const double iv = 1.0 / vw;  // then products: GB300's FP64 divide is slow
+    const double dg = iv + sumw;
     Ent<float>   d;
     d.col        = (int32_t)p;
     d.val        = (float)dg;
-    a.ent[rp]    = d;
+    a.ent[ent_at<W>(a, p, rp, 0)] = d;
+    if (W) {
+        Ent<float> z;
+        z.col = (int32_t)p;
+        z.val = 0.f;
+        for (int u = k + 1; u < W; ++u) a.ent[ent_at<W>(a, p, rp, u)] = z;
+    }
     a.diag[p]    = dg;
     a.dinv[p]    = 1.f / (d.val + FLT_EPSILON);
     R4<double> b;
-    b.x     = P.x / vw;
-    b.y     = P.y / vw;
-    b.z     = P.z / vw;
+    b.x     = P.x * iv;
+    b.y     = P.y * iv;
+    b.z     = P.z * iv;
     b.w     = 0.0;
     a.B[p]  = b;
 }
 
-// R = (float)(B - A X) accumulated in FP64; returns the block's r . D^-1 r
-template <int BT>
-__device__ __forceinline__ double residual(int64_t v0, int64_t v1, const BatchArgs& a, double* s_red)
+// r = B - A x in FP64 for rows [r0, r1) (FP32 off-diagonals promoted, FP64
+// diagonal), z = D^-1 r into Z, d = 0; returns the thread's r . diag^-1 r
+template <int W>
+__device__ __forceinline__ double batch_residual(int64_t r0, int64_t r1, int bt, const BatchArgs& a)
 {
     double part = 0;
-    for (int64_t i = v0 + threadIdx.x; i < v1; i += BT) {
+    for (int64_t i = r0 + threadIdx.x; i < r1; i += bt) {
         const R4<double> xi = a.X[i];
         const double     dg = a.diag[i];
         double           a0 = dg * xi.x, a1 = dg * xi.y, a2 = dg * xi.z;
-        const int32_t    e  = a.row_ptr[i + 1];
-        for (int32_t j = a.row_ptr[i] + 1; j < e; ++j) {
-            const Ent<float> q  = a.ent[j];
+        const int32_t    b0 = W ? 1 : a.row_ptr[i] + 1, e = W ? W : a.row_ptr[i + 1];
+        for (int32_t j = b0; j < e; ++j) {
+            const Ent<float> q  = a.ent[W ? j * a.n + i : j];
             const R4<double> xv = a.X[q.col];
             a0 += (double)q.val * xv.x;
             a1 += (double)q.val * xv.y;
@@ -143,141 +206,164 @@ __device__ __forceinline__ double residual(int64_t v0, int64_t v1, const BatchAr
         }
         const R4<double> b  = a.B[i];
         const double     e0 = b.x - a0, e1 = b.y - a1, e2 = b.z - a2;
-        R4<float>        r;
-        r.x = (float)e0, r.y = (float)e1, r.z = (float)e2, r.w = 0.f;
-        a.R[i] = r;
-        part += (e0 * e0 + e1 * e1 + e2 * e2) / dg;
+        const float      di = a.dinv[i];
+        R4<float>        z, zero;
+        z.x = di * (float)e0, z.y = di * (float)e1, z.z = di * (float)e2, z.w = 0.f;
+        zero.x = zero.y = zero.z = zero.w = 0.f;
+        a.Z[i] = z;
+        a.D[i] = zero;
+        part += (e0 * e0 + e1 * e1 + e2 * e2) * (double)di;  // ~ / diag, no FP64 divide
     }
-    return block_sum<BT>(part, s_red);
+    return part;
 }
 
-// scalar state of a CTA's inner PCG: the FP64 recurrence is touched by
-// thread 0 only; every thread reads the FP32 step sizes and the flag
-struct BatchPCG
+// scalar state of the job's solve (thread 0) and the values all threads read
+struct BatchScalars
 {
-    double delta0, delta;
-    int    it;
-    float  al, bt;
-    int    done;
+    double rr0, rr, delta, rep;
+    int    it, total;
+    bool   conv, conv_all;
+};
+struct BatchShared
+{
+    float al, bt;
+    int   first, replace, stop;
 };
 
-// block-level Jacobi-PCG for A D = R (R is overwritten as the residual);
-// returns the iterations completed.  Dot products: FP32 per thread and
-// warp, FP64 per CTA (rxg_gridsum.cuh).
-template <int BT>
-__device__ int inner_pcg(int64_t v0, int64_t v1, const BatchArgs& a, double rel2, int max_it,
-                         RedSmem& red, BatchPCG& c)
+// all flow steps of one mesh, rows [r0, r1) of it on this CTA, gang g
+template <int BT, int W>
+__device__ bool batch_job(int64_t r0, int64_t r1, const BatchArgs& a, GridSum& g, RedSmem& red,
+                          BatchScalars& c, BatchShared& sh)
 {
-    float tp = 0.f;
-    for (int64_t i = v0 + threadIdx.x; i < v1; i += BT) {
-        const float     di = a.dinv[i];
-        const R4<float> r  = a.R[i];
-        R4<float>       z;
-        z.x = di * r.x, z.y = di * r.y, z.z = di * r.z, z.w = 0.f;
-        a.Z[i] = z;
-        a.P[i] = z;
-        R4<float> zero;
-        zero.x = zero.y = zero.z = zero.w = 0.f;
-        a.D[i] = zero;
-        tp += r.x * z.x + r.y * z.y + r.z * z.z;
+    const double target = a.tol * a.tol;
+    if (threadIdx.x == 0) {
+        c.total    = 0;
+        c.conv_all = true;
     }
-    block_sum_post<BT>(tp, red, [&](double t) {
-        c.delta0 = c.delta = t;
-        c.it               = 0;
-        c.done             = !(t > 0) || max_it <= 0;
-    });
-    while (!c.done) {
-        // S = A P, P.S   (the block barriers order P before the gathers)
-        tp = 0.f;
-        for (int64_t i = v0 + threadIdx.x; i < v1; i += BT) {
-            float ax = 0, ay = 0, az = 0;
-            row_spmv4<float>(a.row_ptr, a.ent, i, a.P, ax, ay, az, (float*)nullptr);
-            R4<float> s;
-            s.x = ax, s.y = ay, s.z = az, s.w = 0.f;
-            a.S[i]            = s;
-            const R4<float> p = a.P[i];
-            tp += s.x * p.x + s.y * p.y + s.z * p.z;
-        }
-        block_sum_post<BT>(tp, red, [&](double sp) { c.al = (float)(c.delta / sp); });
-        const float al = c.al;
-        tp             = 0.f;
-        for (int64_t i = v0 + threadIdx.x; i < v1; i += BT) {
-            const float     di = a.dinv[i];
-            const R4<float> p = a.P[i], s = a.S[i];
-            R4<float>       d = a.D[i], r = a.R[i], z;
-            d.x += al * p.x, d.y += al * p.y, d.z += al * p.z;
-            r.x -= al * s.x, r.y -= al * s.y, r.z -= al * s.z;
-            z.x = di * r.x, z.y = di * r.y, z.z = di * r.z, z.w = 0.f;
-            a.D[i] = d;
-            a.R[i] = r;
-            a.Z[i] = z;
-            tp += r.x * z.x + r.y * z.y + r.z * z.z;
-        }
-        block_sum_post<BT>(tp, red, [&](double dn) {
-            if (dn < rel2 * c.delta0) {
-                c.done = 1;
-                return;
+    for (int step = 0; step < a.nsteps; ++step) {
+        // positions of the whole mesh are final (the previous step ended with
+        // a gang barrier after its last x update)
+        for (int64_t p = r0 + threadIdx.x; p < r1; p += BT) assemble_row<W>(p, a);
+        __syncthreads();
+        if (!grid_sum<BT>(batch_residual<W>(r0, r1, BT, a), g, red, [&](double t) {
+                c.rr0 = c.rr = c.delta = c.rep = t;
+                c.it                           = 0;
+                c.conv                         = !(t > 0.0);
+                sh.stop                        = c.conv || a.max_iter - c.total <= 0;
+                sh.first                       = 1;
+                sh.bt                          = 0.f;
+            }))
+            return false;
+        while (!sh.stop) {
+            const float bt    = sh.bt;
+            const bool  first = sh.first != 0;
+            // s = A z + beta s, p = z + beta p, s . p
+            float tp = 0.f;
+            for (int64_t i = r0 + threadIdx.x; i < r1; i += BT) {
+                float ax = 0.f, ay = 0.f, az = 0.f;
+                if (W) {
+                    Ent<float> q[W ? W : 1];
+#pragma unroll
+                    for (int u = 0; u < W; ++u) q[u] = a.ent[u * a.n + i];
+#pragma unroll
+                    for (int u = 0; u < W; ++u) {
+                        const R4<float> zv = a.Z[q[u].col];
+                        ax += q[u].val * zv.x, ay += q[u].val * zv.y, az += q[u].val * zv.z;
+                    }
+                } else {
+                    row_spmv4<float>(a.row_ptr, a.ent, i, a.Z, ax, ay, az, (float*)nullptr);
+                }
+                const R4<float> zi = a.Z[i];
+                R4<float>       si, pi;
+                if (first) {
+                    si.x = ax, si.y = ay, si.z = az;
+                    pi = zi;
+                } else {
+                    const R4<float> so = a.S[i], po = a.P[i];
+                    si.x = ax + bt * so.x, si.y = ay + bt * so.y, si.z = az + bt * so.z;
+                    pi.x = zi.x + bt * po.x, pi.y = zi.y + bt * po.y, pi.z = zi.z + bt * po.z;
+                }
+                si.w = pi.w = 0.f;
+                a.S[i] = si;
+                a.P[i] = pi;
+                tp += si.x * pi.x + si.y * pi.y + si.z * pi.z;
             }
-            c.bt    = (float)(dn / c.delta);
-            c.delta = dn;
-            ++c.it;
-            c.done = c.it >= max_it;
-        });
-        if (c.done) break;
-        const float bt = c.bt;
-        for (int64_t i = v0 + threadIdx.x; i < v1; i += BT) {
-            const R4<float> z = a.Z[i];
-            R4<float>       p = a.P[i];
-            p.x = z.x + bt * p.x, p.y = z.y + bt * p.y, p.z = z.z + bt * p.z;
-            a.P[i] = p;
-        }
-        __syncthreads();
-    }
-    return c.it;
-}
-
-template <int BT>
-__global__ void __launch_bounds__(BT) k_mcf_batch(BatchArgs a)
-{
-    __shared__ int      s_job;
-    __shared__ double   s_red[BT / 32 + 2];
-    __shared__ RedSmem  red;
-    __shared__ BatchPCG pcg;
-    while (true) {
-        if (threadIdx.x == 0) s_job = atomicAdd(a.queue, 1);
-        __syncthreads();
-        const int job = s_job;
-        __syncthreads();
-        if (job >= a.nmesh) return;
-        const int     m  = a.order[job];
-        const int64_t v0 = a.vstart[m], v1 = v0 + a.vcount[m];
-        int           total_it = 0;
-        bool          conv_all = true;
-        for (int step = 0; step < a.nsteps; ++step) {
-            for (int64_t p = v0 + threadIdx.x; p < v1; p += BT) assemble_row(p, a);
-            __syncthreads();
-            const double rr0  = residual<BT>(v0, v1, a, s_red);
-            double       rr   = rr0;
-            bool         conv = !(rr0 > 0);
-            for (int sweep = 0; sweep < 16 && !conv && total_it < a.max_iter; ++sweep) {
-                const double need  = a.tol * sqrt(rr0 / rr);
-                const double inner = fmax(1e-4, 0.3 * need);
-                total_it += inner_pcg<BT>(v0, v1, a, inner * inner, a.max_iter - total_it, red, pcg) + 1;
-                for (int64_t i = v0 + threadIdx.x; i < v1; i += BT) {
+            if (!grid_sum<BT>(tp, g, red, [&](double sp) { sh.al = (float)(c.delta / sp); })) return false;
+            const float al = sh.al;
+            // d += alpha p, z -= alpha D^-1 s, r . z
+            tp = 0.f;
+            for (int64_t i = r0 + threadIdx.x; i < r1; i += BT) {
+                const float     di = a.dinv[i];
+                const R4<float> pi = a.P[i], si = a.S[i];
+                R4<float>       d = a.D[i], z = a.Z[i];
+                d.x += al * pi.x, d.y += al * pi.y, d.z += al * pi.z;
+                const float ad = al * di;
+                z.x -= ad * si.x, z.y -= ad * si.y, z.z -= ad * si.z;
+                a.D[i] = d;
+                a.Z[i] = z;
+                tp += __fdividef(z.x * z.x + z.y * z.y + z.z * z.z, di);
+            }
+            if (!grid_sum<BT>(tp, g, red, [&](double dn) {
+                    ++c.it;
+                    sh.replace = dn < 1e-4 * c.rep || dn < 0.25 * target * c.rr0 ||
+                                 c.total + c.it >= a.max_iter || !(dn > 0.0);
+                    if (!sh.replace) {
+                        sh.bt    = (float)(dn / c.delta);
+                        c.delta  = dn;
+                        sh.first = 0;
+                    }
+                }))
+                return false;
+            if (sh.replace) {
+                for (int64_t i = r0 + threadIdx.x; i < r1; i += BT) {
                     R4<double>      x = a.X[i];
                     const R4<float> d = a.D[i];
                     x.x += (double)d.x, x.y += (double)d.y, x.z += (double)d.z;
                     a.X[i] = x;
                 }
-                __syncthreads();
-                rr   = residual<BT>(v0, v1, a, s_red);
-                conv = rr < a.tol * a.tol * rr0;
+                if (!grid_sum<BT>(0.f, g, red, [](double) {})) return false;
+                if (!grid_sum<BT>(batch_residual<W>(r0, r1, BT, a), g, red, [&](double t) {
+                        c.rr     = t;
+                        c.conv   = t < target * c.rr0;
+                        sh.stop  = c.conv || c.total + c.it >= a.max_iter || !(t > 0.0);
+                        sh.bt    = (float)(t / c.delta);
+                        c.delta  = t;
+                        c.rep    = t;
+                        sh.first = 0;
+                    }))
+                    return false;
             }
-            conv_all = conv_all && conv;
         }
         if (threadIdx.x == 0) {
-            a.iters[m] = total_it;
-            a.conv[m]  = conv_all ? 1 : 0;
+            c.total += c.it;
+            c.conv_all = c.conv_all && c.conv;
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
+// MINB: CTAs per SM the register allocation must allow (occupancy knob)
+template <int BT, int W, int MINB>
+__global__ void __launch_bounds__(BT, MINB) k_mcf_batch(BatchArgs a)
+{
+    __shared__ RedSmem      red;
+    __shared__ BatchScalars c;
+    __shared__ BatchShared  sh;
+    for (int32_t e = a.cta_off[blockIdx.x]; e < a.cta_off[blockIdx.x + 1]; ++e) {
+        const int32_t job = a.cta_job[e], rank = a.cta_rank[e];
+        const int32_t m = a.job_mesh[job], k = a.job_k[job];
+        const int64_t v0 = a.vstart[m], nv = a.vcount[m];
+        const int64_t chunk = (nv + k - 1) / k;
+        const int64_t lo    = rank * chunk, hi = lo + chunk;
+        const int64_t r0    = v0 + (lo < nv ? lo : nv);
+        const int64_t r1    = v0 + (hi < nv ? hi : nv);
+        GridSum       g{a.bar + 4 * job, a.part + 2 * a.kmax * job, a.err, (unsigned)k, 0u,
+                  (unsigned)rank};
+        if (!batch_job<BT, W>(r0, r1, a, g, red, c, sh)) return;
+        if (rank == 0 && threadIdx.x == 0) {
+            a.iters[m] = c.total;
+            a.conv[m]  = c.conv_all ? 1 : 0;
         }
     }
 }
@@ -317,22 +403,122 @@ static int batch_sms()
     return std::max(1, sms);
 }
 
-template <int BT>
-static int batch_max_per_sm()
+// the kernel for a CTA size, ELL width and CTAs per SM
+static const void* batch_kernel(int bt, int w, int bps)
+{
+#define RXG_BK(BTV, MB) (w == 8 ? (const void*)k_mcf_batch<BTV, 8, MB>       \
+                         : w == 16 ? (const void*)k_mcf_batch<BTV, 16, MB> \
+                                   : (const void*)k_mcf_batch<BTV, 0, MB>)
+    if (bt == 256) return bps >= 4 ? RXG_BK(256, 4) : RXG_BK(256, 2);
+    if (bt == 1024) return RXG_BK(1024, 1);
+    return bps >= 2 ? RXG_BK(512, 2) : RXG_BK(512, 1);
+#undef RXG_BK
+}
+
+static int max_per_sm(int bt, int w, int bps)
 {
     int per = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mcf_batch<BT>, BT, 0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_kernel(bt, w, bps), bt, 0) !=
+        cudaSuccess)
         per = 1;
     return std::max(1, per);
 }
 
-static int max_per_sm(int bt)
+constexpr int kGangMax = 32;  // most CTAs one mesh is split across
+
+// Gang schedule for G CTAs and the given tile (rows per CTA): longest job
+// first, each onto the k CTAs that are free first; a job's start is the
+// latest of their finish times.  Cost model: rows^1.5 (rows x the ~sqrt(rows)
+// PCG iterations of a mesh Laplacian system).
+static int batch_ell_width(const rxg_batch* b);
+
+static rxg_status build_plan(rxg_batch* b, int bt, int bps, int tile, GangPlan* out)
 {
-    switch (bt) {
-        case 256: return batch_max_per_sm<256>();
-        case 1024: return batch_max_per_sm<1024>();
-        default: return batch_max_per_sm<512>();
+    const int G = batch_sms() * std::min(bps, max_per_sm(bt, batch_ell_width(b), bps));
+    const int nm = b->nmesh;
+    std::vector<int32_t> order(nm);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int32_t x, int32_t y) { return b->vcount[x] > b->vcount[y]; });
+    std::vector<int32_t> job_mesh(nm), job_k(nm);  // jobs in longest-first order
+    std::vector<double>  start(nm);
+    std::vector<std::vector<int32_t>> members(nm);
+    using Slot = std::pair<double, int32_t>;  // (free at, CTA)
+    std::priority_queue<Slot, std::vector<Slot>, std::greater<Slot>> freeq;
+    for (int c = 0; c < G; ++c) freeq.push({0.0, c});
+    int kmax = 1;
+    for (int j = 0; j < nm; ++j) {
+        const int32_t m = order[j];
+        const int     k = (int)std::max<int64_t>(
+            1, std::min<int64_t>({(b->vcount[m] + tile - 1) / tile, (int64_t)kGangMax, (int64_t)G}));
+        kmax = std::max(kmax, k);
+        double t0 = 0.0;
+        for (int i = 0; i < k; ++i) {
+            const Slot s = freeq.top();
+            freeq.pop();
+            members[j].push_back(s.second);
+            t0 = std::max(t0, s.first);
+        }
+        // a mesh's PCG takes ~sqrt(rows) iterations, so its work grows as rows^1.5
+        const double t1 = t0 + std::pow((double)b->vcount[m], 1.5) / k;
+        for (int32_t c : members[j]) freeq.push({t1, c});
+        job_mesh[j] = m;
+        job_k[j]    = k;
+        start[j]    = t0;
     }
+    // every CTA walks its jobs in the one global order (planned start, job)
+    std::vector<int32_t> jobs_by_start(nm);
+    std::iota(jobs_by_start.begin(), jobs_by_start.end(), 0);
+    std::stable_sort(jobs_by_start.begin(), jobs_by_start.end(),
+                     [&](int32_t x, int32_t y) { return start[x] < start[y]; });
+    std::vector<std::vector<std::pair<int32_t, int32_t>>> per(G);  // (job, rank)
+    for (int32_t j : jobs_by_start)
+        for (int r = 0; r < (int)members[j].size(); ++r) per[members[j][r]].push_back({j, r});
+    std::vector<int32_t> off(G + 1, 0), cjob, crank;
+    for (int c = 0; c < G; ++c) {
+        off[c + 1] = off[c] + (int32_t)per[c].size();
+        for (auto& e : per[c]) {
+            cjob.push_back(e.first);
+            crank.push_back(e.second);
+        }
+    }
+    GangPlan p;
+    p.G = G, p.bt = bt, p.bps = bps, p.tile = tile, p.kmax = kmax, p.njobs = nm;
+    auto up = [](int32_t** d, const std::vector<int32_t>& h) -> cudaError_t {
+        cudaError_t e = cudaMalloc(d, std::max<size_t>(h.size(), 1) * 4);
+        if (e == cudaSuccess && !h.empty())
+            e = cudaMemcpy(*d, h.data(), h.size() * 4, cudaMemcpyHostToDevice);
+        return e;
+    };
+    cudaError_t e = up(&p.d_job_mesh, job_mesh);
+    if (e == cudaSuccess) e = up(&p.d_job_k, job_k);
+    if (e == cudaSuccess) e = up(&p.d_cta_off, off);
+    if (e == cudaSuccess) e = up(&p.d_cta_job, cjob);
+    if (e == cudaSuccess) e = up(&p.d_cta_rank, crank);
+    if (e == cudaSuccess) e = cudaMalloc(&p.d_bar, sizeof(unsigned) * 4 * nm);
+    if (e == cudaSuccess) e = cudaMalloc(&p.d_part, sizeof(double) * 2 * kmax * nm);
+    if (e != cudaSuccess) {
+        p.free_all();
+        return cuda_status(e, "rxg_batch: gang schedule");
+    }
+    *out = p;
+    return RXG_OK;
+}
+
+// the batch's current plan for (threads, CTAs per SM, tile), rebuilt on change
+static rxg_status ensure_plan(rxg_batch* b, int bt, int bps, int tile)
+{
+    std::lock_guard<std::mutex> g(b->mu);
+    if (b->plan.G && b->plan.bt == bt && b->plan.bps == bps && b->plan.tile == tile) return RXG_OK;
+    b->plan.free_all();
+    return build_plan(b, bt, bps, tile, &b->plan);
+}
+
+// ELL width of the union's matrix (rows = valence + 1), 0 for CSR
+static int batch_ell_width(const rxg_batch* b)
+{
+    const int64_t r = b->mesh->m.max_valence + 1;
+    return r <= 8 ? 8 : (r <= 16 ? 16 : 0);
 }
 
 static rxg_status batch_buffers(rxg_batch* b, size_t bytes)
@@ -354,28 +540,26 @@ static rxg_status batch_args(rxg_batch* b, cudaStream_t s, BatchArgs* out, R4<do
     Lazy*      z;
     rxg_status st = ensure_pattern(&b->mesh->m, s, &z);
     if (st) return st;
-    const int64_t n = b->mesh->m.nv, nnz = z->nnz;
+    const int64_t n = b->mesh->m.nv, w = batch_ell_width(b);
+    const int64_t nnz   = w ? w * n : z->nnz;
     const size_t  bytes = a256(sizeof(Ent<float>) * nnz) + 2 * a256(sizeof(R4<double>) * n) +
-                         5 * a256(sizeof(R4<float>) * n) + a256(sizeof(float) * n) +
+                         4 * a256(sizeof(R4<float>) * n) + a256(sizeof(float) * n) +
                          a256(sizeof(double) * n);
     {
         std::lock_guard<std::mutex> g(b->mu);
         if ((st = batch_buffers(b, bytes))) return st;
     }
-    uint8_t* q = (uint8_t*)b->buf;
+    uint8_t*  q = (uint8_t*)b->buf;
     BatchArgs a;
-    a.nmesh   = b->nmesh;
-    a.order   = b->d_order;
     a.vstart  = b->d_vstart;
     a.vcount  = b->d_vcount;
-    a.queue   = b->d_queue;
     a.row_ptr = z->row_ptr;
     a.col     = z->col;
     a.bnd     = z->bnd;
+    a.n       = n;
     a.ent = (Ent<float>*)q, q += a256(sizeof(Ent<float>) * nnz);
     a.X = (R4<double>*)q, q += a256(sizeof(R4<double>) * n);
     a.B = (R4<double>*)q, q += a256(sizeof(R4<double>) * n);
-    a.R = (R4<float>*)q, q += a256(sizeof(R4<float>) * n);
     a.P = (R4<float>*)q, q += a256(sizeof(R4<float>) * n);
     a.S = (R4<float>*)q, q += a256(sizeof(R4<float>) * n);
     a.Z = (R4<float>*)q, q += a256(sizeof(R4<float>) * n);
@@ -384,21 +568,39 @@ static rxg_status batch_args(rxg_batch* b, cudaStream_t s, BatchArgs* out, R4<do
     a.diag  = (double*)q;
     a.iters = b->d_iters;
     a.conv  = b->d_conv;
+    a.err   = device_error_word();
     *out    = a;
     *X4     = a.X;
     return RXG_OK;
 }
 
-static rxg_status batch_launch(rxg_batch* b, BatchArgs a, int bt, int bps, cudaStream_t s)
+static rxg_status batch_launch(rxg_batch* b, BatchArgs a, int bt, int bps, int tile, cudaStream_t s)
 {
-    RXG_CUDA_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(int32_t), s));
-    const int grid = std::min(b->nmesh, batch_sms() * std::min(bps, max_per_sm(bt)));
-    switch (bt) {
-        case 256: k_mcf_batch<256><<<grid, 256, 0, s>>>(a); break;
-        case 1024: k_mcf_batch<1024><<<grid, 1024, 0, s>>>(a); break;
-        default: k_mcf_batch<512><<<grid, 512, 0, s>>>(a); break;
-    }
-    RXG_CUDA_TRY(cudaGetLastError());
+    rxg_status st = ensure_plan(b, bt, bps, tile);
+    if (st) return st;
+    const GangPlan& p = b->plan;
+    a.job_mesh = p.d_job_mesh;
+    a.job_k    = p.d_job_k;
+    a.cta_off  = p.d_cta_off;
+    a.cta_job  = p.d_cta_job;
+    a.cta_rank = p.d_cta_rank;
+    a.bar      = p.d_bar;
+    a.part     = p.d_part;
+    a.kmax     = p.kmax;
+    RXG_CUDA_TRY(cudaMemsetAsync(p.d_bar, 0, sizeof(unsigned) * 4 * p.njobs, s));
+    void*       args[] = {&a};
+    const void* kern = batch_kernel(bt, batch_ell_width(b), bps);
+    cudaLaunchConfig_t   cfg  = {};
+    cudaLaunchAttribute  attr = {};
+    attr.id               = cudaLaunchAttributeCooperative;
+    attr.val.cooperative  = 1;
+    cfg.gridDim           = dim3(p.G);
+    cfg.blockDim          = dim3(bt);
+    cfg.dynamicSmemBytes  = 0;
+    cfg.stream            = s;
+    cfg.attrs             = &attr;
+    cfg.numAttrs          = 1;
+    RXG_CUDA_TRY(cudaLaunchKernelExC(&cfg, kern, args));
     return RXG_OK;
 }
 
@@ -465,20 +667,13 @@ rxg_status rxg_batch_create(int32_t nmesh, const int32_t* fv, const int64_t* nf,
         b->vstart[m] = lo;
         b->vcount[m] = (int32_t)nv[m];
     }
-    // largest meshes first (longest-processing-time order for the work queue)
-    std::vector<int32_t> order(nmesh);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int32_t x, int32_t y) { return b->vcount[x] > b->vcount[y]; });
     auto up = [&](int32_t** d, const void* h, size_t n) -> cudaError_t {
         cudaError_t e = cudaMalloc(d, std::max<size_t>(n, 1) * 4);
         if (e == cudaSuccess && h) e = cudaMemcpy(*d, h, n * 4, cudaMemcpyHostToDevice);
         return e;
     };
-    cudaError_t e = up(&b->d_order, order.data(), nmesh);
-    if (e == cudaSuccess) e = up(&b->d_vstart, b->vstart.data(), nmesh);
+    cudaError_t e = up(&b->d_vstart, b->vstart.data(), nmesh);
     if (e == cudaSuccess) e = up(&b->d_vcount, b->vcount.data(), nmesh);
-    if (e == cudaSuccess) e = up(&b->d_queue, nullptr, 1);
     if (e == cudaSuccess) e = up(&b->d_iters, nullptr, nmesh);
     if (e == cudaSuccess) e = up(&b->d_conv, nullptr, nmesh);
     if (e != cudaSuccess) {
@@ -492,10 +687,9 @@ rxg_status rxg_batch_create(int32_t nmesh, const int32_t* fv, const int64_t* nf,
 void rxg_batch_destroy(rxg_batch* b)
 {
     if (!b) return;
-    cudaFree(b->d_order);
+    b->plan.free_all();
     cudaFree(b->d_vstart);
     cudaFree(b->d_vcount);
-    cudaFree(b->d_queue);
     cudaFree(b->d_iters);
     cudaFree(b->d_conv);
     cudaFree(b->buf);
@@ -536,7 +730,7 @@ rxg_status rxg_batch_mcf(rxg_batch* b, double dt, int32_t nsteps, double tol, in
     const int64_t n = b->mesh->m.nv;
     const int     g = (int)std::min<int64_t>((n + 255) / 256, 152 * 32);
     k_batch_pack<<<g, 256, 0, s>>>(n, b->mesh->m.d.v_l2i, xyz, X4);
-    if ((st = batch_launch(b, a, b->threads, b->blocks_per_sm, s))) return st;
+    if ((st = batch_launch(b, a, b->threads, b->blocks_per_sm, b->tile, s))) return st;
     k_batch_unpack<<<g, 256, 0, s>>>(n, b->mesh->m.d.v_l2i, X4, xyz);
     RXG_CUDA_TRY(cudaGetLastError());
     return RXG_OK;
@@ -553,6 +747,8 @@ rxg_status rxg_batch_stats(const rxg_batch* b, int32_t* iters, int32_t* converge
     return RXG_OK;
 }
 
+// Times the CTA size x CTAs per SM x tile (rows per CTA of a mesh's gang)
+// grid on the caller's batch and keeps the fastest (xyz is not modified).
 rxg_status rxg_batch_autotune(rxg_batch* b, double dt, int32_t nsteps, double tol, int32_t max_iter,
                               const double* xyz, int32_t* threads, int32_t* blocks_per_sm,
                               float* best_ms, void* stream)
@@ -576,32 +772,39 @@ rxg_status rxg_batch_autotune(rxg_batch* b, double dt, int32_t nsteps, double to
     RXG_CUDA_TRY(cudaEventCreate(&e0));
     RXG_CUDA_TRY(cudaEventCreate(&e1));
     float best = 1e30f;
-    int   bt_best = b->threads, bps_best = b->blocks_per_sm;
+    int   bt_best = b->threads, bps_best = b->blocks_per_sm, tile_best = b->tile;
     for (int bt : {256, 512, 1024}) {
-        for (int bps : {1, 2, 4, 8}) {
-            if (bps > max_per_sm(bt)) continue;
-            float t = 0;
-            for (int rep = 0; rep < 2 && st == RXG_OK; ++rep) {
-                k_batch_pack<<<g, 256, 0, s>>>(n, b->mesh->m.d.v_l2i, xyz, X4);
-                cudaEventRecord(e0, s);
-                st = batch_launch(b, a, bt, bps, s);
-                cudaEventRecord(e1, s);
-                cudaEventSynchronize(e1);
-                cudaEventElapsedTime(&t, e0, e1);  // second repetition is kept
+        for (int bps : {1, 2, 4}) {
+            if (bps > max_per_sm(bt, batch_ell_width(b), bps) || bt * bps > 2048) continue;
+            for (int tile : {1024, 2048, 4096, 8192}) {
+                float t = 0;
+                for (int rep = 0; rep < 2 && st == RXG_OK; ++rep) {
+                    k_batch_pack<<<g, 256, 0, s>>>(n, b->mesh->m.d.v_l2i, xyz, X4);
+                    cudaEventRecord(e0, s);
+                    st = batch_launch(b, a, bt, bps, tile, s);
+                    cudaEventRecord(e1, s);
+                    cudaEventSynchronize(e1);
+                    cudaEventElapsedTime(&t, e0, e1);  // second repetition is kept
+                }
+                if (st) break;
+                if (t < best) {
+                    best      = t;
+                    bt_best   = bt;
+                    bps_best  = bps;
+                    tile_best = tile;
+                }
             }
             if (st) break;
-            if (t < best) {
-                best     = t;
-                bt_best  = bt;
-                bps_best = bps;
-            }
         }
+        if (st) break;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (st) return st;
     b->threads       = bt_best;
     b->blocks_per_sm = bps_best;
+    b->tile          = tile_best;
+    if ((st = ensure_plan(b, bt_best, bps_best, tile_best))) return st;
     if (threads) *threads = bt_best;
     if (blocks_per_sm) *blocks_per_sm = bps_best;
     if (best_ms) *best_ms = best;

@@ -42,8 +42,9 @@ struct GridSum
     unsigned* bar;
     double*   part;
     int*      err;
-    unsigned  G;
-    unsigned  round;
+    unsigned  G;      // CTAs taking part
+    unsigned  round;  // sums done so far
+    unsigned  slot;   // this CTA's partial slot, 0..G-1
 };
 
 // per-CTA shared scratch of the reductions
@@ -82,9 +83,9 @@ __device__ __forceinline__ double block_total_warp0(const RedSmem& r)
     return t;
 }
 
-// Grid exchange of the CTA totals already in RedSmem::warp[0..NW): thread 0
-// of each CTA runs post(grid total) before the CTA's threads continue.
-// Returns false on timeout.
+// Exchange of the CTA totals already in RedSmem::warp[0..NW) among the G CTAs
+// of a grid or gang: thread 0 of each CTA runs post(total) before the CTA's
+// threads continue.  Returns false on timeout.
 template <int NW, typename Post>
 __device__ __forceinline__ bool grid_sum_core(GridSum& g, RedSmem& r, Post post)
 {
@@ -96,8 +97,15 @@ __device__ __forceinline__ bool grid_sum_core(GridSum& g, RedSmem& r, Post post)
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
         double* pk = g.part + (g.round & 1u) * g.G;
         int     ok = 1;
+        if (g.G == 1) {  // a CTA on its own: no exchange
+            if (lane == 0) {
+                r.ok = 1;
+                post(t);
+            }
+            goto done;
+        }
         if (lane == 0) {
-            __stcg(pk + blockIdx.x, t);
+            __stcg(pk + g.slot, t);
             red_add_release(g.bar, 1u);
             const unsigned target = (g.round + 1u) * g.G;
             uint32_t       it     = 0;
@@ -139,6 +147,7 @@ __device__ __forceinline__ bool grid_sum_core(GridSum& g, RedSmem& r, Post post)
             if (ok) post(acc);
         }
     }
+done:
     __syncthreads();
     ++g.round;
     return r.ok != 0;

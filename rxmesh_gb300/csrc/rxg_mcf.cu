@@ -356,11 +356,14 @@ __global__ void __launch_bounds__(256) k_mcf_assemble(int64_t nv, const int32_t*
                 R = S;
             }
         }
+        // v_weight = 0.5 / area and its inverse as the reference forms them;
+        // one more division, then products (GB300's FP64 divide is slow)
         const TB vw = TB(0.5) / area;
-        const TB dg = TB(1) / vw + sumw;
+        const TB iv = TB(1) / vw;
+        const TB dg = iv + sumw;
         out.entry(rp, (int32_t)p, (T)dg);
         out.diag_full(p, dg);
-        out.rhs(p, (TB)P.x / vw, (TB)P.y / vw, (TB)P.z / vw);
+        out.rhs(p, (TB)P.x * iv, (TB)P.y * iv, (TB)P.z * iv);
     }
 }
 
@@ -571,7 +574,7 @@ __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
     const int64_t r0    = blockIdx.x * chunk;
     const int64_t r1    = min(a.n, r0 + chunk);
     T* const      src   = PC ? a.Z : a.R;  // vector the direction is built from
-    GridSum       g{a.bar, a.part, a.err, gridDim.x, 0u};
+    GridSum       g{a.bar, a.part, a.err, gridDim.x, 0u, blockIdx.x};
     auto          conv = [&](double d) { return d < a.abs_tol || d / c.delta0 < a.rel_tol; };
     // Per-thread partial dot products stay in T over the thread's few rows;
     // the block and grid reductions are in FP64, and the scalar recurrence
@@ -951,7 +954,7 @@ __global__ void __launch_bounds__(kBT) k_cgm(CGMArgs<T> a)
     const int64_t r0    = blockIdx.x * chunk;
     const int64_t r1    = min(a.n, r0 + chunk);
     const T       eps   = sizeof(T) == 4 ? (T)FLT_EPSILON : (T)DBL_EPSILON;
-    GridSum       g{a.bar, a.part, a.err, gridDim.x, 0u};
+    GridSum       g{a.bar, a.part, a.err, gridDim.x, 0u, blockIdx.x};
     auto          conv = [&](double d) { return d < a.abs_tol || d / c.delta0 < a.rel_tol; };
 
     // ---- pre_solve: R = B - A X, Z = D^-1 R, delta = R.Z

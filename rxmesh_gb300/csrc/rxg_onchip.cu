@@ -107,7 +107,7 @@ __device__ __forceinline__ double onchip_residual(const OnchipArgs& a, int64_t r
         z.x = di * (float)e0, z.y = di * (float)e1, z.z = di * (float)e2, z.w = 0.f;
         Zx[l] = z.x, Zy[l] = z.y, Zz[l] = z.z;
         a.Z[i] = z;
-        part += (e0 * e0 + e1 * e1 + e2 * e2) / d;
+        part += (e0 * e0 + e1 * e1 + e2 * e2) * (double)di;  // ~ / diag, no FP64 divide
     }
     return part;
 }
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(BT, 1) k_mcf_onchip(OnchipArgs a)
     const int32_t r0i = a.bounds[blockIdx.x];
     const int64_t r0  = r0i;
     const int     m   = a.bounds[blockIdx.x + 1] - r0i;
-    GridSum       g{a.bar, a.part, a.err, gridDim.x, 0u};
+    GridSum       g{a.bar, a.part, a.err, gridDim.x, 0u, blockIdx.x};
     const double  target = a.tol * a.tol;  // on rr / rr0
 
     for (int l = threadIdx.x; l < m; l += BT) {

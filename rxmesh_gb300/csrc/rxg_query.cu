@@ -274,18 +274,10 @@ __global__ void __launch_bounds__(kQT) k_query_elem(const PatchHdr* __restrict__
 }
 
 // ---------------------------------------------------------------------
-// Vertex normals (OP 5).  Formula of compute_vertex_normal
-// (apps/VertexNormal/vertex_normal_kernel.cuh:10-43): every face adds its
-// (unnormalised) normal to its three vertices, weighted per corner by the
-// inverse sum of the squared lengths of the corner's two edges (Max
-// weights) or not at all (area weights).
-//
-// Per patch, in shared memory: each local face (owned and ribbon) computes
-// its normal and corner weights once; a counting sort of the face corners
-// by owned vertex (integer shared atomics, which run about 2.5x faster on
-// GB300 than FP32 shared atomics) builds each owned vertex's corner list;
-// one thread per owned vertex then sums its corners and writes its normal
-// once: no float atomics, no global atomics, no zero-fill pass.
+// Vertex normals (OP 5): per patch, every local face (owned + ribbon)
+// contributes to the patch's owned vertices in shared memory, so owned
+// normals are written once, with no global atomics and no zero-fill pass.
+// Formula of compute_vertex_normal (apps/VertexNormal/vertex_normal_kernel.cuh:10-43).
 // ---------------------------------------------------------------------
 
 template <int W, int kQT>
@@ -296,36 +288,40 @@ __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restri
 {
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ uint64_t bar;
-    __shared__ int32_t  s_warp[kQT / 32];
-    constexpr int FN = W == RXG_NORMAL_MAX ? 6 : 3;  // floats per face: normal (+ corner weights)
 
     const PatchHdr h   = load_hdr(hdrs);
-    const int32_t  nVo = h.nVo, nVr = h.nVl - h.nVo, nF = h.nFl;
+    const int32_t  nVo = h.nVo, nVr = h.nVl - h.nVo;
     uint32_t* s_ev  = smem;
     uint32_t* s_fe  = s_ev + pad4i(h.nEl);
-    uint32_t* s_rv  = s_fe + pad4i((int32_t)fe_words(nF));
-    int32_t*  s_cnt = reinterpret_cast<int32_t*>(s_rv + pad4i(nVr));
-    float*    s_fn  = reinterpret_cast<float*>(s_cnt + pad4i(nVo + 1));
-    // positions, then (once the face pass is done) the sorted corner list
-    float*    s_pos = s_fn + pad4i(FN * nF);
-    uint32_t* s_cor = reinterpret_cast<uint32_t*>(s_pos);
+    float*    s_pos = reinterpret_cast<float*>(s_fe + pad4i((int32_t)fe_words(h.nFl)));
+    float*    s_acc = s_pos + pad4i(3 * h.nVl);
 
     if (threadIdx.x == 0) mbar_init(&bar, 1);
-    for (int i = threadIdx.x; i <= nVo; i += kQT) s_cnt[i] = 0;
-    for (int i = threadIdx.x; i < 3 * nVo; i += kQT) s_pos[i] = __ldg(xyz + 3 * (int64_t)h.v_base + i);
     __syncthreads();
-    uint32_t* const dst[3] = {s_ev, s_fe, s_rv};
-    const Slice     sl[3]  = {{arena + h.ev_off, pad16_bytes(h.nEl)},
-                              {arena + h.fe_off, pad16_bytes((int32_t)fe_words(nF))},
-                              {arena + h.rv_off, pad16_bytes(nVr)}};
-    if (!stage(&bar, dst, sl, err)) return;
-    for (int i = threadIdx.x; i < 3 * nVr; i += kQT)
-        s_pos[3 * nVo + i] = __ldg(xyz + 3 * (int64_t)s_rv[i / 3] + (i % 3));
-    __syncthreads();
+    // EV and FE come in by TMA while the threads fetch the positions: owned
+    // ones contiguously, ribbon ones through the ribbon table read straight
+    // from global memory (so neither waits for the other)
+    if (threadIdx.x == 0) {
+        const uint32_t eb = pad16_bytes(h.nEl), fb = pad16_bytes((int32_t)fe_words(h.nFl));
+        mbar_arrive_expect_tx(&bar, eb + fb);
+        if (eb) bulk_g2s(s_ev, arena + h.ev_off, eb, &bar);
+        if (fb) bulk_g2s(s_fe, arena + h.fe_off, fb, &bar);
+    }
+    for (int i = threadIdx.x; i < 3 * nVo; i += kQT) {
+        s_acc[i] = 0.f;
+        s_pos[i] = __ldg(xyz + 3 * (int64_t)h.v_base + i);
+    }
+    for (int i = threadIdx.x; i < nVr; i += kQT) {
+        const int64_t g = 3 * (int64_t)__ldg(arena + h.rv_off + i);
+        float*        d = s_pos + 3 * (nVo + i);
+        d[0]            = __ldg(xyz + g);
+        d[1]            = __ldg(xyz + g + 1);
+        d[2]            = __ldg(xyz + g + 2);
+    }
+    if (!wait_stage(&bar, err)) return;  // its CTA barrier also orders the position stores
 
-    // 1. face normals and corner weights; count the corners of owned vertices
     const uint16_t* fe16 = reinterpret_cast<const uint16_t*>(s_fe);
-    for (int f = threadIdx.x; f < nF; f += kQT) {
+    for (int f = threadIdx.x; f < h.nFl; f += kQT) {
         uint32_t v[3];
         float3   c[3];
 #pragma unroll
@@ -333,55 +329,29 @@ __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restri
             v[k] = face_vertex(fe16, s_ev, f, k);
             c[k] = make_float3(s_pos[3 * v[k]], s_pos[3 * v[k] + 1], s_pos[3 * v[k] + 2]);
         }
+        if ((int32_t)v[0] >= nVo && (int32_t)v[1] >= nVo && (int32_t)v[2] >= nVo) continue;
         const float3 u = make_float3(c[1].x - c[0].x, c[1].y - c[0].y, c[1].z - c[0].z);
         const float3 w = make_float3(c[2].x - c[0].x, c[2].y - c[0].y, c[2].z - c[0].z);
-        float*       o = s_fn + FN * f;
-        o[0]           = u.y * w.z - w.y * u.z;
-        o[1]           = u.z * w.x - w.z * u.x;
-        o[2]           = u.x * w.y - w.x * u.y;
-        if (W == RXG_NORMAL_MAX) {
-            float l[3];
+        const float  n[3] = {u.y * w.z - w.y * u.z, u.z * w.x - w.z * u.x, u.x * w.y - w.x * u.y};
+        float        l[3];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const float3 a = c[k], b = c[(k + 1) % 3];
-                const float  dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
-                l[k]            = dx * dx + dy * dy + dz * dz;
-            }
-#pragma unroll
-            for (int k = 0; k < 3; ++k) o[3 + k] = l[k] + l[(k + 2) % 3];
+        for (int k = 0; k < 3; ++k) {
+            const float3 a = c[k], b = c[(k + 1) % 3];
+            const float  dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+            l[k]            = dx * dx + dy * dy + dz * dz;
         }
 #pragma unroll
-        for (int k = 0; k < 3; ++k)
-            if ((int32_t)v[k] < nVo) atomicAdd(&s_cnt[v[k]], 1);
+        for (int k = 0; k < 3; ++k) {
+            if ((int32_t)v[k] >= nVo) continue;
+            const float d = W == RXG_NORMAL_MAX ? (l[k] + l[(k + 2) % 3]) : 1.f;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+                atomicAdd(&s_acc[3 * v[k] + i], W == RXG_NORMAL_MAX ? n[i] / d : n[i]);
+        }
     }
     __syncthreads();
-
-    // 2. corner list offsets; 3. scatter corners (face << 2 | k) by vertex
-    block_exclusive_scan<kQT>(s_cnt, nVo + 1, s_warp);
-    for (int i = threadIdx.x; i < 3 * nF; i += kQT) {
-        const int      f = i / 3, k = i - 3 * f;
-        const uint32_t v = face_vertex(fe16, s_ev, f, k);
-        if ((int32_t)v < nVo) s_cor[atomicAdd(&s_cnt[v], 1)] = ((uint32_t)f << 2) | (uint32_t)k;
-    }
-    __syncthreads();
-
-    // 4. one thread per owned vertex sums its corners (s_cnt[v] now ends v's list)
     float* o = out + 3 * (int64_t)h.v_base;
-    for (int v = threadIdx.x; v < nVo; v += kQT) {
-        const int32_t e = s_cnt[v];
-        float         ax = 0.f, ay = 0.f, az = 0.f;
-        for (int32_t j = v > 0 ? s_cnt[v - 1] : 0; j < e; ++j) {
-            const uint32_t cr = s_cor[j];
-            const float*   fn = s_fn + FN * (cr >> 2);
-            if (W == RXG_NORMAL_MAX) {
-                const float d = fn[3 + (cr & 3u)];
-                ax += fn[0] / d, ay += fn[1] / d, az += fn[2] / d;
-            } else {
-                ax += fn[0], ay += fn[1], az += fn[2];
-            }
-        }
-        o[3 * v] = ax, o[3 * v + 1] = ay, o[3 * v + 2] = az;
-    }
+    for (int i = threadIdx.x; i < 3 * nVo; i += kQT) o[i] = s_acc[i];
 }
 
 // ---------------------------------------------------------------------
@@ -402,11 +372,8 @@ static size_t smem_words(const PatchHdr& h, int kind)
             return pad4i(h.nEl) + few + pad4i(nFr) + pad4i(h.nVo + 1) + (3 * h.nFl + 1) / 2 + 4;
         case RXG_OP_FV: return pad4i(h.nEl) + pad4i((3 * h.nFo + 1) / 2) + pad4i(nVr);
         case RXG_OP_EV: return pad4i(h.nEo) + pad4i(nVr);
-        default: {  // normals: EV, FE, ribbon ids, counts, per-face data, max(positions, corners)
-            const int32_t fn = kind == 6 ? 6 : 3;
-            return pad4i(h.nEl) + few + pad4i(nVr) + pad4i(h.nVo + 1) + pad4i(fn * h.nFl) +
-                   std::max(pad4i(3 * h.nVl), pad4i(3 * h.nFl));
-        }
+        default:  // normals
+            return pad4i(h.nEl) + few + pad4i(3 * h.nVl) + 3 * h.nVo;
     }
 }
 
