@@ -318,7 +318,43 @@ def run_mcf(args, torch):
                      "rel_err_of_update_step1": err_upd}
     res["mixed_speedup_vs_f64"] = res["mixed"]["steps_per_s"] / res["f64"]["steps_per_s"]
     res["oracle_pcg_iters_step1"] = it_o
+    res["spmv"] = run_spmv(torch, rx, x0l, dt)
     return res
+
+
+def run_spmv(torch, rx, x0l, dt):
+    """Y = A X (rxg_spmm, SparseMatrix::multiply) on the level-8 MCF matrix,
+    3 right-hand sides, FP64 and FP32, each launch after an L2 flush."""
+    from rxmesh_gb300._solvers import mcf_assemble
+    peak, _ = peaks()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    clean = torch.ones(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    out = {}
+    for name, dtype, sz in (("f64", torch.float64, 8), ("f32", torch.float32, 4)):
+        A, _ = mcf_assemble(rx, x0l, dt, dtype=dtype)
+        X = x0l.to(dtype).contiguous()
+        Y = torch.empty_like(X)
+        n, nnz = A.rows(), A.col.numel()
+        algo = nnz * (4 + sz) + 4 * (n + 1) + 2 * 3 * n * sz
+        for _ in range(3):
+            A.multiply(X, Y)
+        torch.cuda.synchronize()
+        evs = []
+        for _ in range(20):
+            flush.fill_(1.0)
+            clean.sum()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            A.multiply(X, Y)
+            b.record()
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        ms = statistics.median([a.elapsed_time(b) for a, b in evs])
+        gbs = algo / (ms * 1e-3) / 1e9
+        out[name] = {"ms": ms, "gbs_algorithmic": gbs, "frac_of_measured_hbm": gbs / peak,
+                     "algorithmic_bytes": algo}
+    return out
 
 
 def run_arap(args, torch):

@@ -238,7 +238,10 @@ __device__ __forceinline__ double block_sum_d(double v, double* s_red)
 // One thread per vertex p: gradient row, Hessian block row [diag, ring...],
 // and (for faces whose first vertex is p) the face energy.
 template <typename T, bool HESS>
-__global__ void __launch_bounds__(128) k_arap_vertex(
+// FP32: registers capped for 5 CTAs per SM (96, with a 32-byte spill): 0.155
+// against 0.164 ms uncapped (120 registers, 4 CTAs) on the 512^2 cloth; FP64
+// keeps its registers
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 5 : 1) k_arap_vertex(
     int64_t nv, const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ ring_off,
     const int32_t* __restrict__ ring, const int32_t* __restrict__ ring_face,
     const int8_t* __restrict__ bnd, const int32_t* __restrict__ fv, const T* __restrict__ x,

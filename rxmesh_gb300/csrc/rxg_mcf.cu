@@ -382,17 +382,28 @@ __global__ void __launch_bounds__(256) k_spmm(int64_t n, const int32_t* __restri
         TACC acc[NC];
 #pragma unroll
         for (int c = 0; c < NC; ++c) acc[c] = TACC(0);
-        const int32_t e = rp[i + 1];
-        for (int32_t j = rp[i]; j < e; ++j) {
-            const TACC    a  = (TACC)val[j];
-            const int64_t cj = (int64_t)col[j] * NC;
+        const int32_t e = __ldg(rp + i + 1);
+        // eight entries per round: all column/value loads, then all gathers,
+        // in flight together (MCF rows have about seven entries)
+        for (int32_t j0 = __ldg(rp + i); j0 < e; j0 += 8) {
+            int32_t cj[8];
+            TACC    v[8];
 #pragma unroll
-            for (int c = 0; c < NC; ++c) acc[c] += a * (TACC)x[cj + c];
+            for (int u = 0; u < 8; ++u) {
+                const bool ok = j0 + u < e;
+                cj[u]         = ok ? __ldg(col + j0 + u) : (int32_t)i;
+                v[u]          = ok ? (TACC)__ldg(val + j0 + u) : TACC(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+#pragma unroll
+                for (int c = 0; c < NC; ++c) acc[c] += v[u] * (TACC)__ldg(x + (int64_t)cj[u] * NC + c);
         }
 #pragma unroll
         for (int c = 0; c < NC; ++c) y[i * NC + c] = RESID ? b[i * NC + c] - acc[c] : acc[c];
     }
 }
+
 
 // ---------------------------------------------------------------------
 // Persistent CG / Jacobi-PCG (CGSolver / PCGSolver, cg_solver.h:37-125,
@@ -837,9 +848,9 @@ static rxg_status spmm_launch(int nc, int64_t n, const int32_t* rp, const int32_
 #define RXG_SPMM_CASE(NCV)                                                                     \
     case NCV:                                                                                  \
         if (b)                                                                                 \
-            k_spmm<TA, TX, TACC, NCV, true><<<g, 256, 0, s>>>(n, rp, col, val, x, b, y);       \
+            k_spmm<TA, TX, TACC, NCV, true><<<g, 256, 0, s>>>(n, rp, col, val, x, b, y);     \
         else                                                                                   \
-            k_spmm<TA, TX, TACC, NCV, false><<<g, 256, 0, s>>>(n, rp, col, val, x, b, y);      \
+            k_spmm<TA, TX, TACC, NCV, false><<<g, 256, 0, s>>>(n, rp, col, val, x, b, y);    \
         break;
     switch (nc) {
         RXG_SPMM_CASE(1)
