@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -69,6 +70,12 @@ struct Mesh
 
     int64_t device_bytes = 0;
     size_t  smem_bytes[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // per query kind, max over patches
+
+    // calls with host arrays: a copy stream and events that overlap the
+    // device-to-host copy of each slice of patches with the kernel of the next
+    mutable std::mutex   stage_mu;
+    mutable cudaStream_t copy_stream = nullptr;
+    mutable cudaEvent_t  copy_ev[4]  = {nullptr, nullptr, nullptr, nullptr};
 };
 
 void compute_smem_table(Mesh& m);

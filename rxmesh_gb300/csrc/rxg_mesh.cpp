@@ -398,6 +398,12 @@ static void free_device(Mesh& M)
     cudaFree(M.d.f_l2i);
     cudaFree(M.d.fv_lin);
     M.d = DeviceTopo{};
+    if (M.copy_stream) cudaStreamDestroy(M.copy_stream);
+    M.copy_stream = nullptr;
+    for (cudaEvent_t& e : M.copy_ev) {
+        if (e) cudaEventDestroy(e);
+        e = nullptr;
+    }
 }
 
 }  // namespace rxg

@@ -401,16 +401,24 @@ static rxg_status launch_patch_kernel(K kern, const Mesh* m, size_t smem, cudaSt
     return RXG_OK;
 }
 
+// Patches [p0, p0 + np) of a patch kernel: CTA b works on patch p0 + b (its
+// header pointer is offset; every other index in the headers is absolute).
+struct PatchRange
+{
+    int32_t p0, np;
+};
+
 template <typename F, typename... Args>
 static rxg_status launch(F* kern, int threads, const Mesh* m, size_t smem, cudaStream_t s,
-                         const char* name, Args... args)
+                         const char* name, PatchRange r, const PatchHdr* hd, Args... args)
 {
     rxg_status st = launch_patch_kernel(kern, m, smem, s, name);
     if (st) return st;
+    if (r.np <= 0) return RXG_OK;
     if (smem > 48 * 1024)
         RXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem));
-    kern<<<m->num_patches, threads, smem, s>>>(args...);
+    kern<<<r.np, threads, smem, s>>>(hd + r.p0, args...);
     RXG_CUDA_TRY(cudaGetLastError());
     return RXG_OK;
 }
@@ -430,55 +438,62 @@ int query_threads()
 
 template <int BT>
 static rxg_status launch_query_bt(const Mesh* m, int op, int32_t* d_off, int32_t* d_val,
-                                  cudaStream_t s)
+                                  cudaStream_t s, PatchRange r)
 {
     const size_t    smem = query_smem_bytes(m, op);
     int*            err  = device_error_word();
     const PatchHdr* hd   = m->d.hdr;
     const uint32_t* ar   = m->d.arena;
     switch (op) {
-        case RXG_OP_VV: return launch(k_query_vertex<0, BT>, BT, m, smem, s, "VV", hd, ar, d_off, d_val, err);
-        case RXG_OP_VE: return launch(k_query_vertex<1, BT>, BT, m, smem, s, "VE", hd, ar, d_off, d_val, err);
-        case RXG_OP_VF: return launch(k_query_vertex<2, BT>, BT, m, smem, s, "VF", hd, ar, d_off, d_val, err);
-        case RXG_OP_FV: return launch(k_query_elem<3, BT>, BT, m, smem, s, "FV", hd, ar, d_val, err);
-        case RXG_OP_EV: return launch(k_query_elem<4, BT>, BT, m, smem, s, "EV", hd, ar, d_val, err);
+        case RXG_OP_VV: return launch(k_query_vertex<0, BT>, BT, m, smem, s, "VV", r, hd, ar, d_off, d_val, err);
+        case RXG_OP_VE: return launch(k_query_vertex<1, BT>, BT, m, smem, s, "VE", r, hd, ar, d_off, d_val, err);
+        case RXG_OP_VF: return launch(k_query_vertex<2, BT>, BT, m, smem, s, "VF", r, hd, ar, d_off, d_val, err);
+        case RXG_OP_FV: return launch(k_query_elem<3, BT>, BT, m, smem, s, "FV", r, hd, ar, d_val, err);
+        case RXG_OP_EV: return launch(k_query_elem<4, BT>, BT, m, smem, s, "EV", r, hd, ar, d_val, err);
     }
     set_error("rxg_query: unknown op %d", op);
     return RXG_ERR_INVALID;
 }
 
-rxg_status launch_query(const Mesh* m, int op, int32_t* d_off, int32_t* d_val, cudaStream_t s)
+static rxg_status launch_query_range(const Mesh* m, int op, int32_t* d_off, int32_t* d_val,
+                                     cudaStream_t s, PatchRange r)
 {
     switch (query_threads()) {
-        case 32: return launch_query_bt<32>(m, op, d_off, d_val, s);
-        case 64: return launch_query_bt<64>(m, op, d_off, d_val, s);
-        case 256: return launch_query_bt<256>(m, op, d_off, d_val, s);
-        default: return launch_query_bt<128>(m, op, d_off, d_val, s);
+        case 32: return launch_query_bt<32>(m, op, d_off, d_val, s, r);
+        case 64: return launch_query_bt<64>(m, op, d_off, d_val, s, r);
+        case 256: return launch_query_bt<256>(m, op, d_off, d_val, s, r);
+        default: return launch_query_bt<128>(m, op, d_off, d_val, s, r);
     }
+}
+
+rxg_status launch_query(const Mesh* m, int op, int32_t* d_off, int32_t* d_val, cudaStream_t s)
+{
+    return launch_query_range(m, op, d_off, d_val, s, PatchRange{0, m->num_patches});
 }
 
 template <int BT>
 static rxg_status launch_normals_bt(const Mesh* m, int weighting, const float* xyz, float* out,
-                                    cudaStream_t s)
+                                    cudaStream_t s, PatchRange r)
 {
     // kind 6: Max weights (normal + corner weights per face), 5: area weights
-    const size_t smem = query_smem_bytes(m, weighting == RXG_NORMAL_MAX ? 6 : 5);
-    int*         err  = device_error_word();
+    const size_t    smem = query_smem_bytes(m, weighting == RXG_NORMAL_MAX ? 6 : 5);
+    int*            err  = device_error_word();
+    const PatchHdr* hd   = m->d.hdr;
     if (weighting == RXG_NORMAL_MAX)
-        return launch(k_vertex_normals<RXG_NORMAL_MAX, BT>, BT, m, smem, s, "normals",
-                      (const PatchHdr*)m->d.hdr, (const uint32_t*)m->d.arena, xyz, out, err);
-    return launch(k_vertex_normals<RXG_NORMAL_AREA, BT>, BT, m, smem, s, "normals",
-                  (const PatchHdr*)m->d.hdr, (const uint32_t*)m->d.arena, xyz, out, err);
+        return launch(k_vertex_normals<RXG_NORMAL_MAX, BT>, BT, m, smem, s, "normals", r, hd,
+                      (const uint32_t*)m->d.arena, xyz, out, err);
+    return launch(k_vertex_normals<RXG_NORMAL_AREA, BT>, BT, m, smem, s, "normals", r, hd,
+                  (const uint32_t*)m->d.arena, xyz, out, err);
 }
 
-rxg_status launch_normals(const Mesh* m, int weighting, const float* xyz, float* out,
-                          cudaStream_t s)
+static rxg_status launch_normals(const Mesh* m, int weighting, const float* xyz, float* out,
+                                 cudaStream_t s, PatchRange r)
 {
     switch (query_threads()) {
-        case 32: return launch_normals_bt<32>(m, weighting, xyz, out, s);
-        case 64: return launch_normals_bt<64>(m, weighting, xyz, out, s);
-        case 256: return launch_normals_bt<256>(m, weighting, xyz, out, s);
-        default: return launch_normals_bt<128>(m, weighting, xyz, out, s);
+        case 32: return launch_normals_bt<32>(m, weighting, xyz, out, s, r);
+        case 64: return launch_normals_bt<64>(m, weighting, xyz, out, s, r);
+        case 256: return launch_normals_bt<256>(m, weighting, xyz, out, s, r);
+        default: return launch_normals_bt<128>(m, weighting, xyz, out, s, r);
     }
 }
 
@@ -519,12 +534,59 @@ static rxg_status stage_in(const void* user, size_t bytes, cudaStream_t s, Stage
     return RXG_OK;
 }
 
-static rxg_status finish_out(void* user, const Staged& st, size_t bytes, cudaStream_t s)
+// One output array of a host-array call: element e of the device copy goes
+// to element e of the host array; eb[k] is the first element slice k writes.
+struct HostPiece
 {
-    if (!st.owns) return RXG_OK;
-    RXG_CUDA_TRY(cudaMemcpyAsync(user, st.d, bytes, cudaMemcpyDeviceToHost, s));
+    char*                host;
+    const char*          dev;
+    size_t               esz;
+    std::vector<int64_t> eb;  // kSlices + 1 element bounds
+};
+
+constexpr int kSlices = 4;
+
+// Host arrays: the kernel runs over kSlices slices of patches on stream s;
+// as each slice finishes (an event), its output ranges are copied to the host
+// on the mesh's copy stream, so the copies overlap the following slices.
+// Every patch writes a contiguous range of each output (linear ids are
+// patch-ordered), so the slices' ranges are disjoint.  Returns after the
+// copies have landed.
+template <typename Run>
+static rxg_status run_to_host(const Mesh& M, cudaStream_t s, const int32_t* pb, Run run,
+                              std::vector<HostPiece>& pieces)
+{
+    std::lock_guard<std::mutex> lk(M.stage_mu);
+    if (!M.copy_stream) {
+        RXG_CUDA_TRY(cudaStreamCreateWithFlags(&M.copy_stream, cudaStreamNonBlocking));
+        for (cudaEvent_t& e : M.copy_ev) RXG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    for (int k = 0; k < kSlices; ++k) {
+        rxg_status st = run(PatchRange{pb[k], pb[k + 1] - pb[k]});
+        if (st) return st;
+        RXG_CUDA_TRY(cudaEventRecord(M.copy_ev[k], s));
+        RXG_CUDA_TRY(cudaStreamWaitEvent(M.copy_stream, M.copy_ev[k], 0));
+        for (HostPiece& q : pieces) {
+            const size_t off = (size_t)q.eb[k] * q.esz, bytes = (size_t)(q.eb[k + 1] - q.eb[k]) * q.esz;
+            if (bytes)
+                RXG_CUDA_TRY(cudaMemcpyAsync(q.host + off, q.dev + off, bytes, cudaMemcpyDeviceToHost,
+                                             M.copy_stream));
+        }
+    }
+    RXG_CUDA_TRY(cudaStreamSynchronize(M.copy_stream));
     return RXG_OK;
 }
+
+// patch bounds of the slices
+static void slice_patches(const Mesh& M, int32_t* pb)
+{
+    for (int k = 0; k <= kSlices; ++k) pb[k] = (int32_t)((int64_t)M.num_patches * k / kSlices);
+}
+
+// first linear vertex / edge / face of patch p (the total for p = num_patches)
+static int64_t v_first(const Mesh& M, int32_t p) { return p < M.num_patches ? M.hdr[p].v_base : M.nv; }
+static int64_t e_first(const Mesh& M, int32_t p) { return p < M.num_patches ? M.hdr[p].e_base : M.ne; }
+static int64_t f_first(const Mesh& M, int32_t p) { return p < M.num_patches ? M.hdr[p].f_base : M.nf; }
 
 }  // namespace rxg
 
@@ -570,11 +632,36 @@ rxg_status rxg_query(const rxg_mesh* h, int32_t op, int32_t* offsets, int32_t* v
     const size_t off_bytes = csr ? (size_t)(rows + 1) * 4 : 0, val_bytes = (size_t)nval * 4;
     if ((st = stage_out(csr ? offsets : nullptr, off_bytes, s, so))) return st;
     if ((st = stage_out(values, val_bytes, s, sv))) return st;
-    if ((st = launch_query(&h->m, op, (int32_t*)so.d, (int32_t*)sv.d, s))) return st;
-    if (csr && (st = finish_out(offsets, so, off_bytes, s))) return st;
-    if ((st = finish_out(values, sv, val_bytes, s))) return st;
-    if (so.owns || sv.owns) RXG_CUDA_TRY(cudaStreamSynchronize(s));
-    return RXG_OK;
+    const Mesh& M = h->m;
+    if (!so.owns && !sv.owns) return launch_query(&M, op, (int32_t*)so.d, (int32_t*)sv.d, s);
+    // host outputs: sliced launch, each slice's rows copied while the next runs
+    int32_t pb[kSlices + 1];
+    slice_patches(M, pb);
+    std::vector<HostPiece> pieces;
+    if (csr && so.owns) {
+        HostPiece q{(char*)offsets, (const char*)so.d, 4, {}};
+        for (int k = 0; k <= kSlices; ++k) q.eb.push_back(k == kSlices ? rows + 1 : v_first(M, pb[k]));
+        pieces.push_back(q);
+    }
+    if (sv.owns) {
+        HostPiece q{(char*)values, (const char*)sv.d, 4, {}};
+        for (int k = 0; k <= kSlices; ++k) {
+            const int32_t p = pb[k];
+            int64_t       e;
+            if (op == RXG_OP_FV) e = 3 * f_first(M, p);
+            else if (op == RXG_OP_EV) e = 2 * e_first(M, p);
+            else if (p == M.num_patches) e = nval;
+            else e = op == RXG_OP_VF ? M.hdr[p].vf_base : M.hdr[p].vv_base;
+            q.eb.push_back(e);
+        }
+        pieces.push_back(q);
+    }
+    st = run_to_host(M, s, pb,
+                     [&](PatchRange r) {
+                         return launch_query_range(&M, op, (int32_t*)so.d, (int32_t*)sv.d, s, r);
+                     },
+                     pieces);
+    return st;
 }
 
 rxg_status rxg_vertex_normals(const rxg_mesh* h, int32_t weighting, const float* xyz, float* out,
@@ -590,10 +677,22 @@ rxg_status rxg_vertex_normals(const rxg_mesh* h, int32_t weighting, const float*
     rxg_status   st;
     if ((st = stage_in(xyz, bytes, s, si))) return st;
     if ((st = stage_out(out, bytes, s, so))) return st;
-    if ((st = launch_normals(&h->m, weighting, (const float*)si.d, (float*)so.d, s))) return st;
-    if ((st = finish_out(out, so, bytes, s))) return st;
-    if (si.owns || so.owns) RXG_CUDA_TRY(cudaStreamSynchronize(s));
-    return RXG_OK;
+    const Mesh& M = h->m;
+    if (!so.owns) {
+        st = launch_normals(&M, weighting, (const float*)si.d, (float*)so.d, s,
+                            PatchRange{0, M.num_patches});
+        if (st == RXG_OK && si.owns) RXG_CUDA_TRY(cudaStreamSynchronize(s));
+        return st;
+    }
+    int32_t pb[kSlices + 1];
+    slice_patches(M, pb);
+    std::vector<HostPiece> pieces(1, HostPiece{(char*)out, (const char*)so.d, 12, {}});
+    for (int k = 0; k <= kSlices; ++k) pieces[0].eb.push_back(v_first(M, pb[k]));
+    return run_to_host(M, s, pb,
+                       [&](PatchRange r) {
+                           return launch_normals(&M, weighting, (const float*)si.d, (float*)so.d, s, r);
+                       },
+                       pieces);
 }
 
 // Syncs `stream`, reads and clears the device error word set by bounded waits.

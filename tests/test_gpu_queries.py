@@ -60,17 +60,33 @@ def test_queries_bit_exact(oracle, name, patch):
     device_check()
 
 
-def test_query_into_host_buffers(oracle):
-    from rxmesh_gb300 import Op, RXMeshStatic
-    x, f = meshgen.icosphere(3)
-    rx = RXMeshStatic(f, len(x), patch_size=128)
-    rows, nval = rx.query_size(Op.VV)
-    off = np.empty(rows + 1, np.int32)
-    val = np.empty(nval, np.int32)
-    rx.query_host(Op.VV, off, val)
-    d_off, d_val = rx.query(Op.VV)
-    assert np.array_equal(off, d_off.cpu().numpy())
-    assert sorted_rows(off, val) == sorted_rows(off, d_val.cpu().numpy())
+@pytest.mark.parametrize("level,patch", [(3, 128), (5, 128)])
+def test_query_into_host_buffers(oracle, level, patch):
+    """Host outputs (sliced launches, copies overlapped) equal the device outputs."""
+    import ctypes
+    from rxmesh_gb300 import Op, RXMeshStatic, _lib
+    x, f = meshgen.icosphere(level)
+    rx = RXMeshStatic(f, len(x), patch_size=patch)
+    for op in (Op.VV, Op.VE, Op.VF, Op.FV, Op.EV):
+        rows, nval = rx.query_size(op)
+        csr = op <= Op.VF
+        off = np.full(rows + 1, -7, np.int32) if csr else None
+        val = np.full(nval, -7, np.int32)
+        rx.query_host(op, off, val)
+        d_off, d_val = rx.query(op)
+        if csr:  # rows are sets (their order comes from shared-memory atomics)
+            assert np.array_equal(off, d_off.cpu().numpy()), op
+            assert sorted_rows(off, val) == sorted_rows(off, d_val.cpu().numpy()), op
+        else:
+            assert np.array_equal(val, d_val.cpu().numpy()), op
+    # normals: host positions in, host normals out
+    x32 = np.ascontiguousarray(rx.to_linear(torch.tensor(x, device="cuda")).cpu().numpy(), np.float32)
+    out = np.full_like(x32, np.nan)
+    L = _lib.load()
+    _lib.check(L.rxg_vertex_normals(rx._h, 1, ctypes.c_void_p(x32.ctypes.data),
+                                    ctypes.c_void_p(out.ctypes.data), None))
+    dev = rx.vertex_normals(torch.tensor(x32, device="cuda"), "area").cpu().numpy()
+    assert np.allclose(out, dev, rtol=1e-6, atol=1e-7)
 
 
 @pytest.mark.parametrize("name", ["sphere3", "torus", "cloth", "bunnyhead"])
