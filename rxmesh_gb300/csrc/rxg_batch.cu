@@ -5,16 +5,15 @@
 // range of linear vertex ids (the reference packs several meshes into one
 // RXMeshStatic the same way, rxmesh_static.cu:66-160).
 //
-// Scheduling.  A mesh is a job for a gang of k CTAs, k = ceil(rows / tile),
-// so a 65 K-vertex grid is solved by 16 SMs while a 162-vertex sphere gets one
-// CTA.  The host builds a gang schedule once per (CTA shape, tile): jobs in
-// longest-first order each take the k CTAs that become free first (list
-// scheduling), and every CTA walks its own jobs in the order of their planned
-// start.  All CTAs share that one order, so a CTA can wait for the other
-// members of its gang without a deadlock; the launch is cooperative, so all
-// of them are resident.  A gang synchronises through its own ticket counter
-// (rxg_gridsum.cuh protocol with the gang's size), a one-CTA job only with
-// __syncthreads.
+// Scheduling.  A mesh is a job for a gang of k CTAs: enough that no CTA holds
+// more rows than the tile (its PCG state lives in shared memory) and that no
+// job runs longer than half the ideal makespan.  Gangs run in waves: the
+// host packs them longest first into waves of G CTAs, and all CTAs start
+// each wave together after a grid barrier, so a gang's members arrive at
+// once.  One-CTA jobs then come off a queue, largest first.  A gang
+// synchronises through its own ticket counter (rxg_gridsum.cuh protocol with
+// the gang's size), a one-CTA job only with __syncthreads; the launch is
+// cooperative, so every CTA is resident.
 //
 // Per job, all flow steps run inside the launch: FP32 cotangent assembly (FP64
 // for near-degenerate triangles and near-right Voronoi corners), FP64
@@ -39,21 +38,23 @@ namespace rxg {
 // one gang schedule (device arrays), built for a grid of G CTAs
 struct GangPlan
 {
-    int      G = 0, bt = 0, bps = 0, tile = 0, kmax = 1, njobs = 0;
+    int      G = 0, bt = 0, bps = 0, tile = 0, kmax = 1, njobs = 0, cp = 0, nwaves = 0, nsingle = 0;
+    size_t   smem  = 0;  // dynamic shared memory per CTA
+    int      hints = 0;  // built with measured iteration counts
     int32_t* d_job_mesh  = nullptr;  // per job: mesh
     int32_t* d_job_k     = nullptr;  // per job: CTAs in its gang
-    int32_t* d_cta_off   = nullptr;  // G+1: CTA b walks entries [off[b], off[b+1])
-    int32_t* d_cta_job   = nullptr;  // per entry: job
-    int32_t* d_cta_rank  = nullptr;  // per entry: rank of the CTA in the job's gang
-    unsigned* d_bar      = nullptr;  // 4 words per job (ticket, abort)
-    double*   d_part     = nullptr;  // 2 * kmax per job
+    int32_t* d_wave_job  = nullptr;  // nwaves x G: the gang job CTA c runs in wave w, or -1
+    int32_t* d_wave_rank = nullptr;  // nwaves x G: its rank in that gang
+    int32_t* d_single    = nullptr;  // one-CTA jobs, largest first, taken from a queue
+    unsigned* d_bar      = nullptr;  // 4 words per job, 4 for the grid barrier, 1 queue counter
+    double*   d_part     = nullptr;  // 2 * kmax per job, then 2 * G for the grid barrier
     void free_all()
     {
         cudaFree(d_job_mesh);
         cudaFree(d_job_k);
-        cudaFree(d_cta_off);
-        cudaFree(d_cta_job);
-        cudaFree(d_cta_rank);
+        cudaFree(d_wave_job);
+        cudaFree(d_wave_rank);
+        cudaFree(d_single);
         cudaFree(d_bar);
         cudaFree(d_part);
         *this = GangPlan();
@@ -77,6 +78,7 @@ struct rxg_batch
     int32_t              threads  = 512;
     int32_t              blocks_per_sm = 1;
     int32_t              tile          = 4096;
+    std::vector<int32_t> iters_hint;  // PCG iterations per mesh seen by the autotuner (0: unknown)
     rxg::GangPlan        plan;
     std::mutex           mu;
 };
@@ -89,12 +91,14 @@ struct BatchArgs
     const int32_t*    vcount;
     const int32_t*    job_mesh;
     const int32_t*    job_k;
-    const int32_t*    cta_off;
-    const int32_t*    cta_job;
-    const int32_t*    cta_rank;
+    int               nwaves, nsingle, njobs;
+    const int32_t*    wave_job;
+    const int32_t*    wave_rank;
+    const int32_t*    single;
     unsigned*         bar;
     double*           part;
     int               kmax;
+    int32_t           cp;    // shared-memory stride of one component (>= any CTA's rows)
     const int32_t*    row_ptr;
     const int32_t*    col;
     const int8_t*     bnd;
@@ -102,10 +106,7 @@ struct BatchArgs
     Ent<float>*       ent;   // CSR entries (W = 0) or slot-major ELL of width W
     R4<double>*       X;
     R4<double>*       B;
-    R4<float>*        P;
-    R4<float>*        S;
-    R4<float>*        Z;
-    R4<float>*        D;
+    R4<float>*        Z;     // z = D^-1 r of every row (read by the other CTAs of a gang)
     float*            dinv;
     double*           diag;  // FP64 diagonal (2*area + sum of the FP32 weights)
     float             dt;
@@ -186,32 +187,57 @@ __device__ __forceinline__ void assemble_row(int64_t p, const BatchArgs& a)
     a.B[p]  = b;
 }
 
-// r = B - A x in FP64 for rows [r0, r1) (FP32 off-diagonals promoted, FP64
-// diagonal), z = D^-1 r into Z, d = 0; returns the thread's r . diag^-1 r
+// Per job, the CTA keeps its rows' PCG state in shared memory (the on-chip
+// solver's layout, rxg_onchip.cu): p, s, z = D^-1 r, d (3 floats each) and
+// D^-1, 52 bytes a row.  Neighbours inside the CTA's own rows are gathered
+// from shared memory, the others (rows of the same mesh on another CTA of
+// its gang) from the global z.
+struct BatchSmem
+{
+    float *Px, *Py, *Pz, *Sx, *Sy, *Sz, *Zx, *Zy, *Zz, *Dx, *Dy, *Dz, *Dv;
+};
+
+// entry u of row i (ELL slot, or CSR position within the row)
 template <int W>
-__device__ __forceinline__ double batch_residual(int64_t r0, int64_t r1, int bt, const BatchArgs& a)
+__device__ __forceinline__ int32_t row_len(const BatchArgs& a, int64_t i)
+{
+    return W ? W : a.row_ptr[i + 1] - a.row_ptr[i];
+}
+template <int W>
+__device__ __forceinline__ Ent<float> row_ent(const BatchArgs& a, int64_t i, int32_t u)
+{
+    return a.ent[W ? u * a.n + i : a.row_ptr[i] + u];
+}
+
+// r = B - A x in FP64 for rows [r0, r0 + m) (FP32 off-diagonals promoted,
+// FP64 diagonal), z = D^-1 r into shared memory and the global z, d = 0;
+// returns the thread's r . D^-1 r
+template <int BT, int W>
+__device__ __forceinline__ double batch_residual(int64_t r0, int m, const BatchArgs& a,
+                                                 const BatchSmem& q)
 {
     double part = 0;
-    for (int64_t i = r0 + threadIdx.x; i < r1; i += bt) {
+    for (int l = threadIdx.x; l < m; l += BT) {
+        const int64_t    i  = r0 + l;
         const R4<double> xi = a.X[i];
         const double     dg = a.diag[i];
         double           a0 = dg * xi.x, a1 = dg * xi.y, a2 = dg * xi.z;
-        const int32_t    b0 = W ? 1 : a.row_ptr[i] + 1, e = W ? W : a.row_ptr[i + 1];
-        for (int32_t j = b0; j < e; ++j) {
-            const Ent<float> q  = a.ent[W ? j * a.n + i : j];
-            const R4<double> xv = a.X[q.col];
-            a0 += (double)q.val * xv.x;
-            a1 += (double)q.val * xv.y;
-            a2 += (double)q.val * xv.z;
+        const int32_t    len = row_len<W>(a, i);
+        for (int32_t u = 1; u < len; ++u) {
+            const Ent<float> e  = row_ent<W>(a, i, u);
+            const R4<double> xv = a.X[e.col];
+            a0 += (double)e.val * xv.x;
+            a1 += (double)e.val * xv.y;
+            a2 += (double)e.val * xv.z;
         }
         const R4<double> b  = a.B[i];
         const double     e0 = b.x - a0, e1 = b.y - a1, e2 = b.z - a2;
-        const float      di = a.dinv[i];
-        R4<float>        z, zero;
+        const float      di = q.Dv[l];
+        R4<float>        z;
         z.x = di * (float)e0, z.y = di * (float)e1, z.z = di * (float)e2, z.w = 0.f;
-        zero.x = zero.y = zero.z = zero.w = 0.f;
+        q.Zx[l] = z.x, q.Zy[l] = z.y, q.Zz[l] = z.z;
+        q.Dx[l] = q.Dy[l] = q.Dz[l] = 0.f;
         a.Z[i] = z;
-        a.D[i] = zero;
         part += (e0 * e0 + e1 * e1 + e2 * e2) * (double)di;  // ~ / diag, no FP64 divide
     }
     return part;
@@ -230,12 +256,13 @@ struct BatchShared
     int   first, replace, stop;
 };
 
-// all flow steps of one mesh, rows [r0, r1) of it on this CTA, gang g
+// all flow steps of one mesh, rows [r0, r0 + m) of it on this CTA, gang g
 template <int BT, int W>
-__device__ bool batch_job(int64_t r0, int64_t r1, const BatchArgs& a, GridSum& g, RedSmem& red,
-                          BatchScalars& c, BatchShared& sh)
+__device__ bool batch_job(int64_t r0, int m, const BatchArgs& a, const BatchSmem& q, GridSum& g,
+                          RedSmem& red, BatchScalars& c, BatchShared& sh)
 {
-    const double target = a.tol * a.tol;
+    const double  target = a.tol * a.tol;
+    const int32_t r0i    = (int32_t)r0;
     if (threadIdx.x == 0) {
         c.total    = 0;
         c.conv_all = true;
@@ -243,9 +270,13 @@ __device__ bool batch_job(int64_t r0, int64_t r1, const BatchArgs& a, GridSum& g
     for (int step = 0; step < a.nsteps; ++step) {
         // positions of the whole mesh are final (the previous step ended with
         // a gang barrier after its last x update)
-        for (int64_t p = r0 + threadIdx.x; p < r1; p += BT) assemble_row<W>(p, a);
+        for (int l = threadIdx.x; l < m; l += BT) {
+            assemble_row<W>(r0 + l, a);
+            q.Dv[l] = a.dinv[r0 + l];
+            q.Px[l] = q.Py[l] = q.Pz[l] = q.Sx[l] = q.Sy[l] = q.Sz[l] = 0.f;
+        }
         __syncthreads();
-        if (!grid_sum<BT>(batch_residual<W>(r0, r1, BT, a), g, red, [&](double t) {
+        if (!grid_sum<BT>(batch_residual<BT, W>(r0, m, a, q), g, red, [&](double t) {
                 c.rr0 = c.rr = c.delta = c.rep = t;
                 c.it                           = 0;
                 c.conv                         = !(t > 0.0);
@@ -259,48 +290,60 @@ __device__ bool batch_job(int64_t r0, int64_t r1, const BatchArgs& a, GridSum& g
             const bool  first = sh.first != 0;
             // s = A z + beta s, p = z + beta p, s . p
             float tp = 0.f;
-            for (int64_t i = r0 + threadIdx.x; i < r1; i += BT) {
-                float ax = 0.f, ay = 0.f, az = 0.f;
-                if (W) {
-                    Ent<float> q[W ? W : 1];
+            for (int l = threadIdx.x; l < m; l += BT) {
+                const int64_t i   = r0 + l;
+                const int32_t len = row_len<W>(a, i);
+                float         ax = 0.f, ay = 0.f, az = 0.f;
+                for (int32_t u0 = 0; u0 < len; u0 += 8) {
+                    Ent<float> e[8];
 #pragma unroll
-                    for (int u = 0; u < W; ++u) q[u] = a.ent[u * a.n + i];
-#pragma unroll
-                    for (int u = 0; u < W; ++u) {
-                        const R4<float> zv = a.Z[q[u].col];
-                        ax += q[u].val * zv.x, ay += q[u].val * zv.y, az += q[u].val * zv.z;
+                    for (int u = 0; u < 8; ++u) {
+                        if (u0 + u < len) {
+                            e[u] = row_ent<W>(a, i, u0 + u);
+                        } else {
+                            e[u].col = (int32_t)i;
+                            e[u].val = 0.f;
+                        }
                     }
-                } else {
-                    row_spmv4<float>(a.row_ptr, a.ent, i, a.Z, ax, ay, az, (float*)nullptr);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int32_t lc = e[u].col - r0i;
+                        float         zx, zy, zz;
+                        if ((uint32_t)lc < (uint32_t)m) {
+                            zx = q.Zx[lc], zy = q.Zy[lc], zz = q.Zz[lc];
+                        } else {
+                            const R4<float> zv = a.Z[e[u].col];
+                            zx = zv.x, zy = zv.y, zz = zv.z;
+                        }
+                        ax += e[u].val * zx, ay += e[u].val * zy, az += e[u].val * zz;
+                    }
                 }
-                const R4<float> zi = a.Z[i];
-                R4<float>       si, pi;
+                const float zx = q.Zx[l], zy = q.Zy[l], zz = q.Zz[l];
+                float       sx, sy, sz, px, py, pz;
                 if (first) {
-                    si.x = ax, si.y = ay, si.z = az;
-                    pi = zi;
+                    sx = ax, sy = ay, sz = az;
+                    px = zx, py = zy, pz = zz;
                 } else {
-                    const R4<float> so = a.S[i], po = a.P[i];
-                    si.x = ax + bt * so.x, si.y = ay + bt * so.y, si.z = az + bt * so.z;
-                    pi.x = zi.x + bt * po.x, pi.y = zi.y + bt * po.y, pi.z = zi.z + bt * po.z;
+                    sx = ax + bt * q.Sx[l], sy = ay + bt * q.Sy[l], sz = az + bt * q.Sz[l];
+                    px = zx + bt * q.Px[l], py = zy + bt * q.Py[l], pz = zz + bt * q.Pz[l];
                 }
-                si.w = pi.w = 0.f;
-                a.S[i] = si;
-                a.P[i] = pi;
-                tp += si.x * pi.x + si.y * pi.y + si.z * pi.z;
+                q.Sx[l] = sx, q.Sy[l] = sy, q.Sz[l] = sz;
+                q.Px[l] = px, q.Py[l] = py, q.Pz[l] = pz;
+                tp += sx * px + sy * py + sz * pz;
             }
             if (!grid_sum<BT>(tp, g, red, [&](double sp) { sh.al = (float)(c.delta / sp); })) return false;
             const float al = sh.al;
             // d += alpha p, z -= alpha D^-1 s, r . z
             tp = 0.f;
-            for (int64_t i = r0 + threadIdx.x; i < r1; i += BT) {
-                const float     di = a.dinv[i];
-                const R4<float> pi = a.P[i], si = a.S[i];
-                R4<float>       d = a.D[i], z = a.Z[i];
-                d.x += al * pi.x, d.y += al * pi.y, d.z += al * pi.z;
+            for (int l = threadIdx.x; l < m; l += BT) {
+                const float di = q.Dv[l];
+                q.Dx[l] += al * q.Px[l], q.Dy[l] += al * q.Py[l], q.Dz[l] += al * q.Pz[l];
                 const float ad = al * di;
-                z.x -= ad * si.x, z.y -= ad * si.y, z.z -= ad * si.z;
-                a.D[i] = d;
-                a.Z[i] = z;
+                R4<float>   z;
+                z.x = q.Zx[l] - ad * q.Sx[l], z.y = q.Zy[l] - ad * q.Sy[l], z.z = q.Zz[l] - ad * q.Sz[l];
+                z.w = 0.f;
+                q.Zx[l] = z.x, q.Zy[l] = z.y, q.Zz[l] = z.z;
+                a.Z[r0 + l] = z;
                 tp += __fdividef(z.x * z.x + z.y * z.y + z.z * z.z, di);
             }
             if (!grid_sum<BT>(tp, g, red, [&](double dn) {
@@ -315,14 +358,13 @@ __device__ bool batch_job(int64_t r0, int64_t r1, const BatchArgs& a, GridSum& g
                 }))
                 return false;
             if (sh.replace) {
-                for (int64_t i = r0 + threadIdx.x; i < r1; i += BT) {
-                    R4<double>      x = a.X[i];
-                    const R4<float> d = a.D[i];
-                    x.x += (double)d.x, x.y += (double)d.y, x.z += (double)d.z;
-                    a.X[i] = x;
+                for (int l = threadIdx.x; l < m; l += BT) {
+                    R4<double> x = a.X[r0 + l];
+                    x.x += (double)q.Dx[l], x.y += (double)q.Dy[l], x.z += (double)q.Dz[l];
+                    a.X[r0 + l] = x;
                 }
                 if (!grid_sum<BT>(0.f, g, red, [](double) {})) return false;
-                if (!grid_sum<BT>(batch_residual<W>(r0, r1, BT, a), g, red, [&](double t) {
+                if (!grid_sum<BT>(batch_residual<BT, W>(r0, m, a, q), g, red, [&](double t) {
                         c.rr     = t;
                         c.conv   = t < target * c.rr0;
                         sh.stop  = c.conv || c.total + c.it >= a.max_iter || !(t > 0.0);
@@ -347,23 +389,56 @@ __device__ bool batch_job(int64_t r0, int64_t r1, const BatchArgs& a, GridSum& g
 template <int BT, int W, int MINB>
 __global__ void __launch_bounds__(BT, MINB) k_mcf_batch(BatchArgs a)
 {
+    extern __shared__ __align__(16) float sm[];
     __shared__ RedSmem      red;
     __shared__ BatchScalars c;
     __shared__ BatchShared  sh;
-    for (int32_t e = a.cta_off[blockIdx.x]; e < a.cta_off[blockIdx.x + 1]; ++e) {
-        const int32_t job = a.cta_job[e], rank = a.cta_rank[e];
-        const int32_t m = a.job_mesh[job], k = a.job_k[job];
-        const int64_t v0 = a.vstart[m], nv = a.vcount[m];
-        const int64_t chunk = (nv + k - 1) / k;
-        const int64_t lo    = rank * chunk, hi = lo + chunk;
-        const int64_t r0    = v0 + (lo < nv ? lo : nv);
-        const int64_t r1    = v0 + (hi < nv ? hi : nv);
-        GridSum       g{a.bar + 4 * job, a.part + 2 * a.kmax * job, a.err, (unsigned)k, 0u,
-                  (unsigned)rank};
-        if (!batch_job<BT, W>(r0, r1, a, g, red, c, sh)) return;
-        if (rank == 0 && threadIdx.x == 0) {
-            a.iters[m] = c.total;
-            a.conv[m]  = c.conv_all ? 1 : 0;
+    const int32_t cp = a.cp;
+    BatchSmem     q;
+    q.Px = sm, q.Py = q.Px + cp, q.Pz = q.Py + cp;
+    q.Sx = q.Pz + cp, q.Sy = q.Sx + cp, q.Sz = q.Sy + cp;
+    q.Zx = q.Sz + cp, q.Zy = q.Zx + cp, q.Zz = q.Zy + cp;
+    q.Dx = q.Zz + cp, q.Dy = q.Dx + cp, q.Dz = q.Dy + cp;
+    q.Dv = q.Dz + cp;
+    __shared__ int s_job;
+    GridSum         grid{a.bar + 4 * a.njobs, a.part + 2 * a.kmax * a.njobs, a.err, gridDim.x, 0u,
+                 blockIdx.x};
+    // waves of gangs: every CTA takes part in every wave barrier
+    for (int w = 0; w < a.nwaves; ++w) {
+        const int32_t job = a.wave_job[w * gridDim.x + blockIdx.x];
+        if (job >= 0) {
+            const int32_t rank = a.wave_rank[w * gridDim.x + blockIdx.x];
+            const int32_t mesh = a.job_mesh[job], k = a.job_k[job];
+            const int64_t v0 = a.vstart[mesh], nv = a.vcount[mesh];
+            const int64_t chunk = (nv + k - 1) / k;
+            const int64_t lo    = rank * chunk, hi = lo + chunk;
+            const int64_t r0    = v0 + (lo < nv ? lo : nv);
+            const int64_t r1    = v0 + (hi < nv ? hi : nv);
+            GridSum       g{a.bar + 4 * job, a.part + 2 * a.kmax * job, a.err, (unsigned)k, 0u,
+                      (unsigned)rank};
+            if (!batch_job<BT, W>(r0, (int)(r1 - r0), a, q, g, red, c, sh)) return;
+            if (rank == 0 && threadIdx.x == 0) {
+                a.iters[mesh] = c.total;
+                a.conv[mesh]  = c.conv_all ? 1 : 0;
+            }
+        }
+        if (!grid_sum<BT>(0.f, grid, red, [](double) {})) return;
+    }
+    // one-CTA jobs from a queue, largest first
+    unsigned* queue = a.bar + 4 * a.njobs + 4;
+    while (true) {
+        if (threadIdx.x == 0) s_job = (int)atomicAdd(queue, 1u);
+        __syncthreads();
+        const int t = s_job;
+        __syncthreads();
+        if (t >= a.nsingle) break;
+        const int32_t job  = a.single[t];
+        const int32_t mesh = a.job_mesh[job];
+        GridSum       g{a.bar + 4 * job, a.part + 2 * a.kmax * job, a.err, 1u, 0u, 0u};
+        if (!batch_job<BT, W>(a.vstart[mesh], a.vcount[mesh], a, q, g, red, c, sh)) return;
+        if (threadIdx.x == 0) {
+            a.iters[mesh] = c.total;
+            a.conv[mesh]  = c.conv_all ? 1 : 0;
         }
     }
 }
@@ -415,75 +490,112 @@ static const void* batch_kernel(int bt, int w, int bps)
 #undef RXG_BK
 }
 
-static int max_per_sm(int bt, int w, int bps)
+static int max_per_sm(int bt, int w, int bps, size_t smem = 0)
 {
-    int per = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_kernel(bt, w, bps), bt, 0) !=
-        cudaSuccess)
-        per = 1;
-    return std::max(1, per);
+    const void* kern = batch_kernel(bt, w, bps);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, bt, smem) != cudaSuccess) per = 0;
+    return per;
 }
 
-constexpr int kGangMax = 32;  // most CTAs one mesh is split across
+constexpr int kGangMax     = 64;    // most CTAs one mesh is split across
+constexpr int kBatchStatic = 1024;  // static shared memory of the kernel, with slack
 
-// Gang schedule for G CTAs and the given tile (rows per CTA): longest job
-// first, each onto the k CTAs that are free first; a job's start is the
-// latest of their finish times.  Cost model: rows^1.5 (rows x the ~sqrt(rows)
-// PCG iterations of a mesh Laplacian system).
+static int batch_optin_smem()
+{
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return optin;
+}
+
+// Schedule for G CTAs and the given tile (most rows per CTA).  A job's work
+// is rows x PCG iterations: the iterations the autotuner measured when
+// known, else sqrt(rows) (a mesh Laplacian's PCG count grows like its
+// diameter).
 static int batch_ell_width(const rxg_batch* b);
 
 static rxg_status build_plan(rxg_batch* b, int bt, int bps, int tile, GangPlan* out)
 {
-    const int G = batch_sms() * std::min(bps, max_per_sm(bt, batch_ell_width(b), bps));
-    const int nm = b->nmesh;
-    std::vector<int32_t> order(nm);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int32_t x, int32_t y) { return b->vcount[x] > b->vcount[y]; });
-    std::vector<int32_t> job_mesh(nm), job_k(nm);  // jobs in longest-first order
-    std::vector<double>  start(nm);
-    std::vector<std::vector<int32_t>> members(nm);
-    using Slot = std::pair<double, int32_t>;  // (free at, CTA)
-    std::priority_queue<Slot, std::vector<Slot>, std::greater<Slot>> freeq;
-    for (int c = 0; c < G; ++c) freeq.push({0.0, c});
-    int kmax = 1;
-    for (int j = 0; j < nm; ++j) {
-        const int32_t m = order[j];
-        const int     k = (int)std::max<int64_t>(
-            1, std::min<int64_t>({(b->vcount[m] + tile - 1) / tile, (int64_t)kGangMax, (int64_t)G}));
-        kmax = std::max(kmax, k);
-        double t0 = 0.0;
-        for (int i = 0; i < k; ++i) {
-            const Slot s = freeq.top();
-            freeq.pop();
-            members[j].push_back(s.second);
-            t0 = std::max(t0, s.first);
-        }
-        // a mesh's PCG takes ~sqrt(rows) iterations, so its work grows as rows^1.5
-        const double t1 = t0 + std::pow((double)b->vcount[m], 1.5) / k;
-        for (int32_t c : members[j]) freeq.push({t1, c});
-        job_mesh[j] = m;
-        job_k[j]    = k;
-        start[j]    = t0;
+    const int  w    = batch_ell_width(b);
+    const int  nm   = b->nmesh;
+    const bool hint = (int)b->iters_hint.size() == nm;
+    std::vector<double> it(nm), work(nm);
+    double              total = 0.0;
+    for (int m = 0; m < nm; ++m) {
+        it[m]   = hint && b->iters_hint[m] > 0 ? (double)b->iters_hint[m] : std::sqrt((double)b->vcount[m]);
+        work[m] = it[m] * (double)b->vcount[m];
+        total += work[m];
     }
-    // every CTA walks its jobs in the one global order (planned start, job)
-    std::vector<int32_t> jobs_by_start(nm);
-    std::iota(jobs_by_start.begin(), jobs_by_start.end(), 0);
-    std::stable_sort(jobs_by_start.begin(), jobs_by_start.end(),
-                     [&](int32_t x, int32_t y) { return start[x] < start[y]; });
-    std::vector<std::vector<std::pair<int32_t, int32_t>>> per(G);  // (job, rank)
-    for (int32_t j : jobs_by_start)
-        for (int r = 0; r < (int)members[j].size(); ++r) per[members[j][r]].push_back({j, r});
-    std::vector<int32_t> off(G + 1, 0), cjob, crank;
-    for (int c = 0; c < G; ++c) {
-        off[c + 1] = off[c] + (int32_t)per[c].size();
-        for (auto& e : per[c]) {
-            cjob.push_back(e.first);
-            crank.push_back(e.second);
+    // rows per CTA bound the shared memory: 13 floats a row
+    const int optin = batch_optin_smem();
+    const int G     = batch_sms() * bps;
+    // gang sizes
+    std::vector<int32_t> kk(nm);
+    int                  kmax      = 1;
+    int64_t              max_chunk = 1;
+    for (int m = 0; m < nm; ++m) {
+        const int64_t nv = b->vcount[m];
+        int64_t       k  = (nv + tile - 1) / tile;
+        k = std::max<int64_t>(k, (int64_t)std::ceil(work[m] * G / (0.5 * total)));
+        k = std::max<int64_t>(1, std::min<int64_t>({k, (int64_t)kGangMax, (int64_t)G, nv}));
+        kk[m]     = (int32_t)k;
+        kmax      = std::max(kmax, (int)k);
+        max_chunk = std::max(max_chunk, (nv + k - 1) / k);
+    }
+    const int    cp   = (int)((max_chunk + 31) & ~int64_t(31));
+    const size_t smem = (size_t)13 * 4 * cp;
+    if ((int64_t)smem + kBatchStatic > optin || max_per_sm(bt, w, bps, smem) < bps) {
+        set_error("rxg_batch: %d CTAs of %d threads per SM with %lld rows each do not fit an SM",
+                  bps, bt, (long long)max_chunk);
+        return RXG_ERR_UNSUPPORTED;
+    }
+    // Gangs (k >= 2) run in waves that start together after a grid barrier,
+    // longest first, first-fit into G CTAs; one-CTA jobs then come off a queue,
+    // largest first, so their durations need no estimate.
+    const double         sync_rows = 1000.0;  // a gang's two grid sums, in row-iterations
+    std::vector<int32_t> gangs, singles;
+    for (int m = 0; m < nm; ++m) (kk[m] > 1 ? gangs : singles).push_back(m);
+    auto dur = [&](int32_t m) { return work[m] / kk[m] + (kk[m] > 1 ? it[m] * sync_rows : 0.0); };
+    std::stable_sort(gangs.begin(), gangs.end(), [&](int32_t x, int32_t y) { return dur(x) > dur(y); });
+    std::stable_sort(singles.begin(), singles.end(), [&](int32_t x, int32_t y) { return work[x] > work[y]; });
+    std::vector<std::vector<int32_t>> waves;
+    std::vector<int>                  used;
+    for (int32_t m : gangs) {
+        size_t wv = 0;
+        while (wv < waves.size() && used[wv] + kk[m] > G) ++wv;
+        if (wv == waves.size()) {
+            waves.emplace_back();
+            used.push_back(0);
         }
+        waves[wv].push_back(m);
+        used[wv] += kk[m];
+    }
+    // jobs: gangs in wave order, then the singles; job index = position
+    std::vector<int32_t> job_mesh, job_k, wave_job(waves.size() * (size_t)G, -1),
+        wave_rank(waves.size() * (size_t)G, 0), single;
+    for (size_t wv = 0; wv < waves.size(); ++wv) {
+        int c = 0;
+        for (int32_t m : waves[wv]) {
+            const int32_t job = (int32_t)job_mesh.size();
+            job_mesh.push_back(m);
+            job_k.push_back(kk[m]);
+            for (int r = 0; r < kk[m]; ++r, ++c) {
+                wave_job[wv * G + c]  = job;
+                wave_rank[wv * G + c] = r;
+            }
+        }
+    }
+    for (int32_t m : singles) {
+        single.push_back((int32_t)job_mesh.size());
+        job_mesh.push_back(m);
+        job_k.push_back(1);
     }
     GangPlan p;
     p.G = G, p.bt = bt, p.bps = bps, p.tile = tile, p.kmax = kmax, p.njobs = nm;
+    p.cp = cp, p.smem = smem, p.hints = hint ? 1 : 0;
+    p.nwaves = (int)waves.size(), p.nsingle = (int)single.size();
     auto up = [](int32_t** d, const std::vector<int32_t>& h) -> cudaError_t {
         cudaError_t e = cudaMalloc(d, std::max<size_t>(h.size(), 1) * 4);
         if (e == cudaSuccess && !h.empty())
@@ -492,11 +604,11 @@ static rxg_status build_plan(rxg_batch* b, int bt, int bps, int tile, GangPlan* 
     };
     cudaError_t e = up(&p.d_job_mesh, job_mesh);
     if (e == cudaSuccess) e = up(&p.d_job_k, job_k);
-    if (e == cudaSuccess) e = up(&p.d_cta_off, off);
-    if (e == cudaSuccess) e = up(&p.d_cta_job, cjob);
-    if (e == cudaSuccess) e = up(&p.d_cta_rank, crank);
-    if (e == cudaSuccess) e = cudaMalloc(&p.d_bar, sizeof(unsigned) * 4 * nm);
-    if (e == cudaSuccess) e = cudaMalloc(&p.d_part, sizeof(double) * 2 * kmax * nm);
+    if (e == cudaSuccess) e = up(&p.d_wave_job, wave_job);
+    if (e == cudaSuccess) e = up(&p.d_wave_rank, wave_rank);
+    if (e == cudaSuccess) e = up(&p.d_single, single);
+    if (e == cudaSuccess) e = cudaMalloc(&p.d_bar, sizeof(unsigned) * (4 * nm + 8));
+    if (e == cudaSuccess) e = cudaMalloc(&p.d_part, sizeof(double) * (2 * kmax * nm + 2 * G));
     if (e != cudaSuccess) {
         p.free_all();
         return cuda_status(e, "rxg_batch: gang schedule");
@@ -509,7 +621,10 @@ static rxg_status build_plan(rxg_batch* b, int bt, int bps, int tile, GangPlan* 
 static rxg_status ensure_plan(rxg_batch* b, int bt, int bps, int tile)
 {
     std::lock_guard<std::mutex> g(b->mu);
-    if (b->plan.G && b->plan.bt == bt && b->plan.bps == bps && b->plan.tile == tile) return RXG_OK;
+    const int hints = (int)b->iters_hint.size() == b->nmesh ? 1 : 0;
+    if (b->plan.G && b->plan.bt == bt && b->plan.bps == bps && b->plan.tile == tile &&
+        b->plan.hints == hints)
+        return RXG_OK;
     b->plan.free_all();
     return build_plan(b, bt, bps, tile, &b->plan);
 }
@@ -543,7 +658,7 @@ static rxg_status batch_args(rxg_batch* b, cudaStream_t s, BatchArgs* out, R4<do
     const int64_t n = b->mesh->m.nv, w = batch_ell_width(b);
     const int64_t nnz   = w ? w * n : z->nnz;
     const size_t  bytes = a256(sizeof(Ent<float>) * nnz) + 2 * a256(sizeof(R4<double>) * n) +
-                         4 * a256(sizeof(R4<float>) * n) + a256(sizeof(float) * n) +
+                         a256(sizeof(R4<float>) * n) + a256(sizeof(float) * n) +
                          a256(sizeof(double) * n);
     {
         std::lock_guard<std::mutex> g(b->mu);
@@ -560,10 +675,7 @@ static rxg_status batch_args(rxg_batch* b, cudaStream_t s, BatchArgs* out, R4<do
     a.ent = (Ent<float>*)q, q += a256(sizeof(Ent<float>) * nnz);
     a.X = (R4<double>*)q, q += a256(sizeof(R4<double>) * n);
     a.B = (R4<double>*)q, q += a256(sizeof(R4<double>) * n);
-    a.P = (R4<float>*)q, q += a256(sizeof(R4<float>) * n);
-    a.S = (R4<float>*)q, q += a256(sizeof(R4<float>) * n);
     a.Z = (R4<float>*)q, q += a256(sizeof(R4<float>) * n);
-    a.D = (R4<float>*)q, q += a256(sizeof(R4<float>) * n);
     a.dinv  = (float*)q, q += a256(sizeof(float) * n);
     a.diag  = (double*)q;
     a.iters = b->d_iters;
@@ -579,24 +691,29 @@ static rxg_status batch_launch(rxg_batch* b, BatchArgs a, int bt, int bps, int t
     rxg_status st = ensure_plan(b, bt, bps, tile);
     if (st) return st;
     const GangPlan& p = b->plan;
-    a.job_mesh = p.d_job_mesh;
-    a.job_k    = p.d_job_k;
-    a.cta_off  = p.d_cta_off;
-    a.cta_job  = p.d_cta_job;
-    a.cta_rank = p.d_cta_rank;
+    a.job_mesh  = p.d_job_mesh;
+    a.job_k     = p.d_job_k;
+    a.nwaves    = p.nwaves;
+    a.nsingle   = p.nsingle;
+    a.njobs     = p.njobs;
+    a.wave_job  = p.d_wave_job;
+    a.wave_rank = p.d_wave_rank;
+    a.single    = p.d_single;
     a.bar      = p.d_bar;
     a.part     = p.d_part;
     a.kmax     = p.kmax;
-    RXG_CUDA_TRY(cudaMemsetAsync(p.d_bar, 0, sizeof(unsigned) * 4 * p.njobs, s));
+    a.cp       = p.cp;
+    RXG_CUDA_TRY(cudaMemsetAsync(p.d_bar, 0, sizeof(unsigned) * (4 * p.njobs + 8), s));
     void*       args[] = {&a};
     const void* kern = batch_kernel(bt, batch_ell_width(b), bps);
+    RXG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem));
     cudaLaunchConfig_t   cfg  = {};
     cudaLaunchAttribute  attr = {};
     attr.id               = cudaLaunchAttributeCooperative;
     attr.val.cooperative  = 1;
     cfg.gridDim           = dim3(p.G);
     cfg.blockDim          = dim3(bt);
-    cfg.dynamicSmemBytes  = 0;
+    cfg.dynamicSmemBytes  = p.smem;
     cfg.stream            = s;
     cfg.attrs             = &attr;
     cfg.numAttrs          = 1;
@@ -747,8 +864,10 @@ rxg_status rxg_batch_stats(const rxg_batch* b, int32_t* iters, int32_t* converge
     return RXG_OK;
 }
 
-// Times the CTA size x CTAs per SM x tile (rows per CTA of a mesh's gang)
-// grid on the caller's batch and keeps the fastest (xyz is not modified).
+// Runs the batch once to learn each mesh's PCG iteration count (the cost of
+// its job in every later schedule), then times CTA size x CTAs per SM x tile
+// (most rows per CTA) on the caller's batch and keeps the fastest (xyz is
+// not modified).
 rxg_status rxg_batch_autotune(rxg_batch* b, double dt, int32_t nsteps, double tol, int32_t max_iter,
                               const double* xyz, int32_t* threads, int32_t* blocks_per_sm,
                               float* best_ms, void* stream)
@@ -771,23 +890,43 @@ rxg_status rxg_batch_autotune(rxg_batch* b, double dt, int32_t nsteps, double to
     cudaEvent_t   e0, e1;
     RXG_CUDA_TRY(cudaEventCreate(&e0));
     RXG_CUDA_TRY(cudaEventCreate(&e1));
+    // one run of the current configuration gives every mesh's iteration count,
+    // which the schedules below use as the cost of its job
+    k_batch_pack<<<g, 256, 0, s>>>(n, b->mesh->m.d.v_l2i, xyz, X4);
+    if ((st = batch_launch(b, a, b->threads, b->blocks_per_sm, b->tile, s))) return st;
+    {
+        std::vector<int32_t> it(b->nmesh);
+        RXG_CUDA_TRY(cudaMemcpyAsync(it.data(), b->d_iters, 4 * b->nmesh, cudaMemcpyDeviceToHost, s));
+        RXG_CUDA_TRY(cudaStreamSynchronize(s));
+        std::lock_guard<std::mutex> lk(b->mu);
+        b->iters_hint = it;
+    }
     float best = 1e30f;
     int   bt_best = b->threads, bps_best = b->blocks_per_sm, tile_best = b->tile;
     for (int bt : {256, 512, 1024}) {
-        for (int bps : {1, 2, 4}) {
-            if (bps > max_per_sm(bt, batch_ell_width(b), bps) || bt * bps > 2048) continue;
-            for (int tile : {1024, 2048, 4096, 8192}) {
+        for (int bps : {1, 2}) {
+            if (bt * bps > 2048) continue;
+            for (int tile : {1024, 2048, 4096}) {
                 float t = 0;
-                for (int rep = 0; rep < 2 && st == RXG_OK; ++rep) {
+                bool  ok = true;
+                for (int rep = 0; rep < 2; ++rep) {
                     k_batch_pack<<<g, 256, 0, s>>>(n, b->mesh->m.d.v_l2i, xyz, X4);
                     cudaEventRecord(e0, s);
-                    st = batch_launch(b, a, bt, bps, tile, s);
+                    rxg_status r = batch_launch(b, a, bt, bps, tile, s);
                     cudaEventRecord(e1, s);
                     cudaEventSynchronize(e1);
+                    if (r == RXG_ERR_UNSUPPORTED) {  // this shape does not fit an SM
+                        ok = false;
+                        break;
+                    }
+                    if (r) {
+                        st = r;
+                        break;
+                    }
                     cudaEventElapsedTime(&t, e0, e1);  // second repetition is kept
                 }
                 if (st) break;
-                if (t < best) {
+                if (ok && t < best) {
                     best      = t;
                     bt_best   = bt;
                     bps_best  = bps;
