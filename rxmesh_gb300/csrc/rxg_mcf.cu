@@ -439,90 +439,9 @@ struct CGArgs
     int*           err;
 };
 
-// Grid-wide sum of one double per block, fused with the grid barrier.
-// Thread 0 of every block posts its block's value and arrives on a counter
-// that only ever grows (reduction k ends at arrival G*(k+1)); the last block
-// to arrive sums all posts in a fixed order, so every run and every block
-// sees the same value, and publishes it in slot[k & 1], a 64-bit word that
-// reads all-ones (a NaN) until then.  Before publishing it re-arms the other
-// slot for reduction k+1, which no block can still be reading.  The other
-// blocks poll that one word: one round trip instead of a flag and a value.
-// The wait is bounded: on timeout the error word and an abort flag are set
-// and false is returned.  bar[0] arrivals, bar[2] abort, bar[4..7] slots
-// (16-byte aligned); the host sets bar[0..3] to 0 and the slots to all-ones.
-__device__ __forceinline__ bool grid_reduce(double v, double* part, unsigned* bar, unsigned G,
-                                            unsigned k, int* err, double* s_red, int* s_ok,
-                                            double* out)
-{
-    unsigned long long* slot = reinterpret_cast<unsigned long long*>(bar + 4);
-    const unsigned long long kNotYet = ~0ull;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        const unsigned lane = threadIdx.x;
-        unsigned       last = 0;
-        if (lane == 0) {
-            part[blockIdx.x] = v;
-            __threadfence();
-            last = (atomicAdd(bar, 1u) % G) == G - 1 ? 1u : 0u;
-        }
-        last       = __shfl_sync(0xffffffffu, last, 0);
-        int    ok  = 1;
-        double sum = 0;
-        if (last) {
-            __threadfence();
-            double acc = 0;
-#pragma unroll 4
-            for (unsigned i = lane; i < G; i += 32) acc += __ldcg(part + i);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            sum = acc;
-            if (lane == 0) {
-                *((volatile unsigned long long*)(slot + ((k + 1) & 1))) = kNotYet;
-                __threadfence();
-                *((volatile unsigned long long*)(slot + (k & 1))) =
-                    (unsigned long long)__double_as_longlong(acc);
-            }
-        } else if (lane == 0) {
-            volatile unsigned* vab = bar + 2;
-            uint32_t           it  = 0;
-            while (true) {
-                const unsigned long long w = *((volatile unsigned long long*)(slot + (k & 1)));
-                if (w != kNotYet) {
-                    sum = __longlong_as_double((long long)w);
-                    break;
-                }
-                if (*vab) {
-                    ok = 0;
-                    break;
-                }
-                if (++it > kWaitLimit) {
-                    atomicOr(err, DEVERR_GRID_TIMEOUT);
-                    atomicExch(bar + 2, 1u);
-                    ok = 0;
-                    break;
-                }
-            }
-            __threadfence();
-        }
-        if (lane == 0) {
-            s_red[0] = sum;
-            *s_ok    = ok;
-        }
-    }
-    __syncthreads();
-    *out          = s_red[0];
-    const bool ok = *s_ok != 0;
-    __syncthreads();
-    return ok;
-}
-
-// host side of the barrier state: counter and abort to 0, slots to all-ones
-static cudaError_t reset_grid_reduce(unsigned* bar, cudaStream_t s)
-{
-    cudaError_t e = cudaMemsetAsync(bar, 0, 16, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(bar + 4, 0xFF, 32, s);  // up to two value slots
-    return e;
-}
+// host side of the grid-sum state (rxg_gridsum.cuh): ticket counter and
+// abort word to 0 before every launch
+static cudaError_t reset_grid_sum(unsigned* bar, cudaStream_t s) { return cudaMemsetAsync(bar, 0, 16, s); }
 
 // acc = sum_j A_ij x_j over row i, eight non-zeros per round so that all
 // column/value loads and then all gathers of a round are in flight together
@@ -783,7 +702,7 @@ static rxg_status cg_launch(int64_t n, const int32_t* rp, const int32_t* col, co
     a.abs_tol  = o.abs_tol;
     a.rel_tol  = o.rel_tol;
     a.err      = device_error_word();
-    RXG_CUDA_TRY(reset_grid_reduce(a.bar, s));
+    RXG_CUDA_TRY(reset_grid_sum(a.bar, s));
     void* args[] = {&a};
     const void* kern = cg_threads() == 256    ? (const void*)k_cg<T, NC, PC, 256>
                        : cg_threads() == 1024 ? (const void*)k_cg<T, NC, PC, 1024>
@@ -1057,278 +976,6 @@ __global__ void __launch_bounds__(kBT) k_cgm(CGMArgs<T> a)
     }
 }
 
-// ---------------------------------------------------------------------
-// Pipelined Jacobi-PCG (Ghysels & Vanroose 2014, "Hiding global
-// synchronization latency in the preconditioned conjugate gradient
-// algorithm") for the FP32 inner solves of the mixed MCF step.  With the
-// Jacobi preconditioner M = D^-1 applied elementwise, u = M r, m = M w and
-// q = M s are never stored, and every iteration is ONE pass over the rows:
-//   n = A (M w_old)             gathered from the other w buffer
-//   z = n + beta z,  s = w + beta s,  p = M r + beta p
-//   x += alpha p,  r -= alpha s,  w_new = w_old - alpha z
-//   gamma' = r . M r,  delta' = w_new . M r
-// followed by ONE grid reduction of (gamma', delta').  alpha, beta come from
-// the previous reduction: beta = gamma / gamma_prev,
-// alpha = gamma / (delta - beta gamma / alpha_prev).  w is double-buffered
-// (neighbours read the old one) and carries dinv in its fourth lane.
-// The stopping rule is the PCG one on gamma = r . M r.
-// ---------------------------------------------------------------------
-
-template <typename T>
-struct PipeArgs
-{
-    int64_t        n;
-    const int32_t* rp;
-    const Ent<T>*  ent;
-    const R4<T>*   B;
-    R4<T>*         X;
-    R4<T>*         R;   // w lane: dinv
-    R4<T>*         W0;  // w lane: dinv
-    R4<T>*         W1;
-    R4<T>*         Z;
-    R4<T>*         S;
-    R4<T>*         P;
-    double*        part;  // 2 * G
-    unsigned*      bar;
-    double*        dstat;
-    int*           istat;
-    int            max_iter;
-    double         abs_tol, rel_tol;
-    int*           err;
-};
-
-// two-value version of grid_reduce (gamma and delta in one barrier); the
-// second value uses part[G..2G) and slot pair bar[8..11]
-__device__ __forceinline__ bool grid_reduce2v(double v0, double v1, double* part, unsigned* bar,
-                                              unsigned G, unsigned k, int* err, double* s_red,
-                                              int* s_ok, double* o0, double* o1)
-{
-    unsigned long long* slot = reinterpret_cast<unsigned long long*>(bar + 4);  // [2] v0, [2] v1
-    const unsigned long long kNotYet = ~0ull;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        const unsigned lane = threadIdx.x;
-        unsigned       last = 0;
-        if (lane == 0) {
-            part[blockIdx.x]     = v0;
-            part[G + blockIdx.x] = v1;
-            __threadfence();
-            last = (atomicAdd(bar, 1u) % G) == G - 1 ? 1u : 0u;
-        }
-        last      = __shfl_sync(0xffffffffu, last, 0);
-        int    ok = 1;
-        double s0 = 0, s1 = 0;
-        if (last) {
-            __threadfence();
-            double a0 = 0, a1 = 0;
-#pragma unroll 4
-            for (unsigned i = lane; i < G; i += 32) {
-                a0 += __ldcg(part + i);
-                a1 += __ldcg(part + G + i);
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-                a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-            }
-            s0 = a0, s1 = a1;
-            if (lane == 0) {
-                // v1 first: pollers read v0's slot last (published last)
-                *((volatile unsigned long long*)(slot + 2 + ((k + 1) & 1))) = kNotYet;
-                *((volatile unsigned long long*)(slot + ((k + 1) & 1)))     = kNotYet;
-                __threadfence();
-                *((volatile unsigned long long*)(slot + 2 + (k & 1))) =
-                    (unsigned long long)__double_as_longlong(a1);
-                __threadfence();
-                *((volatile unsigned long long*)(slot + (k & 1))) =
-                    (unsigned long long)__double_as_longlong(a0);
-            }
-        } else if (lane == 0) {
-            volatile unsigned* vab = bar + 2;
-            uint32_t           it  = 0;
-            while (true) {
-                const unsigned long long w = *((volatile unsigned long long*)(slot + (k & 1)));
-                if (w != kNotYet) {
-                    s0 = __longlong_as_double((long long)w);
-                    break;
-                }
-                if (*vab) {
-                    ok = 0;
-                    break;
-                }
-                if (++it > kWaitLimit) {
-                    atomicOr(err, DEVERR_GRID_TIMEOUT);
-                    atomicExch(bar + 2, 1u);
-                    ok = 0;
-                    break;
-                }
-            }
-            __threadfence();
-            s1 = __longlong_as_double(
-                (long long)*((volatile unsigned long long*)(slot + 2 + (k & 1))));
-        }
-        if (lane == 0) {
-            s_red[0] = s0;
-            s_red[1] = s1;
-            *s_ok    = ok;
-        }
-    }
-    __syncthreads();
-    *o0           = s_red[0];
-    *o1           = s_red[1];
-    const bool ok = *s_ok != 0;
-    __syncthreads();
-    return ok;
-}
-
-// acc = sum_j A_ij (dinv_j v_j) with dinv_j in lane w of v_j
-template <typename T>
-__device__ __forceinline__ void row_spmv_scaled(const int32_t* __restrict__ rp,
-                                                const Ent<T>* __restrict__ ent, int64_t i,
-                                                const R4<T>* v, T& ax, T& ay, T& az)
-{
-    const int32_t b = __ldg(rp + i), e = __ldg(rp + i + 1);
-    for (int32_t j0 = b; j0 < e; j0 += 8) {
-        Ent<T> q[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            if (j0 + u < e) {
-                q[u] = ent[j0 + u];
-            } else {
-                q[u].col = (int32_t)i;
-                q[u].val = T(0);
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const R4<T> xv = v[q[u].col];
-            const T     c  = q[u].val * xv.w;
-            ax += c * xv.x;
-            ay += c * xv.y;
-            az += c * xv.z;
-        }
-    }
-}
-
-template <typename T, int kBT>
-__global__ void __launch_bounds__(kBT) k_pcg_pipe(PipeArgs<T> a)
-{
-    __shared__ double s_red[kBT / 32 + 2];
-    __shared__ int    s_ok;
-    const unsigned G     = gridDim.x;
-    const int64_t  chunk = (a.n + G - 1) / G;
-    const int64_t  r0    = blockIdx.x * chunk;
-    const int64_t  r1    = min(a.n, r0 + chunk);
-    unsigned       kred  = 0;
-    const T        eps   = sizeof(T) == 4 ? (T)FLT_EPSILON : (T)DBL_EPSILON;
-
-    // ---- r = B - A X (dinv into lane w), then barrier
-    for (int64_t i = r0 + threadIdx.x; i < r1; i += kBT) {
-        T ax = 0, ay = 0, az = 0, diag = 0;
-        row_spmv4<T>(a.rp, a.ent, i, a.X, ax, ay, az, &diag);
-        const R4<T> b = a.B[i];
-        R4<T>       r;
-        r.x = b.x - ax, r.y = b.y - ay, r.z = b.z - az, r.w = T(1) / (diag + eps);
-        a.R[i] = r;
-    }
-    double d0, d1;
-    if (!grid_reduce2v(0.0, 0.0, a.part, a.bar, G, kred++, a.err, s_red, &s_ok, &d0, &d1)) return;
-    // ---- w = A M r; gamma = r.Mr, delta = w.Mr
-    T tg = T(0), td = T(0);
-    for (int64_t i = r0 + threadIdx.x; i < r1; i += kBT) {
-        T ax = 0, ay = 0, az = 0;
-        row_spmv_scaled<T>(a.rp, a.ent, i, a.R, ax, ay, az);
-        const R4<T> r = a.R[i];
-        R4<T>       w;
-        w.x = ax, w.y = ay, w.z = az, w.w = r.w;
-        a.W0[i]    = w;
-        const T ux = r.w * r.x, uy = r.w * r.y, uz = r.w * r.z;
-        tg += r.x * ux + r.y * uy + r.z * uz;
-        td += w.x * ux + w.y * uy + w.z * uz;
-    }
-    double gamma, delta;
-    if (!grid_reduce2v(block_sum<kBT>((double)tg, s_red), block_sum<kBT>((double)td, s_red), a.part,
-                       a.bar, G, kred++, a.err, s_red, &s_ok, &gamma, &delta))
-        return;
-    const double gamma0 = gamma;
-    auto   conv  = [&](double g) { return g < a.abs_tol || g / gamma0 < a.rel_tol; };
-    double alpha_prev = 1.0, gamma_prev = 1.0;
-    int    it   = 0;
-    bool   done = conv(gamma0);
-    // stagnation guard: in FP32 the recursive residual of the pipelined
-    // recurrences can stall above a tight target; the caller's FP64
-    // refinement restarts from a fresh residual instead
-    double best = gamma0;
-    int    best_it = 0;
-    while (!done && it < a.max_iter) {
-        double alpha, beta;
-        if (it == 0) {
-            beta  = 0.0;
-            alpha = gamma / delta;
-        } else {
-            beta  = gamma / gamma_prev;
-            alpha = gamma / (delta - beta * gamma / alpha_prev);
-        }
-        const T     al = (T)alpha, bt = (T)beta;
-        R4<T>*      Wo = (it & 1) ? a.W1 : a.W0;
-        R4<T>*      Wn = (it & 1) ? a.W0 : a.W1;
-        tg = T(0), td = T(0);
-        for (int64_t i = r0 + threadIdx.x; i < r1; i += kBT) {
-            T nx = 0, ny = 0, nz = 0;
-            row_spmv_scaled<T>(a.rp, a.ent, i, Wo, nx, ny, nz);
-            const R4<T> w = Wo[i];
-            R4<T>       r = a.R[i], x = a.X[i], z, s, p;
-            const T     di = r.w;
-            if (it == 0) {
-                z.x = nx, z.y = ny, z.z = nz;
-                s.x = w.x, s.y = w.y, s.z = w.z;
-                p.x = di * r.x, p.y = di * r.y, p.z = di * r.z;
-            } else {
-                const R4<T> zo = a.Z[i], so = a.S[i], po = a.P[i];
-                z.x = nx + bt * zo.x, z.y = ny + bt * zo.y, z.z = nz + bt * zo.z;
-                s.x = w.x + bt * so.x, s.y = w.y + bt * so.y, s.z = w.z + bt * so.z;
-                p.x = di * r.x + bt * po.x, p.y = di * r.y + bt * po.y, p.z = di * r.z + bt * po.z;
-            }
-            z.w = s.w = p.w = T(0);
-            x.x += al * p.x, x.y += al * p.y, x.z += al * p.z;
-            r.x -= al * s.x, r.y -= al * s.y, r.z -= al * s.z;
-            R4<T> wn;
-            wn.x = w.x - al * z.x, wn.y = w.y - al * z.y, wn.z = w.z - al * z.z, wn.w = di;
-            a.Z[i] = z;
-            a.S[i] = s;
-            a.P[i] = p;
-            a.X[i] = x;
-            a.R[i] = r;
-            Wn[i]  = wn;
-            const T ux = di * r.x, uy = di * r.y, uz = di * r.z;
-            tg += r.x * ux + r.y * uy + r.z * uz;
-            td += wn.x * ux + wn.y * uy + wn.z * uz;
-        }
-        double gn, dn;
-        if (!grid_reduce2v(block_sum<kBT>((double)tg, s_red), block_sum<kBT>((double)td, s_red),
-                           a.part, a.bar, G, kred++, a.err, s_red, &s_ok, &gn, &dn))
-            return;
-        alpha_prev = alpha;
-        gamma_prev = gamma;
-        gamma      = gn;
-        delta      = dn;
-        ++it;
-        done = conv(gn);
-        if (gn < 0.25 * best) {
-            best    = gn;
-            best_it = it;
-        } else if (it - best_it > 40) {
-            break;
-        }
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.dstat[0] = gamma0;
-        a.dstat[1] = gamma;
-        a.istat[0] = it;
-        a.istat[1] = done ? 1 : 0;
-    }
-}
-
 // CTA size of the packed MCF solver: RXG_MCF_CG_THREADS=256|512|1024 (default 1024)
 static int cgm_threads()
 {
@@ -1398,103 +1045,12 @@ static rxg_status cgm_launch(int64_t n, const int32_t* rp, const Ent<T>* ent, co
     a.abs_tol  = o.abs_tol;
     a.rel_tol  = o.rel_tol;
     a.err      = device_error_word();
-    RXG_CUDA_TRY(reset_grid_reduce(a.bar, s));
+    RXG_CUDA_TRY(reset_grid_sum(a.bar, s));
     void*       args[] = {&a};
     const void* kern   = cgm_threads() == 256   ? (const void*)k_cgm<T, 256>
                          : cgm_threads() == 512 ? (const void*)k_cgm<T, 512>
                                                 : (const void*)k_cgm<T, 1024>;
     RXG_CUDA_TRY(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(cgm_threads()), args, 0, s));
-    double ds[2];
-    int    is[2];
-    RXG_CUDA_TRY(cudaMemcpyAsync(ds, a.dstat, sizeof(ds), cudaMemcpyDeviceToHost, s));
-    RXG_CUDA_TRY(cudaMemcpyAsync(is, a.istat, sizeof(is), cudaMemcpyDeviceToHost, s));
-    RXG_CUDA_TRY(cudaStreamSynchronize(s));
-    rxg_status e = check_device_error(s);
-    if (e) return e;
-    st->start_res = ds[0];
-    st->final_res = ds[1];
-    st->iters     = is[0];
-    st->converged = is[1];
-    return RXG_OK;
-}
-
-template <typename T>
-static size_t pipe_scratch_bytes(int64_t n, int G)
-{
-    return 6 * align256(sizeof(R4<T>) * n) + align256(sizeof(double) * 2 * G) + 3 * 256;
-}
-
-template <typename T, int BT>
-static int pipe_grid_bt(int64_t n)
-{
-    static int per_sm = -1;
-    if (per_sm < 0) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_pipe<T, BT>, BT, 0) !=
-            cudaSuccess)
-            per_sm = 1;
-        per_sm = std::max(1, std::min(per_sm, 2048 / BT));
-    }
-    int64_t g = (int64_t)num_sms() * per_sm;
-    return (int)std::min<int64_t>(g, std::max<int64_t>(1, (n + 31) / 32));
-}
-
-// CTA size of the pipelined solver: RXG_MCF_PIPE_THREADS=256|512|1024 (default
-// 512: at 1024 threads the 64-register cap makes it spill)
-static int pipe_threads()
-{
-    static int t = 0;
-    if (!t) {
-        const char* e = getenv("RXG_MCF_PIPE_THREADS");
-        t             = e ? atoi(e) : 512;
-        if (t != 256 && t != 512 && t != 1024) t = 512;
-    }
-    return t;
-}
-
-template <typename T>
-static int pipe_grid(int64_t n)
-{
-    switch (pipe_threads()) {
-        case 256: return pipe_grid_bt<T, 256>(n);
-        case 512: return pipe_grid_bt<T, 512>(n);
-        default: return pipe_grid_bt<T, 1024>(n);
-    }
-}
-
-template <typename T>
-static rxg_status pipe_launch(int64_t n, const int32_t* rp, const Ent<T>* ent, const R4<T>* B,
-                              R4<T>* X, const rxg_solver_opts& o, rxg_solver_stats* st,
-                              uint8_t* scratch, cudaStream_t s)
-{
-    const int    G  = pipe_grid<T>(n);
-    const size_t vb = align256(sizeof(R4<T>) * n);
-    PipeArgs<T>  a;
-    uint8_t*     q = scratch;
-    a.n   = n;
-    a.rp  = rp;
-    a.ent = ent;
-    a.B   = B;
-    a.X   = X;
-    a.R  = (R4<T>*)q, q += vb;
-    a.W0 = (R4<T>*)q, q += vb;
-    a.W1 = (R4<T>*)q, q += vb;
-    a.Z  = (R4<T>*)q, q += vb;
-    a.S  = (R4<T>*)q, q += vb;
-    a.P  = (R4<T>*)q, q += vb;
-    a.part  = (double*)q, q += align256(sizeof(double) * 2 * G);
-    a.bar   = (unsigned*)q, q += 256;
-    a.dstat = (double*)q, q += 256;
-    a.istat = (int*)q, q += 256;
-    a.max_iter = o.max_iter;
-    a.abs_tol  = o.abs_tol;
-    a.rel_tol  = o.rel_tol;
-    a.err      = device_error_word();
-    RXG_CUDA_TRY(reset_grid_reduce(a.bar, s));
-    void*       args[] = {&a};
-    const void* kern   = pipe_threads() == 256   ? (const void*)k_pcg_pipe<T, 256>
-                         : pipe_threads() == 512 ? (const void*)k_pcg_pipe<T, 512>
-                                                 : (const void*)k_pcg_pipe<T, 1024>;
-    RXG_CUDA_TRY(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(pipe_threads()), args, 0, s));
     double ds[2];
     int    is[2];
     RXG_CUDA_TRY(cudaMemcpyAsync(ds, a.dstat, sizeof(ds), cudaMemcpyDeviceToHost, s));
@@ -1515,20 +1071,6 @@ static bool mcf_verbose()
     static int v = -1;
     if (v < 0) {
         const char* e = getenv("RXG_MCF_VERBOSE");
-        v             = (e && e[0] == '1') ? 1 : 0;
-    }
-    return v == 1;
-}
-
-// Inner solver of the mixed MCF step: the standard PCG recurrence (k_cgm);
-// RXG_MCF_PIPELINED=1 selects the pipelined one (one grid barrier per
-// iteration, but its FP32 recursive residual can stall over many flow
-// steps, which costs more refinement sweeps than the barrier saves).
-static bool mixed_pipelined()
-{
-    static int v = -1;
-    if (v < 0) {
-        const char* e = getenv("RXG_MCF_PIPELINED");
         v             = (e && e[0] == '1') ? 1 : 0;
     }
     return v == 1;
@@ -1804,9 +1346,8 @@ rxg_status rxg_mcf_step(const rxg_mesh* h, double dt, int32_t nsteps, int32_t pr
     const int64_t max_row = h->m.max_valence + 1;  // diagonal + one-ring
     const size_t mixed = 2 * x4b + align256(sizeof(Ent<float>) * nnz) +
                          2 * align256(sizeof(R4<float>) * n) + align256(8 * Gr) + align256(8 * n) +
-                         std::max({cgm_scratch_bytes<float>(n, cgm_grid<float>(n)),
-                                   pipe_scratch_bytes<float>(n, pipe_grid<float>(n)),
-                                   mcf_onchip_scratch_bytes(n, max_row)});
+                         std::max(cgm_scratch_bytes<float>(n, cgm_grid<float>(n)),
+                                  mcf_onchip_scratch_bytes(n, max_row));
     {
         std::lock_guard<std::mutex> g(z->mu);
         if ((st = mcf_buffers(z, std::max(plain, mixed), s))) return st;
@@ -1825,7 +1366,7 @@ rxg_status rxg_mcf_step(const rxg_mesh* h, double dt, int32_t nsteps, int32_t pr
     uint8_t*    p  = q + 2 * x4b;
     rxg_solver_stats last   = {0, 1, 0.0, 0.0};
     const int        ga     = grid_for(n);
-    const bool       onchip = precision == RXG_F32 && !mixed_pipelined() && mcf_onchip_fits(n, max_row);
+    const bool       onchip = precision == RXG_F32 && mcf_onchip_fits(n, max_row);
     k_pack3<<<ga, 256, 0, s>>>(n, X, X4);
     for (int step = 0; step < nsteps && st == RXG_OK; ++step) {
         // the assembly reads the caller-layout positions of this step
@@ -1872,9 +1413,7 @@ rxg_status rxg_mcf_step(const rxg_mesh* h, double dt, int32_t nsteps, int32_t pr
                 RXG_CUDA_TRY(cudaMemsetAsync(d32, 0, sizeof(R4<float>) * n, s));
                 rxg_solver_opts  o = {max_iter - total_it, 0.0, inner * inner, 1};
                 rxg_solver_stats si;
-                st = mixed_pipelined()
-                         ? pipe_launch<float>(n, z->row_ptr, ent, r32, d32, o, &si, scr, s)
-                         : cgm_launch<float>(n, z->row_ptr, ent, r32, d32, o, &si, scr, s);
+                st = cgm_launch<float>(n, z->row_ptr, ent, r32, d32, o, &si, scr, s);
                 if (st) break;
                 total_it += si.iters + 1;
                 k_add_correction4<<<ga, 256, 0, s>>>(n, X4, d32);
