@@ -130,29 +130,6 @@ __device__ __forceinline__ int32_t block_exclusive_scan(int32_t* s, int32_t n, i
     return total;
 }
 
-// Copy n ints from shared (sbuf holds element g - gbase at sbuf[shift + ...],
-// shift = gbase & 3) to global dst[gbase .. gbase+n) with 16-byte stores in
-// the aligned middle and scalar stores at the ragged ends.
-template <int BT>
-__device__ __forceinline__ void store_ints_aligned(int32_t* __restrict__ dst, int64_t gbase,
-                                                   const int32_t* sbuf, int32_t n)
-{
-    const int64_t g_end   = gbase + n;
-    const int64_t g0      = (gbase + 3) & ~int64_t(3);
-    const int64_t g1      = g_end & ~int64_t(3);
-    const int64_t sbase   = gbase & ~int64_t(3);  // sbuf[j] <-> global sbase + j
-    if (g0 >= g1) {
-        for (int64_t g = gbase + threadIdx.x; g < g_end; g += BT) dst[g] = sbuf[g - sbase];
-        return;
-    }
-    for (int64_t g = gbase + threadIdx.x; g < g0; g += BT) dst[g] = sbuf[g - sbase];
-    for (int64_t g = g1 + threadIdx.x; g < g_end; g += BT) dst[g] = sbuf[g - sbase];
-    const int32_t nv4 = (int32_t)((g1 - g0) >> 2);
-    const int4*   s4  = reinterpret_cast<const int4*>(sbuf + (g0 - sbase));
-    int4*         d4  = reinterpret_cast<int4*>(dst + g0);
-    for (int32_t i = threadIdx.x; i < nv4; i += BT) d4[i] = s4[i];
-}
-
 // Write n values to global dst[gbase .. gbase+n) from 16-bit local ids in
 // shared memory (sbuf[j] <-> global (gbase & ~3) + j), each mapped to its
 // 32-bit id by map(): 8-byte shared loads and 16-byte global stores in the
@@ -161,20 +138,15 @@ template <int BT, typename Map>
 __device__ __forceinline__ void store_u16_mapped(int32_t* __restrict__ dst, int64_t gbase,
                                                  const uint16_t* sbuf, int32_t n, const Map& map)
 {
-    const int64_t g_end = gbase + n;
-    const int64_t g0    = (gbase + 3) & ~int64_t(3);
-    const int64_t g1    = g_end & ~int64_t(3);
-    const int64_t sbase = gbase & ~int64_t(3);
-    if (g0 >= g1) {
-        for (int64_t g = gbase + threadIdx.x; g < g_end; g += BT) dst[g] = map(sbuf[g - sbase]);
-        return;
-    }
-    for (int64_t g = gbase + threadIdx.x; g < g0; g += BT) dst[g] = map(sbuf[g - sbase]);
-    for (int64_t g = g1 + threadIdx.x; g < g_end; g += BT) dst[g] = map(sbuf[g - sbase]);
-    const int32_t nv4 = (int32_t)((g1 - g0) >> 2);
-    const uint2*  s4  = reinterpret_cast<const uint2*>(sbuf + (g0 - sbase));
-    int4*         d4  = reinterpret_cast<int4*>(dst + g0);
-    for (int32_t i = threadIdx.x; i < nv4; i += BT) {
+    int32_t* const        d    = dst + gbase;           // 64-bit arithmetic once
+    const uint16_t* const s    = sbuf + (gbase & 3);    // s[j] <-> d[j]
+    const int32_t         lead = min(n, (int32_t)((4 - (gbase & 3)) & 3));
+    const int32_t         body = (n - lead) & ~3;
+    if ((int32_t)threadIdx.x < lead) d[threadIdx.x] = map(s[threadIdx.x]);
+    for (int32_t j = lead + body + threadIdx.x; j < n; j += BT) d[j] = map(s[j]);
+    const uint2* s4 = reinterpret_cast<const uint2*>(s + lead);  // 8-byte aligned
+    int4*        d4 = reinterpret_cast<int4*>(d + lead);         // 16-byte aligned
+    for (int32_t i = threadIdx.x; i < (body >> 2); i += BT) {
         const uint2 w = s4[i];
         int4        o;
         o.x   = map(w.x & 0xffffu);

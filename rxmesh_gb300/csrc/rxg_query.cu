@@ -168,9 +168,12 @@ __global__ void __launch_bounds__(kQT) k_query_vertex(const PatchHdr* __restrict
 
     // 1. count owned-vertex incidences
     if (OP == 2) {
-        for (int i = threadIdx.x; i < 3 * h.nFl; i += kQT) {
-            uint32_t v = face_vertex(fe16, s_ev, i / 3, i % 3);
-            if ((int32_t)v < nVo) atomicAdd(&s_cnt[v], 1);
+        for (int f = threadIdx.x; f < h.nFl; f += kQT) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t v = face_vertex(fe16, s_ev, f, k);
+                if ((int32_t)v < nVo) atomicAdd(&s_cnt[v], 1);
+            }
         }
     } else {
         for (int e2 = threadIdx.x; e2 < nE2; e2 += kQT) {
@@ -194,10 +197,12 @@ __global__ void __launch_bounds__(kQT) k_query_vertex(const PatchHdr* __restrict
     // 3. scatter 16-bit local ids into the staged chunk
     uint16_t* sbuf = s_out + (vbase & 3);  // element g lives at s_out[g - (vbase & ~3)]
     if (OP == 2) {
-        for (int i = threadIdx.x; i < 3 * h.nFl; i += kQT) {
-            const int      f = i / 3;
-            const uint32_t v = face_vertex(fe16, s_ev, f, i % 3);
-            if ((int32_t)v < nVo) sbuf[atomicAdd(&s_cnt[v], 1)] = (uint16_t)f;
+        for (int f = threadIdx.x; f < h.nFl; f += kQT) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t v = face_vertex(fe16, s_ev, f, k);
+                if ((int32_t)v < nVo) sbuf[atomicAdd(&s_cnt[v], 1)] = (uint16_t)f;
+            }
         }
     } else {
         for (int e2 = threadIdx.x; e2 < nE2; e2 += kQT) {
