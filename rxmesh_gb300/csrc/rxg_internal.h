@@ -44,6 +44,9 @@ struct DeviceTopo
     int32_t* f_l2i = nullptr;
     // face -> 3 linear vertex ids (face linear order), used by per-face kernels
     int32_t* fv_lin = nullptr;
+    // per-patch incidence blocks of the vertex-normal kernel (see Mesh::nrm)
+    uint32_t* nrm     = nullptr;
+    int32_t*  nrm_off = nullptr;
 };
 
 struct Mesh
@@ -62,6 +65,13 @@ struct Mesh
     std::vector<int32_t> v_i2l, e_i2l, f_i2l;
     std::vector<PatchHdr> hdr;
     std::vector<uint32_t> arena;
+    // Per patch p, words [nrm_off[p], nrm_off[p+1]) of nrm (16-byte aligned):
+    // local face -> 3 local vertex ids (u16 triples, pad4 words), offsets of
+    // the owned vertices' incident-face lists (u32 x nVo+1, pad4), and the
+    // lists themselves (u16 local face ids, pad4).  Static topology, built
+    // once with the patches.
+    std::vector<uint32_t> nrm;
+    std::vector<int32_t>  nrm_off;
 
     DeviceTopo d;
 

@@ -228,11 +228,15 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
     for (int64_t i = 0; i < nf; ++i) M.f_i2l[M.f_l2i[i]] = (int32_t)i;
 
     // ---- per-patch local topology ---------------------------------------
-    std::vector<int32_t> vstamp(nv, -1), vloc(nv), estamp(ne, -1), eloc(ne), fstamp(nf, -1);
+    std::vector<int32_t> vstamp(nv, -1), vloc(nv), estamp(ne, -1), eloc(ne), fstamp(nf, -1),
+        floc(nf);
     std::vector<int32_t> lf, lv, le;
     M.hdr.resize(np);
     M.arena.clear();
     M.arena.reserve((size_t)(ne * 1.4 + nf * 2.2 + nv * 0.6) + 64 * (size_t)np);
+    M.nrm.clear();
+    M.nrm.reserve((size_t)(nf * 2.0 + nv * 1.6) + 16 * (size_t)np);
+    M.nrm_off.assign((size_t)np + 1, 0);
     int64_t vv_acc = 0, vf_acc = 0;
     for (int32_t p = 0; p < np; ++p) {
         lf.clear();
@@ -337,6 +341,35 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
                 }
             }
         }
+        // vertex-normal incidence block: local FV, then the owned vertices'
+        // incident local faces (input VF order) behind 32-bit offsets
+        {
+            for (int32_t i = 0; i < nFl; ++i) floc[lf[i]] = i;
+            const size_t  b0    = M.nrm.size();
+            const int32_t fvw   = pad4((3 * nFl + 1) / 2);
+            const int32_t offw  = pad4(nVo + 1);
+            int64_t       ninc  = 0;
+            for (int32_t i = 0; i < nVo; ++i) ninc += vf_off[lv[i] + 1] - vf_off[lv[i]];
+            const int32_t incw  = pad4((int32_t)((ninc + 1) / 2));
+            M.nrm.resize(b0 + fvw + offw + incw, 0u);
+            uint16_t* fv16 = reinterpret_cast<uint16_t*>(M.nrm.data() + b0);
+            for (int32_t i = 0; i < nFl; ++i)
+                for (int k = 0; k < 3; ++k) fv16[3 * i + k] = (uint16_t)vloc[fv[3 * lf[i] + k]];
+            uint32_t* off   = M.nrm.data() + b0 + fvw;
+            uint16_t* inc16 = reinterpret_cast<uint16_t*>(off + offw);
+            uint32_t  j     = 0;
+            for (int32_t i = 0; i < nVo; ++i) {
+                off[i] = j;
+                for (int32_t t = vf_off[lv[i]]; t < vf_off[lv[i] + 1]; ++t)
+                    inc16[j++] = (uint16_t)floc[vf_val[t]];
+            }
+            off[nVo] = j;
+            if (M.nrm.size() > (size_t)INT32_MAX) {
+                set_error("vertex-normal incidence tables exceed 2^31 words");
+                return RXG_ERR_PATCH_LIMIT;
+            }
+            M.nrm_off[p + 1] = (int32_t)M.nrm.size();
+        }
         h.rv_off = (int32_t)M.arena.size();
         for (int32_t i = nVo; i < nVl; ++i) M.arena.push_back((uint32_t)M.v_i2l[lv[i]]);
         M.arena.resize(h.rv_off + pad4(nVl - nVo), 0u);
@@ -383,6 +416,8 @@ static rxg_status upload(Mesh& M)
     if ((s = up((void**)&M.d.hdr, M.hdr.data(), M.hdr.size() * sizeof(PatchHdr)))) return s;
     M.d.arena_words = (int64_t)M.arena.size();
     if ((s = up((void**)&M.d.arena, M.arena.data(), M.arena.size() * 4))) return s;
+    if ((s = up((void**)&M.d.nrm, M.nrm.data(), M.nrm.size() * 4))) return s;
+    if ((s = up((void**)&M.d.nrm_off, M.nrm_off.data(), M.nrm_off.size() * 4))) return s;
     if ((s = up((void**)&M.d.v_l2i, M.v_l2i.data(), M.v_l2i.size() * 4))) return s;
     if ((s = up((void**)&M.d.e_l2i, M.e_l2i.data(), M.e_l2i.size() * 4))) return s;
     if ((s = up((void**)&M.d.f_l2i, M.f_l2i.data(), M.f_l2i.size() * 4))) return s;
@@ -393,6 +428,8 @@ static void free_device(Mesh& M)
 {
     cudaFree(M.d.hdr);
     cudaFree(M.d.arena);
+    cudaFree(M.d.nrm);
+    cudaFree(M.d.nrm_off);
     cudaFree(M.d.v_l2i);
     cudaFree(M.d.e_l2i);
     cudaFree(M.d.f_l2i);

@@ -279,14 +279,20 @@ __global__ void __launch_bounds__(kQT) k_query_elem(const PatchHdr* __restrict__
 }
 
 // ---------------------------------------------------------------------
-// Vertex normals (OP 5): per patch, every local face (owned + ribbon)
-// contributes to the patch's owned vertices in shared memory, so owned
-// normals are written once, with no global atomics and no zero-fill pass.
+// Vertex normals (OP 5): per patch, each owned vertex sums the normals of
+// its incident faces (owned and ribbon), listed in the patch's incidence
+// block, which the static topology builds once: no shared-memory float
+// atomics, and a fixed summation order (input VF order), so the result is
+// deterministic.  Each face normal is formed from the face's corners in
+// their input order, the arithmetic of a per-face scatter, so every
+// contribution is the same float as in a face-centred kernel.
 // Formula of compute_vertex_normal (apps/VertexNormal/vertex_normal_kernel.cuh:10-43).
 // ---------------------------------------------------------------------
 
 template <int W, int kQT>
 __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restrict__ hdrs,
+                                                        const int32_t* __restrict__ nrm_off,
+                                                        const uint32_t* __restrict__ nrm,
                                                         const uint32_t* __restrict__ arena,
                                                         const float* __restrict__ xyz,
                                                         float* __restrict__ out, int* err)
@@ -294,69 +300,68 @@ __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restri
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ uint64_t bar;
 
-    const PatchHdr h   = load_hdr(hdrs);
-    const int32_t  nVo = h.nVo, nVr = h.nVl - h.nVo;
-    uint32_t* s_ev  = smem;
-    uint32_t* s_fe  = s_ev + pad4i(h.nEl);
-    float*    s_pos = reinterpret_cast<float*>(s_fe + pad4i((int32_t)fe_words(h.nFl)));
-    float*    s_acc = s_pos + pad4i(3 * h.nVl);
+    const PatchHdr h     = load_hdr(hdrs);
+    const int32_t  nVo   = h.nVo, nVr = h.nVl - h.nVo;
+    const int32_t  b0    = __ldg(nrm_off + blockIdx.x);
+    const int32_t  words = __ldg(nrm_off + blockIdx.x + 1) - b0;  // > 0, multiple of 4
+    uint32_t*       s_blk = smem;
+    const uint16_t* s_fv  = reinterpret_cast<const uint16_t*>(s_blk);
+    const uint32_t* s_off = s_blk + pad4i((int32_t)fe_words(h.nFl));
+    const uint16_t* s_inc = reinterpret_cast<const uint16_t*>(s_off + pad4i(nVo + 1));
+    float4*         s_pos = reinterpret_cast<float4*>(s_blk + words);
 
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
-    // EV and FE come in by TMA while the threads fetch the positions: owned
-    // ones contiguously, ribbon ones through the ribbon table read straight
-    // from global memory (so neither waits for the other)
+    // the incidence block comes in by TMA while the threads gather the
+    // positions: owned ones from the patch's contiguous range, ribbon ones
+    // through the ribbon table read straight from global memory
     if (threadIdx.x == 0) {
-        const uint32_t eb = pad16_bytes(h.nEl), fb = pad16_bytes((int32_t)fe_words(h.nFl));
-        mbar_arrive_expect_tx(&bar, eb + fb);
-        if (eb) bulk_g2s(s_ev, arena + h.ev_off, eb, &bar);
-        if (fb) bulk_g2s(s_fe, arena + h.fe_off, fb, &bar);
+        mbar_arrive_expect_tx(&bar, 4u * (uint32_t)words);
+        bulk_g2s(s_blk, nrm + b0, 4u * (uint32_t)words, &bar);
     }
-    for (int i = threadIdx.x; i < 3 * nVo; i += kQT) {
-        s_acc[i] = 0.f;
-        s_pos[i] = __ldg(xyz + 3 * (int64_t)h.v_base + i);
-    }
+    const float* xo = xyz + 3 * (int64_t)h.v_base;
+    for (int i = threadIdx.x; i < nVo; i += kQT)
+        s_pos[i] = make_float4(__ldg(xo + 3 * i), __ldg(xo + 3 * i + 1), __ldg(xo + 3 * i + 2), 0.f);
     for (int i = threadIdx.x; i < nVr; i += kQT) {
         const int64_t g = 3 * (int64_t)__ldg(arena + h.rv_off + i);
-        float*        d = s_pos + 3 * (nVo + i);
-        d[0]            = __ldg(xyz + g);
-        d[1]            = __ldg(xyz + g + 1);
-        d[2]            = __ldg(xyz + g + 2);
+        s_pos[nVo + i]  = make_float4(__ldg(xyz + g), __ldg(xyz + g + 1), __ldg(xyz + g + 2), 0.f);
     }
     if (!wait_stage(&bar, err)) return;  // its CTA barrier also orders the position stores
 
-    const uint16_t* fe16 = reinterpret_cast<const uint16_t*>(s_fe);
-    for (int f = threadIdx.x; f < h.nFl; f += kQT) {
-        uint32_t v[3];
-        float3   c[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            v[k] = face_vertex(fe16, s_ev, f, k);
-            c[k] = make_float3(s_pos[3 * v[k]], s_pos[3 * v[k] + 1], s_pos[3 * v[k] + 2]);
-        }
-        if ((int32_t)v[0] >= nVo && (int32_t)v[1] >= nVo && (int32_t)v[2] >= nVo) continue;
-        const float3 u = make_float3(c[1].x - c[0].x, c[1].y - c[0].y, c[1].z - c[0].z);
-        const float3 w = make_float3(c[2].x - c[0].x, c[2].y - c[0].y, c[2].z - c[0].z);
-        const float  n[3] = {u.y * w.z - w.y * u.z, u.z * w.x - w.z * u.x, u.x * w.y - w.x * u.y};
-        float        l[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const float3 a = c[k], b = c[(k + 1) % 3];
-            const float  dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
-            l[k]            = dx * dx + dy * dy + dz * dz;
-        }
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            if ((int32_t)v[k] >= nVo) continue;
-            const float d = W == RXG_NORMAL_MAX ? (l[k] + l[(k + 2) % 3]) : 1.f;
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-                atomicAdd(&s_acc[3 * v[k] + i], W == RXG_NORMAL_MAX ? n[i] / d : n[i]);
-        }
-    }
-    __syncthreads();
     float* o = out + 3 * (int64_t)h.v_base;
-    for (int i = threadIdx.x; i < 3 * nVo; i += kQT) o[i] = s_acc[i];
+    for (int v = threadIdx.x; v < nVo; v += kQT) {
+        float          a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        const uint32_t j1 = s_off[v + 1];
+        for (uint32_t j = s_off[v]; j < j1; ++j) {
+            const uint32_t f  = s_inc[j];
+            const uint32_t i0 = s_fv[3 * f], i1 = s_fv[3 * f + 1], i2 = s_fv[3 * f + 2];
+            const float4   c0 = s_pos[i0], c1 = s_pos[i1], c2 = s_pos[i2];
+            const float3   u  = make_float3(c1.x - c0.x, c1.y - c0.y, c1.z - c0.z);
+            const float3   w  = make_float3(c2.x - c0.x, c2.y - c0.y, c2.z - c0.z);
+            const float    n0 = u.y * w.z - w.y * u.z, n1 = u.z * w.x - w.z * u.x,
+                        n2 = u.x * w.y - w.x * u.y;
+            if (W == RXG_NORMAL_MAX) {
+                // corner k's two edges: l[k] = |c_k - c_k+1|^2 and l[k+2]
+                const float3 e0 = make_float3(c0.x - c1.x, c0.y - c1.y, c0.z - c1.z);
+                const float3 e1 = make_float3(c1.x - c2.x, c1.y - c2.y, c1.z - c2.z);
+                const float3 e2 = make_float3(c2.x - c0.x, c2.y - c0.y, c2.z - c0.z);
+                const float  l0 = e0.x * e0.x + e0.y * e0.y + e0.z * e0.z;
+                const float  l1 = e1.x * e1.x + e1.y * e1.y + e1.z * e1.z;
+                const float  l2 = e2.x * e2.x + e2.y * e2.y + e2.z * e2.z;
+                const float  d  = i0 == (uint32_t)v ? l0 + l2 : (i1 == (uint32_t)v ? l1 + l0 : l2 + l1);
+                a0 += n0 / d;
+                a1 += n1 / d;
+                a2 += n2 / d;
+            } else {
+                a0 += n0;
+                a1 += n1;
+                a2 += n2;
+            }
+        }
+        o[3 * v]     = a0;
+        o[3 * v + 1] = a1;
+        o[3 * v + 2] = a2;
+    }
 }
 
 // ---------------------------------------------------------------------
@@ -377,8 +382,8 @@ static size_t smem_words(const PatchHdr& h, int kind)
             return pad4i(h.nEl) + few + pad4i(nFr) + pad4i(h.nVo + 1) + (3 * h.nFl + 1) / 2 + 4;
         case RXG_OP_FV: return pad4i(h.nEl) + pad4i((3 * h.nFo + 1) / 2) + pad4i(nVr);
         case RXG_OP_EV: return pad4i(h.nEo) + pad4i(nVr);
-        default:  // normals
-            return pad4i(h.nEl) + few + pad4i(3 * h.nVl) + 3 * h.nVo;
+        default:  // normals: positions as float4 behind the incidence block
+            return 4 * (size_t)h.nVl;
     }
 }
 
@@ -386,7 +391,11 @@ void compute_smem_table(Mesh& m)
 {
     for (int kind = 0; kind < 7; ++kind) {
         size_t w = 0;
-        for (const PatchHdr& h : m.hdr) w = std::max(w, smem_words(h, kind));
+        for (size_t p = 0; p < m.hdr.size(); ++p) {
+            size_t pw = smem_words(m.hdr[p], kind);
+            if (kind >= 5) pw += (size_t)(m.nrm_off[p + 1] - m.nrm_off[p]);
+            w = std::max(w, pw);
+        }
         m.smem_bytes[kind] = w * 4;
     }
 }
@@ -480,15 +489,16 @@ template <int BT>
 static rxg_status launch_normals_bt(const Mesh* m, int weighting, const float* xyz, float* out,
                                     cudaStream_t s, PatchRange r)
 {
-    // kind 6: Max weights (normal + corner weights per face), 5: area weights
+    // kind 6: Max weights, 5: area weights (the same shared-memory layout)
     const size_t    smem = query_smem_bytes(m, weighting == RXG_NORMAL_MAX ? 6 : 5);
     int*            err  = device_error_word();
     const PatchHdr* hd   = m->d.hdr;
+    const int32_t*  no   = m->d.nrm_off + r.p0;  // CTA b reads nrm_off[p0 + b], [p0 + b + 1]
     if (weighting == RXG_NORMAL_MAX)
-        return launch(k_vertex_normals<RXG_NORMAL_MAX, BT>, BT, m, smem, s, "normals", r, hd,
-                      (const uint32_t*)m->d.arena, xyz, out, err);
-    return launch(k_vertex_normals<RXG_NORMAL_AREA, BT>, BT, m, smem, s, "normals", r, hd,
-                  (const uint32_t*)m->d.arena, xyz, out, err);
+        return launch(k_vertex_normals<RXG_NORMAL_MAX, BT>, BT, m, smem, s, "normals", r, hd, no,
+                      (const uint32_t*)m->d.nrm, (const uint32_t*)m->d.arena, xyz, out, err);
+    return launch(k_vertex_normals<RXG_NORMAL_AREA, BT>, BT, m, smem, s, "normals", r, hd, no,
+                  (const uint32_t*)m->d.nrm, (const uint32_t*)m->d.arena, xyz, out, err);
 }
 
 static rxg_status launch_normals(const Mesh* m, int weighting, const float* xyz, float* out,
