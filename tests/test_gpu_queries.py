@@ -89,6 +89,48 @@ def test_query_into_host_buffers(oracle, level, patch):
     assert np.allclose(out, dev, rtol=1e-6, atol=1e-7)
 
 
+@pytest.mark.parametrize("level,patch", [(3, 128), (5, 512)])
+def test_query_into_pinned_host_buffers(oracle, level, patch):
+    """Page-locked (and mixed page-locked / pageable) host outputs and inputs
+    through the C ABI give the device results bit for bit (normals) or as the
+    same row sets (adjacency rows are ordered by shared-memory atomics)."""
+    import ctypes
+    from rxmesh_gb300 import Op, RXMeshStatic, _lib
+    L = _lib.load()
+    x, f = meshgen.icosphere(level)
+    rx = RXMeshStatic(f, len(x), patch_size=patch)
+    for op in (Op.VV, Op.VE, Op.VF, Op.FV, Op.EV):
+        rows, nval = rx.query_size(op)
+        csr = op <= Op.VF
+        d_off, d_val = rx.query(op)
+        for pin_off, pin_val in ((True, True), (False, True), (True, False)):
+            if not csr and not pin_val:
+                continue
+            off = None
+            if csr:
+                off = torch.full((rows + 1,), -7, dtype=torch.int32)
+                off = off.pin_memory() if pin_off else off
+            val = torch.full((nval,), -7, dtype=torch.int32)
+            val = val.pin_memory() if pin_val else val
+            _lib.check(L.rxg_query(rx._h, int(op),
+                                   ctypes.c_void_p(off.data_ptr()) if csr else None,
+                                   ctypes.c_void_p(val.data_ptr()), None))
+            if csr:
+                assert torch.equal(off, d_off.cpu()), (op, pin_off, pin_val)
+                assert sorted_rows(off.numpy(), val.numpy()) == \
+                    sorted_rows(off.numpy(), d_val.cpu().numpy()), (op, pin_off, pin_val)
+            else:
+                assert torch.equal(val, d_val.cpu()), op
+    x32 = rx.to_linear(torch.tensor(x, device="cuda")).float()
+    dev = rx.vertex_normals(x32, "max").cpu()
+    for pin_in in (True, False):
+        xin = x32.cpu().pin_memory() if pin_in else x32.cpu()
+        out = torch.full_like(xin, float("nan")).pin_memory()
+        _lib.check(L.rxg_vertex_normals(rx._h, 0, ctypes.c_void_p(xin.data_ptr()),
+                                        ctypes.c_void_p(out.data_ptr()), None))
+        assert torch.equal(out, dev), pin_in
+
+
 @pytest.mark.parametrize("name", ["sphere3", "torus", "cloth", "bunnyhead"])
 def test_normals_against_reference_fixture(oracle, name):
     # fixtures: output of the reference's own vertex_normal_ref (FP64 and FP32)
