@@ -10,11 +10,15 @@
 // with R(J) the polar factor and s1, s2 the singular values of J.
 //
 // Assembly is a vertex-centred gather: each vertex walks the faces of its
-// oriented fan, recomputes their 6x6 Hessians in J-space and writes its own
-// block row [diag, ring...] once, so no atomics are needed and the result
-// is deterministic.
+// oriented fan and writes its own block row [diag, ring...] once, so no
+// atomics are needed and the result is deterministic.  In FP32 each vertex
+// evaluates its fan's faces itself (k_arap_vertex); in FP64, which runs at a
+// small fraction of the FP32 rate, each face is evaluated once into a global
+// record (k_arap_face) that its three vertices then read (k_arap_gather).
 #include <algorithm>
 #include <cfloat>
+#include <cstdlib>
+#include <type_traits>
 
 #include "rxg_device.cuh"
 #include "rxg_lazy.h"
@@ -316,6 +320,158 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 5 : 1) k_arap_vertex(
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
+// Words of one face record: E, dE/du (6), and with the Hessian its 21
+// upper-triangle entries (row-major, a <= b), then the rest-frame inverse
+// (4); padded to whole 16-byte vectors.
+template <bool HESS>
+__host__ __device__ constexpr int rec_words() { return HESS ? 32 : 12; }
+
+// One thread per face: each face's energy, gradient and J-space Hessian are
+// evaluated once into its record (face_E and the energy partials as well).
+template <typename T, bool HESS>
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 5 : 1) k_arap_face(
+    int64_t nf, const int32_t* __restrict__ fv, const T* __restrict__ x,
+    const T* __restrict__ minv, T* __restrict__ rec, T* __restrict__ face_E,
+    double* __restrict__ part)
+{
+    __shared__ double s_red[128 / 32];
+    double            esum = 0;
+    for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nf;
+         f += (int64_t)gridDim.x * blockDim.x) {
+        int32_t v[3];
+        T       x9[9], mi[4], area;
+        load_face(fv, x, minv, (int32_t)f, v, x9, mi, area);
+        FaceDeriv<T> o;
+        arap_face<T, HESS>(x9, mi, area, o);
+        T r[rec_words<HESS>()];
+        r[0] = o.E;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) r[1 + i] = o.gE[i];
+        int t = 7;
+        if (HESS) {
+#pragma unroll
+            for (int a = 0; a < 6; ++a)
+#pragma unroll
+                for (int c = a; c < 6; ++c) r[t++] = o.Hu[a][c];
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) r[t + i] = mi[i];
+#pragma unroll
+        for (int i = t + 4; i < rec_words<HESS>(); ++i) r[i] = T(0);
+        // 16-byte stores of the whole record
+        using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+        constexpr int per = 16 / sizeof(T);
+        V*       dst = reinterpret_cast<V*>(rec + (int64_t)rec_words<HESS>() * f);
+        const V* src = reinterpret_cast<const V*>(r);
+#pragma unroll
+        for (int i = 0; i < rec_words<HESS>() / per; ++i) dst[i] = src[i];
+        if (face_E) face_E[f] = o.E;
+        esum += (double)o.E;
+    }
+    const double t = block_sum_d<128>(esum, s_red);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// the fields of face f's record that the vertex gather needs
+template <typename T, bool HESS>
+__device__ __forceinline__ void load_record(const T* __restrict__ rec, int32_t f, FaceDeriv<T>& o)
+{
+    using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+    constexpr int per = 16 / sizeof(T);
+    T             r[rec_words<HESS>()];
+    const V*      src = reinterpret_cast<const V*>(rec + (int64_t)rec_words<HESS>() * f);
+    V*            dst = reinterpret_cast<V*>(r);
+#pragma unroll
+    for (int i = 0; i < rec_words<HESS>() / per; ++i) dst[i] = __ldg(src + i);
+    o.E = r[0];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) o.gE[i] = r[1 + i];
+    int t = 7;
+    if (HESS) {
+#pragma unroll
+        for (int a = 0; a < 6; ++a)
+#pragma unroll
+            for (int c = a; c < 6; ++c) {
+                o.Hu[a][c] = r[t];
+                o.Hu[c][a] = r[t];
+                ++t;
+            }
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        o.d[1][k] = r[t + k];
+        o.d[2][k] = r[t + 2 + k];
+        o.d[0][k] = -(o.d[1][k] + o.d[2][k]);
+    }
+}
+
+// One thread per vertex p: gradient row and Hessian block row [diag,
+// ring...] from the records of its fan's faces (the same contractions, in
+// the same order, as k_arap_vertex).
+template <typename T, bool HESS>
+__global__ void __launch_bounds__(128) k_arap_gather(
+    int64_t nv, const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ ring_off,
+    const int32_t* __restrict__ ring, const int32_t* __restrict__ ring_face,
+    const int8_t* __restrict__ bnd, const int32_t* __restrict__ fv, const T* __restrict__ rec,
+    T* __restrict__ grad, T* __restrict__ hval)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nv;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t ro = ring_off[p];
+        const int32_t k  = ring_off[p + 1] - ro;
+        const int32_t nf = bnd[p] ? k - 1 : k;
+        const int32_t rp = row_ptr[p];
+        T             g[3] = {0, 0, 0}, D[9], carry[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) D[i] = carry[i] = T(0);
+        for (int32_t i = 0; i < nf; ++i) {
+            const int32_t f    = ring_face[ro + i];
+            const int32_t v[3] = {__ldg(fv + 3 * (int64_t)f), __ldg(fv + 3 * (int64_t)f + 1),
+                                  __ldg(fv + 3 * (int64_t)f + 2)};
+            FaceDeriv<T>  o;
+            load_record<T, HESS>(rec, f, o);
+            const int lp = local_index(v, (int32_t)p);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) g[c] += dsel(o, lp, 0) * o.gE[c] + dsel(o, lp, 1) * o.gE[3 + c];
+            if (HESS) {
+                const int li = local_index(v, ring[ro + i]);
+                const int lj = local_index(v, ring[ro + (i + 1 < k ? i + 1 : 0)]);
+                block_of(o, lp, lp, D);
+                T bi[9];
+#pragma unroll
+                for (int t = 0; t < 9; ++t) bi[t] = carry[t];
+                block_of(o, lp, li, bi);
+                T* slot = hval + 9 * (int64_t)(rp + 1 + i);
+#pragma unroll
+                for (int t = 0; t < 9; ++t) {
+                    slot[t]  = bi[t];
+                    carry[t] = T(0);
+                }
+                block_of(o, lp, lj, carry);
+            }
+        }
+        if (HESS) {
+            if (k > 0) {
+                T* slot = hval + 9 * (int64_t)(rp + 1 + (bnd[p] ? k - 1 : 0));
+                if (bnd[p]) {
+#pragma unroll
+                    for (int t = 0; t < 9; ++t) slot[t] = carry[t];
+                } else {
+#pragma unroll
+                    for (int t = 0; t < 9; ++t) slot[t] += carry[t];
+                }
+            }
+            T* dslot = hval + 9 * (int64_t)rp;
+#pragma unroll
+            for (int t = 0; t < 9; ++t) dslot[t] = D[t];
+        }
+        if (grad) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) grad[3 * p + c] = g[c];
+        }
+    }
+}
+
 __global__ void k_sum_partials(const double* __restrict__ part, int n, double* __restrict__ out)
 {
     double v = 0;
@@ -326,6 +482,7 @@ __global__ void k_sum_partials(const double* __restrict__ part, int n, double* _
 }
 
 }  // namespace rxg
+
 
 using namespace rxg;
 
@@ -380,32 +537,58 @@ rxg_status rxg_arap_eval(const rxg_mesh* h, int32_t dtype, const void* x, const 
         RXG_CUDA_TRY(cudaMemcpyAsync(hess->row_ptr, z->row_ptr, 4 * (nv + 1), cudaMemcpyDeviceToDevice, s));
         RXG_CUDA_TRY(cudaMemcpyAsync(hess->col, z->col, 4 * z->nnz, cudaMemcpyDeviceToDevice, s));
     }
-    const int G = std::min<int>(grid_for_items(nv) * 2, 152 * 16);
-    double*   part;
-    RXG_CUDA_TRY(cudaMallocAsync((void**)&part, sizeof(double) * (G + 1), s));
-#define RXG_ARAP_LAUNCH(T, H)                                                                      \
-    k_arap_vertex<T, H><<<G, 128, 0, s>>>(nv, z->row_ptr, z->ring_off, z->ring, z->ring_face,       \
-                                          z->bnd, h->m.d.fv_lin, (const T*)x, (const T*)rest,       \
-                                          (T*)face_E, (T*)grad, hess ? (T*)hess->val : nullptr, part)
-    if (dtype == RXG_F64) {
-        if (hess)
-            RXG_ARAP_LAUNCH(double, true);
-        else
-            RXG_ARAP_LAUNCH(double, false);
-    } else {
-        if (hess)
-            RXG_ARAP_LAUNCH(float, true);
-        else
-            RXG_ARAP_LAUNCH(float, false);
+    const Mesh&   M  = h->m;
+    const int64_t nf = M.nf;
+    const int     G  = std::min<int>(grid_for_items(nv) * 2, 152 * 16);
+    const int     GF = std::min<int>(grid_for_items(nf) * 2, 152 * 16);
+    // FP32: one thread per vertex evaluating its fan (cheap FP32 arithmetic,
+    // no record traffic).  FP64 (bound by the FP64 pipe): each face evaluated
+    // once into a global record, then the vertex gather.
+    const bool    f64  = dtype == RXG_F64;
+    const int     NP   = f64 ? GF : G;  // energy partials
+    double*       part;
+    void*         rec = nullptr;
+    RXG_CUDA_TRY(scratch_alloc((void**)&part, sizeof(double) * (NP + 1), s));
+    if (f64) {
+        const size_t rb = (size_t)nf * (hess ? rec_words<true>() : rec_words<false>()) * 8;
+        cudaError_t  ea = scratch_alloc(&rec, rb, s);
+        if (ea != cudaSuccess) {
+            cudaFreeAsync(part, s);
+            return cuda_status(ea, "rxg_arap_eval: face records");
+        }
     }
-#undef RXG_ARAP_LAUNCH
-    k_sum_partials<<<1, 32, 0, s>>>(part, G, part + G);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaSuccess;
+    auto launch = [&](auto tag, auto hs) {
+        using T         = decltype(tag);
+        constexpr bool H = decltype(hs)::value;
+        T* hv            = hess ? (T*)hess->val : nullptr;
+        if constexpr (std::is_same<T, float>::value) {
+            k_arap_vertex<T, H><<<G, 128, 0, s>>>(nv, z->row_ptr, z->ring_off, z->ring,
+                                                  z->ring_face, z->bnd, M.d.fv_lin, (const T*)x,
+                                                  (const T*)rest, (T*)face_E, (T*)grad, hv, part);
+        } else {
+            k_arap_face<T, H><<<GF, 128, 0, s>>>(nf, M.d.fv_lin, (const T*)x, (const T*)rest,
+                                                 (T*)rec, (T*)face_E, part);
+            k_arap_gather<T, H><<<G, 128, 0, s>>>(nv, z->row_ptr, z->ring_off, z->ring,
+                                                  z->ring_face, z->bnd, M.d.fv_lin, (const T*)rec,
+                                                  (T*)grad, hv);
+        }
+    };
+    if (dtype == RXG_F64) {
+        if (hess) launch(double{}, std::true_type{});
+        else launch(double{}, std::false_type{});
+    } else {
+        if (hess) launch(float{}, std::true_type{});
+        else launch(float{}, std::false_type{});
+    }
+    k_sum_partials<<<1, 32, 0, s>>>(part, NP, part + NP);
+    if (rec) cudaFreeAsync(rec, s);
+    e = cudaGetLastError();
     if (e == cudaSuccess && energy) {
         if (is_device_ptr(energy))
-            e = cudaMemcpyAsync(energy, part + G, sizeof(double), cudaMemcpyDeviceToDevice, s);
+            e = cudaMemcpyAsync(energy, part + NP, sizeof(double), cudaMemcpyDeviceToDevice, s);
         else {
-            e = cudaMemcpyAsync(energy, part + G, sizeof(double), cudaMemcpyDeviceToHost, s);
+            e = cudaMemcpyAsync(energy, part + NP, sizeof(double), cudaMemcpyDeviceToHost, s);
             if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         }
     }

@@ -105,6 +105,10 @@ rxg_status  cuda_status(cudaError_t e, const char* what);
 // pinned or registered) returns false.
 bool is_device_ptr(const void* p);
 
+// Stream-ordered device scratch from the library's own pool (freed with
+// cudaFreeAsync); freed blocks stay in the pool for later calls.
+cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t s);
+
 // Lazily allocated per-mesh device scratch and the oriented ring.
 struct Lazy;
 Lazy* lazy_of(const Mesh* m);

@@ -1215,7 +1215,7 @@ rxg_status rxg_query_oriented_vv(const rxg_mesh* h, int32_t* offsets, int32_t* v
         return RXG_ERR_NONMANIFOLD;
     }
     int8_t* b = boundary;
-    if (!b) RXG_CUDA_TRY(cudaMallocAsync((void**)&b, std::max<int64_t>(16, h->m.nv), S_(stream)));
+    if (!b) RXG_CUDA_TRY(scratch_alloc((void**)&b, std::max<int64_t>(16, h->m.nv), S_(stream)));
     rxg_status st = launch_oriented(&h->m, offsets, values, b, nullptr, S_(stream));
     if (!boundary) cudaFreeAsync(b, S_(stream));
     if (st) return st;
@@ -1298,12 +1298,12 @@ rxg_status rxg_cg_solve(const rxg_csr* A, int32_t nc, const void* B, void* X,
     uint8_t*         scratch = nullptr;
     if (A->dtype == RXG_F64) {
         const size_t bytes = cg_scratch_bytes<double>(A->n, nc, cg_grid_any<double>(nc, pc, A->n));
-        RXG_CUDA_TRY(cudaMallocAsync((void**)&scratch, bytes, s));
+        RXG_CUDA_TRY(scratch_alloc((void**)&scratch, bytes, s));
         st = cg_dispatch<double>(nc, A->n, A->row_ptr, A->col, (const double*)A->val,
                                  (const double*)B, (double*)X, *opts, &local, scratch, s);
     } else {
         const size_t bytes = cg_scratch_bytes<float>(A->n, nc, cg_grid_any<float>(nc, pc, A->n));
-        RXG_CUDA_TRY(cudaMallocAsync((void**)&scratch, bytes, s));
+        RXG_CUDA_TRY(scratch_alloc((void**)&scratch, bytes, s));
         st = cg_dispatch<float>(nc, A->n, A->row_ptr, A->col, (const float*)A->val,
                                 (const float*)B, (float*)X, *opts, &local, scratch, s);
     }
@@ -1356,7 +1356,7 @@ rxg_status rxg_mcf_step(const rxg_mesh* h, double dt, int32_t nsteps, int32_t pr
     double* X      = xyz;
     bool    staged = false;
     if (!is_device_ptr(xyz)) {
-        RXG_CUDA_TRY(cudaMallocAsync((void**)&X, 24 * n, s));
+        RXG_CUDA_TRY(scratch_alloc((void**)&X, 24 * n, s));
         RXG_CUDA_TRY(cudaMemcpyAsync(X, xyz, 24 * n, cudaMemcpyHostToDevice, s));
         staged = true;
     }

@@ -34,6 +34,38 @@ rxg_status cuda_status(cudaError_t e, const char* what)
     return RXG_ERR_CUDA;
 }
 
+// Stream-ordered scratch from a pool the library owns, one per device,
+// created on first use.  Its release threshold keeps freed blocks for reuse,
+// so a call that allocates and frees tens of MB (host-array staging, face
+// records) does not map memory again after every synchronisation, as the
+// device's default pool (release threshold 0) may.
+cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t s)
+{
+    static std::mutex       mu;
+    static cudaMemPool_t    pools[64] = {};
+    int                     dev       = 0;
+    cudaError_t             e         = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaMallocAsync(p, bytes, s);
+    cudaMemPool_t pool;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!pools[dev]) {
+            cudaMemPoolProps props = {};
+            props.allocType        = cudaMemAllocationTypePinned;
+            props.location.type    = cudaMemLocationTypeDevice;
+            props.location.id      = dev;
+            if ((e = cudaMemPoolCreate(&pools[dev], &props)) != cudaSuccess) return e;
+            uint64_t keep = UINT64_MAX;
+            if ((e = cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep)) !=
+                cudaSuccess)
+                return e;
+        }
+        pool = pools[dev];
+    }
+    return cudaMallocFromPoolAsync(p, bytes ? bytes : 16, pool, s);
+}
+
 bool is_device_ptr(const void* p)
 {
     if (p == nullptr) return false;

@@ -531,7 +531,7 @@ static rxg_status stage_out(void* user, size_t bytes, cudaStream_t s, Staged& st
         st.d = user;
         return RXG_OK;
     }
-    RXG_CUDA_TRY(cudaMallocAsync(&st.d, bytes ? bytes : 16, s));
+    RXG_CUDA_TRY(scratch_alloc(&st.d, bytes ? bytes : 16, s));
     st.owns = true;
     return RXG_OK;
 }
@@ -543,7 +543,7 @@ static rxg_status stage_in(const void* user, size_t bytes, cudaStream_t s, Stage
         st.d = const_cast<void*>(user);
         return RXG_OK;
     }
-    RXG_CUDA_TRY(cudaMallocAsync(&st.d, bytes ? bytes : 16, s));
+    RXG_CUDA_TRY(scratch_alloc(&st.d, bytes ? bytes : 16, s));
     st.owns = true;
     RXG_CUDA_TRY(cudaMemcpyAsync(st.d, user, bytes, cudaMemcpyHostToDevice, s));
     return RXG_OK;

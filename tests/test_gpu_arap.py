@@ -42,11 +42,18 @@ def oracle_ref(oracle, f, x0, x, rx, prob):
 
 
 @pytest.mark.parametrize("dtype,rtol", [(torch.float64, 1e-11), (torch.float32, 2e-4)])
-@pytest.mark.parametrize("kind", ["cloth", "bunnyhead", "sphere"])
-def test_arap_matches_oracle(oracle, dtype, rtol, kind):
+@pytest.mark.parametrize("kind", ["cloth", "bunnyhead", "sphere", "cloth_one_patch"])
+@pytest.mark.parametrize("with_hessian", [True, False])
+def test_arap_matches_oracle(oracle, dtype, rtol, kind, with_hessian):
+    """cloth_one_patch: the whole 3,042-face cloth in one patch.  with_hessian
+    False: the gradient-only evaluation agrees with the full one."""
     from rxmesh_gb300 import DiffScalarProblem, RXMeshStatic
+    patch = 128
     if kind == "cloth":
         x0, x, f = cloth()
+    elif kind == "cloth_one_patch":
+        x0, x, f = cloth(40, 6)
+        patch = 4096
     elif kind == "bunnyhead":
         g = golden("bunnyhead")
         x0, f = g["xyz"], g["fv"]
@@ -55,12 +62,22 @@ def test_arap_matches_oracle(oracle, dtype, rtol, kind):
         v, f = meshgen.icosphere(3)
         x0 = v
         x = meshgen.radial_noise(v, 0.05, 2)
-    rx = RXMeshStatic(f, len(x0), patch_size=128)
+    rx = RXMeshStatic(f, len(x0), patch_size=patch)
     dev = "cuda"
     x0l = rx.to_linear(torch.tensor(x0, device=dev))
     xl = rx.to_linear(torch.tensor(x, device=dev))
     prob = DiffScalarProblem(rx, dtype).add_arap_term(x0l)
+    if not with_hessian:
+        # gradient and energies alone first; the full evaluation below must agree
+        prob.eval_terms(xl, with_hessian=False)
+        g_only = prob.grad.clone()
+        e_only = prob.get_current_loss()
     prob.eval_terms(xl)
+    if not with_hessian:
+        tol = 1e-12 if dtype == torch.float64 else 1e-6
+        scale = prob.grad.abs().max().item()
+        assert (g_only - prob.grad).abs().max().item() <= tol * scale
+        assert abs(e_only - prob.get_current_loss()) <= tol * abs(e_only)
     E, fE, g, H, minv = oracle_ref(oracle, f, x0, x, rx, prob)
     # rest frames
     fl = rx.linear_to_input("f")
