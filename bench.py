@@ -42,6 +42,75 @@ def canonical_bytes(V, E, F):
     }
 
 
+EXTRA_OPS = ["EF", "FE", "FF", "EVD"]
+
+
+def extra_canonical_bytes(V, E, F, nff):
+    """Algorithmic bytes of the edge/face queries, in the same canonical form
+    (int16 FE/EV topology read once, int32 ids and offsets written once)."""
+    return {
+        "EF": 6 * F + 12 * F + 4 * (E + 1),
+        "FE": 6 * F + 12 * F,
+        "FF": 6 * F + 4 * nff + 4 * (F + 1),
+        "EVD": 4 * E + 6 * F + 16 * E,
+    }
+
+
+def run_edge_face_queries(args, torch, rx, sizes):
+    """EF, FE, FF and EVDiamond on the sweep's torus, each timed alone after
+    an L2 flush with CUDA events, as in run_sweep (not part of the headline
+    sweep value)."""
+    from rxmesh_gb300 import Op
+    V, E, F = sizes
+    dev = torch.device("cuda")
+    stream = torch.cuda.current_stream()
+    outs = {}
+    for name in EXTRA_OPS:
+        op = getattr(Op, name)
+        rows, nval = rx.query_size(op)
+        outs[name] = (torch.empty(rows + 1, dtype=torch.int32, device=dev) if op in Op.CSR else None,
+                      torch.empty(nval, dtype=torch.int32, device=dev))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    clean = torch.ones(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def one(name):
+        rx.query(getattr(Op, name), offsets=outs[name][0], values=outs[name][1])
+
+    for _ in range(args.warmup):
+        for name in EXTRA_OPS:
+            flush.fill_(1.0)
+            clean.sum()
+            one(name)
+    torch.cuda.synchronize()
+    evs = []
+    for _ in range(3):
+        flush.fill_(1.0)
+        clean.sum()
+    for _ in range(args.steps):
+        for name in EXTRA_OPS:
+            flush.fill_(1.0)
+            clean.sum()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            one(name)
+            b.record(stream)
+            evs.append((name, a, b))
+    torch.cuda.synchronize()
+    per = {k: [] for k in EXTRA_OPS}
+    for name, a, b in evs:
+        per[name].append(a.elapsed_time(b))
+    cb = extra_canonical_bytes(V, E, F, rx.query_size(Op.FF)[1])
+    peak, peak_kind = peaks()
+    res = {"workload": "torus 1024x1024, patches<=512 faces; each op timed alone after an L2 flush"}
+    for k in EXTRA_OPS:
+        ms = statistics.mean(per[k])
+        gbs = cb[k] / (ms * 1e-3) / 1e9
+        res[k] = {"us": 1e3 * ms, "gbs_algorithmic": gbs, "algorithmic_bytes": cb[k],
+                  "frac_of_%s_hbm" % peak_kind: gbs / peak}
+    return res
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -492,13 +561,22 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-arap", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
-    ap.add_argument("--only", choices=["sweep", "mcf", "arap", "batch"],
+    ap.add_argument("--only", choices=["sweep", "queries", "mcf", "arap", "batch"],
                     help="run one workload and print only its results (for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
 
     import torch
+    if args.only == "queries":
+        # the edge / face queries alone (EF, FE, FF, EVDiamond on the sweep's torus)
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        from rxmesh_gb300 import RXMeshStatic, meshgen
+        x, f = meshgen.torus(1024, 1024, jitter=1e-3, seed=0)
+        rx = RXMeshStatic(f, len(x), patch_size=512)
+        sz = (rx.get_num_vertices(), rx.get_num_edges(), rx.get_num_faces())
+        print(json.dumps({"only": "queries", "queries": run_edge_face_queries(args, torch, rx, sz)}))
+        return
     if args.only and args.only != "sweep":
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         fn = {"mcf": run_mcf, "arap": run_arap, "batch": run_batch}[args.only]
@@ -552,6 +630,8 @@ def main():
         "gpu_launches": len(OPS) * args.steps,
         "clocks": clocks,
     }
+    if rank == 0:
+        line["edge_face_queries"] = run_edge_face_queries(args, torch, rx, (V, E, F))
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
         O.build()

@@ -48,7 +48,15 @@ enum {
     RXG_OP_VE = 1, /* vertex -> incident edges      (CSR over vertices) */
     RXG_OP_VF = 2, /* vertex -> incident faces      (CSR over vertices) */
     RXG_OP_FV = 3, /* face   -> 3 vertices          (dense nf x 3)      */
-    RXG_OP_EV = 4  /* edge   -> 2 vertices          (dense ne x 2)      */
+    RXG_OP_EV = 4, /* edge   -> 2 vertices          (dense ne x 2)      */
+    RXG_OP_EF = 5, /* edge   -> incident faces      (CSR over edges)    */
+    RXG_OP_FE = 6, /* face   -> 3 edges, edge k from corner k to k+1 (dense nf x 3) */
+    RXG_OP_FF = 7, /* face   -> faces sharing an edge (CSR over faces)  */
+    RXG_OP_EVD = 8 /* edge   -> diamond: v0, vertex opposite in the face traversing
+                      v0->v1, v1, vertex opposite in the face traversing v1->v0;
+                      -1 where there is no such face (dense ne x 4; Op::EVDiamond,
+                      kernels/rxmesh_queries.cuh:197-262; edge-manifold, consistently
+                      oriented meshes, else RXG_ERR_NONMANIFOLD) */
 };
 
 enum { RXG_ELEM_VERTEX = 0, RXG_ELEM_EDGE = 1, RXG_ELEM_FACE = 2 };
@@ -137,10 +145,12 @@ rxg_status rxg_query_size(const rxg_mesh* m, int32_t op, int64_t* n_rows,
                           int64_t* n_values);
 
 /*
- * Materialise a query for every owned element, in linear ids.  For VV/VE/VF,
- * offsets has n_rows+1 entries (CSR, row = linear vertex id); for FV/EV
- * offsets may be NULL (fixed 3 or 2 entries per row).  Order inside a row is
- * unspecified (RXMesh compares rows as sets, tests/RXMesh_test/rxmesh_test.h:347-440).
+ * Materialise a query for every owned element, in linear ids.  For
+ * VV/VE/VF/EF/FF, offsets has n_rows+1 entries (CSR, row = linear id of the
+ * vertex, edge or face); for FV/EV/FE/EVD offsets may be NULL (fixed 3, 2, 3
+ * or 4 entries per row).  Order inside a CSR row is unspecified (RXMesh
+ * compares rows as sets, tests/RXMesh_test/rxmesh_test.h:347-440).  EF, FE
+ * and FF are Op::EF/FE/FF of kernels/rxmesh_queries.cuh:733-858.
  */
 rxg_status rxg_query(const rxg_mesh* m, int32_t op, int32_t* offsets,
                      int32_t* values, void* stream);

@@ -55,7 +55,11 @@ enum class Op : int32_t {
     VE = RXG_OP_VE,
     VF = RXG_OP_VF,
     FV = RXG_OP_FV,
-    EV = RXG_OP_EV
+    EV = RXG_OP_EV,
+    EF = RXG_OP_EF,
+    FE = RXG_OP_FE,
+    FF = RXG_OP_FF,
+    EVDiamond = RXG_OP_EVD
 };
 
 // where a buffer lives (RXMesh's locationT)
@@ -262,7 +266,7 @@ class RXMeshStatic
         QueryResult r;
         int64_t     nval = 0;
         check(rxg_query_size(handle(), (int32_t)op, &r.rows, &nval));
-        const bool csr = op == Op::VV || op == Op::VE || op == Op::VF;
+        const bool csr = op == Op::VV || op == Op::VE || op == Op::VF || op == Op::EF || op == Op::FF;
         if (csr) r.offsets.resize((size_t)r.rows + 1);
         r.values.resize((size_t)nval);
         check(rxg_query(handle(), (int32_t)op, csr ? r.offsets.data() : nullptr, r.values.data(), s));

@@ -38,6 +38,10 @@ def lib():
         L.orc_build_edges.argtypes = [I64, i32p, i32p, i32p]
         L.orc_vv_ve.argtypes = [I64, I64, i32p, ctypes.c_int, i64p, i32p]
         L.orc_vf.argtypes = [I64, I64, i32p, i64p, i32p]
+        L.orc_ef.argtypes = [I64, I64, i32p, i64p, i32p]
+        L.orc_ff.restype = I64
+        L.orc_ff.argtypes = [I64, I64, i64p, i32p, i64p, ctypes.c_void_p]
+        L.orc_ev_diamond.argtypes = [I64, I64, i32p, i32p, i32p, i32p]
         L.orc_vertex_normals.argtypes = [I64, I64, i32p, f64p, ctypes.c_int, f64p]
         L.orc_oriented_vv.restype = ctypes.c_int
         L.orc_oriented_vv.argtypes = [I64, i32p, i64p, i32p, i64p, i32p, i8p]
@@ -112,6 +116,38 @@ def vf(nv, fv):
     val = np.empty(f.size, np.int32)
     lib().orc_vf(nv, f.size // 3, f, off, val)
     return off, val
+
+
+def ef(fv):
+    """Sorted EF rows as CSR over the reference edge numbering (edges(fv))."""
+    f = _fv(fv)
+    ev, fe = edges(fv)
+    off = np.empty(len(ev) + 1, np.int64)
+    val = np.empty(f.size, np.int32)
+    lib().orc_ef(len(ev), f.size // 3, np.ascontiguousarray(fe, np.int32).reshape(-1), off, val)
+    return off, val
+
+
+def ff(fv):
+    """Sorted FF rows (faces sharing an edge) as CSR."""
+    f = _fv(fv)
+    nf = f.size // 3
+    eoff, eval_ = ef(fv)
+    off = np.empty(nf + 1, np.int64)
+    n = lib().orc_ff(nf, len(eoff) - 1, eoff, eval_, off, None)
+    val = np.empty(max(n, 1), np.int32)
+    lib().orc_ff(nf, len(eoff) - 1, eoff, eval_, off, val.ctypes.data)
+    return off, val[:n]
+
+
+def ev_diamond(fv):
+    """EVDiamond rows (ne, 4): [v0, opposite in the v0->v1 face, v1, opposite in the v1->v0 face], -1 = none."""
+    f = _fv(fv)
+    ev, fe = edges(fv)
+    out = np.empty(4 * len(ev), np.int32)
+    lib().orc_ev_diamond(len(ev), f.size // 3, f, np.ascontiguousarray(ev, np.int32).reshape(-1),
+                         np.ascontiguousarray(fe, np.int32).reshape(-1), out)
+    return out.reshape(-1, 4)
 
 
 def vertex_normals(fv, xyz, weighting=0):

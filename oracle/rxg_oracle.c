@@ -140,6 +140,79 @@ void orc_vf(int64_t nv, int64_t nf, const int32_t* fv, int64_t* off, int32_t* va
     sort_rows(nv, off, val);
 }
 
+/*
+ * EF ground truth (the e_f lists of tests/RXMesh_test/rxmesh_test.h:297-315):
+ * every face adds itself to the lists of its three edges (fe from
+ * orc_build_edges).  off: ne+1, val: 3*nf, rows sorted.
+ */
+void orc_ef(int64_t ne, int64_t nf, const int32_t* fe, int64_t* off, int32_t* val)
+{
+    memset(off, 0, sizeof(int64_t) * (size_t)(ne + 1));
+    for (int64_t i = 0; i < 3 * nf; ++i) off[fe[i] + 1]++;
+    for (int64_t e = 0; e < ne; ++e) off[e + 1] += off[e];
+    int64_t* cur = (int64_t*)malloc(sizeof(int64_t) * (size_t)(ne + 1));
+    memcpy(cur, off, sizeof(int64_t) * (size_t)(ne + 1));
+    for (int64_t f = 0; f < nf; ++f)
+        for (int k = 0; k < 3; ++k) val[cur[fe[3 * f + k]]++] = (int32_t)f;
+    free(cur);
+    sort_rows(ne, off, val);
+}
+
+/*
+ * FF ground truth (tests/RXMesh_test/rxmesh_test.h:290-330): for every edge,
+ * each pair of its faces adds each face to the other's list.  ef_off/ef_val
+ * from orc_ef.  With val == NULL only the row counts are written to off
+ * (off[f+1] = count of face f, off[0] = 0, then prefix-summed) and the total
+ * is returned; otherwise the rows are filled (sorted) and the total returned.
+ */
+int64_t orc_ff(int64_t nf, int64_t ne, const int64_t* ef_off, const int32_t* ef_val,
+               int64_t* off, int32_t* val)
+{
+    memset(off, 0, sizeof(int64_t) * (size_t)(nf + 1));
+    for (int64_t e = 0; e < ne; ++e) {
+        const int64_t k = ef_off[e + 1] - ef_off[e];
+        for (int64_t i = ef_off[e]; i < ef_off[e + 1]; ++i) off[ef_val[i] + 1] += k - 1;
+    }
+    for (int64_t f = 0; f < nf; ++f) off[f + 1] += off[f];
+    if (val == NULL) return off[nf];
+    int64_t* cur = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nf + 1));
+    memcpy(cur, off, sizeof(int64_t) * (size_t)(nf + 1));
+    for (int64_t e = 0; e < ne; ++e)
+        for (int64_t i = ef_off[e]; i < ef_off[e + 1]; ++i)
+            for (int64_t j = i + 1; j < ef_off[e + 1]; ++j) {
+                val[cur[ef_val[i]]++] = ef_val[j];
+                val[cur[ef_val[j]]++] = ef_val[i];
+            }
+    free(cur);
+    sort_rows(nf, off, val);
+    return off[nf];
+}
+
+/*
+ * EVDiamond of e_v_diamond (include/rxmesh/kernels/rxmesh_queries.cuh:197-262):
+ * four vertices per edge, out[4e+0] = ev[e][0], out[4e+2] = ev[e][1], and in
+ * slot 1 (slot 3) the vertex opposite the edge in the face that traverses
+ * it from ev[e][0] to ev[e][1] (from ev[e][1] to ev[e][0]); -1 where there is
+ * no such face (boundary).  Face f's edge k runs from corner k to corner
+ * k+1, so its opposite vertex is corner k+2.  Edge-manifold meshes.
+ */
+void orc_ev_diamond(int64_t ne, int64_t nf, const int32_t* fv, const int32_t* ev,
+                    const int32_t* fe, int32_t* out)
+{
+    for (int64_t e = 0; e < ne; ++e) {
+        out[4 * e + 0] = ev[2 * e];
+        out[4 * e + 1] = -1;
+        out[4 * e + 2] = ev[2 * e + 1];
+        out[4 * e + 3] = -1;
+    }
+    for (int64_t f = 0; f < nf; ++f)
+        for (int k = 0; k < 3; ++k) {
+            const int32_t e   = fe[3 * f + k];
+            const int     dir = ev[2 * e] == fv[3 * f + k] ? 0 : 1;
+            out[4 * e + 1 + 2 * dir] = fv[3 * f + (k + 2) % 3];
+        }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Vertex normals                                                            */
 /* ------------------------------------------------------------------------ */

@@ -19,9 +19,12 @@ __all__ = ["Op", "RXMeshStatic", "SparseMatrix", "CGSolver", "PCGSolver", "RXGEr
 
 
 class Op:
-    """Query operations (RXMesh's Op enum, include/rxmesh/types.h)."""
-    VV, VE, VF, FV, EV = 0, 1, 2, 3, 4
-    NAMES = {"VV": 0, "VE": 1, "VF": 2, "FV": 3, "EV": 4}
+    """Query operations (RXMesh's Op enum, include/rxmesh/types.h).  EVD is
+    Op::EVDiamond.  CSR (offsets + values): VV, VE, VF, EF, FF; fixed rows:
+    FV (3), EV (2), FE (3), EVD (4, -1 where the edge has no such face)."""
+    VV, VE, VF, FV, EV, EF, FE, FF, EVD = 0, 1, 2, 3, 4, 5, 6, 7, 8
+    NAMES = {"VV": 0, "VE": 1, "VF": 2, "FV": 3, "EV": 4, "EF": 5, "FE": 6, "FF": 7, "EVD": 8}
+    CSR = (0, 1, 2, 5, 7)
 
 
 _ELEM = {"v": 0, "vertex": 0, "e": 1, "edge": 1, "f": 2, "face": 2}
@@ -156,12 +159,12 @@ class RXMeshStatic:
     def query(self, op, stream=None, offsets=None, values=None):
         """Materialise query `op` for all owned elements, in linear ids.
 
-        Returns (offsets, values) int32 CUDA tensors; offsets is None for FV/EV
-        (3 or 2 values per row)."""
+        Returns (offsets, values) int32 CUDA tensors; offsets is None for the
+        fixed-row ops FV, EV, FE, EVD (3, 2, 3, 4 values per row)."""
         op = Op.NAMES.get(op, op) if isinstance(op, str) else int(op)
         rows, nval = self.query_size(op)
         dev = torch.device("cuda", torch.cuda.current_device())
-        csr = op <= Op.VF
+        csr = int(op) in Op.CSR
         if csr and offsets is None:
             offsets = torch.empty(rows + 1, dtype=torch.int32, device=dev)
         if values is None:

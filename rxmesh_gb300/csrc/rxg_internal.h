@@ -47,6 +47,8 @@ struct DeviceTopo
     // per-patch incidence blocks of the vertex-normal kernel (see Mesh::nrm)
     uint32_t* nrm     = nullptr;
     int32_t*  nrm_off = nullptr;
+    // ef_base (np+1) then ff_base (np+1), see Mesh::ef_base
+    int32_t* qbase = nullptr;
 };
 
 struct Mesh
@@ -56,6 +58,7 @@ struct Mesh
     int32_t num_patches = 0;
     int32_t device      = 0;
     bool    closed = true, edge_manifold = true;
+    bool    oriented = true;  // no edge traversed in the same direction by two of its faces
     int64_t max_valence = 0;
     int32_t max_vl = 0, max_el = 0, max_fl = 0, max_vo = 0, max_eo = 0, max_fo = 0;
     int64_t ribbon_v = 0, ribbon_f = 0;
@@ -72,6 +75,9 @@ struct Mesh
     // once with the patches.
     std::vector<uint32_t> nrm;
     std::vector<int32_t>  nrm_off;
+    // first EF / FF value of each patch's owned rows (np+1 each; the last
+    // entry is the total): the CSR bases of the edge and face queries
+    std::vector<int32_t> ef_base, ff_base;
 
     DeviceTopo d;
 
@@ -79,7 +85,7 @@ struct Mesh
     void* lazy = nullptr;
 
     int64_t device_bytes = 0;
-    size_t  smem_bytes[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // per query kind, max over patches
+    size_t  smem_bytes[16] = {};  // per kernel kind (query op; 9, 10: normals), max over patches
 
     // calls with host arrays: a copy stream and events that overlap the
     // device-to-host copy of each slice of patches with the kernel of the next

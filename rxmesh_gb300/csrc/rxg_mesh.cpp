@@ -153,8 +153,15 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
     }
     {
         std::vector<int32_t> cur(ef_off.begin(), ef_off.end() - 1);
+        std::vector<uint8_t> dirs(ne, 0);  // bit 0 / 1: traversed from ev[0] / ev[1]
         for (int64_t f = 0; f < nf; ++f)
-            for (int k = 0; k < 3; ++k) ef_val[cur[fe[3 * f + k]]++] = (int32_t)f;
+            for (int k = 0; k < 3; ++k) {
+                const int32_t e = fe[3 * f + k];
+                ef_val[cur[e]++] = (int32_t)f;
+                const uint8_t bit = M.ev_in[2 * e] == fv[3 * f + k] ? 1 : 2;
+                if (dirs[e] & bit) M.oriented = false;
+                dirs[e] |= bit;
+            }
     }
     std::vector<int32_t> vf_off(nv + 1, 0), vf_val(3 * nf), valence(nv, 0);
     for (int64_t i = 0; i < 3 * nf; ++i) vf_off[fv[i] + 1]++;
@@ -269,7 +276,9 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
     M.nrm.clear();
     M.nrm.reserve((size_t)(nf * 2.0 + nv * 1.6) + 16 * (size_t)np);
     M.nrm_off.assign((size_t)np + 1, 0);
-    int64_t vv_acc = 0, vf_acc = 0;
+    int64_t vv_acc = 0, vf_acc = 0, ef_acc = 0, ff_acc = 0;
+    M.ef_base.assign((size_t)np + 1, 0);
+    M.ff_base.assign((size_t)np + 1, 0);
     for (int32_t p = 0; p < np; ++p) {
         lf.clear();
         lv.clear();
@@ -302,6 +311,22 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
                 if (fstamp[f] != p) {
                     fstamp[f] = p;
                     lf.push_back(f);
+                }
+            }
+        }
+        // and the faces sharing an edge with an owned face, so that every
+        // face of an owned edge, and every edge neighbour of an owned face,
+        // is local (the edge and face queries read them)
+        for (int32_t i = 0; i < nFo; ++i) {
+            const int32_t f = lf[i];
+            for (int k = 0; k < 3; ++k) {
+                const int32_t e = fe[3 * f + k];
+                for (int32_t t = ef_off[e]; t < ef_off[e + 1]; ++t) {
+                    const int32_t g = ef_val[t];
+                    if (fstamp[g] != p) {
+                        fstamp[g] = p;
+                        lf.push_back(g);
+                    }
                 }
             }
         }
@@ -351,6 +376,20 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
             vv_acc += valence[lv[i]];
             vf_acc += vf_off[lv[i] + 1] - vf_off[lv[i]];
         }
+        M.ef_base[p] = (int32_t)ef_acc;
+        M.ff_base[p] = (int32_t)ff_acc;
+        for (int32_t i = 0; i < nEo; ++i) ef_acc += ef_off[le[i] + 1] - ef_off[le[i]];
+        for (int32_t i = 0; i < nFo; ++i)
+            for (int k = 0; k < 3; ++k) {
+                const int32_t e = fe[3 * lf[i] + k];
+                ff_acc += ef_off[e + 1] - ef_off[e] - 1;
+            }
+        if (ef_acc > INT32_MAX || ff_acc > INT32_MAX) {
+            set_error("edge/face query sizes exceed 2^31 values");
+            return RXG_ERR_PATCH_LIMIT;
+        }
+        M.ef_base[p + 1] = (int32_t)ef_acc;
+        M.ff_base[p + 1] = (int32_t)ff_acc;
         // arena slices
         h.ev_off = (int32_t)M.arena.size();
         for (int32_t i = 0; i < nEl; ++i) {
@@ -426,7 +465,7 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
         M.ribbon_f += nFl - nFo;
     }
     (void)nfp;
-    if (vv_acc != 2 * ne || vf_acc != 3 * nf) {
+    if (vv_acc != 2 * ne || vf_acc != 3 * nf || ef_acc != 3 * nf) {
         set_error("internal: value counts %lld/%lld do not match 2E/3F", (long long)vv_acc,
                   (long long)vf_acc);
         return RXG_ERR_INVALID;
@@ -450,6 +489,11 @@ static rxg_status upload(Mesh& M)
     if ((s = up((void**)&M.d.arena, M.arena.data(), M.arena.size() * 4))) return s;
     if ((s = up((void**)&M.d.nrm, M.nrm.data(), M.nrm.size() * 4))) return s;
     if ((s = up((void**)&M.d.nrm_off, M.nrm_off.data(), M.nrm_off.size() * 4))) return s;
+    {
+        std::vector<int32_t> qb(M.ef_base);
+        qb.insert(qb.end(), M.ff_base.begin(), M.ff_base.end());
+        if ((s = up((void**)&M.d.qbase, qb.data(), qb.size() * 4))) return s;
+    }
     if ((s = up((void**)&M.d.v_l2i, M.v_l2i.data(), M.v_l2i.size() * 4))) return s;
     if ((s = up((void**)&M.d.e_l2i, M.e_l2i.data(), M.e_l2i.size() * 4))) return s;
     if ((s = up((void**)&M.d.f_l2i, M.f_l2i.data(), M.f_l2i.size() * 4))) return s;
@@ -462,6 +506,7 @@ static void free_device(Mesh& M)
     cudaFree(M.d.arena);
     cudaFree(M.d.nrm);
     cudaFree(M.d.nrm_off);
+    cudaFree(M.d.qbase);
     cudaFree(M.d.v_l2i);
     cudaFree(M.d.e_l2i);
     cudaFree(M.d.f_l2i);

@@ -120,35 +120,47 @@ __device__ __forceinline__ uint32_t face_vertex(const uint16_t* s_fe, const uint
 // VV / VE  (OP 0 / 1) and VF (OP 2): vertex-centred transposes
 // ---------------------------------------------------------------------
 
+// EF (OP 5) is the same transpose with rows = owned edges: every local
+// face adds itself to the rows of its owned edges.  qb: first EF value of
+// each patch's rows (indexed like hdrs; unused by the other ops).
 template <int OP, int kQT>
 __global__ void __launch_bounds__(kQT) k_query_vertex(const PatchHdr* __restrict__ hdrs,
                                                       const uint32_t* __restrict__ arena,
                                                       int32_t* __restrict__ out_off,
-                                                      int32_t* __restrict__ out_val, int* err)
+                                                      int32_t* __restrict__ out_val, int* err,
+                                                      const int32_t* __restrict__ qb)
 {
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ uint64_t bar;
     __shared__ int32_t  s_warp[kQT / 32];
 
+    constexpr bool EF  = OP == RXG_OP_EF;
+    constexpr bool FCE = OP == 2 || EF;  // walks the local faces
     const PatchHdr h   = load_hdr(hdrs);
     const int32_t  nVo = h.nVo;
+    const int32_t  nRows = EF ? h.nEo : nVo;
     const int32_t  nRib = OP == 0 ? h.nVl - h.nVo : (OP == 1 ? h.nEl - h.nEo : h.nFl - h.nFo);
     const int32_t  ribOff = OP == 0 ? h.rv_off : (OP == 1 ? h.re_off : h.rf_off);
 
     // shared layout (all 16-byte aligned); the patch's rows are staged as
     // 16-bit local ids and mapped to linear ids on the way out
     uint32_t* s_ev  = smem;
-    uint32_t* s_fe  = s_ev + pad4i(h.nEl);
-    uint32_t* s_rib = s_fe + (OP == 2 ? pad4i((int32_t)fe_words(h.nFl)) : 0);
+    uint32_t* s_fe  = s_ev + (EF ? 0 : pad4i(h.nEl));
+    uint32_t* s_rib = s_fe + (FCE ? pad4i((int32_t)fe_words(h.nFl)) : 0);
     int32_t*  s_cnt = reinterpret_cast<int32_t*>(s_rib + pad4i(nRib));
-    uint16_t* s_out = reinterpret_cast<uint16_t*>(s_cnt + pad4i(nVo + 1));
+    uint16_t* s_out = reinterpret_cast<uint16_t*>(s_cnt + pad4i(nRows + 1));
 
     if (threadIdx.x == 0) mbar_init(&bar, 1);
-    for (int i = threadIdx.x; i <= nVo; i += kQT) s_cnt[i] = 0;
+    for (int i = threadIdx.x; i <= nRows; i += kQT) s_cnt[i] = 0;
     __syncthreads();
 
     bool ok;
-    if (OP == 2) {
+    if (EF) {
+        uint32_t* const dst[2] = {s_fe, s_rib};
+        const Slice     sl[2]  = {{arena + h.fe_off, pad16_bytes((int32_t)fe_words(h.nFl))},
+                                  {arena + ribOff, pad16_bytes(nRib)}};
+        ok = stage(&bar, dst, sl, err);
+    } else if (OP == 2) {
         uint32_t* const dst[3] = {s_ev, s_fe, s_rib};
         const Slice     sl[3]  = {{arena + h.ev_off, pad16_bytes(h.nEl)},
                                   {arena + h.fe_off, pad16_bytes((int32_t)fe_words(h.nFl))},
@@ -166,8 +178,16 @@ __global__ void __launch_bounds__(kQT) k_query_vertex(const PatchHdr* __restrict
     const uint2*    ev2  = reinterpret_cast<const uint2*>(s_ev);  // two edges per load
     const int32_t   nE2  = (h.nEl + 1) >> 1;
 
-    // 1. count owned-vertex incidences
-    if (OP == 2) {
+    // 1. count owned-vertex (EF: owned-edge) incidences
+    if (EF) {
+        for (int f = threadIdx.x; f < h.nFl; f += kQT) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t e = (uint32_t)fe16[3 * f + k] >> 1;
+                if ((int32_t)e < nRows) atomicAdd(&s_cnt[e], 1);
+            }
+        }
+    } else if (OP == 2) {
         for (int f = threadIdx.x; f < h.nFl; f += kQT) {
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
@@ -189,14 +209,23 @@ __global__ void __launch_bounds__(kQT) k_query_vertex(const PatchHdr* __restrict
     __syncthreads();
 
     // 2. exclusive scan -> row offsets of the patch's owned rows
-    const int32_t total = block_exclusive_scan<kQT>(s_cnt, nVo + 1, s_warp);
-    const int32_t vbase = OP == 2 ? h.vf_base : h.vv_base;
-    for (int v = threadIdx.x; v <= nVo; v += kQT) out_off[h.v_base + v] = vbase + s_cnt[v];
+    const int32_t total   = block_exclusive_scan<kQT>(s_cnt, nRows + 1, s_warp);
+    const int32_t vbase   = EF ? __ldg(qb + blockIdx.x) : (OP == 2 ? h.vf_base : h.vv_base);
+    const int32_t rowbase = EF ? h.e_base : h.v_base;
+    for (int v = threadIdx.x; v <= nRows; v += kQT) out_off[rowbase + v] = vbase + s_cnt[v];
     __syncthreads();
 
     // 3. scatter 16-bit local ids into the staged chunk
     uint16_t* sbuf = s_out + (vbase & 3);  // element g lives at s_out[g - (vbase & ~3)]
-    if (OP == 2) {
+    if (EF) {
+        for (int f = threadIdx.x; f < h.nFl; f += kQT) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t e = (uint32_t)fe16[3 * f + k] >> 1;
+                if ((int32_t)e < nRows) sbuf[atomicAdd(&s_cnt[e], 1)] = (uint16_t)f;
+            }
+        }
+    } else if (OP == 2) {
         for (int f = threadIdx.x; f < h.nFl; f += kQT) {
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
@@ -220,7 +249,7 @@ __global__ void __launch_bounds__(kQT) k_query_vertex(const PatchHdr* __restrict
 
     // 4. contiguous, vectorised write-out, local -> linear ids
     const int32_t   nOwn = OP == 0 ? nVo : (OP == 1 ? h.nEo : h.nFo);
-    const int32_t   base = OP == 0 ? h.v_base : (OP == 1 ? h.e_base : h.f_base);
+    const int32_t   base = OP == 0 ? h.v_base : (OP == 1 ? h.e_base : h.f_base);  // VF, EF: faces
     const uint32_t* rib  = s_rib;
     store_u16_mapped<kQT>(out_val, vbase, s_out, total, [=](uint32_t loc) -> int32_t {
         return (int32_t)loc < nOwn ? base + (int32_t)loc : (int32_t)rib[loc - nOwn];
@@ -239,13 +268,19 @@ __global__ void __launch_bounds__(kQT) k_query_elem(const PatchHdr* __restrict__
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ uint64_t bar;
 
+    constexpr bool FE  = OP == RXG_OP_FE, EVD = OP == RXG_OP_EVD;
     const PatchHdr h   = load_hdr(hdrs);
     const int32_t  nVo = h.nVo;
     const int32_t  nVr = h.nVl - h.nVo;
     // FV needs every local edge an owned face uses, i.e. the whole EV slice;
-    // EV needs only the owned prefix.
-    const int32_t ev_words = OP == 3 ? h.nEl : h.nEo;
-    const int32_t fe_w     = OP == 3 ? (int32_t)fe_words(h.nFo) : 0;
+    // EV needs only the owned prefix; FE needs no EV; EVD needs the whole
+    // EV slice and every local face (the faces of the owned edges).
+    const int32_t ev_words = (OP == 3 || EVD) ? h.nEl : (FE ? 0 : h.nEo);
+    const int32_t fe_w     = EVD ? (int32_t)fe_words(h.nFl)
+                                 : ((OP == 3 || FE) ? (int32_t)fe_words(h.nFo) : 0);
+    // ribbon table of the output ids: vertices, or edges for FE
+    const int32_t rib_n   = FE ? h.nEl - h.nEo : nVr;
+    const int32_t rib_off = FE ? h.re_off : h.rv_off;
 
     uint32_t* s_ev = smem;
     uint32_t* s_fe = s_ev + pad4i(ev_words);
@@ -256,11 +291,51 @@ __global__ void __launch_bounds__(kQT) k_query_elem(const PatchHdr* __restrict__
     uint32_t* const dst[3] = {s_ev, s_fe, s_rv};
     const Slice     sl[3]  = {{arena + h.ev_off, pad16_bytes(ev_words)},
                               {arena + h.fe_off, pad16_bytes(fe_w)},
-                              {arena + h.rv_off, pad16_bytes(nVr)}};
+                              {arena + rib_off, pad16_bytes(rib_n)}};
     if (!stage(&bar, dst, sl, err)) return;
 
     const uint16_t* fe16 = reinterpret_cast<const uint16_t*>(s_fe);
-    if (OP == 3) {
+    if (FE) {
+        // edge k of face f runs from corner k to corner k+1 (FE order)
+        const int32_t n    = 3 * h.nFo;
+        int32_t*      base = out_val + 3 * (int64_t)h.f_base;
+        for (int i = threadIdx.x; i < n; i += kQT) {
+            const uint32_t e = (uint32_t)fe16[i] >> 1;
+            base[i] = (int32_t)e < h.nEo ? h.e_base + (int32_t)e : (int32_t)s_rv[e - h.nEo];
+        }
+    } else if (EVD) {
+        // four 16-bit slots per owned edge: v0, opposite vertex in the face
+        // traversing v0->v1, v1, opposite vertex in the face traversing
+        // v1->v0 (0xffff: no such face).  Local ids fit 16 bits with 0xffff
+        // to spare (at most 65,535 local vertices).
+        uint16_t* slot = reinterpret_cast<uint16_t*>(s_rv + pad4i(nVr));
+        for (int e = threadIdx.x; e < h.nEo; e += kQT) {
+            const uint32_t ev = s_ev[e];
+            slot[4 * e + 0]   = (uint16_t)(ev & 0xffffu);
+            slot[4 * e + 1]   = 0xffffu;
+            slot[4 * e + 2]   = (uint16_t)(ev >> 16);
+            slot[4 * e + 3]   = 0xffffu;
+        }
+        __syncthreads();
+        // every local face names the vertex opposite each of its edges
+        // (corner k+2 for edge k); on an edge-manifold mesh the two faces of
+        // an edge traverse it in opposite directions, so each slot has one writer
+        for (int i = threadIdx.x; i < 3 * h.nFl; i += kQT) {
+            const uint32_t fe = fe16[i];
+            const uint32_t e  = fe >> 1;
+            if ((int32_t)e >= h.nEo) continue;
+            const int f = i / 3, k = i - 3 * f;
+            slot[4 * e + 1 + 2 * (fe & 1u)] = (uint16_t)face_vertex(fe16, s_ev, f, k == 0 ? 2 : k - 1);
+        }
+        __syncthreads();
+        const int32_t n    = 4 * h.nEo;
+        int32_t*      base = out_val + 4 * (int64_t)h.e_base;
+        for (int i = threadIdx.x; i < n; i += kQT) {
+            const uint32_t v = slot[i];
+            base[i] = v == 0xffffu ? -1
+                                   : ((int32_t)v < nVo ? h.v_base + (int32_t)v : (int32_t)s_rv[v - nVo]);
+        }
+    } else if (OP == 3) {
         const int32_t n    = 3 * h.nFo;
         int32_t*      base = out_val + 3 * (int64_t)h.f_base;
         for (int i = threadIdx.x; i < n; i += kQT) {
@@ -279,7 +354,157 @@ __global__ void __launch_bounds__(kQT) k_query_elem(const PatchHdr* __restrict__
 }
 
 // ---------------------------------------------------------------------
-// Vertex normals (OP 5): per patch, each owned vertex sums the normals of
+// FF (OP 7): faces sharing an edge with each owned face.  Per patch: the
+// local EF lists of every local edge (counting sort over the local faces,
+// which include every edge neighbour of an owned face), then one thread per
+// owned face walks its three edges' lists.  qb: first FF value of each
+// patch's rows (indexed like hdrs).  Ground truth of
+// tests/RXMesh_test/rxmesh_test.h:290-330.
+// ---------------------------------------------------------------------
+
+// FF on an edge-manifold, consistently oriented mesh: every edge has at most
+// one face per traversal direction, so two 16-bit face slots per local edge
+// (no atomics, no scan) give each owned face its neighbour across edge k in
+// the slot of the opposite direction; rows list the neighbours in edge order.
+template <int kQT>
+__global__ void __launch_bounds__(kQT) k_query_ff_oriented(const PatchHdr* __restrict__ hdrs,
+                                                           const uint32_t* __restrict__ arena,
+                                                           int32_t* __restrict__ out_off,
+                                                           int32_t* __restrict__ out_val,
+                                                           int* err,
+                                                           const int32_t* __restrict__ qb)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ uint64_t bar;
+    __shared__ int32_t  s_warp[kQT / 32];
+
+    const PatchHdr h   = load_hdr(hdrs);
+    const int32_t  nFo = h.nFo, nFl = h.nFl, nEl = h.nEl;
+    const int32_t  nFr = nFl - nFo;
+    uint32_t* s_fe   = smem;
+    uint32_t* s_rf   = s_fe + pad4i((int32_t)fe_words(nFl));
+    uint32_t* s_slot = s_rf + pad4i(nFr);                                      // nEl words
+    int32_t*  s_fc   = reinterpret_cast<int32_t*>(s_slot + pad4i(nEl));        // nFo+1
+    uint16_t* s_out  = reinterpret_cast<uint16_t*>(s_fc + pad4i(nFo + 1));
+
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    for (int i = threadIdx.x; i < nEl; i += kQT) s_slot[i] = 0xffffffffu;
+    __syncthreads();
+    uint32_t* const dst[2] = {s_fe, s_rf};
+    const Slice     sl[2]  = {{arena + h.fe_off, pad16_bytes((int32_t)fe_words(nFl))},
+                              {arena + h.rf_off, pad16_bytes(nFr)}};
+    if (!stage(&bar, dst, sl, err)) return;
+    const uint16_t* fe16 = reinterpret_cast<const uint16_t*>(s_fe);
+    uint16_t*       slot = reinterpret_cast<uint16_t*>(s_slot);  // [2e + dir]
+
+    for (int i = threadIdx.x; i < 3 * nFl; i += kQT) slot[fe16[i]] = (uint16_t)(i / 3);
+    __syncthreads();
+    for (int f = threadIdx.x; f < nFo; f += kQT) {
+        int32_t c = 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) c += slot[fe16[3 * f + k] ^ 1u] != 0xffffu;
+        s_fc[f] = c;
+    }
+    if (threadIdx.x == 0) s_fc[nFo] = 0;
+    __syncthreads();
+    const int32_t total = block_exclusive_scan<kQT>(s_fc, nFo + 1, s_warp);
+    const int32_t vbase = __ldg(qb + blockIdx.x);
+    for (int f = threadIdx.x; f <= nFo; f += kQT) out_off[h.f_base + f] = vbase + s_fc[f];
+    uint16_t* sbuf = s_out + (vbase & 3);
+    for (int f = threadIdx.x; f < nFo; f += kQT) {
+        int32_t pos = s_fc[f];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const uint16_t g = slot[fe16[3 * f + k] ^ 1u];
+            if (g != 0xffffu) sbuf[pos++] = g;
+        }
+    }
+    __syncthreads();
+    const uint32_t* rf = s_rf;
+    const int32_t   fb = h.f_base;
+    store_u16_mapped<kQT>(out_val, vbase, s_out, total, [=](uint32_t loc) -> int32_t {
+        return (int32_t)loc < nFo ? fb + (int32_t)loc : (int32_t)rf[loc - nFo];
+    });
+}
+
+template <int kQT>
+__global__ void __launch_bounds__(kQT) k_query_ff(const PatchHdr* __restrict__ hdrs,
+                                                  const uint32_t* __restrict__ arena,
+                                                  int32_t* __restrict__ out_off,
+                                                  int32_t* __restrict__ out_val, int* err,
+                                                  const int32_t* __restrict__ qb)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ uint64_t bar;
+    __shared__ int32_t  s_warp[kQT / 32];
+
+    const PatchHdr h   = load_hdr(hdrs);
+    const int32_t  nFo = h.nFo, nFl = h.nFl, nEl = h.nEl;
+    const int32_t  nFr = nFl - nFo;
+    uint32_t* s_fe  = smem;
+    uint32_t* s_rf  = s_fe + pad4i((int32_t)fe_words(nFl));
+    int32_t*  s_ec  = reinterpret_cast<int32_t*>(s_rf + pad4i(nFr));           // nEl+1
+    uint16_t* s_ef  = reinterpret_cast<uint16_t*>(s_ec + pad4i(nEl + 1));       // 3 nFl
+    int32_t*  s_fc  = reinterpret_cast<int32_t*>(s_ef) + pad4i((3 * nFl + 1) / 2);  // nFo+1
+    uint16_t* s_out = reinterpret_cast<uint16_t*>(s_fc + pad4i(nFo + 1));
+
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    for (int i = threadIdx.x; i <= nEl; i += kQT) s_ec[i] = 0;
+    __syncthreads();
+    uint32_t* const dst[2] = {s_fe, s_rf};
+    const Slice     sl[2]  = {{arena + h.fe_off, pad16_bytes((int32_t)fe_words(nFl))},
+                              {arena + h.rf_off, pad16_bytes(nFr)}};
+    if (!stage(&bar, dst, sl, err)) return;
+    const uint16_t* fe16 = reinterpret_cast<const uint16_t*>(s_fe);
+
+    // 1. local EF: count, scan, scatter (afterwards s_ec[e] is the end of
+    //    row e, so row e is [e ? s_ec[e-1] : 0, s_ec[e]))
+    for (int i = threadIdx.x; i < 3 * nFl; i += kQT) atomicAdd(&s_ec[fe16[i] >> 1], 1);
+    __syncthreads();
+    block_exclusive_scan<kQT>(s_ec, nEl + 1, s_warp);
+    for (int i = threadIdx.x; i < 3 * nFl; i += kQT)
+        s_ef[atomicAdd(&s_ec[fe16[i] >> 1], 1)] = (uint16_t)(i / 3);
+    __syncthreads();
+
+    // 2. FF row lengths of the owned faces: sum over the edges of (faces - 1)
+    for (int f = threadIdx.x; f < nFo; f += kQT) {
+        int32_t c = 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int32_t e = fe16[3 * f + k] >> 1;
+            c += s_ec[e] - (e ? s_ec[e - 1] : 0) - 1;
+        }
+        s_fc[f] = c;
+    }
+    if (threadIdx.x == 0) s_fc[nFo] = 0;
+    __syncthreads();
+    const int32_t total = block_exclusive_scan<kQT>(s_fc, nFo + 1, s_warp);
+    const int32_t vbase = __ldg(qb + blockIdx.x);
+    for (int f = threadIdx.x; f <= nFo; f += kQT) out_off[h.f_base + f] = vbase + s_fc[f];
+
+    // 3. rows: each owned face lists the other faces of its three edges
+    uint16_t* sbuf = s_out + (vbase & 3);
+    for (int f = threadIdx.x; f < nFo; f += kQT) {
+        int32_t pos = s_fc[f];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int32_t e = fe16[3 * f + k] >> 1;
+            for (int32_t j = e ? s_ec[e - 1] : 0; j < s_ec[e]; ++j) {
+                const uint16_t g = s_ef[j];
+                if (g != (uint16_t)f) sbuf[pos++] = g;
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t* rf = s_rf;
+    const int32_t   fb = h.f_base;
+    store_u16_mapped<kQT>(out_val, vbase, s_out, total, [=](uint32_t loc) -> int32_t {
+        return (int32_t)loc < nFo ? fb + (int32_t)loc : (int32_t)rf[loc - nFo];
+    });
+}
+
+// ---------------------------------------------------------------------
+// Vertex normals: per patch, each owned vertex sums the normals of
 // its incident faces (owned and ribbon), listed in the patch's incidence
 // block, which the static topology builds once: no shared-memory float
 // atomics, and a fixed summation order (input VF order), so the result is
@@ -368,6 +593,11 @@ __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restri
 // host side
 // ---------------------------------------------------------------------
 
+// shared-memory table kinds of the normal kernels (after the query ops)
+constexpr int kNormalArea = 9, kNormalMax = 10;
+// and of the oriented-mesh FF kernel
+constexpr int kFFOriented = 11;
+
 // dynamic shared memory (bytes) of one patch for a kernel kind
 static size_t smem_words(const PatchHdr& h, int kind)
 {
@@ -382,6 +612,13 @@ static size_t smem_words(const PatchHdr& h, int kind)
             return pad4i(h.nEl) + few + pad4i(nFr) + pad4i(h.nVo + 1) + (3 * h.nFl + 1) / 2 + 4;
         case RXG_OP_FV: return pad4i(h.nEl) + pad4i((3 * h.nFo + 1) / 2) + pad4i(nVr);
         case RXG_OP_EV: return pad4i(h.nEo) + pad4i(nVr);
+        case RXG_OP_EF: return few + pad4i(nFr) + pad4i(h.nEo + 1) + (3 * h.nFl + 1) / 2 + 4;
+        case RXG_OP_FE: return pad4i((3 * h.nFo + 1) / 2) + pad4i(nEr);
+        case RXG_OP_FF:  // + the patch's FF values, added by compute_smem_table
+            return few + pad4i(nFr) + pad4i(h.nEl + 1) + few + pad4i(h.nFo + 1) + 4;
+        case RXG_OP_EVD: return pad4i(h.nEl) + few + pad4i(nVr) + 2 * (size_t)h.nEo;
+        case kFFOriented:  // + the patch's FF values, added by compute_smem_table
+            return few + pad4i(nFr) + pad4i(h.nEl) + pad4i(h.nFo + 1) + 4;
         default:  // normals: positions as float4 behind the incidence block
             return 4 * (size_t)h.nVl;
     }
@@ -389,11 +626,15 @@ static size_t smem_words(const PatchHdr& h, int kind)
 
 void compute_smem_table(Mesh& m)
 {
-    for (int kind = 0; kind < 7; ++kind) {
+    for (int kind = 0; kind <= kFFOriented; ++kind) {
+        if (kind > RXG_OP_EVD && kind < kNormalArea) continue;
         size_t w = 0;
         for (size_t p = 0; p < m.hdr.size(); ++p) {
             size_t pw = smem_words(m.hdr[p], kind);
-            if (kind >= 5) pw += (size_t)(m.nrm_off[p + 1] - m.nrm_off[p]);
+            if (kind == kNormalArea || kind == kNormalMax)
+                pw += (size_t)(m.nrm_off[p + 1] - m.nrm_off[p]);
+            if (kind == RXG_OP_FF || kind == kFFOriented)
+                pw += (size_t)(m.ff_base[p + 1] - m.ff_base[p] + 1) / 2;
             w = std::max(w, pw);
         }
         m.smem_bytes[kind] = w * 4;
@@ -458,12 +699,22 @@ static rxg_status launch_query_bt(const Mesh* m, int op, int32_t* d_off, int32_t
     int*            err  = device_error_word();
     const PatchHdr* hd   = m->d.hdr;
     const uint32_t* ar   = m->d.arena;
+    const int32_t*  ef_b = m->d.qbase + r.p0;                         // EF bases, indexed like hd
+    const int32_t*  ff_b = m->d.qbase + (m->num_patches + 1) + r.p0;  // FF bases
     switch (op) {
-        case RXG_OP_VV: return launch(k_query_vertex<0, BT>, BT, m, smem, s, "VV", r, hd, ar, d_off, d_val, err);
-        case RXG_OP_VE: return launch(k_query_vertex<1, BT>, BT, m, smem, s, "VE", r, hd, ar, d_off, d_val, err);
-        case RXG_OP_VF: return launch(k_query_vertex<2, BT>, BT, m, smem, s, "VF", r, hd, ar, d_off, d_val, err);
+        case RXG_OP_VV: return launch(k_query_vertex<0, BT>, BT, m, smem, s, "VV", r, hd, ar, d_off, d_val, err, ef_b);
+        case RXG_OP_VE: return launch(k_query_vertex<1, BT>, BT, m, smem, s, "VE", r, hd, ar, d_off, d_val, err, ef_b);
+        case RXG_OP_VF: return launch(k_query_vertex<2, BT>, BT, m, smem, s, "VF", r, hd, ar, d_off, d_val, err, ef_b);
+        case RXG_OP_EF: return launch(k_query_vertex<RXG_OP_EF, BT>, BT, m, smem, s, "EF", r, hd, ar, d_off, d_val, err, ef_b);
+        case RXG_OP_FF:
+            if (m->edge_manifold && m->oriented)
+                return launch(k_query_ff_oriented<BT>, BT, m, query_smem_bytes(m, kFFOriented), s,
+                              "FF", r, hd, ar, d_off, d_val, err, ff_b);
+            return launch(k_query_ff<BT>, BT, m, smem, s, "FF", r, hd, ar, d_off, d_val, err, ff_b);
         case RXG_OP_FV: return launch(k_query_elem<3, BT>, BT, m, smem, s, "FV", r, hd, ar, d_val, err);
         case RXG_OP_EV: return launch(k_query_elem<4, BT>, BT, m, smem, s, "EV", r, hd, ar, d_val, err);
+        case RXG_OP_FE: return launch(k_query_elem<RXG_OP_FE, BT>, BT, m, smem, s, "FE", r, hd, ar, d_val, err);
+        case RXG_OP_EVD: return launch(k_query_elem<RXG_OP_EVD, BT>, BT, m, smem, s, "EVD", r, hd, ar, d_val, err);
     }
     set_error("rxg_query: unknown op %d", op);
     return RXG_ERR_INVALID;
@@ -490,7 +741,7 @@ static rxg_status launch_normals_bt(const Mesh* m, int weighting, const float* x
                                     cudaStream_t s, PatchRange r)
 {
     // kind 6: Max weights, 5: area weights (the same shared-memory layout)
-    const size_t    smem = query_smem_bytes(m, weighting == RXG_NORMAL_MAX ? 6 : 5);
+    const size_t    smem = query_smem_bytes(m, weighting == RXG_NORMAL_MAX ? kNormalMax : kNormalArea);
     int*            err  = device_error_word();
     const PatchHdr* hd   = m->d.hdr;
     const int32_t*  no   = m->d.nrm_off + r.p0;  // CTA b reads nrm_off[p0 + b], [p0 + b + 1]
@@ -622,6 +873,10 @@ rxg_status rxg_query_size(const rxg_mesh* h, int32_t op, int64_t* n_rows, int64_
         case RXG_OP_VF: *n_rows = M.nv; *n_values = 3 * M.nf; return RXG_OK;
         case RXG_OP_FV: *n_rows = M.nf; *n_values = 3 * M.nf; return RXG_OK;
         case RXG_OP_EV: *n_rows = M.ne; *n_values = 2 * M.ne; return RXG_OK;
+        case RXG_OP_EF: *n_rows = M.ne; *n_values = 3 * M.nf; return RXG_OK;
+        case RXG_OP_FE: *n_rows = M.nf; *n_values = 3 * M.nf; return RXG_OK;
+        case RXG_OP_FF: *n_rows = M.nf; *n_values = M.ff_base.empty() ? 0 : M.ff_base.back(); return RXG_OK;
+        case RXG_OP_EVD: *n_rows = M.ne; *n_values = 4 * M.ne; return RXG_OK;
     }
     set_error("rxg_query_size: unknown op %d", op);
     return RXG_ERR_INVALID;
@@ -633,7 +888,12 @@ rxg_status rxg_query(const rxg_mesh* h, int32_t op, int32_t* offsets, int32_t* v
     int64_t rows, nval;
     rxg_status st = rxg_query_size(h, op, &rows, &nval);
     if (st) return st;
-    const bool csr = op <= RXG_OP_VF;
+    const bool csr = op <= RXG_OP_VF || op == RXG_OP_EF || op == RXG_OP_FF;
+    if (op == RXG_OP_EVD && (!h->m.edge_manifold || !h->m.oriented)) {
+        set_error("rxg_query: EVDiamond needs an edge-manifold, consistently oriented mesh "
+                  "(each edge's two faces traverse it in opposite directions)");
+        return RXG_ERR_NONMANIFOLD;
+    }
     if (!values || (csr && !offsets)) {
         set_error("rxg_query: values%s must not be NULL", csr ? " and offsets" : "");
         return RXG_ERR_INVALID;
@@ -655,7 +915,12 @@ rxg_status rxg_query(const rxg_mesh* h, int32_t op, int32_t* offsets, int32_t* v
     std::vector<HostPiece> pieces;
     if (csr && so.owns) {
         HostPiece q{(char*)offsets, (const char*)so.d, 4, {}};
-        for (int k = 0; k <= kSlices; ++k) q.eb.push_back(k == kSlices ? rows + 1 : v_first(M, pb[k]));
+        // CSR rows are vertices (VV/VE/VF), edges (EF) or faces (FF)
+        for (int k = 0; k <= kSlices; ++k)
+            q.eb.push_back(k == kSlices ? rows + 1
+                                        : (op == RXG_OP_EF   ? e_first(M, pb[k])
+                                           : op == RXG_OP_FF ? f_first(M, pb[k])
+                                                             : v_first(M, pb[k])));
         pieces.push_back(q);
     }
     if (sv.owns) {
@@ -663,8 +928,11 @@ rxg_status rxg_query(const rxg_mesh* h, int32_t op, int32_t* offsets, int32_t* v
         for (int k = 0; k <= kSlices; ++k) {
             const int32_t p = pb[k];
             int64_t       e;
-            if (op == RXG_OP_FV) e = 3 * f_first(M, p);
+            if (op == RXG_OP_FV || op == RXG_OP_FE) e = 3 * f_first(M, p);
             else if (op == RXG_OP_EV) e = 2 * e_first(M, p);
+            else if (op == RXG_OP_EVD) e = 4 * e_first(M, p);
+            else if (op == RXG_OP_EF) e = M.ef_base[p];
+            else if (op == RXG_OP_FF) e = M.ff_base[p];
             else if (p == M.num_patches) e = nval;
             else e = op == RXG_OP_VF ? M.hdr[p].vf_base : M.hdr[p].vv_base;
             q.eb.push_back(e);

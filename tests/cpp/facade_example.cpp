@@ -120,6 +120,20 @@ static int gpu_checks()
         REQUIRE(same);
     }
 
+    // FF on the closed torus: every face has three edge neighbours; EVDiamond:
+    // every edge has both opposite vertices, distinct from its endpoints
+    QueryResult                ffq   = rx.query(Op::FF);
+    const std::vector<int32_t> ffoff = ffq.offsets.to_host();
+    for (size_t f = 0; f + 1 < ffoff.size(); ++f) REQUIRE(ffoff[f + 1] - ffoff[f] == 3);
+    QueryResult                dq = rx.query(Op::EVDiamond);
+    const std::vector<int32_t> dv = dq.values.to_host();
+    REQUIRE(dv.size() == 4 * (size_t)rx.get_num_edges());
+    for (size_t e = 0; e < dv.size() / 4; ++e) {
+        const int32_t* d = &dv[4 * e];
+        REQUIRE(d[1] >= 0 && d[3] >= 0 && d[1] != d[3]);
+        REQUIRE(d[1] != d[0] && d[1] != d[2] && d[3] != d[0] && d[3] != d[2]);
+    }
+
     // MCF system + Jacobi PCG: |A X - B| / |B| small
     const double        dt = 1e-3;
     SparseMatrix<double> A(rx);

@@ -6,7 +6,10 @@ vertex_normal_ref.h, compiled into oracle/_ref by oracle/Makefile) on them.
 Writes <name>.npz with fv (int32), xyz (float64), and the reference normals
 in FP32 and FP64.  Run here, where the reference tree exists:
 
-    python tests/golden/make_golden.py [/path/to/RXMesh]
+    python tests/golden/make_golden.py [/path/to/RXMesh [name ...]]
+
+plane_5 is the fixture of the reference's EVDiamond test
+(tests/RXMesh_test/test_ev_diamond.cu).
 """
 import os
 import sys
@@ -19,14 +22,14 @@ sys.path.insert(0, os.path.join(HERE, "..", ".."))
 from oracle import oracle as O  # noqa: E402
 from rxmesh_gb300.meshgen import read_obj  # noqa: E402
 
-MESHES = ["sphere3", "torus", "cloth", "bunnyhead"]
+MESHES = ["sphere3", "torus", "cloth", "bunnyhead", "plane_5"]
 
 
-def main(ref_root):
+def main(ref_root, names=None):
     O.build()
     if O.ref_lib() is None:
         raise SystemExit("oracle/_ref was not built (reference tree missing?)")
-    for name in MESHES:
+    for name in names or MESHES:
         xyz, fv = read_obj(os.path.join(ref_root, "input", name + ".obj"))
         n32 = O.ref_vertex_normals(fv, xyz.astype(np.float32), np.float32)
         n64 = O.ref_vertex_normals(fv, xyz, np.float64)
@@ -36,4 +39,4 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", sys.argv[2:])

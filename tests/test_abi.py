@@ -51,6 +51,10 @@ def decode(rx):
     vf = [None] * nv
     fvq = np.full((nf, 3), -1, np.int64)
     evq = np.full((ne, 2), -1, np.int64)
+    ef = [None] * ne
+    ff = [None] * nf
+    feq = np.full((nf, 3), -1, np.int64)
+    evd = np.full((ne, 4), -2, np.int64)
     for h in hdr:
         nVo, nVl, nEo, nEl, nFo, nFl, vb, eb, fb, vvb, vfb, evo, feo, rvo, reo, rfo = h.tolist()
         ev = arena[evo:evo + nEl]
@@ -72,7 +76,23 @@ def decode(rx):
             fvq[fb:fb + nFo] = linv(fvl[:nFo])
         if nEo:
             evq[eb:eb + nEo] = np.stack([linv(a[:nEo]), linv(b[:nEo])], 1)
-    return vv, ve, vf, fvq, evq
+        # edge / face queries from the same slices: every face of an owned
+        # edge and every edge neighbour of an owned face must be local
+        fel = fe >> 1
+        for e in range(nEo):
+            ef[eb + e] = sorted(linf(np.nonzero((fel == e).any(1))[0]).tolist())
+            d = [linv(np.array([a[e]]))[0], -1, linv(np.array([b[e]]))[0], -1]
+            for f, k in zip(*np.nonzero(fel == e)):
+                d[1 + 2 * int(fe[f, k] & 1)] = int(linv(np.array([fvl[f, (k + 2) % 3]]))[0])
+            evd[eb + e] = d
+        for f in range(nFo):
+            nb = set()
+            for k in range(3):
+                nb |= set(np.nonzero((fel == fel[f, k]).any(1))[0].tolist())
+            nb.discard(f)
+            ff[fb + f] = sorted(linf(np.array(sorted(nb), np.int64)).tolist()) if nb else []
+            feq[fb + f] = line(fel[f])
+    return vv, ve, vf, fvq, evq, ef, ff, feq, evd
 
 
 MESHES = {
@@ -98,7 +118,7 @@ def test_patch_layout_encodes_exact_queries(oracle, name, patch):
         assert np.array_equal(np.sort(m), np.arange(n))
     hdr, _ = rx.patches()
     assert (hdr[:, 4] <= patch).all()
-    vv, ve, vf, fvq, evq = decode(rx)
+    vv, ve, vf, fvq, evq, ef, ff, feq, evd = decode(rx)
     off, val = oracle.vv(nv, ev_ref)
     want = sorted_rows(off, val)
     got = [None] * nv
@@ -117,3 +137,34 @@ def test_patch_layout_encodes_exact_queries(oracle, name, patch):
     assert got == want
     assert np.array_equal(vl[fvq][np.argsort(fl)], np.asarray(fv))  # FV in input vertex order
     assert np.array_equal(vl[evq][np.argsort(el)], ev_ref)          # EV as first encountered
+    ne, nf = len(ev_ref), len(fv)
+    off, val = oracle.ef(fv)
+    got_e = [None] * ne
+    for lin in range(ne):
+        got_e[el[lin]] = tuple(sorted(fl[np.array(ef[lin], np.int64)].tolist()))
+    assert got_e == sorted_rows(off, val)
+    off, val = oracle.ff(fv)
+    got_f = [None] * nf
+    for lin in range(nf):
+        got_f[fl[lin]] = tuple(sorted(fl[np.array(ff[lin], np.int64)].tolist()))
+    assert got_f == sorted_rows(off, val)
+    _, fe_ref = oracle.edges(fv)
+    assert np.array_equal(el[feq][np.argsort(fl)], fe_ref)          # FE in face-edge order
+    d = np.where(evd >= 0, vl[np.maximum(evd, 0)], -1)[np.argsort(el)]
+    assert np.array_equal(d, oracle.ev_diamond(fv))
+
+
+def test_ev_diamond_needs_consistent_orientation():
+    """One flipped face: the two faces of its edges traverse them the same
+    way, so EVDiamond is refused (RXG_ERR_NONMANIFOLD) before any launch."""
+    import ctypes
+    from rxmesh_gb300 import Op, RXMeshStatic, _lib
+    L = _lib.load()
+    _, f = meshgen.icosphere(2)
+    good = RXMeshStatic(f, f.max() + 1, patch_size=64, host_only=True)
+    assert L.rxg_query(good._h, Op.EVD, None, None, None) == 1   # only the NULL buffer
+    g = np.array(f, np.int32).copy()
+    g[5] = g[5][::-1]
+    bad = RXMeshStatic(g, g.max() + 1, patch_size=64, host_only=True)
+    assert L.rxg_query(bad._h, Op.EVD, None, None, None) == 4
+    assert b"oriented" in L.rxg_last_error()

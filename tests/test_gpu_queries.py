@@ -18,6 +18,7 @@ MESHES = {
     "sphere3": lambda: (golden("sphere3")["xyz"], golden("sphere3")["fv"]),
     "cloth": lambda: (golden("cloth")["xyz"], golden("cloth")["fv"]),
     "bunnyhead": lambda: (golden("bunnyhead")["xyz"], golden("bunnyhead")["fv"]),
+    "plane_5": lambda: (golden("plane_5")["xyz"], golden("plane_5")["fv"]),
 }
 
 
@@ -60,6 +61,63 @@ def test_queries_bit_exact(oracle, name, patch):
     device_check()
 
 
+@pytest.mark.parametrize("name", list(MESHES))
+@pytest.mark.parametrize("patch", [64, 512])
+def test_edge_and_face_queries_bit_exact(oracle, name, patch):
+    """EF, FF (rows as sets), FE and EVDiamond (rows in order) against the
+    oracle, in input ids (Op::EF/FE/FF/EVDiamond, kernels/rxmesh_queries.cuh)."""
+    from rxmesh_gb300 import Op, RXMeshStatic, device_check
+    x, f = MESHES[name]()
+    rx = RXMeshStatic(f, len(x), patch_size=patch)
+    vl, el, fl = rx.linear_to_input("v"), rx.linear_to_input("e"), rx.linear_to_input("f")
+    ev, fe = oracle.edges(f)
+
+    def rows_in_input(op, row_ids, val_ids):
+        off, val = rx.query(op)
+        off, val = off.cpu().numpy(), val.cpu().numpy()
+        rows = [None] * len(row_ids)
+        for lin in range(len(row_ids)):
+            rows[row_ids[lin]] = tuple(sorted(val_ids[val[off[lin]:off[lin + 1]]].tolist()))
+        return rows, off
+
+    o, v = oracle.ef(f)
+    got, off = rows_in_input(Op.EF, el, fl)
+    assert got == sorted_rows(o, v) and off[-1] == 3 * len(f)
+    o, v = oracle.ff(f)
+    got, off = rows_in_input(Op.FF, fl, fl)
+    assert got == sorted_rows(o, v) and off[-1] == len(v)
+    _, feq = rx.query(Op.FE)
+    feq = feq.cpu().numpy().reshape(-1, 3)
+    assert np.array_equal(el[feq][np.argsort(fl)], fe)
+    _, dq = rx.query(Op.EVD)
+    dq = dq.cpu().numpy().reshape(-1, 4)
+    din = np.where(dq >= 0, vl[np.maximum(dq, 0)], -1)[np.argsort(el)]
+    assert np.array_equal(din, oracle.ev_diamond(f))
+    device_check()
+
+
+@pytest.mark.parametrize("patch", [64, 512])
+def test_ff_ef_on_inconsistently_oriented_mesh(oracle, patch):
+    """One flipped face: FF takes the general per-patch EF counting sort (the
+    two-slot kernel needs consistent orientation); EF and FE do not depend on
+    orientation; EVDiamond is refused."""
+    from rxmesh_gb300 import Op, RXMeshStatic, RXGError
+    _, f = meshgen.icosphere(4)
+    f = np.array(f, np.int32).copy()
+    f[17] = f[17][::-1]
+    rx = RXMeshStatic(f, int(f.max()) + 1, patch_size=patch)
+    el, fl = rx.linear_to_input("e"), rx.linear_to_input("f")
+    for op, rows_ids, val_ids, ref in ((Op.FF, fl, fl, oracle.ff(f)), (Op.EF, el, fl, oracle.ef(f))):
+        off, val = rx.query(op)
+        off, val = off.cpu().numpy(), val.cpu().numpy()
+        got = [None] * len(rows_ids)
+        for lin in range(len(rows_ids)):
+            got[rows_ids[lin]] = tuple(sorted(val_ids[val[off[lin]:off[lin + 1]]].tolist()))
+        assert got == sorted_rows(*ref), op
+    with pytest.raises(RXGError):
+        rx.query(Op.EVD)
+
+
 @pytest.mark.parametrize("level,patch", [(3, 128), (5, 128)])
 def test_query_into_host_buffers(oracle, level, patch):
     """Host outputs (sliced launches, copies overlapped) equal the device outputs."""
@@ -67,9 +125,9 @@ def test_query_into_host_buffers(oracle, level, patch):
     from rxmesh_gb300 import Op, RXMeshStatic, _lib
     x, f = meshgen.icosphere(level)
     rx = RXMeshStatic(f, len(x), patch_size=patch)
-    for op in (Op.VV, Op.VE, Op.VF, Op.FV, Op.EV):
+    for op in (Op.VV, Op.VE, Op.VF, Op.FV, Op.EV, Op.EF, Op.FE, Op.FF, Op.EVD):
         rows, nval = rx.query_size(op)
-        csr = op <= Op.VF
+        csr = op in Op.CSR
         off = np.full(rows + 1, -7, np.int32) if csr else None
         val = np.full(nval, -7, np.int32)
         rx.query_host(op, off, val)
@@ -99,9 +157,9 @@ def test_query_into_pinned_host_buffers(oracle, level, patch):
     L = _lib.load()
     x, f = meshgen.icosphere(level)
     rx = RXMeshStatic(f, len(x), patch_size=patch)
-    for op in (Op.VV, Op.VE, Op.VF, Op.FV, Op.EV):
+    for op in (Op.VV, Op.VE, Op.VF, Op.FV, Op.EV, Op.EF, Op.FE, Op.FF, Op.EVD):
         rows, nval = rx.query_size(op)
-        csr = op <= Op.VF
+        csr = op in Op.CSR
         d_off, d_val = rx.query(op)
         for pin_off, pin_val in ((True, True), (False, True), (True, False)):
             if not csr and not pin_val:

@@ -52,6 +52,53 @@ def test_vv_ve_vf_ground_truth_small(oracle):
     assert sorted_rows(off, val) == [tuple(sorted(s)) for s in wantf]
 
 
+def test_ef_fe_ff_ground_truth(oracle):
+    """EF, FE and FF as the reference's verifier builds them
+    (tests/RXMesh_test/rxmesh_test.h:290-330), on a closed and an open mesh."""
+    for v, f in (meshgen.icosphere(2), meshgen.plane(7, 5)):
+        ev, fe = oracle.edges(f)
+        eoff, eval_ = oracle.ef(f)
+        want_ef = [set() for _ in range(len(ev))]
+        for i, t in enumerate(fe):
+            for e in t:
+                want_ef[e].add(i)
+        assert sorted_rows(eoff, eval_) == [tuple(sorted(s)) for s in want_ef]
+        foff, fval = oracle.ff(f)
+        want_ff = [set() for _ in range(len(f))]
+        for fs in want_ef:
+            for a in fs:
+                want_ff[a] |= fs - {a}
+        assert sorted_rows(foff, fval) == [tuple(sorted(s)) for s in want_ff]
+        # FE edge k joins corners k and k+1
+        for i, t in enumerate(f):
+            for k in range(3):
+                assert set(ev[fe[i][k]]) == {t[k], t[(k + 1) % 3]}
+
+
+def test_ev_diamond_reference_kat(oracle):
+    """tests/RXMesh_test/test_ev_diamond.cu: on plane_5, every edge with four
+    valid diamond vertices has tri_area(v0,v1,v2) + tri_area(v0,v2,v3) = 1."""
+    g = golden("plane_5")
+    x, f = g["xyz"], g["fv"]
+    d = oracle.ev_diamond(f)
+    ev, _ = oracle.edges(f)
+    assert np.array_equal(d[:, 0], ev[:, 0]) and np.array_equal(d[:, 2], ev[:, 1])
+
+    def area(a, b, c):
+        return 0.5 * np.linalg.norm(np.cross(x[b] - x[a], x[c] - x[a]))
+
+    full = (d >= 0).all(axis=1)
+    assert full.sum() == 40  # the 40 interior edges of the 4 x 4 grid
+    for r in d[full]:
+        assert abs(area(r[0], r[1], r[2]) + area(r[0], r[2], r[3]) - 1.0) < 1e-5
+    # slot 1 is opposite the edge in the face traversing v0 -> v1, slot 3 in the other
+    for i, t in enumerate(f):
+        for k in range(3):
+            a, b, c = int(t[k]), int(t[(k + 1) % 3]), int(t[(k + 2) % 3])
+            e = [j for j in range(len(ev)) if set(ev[j]) == {a, b}][0]
+            assert d[e][1 if ev[e][0] == a else 3] == c
+
+
 @pytest.mark.parametrize("name", ["sphere3", "torus", "cloth", "bunnyhead"])
 def test_normals_match_reference_vertex_normal_ref(oracle, name):
     # fixtures hold the output of apps/VertexNormal/vertex_normal_ref.h itself
