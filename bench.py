@@ -367,6 +367,12 @@ def run_mcf(args, torch):
     # FP64 oracle for the first step (CPU, solved to 1e-12 relative residual)
     rp, col, val, B = O.mcf_system(f, x0, dt)
     Xo, it_o, _, _, _ = O.cg(rp, col, val, B, x0, 20000, 0.0, 1e-24, True)
+    # CPU baseline: one step of the oracle port (assembly + FP64 Jacobi PCG,
+    # stopped at the GPU steps' rule: r.D^-1 r fallen by tol^2), 1 thread
+    t0 = time.perf_counter()
+    rp_c, col_c, val_c, B_c = O.mcf_system(f, x0, dt)
+    _, it_c, _, _, _ = O.cg(rp_c, col_c, val_c, B_c, x0, 20000, 0.0, tol * tol, True)
+    t_cpu = time.perf_counter() - t0
     for prec in ("f64", "mixed"):
         x = x0l.clone()
         mcf_step(rx, x, dt, 1, prec, tol=tol)  # warm-up + error of step 1
@@ -386,6 +392,10 @@ def run_mcf(args, torch):
                      "cg_iters_last_step": st["iters"], "rel_err_step1": err,
                      "rel_err_of_update_step1": err_upd}
     res["mixed_speedup_vs_f64"] = res["mixed"]["steps_per_s"] / res["f64"]["steps_per_s"]
+    res["cpu_baseline_f64"] = {"steps_per_s": 1.0 / t_cpu, "ms_per_step": 1e3 * t_cpu, "pcg_iters": it_c,
+                               "cores": 1, "kind": "port",
+                               "sample": "one implicit step of the same level-8 system: assembly + FP64 "
+                                         "Jacobi PCG to the same stopping rule (oracle port, 1 thread)"}
     res["oracle_pcg_iters_step1"] = it_o
     # per PCG iteration, algorithmic bytes: FP64 packed solver = 16 B per entry
     # + 4 vectors of 32 B read and 4 written per row; on-chip FP32 solver =
@@ -459,8 +469,10 @@ def run_arap(args, torch):
     xl = rx.to_linear(torch.tensor(x, device="cuda"))
     bytes_eg = 12 * V + 16 * F + 4 * F + 12 * V
     bytes_h = 36 * nnzb + 4 * nnzb
-    for dt_name, dt in (("f32", torch.float32), ("f64", torch.float64)):
-        prob = DiffScalarProblem(rx, dt).add_arap_term(rest)
+    for dt_name, dt, proj in (("f32", torch.float32, False), ("f64", torch.float64, False),
+                              ("f32_projected", torch.float32, True),
+                              ("f64_projected", torch.float64, True)):
+        prob = DiffScalarProblem(rx, dt).add_arap_term(rest, project_hessian=proj)
         xs = xl.to(dt)
         for _ in range(3):
             prob.eval_terms(xs)

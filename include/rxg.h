@@ -378,6 +378,20 @@ rxg_status rxg_arap_eval(const rxg_mesh* m, int32_t dtype, const void* x,
                          const void* rest, double* energy, void* face_E,
                          void* grad, rxg_bcsr* hess, void* stream);
 
+/*
+ * rxg_arap_eval with flags.  RXG_ARAP_PROJECT_HESSIAN: each face's 9x9
+ * Hessian is made positive definite before assembly, as the reference's
+ * add_term<Op::FV, ProjectHess = true> (diff/diff_query_kernel.cuh:244-251,
+ * project_positive_definite of diff/hessian_projection.h:21-95: left alone
+ * when positive diagonally dominant with margin eps, else eigenvalues below
+ * eps raised to eps; eps 1e-9 FP64, 1e-6 FP32).  Energy and gradient are
+ * unaffected; without a Hessian the flag has no effect.
+ */
+enum { RXG_ARAP_PROJECT_HESSIAN = 1 };
+rxg_status rxg_arap_eval_ex(const rxg_mesh* m, int32_t dtype, const void* x,
+                            const void* rest, int32_t flags, double* energy,
+                            void* face_E, void* grad, rxg_bcsr* hess, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -487,8 +487,11 @@ class DiffScalarProblem
         if (assemble_hessian) hess.reset(new BlockSparseMatrix<T>(n, nnz));
     }
     // rest: linear-order FP64 positions of the flat rest shape
-    void add_arap_term(const DenseMatrix<double>& rest, cudaStream_t s = nullptr)
+    // project_hessian: the reference's add_term<Op::FV, ProjectHess = true>
+    void add_arap_term(const DenseMatrix<double>& rest, cudaStream_t s = nullptr,
+                       bool project_hessian = false)
     {
+        m_project = project_hessian;
         m_rest.resize(4 * (size_t)m_rx->get_num_faces());
         check(rxg_arap_rest(m_rx->handle(), rest.data(), dtype_of<T>::value, m_rest.data(), s));
     }
@@ -497,8 +500,9 @@ class DiffScalarProblem
     {
         if (!m_rest.size()) throw Error(RXG_ERR_INVALID, "add_arap_term() first");
         rxg_bcsr  b  = hess ? hess->bcsr() : rxg_bcsr{};
-        check(rxg_arap_eval(m_rx->handle(), dtype_of<T>::value, x.data(), m_rest.data(), &m_loss,
-                            face_energy.data(), grad.data(), hess ? &b : nullptr, s));
+        check(rxg_arap_eval_ex(m_rx->handle(), dtype_of<T>::value, x.data(), m_rest.data(),
+                               m_project ? RXG_ARAP_PROJECT_HESSIAN : 0, &m_loss,
+                               face_energy.data(), grad.data(), hess ? &b : nullptr, s));
     }
     T get_current_loss() const { return (T)m_loss; }
 
@@ -509,7 +513,8 @@ class DiffScalarProblem
    private:
     const RXMeshStatic* m_rx;
     DeviceArray<T>      m_rest;
-    double              m_loss = 0.0;
+    double              m_loss    = 0.0;
+    bool                m_project = false;
 };
 
 // Many meshes of uneven size, mixed-precision implicit MCF in one persistent

@@ -59,6 +59,11 @@ def lib():
         L.orc_arap_assemble.restype = ctypes.c_double
         L.orc_arap_assemble.argtypes = [I64, I64, i32p, f64p, f64p, f64p, i64p, i32p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_arap_assemble_ex.restype = ctypes.c_double
+        L.orc_arap_assemble_ex.argtypes = [I64, I64, i32p, f64p, f64p, f64p, i64p, i32p,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_int, ctypes.c_double]
+        L.orc_project_pd.argtypes = [ctypes.c_int, f64p, ctypes.c_double]
         L.orc_partial_voronoi_area.restype = ctypes.c_double
         L.orc_partial_voronoi_area.argtypes = [f64p, f64p, f64p]
         L.orc_half_cot.restype = ctypes.c_double
@@ -250,8 +255,16 @@ def arap_face(x9, minv, area, want_hess=True):
     return E, g, H.reshape(9, 9)
 
 
-def arap_assemble(fv, x, minv, area, rp, col, want_hess=True):
-    """Total energy, per-face energy, gradient (nv,3), Hessian blocks (nnz,3,3)."""
+def project_pd(H, eps=1e-9):
+    """project_positive_definite of one symmetric k x k matrix (copy)."""
+    h = np.ascontiguousarray(H, np.float64).copy()
+    lib().orc_project_pd(h.shape[0], h.reshape(-1), float(eps))
+    return h
+
+
+def arap_assemble(fv, x, minv, area, rp, col, want_hess=True, project=False, eps=1e-9):
+    """Total energy, per-face energy, gradient (nv,3), Hessian blocks (nnz,3,3);
+    project: each face's 9x9 Hessian made positive definite first."""
     f = _fv(fv)
     xx = np.ascontiguousarray(x, np.float64).reshape(-1)
     nv = xx.size // 3
@@ -260,8 +273,8 @@ def arap_assemble(fv, x, minv, area, rp, col, want_hess=True):
     g = np.empty(3 * nv, np.float64)
     nnz = int(rp[-1])
     H = np.empty(9 * nnz, np.float64) if want_hess else None
-    E = lib().orc_arap_assemble(nv, nf, f, xx, np.ascontiguousarray(minv, np.float64).reshape(-1),
-                                np.ascontiguousarray(area, np.float64), np.ascontiguousarray(rp, np.int64),
-                                np.ascontiguousarray(col, np.int32), fe.ctypes.data, g.ctypes.data,
-                                H.ctypes.data if want_hess else None)
+    E = lib().orc_arap_assemble_ex(nv, nf, f, xx, np.ascontiguousarray(minv, np.float64).reshape(-1),
+                                   np.ascontiguousarray(area, np.float64), np.ascontiguousarray(rp, np.int64),
+                                   np.ascontiguousarray(col, np.int32), fe.ctypes.data, g.ctypes.data,
+                                   H.ctypes.data if want_hess else None, int(project), float(eps))
     return E, fe, g.reshape(nv, 3), (H.reshape(nnz, 3, 3) if want_hess else None)

@@ -692,10 +692,107 @@ double orc_arap_face(const double* x9, const double* minv, double A,
  * the Hessian as 3x3 blocks (row-major) on a block-CSR pattern (rp, col)
  * that contains the diagonal and every edge.  Returns the total energy.
  */
+/*
+ * Cyclic Jacobi eigen-decomposition of a symmetric k x k matrix (k <= 9;
+ * Golub and Van Loan, Matrix Computations, sec. 8.5): A (row-major) is
+ * rotated until its off-diagonal part vanishes, leaving the eigenvalues on
+ * its diagonal; V receives the eigenvectors as columns.  Each rotation
+ * zeroes A[p][q] with t = sgn(th) / (|th| + sqrt(th^2 + 1)),
+ * th = (A[q][q] - A[p][p]) / (2 A[p][q]), c = 1/sqrt(1 + t^2), s = t c.
+ */
+static void jacobi_eig(int k, double* A, double* V)
+{
+    for (int i = 0; i < k * k; ++i) V[i] = (i % (k + 1)) == 0 ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 50; ++sweep) {
+        double off = 0, all = 0;
+        for (int i = 0; i < k; ++i)
+            for (int j = 0; j < k; ++j) {
+                all += A[i * k + j] * A[i * k + j];
+                if (i != j) off += A[i * k + j] * A[i * k + j];
+            }
+        if (off <= 1e-30 * all) break;
+        for (int p = 0; p < k - 1; ++p)
+            for (int q = p + 1; q < k; ++q) {
+                const double apq = A[p * k + q];
+                if (apq == 0.0) continue;
+                const double th = (A[q * k + q] - A[p * k + p]) / (2.0 * apq);
+                const double t  = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+                const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                for (int r = 0; r < k; ++r) {
+                    const double arp = A[r * k + p], arq = A[r * k + q];
+                    A[r * k + p] = c * arp - s * arq;
+                    A[r * k + q] = s * arp + c * arq;
+                }
+                for (int r = 0; r < k; ++r) {
+                    const double apr = A[p * k + r], aqr = A[q * k + r];
+                    A[p * k + r] = c * apr - s * aqr;
+                    A[q * k + r] = s * apr + c * aqr;
+                }
+                for (int r = 0; r < k; ++r) {
+                    const double vrp = V[r * k + p], vrq = V[r * k + q];
+                    V[r * k + p] = c * vrp - s * vrq;
+                    V[r * k + q] = s * vrp + c * vrq;
+                }
+            }
+    }
+}
+
+/*
+ * project_positive_definite (include/rxmesh/diff/hessian_projection.h:21-95):
+ * a symmetric k x k H (k <= 9) that is positive diagonally dominant with
+ * margin eps (H_ii >= sum_j!=i |H_ij| + eps for every i) is left alone;
+ * otherwise its eigenvalues below eps are raised to eps and, if any was,
+ * H = V diag(lambda) V^T.  eps: 1e-9 (FP64) / 1e-6 (FP32) in the reference.
+ */
+void orc_project_pd(int k, double* H, double eps)
+{
+    int dd = 1;
+    for (int i = 0; i < k && dd; ++i) {
+        double off = 0;
+        for (int j = 0; j < k; ++j)
+            if (j != i) off += fabs(H[i * k + j]);
+        if (H[i * k + i] < off + eps) dd = 0;
+    }
+    if (dd) return;
+    double A[81], V[81], lam[9];
+    memcpy(A, H, sizeof(double) * (size_t)(k * k));
+    jacobi_eig(k, A, V);
+    int clamped = 0;
+    for (int i = 0; i < k; ++i) {
+        lam[i] = A[i * k + i];
+        if (lam[i] < eps) {
+            lam[i]  = eps;
+            clamped = 1;
+        }
+    }
+    if (!clamped) return;
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < k; ++j) {
+            double v = 0;
+            for (int m = 0; m < k; ++m) v += V[i * k + m] * lam[m] * V[j * k + m];
+            H[i * k + j] = v;
+        }
+}
+
+/* orc_arap_assemble with each face's 9x9 Hessian projected (project != 0,
+ * the reference's add_term<Op::FV, ProjectHess = true>) before the scatter. */
+double orc_arap_assemble_ex(int64_t nv, int64_t nf, const int32_t* fv,
+                            const double* x, const double* minv, const double* area,
+                            const int64_t* rp, const int32_t* col, double* face_E,
+                            double* grad, double* hblk, int project, double eps);
+
 double orc_arap_assemble(int64_t nv, int64_t nf, const int32_t* fv,
                          const double* x, const double* minv, const double* area,
                          const int64_t* rp, const int32_t* col, double* face_E,
                          double* grad, double* hblk)
+{
+    return orc_arap_assemble_ex(nv, nf, fv, x, minv, area, rp, col, face_E, grad, hblk, 0, 0.0);
+}
+
+double orc_arap_assemble_ex(int64_t nv, int64_t nf, const int32_t* fv,
+                         const double* x, const double* minv, const double* area,
+                            const int64_t* rp, const int32_t* col, double* face_E,
+                            double* grad, double* hblk, int project, double eps)
 {
     double total = 0;
     if (grad) memset(grad, 0, sizeof(double) * (size_t)(3 * nv));
@@ -706,6 +803,7 @@ double orc_arap_assemble(int64_t nv, int64_t nf, const int32_t* fv,
         for (int i = 0; i < 3; ++i)
             for (int c = 0; c < 3; ++c) x9[3 * i + c] = x[3 * v[i] + c];
         double E = orc_arap_face(x9, minv + 4 * f, area[f], g, hblk ? H : NULL);
+        if (hblk && project) orc_project_pd(9, H, eps);
         if (face_E) face_E[f] = E;
         total += E;
         if (grad)

@@ -66,10 +66,14 @@ class DiffScalarProblem:
         self.face_energy = torch.zeros(rx.get_num_faces(), dtype=dtype, device=dev)
         self.hess = BlockSparseMatrix(n.value, nnz.value, dtype, dev) if assemble_hessian else None
         self.rest = None
+        self.project_hessian = False
         self._loss = None
 
-    def add_arap_term(self, rest_xyz_lin):
-        """Per-face ARAP term against the flat rest frame of rest_xyz_lin (nv,3, linear order)."""
+    def add_arap_term(self, rest_xyz_lin, project_hessian=False):
+        """Per-face ARAP term against the flat rest frame of rest_xyz_lin (nv,3,
+        linear order).  project_hessian: each face's 9x9 Hessian made positive
+        definite before assembly (add_term<Op::FV, ProjectHess = true>)."""
+        self.project_hessian = bool(project_hessian)
         xr = rest_xyz_lin.to(torch.float64).contiguous()
         self.rest = torch.empty(self.rx.get_num_faces(), 4, dtype=self.dtype, device=xr.device)
         check(self._L.rxg_arap_rest(self.rx._h, _p(xr), _DT[self.dtype], _p(self.rest), _stream()))
@@ -83,9 +87,10 @@ class DiffScalarProblem:
         h = self.assemble_hessian if with_hessian is None else with_hessian
         e = torch.zeros(1, dtype=torch.float64, device=x.device)
         b = self.hess.bcsr() if (h and self.hess is not None) else None
-        check(self._L.rxg_arap_eval(self.rx._h, _DT[self.dtype], _p(x), _p(self.rest), _p(e),
-                                    _p(self.face_energy), _p(self.grad),
-                                    ctypes.byref(b) if b is not None else None, _stream(stream)))
+        check(self._L.rxg_arap_eval_ex(self.rx._h, _DT[self.dtype], _p(x), _p(self.rest),
+                                       1 if self.project_hessian else 0, _p(e),
+                                       _p(self.face_energy), _p(self.grad),
+                                       ctypes.byref(b) if b is not None else None, _stream(stream)))
         self._loss = e
         return e
 

@@ -89,6 +89,7 @@ SIGNATURES = {
     "rxg_batch_stats": [P, P, P],
     "rxg_batch_autotune": [P, D, I32, D, I32, P, P, P, P, P],
     "rxg_arap_eval": [P, I32, P, P, P, P, P, P, P],
+    "rxg_arap_eval_ex": [P, I32, P, P, I32, P, P, P, P, P],
 }
 _RESTYPE = {"rxg_status_string": ctypes.c_char_p, "rxg_last_error": ctypes.c_char_p,
             "rxg_mesh_destroy": None, "rxg_batch_destroy": None}

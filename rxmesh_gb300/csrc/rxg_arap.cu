@@ -472,6 +472,217 @@ __global__ void __launch_bounds__(128) k_arap_gather(
     }
 }
 
+// ---------------------------------------------------------------------
+// Hessian projection (the reference's add_term<Op::FV, ProjectHess = true>,
+// include/rxmesh/diff/hessian_projection.h:21-95): each face's 9x9 Hessian
+// in vertex space is made positive definite before assembly.
+// ---------------------------------------------------------------------
+
+// Cyclic Jacobi eigen-decomposition of a symmetric K x K matrix (Golub and
+// Van Loan, Matrix Computations, sec. 8.5): A (row-major) is rotated until
+// its off-diagonal part vanishes, leaving the eigenvalues on its diagonal;
+// V receives the eigenvectors as columns.  Each rotation zeroes A[p][q] with
+// t = sgn(th) / (|th| + sqrt(th^2 + 1)), th = (A[q][q] - A[p][p]) / (2 A[p][q]).
+template <typename T, int K>
+__device__ void jacobi_eigen(T* A, T* V)
+{
+    for (int i = 0; i < K * K; ++i) V[i] = (i % (K + 1)) == 0 ? T(1) : T(0);
+    const T rel = sizeof(T) == 4 ? T(1e-14) : T(1e-30);
+    for (int sweep = 0; sweep < 40; ++sweep) {
+        T off = 0, all = 0;
+        for (int i = 0; i < K; ++i)
+            for (int j = 0; j < K; ++j) {
+                const T a = A[i * K + j];
+                all += a * a;
+                if (i != j) off += a * a;
+            }
+        if (off <= rel * all) break;
+        for (int p = 0; p < K - 1; ++p)
+            for (int q = p + 1; q < K; ++q) {
+                const T apq = A[p * K + q];
+                if (apq == T(0)) continue;
+                const T th = (A[q * K + q] - A[p * K + p]) / (T(2) * apq);
+                const T t  = (th >= T(0) ? T(1) : T(-1)) / (fabs(th) + sqrt(th * th + T(1)));
+                const T c = T(1) / sqrt(t * t + T(1)), sn = t * c;
+                for (int r = 0; r < K; ++r) {
+                    const T arp = A[r * K + p], arq = A[r * K + q];
+                    A[r * K + p] = c * arp - sn * arq;
+                    A[r * K + q] = sn * arp + c * arq;
+                }
+                for (int r = 0; r < K; ++r) {
+                    const T apr = A[p * K + r], aqr = A[q * K + r];
+                    A[p * K + r] = c * apr - sn * aqr;
+                    A[q * K + r] = sn * apr + c * aqr;
+                }
+                for (int r = 0; r < K; ++r) {
+                    const T vrp = V[r * K + p], vrq = V[r * K + q];
+                    V[r * K + p] = c * vrp - sn * vrq;
+                    V[r * K + q] = sn * vrp + c * vrq;
+                }
+            }
+    }
+}
+
+// H (K x K, symmetric, row-major) left alone when positive diagonally
+// dominant with margin eps; otherwise eigenvalues below eps are raised to eps
+// and, if any was, H = V diag(lambda) V^T.
+template <typename T, int K>
+__device__ void project_pd(T* H, T eps)
+{
+    bool dd = true;
+    for (int i = 0; i < K && dd; ++i) {
+        T off = 0;
+        for (int j = 0; j < K; ++j)
+            if (j != i) off += fabs(H[i * K + j]);
+        dd = H[i * K + i] >= off + eps;
+    }
+    if (dd) return;
+    T A[K * K], V[K * K], lam[K];
+    for (int i = 0; i < K * K; ++i) A[i] = H[i];
+    jacobi_eigen<T, K>(A, V);
+    bool clamped = false;
+    for (int i = 0; i < K; ++i) {
+        lam[i] = A[i * K + i];
+        if (lam[i] < eps) {
+            lam[i]  = eps;
+            clamped = true;
+        }
+    }
+    if (!clamped) return;
+    for (int i = 0; i < K; ++i)
+        for (int j = 0; j < K; ++j) {
+            T v = 0;
+            for (int m = 0; m < K; ++m) v += V[i * K + m] * lam[m] * V[j * K + m];
+            H[i * K + j] = v;
+        }
+}
+
+// Projected records: E, dE/du (6), the rest-frame inverse (4), then the
+// projected 9x9 vertex-space Hessian's upper triangle (45, row-major).
+constexpr int kProjRec = 56;
+
+__host__ __device__ constexpr int upper9(int i, int j) { return i * 9 - i * (i - 1) / 2 + (j - i); }
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_arap_face_proj(
+    int64_t nf, const int32_t* __restrict__ fv, const T* __restrict__ x,
+    const T* __restrict__ minv, T* __restrict__ rec, T* __restrict__ face_E,
+    double* __restrict__ part)
+{
+    __shared__ double s_red[128 / 32];
+    double            esum = 0;
+    const T           eps  = sizeof(T) == 4 ? T(1e-6) : T(1e-9);
+    for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nf;
+         f += (int64_t)gridDim.x * blockDim.x) {
+        int32_t v[3];
+        T       x9[9], mi[4], area;
+        load_face(fv, x, minv, (int32_t)f, v, x9, mi, area);
+        FaceDeriv<T> o;
+        arap_face<T, true>(x9, mi, area, o);
+        T H[81];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                T b[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                block_of(o, i, j, b);
+                for (int a = 0; a < 3; ++a)
+                    for (int c = 0; c < 3; ++c) H[(3 * i + a) * 9 + 3 * j + c] = b[3 * a + c];
+            }
+        project_pd<T, 9>(H, eps);
+        T* r = rec + (int64_t)kProjRec * f;
+        r[0] = o.E;
+        for (int i = 0; i < 6; ++i) r[1 + i] = o.gE[i];
+        for (int i = 0; i < 4; ++i) r[7 + i] = mi[i];
+        for (int i = 0; i < 9; ++i)
+            for (int j = i; j < 9; ++j) r[11 + upper9(i, j)] = H[i * 9 + j];
+        if (face_E) face_E[f] = o.E;
+        esum += (double)o.E;
+    }
+    const double t = block_sum_d<128>(esum, s_red);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// block (li, lj) of a projected record, accumulated into out (3x3 row-major)
+template <typename T>
+__device__ __forceinline__ void proj_block(const T* __restrict__ r, int li, int lj, T* out)
+{
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const int i = 3 * li + a, j = 3 * lj + c;
+            out[3 * a + c] += __ldg(r + 11 + (i <= j ? upper9(i, j) : upper9(j, i)));
+        }
+}
+
+// One thread per vertex: gradient row and projected Hessian block row, in
+// the fan order of k_arap_gather.
+template <typename T>
+__global__ void __launch_bounds__(128) k_arap_gather_proj(
+    int64_t nv, const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ ring_off,
+    const int32_t* __restrict__ ring, const int32_t* __restrict__ ring_face,
+    const int8_t* __restrict__ bnd, const int32_t* __restrict__ fv, const T* __restrict__ rec,
+    T* __restrict__ grad, T* __restrict__ hval)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nv;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t ro = ring_off[p];
+        const int32_t k  = ring_off[p + 1] - ro;
+        const int32_t nf = bnd[p] ? k - 1 : k;
+        const int32_t rp = row_ptr[p];
+        T             g[3] = {0, 0, 0}, D[9], carry[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) D[i] = carry[i] = T(0);
+        for (int32_t i = 0; i < nf; ++i) {
+            const int32_t f    = ring_face[ro + i];
+            const int32_t v[3] = {__ldg(fv + 3 * (int64_t)f), __ldg(fv + 3 * (int64_t)f + 1),
+                                  __ldg(fv + 3 * (int64_t)f + 2)};
+            const T*      r    = rec + (int64_t)kProjRec * f;
+            const int     lp   = local_index(v, (int32_t)p);
+            // u_k = sum_v d[v][k] x_v: d[1] = mi[0..1], d[2] = mi[2..3], d[0] = -(d[1] + d[2])
+            const T m0 = __ldg(r + 7), m1 = __ldg(r + 8), m2 = __ldg(r + 9), m3 = __ldg(r + 10);
+            const T d0 = lp == 0 ? -(m0 + m2) : (lp == 1 ? m0 : m2);
+            const T d1 = lp == 0 ? -(m1 + m3) : (lp == 1 ? m1 : m3);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) g[c] += d0 * __ldg(r + 1 + c) + d1 * __ldg(r + 4 + c);
+            if (hval) {
+                const int li = local_index(v, ring[ro + i]);
+                const int lj = local_index(v, ring[ro + (i + 1 < k ? i + 1 : 0)]);
+                proj_block(r, lp, lp, D);
+                T bi[9];
+#pragma unroll
+                for (int t = 0; t < 9; ++t) bi[t] = carry[t];
+                proj_block(r, lp, li, bi);
+                T* slot = hval + 9 * (int64_t)(rp + 1 + i);
+#pragma unroll
+                for (int t = 0; t < 9; ++t) {
+                    slot[t]  = bi[t];
+                    carry[t] = T(0);
+                }
+                proj_block(r, lp, lj, carry);
+            }
+        }
+        if (hval) {
+            if (k > 0) {
+                T* slot = hval + 9 * (int64_t)(rp + 1 + (bnd[p] ? k - 1 : 0));
+                if (bnd[p]) {
+#pragma unroll
+                    for (int t = 0; t < 9; ++t) slot[t] = carry[t];
+                } else {
+#pragma unroll
+                    for (int t = 0; t < 9; ++t) slot[t] += carry[t];
+                }
+            }
+            T* dslot = hval + 9 * (int64_t)rp;
+#pragma unroll
+            for (int t = 0; t < 9; ++t) dslot[t] = D[t];
+        }
+        if (grad) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) grad[3 * p + c] = g[c];
+        }
+    }
+}
+
 __global__ void k_sum_partials(const double* __restrict__ part, int n, double* __restrict__ out)
 {
     double v = 0;
@@ -513,6 +724,13 @@ rxg_status rxg_arap_rest(const rxg_mesh* h, const double* xyz_rest, int32_t dtyp
 rxg_status rxg_arap_eval(const rxg_mesh* h, int32_t dtype, const void* x, const void* rest,
                          double* energy, void* face_E, void* grad, rxg_bcsr* hess, void* stream)
 {
+    return rxg_arap_eval_ex(h, dtype, x, rest, 0, energy, face_E, grad, hess, stream);
+}
+
+rxg_status rxg_arap_eval_ex(const rxg_mesh* h, int32_t dtype, const void* x, const void* rest,
+                            int32_t flags, double* energy, void* face_E, void* grad,
+                            rxg_bcsr* hess, void* stream)
+{
     if (!h || !x || !rest || (dtype != RXG_F32 && dtype != RXG_F64)) {
         set_error("rxg_arap_eval: bad argument");
         return RXG_ERR_INVALID;
@@ -544,12 +762,23 @@ rxg_status rxg_arap_eval(const rxg_mesh* h, int32_t dtype, const void* x, const 
     // FP32: one thread per vertex evaluating its fan (cheap FP32 arithmetic,
     // no record traffic).  FP64 (bound by the FP64 pipe): each face evaluated
     // once into a global record, then the vertex gather.
+    // Projected Hessians (flags & RXG_ARAP_PROJECT_HESSIAN, with a Hessian
+    // requested): each face evaluated and projected once into a global
+    // record, in either precision.
     const bool    f64  = dtype == RXG_F64;
-    const int     NP   = f64 ? GF : G;  // energy partials
+    const bool    proj = hess && (flags & RXG_ARAP_PROJECT_HESSIAN);
+    const int     NP   = (f64 || proj) ? GF : G;  // energy partials
     double*       part;
     void*         rec = nullptr;
     RXG_CUDA_TRY(scratch_alloc((void**)&part, sizeof(double) * (NP + 1), s));
-    if (f64) {
+    if (proj) {
+        const size_t rb = (size_t)nf * kProjRec * (f64 ? 8 : 4);
+        cudaError_t  ea = scratch_alloc(&rec, rb, s);
+        if (ea != cudaSuccess) {
+            cudaFreeAsync(part, s);
+            return cuda_status(ea, "rxg_arap_eval: face records");
+        }
+    } else if (f64) {
         const size_t rb = (size_t)nf * (hess ? rec_words<true>() : rec_words<false>()) * 8;
         cudaError_t  ea = scratch_alloc(&rec, rb, s);
         if (ea != cudaSuccess) {
@@ -574,7 +803,18 @@ rxg_status rxg_arap_eval(const rxg_mesh* h, int32_t dtype, const void* x, const 
                                                   (T*)grad, hv);
         }
     };
-    if (dtype == RXG_F64) {
+    auto launch_proj = [&](auto tag) {
+        using T = decltype(tag);
+        k_arap_face_proj<T><<<GF, 128, 0, s>>>(nf, M.d.fv_lin, (const T*)x, (const T*)rest,
+                                              (T*)rec, (T*)face_E, part);
+        k_arap_gather_proj<T><<<G, 128, 0, s>>>(nv, z->row_ptr, z->ring_off, z->ring,
+                                               z->ring_face, z->bnd, M.d.fv_lin, (const T*)rec,
+                                               (T*)grad, (T*)hess->val);
+    };
+    if (proj) {
+        if (f64) launch_proj(double{});
+        else launch_proj(float{});
+    } else if (dtype == RXG_F64) {
         if (hess) launch(double{}, std::true_type{});
         else launch(double{}, std::false_type{});
     } else {

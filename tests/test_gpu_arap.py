@@ -20,7 +20,7 @@ def cloth(n=24, seed=4):
     return x0, x, f
 
 
-def oracle_ref(oracle, f, x0, x, rx, prob):
+def oracle_ref(oracle, f, x0, x, rx, prob, project=False, eps=1e-9):
     minv, area = oracle.rest_frame(f, x0)
     rp = prob.hess.row_ptr.cpu().numpy().astype(np.int64)
     vl = rx.linear_to_input("v")
@@ -35,7 +35,8 @@ def oracle_ref(oracle, f, x0, x, rx, prob):
         order.append(np.arange(rp[lin], rp[lin + 1]))
         rp_in[p + 1] = rp_in[p] + rp[lin + 1] - rp[lin]
     order = np.concatenate(order)
-    E, fE, g, H = oracle.arap_assemble(f, x, minv, area, rp_in, col_in[order].astype(np.int32))
+    E, fE, g, H = oracle.arap_assemble(f, x, minv, area, rp_in, col_in[order].astype(np.int32),
+                                       project=project, eps=eps)
     Hlin = np.empty_like(H)
     Hlin[order] = H
     return E, fE, g, Hlin, minv
@@ -118,3 +119,44 @@ def test_arap_gradient_central_differences():
         fdg = ((gp - gm) / (2 * h)).cpu().numpy().ravel()
         hd = Hs @ d.cpu().numpy().ravel()
         assert np.abs(fdg - hd).max() <= 1e-5 * max(1.0, np.abs(hd).max())
+
+
+@pytest.mark.parametrize("dtype,rtol,eps", [(torch.float64, 1e-10, 1e-9), (torch.float32, 5e-4, 1e-6)])
+@pytest.mark.parametrize("kind", ["cloth", "bunnyhead", "sphere"])
+def test_projected_hessian_matches_oracle(oracle, dtype, rtol, eps, kind):
+    """add_term<Op::FV, ProjectHess = true>: every face's 9x9 Hessian made
+    positive definite before assembly; the assembled Hessian is then positive
+    semi-definite, and energy and gradient are those of the plain evaluation."""
+    from rxmesh_gb300 import DiffScalarProblem, RXMeshStatic
+    if kind == "cloth":
+        x0, x, f = cloth()
+    elif kind == "bunnyhead":
+        g = golden("bunnyhead")
+        x0, f = g["xyz"], g["fv"]
+        x = x0 + 0.002 * np.random.default_rng(1).normal(size=x0.shape)
+    else:
+        v, f = meshgen.icosphere(3)
+        x0 = v
+        x = meshgen.radial_noise(v, 0.05, 2)
+    rx = RXMeshStatic(f, len(x0), patch_size=128)
+    x0l = rx.to_linear(torch.tensor(x0, device="cuda"))
+    xl = rx.to_linear(torch.tensor(x, device="cuda"))
+    plain = DiffScalarProblem(rx, dtype).add_arap_term(x0l)
+    plain.eval_terms(xl)
+    prob = DiffScalarProblem(rx, dtype).add_arap_term(x0l, project_hessian=True)
+    prob.eval_terms(xl)
+    E, fE, g, H, _ = oracle_ref(oracle, f, x0, x, rx, prob, project=True, eps=eps)
+    assert abs(prob.get_current_loss() - E) <= rtol * abs(E)
+    gg = rx.to_input(prob.grad).double().cpu().numpy()
+    assert np.abs(gg - g).max() <= rtol * np.abs(g).max()
+    assert torch.allclose(prob.grad, plain.grad, rtol=0, atol=1e-6 * plain.grad.abs().max().item())
+    Hg = prob.hess.val.double().cpu().numpy()
+    assert np.abs(Hg - H).max() <= rtol * np.abs(H).max()
+    if kind == "cloth":  # displaced corners: some faces are indefinite, so projection acts
+        assert np.abs(Hg - plain.hess.val.double().cpu().numpy()).max() > 1e-3 * np.abs(H).max()
+    A = prob.hess.to_scipy().astype(np.float64)
+    rng = np.random.default_rng(3)
+    for _ in range(8):
+        z = rng.normal(size=A.shape[0])
+        assert z @ (A @ z) >= -1e-6 * abs(z @ z) * np.abs(H).max()
+
