@@ -523,37 +523,68 @@ __device__ void jacobi_eigen(T* A, T* V)
     }
 }
 
-// H (K x K, symmetric, row-major) left alone when positive diagonally
-// dominant with margin eps; otherwise eigenvalues below eps are raised to eps
-// and, if any was, H = V diag(lambda) V^T.
-template <typename T, int K>
-__device__ void project_pd(T* H, T eps)
+// The rule of project_positive_definite on a face's 9x9 vertex-space
+// Hessian H9 = D^T Hu D, with D = d^T (x) I3 (u_k = sum_v d[v][k] x_v): left
+// alone when positive diagonally dominant with margin eps; otherwise
+// eigenvalues below eps raised to eps and H9 rebuilt.  d's two columns sum
+// to zero, so with d = q R2 (Gram-Schmidt, q orthonormal 3x2) H9 = Q M Q^T,
+// Q = q (x) I3, M = (R2 (x) I3) Hu (R2^T (x) I3) (6x6); H9's other three
+// eigenvalues are 0 (the translations t (x) I3, t = (1,1,1)/sqrt 3).  So the
+// 9x9 eigenproblem is M's 6x6 one, and the translations (eigenvalue 0 < eps)
+// are always raised to eps: H9' = (QW) diag(max(lambda, eps)) (QW)^T +
+// eps (t t^T (x) I3) -- the same matrix as projecting H9 directly.
+template <typename T>
+__device__ void project_face_hessian(const FaceDeriv<T>& o, T eps, T* H)
 {
     bool dd = true;
-    for (int i = 0; i < K && dd; ++i) {
+    for (int i = 0; i < 9 && dd; ++i) {
         T off = 0;
-        for (int j = 0; j < K; ++j)
-            if (j != i) off += fabs(H[i * K + j]);
-        dd = H[i * K + i] >= off + eps;
+        for (int j = 0; j < 9; ++j)
+            if (j != i) off += fabs(H[i * 9 + j]);
+        dd = H[i * 9 + i] >= off + eps;
     }
     if (dd) return;
-    T A[K * K], V[K * K], lam[K];
-    for (int i = 0; i < K * K; ++i) A[i] = H[i];
-    jacobi_eigen<T, K>(A, V);
-    bool clamped = false;
-    for (int i = 0; i < K; ++i) {
-        lam[i] = A[i * K + i];
-        if (lam[i] < eps) {
-            lam[i]  = eps;
-            clamped = true;
-        }
+    // d = q R2
+    T a[3], b[3], q[3][2];
+    for (int v = 0; v < 3; ++v) {
+        a[v] = o.d[v][0];
+        b[v] = o.d[v][1];
     }
-    if (!clamped) return;
-    for (int i = 0; i < K; ++i)
-        for (int j = 0; j < K; ++j) {
-            T v = 0;
-            for (int m = 0; m < K; ++m) v += V[i * K + m] * lam[m] * V[j * K + m];
-            H[i * K + j] = v;
+    const T r11 = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    for (int v = 0; v < 3; ++v) q[v][0] = a[v] / r11;
+    const T r12 = q[0][0] * b[0] + q[1][0] * b[1] + q[2][0] * b[2];
+    for (int v = 0; v < 3; ++v) b[v] -= r12 * q[v][0];
+    const T r22 = sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+    for (int v = 0; v < 3; ++v) q[v][1] = b[v] / r22;
+    const T R[2][2] = {{r11, r12}, {T(0), r22}};
+    // M[(m,c),(n,e)] = sum_kl R[m][k] Hu[(k,c),(l,e)] R[n][l]
+    T M[36], W[36];
+    for (int m = 0; m < 2; ++m)
+        for (int c = 0; c < 3; ++c)
+            for (int n = 0; n < 2; ++n)
+                for (int e = 0; e < 3; ++e) {
+                    T acc = 0;
+                    for (int k = 0; k < 2; ++k)
+                        for (int l = 0; l < 2; ++l)
+                            acc += R[m][k] * o.Hu[3 * k + c][3 * l + e] * R[n][l];
+                    M[(3 * m + c) * 6 + 3 * n + e] = acc;
+                }
+    jacobi_eigen<T, 6>(M, W);
+    T lam[6];
+    for (int j = 0; j < 6; ++j) lam[j] = M[j * 6 + j] < eps ? eps : M[j * 6 + j];
+    // QW[(v,c), j] = sum_m q[v][m] W[(m,c), j]
+    T QW[54];
+    for (int v = 0; v < 3; ++v)
+        for (int c = 0; c < 3; ++c)
+            for (int j = 0; j < 6; ++j)
+                QW[(3 * v + c) * 6 + j] = q[v][0] * W[(0 + c) * 6 + j] + q[v][1] * W[(3 + c) * 6 + j];
+    const T et = eps / T(3);
+    for (int r = 0; r < 9; ++r)
+        for (int cc = r; cc < 9; ++cc) {
+            T acc = (r % 3 == cc % 3) ? et : T(0);
+            for (int j = 0; j < 6; ++j) acc += QW[r * 6 + j] * lam[j] * QW[cc * 6 + j];
+            H[r * 9 + cc] = acc;
+            H[cc * 9 + r] = acc;
         }
 }
 
@@ -587,7 +618,7 @@ __global__ void __launch_bounds__(128) k_arap_face_proj(
                 for (int a = 0; a < 3; ++a)
                     for (int c = 0; c < 3; ++c) H[(3 * i + a) * 9 + 3 * j + c] = b[3 * a + c];
             }
-        project_pd<T, 9>(H, eps);
+        project_face_hessian(o, eps, H);
         T* r = rec + (int64_t)kProjRec * f;
         r[0] = o.E;
         for (int i = 0; i < 6; ++i) r[1 + i] = o.gE[i];
