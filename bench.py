@@ -490,6 +490,33 @@ def run_arap(args, torch):
         res[dt_name] = {"ms_energy_grad_hessian": ms,
                         "gbs_algorithmic": (bytes_eg + bytes_h) / (ms * 1e-3) / 1e9,
                         "energy": prob.get_current_loss()}
+    # Newton iterations (diff/newton_solver.h) with the 4 corners fixed:
+    # projected FP32 Hessian, boundary conditions, PCG on its scalar form,
+    # backtracking line search
+    from rxmesh_gb300 import NewtonSolver
+    prob = DiffScalarProblem(rx, torch.float32).add_arap_term(rest, project_hessian=True)
+    xn = xl.to(torch.float32).clone()
+    bc = torch.zeros(V, dtype=torch.int8, device="cuda")
+    il = rx.input_to_linear("v")
+    bc[torch.tensor(il[[0, n - 1, n * (n - 1), n * n - 1]], device="cuda", dtype=torch.long)] = 1
+    newton = NewtonSolver(prob, "pcg", max_iter=1000, abs_tol=0.0, rel_tol=1e-6)
+    prob.eval_terms(xn)
+    e0 = prob.get_current_loss()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    iters = []
+    for _ in range(3):
+        prob.eval_terms(xn)
+        prob.hess.apply_bc(bc, prob.grad)
+        newton.compute_direction()
+        newton.line_search()
+        iters.append(newton.solver.iter_taken())
+    torch.cuda.synchronize()
+    res["newton_f32_projected"] = {"ms_per_iteration": 1e3 * (time.perf_counter() - t0) / 3,
+                                   "pcg_ms_per_iteration": newton.solve_time / 3,
+                                   "pcg_iters": iters, "energy_before": e0,
+                                   "energy_after_3": prob.get_current_loss(),
+                                   "solver": "PCG on the scalar Hessian, rel. tol 1e-6, max 1000"}
     # adjoint through 20 steps
     prob = DiffScalarProblem(rx, torch.float64, assemble_hessian=False).add_arap_term(rest)
     times = []

@@ -392,6 +392,24 @@ rxg_status rxg_arap_eval_ex(const rxg_mesh* m, int32_t dtype, const void* x,
                             const void* rest, int32_t flags, double* energy,
                             void* face_E, void* grad, rxg_bcsr* hess, void* stream);
 
+/*
+ * Scalar CSR (3n x 3n) of a 3x3-block CSR, the form the reference's
+ * CG/PCG solvers work on for a Hessian (HessianSparseMatrix,
+ * diff/hessian_sparse_matrix.h:16-137): scalar row 3i+a lists, block by
+ * block in the block row's order, the entries 3j+0..2 of block (i,j).
+ * out->row_ptr (3n+1), out->col and out->val (9*nnzb) are caller-allocated
+ * device arrays; n, nnz and dtype are set.  Feeds rxg_cg_solve (nc = 1).
+ */
+rxg_status rxg_bcsr_to_csr(const rxg_bcsr* H, rxg_csr* out, void* stream);
+
+/*
+ * apply_bc of NewtonSolver (diff/newton_solver.h): for every vertex i with
+ * bc[i] != 0, block row i gets the identity as its diagonal block and zero
+ * off-diagonal blocks, every block (j, i) is zeroed, and row i of grad
+ * (n*3, H's dtype, may be NULL) is zeroed.  Device arrays.
+ */
+rxg_status rxg_bcsr_apply_bc(rxg_bcsr* H, const int8_t* bc, void* grad, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -14,7 +14,7 @@ from . import _lib
 from ._lib import RXGError, check
 
 __all__ = ["Op", "RXMeshStatic", "SparseMatrix", "CGSolver", "PCGSolver", "RXGError",
-           "DiffScalarProblem", "BlockSparseMatrix", "mcf_step", "MeshBatch",
+           "DiffScalarProblem", "BlockSparseMatrix", "NewtonSolver", "mcf_step", "MeshBatch",
            "device_check"]
 
 
@@ -204,5 +204,5 @@ class RXMeshStatic:
 
 
 from ._solvers import SparseMatrix, CGSolver, PCGSolver, mcf_step, MeshBatch  # noqa: E402
-from ._diff import (DiffScalarProblem, BlockSparseMatrix, ArapEnergy, MCFFlow,  # noqa: E402
+from ._diff import (DiffScalarProblem, BlockSparseMatrix, NewtonSolver, ArapEnergy, MCFFlow,  # noqa: E402
                     arap_energy, mcf_flow, mcf_step_backward)

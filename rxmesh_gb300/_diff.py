@@ -34,6 +34,28 @@ class BlockSparseMatrix:
         self.col = torch.zeros(nnzb, dtype=torch.int32, device=device)
         self.val = torch.zeros(nnzb, 3, 3, dtype=dtype, device=device)
 
+    def to_csr(self, out=None, stream=None):
+        """Scalar 3n x 3n CSR of this block matrix (rxg_bcsr_to_csr), the form
+        the CG/PCG solvers take; out: a SparseMatrix of the right sizes to reuse."""
+        from ._solvers import SparseMatrix
+        n, nnzb = self.row_ptr.numel() - 1, self.col.numel()
+        if out is None:
+            dev = self.val.device
+            out = SparseMatrix(row_ptr=torch.empty(3 * n + 1, dtype=torch.int32, device=dev),
+                               col=torch.empty(9 * nnzb, dtype=torch.int32, device=dev),
+                               val=torch.empty(9 * nnzb, dtype=self.val.dtype, device=dev))
+        b, c = self.bcsr(), out.csr()
+        check(_lib.load().rxg_bcsr_to_csr(ctypes.byref(b), ctypes.byref(c), _stream(stream)))
+        return out
+
+    def apply_bc(self, bc, grad=None, stream=None):
+        """NewtonSolver::apply_bc (diff/newton_solver.h): bc (nv,) bool/int8 in
+        linear order; identity diagonal blocks and zero coupling for
+        constrained vertices, their gradient rows zeroed."""
+        m = bc.to(torch.int8).contiguous()
+        b = self.bcsr()
+        check(_lib.load().rxg_bcsr_apply_bc(ctypes.byref(b), _p(m), _p(grad), _stream(stream)))
+
     def bcsr(self):
         b = _lib.BCSR()
         b.n = self.row_ptr.numel() - 1
@@ -67,6 +89,7 @@ class DiffScalarProblem:
         self.hess = BlockSparseMatrix(n.value, nnz.value, dtype, dev) if assemble_hessian else None
         self.rest = None
         self.project_hessian = False
+        self.opt_var = None
         self._loss = None
 
     def add_arap_term(self, rest_xyz_lin, project_hessian=False):
@@ -79,11 +102,14 @@ class DiffScalarProblem:
         check(self._L.rxg_arap_rest(self.rx._h, _p(xr), _DT[self.dtype], _p(self.rest), _stream()))
         return self
 
-    def eval_terms(self, x_lin, with_hessian=None, stream=None):
-        """Energy, gradient (and Hessian) at x_lin (nv,3, linear order)."""
+    def eval_terms(self, x_lin=None, with_hessian=None, stream=None):
+        """Energy, gradient (and Hessian) at x_lin (nv,3, linear order), which
+        becomes the problem's opt_var (x_lin None: at the current opt_var)."""
         if self.rest is None:
             raise RuntimeError("add_arap_term() first")
-        x = x_lin.to(self.dtype).contiguous()
+        if x_lin is not None:
+            self.opt_var = x_lin
+        x = self.opt_var.to(self.dtype).contiguous()
         h = self.assemble_hessian if with_hessian is None else with_hessian
         e = torch.zeros(1, dtype=torch.float64, device=x.device)
         b = self.hess.bcsr() if (h and self.hess is not None) else None
@@ -94,8 +120,78 @@ class DiffScalarProblem:
         self._loss = e
         return e
 
+    def eval_terms_passive(self, x_lin, stream=None):
+        """Energy alone at x_lin (eval_terms_passive, diff_scalar_problem.h):
+        gradient, Hessian and opt_var are left untouched."""
+        x = x_lin.to(self.dtype).contiguous()
+        e = torch.zeros(1, dtype=torch.float64, device=x.device)
+        check(self._L.rxg_arap_eval_ex(self.rx._h, _DT[self.dtype], _p(x), _p(self.rest), 0,
+                                       _p(e), None, None, None, _stream(stream)))
+        self._loss = e
+        return e
+
     def get_current_loss(self):
         return float(self._loss.item())
+
+
+class NewtonSolver:
+    """NewtonSolver<T, 3, VertexHandle, SolverT> (diff/newton_solver.h:17-330)
+    on a DiffScalarProblem: compute_direction() solves H dir = -grad with a
+    CG or PCG solver on the scalar form of the Hessian (rxg_bcsr_to_csr +
+    rxg_cg_solve); line_search() backtracks on the energy with the Armijo
+    test of diff/armijo_condition.h.  As in the reference, compute_direction
+    leaves problem.grad negated, and the Armijo test then uses dir . grad of
+    that negated gradient."""
+
+    def __init__(self, problem, solver="pcg", max_iter=1000, abs_tol=1e-12, rel_tol=0.0):
+        from ._solvers import CGSolver, PCGSolver
+        self.problem = problem
+        self.dir = torch.zeros_like(problem.grad)
+        self._solver_cls = PCGSolver if solver == "pcg" else CGSolver
+        self.max_iter, self.abs_tol, self.rel_tol = max_iter, abs_tol, rel_tol
+        self._A = None
+        self.solver = None
+        self.solve_time = 0.0
+
+    def compute_direction(self, stream=None):
+        p = self.problem
+        p.grad.mul_(-1)
+        self._A = p.hess.to_csr(out=self._A, stream=stream)
+        self.solver = self._solver_cls(self._A, 1, self.max_iter, self.abs_tol, self.rel_tol)
+        self.dir.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        self.solver.solve(p.grad.reshape(-1, 1), self.dir.view(-1, 1), stream)
+        b.record()
+        b.synchronize()
+        self.solve_time += a.elapsed_time(b)
+
+    def line_search(self, s_max=1.0, shrink=0.8, max_iters=64, armijo_const=1e-4, cb=None,
+                    stream=None):
+        p = self.problem
+        assert s_max > 0.0
+        try_one = s_max > 1.0
+        s = s_max
+        f = p.get_current_loss()
+        slope = float((self.dir * p.grad).sum())  # dir . grad, grad negated by compute_direction
+        x = p.opt_var
+        for _ in range(max_iters):
+            t = x + s * self.dir.to(x.dtype)
+            if cb is not None:
+                cb(t)
+            f_new = float(p.eval_terms_passive(t, stream).item())
+            if f_new <= f + armijo_const * s * slope:
+                x.copy_(t)
+                return True
+            if try_one and s > 1.0 and s * shrink < 1.0:
+                s = 1.0
+            else:
+                s *= shrink
+        return False
+
+    def apply_bc(self, bc, stream=None):
+        self.problem.hess.apply_bc(bc, self.problem.grad, stream)
 
 
 def mcf_step_backward(rx, x_in, x_out, g_out, dt, tol=1e-12, max_iter=20000, stream=None):

@@ -17,6 +17,7 @@
 // record (k_arap_face) that its three vertices then read (k_arap_gather).
 #include <algorithm>
 #include <cfloat>
+#include <climits>
 #include <cstdlib>
 #include <type_traits>
 
@@ -714,6 +715,67 @@ __global__ void __launch_bounds__(128) k_arap_gather_proj(
     }
 }
 
+// ---------------------------------------------------------------------
+// Block-CSR helpers of the Newton step (diff/newton_solver.h)
+// ---------------------------------------------------------------------
+
+// scalar CSR of a 3x3-block CSR: scalar row 3i+a lists, block by block in
+// the block row's order, the three entries (3j+0..2) of each block (i,j)
+template <typename T>
+__global__ void k_bcsr_expand(int64_t n, const int32_t* __restrict__ brp,
+                              const int32_t* __restrict__ bcol, const T* __restrict__ bval,
+                              int32_t* __restrict__ rp, int32_t* __restrict__ col,
+                              T* __restrict__ val)
+{
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < 3 * n;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i  = r / 3;
+        const int     a  = (int)(r - 3 * i);
+        const int32_t b0 = brp[i], nb = brp[i + 1] - b0;
+        const int64_t o  = 9 * (int64_t)b0 + 3 * (int64_t)a * nb;
+        rp[r]            = (int32_t)o;
+        if (r == 3 * n - 1) rp[3 * n] = 9 * brp[n];
+        for (int32_t t = 0; t < nb; ++t) {
+            const int32_t j = bcol[b0 + t];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                col[o + 3 * t + c] = 3 * j + c;
+                val[o + 3 * t + c] = bval[9 * (int64_t)(b0 + t) + 3 * a + c];
+            }
+        }
+    }
+}
+
+// apply_bc of diff/newton_solver.h on the block form: a constrained block
+// row gets the identity as its diagonal block and zero off-diagonal blocks,
+// every block (i, j) with j constrained is zeroed (the symmetric entries),
+// and the constrained rows of the gradient are zeroed.
+template <typename T>
+__global__ void k_bcsr_apply_bc(int64_t n, const int32_t* __restrict__ brp,
+                                const int32_t* __restrict__ bcol, T* __restrict__ bval,
+                                const int8_t* __restrict__ bc, T* __restrict__ grad)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const bool ci = bc[i] != 0;
+        for (int32_t t = brp[i]; t < brp[i + 1]; ++t) {
+            const int32_t j = bcol[t];
+            T*            b = bval + 9 * (int64_t)t;
+            if (j == i) {
+                if (ci)
+#pragma unroll
+                    for (int e = 0; e < 9; ++e) b[e] = (e % 4 == 0) ? T(1) : T(0);
+            } else if (ci || bc[j] != 0) {
+#pragma unroll
+                for (int e = 0; e < 9; ++e) b[e] = T(0);
+            }
+        }
+        if (ci && grad)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) grad[3 * i + c] = T(0);
+    }
+}
+
 __global__ void k_sum_partials(const double* __restrict__ part, int n, double* __restrict__ out)
 {
     double v = 0;
@@ -865,6 +927,53 @@ rxg_status rxg_arap_eval_ex(const rxg_mesh* h, int32_t dtype, const void* x, con
     }
     cudaFreeAsync(part, s);
     if (e != cudaSuccess) return cuda_status(e, "rxg_arap_eval");
+    return RXG_OK;
+}
+
+rxg_status rxg_bcsr_to_csr(const rxg_bcsr* H, rxg_csr* out, void* stream)
+{
+    if (!H || !out || !H->row_ptr || !H->col || !H->val || !out->row_ptr || !out->col ||
+        !out->val || (H->dtype != RXG_F32 && H->dtype != RXG_F64)) {
+        set_error("rxg_bcsr_to_csr: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    if (9 * H->nnzb > (int64_t)INT32_MAX || 3 * H->n > (int64_t)INT32_MAX) {
+        set_error("rxg_bcsr_to_csr: %lld blocks exceed 32-bit scalar indices", (long long)H->nnzb);
+        return RXG_ERR_INVALID;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    out->n         = 3 * H->n;
+    out->nnz       = 9 * H->nnzb;
+    out->dtype     = H->dtype;
+    if (H->n == 0) return RXG_OK;
+    const int g = grid_for_items(3 * H->n);
+    if (H->dtype == RXG_F64)
+        k_bcsr_expand<double><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const double*)H->val,
+                                                out->row_ptr, out->col, (double*)out->val);
+    else
+        k_bcsr_expand<float><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const float*)H->val,
+                                               out->row_ptr, out->col, (float*)out->val);
+    RXG_CUDA_TRY(cudaGetLastError());
+    return RXG_OK;
+}
+
+rxg_status rxg_bcsr_apply_bc(rxg_bcsr* H, const int8_t* bc, void* grad, void* stream)
+{
+    if (!H || !bc || !H->row_ptr || !H->col || !H->val ||
+        (H->dtype != RXG_F32 && H->dtype != RXG_F64)) {
+        set_error("rxg_bcsr_apply_bc: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (H->n == 0) return RXG_OK;
+    const int g = grid_for_items(H->n);
+    if (H->dtype == RXG_F64)
+        k_bcsr_apply_bc<double><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (double*)H->val, bc,
+                                                  (double*)grad);
+    else
+        k_bcsr_apply_bc<float><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (float*)H->val, bc,
+                                                 (float*)grad);
+    RXG_CUDA_TRY(cudaGetLastError());
     return RXG_OK;
 }
 
