@@ -471,6 +471,35 @@ __device__ __forceinline__ void row_spmv(const int32_t* __restrict__ rp, const i
     }
 }
 
+// row i of A times x by a group of L lanes (L = 2, 4, 8; the group is L
+// aligned lanes of one warp): lane l takes entries b+l, b+l+L, ... (adjacent
+// lanes read adjacent entries), then the group sums its partials.  diag
+// (may be null) receives A_ii in every lane of the group.
+template <typename T, int NC, int L>
+__device__ __forceinline__ void row_spmv_group(const int32_t* __restrict__ rp,
+                                               const int32_t* __restrict__ col,
+                                               const T* __restrict__ val, int64_t i, const T* x,
+                                               T* acc, T* diag, int lane)
+{
+    const int32_t b = __ldg(rp + i), e = __ldg(rp + i + 1);
+    T             d = T(0);
+    for (int32_t j = b + lane; j < e; j += L) {
+        const int32_t c = __ldg(col + j);
+        const T       v = __ldg(val + j);
+        if (c == i) d = v;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) acc[k] += v * x[(int64_t)c * NC + k];
+    }
+    const unsigned mask = ((1u << L) - 1u) << ((threadIdx.x & 31) & ~(L - 1));
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < NC; ++k) acc[k] += __shfl_xor_sync(mask, acc[k], o);
+        d += __shfl_xor_sync(mask, d, o);
+    }
+    if (diag) *diag = d;
+}
+
 // scalar recurrence of k_cgm, in shared memory, touched by thread 0 only
 struct CGMScalars
 {
@@ -492,7 +521,8 @@ __device__ __forceinline__ bool cgm_sum(double v, double* s_part, GridSum& g, Re
     return grid_sum_staged<BT>(v, s_part, g, r, post);
 }
 
-template <typename T, int NC, bool PC, int kCGT>
+// L: lanes per matrix row in the two SpMV passes (1, or 4 for long rows)
+template <typename T, int NC, bool PC, int kCGT, int L>
 __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
 {
     __shared__ RedSmem    red;
@@ -511,13 +541,16 @@ __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
     // runs on thread 0 (rxg_gridsum.cuh).
 
     // ---- pre_solve: S = A X, R = B - S, Z = D^-1 R, delta = R.Z (or R.R)
-    T tpart = T(0);
-    for (int64_t i = r0 + threadIdx.x; i < r1; i += kCGT) {
+    const int lane = (int)threadIdx.x & (L - 1);
+    T         tpart = T(0);
+    for (int64_t i = r0 + threadIdx.x / L; i < r1; i += kCGT / L) {
         T acc[NC];
 #pragma unroll
         for (int k = 0; k < NC; ++k) acc[k] = T(0);
         T diag = T(0);
-        row_spmv<T, NC>(a.rp, a.col, a.val, i, a.X, acc, &diag);
+        if (L == 1) row_spmv<T, NC>(a.rp, a.col, a.val, i, a.X, acc, &diag);
+        else row_spmv_group<T, NC, (L > 1 ? L : 2)>(a.rp, a.col, a.val, i, a.X, acc, &diag, lane);
+        if (lane != 0) continue;
         const T di = T(1) / (diag + (sizeof(T) == 4 ? (T)FLT_EPSILON : (T)DBL_EPSILON));
         if (PC) a.dinv[i] = di;
 #pragma unroll
@@ -551,11 +584,13 @@ __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
         //      S.p.  Only own rows of S and p are read back, so the p update
         //      needs neither extra work per non-zero nor another barrier.
         tpart = T(0);
-        for (int64_t i = r0 + threadIdx.x; i < r1; i += kCGT) {
+        for (int64_t i = r0 + threadIdx.x / L; i < r1; i += kCGT / L) {
             T acc[NC];
 #pragma unroll
             for (int k = 0; k < NC; ++k) acc[k] = T(0);
-            row_spmv<T, NC>(a.rp, a.col, a.val, i, src, acc, (T*)nullptr);
+            if (L == 1) row_spmv<T, NC>(a.rp, a.col, a.val, i, src, acc, (T*)nullptr);
+            else row_spmv_group<T, NC, (L > 1 ? L : 2)>(a.rp, a.col, a.val, i, src, acc, (T*)nullptr, lane);
+            if (lane != 0) continue;
 #pragma unroll
             for (int k = 0; k < NC; ++k) {
                 const T si = first ? acc[k] : acc[k] + bt * a.S[i * NC + k];
@@ -642,9 +677,17 @@ static int cg_grid_bt(int64_t n)
 {
     static int per_sm = -1;
     if (per_sm < 0) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg<T, NC, PC, BT>, BT, 0) !=
+        // the grid must fit whichever variant runs (cooperative launch)
+        int p1 = 0, p4 = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p1, k_cg<T, NC, PC, BT, 1>, BT, 0) !=
             cudaSuccess)
-            per_sm = 1;
+            p1 = 1;
+        p4 = p1;
+        if constexpr (NC == 1)
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p4, k_cg<T, NC, PC, BT, 4>, BT, 0) !=
+                cudaSuccess)
+                p4 = 1;
+        per_sm = std::min(p1, p4);
         int cap = 4;
         if (const char* e = getenv("RXG_CG_BLOCKS_PER_SM")) cap = std::max(1, atoi(e));
         per_sm = std::max(1, std::min(per_sm, cap));
@@ -674,9 +717,9 @@ static size_t cg_scratch_bytes(int64_t n, int nc, int G)
 }
 
 template <typename T, int NC, bool PC>
-static rxg_status cg_launch(int64_t n, const int32_t* rp, const int32_t* col, const T* val,
-                            const T* B, T* X, const rxg_solver_opts& o, rxg_solver_stats* st,
-                            uint8_t* scratch, cudaStream_t s)
+static rxg_status cg_launch(int64_t n, int64_t nnz, const int32_t* rp, const int32_t* col,
+                            const T* val, const T* B, T* X, const rxg_solver_opts& o,
+                            rxg_solver_stats* st, uint8_t* scratch, cudaStream_t s)
 {
     const int  G = cg_grid<T, NC, PC>(n);
     CGArgs<T>  a;
@@ -704,9 +747,26 @@ static rxg_status cg_launch(int64_t n, const int32_t* rp, const int32_t* col, co
     a.err      = device_error_word();
     RXG_CUDA_TRY(reset_grid_sum(a.bar, s));
     void* args[] = {&a};
-    const void* kern = cg_threads() == 256    ? (const void*)k_cg<T, NC, PC, 256>
-                       : cg_threads() == 1024 ? (const void*)k_cg<T, NC, PC, 1024>
-                                              : (const void*)k_cg<T, NC, PC, 512>;
+    // rows of 12 or more entries on average (a Hessian's scalar form): four
+    // lanes per row in the SpMV passes, so adjacent lanes read adjacent entries
+    const bool  l4 = n > 0 && nnz >= 12 * n;
+    const int   bt = cg_threads();
+    const void* kern;
+    if constexpr (NC == 1) {
+        if (l4)
+            kern = bt == 256    ? (const void*)k_cg<T, NC, PC, 256, 4>
+                   : bt == 1024 ? (const void*)k_cg<T, NC, PC, 1024, 4>
+                                : (const void*)k_cg<T, NC, PC, 512, 4>;
+        else
+            kern = bt == 256    ? (const void*)k_cg<T, NC, PC, 256, 1>
+                   : bt == 1024 ? (const void*)k_cg<T, NC, PC, 1024, 1>
+                                : (const void*)k_cg<T, NC, PC, 512, 1>;
+    } else {
+        (void)l4;
+        kern = bt == 256    ? (const void*)k_cg<T, NC, PC, 256, 1>
+               : bt == 1024 ? (const void*)k_cg<T, NC, PC, 1024, 1>
+                            : (const void*)k_cg<T, NC, PC, 512, 1>;
+    }
     RXG_CUDA_TRY(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(cg_threads()), args, 0, s));
     if (st) {
         double ds[2];
@@ -725,14 +785,15 @@ static rxg_status cg_launch(int64_t n, const int32_t* rp, const int32_t* col, co
 }
 
 template <typename T>
-static rxg_status cg_dispatch(int nc, int64_t n, const int32_t* rp, const int32_t* col,
-                              const T* val, const T* B, T* X, const rxg_solver_opts& o,
-                              rxg_solver_stats* st, uint8_t* scratch, cudaStream_t s)
+static rxg_status cg_dispatch(int nc, int64_t n, int64_t nnz, const int32_t* rp,
+                              const int32_t* col, const T* val, const T* B, T* X,
+                              const rxg_solver_opts& o, rxg_solver_stats* st, uint8_t* scratch,
+                              cudaStream_t s)
 {
-#define RXG_CG_CASE(NCV)                                                                         \
-    case NCV:                                                                                    \
-        return o.precond ? cg_launch<T, NCV, true>(n, rp, col, val, B, X, o, st, scratch, s)    \
-                         : cg_launch<T, NCV, false>(n, rp, col, val, B, X, o, st, scratch, s);
+#define RXG_CG_CASE(NCV)                                                                          \
+    case NCV:                                                                                     \
+        return o.precond ? cg_launch<T, NCV, true>(n, nnz, rp, col, val, B, X, o, st, scratch, s) \
+                         : cg_launch<T, NCV, false>(n, nnz, rp, col, val, B, X, o, st, scratch, s);
     switch (nc) {
         RXG_CG_CASE(1)
         RXG_CG_CASE(2)
@@ -1299,12 +1360,12 @@ rxg_status rxg_cg_solve(const rxg_csr* A, int32_t nc, const void* B, void* X,
     if (A->dtype == RXG_F64) {
         const size_t bytes = cg_scratch_bytes<double>(A->n, nc, cg_grid_any<double>(nc, pc, A->n));
         RXG_CUDA_TRY(scratch_alloc((void**)&scratch, bytes, s));
-        st = cg_dispatch<double>(nc, A->n, A->row_ptr, A->col, (const double*)A->val,
+        st = cg_dispatch<double>(nc, A->n, A->nnz, A->row_ptr, A->col, (const double*)A->val,
                                  (const double*)B, (double*)X, *opts, &local, scratch, s);
     } else {
         const size_t bytes = cg_scratch_bytes<float>(A->n, nc, cg_grid_any<float>(nc, pc, A->n));
         RXG_CUDA_TRY(scratch_alloc((void**)&scratch, bytes, s));
-        st = cg_dispatch<float>(nc, A->n, A->row_ptr, A->col, (const float*)A->val,
+        st = cg_dispatch<float>(nc, A->n, A->nnz, A->row_ptr, A->col, (const float*)A->val,
                                 (const float*)B, (float*)X, *opts, &local, scratch, s);
     }
     cudaFreeAsync(scratch, s);
@@ -1540,10 +1601,10 @@ extern "C" rxg_status rxg_cg_solve_noalloc(const rxg_csr* A, int32_t nc, const v
     cudaStream_t     s = (cudaStream_t)stream;
     rxg_solver_stats local;
     if (A->dtype == RXG_F64)
-        st = cg_dispatch<double>(nc, A->n, A->row_ptr, A->col, (const double*)A->val,
+        st = cg_dispatch<double>(nc, A->n, A->nnz, A->row_ptr, A->col, (const double*)A->val,
                                  (const double*)B, (double*)X, *opts, &local, scratch, s);
     else
-        st = cg_dispatch<float>(nc, A->n, A->row_ptr, A->col, (const float*)A->val,
+        st = cg_dispatch<float>(nc, A->n, A->nnz, A->row_ptr, A->col, (const float*)A->val,
                                 (const float*)B, (float*)X, *opts, &local, scratch, s);
     if (st) return st;
     if (stats) *stats = local;
@@ -1757,7 +1818,7 @@ extern "C" rxg_status rxg_mcf_step_backward(const rxg_mesh* h, double dt, const 
     RXG_CUDA_TRY(cudaMemsetAsync(lam, 0, 24 * n, s));
     rxg_solver_opts  o = {max_iter, 0.0, tol * tol, 1};
     rxg_solver_stats local;
-    st = cg_dispatch<double>(3, n, z->row_ptr, z->col, val, g_out, lam, o, &local, scr, s);
+    st = cg_dispatch<double>(3, n, z->nnz, z->row_ptr, z->col, val, g_out, lam, o, &local, scr, s);
     if (st) return st;
     RXG_CUDA_TRY(cudaMemsetAsync(g_in, 0, 24 * n, s));
     k_mcf_backward<<<grid_for(n, 128), 128, 0, s>>>(n, z->row_ptr, z->col, z->bnd, x_in, x_out, lam,
