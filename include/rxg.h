@@ -410,6 +410,31 @@ rxg_status rxg_bcsr_to_csr(const rxg_bcsr* H, rxg_csr* out, void* stream);
  */
 rxg_status rxg_bcsr_apply_bc(rxg_bcsr* H, const int8_t* bc, void* grad, void* stream);
 
+/*
+ * Hessian-vector product without an assembled Hessian (the reference's
+ * DiffScalarProblem::eval_matvec, diff/diff_query_kernel.cuh:26-148):
+ * y = H(x) v for the ARAP term at positions x (nv*3, linear order), v, y
+ * nv*3 of dtype; flags as rxg_arap_eval_ex (RXG_ARAP_PROJECT_HESSIAN).  bc
+ * (nv int8, may be NULL): constrained vertices get identity rows and zero
+ * columns, the Hessian that apply_bc would leave.  Device arrays.
+ */
+rxg_status rxg_arap_hvp(const rxg_mesh* m, int32_t dtype, const void* x,
+                        const void* rest, int32_t flags, const int8_t* bc,
+                        const void* v, void* y, void* stream);
+
+/*
+ * Matrix-free CG on H(x) X = B (CGMatFreeSolver, matrix/cg_mat_free_solver.h,
+ * un-preconditioned: opts->precond must be 0), H as in rxg_arap_hvp; each
+ * face is evaluated once per call, then every iteration's product is a
+ * per-vertex gather over the fan faces.  One cooperative launch; stops when
+ * r.r < abs_tol or r.r / r0.r0 < rel_tol, or after max_iter iterations
+ * (RXG_ERR_NOT_CONVERGED).  B, X: nv*3 of dtype, X is the initial guess.
+ */
+rxg_status rxg_arap_cg_matfree(const rxg_mesh* m, int32_t dtype, const void* x,
+                               const void* rest, int32_t flags, const int8_t* bc,
+                               const void* B, void* X, const rxg_solver_opts* opts,
+                               rxg_solver_stats* stats, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

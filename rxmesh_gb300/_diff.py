@@ -130,6 +130,20 @@ class DiffScalarProblem:
         self._loss = e
         return e
 
+    def eval_matvec(self, v, out=None, bc=None, stream=None):
+        """out = H(opt_var) v without an assembled Hessian (eval_matvec,
+        diff/diff_query_kernel.cuh:26-148; rxg_arap_hvp); bc (nv,) int8/bool:
+        identity rows and zero columns for constrained vertices."""
+        x = self.opt_var.to(self.dtype).contiguous()
+        vv = v.to(self.dtype).contiguous()
+        if out is None:
+            out = torch.empty_like(vv)
+        m = bc.to(torch.int8).contiguous() if bc is not None else None
+        check(self._L.rxg_arap_hvp(self.rx._h, _DT[self.dtype], _p(x), _p(self.rest),
+                                   1 if self.project_hessian else 0, _p(m), _p(vv), _p(out),
+                                   _stream(stream)))
+        return out
+
     def get_current_loss(self):
         return float(self._loss.item())
 
@@ -144,9 +158,15 @@ class NewtonSolver:
     that negated gradient."""
 
     def __init__(self, problem, solver="pcg", max_iter=1000, abs_tol=1e-12, rel_tol=0.0):
+        """solver: "pcg" or "cg" on the assembled Hessian's scalar form, or
+        "cg_matfree" (CGMatFreeSolver: CG with Hessian-vector products from
+        the face records, no assembled Hessian; rxg_arap_cg_matfree)."""
         from ._solvers import CGSolver, PCGSolver
         self.problem = problem
         self.dir = torch.zeros_like(problem.grad)
+        self.matfree = solver == "cg_matfree"
+        self._bc = None
+        self._stats = _lib.SolverStats()
         self._solver_cls = PCGSolver if solver == "pcg" else CGSolver
         self.max_iter, self.abs_tol, self.rel_tol = max_iter, abs_tol, rel_tol
         self._A = None
@@ -156,6 +176,23 @@ class NewtonSolver:
     def compute_direction(self, stream=None):
         p = self.problem
         p.grad.mul_(-1)
+        if self.matfree:
+            self.dir.zero_()
+            x = p.opt_var.to(p.dtype).contiguous()
+            o = _lib.SolverOpts(int(self.max_iter), float(self.abs_tol), float(self.rel_tol), 0)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            st = self._L().rxg_arap_cg_matfree(p.rx._h, _DT[p.dtype], _p(x), _p(p.rest),
+                                              1 if p.project_hessian else 0, _p(self._bc),
+                                              _p(p.grad), _p(self.dir), ctypes.byref(o),
+                                              ctypes.byref(self._stats), _stream(stream))
+            b.record()
+            b.synchronize()
+            if st not in (0, 6):
+                check(st)
+            self.solve_time += a.elapsed_time(b)
+            return
         self._A = p.hess.to_csr(out=self._A, stream=stream)
         self.solver = self._solver_cls(self._A, 1, self.max_iter, self.abs_tol, self.rel_tol)
         self.dir.zero_()
@@ -191,7 +228,21 @@ class NewtonSolver:
         return False
 
     def apply_bc(self, bc, stream=None):
+        if self.matfree:
+            # no assembled Hessian: the matrix-free products apply the
+            # constraint; the gradient rows are zeroed here
+            self._bc = bc.to(torch.int8).contiguous()
+            keep = (self._bc == 0).to(self.problem.grad.dtype).unsqueeze(1)
+            self.problem.grad.mul_(keep)
+            return
         self.problem.hess.apply_bc(bc, self.problem.grad, stream)
+
+    def iter_taken(self):
+        return self._stats.iters if self.matfree else self.solver.iter_taken()
+
+    @staticmethod
+    def _L():
+        return _lib.load()
 
 
 def mcf_step_backward(rx, x_in, x_out, g_out, dt, tol=1e-12, max_iter=20000, stream=None):

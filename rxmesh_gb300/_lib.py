@@ -92,6 +92,8 @@ SIGNATURES = {
     "rxg_arap_eval_ex": [P, I32, P, P, I32, P, P, P, P, P],
     "rxg_bcsr_to_csr": [P, P, P],
     "rxg_bcsr_apply_bc": [P, P, P, P],
+    "rxg_arap_hvp": [P, I32, P, P, I32, P, P, P, P],
+    "rxg_arap_cg_matfree": [P, I32, P, P, I32, P, P, P, P, P, P],
 }
 _RESTYPE = {"rxg_status_string": ctypes.c_char_p, "rxg_last_error": ctypes.c_char_p,
             "rxg_mesh_destroy": None, "rxg_batch_destroy": None}

@@ -22,6 +22,7 @@
 #include <type_traits>
 
 #include "rxg_device.cuh"
+#include "rxg_gridsum.cuh"
 #include "rxg_lazy.h"
 
 namespace rxg {
@@ -716,6 +717,186 @@ __global__ void __launch_bounds__(128) k_arap_gather_proj(
 }
 
 // ---------------------------------------------------------------------
+// Hessian-free products and CG (the reference's eval_matvec and
+// CGMatFreeSolver, diff/diff_query_kernel.cuh:26-148 and
+// matrix/cg_mat_free_solver.h): y = H(x) v from the face records of x, no
+// assembled Hessian.  bc (may be null): constrained vertices get identity
+// rows and zero columns, as apply_bc does to an assembled Hessian.
+// ---------------------------------------------------------------------
+
+template <typename T>
+struct MatFreeArgs
+{
+    int64_t        nv;
+    const int32_t* ring_off;
+    const int32_t* ring_face;
+    const int8_t*  bnd;
+    const int32_t* fv;
+    const T*       rec;  // k_arap_face<T, true> records, or projected ones
+    const int8_t*  bc;
+    const T*       B;
+    T*             X;
+    T*             R;
+    T*             P;
+    T*             S;
+    double*        part;   // 2 * gridDim
+    unsigned*      bar;    // 4
+    double*        dstat;  // start, final
+    int*           istat;  // iters, converged
+    int            max_iter;
+    double         abs_tol, rel_tol;
+    int*           err;
+};
+
+// y = row p of H src (3 values)
+template <typename T, bool PROJ>
+__device__ __forceinline__ void hvp_row(const MatFreeArgs<T>& a, int64_t p, const T* src, T y[3])
+{
+    y[0] = y[1] = y[2] = T(0);
+    if (a.bc && a.bc[p]) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) y[c] = src[3 * p + c];
+        return;
+    }
+    const int32_t ro = a.ring_off[p];
+    const int32_t k  = a.ring_off[p + 1] - ro;
+    const int32_t nf = a.bnd[p] ? k - 1 : k;
+    for (int32_t i = 0; i < nf; ++i) {
+        const int32_t f    = a.ring_face[ro + i];
+        const int32_t v[3] = {__ldg(a.fv + 3 * (int64_t)f), __ldg(a.fv + 3 * (int64_t)f + 1),
+                              __ldg(a.fv + 3 * (int64_t)f + 2)};
+        const int     lp   = local_index(v, (int32_t)p);
+        FaceDeriv<T>  o;
+        if (!PROJ) load_record<T, true>(a.rec, f, o);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            if (q != lp && a.bc && a.bc[v[q]]) continue;
+            T b[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            if (PROJ) proj_block(a.rec + (int64_t)kProjRec * f, lp, q, b);
+            else block_of(o, lp, q, b);
+            const T* sv = src + 3 * (int64_t)v[q];
+            const T  s0 = sv[0], s1 = sv[1], s2 = sv[2];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) y[r] += b[3 * r] * s0 + b[3 * r + 1] * s1 + b[3 * r + 2] * s2;
+        }
+    }
+}
+
+template <typename T, bool PROJ>
+__global__ void __launch_bounds__(128) k_arap_hvp(MatFreeArgs<T> a, const T* __restrict__ v,
+                                                  T* __restrict__ y)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < a.nv;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        T r[3];
+        hvp_row<T, PROJ>(a, p, v, r);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) y[3 * p + c] = r[c];
+    }
+}
+
+template <int BT, typename Post>
+__device__ __forceinline__ bool mf_sum(float v, double*, GridSum& g, RedSmem& r, Post post)
+{
+    return grid_sum<BT>(v, g, r, post);
+}
+template <int BT, typename Post>
+__device__ __forceinline__ bool mf_sum(double v, double* s_part, GridSum& g, RedSmem& r, Post post)
+{
+    return grid_sum_staged<BT>(v, s_part, g, r, post);
+}
+
+// Plain CG on H(x) X = B (one cooperative launch, rows = vertices, three
+// values per row): the recurrence of the generic solver, S = H r + beta S
+// carrying H p, two grid sums per iteration; stops when r.r has fallen
+// below abs_tol or by rel_tol from its start, or after max_iter iterations.
+template <typename T, bool PROJ, int BT>
+__global__ void __launch_bounds__(BT) k_cg_matfree(MatFreeArgs<T> a)
+{
+    __shared__ RedSmem red;
+    __shared__ double  s_part[sizeof(T) == 8 ? BT : 1];
+    __shared__ double  s_delta0, s_delta;
+    __shared__ T       s_al, s_bt;
+    __shared__ int     s_first, s_done, s_it, s_conv;
+    const int64_t chunk = (a.nv + gridDim.x - 1) / gridDim.x;
+    const int64_t r0    = blockIdx.x * chunk;
+    const int64_t r1    = min(a.nv, r0 + chunk);
+    GridSum       g{a.bar, a.part, a.err, gridDim.x, 0u, blockIdx.x};
+    auto          conv = [&](double d) { return d < a.abs_tol || d / s_delta0 < a.rel_tol; };
+
+    T tp = T(0);
+    for (int64_t p = r0 + threadIdx.x; p < r1; p += BT) {
+        T y[3];
+        hvp_row<T, PROJ>(a, p, a.X, y);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const T r        = a.B[3 * p + c] - y[c];
+            a.R[3 * p + c]   = r;
+            tp += r * r;
+        }
+    }
+    if (!mf_sum<BT>(tp, s_part, g, red, [&](double t) {
+            s_delta0 = s_delta = t;
+            s_it               = 0;
+            s_conv             = conv(t);
+            s_bt               = T(0);
+            s_first            = 1;
+            s_done             = s_conv || a.max_iter <= 0;
+        }))
+        return;
+    while (!s_done) {
+        const T    bt    = s_bt;
+        const bool first = s_first != 0;
+        tp               = T(0);
+        for (int64_t p = r0 + threadIdx.x; p < r1; p += BT) {
+            T y[3];
+            hvp_row<T, PROJ>(a, p, a.R, y);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const T si     = first ? y[c] : y[c] + bt * a.S[3 * p + c];
+                const T pi     = first ? a.R[3 * p + c] : a.R[3 * p + c] + bt * a.P[3 * p + c];
+                a.P[3 * p + c] = pi;
+                a.S[3 * p + c] = si;
+                tp += si * pi;
+            }
+        }
+        if (!mf_sum<BT>(tp, s_part, g, red, [&](double sp) { s_al = (T)(s_delta / sp); })) return;
+        const T al = s_al;
+        tp         = T(0);
+        for (int64_t p = r0 + threadIdx.x; p < r1; p += BT) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                a.X[3 * p + c] += al * a.P[3 * p + c];
+                const T r       = a.R[3 * p + c] - al * a.S[3 * p + c];
+                a.R[3 * p + c]  = r;
+                tp += r * r;
+            }
+        }
+        if (!mf_sum<BT>(tp, s_part, g, red, [&](double dn) {
+                if (conv(dn)) {
+                    s_delta = dn;
+                    s_conv  = 1;
+                    s_done  = 1;
+                    return;
+                }
+                const double beta = dn / s_delta;
+                s_delta           = dn;
+                ++s_it;
+                s_bt    = (T)beta;
+                s_first = 0;
+                s_done  = s_it >= a.max_iter;
+            }))
+            return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.dstat[0] = s_delta0;
+        a.dstat[1] = s_delta;
+        a.istat[0] = s_it;
+        a.istat[1] = s_conv;
+    }
+}
+
+// ---------------------------------------------------------------------
 // Block-CSR helpers of the Newton step (diff/newton_solver.h)
 // ---------------------------------------------------------------------
 
@@ -928,6 +1109,187 @@ rxg_status rxg_arap_eval_ex(const rxg_mesh* h, int32_t dtype, const void* x, con
     cudaFreeAsync(part, s);
     if (e != cudaSuccess) return cuda_status(e, "rxg_arap_eval");
     return RXG_OK;
+}
+
+}  // extern "C"
+
+namespace rxg {
+
+// Shared set-up of the matrix-free entry points: checks, the ring, and the
+// face records of x (projected ones with RXG_ARAP_PROJECT_HESSIAN).
+struct MatFree
+{
+    Lazy*   z    = nullptr;
+    void*   rec  = nullptr;
+    double* part = nullptr;
+    cudaStream_t s = nullptr;
+    ~MatFree()
+    {
+        if (rec) cudaFreeAsync(rec, s);
+        if (part) cudaFreeAsync(part, s);
+    }
+};
+
+static rxg_status matfree_setup(const rxg_mesh* h, int32_t dtype, const void* x, const void* rest,
+                                int32_t flags, cudaStream_t s, MatFree& mf, const char* who)
+{
+    if (!h || !x || !rest || (dtype != RXG_F32 && dtype != RXG_F64)) {
+        set_error("%s: bad argument", who);
+        return RXG_ERR_INVALID;
+    }
+    if (!is_device_ptr(x) || !is_device_ptr(rest)) {
+        set_error("%s: x and rest must be device arrays", who);
+        return RXG_ERR_INVALID;
+    }
+    mf.s          = s;
+    rxg_status st = ensure_pattern(&h->m, s, &mf.z);
+    if (st) return st;
+    const Mesh&   M    = h->m;
+    const int64_t nf   = M.nf;
+    const bool    proj = (flags & RXG_ARAP_PROJECT_HESSIAN) != 0;
+    const size_t  ts   = dtype == RXG_F64 ? 8 : 4;
+    const int     GF   = std::min<int>(grid_for_items(nf) * 2, 152 * 16);
+    RXG_CUDA_TRY(scratch_alloc((void**)&mf.part, sizeof(double) * (GF + 1), s));
+    RXG_CUDA_TRY(scratch_alloc(&mf.rec, (size_t)nf * (proj ? kProjRec : rec_words<true>()) * ts, s));
+    auto run = [&](auto tag) {
+        using T = decltype(tag);
+        if (proj)
+            k_arap_face_proj<T><<<GF, 128, 0, s>>>(nf, M.d.fv_lin, (const T*)x, (const T*)rest,
+                                                  (T*)mf.rec, nullptr, mf.part);
+        else
+            k_arap_face<T, true><<<GF, 128, 0, s>>>(nf, M.d.fv_lin, (const T*)x, (const T*)rest,
+                                                    (T*)mf.rec, nullptr, mf.part);
+    };
+    if (dtype == RXG_F64) run(double{});
+    else run(float{});
+    RXG_CUDA_TRY(cudaGetLastError());
+    return RXG_OK;
+}
+
+template <typename T>
+static MatFreeArgs<T> matfree_args(const rxg_mesh* h, const MatFree& mf, const int8_t* bc)
+{
+    MatFreeArgs<T> a{};
+    a.nv        = h->m.nv;
+    a.ring_off  = mf.z->ring_off;
+    a.ring_face = mf.z->ring_face;
+    a.bnd       = mf.z->bnd;
+    a.fv        = h->m.d.fv_lin;
+    a.rec       = (const T*)mf.rec;
+    a.bc        = bc;
+    a.err       = device_error_word();
+    return a;
+}
+
+template <typename T, bool PROJ>
+static rxg_status cg_matfree_launch(MatFreeArgs<T> a, const rxg_solver_opts& o,
+                                    rxg_solver_stats* st, cudaStream_t s)
+{
+    constexpr int BT   = 256;
+    auto          kern = k_cg_matfree<T, PROJ, BT>;
+    int           per  = 0;
+    RXG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, BT, 0));
+    int dev = 0, sms = 0;
+    RXG_CUDA_TRY(cudaGetDevice(&dev));
+    RXG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t G = std::max<int64_t>(
+        1, std::min<int64_t>((int64_t)sms * std::max(1, std::min(per, 4)), (a.nv + 31) / 32));
+    const size_t vb    = ((sizeof(T) * 3 * (size_t)a.nv) + 255) & ~size_t(255);
+    const size_t bytes = 3 * vb + ((sizeof(double) * 2 * G + 255) & ~size_t(255)) + 3 * 256;
+    uint8_t*     q     = nullptr;
+    RXG_CUDA_TRY(scratch_alloc((void**)&q, bytes, s));
+    uint8_t* base = q;
+    a.R     = (T*)q, q += vb;
+    a.P     = (T*)q, q += vb;
+    a.S     = (T*)q, q += vb;
+    a.part  = (double*)q, q += (sizeof(double) * 2 * G + 255) & ~size_t(255);
+    a.bar   = (unsigned*)q, q += 256;
+    a.dstat = (double*)q, q += 256;
+    a.istat = (int*)q;
+    a.max_iter = o.max_iter;
+    a.abs_tol  = o.abs_tol;
+    a.rel_tol  = o.rel_tol;
+    cudaError_t e = cudaMemsetAsync(a.bar, 0, 16, s);
+    void*       args[] = {&a};
+    if (e == cudaSuccess)
+        e = cudaLaunchCooperativeKernel((const void*)kern, dim3((unsigned)G), dim3(BT), args, 0, s);
+    double ds[2] = {0, 0};
+    int    is[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ds, a.dstat, sizeof(ds), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(is, a.istat, sizeof(is), cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(base, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e, "rxg_arap_cg_matfree");
+    rxg_status ce = check_device_error(s);
+    if (ce) return ce;
+    if (st) {
+        st->start_res = ds[0];
+        st->final_res = ds[1];
+        st->iters     = is[0];
+        st->converged = is[1];
+    }
+    return is[1] ? RXG_OK : RXG_ERR_NOT_CONVERGED;
+}
+
+}  // namespace rxg
+
+extern "C" {
+
+rxg_status rxg_arap_hvp(const rxg_mesh* h, int32_t dtype, const void* x, const void* rest,
+                        int32_t flags, const int8_t* bc, const void* v, void* y, void* stream)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!v || !y || !is_device_ptr(v) || !is_device_ptr(y) || (bc && !is_device_ptr(bc))) {
+        set_error("rxg_arap_hvp: v, y (and bc) must be device arrays");
+        return RXG_ERR_INVALID;
+    }
+    MatFree    mf;
+    rxg_status st = matfree_setup(h, dtype, x, rest, flags, s, mf, "rxg_arap_hvp");
+    if (st) return st;
+    const bool proj = (flags & RXG_ARAP_PROJECT_HESSIAN) != 0;
+    const int  g    = grid_for_items(h->m.nv);
+    auto       run  = [&](auto tag) {
+        using T = decltype(tag);
+        auto a  = matfree_args<T>(h, mf, bc);
+        if (proj) k_arap_hvp<T, true><<<g, 128, 0, s>>>(a, (const T*)v, (T*)y);
+        else k_arap_hvp<T, false><<<g, 128, 0, s>>>(a, (const T*)v, (T*)y);
+    };
+    if (dtype == RXG_F64) run(double{});
+    else run(float{});
+    RXG_CUDA_TRY(cudaGetLastError());
+    return RXG_OK;
+}
+
+rxg_status rxg_arap_cg_matfree(const rxg_mesh* h, int32_t dtype, const void* x, const void* rest,
+                               int32_t flags, const int8_t* bc, const void* B, void* X,
+                               const rxg_solver_opts* opts, rxg_solver_stats* stats, void* stream)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!opts || opts->max_iter < 0 || !B || !X || !is_device_ptr(B) || !is_device_ptr(X) ||
+        (bc && !is_device_ptr(bc))) {
+        set_error("rxg_arap_cg_matfree: bad argument (B, X, bc must be device arrays)");
+        return RXG_ERR_INVALID;
+    }
+    if (opts->precond) {
+        set_error("rxg_arap_cg_matfree: the matrix-free CG has no preconditioner (precond = 0)");
+        return RXG_ERR_INVALID;
+    }
+    MatFree    mf;
+    rxg_status st = matfree_setup(h, dtype, x, rest, flags, s, mf, "rxg_arap_cg_matfree");
+    if (st) return st;
+    const bool proj = (flags & RXG_ARAP_PROJECT_HESSIAN) != 0;
+    if (dtype == RXG_F64) {
+        auto a = matfree_args<double>(h, mf, bc);
+        a.B    = (const double*)B;
+        a.X    = (double*)X;
+        return proj ? cg_matfree_launch<double, true>(a, *opts, stats, s)
+                    : cg_matfree_launch<double, false>(a, *opts, stats, s);
+    }
+    auto a = matfree_args<float>(h, mf, bc);
+    a.B    = (const float*)B;
+    a.X    = (float*)X;
+    return proj ? cg_matfree_launch<float, true>(a, *opts, stats, s)
+                : cg_matfree_launch<float, false>(a, *opts, stats, s);
 }
 
 rxg_status rxg_bcsr_to_csr(const rxg_bcsr* H, rxg_csr* out, void* stream)
