@@ -740,7 +740,7 @@ template <int BT>
 static rxg_status launch_normals_bt(const Mesh* m, int weighting, const float* xyz, float* out,
                                     cudaStream_t s, PatchRange r)
 {
-    // kind 6: Max weights, 5: area weights (the same shared-memory layout)
+    // Max or area weights: the same shared-memory layout (table kinds kNormalMax / kNormalArea)
     const size_t    smem = query_smem_bytes(m, weighting == RXG_NORMAL_MAX ? kNormalMax : kNormalArea);
     int*            err  = device_error_word();
     const PatchHdr* hd   = m->d.hdr;

@@ -42,6 +42,26 @@ def test_invalid_arguments_return_status():
     assert L.rxg_status_string(6) == b"RXG_ERR_NOT_CONVERGED"
 
 
+def test_newton_and_matfree_entry_points_reject_bad_arguments():
+    """The Newton-step helpers and the matrix-free solver return
+    RXG_ERR_INVALID with a message, without touching a GPU, on NULL or host
+    arguments and on a requested preconditioner."""
+    import ctypes
+    from rxmesh_gb300 import RXMeshStatic, _lib
+    L = _lib.load()
+    assert L.rxg_bcsr_to_csr(None, None, None) == 1
+    assert b"rxg_bcsr_to_csr" in L.rxg_last_error()
+    assert L.rxg_bcsr_apply_bc(None, None, None, None) == 1
+    _, f = meshgen.icosphere(1)
+    rx = RXMeshStatic(f, int(np.max(f)) + 1, patch_size=64, host_only=True)
+    x = np.zeros((rx.get_num_vertices(), 3))
+    o = _lib.SolverOpts(10, 0.0, 1e-12, 1)
+    st = L.rxg_arap_cg_matfree(rx._h, 1, x.ctypes.data, x.ctypes.data, 0, None,
+                               x.ctypes.data, x.ctypes.data, ctypes.byref(o), None, None)
+    assert st == 1 and b"device arrays" in L.rxg_last_error()
+    assert L.rxg_arap_hvp(rx._h, 1, x.ctypes.data, x.ctypes.data, 0, None, None, None, None) == 1
+
+
 def decode(rx):
     """Per-patch decoding of the arena into linear-id queries (CPU)."""
     hdr, arena = rx.patches()
