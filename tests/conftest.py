@@ -54,3 +54,22 @@ def kat_system(oracle, name):
     B = val_[:, None] * np.array([7.4, 2.6, 10.3])
     X0 = g["xyz"] * val_[:, None]
     return rp, col, val, B, X0
+
+
+def edge_case_meshes():
+    """Small meshes on the edge cases of the mesh build: vertices in no face
+    (face-less patches), an edge with three faces (not edge-manifold), and two
+    disconnected components.  name -> (xyz (nv,3), fv (nf,3))."""
+    from rxmesh_gb300 import meshgen
+    out = {}
+    v, f = meshgen.icosphere(2)
+    out["isolated"] = (np.concatenate([v, np.random.default_rng(0).normal(size=(5, 3))]), f)
+    x, g = meshgen.plane(8, 8)
+    a, b = int(g[20][0]), int(g[20][1])          # an interior edge of the grid
+    x = np.concatenate([x, [[0.5, 0.5, 1.0]]])
+    out["nonmanifold"] = (x, np.concatenate([g, [[a, b, len(x) - 1]]]).astype(np.int32))
+    v1, f1 = meshgen.icosphere(1)
+    v2, f2 = meshgen.icosphere(2)
+    out["components"] = (np.concatenate([v1, v2 + 3.0]),
+                         np.concatenate([f1, f2 + len(v1)]).astype(np.int32))
+    return out

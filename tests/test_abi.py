@@ -8,7 +8,7 @@ import re
 import numpy as np
 import pytest
 
-from conftest import ROOT, golden, sorted_rows
+from conftest import ROOT, edge_case_meshes, golden, sorted_rows
 from rxmesh_gb300 import meshgen
 
 
@@ -120,6 +120,9 @@ MESHES = {
     "icosphere": lambda: meshgen.icosphere(3)[::-1],
     "plane": lambda: meshgen.plane(13, 9)[::-1],
     "bunnyhead": lambda: (golden("bunnyhead")["fv"], golden("bunnyhead")["xyz"]),
+    "isolated": lambda: edge_case_meshes()["isolated"][::-1],
+    "nonmanifold": lambda: edge_case_meshes()["nonmanifold"][::-1],
+    "components": lambda: edge_case_meshes()["components"][::-1],
 }
 
 
@@ -170,8 +173,9 @@ def test_patch_layout_encodes_exact_queries(oracle, name, patch):
     assert got_f == sorted_rows(off, val)
     _, fe_ref = oracle.edges(fv)
     assert np.array_equal(el[feq][np.argsort(fl)], fe_ref)          # FE in face-edge order
-    d = np.where(evd >= 0, vl[np.maximum(evd, 0)], -1)[np.argsort(el)]
-    assert np.array_equal(d, oracle.ev_diamond(fv))
+    if rx.info["is_edge_manifold"]:  # EVDiamond is defined on edge-manifold meshes
+        d = np.where(evd >= 0, vl[np.maximum(evd, 0)], -1)[np.argsort(el)]
+        assert np.array_equal(d, oracle.ev_diamond(fv))
 
 
 def test_ev_diamond_needs_consistent_orientation():

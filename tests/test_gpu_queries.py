@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import golden, sorted_rows
+from conftest import edge_case_meshes, golden, sorted_rows
 from rxmesh_gb300 import meshgen
 
 pytestmark = pytest.mark.gpu
@@ -19,6 +19,9 @@ MESHES = {
     "cloth": lambda: (golden("cloth")["xyz"], golden("cloth")["fv"]),
     "bunnyhead": lambda: (golden("bunnyhead")["xyz"], golden("bunnyhead")["fv"]),
     "plane_5": lambda: (golden("plane_5")["xyz"], golden("plane_5")["fv"]),
+    "isolated": lambda: edge_case_meshes()["isolated"],
+    "nonmanifold": lambda: edge_case_meshes()["nonmanifold"],
+    "components": lambda: edge_case_meshes()["components"],
 }
 
 
@@ -89,6 +92,12 @@ def test_edge_and_face_queries_bit_exact(oracle, name, patch):
     _, feq = rx.query(Op.FE)
     feq = feq.cpu().numpy().reshape(-1, 3)
     assert np.array_equal(el[feq][np.argsort(fl)], fe)
+    if not rx.info["is_edge_manifold"]:  # EVDiamond is refused, not raced
+        from rxmesh_gb300 import RXGError
+        with pytest.raises(RXGError):
+            rx.query(Op.EVD)
+        device_check()
+        return
     _, dq = rx.query(Op.EVD)
     dq = dq.cpu().numpy().reshape(-1, 4)
     din = np.where(dq >= 0, vl[np.maximum(dq, 0)], -1)[np.argsort(el)]
