@@ -217,6 +217,31 @@ def _cpu_worker(args):
     return tot, b
 
 
+def cpu_model():
+    """The host CPU's model name (x86 /proc/cpuinfo, else lscpu), and the
+    machine type."""
+    import platform
+    import subprocess
+    name = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                name = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    if not name:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            for line in out.splitlines():
+                if line.strip().lower().startswith("model name"):
+                    name = line.split(":", 1)[1].strip()
+                    break
+        except (OSError, subprocess.SubprocessError):
+            pass
+    return "%s (%s)" % (name or "unknown", platform.machine())
+
+
 def run_reference(args):
     """--impl reference: the CPU implementation of the sweep on all host cores."""
     import multiprocessing as mp
@@ -243,6 +268,7 @@ def run_reference(args):
             "impl": "reference",
             "config": {"workload": WORKLOAD},
             "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port",
+                             "cpu": cpu_model(),
                              "sample": "per step: %d processes, each one sweep of a %dx%d torus (the same "
                                        "queries and normals; sweep time only, mesh set-up excluded)" % (cores, n, n)},
             "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -713,6 +739,7 @@ def main():
             b += bb
             reps += 1
         line["cpu_baseline"] = {"value": b / tot / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                                "cpu": cpu_model(),
                                 "sample": "%d sweeps of a 384x384 torus (oracle port, 1 thread)" % reps}
     if rank == 0 and not args.no_mcf:
         line["mcf"] = run_mcf(args, torch)
