@@ -403,6 +403,19 @@ rxg_status rxg_arap_eval_ex(const rxg_mesh* m, int32_t dtype, const void* x,
 rxg_status rxg_bcsr_to_csr(const rxg_bcsr* H, rxg_csr* out, void* stream);
 
 /*
+ * Dense vector operations of DenseMatrix (matrix/dense_matrix.h:284-334,
+ * 446-640) on device arrays of n values of dtype: y = a*x + b*y
+ * (axpy: b = 1; multiply by a scalar: x = NULL, a = 0; copy: b = 0; with
+ * a = 0 or b = 0 that term is dropped, not multiplied), and the dot product
+ * of x and y (FP64 accumulation, deterministic) into *out, a host or device
+ * double (a host *out synchronises the stream).
+ */
+rxg_status rxg_dense_axpby(int64_t n, int32_t dtype, double a, const void* x, double b,
+                           void* y, void* stream);
+rxg_status rxg_dense_dot(int64_t n, int32_t dtype, const void* x, const void* y,
+                         double* out, void* stream);
+
+/*
  * apply_bc of NewtonSolver (diff/newton_solver.h): for every vertex i with
  * bc[i] != 0, block row i gets the identity as its diagonal block and zero
  * off-diagonal blocks, every block (j, i) is zeroed, and row i of grad

@@ -19,6 +19,7 @@
 #include <cuda_runtime_api.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <memory>
 #include <stdexcept>
@@ -173,7 +174,31 @@ class DenseMatrix
     }
     std::vector<T> to_host(cudaStream_t s = nullptr) const { return m_d.to_host(s); }
 
+    // the vector operations of dense_matrix.h (axpy 442, dot 518, norm2 604,
+    // multiply 717, copy_from 1031) over all rows x cols values
+    void axpy(const DenseMatrix<T>& X, T alpha, cudaStream_t s = nullptr)  // this = alpha X + this
+    {
+        check(rxg_dense_axpby(size(), dtype_of<T>::value, (double)alpha, X.data(), 1.0, data(), s));
+    }
+    T dot(const DenseMatrix<T>& x, bool = false, cudaStream_t s = nullptr) const
+    {
+        double r = 0.0;
+        check(rxg_dense_dot(size(), dtype_of<T>::value, data(), x.data(), &r, s));
+        return (T)r;
+    }
+    T    norm2(cudaStream_t s = nullptr) const { return (T)std::sqrt((double)dot(*this, false, s)); }
+    void multiply(T scalar, cudaStream_t s = nullptr)
+    {
+        check(rxg_dense_axpby(size(), dtype_of<T>::value, 0.0, nullptr, (double)scalar, data(), s));
+    }
+    void copy_from(const DenseMatrix<T>& source, locationT = DEVICE, locationT = DEVICE,
+                   cudaStream_t s = nullptr)
+    {
+        check(rxg_dense_axpby(size(), dtype_of<T>::value, 1.0, source.data(), 0.0, data(), s));
+    }
+
    private:
+    int64_t        size() const { return m_rows * m_cols; }
     int64_t        m_rows = 0, m_cols = 0;
     DeviceArray<T> m_d;
 };
@@ -320,6 +345,11 @@ class SparseMatrix
         m_val.fill_zero();
         check_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
     }
+    // an n x n CSR with room for nnz entries (filled by the caller, e.g.
+    // BlockSparseMatrix::to_csr)
+    SparseMatrix(int64_t n, int64_t nnz) : m_n(n), m_row_ptr((size_t)n + 1), m_col((size_t)nnz), m_val((size_t)nnz)
+    {
+    }
     int64_t rows() const { return m_n; }
     int64_t cols() const { return m_n; }
     int64_t non_zeros() const { return (int64_t)m_col.size(); }
@@ -460,6 +490,19 @@ class BlockSparseMatrix
     }
     int64_t               rows() const { return m_n; }
     int64_t               non_zero_blocks() const { return (int64_t)m_col.size(); }
+    // the scalar 3n x 3n form the CG/PCG solvers take (out: 3n rows, 9 nnzb)
+    void to_csr(SparseMatrix<T>& out, cudaStream_t s = nullptr)
+    {
+        rxg_bcsr b = bcsr();
+        rxg_csr  c = out.csr();
+        check(rxg_bcsr_to_csr(&b, &c, s));
+    }
+    // NewtonSolver::apply_bc on this Hessian and the gradient (bc: n int8, device)
+    void apply_bc(const int8_t* bc, DenseMatrix<T>* grad, cudaStream_t s = nullptr)
+    {
+        rxg_bcsr b = bcsr();
+        check(rxg_bcsr_apply_bc(&b, bc, grad ? grad->data() : nullptr, s));
+    }
     DeviceArray<int32_t>& row_ptr() { return m_row_ptr; }
     DeviceArray<int32_t>& col_idx() { return m_col; }
     DeviceArray<T>&       values() { return m_val; }
@@ -504,6 +547,34 @@ class DiffScalarProblem
                                m_project ? RXG_ARAP_PROJECT_HESSIAN : 0, &m_loss,
                                face_energy.data(), grad.data(), hess ? &b : nullptr, s));
     }
+    // energy alone (eval_terms_passive): gradient and Hessian untouched
+    T eval_terms_passive(const DenseMatrix<T>& x, cudaStream_t s = nullptr)
+    {
+        if (!m_rest.size()) throw Error(RXG_ERR_INVALID, "add_arap_term() first");
+        check(rxg_arap_eval_ex(m_rx->handle(), dtype_of<T>::value, x.data(), m_rest.data(), 0,
+                               &m_loss, nullptr, nullptr, nullptr, s));
+        return (T)m_loss;
+    }
+    // y = H(x) v without an assembled Hessian (eval_matvec); bc may be null
+    void eval_matvec(const DenseMatrix<T>& x, const DenseMatrix<T>& v, DenseMatrix<T>& y,
+                     const int8_t* bc = nullptr, cudaStream_t s = nullptr)
+    {
+        check(rxg_arap_hvp(m_rx->handle(), dtype_of<T>::value, x.data(), m_rest.data(),
+                           m_project ? RXG_ARAP_PROJECT_HESSIAN : 0, bc, v.data(), y.data(), s));
+    }
+    // matrix-free CG on H(x) X = B (CGMatFreeSolver); returns the statistics
+    rxg_solver_stats solve_matfree(const DenseMatrix<T>& x, const int8_t* bc,
+                                   const DenseMatrix<T>& B, DenseMatrix<T>& X, int max_iter,
+                                   double abs_tol, double rel_tol, cudaStream_t s = nullptr)
+    {
+        rxg_solver_opts  o{max_iter, abs_tol, rel_tol, 0};
+        rxg_solver_stats st{};
+        rxg_status r = rxg_arap_cg_matfree(m_rx->handle(), dtype_of<T>::value, x.data(),
+                                           m_rest.data(), m_project ? RXG_ARAP_PROJECT_HESSIAN : 0,
+                                           bc, B.data(), X.data(), &o, &st, s);
+        if (r != RXG_ERR_NOT_CONVERGED) check(r);
+        return st;
+    }
     T get_current_loss() const { return (T)m_loss; }
 
     DenseMatrix<T>                        grad;
@@ -515,6 +586,91 @@ class DiffScalarProblem
     DeviceArray<T>      m_rest;
     double              m_loss    = 0.0;
     bool                m_project = false;
+};
+
+// NewtonSolver (diff/newton_solver.h:17-330) on a DiffScalarProblem and its
+// optimisation variable x (linear-order positions, updated in place by
+// line_search): compute_direction() solves H dir = -grad with PCG (or CG) on
+// the scalar Hessian, or with the matrix-free CG; line_search() backtracks
+// with the Armijo test of diff/armijo_condition.h.  As in the reference,
+// compute_direction leaves grad negated and the Armijo test uses dir . grad.
+template <typename T>
+class NewtonSolver
+{
+   public:
+    enum Kind { PCG, CG, CG_MATFREE };
+    NewtonSolver(DiffScalarProblem<T>& p, DenseMatrix<T>& x, Kind kind = PCG, int max_iter = 1000,
+                 T abs_tol = T(0), T rel_tol = T(1e-6))
+        : problem(p), opt_var(x), dir(x.rows(), 3), m_tmp(x.rows(), 3), m_kind(kind),
+          m_max_iter(max_iter), m_abs_tol(abs_tol), m_rel_tol(rel_tol)
+    {
+        if (kind != CG_MATFREE && !p.hess) throw Error(RXG_ERR_INVALID, "the problem has no Hessian");
+    }
+    void apply_bc(const DeviceArray<int8_t>& bc, cudaStream_t s = nullptr)
+    {
+        m_bc = bc.data();
+        if (m_kind == CG_MATFREE) {
+            std::vector<int8_t> hb(bc.size());
+            check_cuda(cudaMemcpy(hb.data(), bc.data(), hb.size(), cudaMemcpyDeviceToHost), "cudaMemcpy");
+            std::vector<T> g = problem.grad.to_host(s);
+            for (size_t i = 0; i < hb.size(); ++i)
+                if (hb[i]) g[3 * i] = g[3 * i + 1] = g[3 * i + 2] = T(0);
+            problem.grad.from_host(g, s);
+        } else {
+            problem.hess->apply_bc(bc.data(), &problem.grad, s);
+        }
+    }
+    void compute_direction(cudaStream_t s = nullptr)
+    {
+        problem.grad.multiply(T(-1), s);
+        dir.reset(T(0), DEVICE, s);
+        if (m_kind == CG_MATFREE) {
+            m_stats = problem.solve_matfree(opt_var, m_bc, problem.grad, dir, m_max_iter,
+                                            (double)m_abs_tol, (double)m_rel_tol, s);
+            return;
+        }
+        if (!m_A)
+            m_A.reset(new SparseMatrix<T>(3 * problem.hess->rows(), 9 * problem.hess->non_zero_blocks()));
+        problem.hess->to_csr(*m_A, s);
+        rxg_solver_opts o{m_max_iter, (double)m_abs_tol, (double)m_rel_tol, m_kind == PCG ? 1 : 0};
+        rxg_csr         c = m_A->csr();
+        rxg_status      r = rxg_cg_solve(&c, 1, problem.grad.data(), dir.data(), &o, &m_stats, s);
+        if (r != RXG_ERR_NOT_CONVERGED) check(r);
+    }
+    bool line_search(T s_max = T(1), T shrink = T(0.8), int max_iters = 64, T armijo_const = T(1e-4),
+                     cudaStream_t s = nullptr)
+    {
+        const bool try_one = s_max > T(1);
+        T          step    = s_max;
+        const T    f       = problem.get_current_loss();
+        const T    slope   = dir.dot(problem.grad, false, s);
+        for (int i = 0; i < max_iters; ++i) {
+            m_tmp.copy_from(opt_var, DEVICE, DEVICE, s);
+            m_tmp.axpy(dir, step, s);
+            const T f_new = problem.eval_terms_passive(m_tmp, s);
+            if (f_new <= f + armijo_const * step * slope) {
+                opt_var.copy_from(m_tmp, DEVICE, DEVICE, s);
+                return true;
+            }
+            if (try_one && step > T(1) && step * shrink < T(1)) step = T(1);
+            else step *= shrink;
+        }
+        return false;
+    }
+    int iter_taken() const { return m_stats.iters; }
+
+    DiffScalarProblem<T>& problem;
+    DenseMatrix<T>&       opt_var;
+    DenseMatrix<T>        dir;
+
+   private:
+    DenseMatrix<T>                   m_tmp;
+    Kind                             m_kind;
+    int                              m_max_iter;
+    T                                m_abs_tol, m_rel_tol;
+    const int8_t*                    m_bc = nullptr;
+    std::unique_ptr<SparseMatrix<T>> m_A;
+    rxg_solver_stats                 m_stats{};
 };
 
 // Many meshes of uneven size, mixed-precision implicit MCF in one persistent

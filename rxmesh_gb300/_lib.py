@@ -91,6 +91,8 @@ SIGNATURES = {
     "rxg_arap_eval": [P, I32, P, P, P, P, P, P, P],
     "rxg_arap_eval_ex": [P, I32, P, P, I32, P, P, P, P, P],
     "rxg_bcsr_to_csr": [P, P, P],
+    "rxg_dense_axpby": [I64, I32, ctypes.c_double, P, ctypes.c_double, P, P],
+    "rxg_dense_dot": [I64, I32, P, P, P, P],
     "rxg_bcsr_apply_bc": [P, P, P, P],
     "rxg_arap_hvp": [P, I32, P, P, I32, P, P, P, P],
     "rxg_arap_cg_matfree": [P, I32, P, P, I32, P, P, P, P, P, P],

@@ -192,6 +192,83 @@ static int gpu_checks()
     REQUIRE(prob.get_current_loss() > 1e-3);
     REQUIRE(prob.hess && prob.hess->non_zero_blocks() > 0);
 
+    // DenseMatrix vector operations against the same arithmetic on the host
+    {
+        const int64_t       n = gr.get_num_vertices();
+        std::vector<double> ha(3 * n), hb(3 * n);
+        for (int64_t i = 0; i < 3 * n; ++i) {
+            ha[i] = std::sin(0.37 * (double)i);
+            hb[i] = std::cos(0.11 * (double)i) - 0.25;
+        }
+        DenseMatrix<double> a(n, 3), b(n, 3), c(n, 3);
+        a.from_host(ha);
+        b.from_host(hb);
+        double dot = 0, nrm = 0;
+        for (int64_t i = 0; i < 3 * n; ++i) {
+            dot += ha[i] * hb[i];
+            nrm += ha[i] * ha[i];
+        }
+        REQUIRE(std::fabs(a.dot(b) - dot) <= 1e-12 * std::fabs(dot) + 1e-12);
+        REQUIRE(std::fabs(a.norm2() - std::sqrt(nrm)) <= 1e-12 * std::sqrt(nrm));
+        c.copy_from(a);
+        c.multiply(2.5);
+        c.axpy(b, -0.5);
+        const std::vector<double> hc = c.to_host();
+        for (int64_t i = 0; i < 3 * n; ++i) REQUIRE(std::fabs(hc[i] - (2.5 * ha[i] - 0.5 * hb[i])) <= 1e-14);
+        DenseMatrix<float>  fa(n, 3);
+        std::vector<float>  hf(ha.begin(), ha.end());
+        fa.from_host(hf);
+        double fdot = 0;
+        for (float v : hf) fdot += (double)v * (double)v;
+        REQUIRE(std::fabs((double)fa.dot(fa) - fdot) <= 1e-6 * fdot);
+    }
+
+    // Newton with the corners fixed (NewtonSolver): the energy drops, the
+    // corners stay put, and the assembled-PCG and matrix-free paths agree
+    {
+        const int64_t       n = gr.get_num_vertices();
+        const std::vector<int32_t> gl2i = gr.linear_to_input(RXG_ELEM_VERTEX);
+        std::vector<int8_t> hbc((size_t)n, 0);
+        for (int64_t l = 0; l < n; ++l) {
+            const int32_t v = gl2i[(size_t)l];
+            if (v == 0 || v == 23 || v == 24 * 23 || v == 24 * 24 - 1) hbc[(size_t)l] = 1;
+        }
+        DeviceArray<int8_t> bc((size_t)n);
+        bc.upload(hbc.data(), hbc.size());
+        std::vector<double> bent = gr.get_input_vertex_coordinates().to_host();
+        for (int64_t l = 0; l < n; ++l) {
+            const double u = bent[3 * l], w = bent[3 * l + 1];
+            bent[3 * l + 2] = 0.2 * std::sin(3.0 * u) * std::cos(2.0 * w);
+            if (hbc[(size_t)l]) bent[3 * l] *= 1.2;
+        }
+        double last[2] = {0, 0};
+        for (int k = 0; k < 2; ++k) {
+            DiffScalarProblem<double> p(gr, k == 0);
+            p.add_arap_term(gr.get_input_vertex_coordinates(), nullptr, true);
+            DenseMatrix<double> x(n, 3);
+            x.from_host(bent);
+            NewtonSolver<double> newton(p, x, k == 0 ? NewtonSolver<double>::PCG
+                                                     : NewtonSolver<double>::CG_MATFREE,
+                                        5000, 0.0, 1e-24);
+            double first = 0;
+            for (int it = 0; it < 4; ++it) {
+                p.eval_terms(x);
+                if (it == 0) first = p.get_current_loss();
+                newton.apply_bc(bc);
+                newton.compute_direction();
+                REQUIRE(newton.iter_taken() > 0);
+                REQUIRE(newton.line_search());
+            }
+            last[k] = p.get_current_loss();
+            REQUIRE(last[k] < 0.5 * first);
+            const std::vector<double> hx = x.to_host();
+            for (int64_t l = 0; l < n; ++l)
+                if (hbc[(size_t)l])
+                    for (int d = 0; d < 3; ++d) REQUIRE(hx[3 * l + d] == bent[3 * l + d]);
+        }
+        REQUIRE(std::fabs(last[0] - last[1]) <= 1e-8 * std::fabs(last[0]) + 1e-14);
+    }
+
     // batch: two meshes, one launch
     std::vector<int32_t> t1;
     for (const auto& f : fv)
