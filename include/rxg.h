@@ -106,6 +106,41 @@ rxg_status rxg_mesh_create_ex(const int32_t* fv, int64_t nf, int64_t nv,
                               int32_t patch_faces, int32_t flags, rxg_mesh** out);
 
 /*
+ * Build a mesh on a given partition (host arrays, input ids), for
+ * reproducible patches.  face_patch: nf patch ids; every id in [0, np) must
+ * own 1 to 4096 faces.  vertex_patch (nv) and edge_patch (ne, in
+ * rxg_mesh_input_edges order, which is RXMesh's edge numbering) give owners;
+ * each must be the patch of one of the element's faces (entries of vertices
+ * in no face are ignored).  Either may be NULL: the owner is then the lowest
+ * patch among the element's faces (Patcher::assign_patch,
+ * patcher/patcher.cu:719-757).  ne: entries of edge_patch, checked against
+ * the mesh.  flags: RXG_MESH_HOST_ONLY.
+ */
+rxg_status rxg_mesh_create_partitioned(const int32_t* fv, int64_t nf, int64_t nv,
+                                       const int32_t* face_patch, const int32_t* vertex_patch,
+                                       const int32_t* edge_patch, int64_t ne, int32_t flags,
+                                       rxg_mesh** out);
+/* The partition of a mesh in input ids (host arrays; any may be NULL):
+ * nf face, nv vertex and ne edge owner patches.  Vertices in no face are in
+ * patches numbered after the face-owning ones. */
+rxg_status rxg_mesh_partition(const rxg_mesh* m, int32_t* face_patch, int32_t* vertex_patch,
+                              int32_t* edge_patch);
+/*
+ * RXMeshStatic(fv, patcher_file) (rxmesh_static.h:61-100; Patcher(filename),
+ * patcher/patcher.cu:25-32): build on the partition in a patcher file that
+ * RXMesh saved (a cereal portable binary archive of Patcher::serialize,
+ * patcher/patcher.h:162-181).  The file must be written for this mesh (its
+ * vertex, face and edge counts are checked).  RXG_ERR_INVALID with a message
+ * for an unreadable, truncated or mismatched file.
+ */
+rxg_status rxg_mesh_create_from_patch_file(const int32_t* fv, int64_t nf, int64_t nv,
+                                           const char* patcher_file, int32_t flags,
+                                           rxg_mesh** out);
+/* RXMesh::save(filename) (rxmesh.h:326-329): write the mesh's partition as a
+ * patcher file that RXMesh and rxg_mesh_create_from_patch_file load. */
+rxg_status rxg_mesh_save_patch_file(const rxg_mesh* m, const char* patcher_file);
+
+/*
  * Patch layout for inspection: hdr receives num_patches records of 16 int32
  * {nVo,nVl,nEo,nEl,nFo,nFl, v_base,e_base,f_base, vv_base,vf_base,
  *  ev_off,fe_off,rv_off,re_off,rf_off}; arena receives *words uint32 words

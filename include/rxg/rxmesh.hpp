@@ -217,15 +217,13 @@ class RXMeshStatic
 {
    public:
     // fv: one {v0, v1, v2} per face, input vertex ids (rxmesh_static.h:87-92).
-    // patcher_file is accepted for signature parity and must be empty: the
-    // partition is always recomputed (a BFS partitioner, deterministic).
+    // patcher_file: a partition saved by RXMesh (or save()) for this mesh;
+    // empty: the library's own partition into patches of patch_size faces.
     explicit RXMeshStatic(std::vector<std::vector<uint32_t>>& fv,
                           const std::string                   patcher_file = "",
                           const uint32_t                      patch_size   = 512,
                           bool                                host_only    = false)
     {
-        if (!patcher_file.empty())
-            throw Error(RXG_ERR_UNSUPPORTED, "patcher files are not supported");
         std::vector<int32_t> flat;
         flat.reserve(3 * fv.size());
         int64_t nv = 0;
@@ -236,11 +234,21 @@ class RXMeshStatic
                 nv = std::max<int64_t>(nv, (int64_t)v + 1);
             }
         }
-        rxg_mesh* m = nullptr;
-        check(rxg_mesh_create_ex(flat.data(), (int64_t)fv.size(), nv, (int32_t)patch_size,
-                                 host_only ? RXG_MESH_HOST_ONLY : 0, &m));
+        rxg_mesh*     m     = nullptr;
+        const int32_t flags = host_only ? RXG_MESH_HOST_ONLY : 0;
+        if (patcher_file.empty())
+            check(rxg_mesh_create_ex(flat.data(), (int64_t)fv.size(), nv, (int32_t)patch_size,
+                                     flags, &m));
+        else
+            check(rxg_mesh_create_from_patch_file(flat.data(), (int64_t)fv.size(), nv,
+                                                  patcher_file.c_str(), flags, &m));
         m_mesh.reset(m);
         check(rxg_mesh_get_info(m, &m_info));
+    }
+    // RXMesh::save (rxmesh.h:326-329): the partition as a patcher file
+    void save(const std::string& filename) const
+    {
+        check(rxg_mesh_save_patch_file(m_mesh.get(), filename.c_str()));
     }
     RXMeshStatic(const RXMeshStatic&)            = delete;
     RXMeshStatic& operator=(const RXMeshStatic&) = delete;

@@ -6,6 +6,7 @@ PCGSolver (matrix/cg_solver.h, pcg_solver.h).  All compute goes through the C
 ABI of librxg.so (include/rxg.h); device memory and streams come from torch.
 """
 import ctypes
+import os
 
 import numpy as np
 import torch
@@ -52,16 +53,36 @@ class RXMeshStatic:
 
     fv: (nf, 3) int array of input vertex ids.  patch_size: faces per patch.
     The patch topology lives on the current CUDA device unless host_only.
+    patcher_file: a partition that RXMesh (or save()) wrote; face_patch
+    (nf,), with optional vertex_patch (nv,) and edge_patch (ne,) owners: a
+    partition given as arrays (rxg_mesh_create_partitioned).  Either replaces
+    the library's own partition and patch_size.
     """
 
-    def __init__(self, fv, num_vertices=None, patch_size=512, host_only=False):
+    def __init__(self, fv, num_vertices=None, patch_size=512, host_only=False,
+                 patcher_file=None, face_patch=None, vertex_patch=None, edge_patch=None):
         L = _lib.load()
         f = np.ascontiguousarray(fv, dtype=np.int32).reshape(-1, 3)
         nv = int(f.max()) + 1 if num_vertices is None else int(num_vertices)
         self._fv = f
         h = ctypes.c_void_p()
-        check(L.rxg_mesh_create_ex(f.ctypes.data, f.shape[0], nv, int(patch_size),
-                                   1 if host_only else 0, ctypes.byref(h)))
+        flags = 1 if host_only else 0
+        if patcher_file is not None:
+            check(L.rxg_mesh_create_from_patch_file(f.ctypes.data, f.shape[0], nv,
+                                                    os.fsencode(patcher_file), flags,
+                                                    ctypes.byref(h)))
+        elif face_patch is not None:
+            arr = [None if a is None else np.ascontiguousarray(a, dtype=np.int32).reshape(-1)
+                   for a in (face_patch, vertex_patch, edge_patch)]
+            if len(arr[0]) != f.shape[0] or (arr[1] is not None and len(arr[1]) != nv):
+                raise ValueError("face_patch needs one entry per face, vertex_patch one per vertex")
+            ptr = [None if a is None else a.ctypes.data for a in arr]
+            ne = -1 if arr[2] is None else len(arr[2])
+            check(L.rxg_mesh_create_partitioned(f.ctypes.data, f.shape[0], nv, ptr[0], ptr[1],
+                                                ptr[2], ne, flags, ctypes.byref(h)))
+        else:
+            check(L.rxg_mesh_create_ex(f.ctypes.data, f.shape[0], nv, int(patch_size), flags,
+                                       ctypes.byref(h)))
         self._h = h
         self._L = L
         self.host_only = host_only
@@ -86,6 +107,20 @@ class RXMeshStatic:
 
     def get_num_faces(self):
         return self.info["num_faces"]
+
+    def partition(self):
+        """(face_patch, vertex_patch, edge_patch): the owner patch of every
+        face, vertex and edge in input ids (rxg_mesh_partition)."""
+        fp = np.empty(self.get_num_faces(), np.int32)
+        vp = np.empty(self.get_num_vertices(), np.int32)
+        ep = np.empty(self.get_num_edges(), np.int32)
+        check(self._L.rxg_mesh_partition(self._h, fp.ctypes.data, vp.ctypes.data, ep.ctypes.data))
+        return fp, vp, ep
+
+    def save(self, filename):
+        """RXMesh::save (rxmesh.h:326-329): write the partition as a patcher
+        file that RXMesh and RXMeshStatic(..., patcher_file=) load."""
+        check(self._L.rxg_mesh_save_patch_file(self._h, os.fsencode(filename)))
 
     def get_num_patches(self):
         return self.info["num_patches"]

@@ -51,6 +51,19 @@ struct DeviceTopo
     int32_t* qbase = nullptr;
 };
 
+// An explicit partition in input ids (a saved RXMesh patcher, or the
+// caller's own): face -> patch, and optionally the owner patch of each vertex
+// and edge.  Without owners, a vertex or edge goes to the lowest-numbered
+// patch among its faces' patches (RXMesh's Patcher::assign_patch,
+// patcher/patcher.cu:719-757).
+struct Partition {
+    const int32_t* face   = nullptr;  // nf entries
+    const int32_t* vertex = nullptr;  // nv entries or NULL; ignored for vertices in no face
+    const int32_t* edge   = nullptr;  // ne entries or NULL
+    int64_t        ne     = -1;       // entries of edge
+    int32_t        patch_size = 0;    // the patcher's nominal patch size (0: the largest patch)
+};
+
 struct Mesh
 {
     int64_t nv = 0, ne = 0, nf = 0;
@@ -78,6 +91,10 @@ struct Mesh
     // first EF / FF value of each patch's owned rows (np+1 each; the last
     // entry is the total): the CSR bases of the edge and face queries
     std::vector<int32_t> ef_base, ff_base;
+    // the input faces (for rxg_mesh_save_patch_file), the patches that own
+    // faces (the rest hold vertices in no face), face-connected components
+    std::vector<int32_t> fv_in;
+    int32_t              num_face_patches = 0, num_components = 0;
 
     DeviceTopo d;
 
@@ -114,6 +131,12 @@ bool is_device_ptr(const void* p);
 // Stream-ordered device scratch from the library's own pool (freed with
 // cudaFreeAsync); freed blocks stay in the pool for later calls.
 cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t s);
+
+// Mesh construction behind rxg_mesh_create_ex (part == NULL: the library's
+// own BFS partition into patches of at most patch_faces faces) and the
+// partitioned / patch-file constructors (rxg_mesh.cpp).
+rxg_status create_mesh(const int32_t* fv, int64_t nf, int64_t nv, int32_t patch_faces,
+                       int32_t flags, const Partition* part, rxg_mesh** out);
 
 // Lazily allocated per-mesh device scratch and the oriented ring.
 struct Lazy;

@@ -109,14 +109,21 @@ struct EdgeTable
 
 inline int32_t pad4(int32_t words) { return (words + 3) & ~3; }
 
+int32_t find_root(std::vector<int32_t>& up, int32_t x)
+{
+    while (up[x] != x) x = up[x] = up[up[x]];
+    return x;
+}
+
 }  // namespace
 
 static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv, int32_t P,
-                             bool split_components)
+                             bool split_components, const Partition* part = nullptr)
 {
     M.nf          = nf;
     M.nv          = nv;
     M.patch_faces = P;
+    M.fv_in.assign(fv, fv + 3 * nf);
 
     // ---- edge map ------------------------------------------------------
     EdgeTable            tab((uint64_t)nf * 3);
@@ -177,14 +184,60 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
     }
     for (int64_t v = 0; v < nv; ++v) M.max_valence = std::max<int64_t>(M.max_valence, valence[v]);
 
+    // ---- face-connected components (through shared edges) -------------
+    {
+        std::vector<int32_t> up(nf);
+        for (int64_t f = 0; f < nf; ++f) up[f] = (int32_t)f;
+        for (int64_t e = 0; e < ne; ++e)
+            for (int32_t t = ef_off[e] + 1; t < ef_off[e + 1]; ++t) {
+                const int32_t a = find_root(up, ef_val[ef_off[e]]), b = find_root(up, ef_val[t]);
+                if (a != b) up[std::max(a, b)] = std::min(a, b);
+            }
+        M.num_components = 0;
+        for (int64_t f = 0; f < nf; ++f) M.num_components += find_root(up, (int32_t)f) == f;
+    }
+
     // ---- patch partition: BFS region growing on the face graph ----------
     // (RXMesh uses GPU Lloyd k-means, patcher/patcher.cu:828-1035; the query
     //  engine needs only the <= P faces per patch contract.)
     std::vector<int32_t> fpatch(nf, -1);
-    std::vector<int32_t> queue(nf);
+    std::vector<int32_t> queue(part ? 0 : nf);
     int32_t              np = 0;
     int64_t              seed = 0;
-    while (true) {
+    if (part) {
+        // every patch id in [0, np) owns between 1 and 4096 faces
+        int64_t hi = -1;
+        for (int64_t f = 0; f < nf; ++f) {
+            if (part->face[f] < 0) {
+                set_error("face_patch[%lld] = %d is negative", (long long)f, part->face[f]);
+                return RXG_ERR_INVALID;
+            }
+            hi = std::max<int64_t>(hi, part->face[f]);
+        }
+        if (hi >= nf) {
+            set_error("face_patch names patch %lld, more patches than faces", (long long)hi);
+            return RXG_ERR_INVALID;
+        }
+        np = (int32_t)hi + 1;
+        std::vector<int32_t> cnt(np, 0);
+        for (int64_t f = 0; f < nf; ++f) ++cnt[fpatch[f] = part->face[f]];
+        int32_t largest = 0;
+        for (int32_t p = 0; p < np; ++p) {
+            if (cnt[p] == 0 || cnt[p] > 4096) {
+                set_error("patch %d owns %d faces (every patch in [0, %d) must own 1 to 4096)", p,
+                          cnt[p], np);
+                return RXG_ERR_INVALID;
+            }
+            largest = std::max(largest, cnt[p]);
+        }
+        M.patch_faces = std::max(part->patch_size, largest);
+        if (part->edge && part->ne != ne) {
+            set_error("edge_patch has %lld entries, the mesh has %lld edges",
+                      (long long)part->ne, (long long)ne);
+            return RXG_ERR_INVALID;
+        }
+    }
+    while (!part) {
         while (seed < nf && fpatch[seed] >= 0) ++seed;
         if (seed >= nf) break;
         int32_t p = np++;
@@ -220,11 +273,42 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
         }
     }
     const int32_t nfp = np;  // patches that own faces
+    M.num_face_patches = nfp;
     // isolated vertices (in no face) go to extra face-less patches
     std::vector<int32_t> vpatch(nv, -1), epatch(ne);
-    for (int64_t f = 0; f < nf; ++f)
-        for (int k = 0; k < 3; ++k)
-            if (vpatch[fv[3 * f + k]] < 0) vpatch[fv[3 * f + k]] = fpatch[f];
+    if (!part) {
+        // the patch of the vertex's first face, of the edge's first face
+        for (int64_t f = 0; f < nf; ++f)
+            for (int k = 0; k < 3; ++k)
+                if (vpatch[fv[3 * f + k]] < 0) vpatch[fv[3 * f + k]] = fpatch[f];
+        for (int64_t e = 0; e < ne; ++e) epatch[e] = fpatch[e_first_face[e]];
+    } else {
+        // the given owner, which must be the patch of one of the element's
+        // faces, else the lowest such patch
+        auto owner = [&](const int32_t* given, int64_t i, const std::vector<int32_t>& off,
+                         const std::vector<int32_t>& val, const char* what) -> int32_t {
+            int32_t lo = INT32_MAX;
+            bool    ok = false;
+            for (int32_t t = off[i]; t < off[i + 1]; ++t) {
+                lo = std::min(lo, fpatch[val[t]]);
+                ok |= given && fpatch[val[t]] == given[i];
+            }
+            if (!given) return lo;
+            if (!ok) {
+                set_error("%s_patch[%lld] = %d is not the patch of any of its faces", what,
+                          (long long)i, given[i]);
+                return -1;
+            }
+            return given[i];
+        };
+        for (int64_t v = 0; v < nv; ++v)
+            if (vf_off[v + 1] > vf_off[v] &&
+                (vpatch[v] = owner(part->vertex, v, vf_off, vf_val, "vertex")) < 0)
+                return RXG_ERR_INVALID;
+        for (int64_t e = 0; e < ne; ++e)
+            if ((epatch[e] = owner(part->edge, e, ef_off, ef_val, "edge")) < 0)
+                return RXG_ERR_INVALID;
+    }
     {
         int32_t extra = -1, fill = 0;
         for (int64_t v = 0; v < nv; ++v)
@@ -237,7 +321,6 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
                 ++fill;
             }
     }
-    for (int64_t e = 0; e < ne; ++e) epatch[e] = fpatch[e_first_face[e]];
     M.num_patches = np;
 
     // ---- owned lists (counting sort by patch, input order inside) -------
@@ -551,8 +634,10 @@ rxg_status rxg_mesh_create(const int32_t* fv, int64_t nf, int64_t nv, int32_t pa
     return rxg_mesh_create_ex(fv, nf, nv, patch_faces, 0, out);
 }
 
-rxg_status rxg_mesh_create_ex(const int32_t* fv, int64_t nf, int64_t nv, int32_t patch_faces,
-                              int32_t flags, rxg_mesh** out)
+}  // extern "C"
+
+rxg_status rxg::create_mesh(const int32_t* fv, int64_t nf, int64_t nv, int32_t patch_faces,
+                            int32_t flags, const Partition* part, rxg_mesh** out)
 {
     if (!out) {
         set_error("rxg_mesh_create: out is NULL");
@@ -563,7 +648,7 @@ rxg_status rxg_mesh_create_ex(const int32_t* fv, int64_t nf, int64_t nv, int32_t
         set_error("rxg_mesh_create: need fv != NULL, 0 < nf < 2^31/3, 0 < nv < 2^31");
         return RXG_ERR_INVALID;
     }
-    if (patch_faces < 16 || patch_faces > 4096) {
+    if (!part && (patch_faces < 16 || patch_faces > 4096)) {
         set_error("rxg_mesh_create: patch_faces must be in [16, 4096] (got %d)", patch_faces);
         return RXG_ERR_INVALID;
     }
@@ -586,7 +671,8 @@ rxg_status rxg_mesh_create_ex(const int32_t* fv, int64_t nf, int64_t nv, int32_t
     }
     rxg_status s;
     try {
-        s = build_host(h->m, fv, nf, nv, patch_faces, (flags & RXG_MESH_SPLIT_COMPONENTS) != 0);
+        s = build_host(h->m, fv, nf, nv, patch_faces, (flags & RXG_MESH_SPLIT_COMPONENTS) != 0,
+                       part);
     } catch (const std::bad_alloc&) {
         set_error("rxg_mesh_create: host allocation failed");
         s = RXG_ERR_NOMEM;
@@ -616,6 +702,33 @@ rxg_status rxg_mesh_create_ex(const int32_t* fv, int64_t nf, int64_t nv, int32_t
     // the host copy of the arena stays for rxg_mesh_patches (introspection)
     *out = h;
     return RXG_OK;
+}
+
+extern "C" {
+
+rxg_status rxg_mesh_create_ex(const int32_t* fv, int64_t nf, int64_t nv, int32_t patch_faces,
+                              int32_t flags, rxg_mesh** out)
+{
+    return create_mesh(fv, nf, nv, patch_faces, flags, nullptr, out);
+}
+
+rxg_status rxg_mesh_create_partitioned(const int32_t* fv, int64_t nf, int64_t nv,
+                                       const int32_t* face_patch, const int32_t* vertex_patch,
+                                       const int32_t* edge_patch, int64_t ne, int32_t flags,
+                                       rxg_mesh** out)
+{
+    if (out) *out = nullptr;
+    if (!face_patch || (edge_patch && ne < 0) || (flags & RXG_MESH_SPLIT_COMPONENTS)) {
+        set_error("rxg_mesh_create_partitioned: need face_patch, ne >= 0 with edge_patch, and "
+                  "no RXG_MESH_SPLIT_COMPONENTS");
+        return RXG_ERR_INVALID;
+    }
+    Partition part;
+    part.face   = face_patch;
+    part.vertex = vertex_patch;
+    part.edge   = edge_patch;
+    part.ne     = ne;
+    return create_mesh(fv, nf, nv, 0, flags, &part, out);
 }
 
 void rxg_mesh_destroy(rxg_mesh* h)

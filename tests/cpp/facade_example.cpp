@@ -3,7 +3,8 @@
 // queries, assemble the MCF system, solve it with PCGSolver, take MCF steps,
 // evaluate the ARAP term, and run a small batch.
 //
-//   facade_example host   -- mesh build and numbering only (no GPU needed)
+//   facade_example host [dir] -- mesh build and numbering only (no GPU
+//                                needed); with dir, a patcher-file round trip
 //   facade_example gpu    -- the whole path on the current GPU
 // Prints "OK" and exits 0 when every check passes; prints the failing check
 // and exits 1 otherwise.
@@ -60,7 +61,7 @@ static void grid(int k, std::vector<int32_t>& fv, std::vector<double>& xyz)
         }
 }
 
-static int host_checks()
+static int host_checks(const char* dir)
 {
     std::vector<std::vector<uint32_t>> fv;
     std::vector<std::vector<double>>   xyz;
@@ -82,6 +83,22 @@ static int host_checks()
         threw = e.status == RXG_ERR_INVALID;
     }
     REQUIRE(threw);
+    if (dir) {
+        // save the partition, load it back: the same patches and numbering
+        const std::string path = std::string(dir) + "/torus_patches";
+        rx.save(path);
+        RXMeshStatic back(fv, path, 512, true);
+        REQUIRE(back.get_num_patches() == rx.get_num_patches());
+        REQUIRE(back.linear_to_input(RXG_ELEM_VERTEX) == l2i);
+        REQUIRE(back.linear_to_input(RXG_ELEM_EDGE) == rx.linear_to_input(RXG_ELEM_EDGE));
+        threw = false;
+        try {
+            RXMeshStatic r3(fv, std::string(dir) + "/missing_patches", 512, true);
+        } catch (const Error& e) {
+            threw = e.status == RXG_ERR_INVALID;
+        }
+        REQUIRE(threw);
+    }
     return 0;
 }
 
@@ -292,7 +309,7 @@ int main(int argc, char** argv)
 {
     const bool gpu = argc > 1 && std::strcmp(argv[1], "gpu") == 0;
     try {
-        const int rc = gpu ? gpu_checks() : host_checks();
+        const int rc = gpu ? gpu_checks() : host_checks(argc > 2 ? argv[2] : nullptr);
         if (rc) return rc;
     } catch (const Error& e) {
         std::printf("FAILED: exception %s\n", e.what());

@@ -4,7 +4,9 @@ Reads fixture meshes from the RXMesh tree (input/*.obj) and runs the
 reference's own serial vertex-normal routine (apps/VertexNormal/
 vertex_normal_ref.h, compiled into oracle/_ref by oracle/Makefile) on them.
 Writes <name>.npz with fv (int32), xyz (float64), and the reference normals
-in FP32 and FP64.  Run here, where the reference tree exists:
+in FP32 and FP64; where the tree holds a saved partition of the mesh
+(input/<name>_patches, written by RXMesh's Patcher::save), its raw bytes as
+patcher_file (uint8).  Run here, where the reference tree exists:
 
     python tests/golden/make_golden.py [/path/to/RXMesh [name ...]]
 
@@ -34,7 +36,12 @@ def main(ref_root, names=None):
         n32 = O.ref_vertex_normals(fv, xyz.astype(np.float32), np.float32)
         n64 = O.ref_vertex_normals(fv, xyz, np.float64)
         out = os.path.join(HERE, name + ".npz")
-        np.savez_compressed(out, fv=fv, xyz=xyz, ref_normals_f32=n32, ref_normals_f64=n64)
+        extra = {}
+        patches = os.path.join(ref_root, "input", name + "_patches")
+        if os.path.exists(patches):
+            with open(patches, "rb") as fh:
+                extra["patcher_file"] = np.frombuffer(fh.read(), np.uint8)
+        np.savez_compressed(out, fv=fv, xyz=xyz, ref_normals_f32=n32, ref_normals_f64=n64, **extra)
         print(name, xyz.shape, fv.shape, os.path.getsize(out))
 
 

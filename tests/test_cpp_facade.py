@@ -1,7 +1,8 @@
 """The C++ facade (include/rxg/rxmesh.hpp) compiles against the C ABI and runs.
 
 The example program tests/cpp/facade_example.cpp is built with g++ and linked
-to librxg.so; `host` mode runs here (mesh build, numbering, error path),
+to librxg.so; `host` mode runs here (mesh build, numbering, error path,
+a patcher-file round trip),
 `gpu` mode runs the whole path (queries, MCF assembly + PCGSolver, mcf_step,
 DiffScalarProblem ARAP, MeshBatch) on the GPU.
 """
@@ -39,8 +40,9 @@ def example(tmp_path_factory):
     return exe
 
 
-def test_facade_host(example):
-    r = subprocess.run([example, "host"], capture_output=True, text=True, timeout=120)
+def test_facade_host(example, tmp_path):
+    r = subprocess.run([example, "host", str(tmp_path)], capture_output=True, text=True,
+                       timeout=120)
     assert r.returncode == 0 and r.stdout.strip().endswith("OK"), r.stdout + r.stderr
 
 

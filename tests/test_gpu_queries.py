@@ -25,6 +25,22 @@ MESHES = {
 }
 
 
+# (mesh, patch size); "patcher": the partition RXMesh saved for the mesh
+# (input/<name>_patches, kept in the golden fixture)
+CASES = [(n, p) for n in MESHES for p in (64, 512)] + [("sphere3", "patcher"), ("torus", "patcher")]
+
+
+def make_rx(name, patch, tmp_path):
+    from rxmesh_gb300 import RXMeshStatic
+    if patch == "patcher":
+        g = golden(name)
+        path = tmp_path / (name + "_patches")
+        path.write_bytes(g["patcher_file"].tobytes())
+        return g["xyz"], g["fv"], RXMeshStatic(g["fv"], len(g["xyz"]), patcher_file=str(path))
+    x, f = MESHES[name]()
+    return x, f, RXMeshStatic(f, len(x), patch_size=patch)
+
+
 def gpu_rows(rx, op):
     from rxmesh_gb300 import Op
     vl = rx.linear_to_input("v")
@@ -38,13 +54,11 @@ def gpu_rows(rx, op):
     return rows, off
 
 
-@pytest.mark.parametrize("name", list(MESHES))
-@pytest.mark.parametrize("patch", [64, 512])
-def test_queries_bit_exact(oracle, name, patch):
-    from rxmesh_gb300 import Op, RXMeshStatic, device_check
-    x, f = MESHES[name]()
+@pytest.mark.parametrize("name,patch", CASES)
+def test_queries_bit_exact(oracle, name, patch, tmp_path):
+    from rxmesh_gb300 import Op, device_check
+    x, f, rx = make_rx(name, patch, tmp_path)
     nv = len(x)
-    rx = RXMeshStatic(f, nv, patch_size=patch)
     ev, _ = oracle.edges(f)
     o, v = oracle.vv(nv, ev)
     got, off = gpu_rows(rx, Op.VV)
@@ -64,14 +78,12 @@ def test_queries_bit_exact(oracle, name, patch):
     device_check()
 
 
-@pytest.mark.parametrize("name", list(MESHES))
-@pytest.mark.parametrize("patch", [64, 512])
-def test_edge_and_face_queries_bit_exact(oracle, name, patch):
+@pytest.mark.parametrize("name,patch", CASES)
+def test_edge_and_face_queries_bit_exact(oracle, name, patch, tmp_path):
     """EF, FF (rows as sets), FE and EVDiamond (rows in order) against the
     oracle, in input ids (Op::EF/FE/FF/EVDiamond, kernels/rxmesh_queries.cuh)."""
-    from rxmesh_gb300 import Op, RXMeshStatic, device_check
-    x, f = MESHES[name]()
-    rx = RXMeshStatic(f, len(x), patch_size=patch)
+    from rxmesh_gb300 import Op, device_check
+    x, f, rx = make_rx(name, patch, tmp_path)
     vl, el, fl = rx.linear_to_input("v"), rx.linear_to_input("e"), rx.linear_to_input("f")
     ev, fe = oracle.edges(f)
 
@@ -198,12 +210,16 @@ def test_query_into_pinned_host_buffers(oracle, level, patch):
         assert torch.equal(out, dev), pin_in
 
 
-@pytest.mark.parametrize("name", ["sphere3", "torus", "cloth", "bunnyhead"])
-def test_normals_against_reference_fixture(oracle, name):
+@pytest.mark.parametrize("name,patch", [(n, 256) for n in ("sphere3", "torus", "cloth", "bunnyhead")]
+                         + [("sphere3", "patcher"), ("torus", "patcher")])
+def test_normals_against_reference_fixture(oracle, name, patch, tmp_path):
     # fixtures: output of the reference's own vertex_normal_ref (FP64 and FP32)
     from rxmesh_gb300 import RXMeshStatic
     g = golden(name)
-    rx = RXMeshStatic(g["fv"], len(g["xyz"]), patch_size=256)
+    if patch == "patcher":
+        rx = make_rx(name, patch, tmp_path)[2]
+    else:
+        rx = RXMeshStatic(g["fv"], len(g["xyz"]), patch_size=patch)
     x32 = g["xyz"].astype(np.float32)
     x = torch.tensor(x32, device="cuda")
     n = rx.to_input(rx.vertex_normals(rx.to_linear(x), "max")).cpu().numpy()
