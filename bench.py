@@ -648,6 +648,34 @@ def run_batch(args, torch):
             "pcg_iters_mean": float(it.mean()), "host_build_s": build_s}
 
 
+def run_patcher(args, torch):
+    """Mesh build with the GPU Lloyd patcher against the host BFS partitioner
+    (torus 1024x1024, patches <= 512 faces): build wall time, patches, ribbon
+    fractions, and the query + normal sweep on each partition."""
+    from rxmesh_gb300 import RXMeshStatic, meshgen
+    x, f = meshgen.torus(1024, 1024, jitter=1e-3, seed=0)
+    out = {"workload": "torus 1024x1024 (F=2,097,152), patches <= 512 faces; build = "
+                       "RXMeshStatic construction wall time (host topology + upload)"}
+    for name, kw in (("host_bfs", {}), ("gpu_lloyd", {"gpu_patcher": True})):
+        try:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rx = RXMeshStatic(f, len(x), patch_size=512, **kw)
+            torch.cuda.synchronize()
+            build_s = time.perf_counter() - t0
+            V, E, F = rx.get_num_vertices(), rx.get_num_edges(), rx.get_num_faces()
+            xl = rx.to_linear(torch.tensor(x, device="cuda"))
+            _, ms, _, _, _ = run_sweep(args, torch, rx, xl, (V, E, F))
+            out[name] = {"build_s": build_s, "num_patches": rx.get_num_patches(),
+                         "max_local_faces": rx.info["max_local_faces"],
+                         "ribbon_vertex_fraction": rx.info["ribbon_vertices"] / V,
+                         "ribbon_face_fraction": rx.info["ribbon_faces"] / F,
+                         "sweep_ms": ms}
+        except Exception as e:  # reported, not fatal to the rest of the line
+            out[name] = {"error": str(e)}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -658,7 +686,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-arap", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
-    ap.add_argument("--only", choices=["sweep", "queries", "mcf", "arap", "batch"],
+    ap.add_argument("--no-patcher", action="store_true")
+    ap.add_argument("--only", choices=["sweep", "queries", "mcf", "arap", "batch", "patcher"],
                     help="run one workload and print only its results (for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -676,11 +705,11 @@ def main():
         return
     if args.only and args.only != "sweep":
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        fn = {"mcf": run_mcf, "arap": run_arap, "batch": run_batch}[args.only]
+        fn = {"mcf": run_mcf, "arap": run_arap, "batch": run_batch, "patcher": run_patcher}[args.only]
         print(json.dumps({"only": args.only, args.only: fn(args, torch)}))
         return
     if args.only == "sweep":
-        args.no_mcf = args.no_arap = args.no_batch = args.no_cpu = True
+        args.no_mcf = args.no_arap = args.no_batch = args.no_cpu = args.no_patcher = True
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -747,6 +776,8 @@ def main():
         line["arap"] = run_arap(args, torch)
     if rank == 0 and not args.no_batch:
         line["batch"] = run_batch(args, torch)
+    if rank == 0 and not args.no_patcher:
+        line["patcher"] = run_patcher(args, torch)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

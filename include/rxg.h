@@ -100,8 +100,13 @@ void       rxg_mesh_destroy(rxg_mesh* m);
  * mesh can only be passed to the rxg_mesh_* introspection calls).
  * RXG_MESH_SPLIT_COMPONENTS never lets a patch span two connected
  * components, so each component's elements get contiguous linear ids in
- * input order of components (used to pack many meshes into one). */
-enum { RXG_MESH_HOST_ONLY = 1, RXG_MESH_SPLIT_COMPONENTS = 2 };
+ * input order of components (used to pack many meshes into one).
+ * RXG_MESH_GPU_PATCHER partitions on the current CUDA device with Lloyd
+ * region growing (RXMesh's patcher, patcher/patcher.cu:828-960; needs a GPU,
+ * deterministic, patches of at most patch_faces faces, vertex and edge
+ * owners as rxg_mesh_create_partitioned gives them); RXG_ERR_NOT_CONVERGED
+ * if it has not met the bound after 200 iterations. */
+enum { RXG_MESH_HOST_ONLY = 1, RXG_MESH_SPLIT_COMPONENTS = 2, RXG_MESH_GPU_PATCHER = 4 };
 rxg_status rxg_mesh_create_ex(const int32_t* fv, int64_t nf, int64_t nv,
                               int32_t patch_faces, int32_t flags, rxg_mesh** out);
 

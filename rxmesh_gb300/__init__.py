@@ -56,11 +56,14 @@ class RXMeshStatic:
     patcher_file: a partition that RXMesh (or save()) wrote; face_patch
     (nf,), with optional vertex_patch (nv,) and edge_patch (ne,) owners: a
     partition given as arrays (rxg_mesh_create_partitioned).  Either replaces
-    the library's own partition and patch_size.
+    the library's own partition and patch_size.  gpu_patcher: partition on
+    the GPU with Lloyd region growing (RXMesh's patcher) instead of the host
+    BFS partitioner.
     """
 
     def __init__(self, fv, num_vertices=None, patch_size=512, host_only=False,
-                 patcher_file=None, face_patch=None, vertex_patch=None, edge_patch=None):
+                 patcher_file=None, face_patch=None, vertex_patch=None, edge_patch=None,
+                 gpu_patcher=False):
         L = _lib.load()
         f = np.ascontiguousarray(fv, dtype=np.int32).reshape(-1, 3)
         nv = int(f.max()) + 1 if num_vertices is None else int(num_vertices)
@@ -81,6 +84,8 @@ class RXMeshStatic:
             check(L.rxg_mesh_create_partitioned(f.ctypes.data, f.shape[0], nv, ptr[0], ptr[1],
                                                 ptr[2], ne, flags, ctypes.byref(h)))
         else:
+            if gpu_patcher:
+                flags |= 4  # RXG_MESH_GPU_PATCHER
             check(L.rxg_mesh_create_ex(f.ctypes.data, f.shape[0], nv, int(patch_size), flags,
                                        ctypes.byref(h)))
         self._h = h

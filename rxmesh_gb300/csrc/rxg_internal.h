@@ -95,6 +95,7 @@ struct Mesh
     // faces (the rest hold vertices in no face), face-connected components
     std::vector<int32_t> fv_in;
     int32_t              num_face_patches = 0, num_components = 0;
+    int32_t              lloyd_runs = 0;  // GPU patcher iterations (0: not used)
 
     DeviceTopo d;
 
@@ -137,6 +138,14 @@ cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t s);
 // partitioned / patch-file constructors (rxg_mesh.cpp).
 rxg_status create_mesh(const int32_t* fv, int64_t nf, int64_t nv, int32_t patch_faces,
                        int32_t flags, const Partition* part, rxg_mesh** out);
+
+// Partition on the GPU (rxg_patcher.cu): Lloyd region growing on the face
+// graph ff (CSR through shared edges) into regions of at most P faces; comp:
+// per face, the smallest face id of its connected component.
+rxg_status gpu_partition(int64_t nf, const std::vector<int32_t>& ff_off,
+                         const std::vector<int32_t>& ff_val, const std::vector<int32_t>& comp,
+                         int32_t P, std::vector<int32_t>& face_patch, int32_t& np,
+                         int32_t& lloyd_runs);
 
 // Lazily allocated per-mesh device scratch and the oriented ring.
 struct Lazy;

@@ -118,7 +118,8 @@ int32_t find_root(std::vector<int32_t>& up, int32_t x)
 }  // namespace
 
 static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv, int32_t P,
-                             bool split_components, const Partition* part = nullptr)
+                             bool split_components, const Partition* part = nullptr,
+                             bool gpu_patcher = false)
 {
     M.nf          = nf;
     M.nv          = nv;
@@ -185,6 +186,8 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
     for (int64_t v = 0; v < nv; ++v) M.max_valence = std::max<int64_t>(M.max_valence, valence[v]);
 
     // ---- face-connected components (through shared edges) -------------
+    const bool           gpu_partitioning = gpu_patcher && !part;
+    std::vector<int32_t> comp_of;  // smallest face id of each face's component
     {
         std::vector<int32_t> up(nf);
         for (int64_t f = 0; f < nf; ++f) up[f] = (int32_t)f;
@@ -195,6 +198,39 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
             }
         M.num_components = 0;
         for (int64_t f = 0; f < nf; ++f) M.num_components += find_root(up, (int32_t)f) == f;
+        if (gpu_partitioning) {
+            comp_of.resize(nf);
+            for (int64_t f = 0; f < nf; ++f) comp_of[f] = find_root(up, (int32_t)f);
+        }
+    }
+
+    // ---- partition on the GPU (Lloyd region growing), then built like a
+    // given partition
+    Partition            gpart;
+    std::vector<int32_t> gface;
+    if (gpu_partitioning) {
+        std::vector<int32_t> ff_off(nf + 1, 0), ff_val;
+        for (int64_t f = 0; f < nf; ++f)
+            for (int k = 0; k < 3; ++k) {
+                const int32_t e = fe[3 * f + k];
+                ff_off[f + 1] += ef_off[e + 1] - ef_off[e] - 1;
+            }
+        for (int64_t f = 0; f < nf; ++f) ff_off[f + 1] += ff_off[f];
+        ff_val.resize(ff_off[nf]);
+        for (int64_t f = 0; f < nf; ++f) {
+            int32_t j = ff_off[f];
+            for (int k = 0; k < 3; ++k) {
+                const int32_t e = fe[3 * f + k];
+                for (int32_t t = ef_off[e]; t < ef_off[e + 1]; ++t)
+                    if (ef_val[t] != f) ff_val[j++] = ef_val[t];
+            }
+        }
+        int32_t          gnp = 0;
+        const rxg_status st  = gpu_partition(nf, ff_off, ff_val, comp_of, P, gface, gnp, M.lloyd_runs);
+        if (st != RXG_OK) return st;
+        gpart.face       = gface.data();
+        gpart.patch_size = P;
+        part             = &gpart;
     }
 
     // ---- patch partition: BFS region growing on the face graph ----------
@@ -672,7 +708,7 @@ rxg_status rxg::create_mesh(const int32_t* fv, int64_t nf, int64_t nv, int32_t p
     rxg_status s;
     try {
         s = build_host(h->m, fv, nf, nv, patch_faces, (flags & RXG_MESH_SPLIT_COMPONENTS) != 0,
-                       part);
+                       part, (flags & RXG_MESH_GPU_PATCHER) != 0);
     } catch (const std::bad_alloc&) {
         set_error("rxg_mesh_create: host allocation failed");
         s = RXG_ERR_NOMEM;

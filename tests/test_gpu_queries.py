@@ -26,8 +26,10 @@ MESHES = {
 
 
 # (mesh, patch size); "patcher": the partition RXMesh saved for the mesh
-# (input/<name>_patches, kept in the golden fixture)
-CASES = [(n, p) for n in MESHES for p in (64, 512)] + [("sphere3", "patcher"), ("torus", "patcher")]
+# (input/<name>_patches, kept in the golden fixture); "gpu": the GPU patcher
+CASES = ([(n, p) for n in MESHES for p in (64, 512)] + [("sphere3", "patcher"), ("torus", "patcher")]
+         + [(n, "gpu") for n in ("torus64", "icosphere4", "sphere3", "isolated", "nonmanifold",
+                                 "components")])
 
 
 def make_rx(name, patch, tmp_path):
@@ -38,6 +40,8 @@ def make_rx(name, patch, tmp_path):
         path.write_bytes(g["patcher_file"].tobytes())
         return g["xyz"], g["fv"], RXMeshStatic(g["fv"], len(g["xyz"]), patcher_file=str(path))
     x, f = MESHES[name]()
+    if patch == "gpu":  # partitioned on the GPU (Lloyd), 64-face patches
+        return x, f, RXMeshStatic(f, len(x), patch_size=64, gpu_patcher=True)
     return x, f, RXMeshStatic(f, len(x), patch_size=patch)
 
 

@@ -190,3 +190,26 @@ def test_bad_partitions_and_files(tmp_path):
         RXMeshStatic(t["fv"], len(t["xyz"]), host_only=True, patcher_file=str(path))
     with pytest.raises(RXGError):
         RXMeshStatic(fv, nv, host_only=True, patcher_file=str(tmp_path / "missing"))
+
+
+@pytest.mark.parametrize("P", [64, 512])
+def test_lloyd_restatement_gives_valid_partitions(P):
+    """The oracle's restatement of the Lloyd patcher (the GPU patcher's
+    checker): every face in a region of at most P faces, at least one region
+    per component, and the partition builds."""
+    from conftest import edge_case_meshes
+    from oracle.patcher import face_graph, lloyd_partition
+    from rxmesh_gb300 import RXMeshStatic
+    meshes = [meshgen.torus(40, 24, jitter=1e-3, seed=2), meshgen.icosphere(3)]
+    meshes += list(edge_case_meshes().values())
+    for x, f in meshes:
+        fp, runs = lloyd_partition(f, P)
+        again, _ = lloyd_partition(f, P)
+        assert np.array_equal(fp, again) and runs >= 1
+        assert fp.min() == 0 and np.bincount(fp).min() >= 1 and np.bincount(fp).max() <= P
+        _, _, comp = face_graph(f)
+        for c in np.unique(comp):
+            assert len(np.unique(fp[comp == c])) >= 1
+            assert not np.isin(np.unique(fp[comp == c]), fp[comp != c]).any()
+        rx = RXMeshStatic(f, len(x), host_only=True, face_patch=fp)
+        assert rx.get_num_patches() >= fp.max() + 1
