@@ -218,11 +218,14 @@ class RXMeshStatic
    public:
     // fv: one {v0, v1, v2} per face, input vertex ids (rxmesh_static.h:87-92).
     // patcher_file: a partition saved by RXMesh (or save()) for this mesh;
-    // empty: the library's own partition into patches of patch_size faces.
+    // empty: the library's own partition into patches of patch_size faces,
+    // by the host BFS partitioner or, with gpu_patcher, by Lloyd region
+    // growing on the GPU (RXMesh's patcher).
     explicit RXMeshStatic(std::vector<std::vector<uint32_t>>& fv,
                           const std::string                   patcher_file = "",
                           const uint32_t                      patch_size   = 512,
-                          bool                                host_only    = false)
+                          bool                                host_only    = false,
+                          bool                                gpu_patcher  = false)
     {
         std::vector<int32_t> flat;
         flat.reserve(3 * fv.size());
@@ -235,7 +238,8 @@ class RXMeshStatic
             }
         }
         rxg_mesh*     m     = nullptr;
-        const int32_t flags = host_only ? RXG_MESH_HOST_ONLY : 0;
+        const int32_t flags =
+            (host_only ? RXG_MESH_HOST_ONLY : 0) | (gpu_patcher ? RXG_MESH_GPU_PATCHER : 0);
         if (patcher_file.empty())
             check(rxg_mesh_create_ex(flat.data(), (int64_t)fv.size(), nv, (int32_t)patch_size,
                                      flags, &m));
@@ -249,6 +253,16 @@ class RXMeshStatic
     void save(const std::string& filename) const
     {
         check(rxg_mesh_save_patch_file(m_mesh.get(), filename.c_str()));
+    }
+    // owner patch of every face, vertex and edge, in input ids
+    void partition(std::vector<int32_t>& face_patch, std::vector<int32_t>& vertex_patch,
+                   std::vector<int32_t>& edge_patch) const
+    {
+        face_patch.resize((size_t)m_info.num_faces);
+        vertex_patch.resize((size_t)m_info.num_vertices);
+        edge_patch.resize((size_t)m_info.num_edges);
+        check(rxg_mesh_partition(m_mesh.get(), face_patch.data(), vertex_patch.data(),
+                                 edge_patch.data()));
     }
     RXMeshStatic(const RXMeshStatic&)            = delete;
     RXMeshStatic& operator=(const RXMeshStatic&) = delete;

@@ -89,6 +89,11 @@ static int host_checks(const char* dir)
         rx.save(path);
         RXMeshStatic back(fv, path, 512, true);
         REQUIRE(back.get_num_patches() == rx.get_num_patches());
+        std::vector<int32_t> fp0, vp0, ep0, fp1, vp1, ep1;
+        rx.partition(fp0, vp0, ep0);
+        back.partition(fp1, vp1, ep1);
+        REQUIRE(fp0 == fp1 && vp0 == vp1 && ep0 == ep1);
+        REQUIRE((int64_t)fp0.size() == rx.get_num_faces());
         REQUIRE(back.linear_to_input(RXG_ELEM_VERTEX) == l2i);
         REQUIRE(back.linear_to_input(RXG_ELEM_EDGE) == rx.linear_to_input(RXG_ELEM_EDGE));
         threw = false;
