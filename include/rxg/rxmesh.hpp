@@ -21,6 +21,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -237,17 +239,22 @@ class RXMeshStatic
                 nv = std::max<int64_t>(nv, (int64_t)v + 1);
             }
         }
-        rxg_mesh*     m     = nullptr;
-        const int32_t flags =
-            (host_only ? RXG_MESH_HOST_ONLY : 0) | (gpu_patcher ? RXG_MESH_GPU_PATCHER : 0);
-        if (patcher_file.empty())
-            check(rxg_mesh_create_ex(flat.data(), (int64_t)fv.size(), nv, (int32_t)patch_size,
-                                     flags, &m));
-        else
-            check(rxg_mesh_create_from_patch_file(flat.data(), (int64_t)fv.size(), nv,
-                                                  patcher_file.c_str(), flags, &m));
-        m_mesh.reset(m);
-        check(rxg_mesh_get_info(m, &m_info));
+        create(flat, nv, patcher_file, patch_size, host_only, gpu_patcher);
+    }
+    // An OBJ file (RXMeshStatic(file_path, patcher_file, patch_size),
+    // rxmesh_static.h:61-66, which reads it with import_obj): "v x y z" and
+    // "f a b c ..." lines (a, a/t, a//n, a/t/n; negative = relative to the
+    // vertices read so far), polygons fanned into triangles; the positions
+    // become the input vertex coordinates (not on a host_only mesh).
+    explicit RXMeshStatic(const std::string& file_path, const std::string patcher_file = "",
+                          const uint32_t patch_size = 512, bool host_only = false,
+                          bool gpu_patcher = false)
+    {
+        std::vector<std::vector<double>> xyz;
+        std::vector<int32_t>             flat;
+        read_obj(file_path, xyz, flat);
+        create(flat, (int64_t)xyz.size(), patcher_file, patch_size, host_only, gpu_patcher);
+        if (!host_only) add_vertex_coordinates(xyz);
     }
     // RXMesh::save (rxmesh.h:326-329): the partition as a patcher file
     void save(const std::string& filename) const
@@ -344,6 +351,74 @@ class RXMeshStatic
         void operator()(rxg_mesh* m) const { rxg_mesh_destroy(m); }
     };
     std::unique_ptr<rxg_mesh, Del> m_mesh;
+
+    void create(const std::vector<int32_t>& flat, int64_t nv, const std::string& patcher_file,
+                uint32_t patch_size, bool host_only, bool gpu_patcher)
+    {
+        rxg_mesh*     m     = nullptr;
+        const int32_t flags =
+            (host_only ? RXG_MESH_HOST_ONLY : 0) | (gpu_patcher ? RXG_MESH_GPU_PATCHER : 0);
+        const int64_t nf = (int64_t)flat.size() / 3;
+        if (patcher_file.empty())
+            check(rxg_mesh_create_ex(flat.data(), nf, nv, (int32_t)patch_size, flags, &m));
+        else
+            check(rxg_mesh_create_from_patch_file(flat.data(), nf, nv, patcher_file.c_str(), flags,
+                                                  &m));
+        m_mesh.reset(m);
+        check(rxg_mesh_get_info(m, &m_info));
+    }
+    static void read_obj(const std::string& path, std::vector<std::vector<double>>& xyz,
+                         std::vector<int32_t>& flat)
+    {
+        std::FILE* fp = std::fopen(path.c_str(), "r");
+        if (!fp) throw Error(RXG_ERR_INVALID, "cannot open " + path);
+        std::string line;
+        char        buf[4096];
+        auto        fail = [&](const std::string& why) {
+            std::fclose(fp);
+            throw Error(RXG_ERR_INVALID, path + ": " + why);
+        };
+        while (std::fgets(buf, sizeof(buf), fp)) {
+            line.assign(buf);
+            while (!line.empty() && line.back() != '\n' && std::fgets(buf, sizeof(buf), fp))
+                line.append(buf);
+            const char* c = line.c_str();
+            if (c[0] == 'v' && (c[1] == ' ' || c[1] == '\t')) {
+                double p[3];
+                char*  e = const_cast<char*>(c + 1);
+                for (double& q : p) {
+                    char* start = e;
+                    q           = std::strtod(start, &e);
+                    if (e == start) fail("malformed vertex line");
+                }
+                xyz.push_back({p[0], p[1], p[2]});
+            } else if (c[0] == 'f' && (c[1] == ' ' || c[1] == '\t')) {
+                std::vector<int32_t> ids;
+                const char*          q = c + 1;
+                while (true) {
+                    while (*q == ' ' || *q == '\t') ++q;
+                    if (*q == '\0' || *q == '\n' || *q == '\r' || *q == '#') break;
+                    char*      e = nullptr;
+                    const long i = std::strtol(q, &e, 10);
+                    if (e == q || i == 0) fail("malformed face line");
+                    const long n = (long)xyz.size();
+                    const long v = i > 0 ? i - 1 : n + i;  // 1-based, or relative
+                    if (v < 0 || v >= n) fail("face references a vertex not yet defined");
+                    ids.push_back((int32_t)v);
+                    q = e;
+                    while (*q && *q != ' ' && *q != '\t' && *q != '\n' && *q != '\r') ++q;
+                }
+                if (ids.size() < 3) fail("face with fewer than three vertices");
+                for (size_t k = 1; k + 1 < ids.size(); ++k) {
+                    flat.push_back(ids[0]);
+                    flat.push_back(ids[k]);
+                    flat.push_back(ids[k + 1]);
+                }
+            }
+        }
+        std::fclose(fp);
+        if (flat.empty()) throw Error(RXG_ERR_INVALID, path + ": no faces");
+    }
     rxg_mesh_info                  m_info{};
     DenseMatrix<double>            m_xyz;
 };

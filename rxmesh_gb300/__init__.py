@@ -97,6 +97,18 @@ class RXMeshStatic:
         self._maps = {}
         self._dmaps = {}
 
+    @classmethod
+    def from_obj(cls, path, patcher_file=None, patch_size=512, **kw):
+        """RXMeshStatic(file_path, patcher_file, patch_size)
+        (rxmesh_static.h:61-66): the mesh of an OBJ file (polygons fanned
+        into triangles).  The positions (float64, input order) are kept as
+        input_vertex_coordinates."""
+        from .meshgen import read_obj
+        xyz, fv = read_obj(path)
+        rx = cls(fv, len(xyz), patch_size=patch_size, patcher_file=patcher_file, **kw)
+        rx.input_vertex_coordinates = xyz
+        return rx
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:

@@ -78,14 +78,18 @@ def plane(nx, ny, dx=1.0, axis=2, dtype=np.float64):
 
 
 def read_obj(path):
-    """Vertices and triangles of an OBJ file (faces fan-triangulated)."""
+    """Vertices and triangles of an OBJ file (faces fan-triangulated; an
+    index is 1-based, or negative: relative to the vertices read so far)."""
     vs, fs = [], []
     with open(path) as fh:
         for line in fh:
-            if line.startswith("v "):
+            if line.startswith(("v ", "v\t")):
                 vs.append([float(t) for t in line.split()[1:4]])
-            elif line.startswith("f "):
-                ids = [int(t.split("/")[0]) - 1 for t in line.split()[1:]]
+            elif line.startswith(("f ", "f\t")):
+                ids = []
+                for t in line.split("#")[0].split()[1:]:
+                    i = int(t.split("/")[0])
+                    ids.append(i - 1 if i > 0 else len(vs) + i)
                 for k in range(1, len(ids) - 1):
                     fs.append([ids[0], ids[k], ids[k + 1]])
-    return np.array(vs, np.float64), np.array(fs, np.int32)
+    return np.array(vs, np.float64), np.array(fs, np.int32).reshape(-1, 3)

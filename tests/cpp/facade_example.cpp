@@ -103,6 +103,29 @@ static int host_checks(const char* dir)
             threw = e.status == RXG_ERR_INVALID;
         }
         REQUIRE(threw);
+
+        // OBJ constructor: a quad (fanned), a triangle in v/t/n form, a
+        // relative index; the same mesh as its face list
+        const std::string obj = std::string(dir) + "/quad.obj";
+        std::FILE*        fp  = std::fopen(obj.c_str(), "w");
+        REQUIRE(fp != nullptr);
+        std::fputs("# two faces\nv 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nv 2 0 0\n"
+                   "vt 0 0\nvn 0 0 1\nf 1 2 3 4\nf 2/1/1 -1/1/1 3/1/1\n",
+                   fp);
+        std::fclose(fp);
+        RXMeshStatic from_obj(obj, "", 512, true);
+        REQUIRE(from_obj.get_num_vertices() == 5 && from_obj.get_num_faces() == 3);
+        REQUIRE(from_obj.get_num_edges() == 7);
+        std::vector<std::vector<uint32_t>> qf = {{0, 1, 2}, {0, 2, 3}, {1, 4, 2}};
+        RXMeshStatic                       from_fv(qf, "", 512, true);
+        REQUIRE(from_obj.linear_to_input(RXG_ELEM_EDGE) == from_fv.linear_to_input(RXG_ELEM_EDGE));
+        threw = false;
+        try {
+            RXMeshStatic r4(std::string(dir) + "/missing.obj", "", 512, true);
+        } catch (const Error& e) {
+            threw = e.status == RXG_ERR_INVALID;
+        }
+        REQUIRE(threw);
     }
     return 0;
 }

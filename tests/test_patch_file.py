@@ -213,3 +213,18 @@ def test_lloyd_restatement_gives_valid_partitions(P):
             assert not np.isin(np.unique(fp[comp == c]), fp[comp != c]).any()
         rx = RXMeshStatic(f, len(x), host_only=True, face_patch=fp)
         assert rx.get_num_patches() >= fp.max() + 1
+
+
+def test_obj_constructor(tmp_path):
+    """RXMeshStatic.from_obj: the OBJ forms RXMesh's import_obj reads (v/t/n
+    indices, negative indices, polygons)."""
+    from rxmesh_gb300 import RXMeshStatic
+    p = tmp_path / "quad.obj"
+    p.write_text("# two faces\nv 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nv 2 0 0\nvt 0 0\nvn 0 0 1\n"
+                 "f 1 2 3 4\nf 2/1/1 -1/1/1 3/1/1\n")
+    rx = RXMeshStatic.from_obj(str(p), patch_size=64, host_only=True)
+    assert (rx.get_num_vertices(), rx.get_num_edges(), rx.get_num_faces()) == (5, 7, 3)
+    assert rx.input_vertex_coordinates.shape == (5, 3)
+    same = RXMeshStatic(np.array([[0, 1, 2], [0, 2, 3], [1, 4, 2]]), 5, patch_size=64,
+                        host_only=True)
+    assert all(np.array_equal(a, b) for a, b in zip(rx.patches(), same.patches()))
