@@ -256,6 +256,54 @@ class RXMeshStatic
         create(flat, (int64_t)xyz.size(), patcher_file, patch_size, host_only, gpu_patcher);
         if (!host_only) add_vertex_coordinates(xyz);
     }
+    // Several OBJ files as one mesh of disjoint regions (RXMeshStatic(
+    // files_path, patch_size), rxmesh_static.cu:66-160): faces and vertices
+    // follow file after file, and every face, vertex and edge carries the
+    // index of its file as its region label.
+    explicit RXMeshStatic(const std::vector<std::string>& files_path,
+                          const uint32_t patch_size = 512, bool host_only = false)
+    {
+        std::vector<std::vector<double>> xyz;
+        std::vector<int32_t>             flat;
+        for (const auto& path : files_path) {
+            std::vector<std::vector<double>> x;
+            std::vector<int32_t>             f;
+            read_obj(path, x, f);
+            const int32_t base = (int32_t)xyz.size();
+            for (int32_t v : f) flat.push_back(v + base);
+            xyz.insert(xyz.end(), x.begin(), x.end());
+            m_region_faces.push_back((int64_t)flat.size() / 3);
+            m_region_vertices.push_back((int64_t)xyz.size());
+        }
+        if (files_path.empty()) throw Error(RXG_ERR_INVALID, "no files");
+        create(flat, (int64_t)xyz.size(), "", patch_size, host_only, false);
+        if (!host_only) add_vertex_coordinates(xyz);
+    }
+    // number of regions (files; 1 for the other constructors) and the region
+    // label of every face / vertex / edge in input ids (get_face_region_label
+    // and the like, rxmesh_static.h:826-849)
+    int get_num_regions() const { return m_region_faces.empty() ? 1 : (int)m_region_faces.size(); }
+    std::vector<int32_t> get_region_label(int32_t elem) const
+    {
+        const auto label_of = [](const std::vector<int64_t>& ends, int64_t id) {
+            return (int32_t)(std::upper_bound(ends.begin(), ends.end(), id) - ends.begin());
+        };
+        std::vector<int32_t> out;
+        if (elem == RXG_ELEM_FACE || elem == RXG_ELEM_VERTEX) {
+            const int64_t n = elem == RXG_ELEM_FACE ? m_info.num_faces : m_info.num_vertices;
+            out.resize((size_t)n, 0);
+            if (!m_region_faces.empty())
+                for (int64_t i = 0; i < n; ++i)
+                    out[(size_t)i] = label_of(elem == RXG_ELEM_FACE ? m_region_faces : m_region_vertices, i);
+        } else {
+            std::vector<int32_t> ev(2 * (size_t)m_info.num_edges);
+            check(rxg_mesh_input_edges(m_mesh.get(), ev.data()));
+            out.resize((size_t)m_info.num_edges, 0);
+            if (!m_region_faces.empty())
+                for (size_t e = 0; e < out.size(); ++e) out[e] = label_of(m_region_vertices, ev[2 * e]);
+        }
+        return out;
+    }
     // RXMesh::save (rxmesh.h:326-329): the partition as a patcher file
     void save(const std::string& filename) const
     {
@@ -351,6 +399,7 @@ class RXMeshStatic
         void operator()(rxg_mesh* m) const { rxg_mesh_destroy(m); }
     };
     std::unique_ptr<rxg_mesh, Del> m_mesh;
+    std::vector<int64_t>           m_region_faces, m_region_vertices;  // cumulative, per file
 
     void create(const std::vector<int32_t>& flat, int64_t nv, const std::string& patcher_file,
                 uint32_t patch_size, bool host_only, bool gpu_patcher)

@@ -109,6 +109,43 @@ class RXMeshStatic:
         rx.input_vertex_coordinates = xyz
         return rx
 
+    @classmethod
+    def from_objs(cls, paths, patch_size=512, **kw):
+        """RXMeshStatic(files_path, patch_size) (rxmesh_static.cu:66-160):
+        several OBJ files as one mesh of disjoint regions, file after file;
+        get_region_label() gives each element's file index."""
+        from .meshgen import read_obj
+        xs, fs, fends, vends = [], [], [], []
+        base = 0
+        for p in paths:
+            x, f = read_obj(p)
+            xs.append(x)
+            fs.append(f + base)
+            base += len(x)
+            fends.append(sum(len(g) for g in fs))
+            vends.append(base)
+        if not paths:
+            raise ValueError("no files")
+        rx = cls(np.concatenate(fs), base, patch_size=patch_size, **kw)
+        rx.input_vertex_coordinates = np.concatenate(xs)
+        rx._regions = (np.array(fends), np.array(vends))
+        return rx
+
+    def get_num_regions(self):
+        r = getattr(self, "_regions", None)
+        return 1 if r is None else len(r[0])
+
+    def get_region_label(self, elem="f"):
+        """Region (file) index of every face / vertex / edge, input ids
+        (get_face_region_label and the like, rxmesh_static.h:826-849)."""
+        r = getattr(self, "_regions", None)
+        n = {"f": self.get_num_faces(), "v": self.get_num_vertices(), "e": self.get_num_edges()}[elem]
+        if r is None:
+            return np.zeros(n, np.int32)
+        if elem == "e":
+            return np.searchsorted(r[1], self.input_edges()[:, 0], side="right").astype(np.int32)
+        return np.searchsorted(r[0] if elem == "f" else r[1], np.arange(n), side="right").astype(np.int32)
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:

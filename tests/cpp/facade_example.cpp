@@ -119,6 +119,17 @@ static int host_checks(const char* dir)
         std::vector<std::vector<uint32_t>> qf = {{0, 1, 2}, {0, 2, 3}, {1, 4, 2}};
         RXMeshStatic                       from_fv(qf, "", 512, true);
         REQUIRE(from_obj.linear_to_input(RXG_ELEM_EDGE) == from_fv.linear_to_input(RXG_ELEM_EDGE));
+        // two files, two regions
+        const std::string tri = std::string(dir) + "/tri.obj";
+        fp                    = std::fopen(tri.c_str(), "w");
+        REQUIRE(fp != nullptr);
+        std::fputs("v 0 0 1\nv 1 0 1\nv 0 1 1\nf 1 2 3\n", fp);
+        std::fclose(fp);
+        RXMeshStatic both(std::vector<std::string>{obj, tri}, 512, true);
+        REQUIRE(both.get_num_regions() == 2 && both.get_num_faces() == 4);
+        REQUIRE((both.get_region_label(RXG_ELEM_FACE) == std::vector<int32_t>{0, 0, 0, 1}));
+        const std::vector<int32_t> el = both.get_region_label(RXG_ELEM_EDGE);
+        REQUIRE(std::count(el.begin(), el.end(), 1) == 3 && el.size() == 10);
         threw = false;
         try {
             RXMeshStatic r4(std::string(dir) + "/missing.obj", "", 512, true);

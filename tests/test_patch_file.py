@@ -228,3 +228,19 @@ def test_obj_constructor(tmp_path):
     same = RXMeshStatic(np.array([[0, 1, 2], [0, 2, 3], [1, 4, 2]]), 5, patch_size=64,
                         host_only=True)
     assert all(np.array_equal(a, b) for a, b in zip(rx.patches(), same.patches()))
+
+
+def test_multi_file_regions(tmp_path):
+    """RXMeshStatic.from_objs: files become disjoint regions with labels."""
+    from rxmesh_gb300 import RXMeshStatic
+    a = tmp_path / "a.obj"
+    a.write_text("v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nf 1 2 3\nf 1 3 4\n")
+    b = tmp_path / "b.obj"
+    b.write_text("v 0 0 1\nv 1 0 1\nv 0 1 1\nf 1 2 3\n")
+    rx = RXMeshStatic.from_objs([str(a), str(b)], patch_size=64, host_only=True)
+    assert rx.get_num_regions() == 2
+    assert (rx.get_num_vertices(), rx.get_num_faces(), rx.get_num_edges()) == (7, 3, 8)
+    assert rx.get_region_label("f").tolist() == [0, 0, 1]
+    assert rx.get_region_label("v").tolist() == [0, 0, 0, 0, 1, 1, 1]
+    assert sorted(rx.get_region_label("e").tolist()) == [0] * 5 + [1] * 3
+    assert rx.input_vertex_coordinates.shape == (7, 3)
