@@ -62,6 +62,40 @@ def test_newton_and_matfree_entry_points_reject_bad_arguments():
     assert L.rxg_arap_hvp(rx._h, 1, x.ctypes.data, x.ctypes.data, 0, None, None, None, None) == 1
 
 
+def test_dense_and_partition_entry_points_reject_bad_arguments(tmp_path):
+    """rxg_dense_*, the partition and patch-file calls: RXG_ERR_INVALID with a
+    message on NULL, host or inconsistent arguments, without a GPU."""
+    import ctypes
+    from rxmesh_gb300 import RXMeshStatic, _lib
+    L = _lib.load()
+    x = np.zeros(12)
+    out = ctypes.c_double()
+    assert L.rxg_dense_axpby(12, 1, 1.0, x.ctypes.data, 1.0, x.ctypes.data, None) == 1
+    assert b"device arrays" in L.rxg_last_error()
+    assert L.rxg_dense_axpby(12, 1, 1.0, None, 1.0, x.ctypes.data, None) == 1  # x NULL, a != 0
+    assert L.rxg_dense_axpby(12, 7, 0.0, None, 1.0, x.ctypes.data, None) == 1  # bad dtype
+    assert L.rxg_dense_dot(12, 1, x.ctypes.data, x.ctypes.data, ctypes.byref(out), None) == 1
+    assert L.rxg_dense_dot(12, 1, None, x.ctypes.data, ctypes.byref(out), None) == 1
+    assert L.rxg_mesh_partition(None, None, None, None) == 1
+    _, f = meshgen.icosphere(1)
+    f = np.ascontiguousarray(f, np.int32)
+    nv = int(f.max()) + 1
+    h = ctypes.c_void_p()
+    fp = np.zeros(len(f), np.int32)
+    assert L.rxg_mesh_create_partitioned(f.ctypes.data, len(f), nv, None, None, None, -1, 1,
+                                         ctypes.byref(h)) == 1          # no face_patch
+    assert L.rxg_mesh_create_partitioned(f.ctypes.data, len(f), nv, fp.ctypes.data, None, None,
+                                         -1, 3, ctypes.byref(h)) == 1   # split flag
+    assert L.rxg_mesh_create_partitioned(f.ctypes.data, len(f), nv, fp.ctypes.data, None,
+                                         fp.ctypes.data, -1, 1, ctypes.byref(h)) == 1  # ne < 0
+    assert L.rxg_mesh_create_from_patch_file(f.ctypes.data, len(f), nv, None, 1,
+                                             ctypes.byref(h)) == 1
+    rx = RXMeshStatic(f, nv, patch_size=64, host_only=True)
+    assert L.rxg_mesh_save_patch_file(rx._h, None) == 1
+    assert L.rxg_mesh_save_patch_file(rx._h, str(tmp_path / "no" / "such" / "dir").encode()) == 1
+    assert b"cannot create" in L.rxg_last_error()
+
+
 def decode(rx):
     """Per-patch decoding of the arena into linear-id queries (CPU)."""
     hdr, arena = rx.patches()
