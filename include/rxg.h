@@ -161,6 +161,11 @@ rxg_status rxg_mesh_get_info(const rxg_mesh* m, rxg_mesh_info* info);
  * (RXMeshStatic::map_to_global, rxmesh_static.h:874-905). */
 rxg_status rxg_mesh_linear_to_input(const rxg_mesh* m, int32_t elem,
                                     int32_t* lin_to_input);
+/* RXMeshStatic::get_boundary_vertices (rxmesh_static.inl:281-323,
+ * kernels/boundary.cuh): out[v] = 1 for the ends of every edge with fewer
+ * than two faces, else 0; nv int8 in linear order, host or device (a device
+ * copy is made on stream, which is synchronised). */
+rxg_status rxg_mesh_boundary_vertices(const rxg_mesh* m, int8_t* out, void* stream);
 /* Input-numbered edge list (host, ne*2), RXMesh's m_edges_map order. */
 rxg_status rxg_mesh_input_edges(const rxg_mesh* m, int32_t* ev);
 

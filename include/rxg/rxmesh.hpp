@@ -309,6 +309,14 @@ class RXMeshStatic
     {
         check(rxg_mesh_save_patch_file(m_mesh.get(), filename.c_str()));
     }
+    // get_boundary_vertices (rxmesh_static.inl:281-323): 1 for the ends of
+    // edges with fewer than two faces, linear order
+    std::vector<int8_t> get_boundary_vertices() const
+    {
+        std::vector<int8_t> out((size_t)m_info.num_vertices);
+        check(rxg_mesh_boundary_vertices(m_mesh.get(), out.data(), nullptr));
+        return out;
+    }
     // owner patch of every face, vertex and edge, in input ids
     void partition(std::vector<int32_t>& face_patch, std::vector<int32_t>& vertex_patch,
                    std::vector<int32_t>& edge_patch) const

@@ -162,6 +162,18 @@ class RXMeshStatic:
     def get_num_faces(self):
         return self.info["num_faces"]
 
+    def get_boundary_vertices(self, stream=None):
+        """1 for every vertex on an edge with fewer than two faces
+        (get_boundary_vertices, rxmesh_static.inl:281-323): int8 in linear
+        order, a CUDA tensor (numpy for a host-only mesh)."""
+        if self.host_only:
+            out = np.empty(self.get_num_vertices(), np.int8)
+            check(self._L.rxg_mesh_boundary_vertices(self._h, out.ctypes.data, None))
+            return out
+        out = torch.empty(self.get_num_vertices(), dtype=torch.int8, device="cuda")
+        check(self._L.rxg_mesh_boundary_vertices(self._h, _ptr(out), _stream(stream)))
+        return out
+
     def partition(self):
         """(face_patch, vertex_patch, edge_patch): the owner patch of every
         face, vertex and edge in input ids (rxg_mesh_partition)."""

@@ -65,6 +65,7 @@ SIGNATURES = {
     "rxg_mesh_create_ex": [P, I64, I64, I32, I32, P],
     "rxg_mesh_create_partitioned": [P, I64, I64, P, P, P, I64, I32, P],
     "rxg_mesh_partition": [P, P, P, P],
+    "rxg_mesh_boundary_vertices": [P, P, P],
     "rxg_mesh_create_from_patch_file": [P, I64, I64, ctypes.c_char_p, I32, P],
     "rxg_mesh_save_patch_file": [P, ctypes.c_char_p],
     "rxg_mesh_destroy": [P],

@@ -94,6 +94,7 @@ struct Mesh
     // the input faces (for rxg_mesh_save_patch_file), the patches that own
     // faces (the rest hold vertices in no face), face-connected components
     std::vector<int32_t> fv_in;
+    std::vector<int8_t>  vbnd;  // 1 for a boundary vertex, linear order
     int32_t              num_face_patches = 0, num_components = 0;
     int32_t              lloyd_runs = 0;  // GPU patcher iterations (0: not used)
 

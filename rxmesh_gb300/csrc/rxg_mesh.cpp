@@ -382,6 +382,13 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
     M.e_i2l.resize(ne);
     M.f_i2l.resize(nf);
     for (int64_t i = 0; i < nv; ++i) M.v_i2l[M.v_l2i[i]] = (int32_t)i;
+    // boundary vertices: the ends of edges with fewer than two faces
+    M.vbnd.assign(nv, 0);
+    for (int64_t e = 0; e < ne; ++e)
+        if (ef_off[e + 1] - ef_off[e] < 2) {
+            M.vbnd[M.v_i2l[M.ev_in[2 * e]]]     = 1;
+            M.vbnd[M.v_i2l[M.ev_in[2 * e + 1]]] = 1;
+        }
     for (int64_t i = 0; i < ne; ++i) M.e_i2l[M.e_l2i[i]] = (int32_t)i;
     for (int64_t i = 0; i < nf; ++i) M.f_i2l[M.f_l2i[i]] = (int32_t)i;
 
@@ -821,6 +828,24 @@ rxg_status rxg_mesh_patches(const rxg_mesh* h, int32_t* hdr, uint32_t* arena, in
     if (hdr) std::memcpy(hdr, h->m.hdr.data(), h->m.hdr.size() * sizeof(PatchHdr));
     if (arena) std::memcpy(arena, h->m.arena.data(), h->m.arena.size() * 4);
     return RXG_OK;
+}
+
+rxg_status rxg_mesh_boundary_vertices(const rxg_mesh* h, int8_t* out, void* stream)
+{
+    if (!h || !out) {
+        set_error("rxg_mesh_boundary_vertices: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    const std::vector<int8_t>& b = h->m.vbnd;
+    if (!is_device_ptr(out)) {
+        std::memcpy(out, b.data(), b.size());
+        return RXG_OK;
+    }
+    // from the host copy: the flags are static topology, kept with the mesh
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t  e = cudaMemcpyAsync(out, b.data(), b.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e == cudaSuccess ? RXG_OK : cuda_status(e, "rxg_mesh_boundary_vertices");
 }
 
 rxg_status rxg_mesh_input_edges(const rxg_mesh* h, int32_t* ev)

@@ -75,6 +75,8 @@ static int host_checks(const char* dir)
     const std::vector<int32_t> l2i = rx.linear_to_input(RXG_ELEM_VERTEX);
     std::set<int32_t>          seen(l2i.begin(), l2i.end());
     REQUIRE(seen.size() == l2i.size() && *seen.begin() == 0);
+    const std::vector<int8_t> bnd = rx.get_boundary_vertices();  // closed torus: none
+    REQUIRE(bnd.size() == l2i.size() && std::count(bnd.begin(), bnd.end(), 1) == 0);
     bool threw = false;
     try {
         std::vector<std::vector<uint32_t>> bad = {{0, 1}};

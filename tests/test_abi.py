@@ -226,3 +226,41 @@ def test_ev_diamond_needs_consistent_orientation():
     bad = RXMeshStatic(g, g.max() + 1, patch_size=64, host_only=True)
     assert L.rxg_query(bad._h, Op.EVD, None, None, None) == 4
     assert b"oriented" in L.rxg_last_error()
+
+
+def test_boundary_vertices_known_answer():
+    """RXMesh's own test (tests/RXMesh_test/test_boundary.cu): bunnyhead has
+    98 boundary vertices; closed meshes have none; an open grid's border."""
+    from conftest import golden
+    from rxmesh_gb300 import RXMeshStatic
+    g = golden("bunnyhead")
+    rx = RXMeshStatic(g["fv"], len(g["xyz"]), patch_size=256, host_only=True)
+    b = rx.get_boundary_vertices()
+    assert b.dtype == np.int8 and int(b.sum()) == 98
+    # the same set from the edge face counts, in input ids
+    ev, fe = meshgen_edges(g["fv"])
+    cnt = np.bincount(fe.reshape(-1), minlength=len(ev))
+    want = np.zeros(len(g["xyz"]), np.int8)
+    want[ev[cnt < 2].reshape(-1)] = 1
+    assert np.array_equal(b[rx.input_to_linear("v")], want)
+    _, f = meshgen.icosphere(2)
+    assert RXMeshStatic(f, int(np.max(f)) + 1, patch_size=64,
+                        host_only=True).get_boundary_vertices().sum() == 0
+    x, f = meshgen.plane(7, 5)
+    assert RXMeshStatic(f, len(x), patch_size=64, host_only=True).get_boundary_vertices().sum() == 2 * (7 + 5) - 4
+
+
+def meshgen_edges(fv):
+    """Edge list in first-appearance order and each face's three edge ids."""
+    ids, ev, fe = {}, [], []
+    for t in np.asarray(fv):
+        row = []
+        for k in range(3):
+            a, b = int(t[k]), int(t[(k + 1) % 3])
+            key = (min(a, b), max(a, b))
+            if key not in ids:
+                ids[key] = len(ev)
+                ev.append((a, b))
+            row.append(ids[key])
+        fe.append(row)
+    return np.array(ev), np.array(fe)

@@ -286,3 +286,15 @@ def test_full_torus_properties():
     assert torch.equal(torch.sort(fwd).values, torch.sort(bwd).values)
     _, fvq = rx.query(Op.FV)
     assert int(torch.bincount(fvq.long(), minlength=len(deg)).min()) == 6
+
+
+def test_boundary_vertices_device():
+    """get_boundary_vertices into device memory equals the host copy;
+    bunnyhead's 98 (tests/RXMesh_test/test_boundary.cu)."""
+    from rxmesh_gb300 import RXMeshStatic
+    g = golden("bunnyhead")
+    rx = RXMeshStatic(g["fv"], len(g["xyz"]), patch_size=256)
+    host = RXMeshStatic(g["fv"], len(g["xyz"]), patch_size=256, host_only=True)
+    b = rx.get_boundary_vertices()
+    assert b.is_cuda and int(b.sum().item()) == 98
+    assert np.array_equal(b.cpu().numpy(), host.get_boundary_vertices())
