@@ -527,6 +527,28 @@ class SparseMatrix
     DeviceArray<int32_t>& row_ptr() { return m_row_ptr; }
     DeviceArray<int32_t>& col_idx() { return m_col; }
     DeviceArray<T>&       values() { return m_val; }
+    // A(row, col), 0 where the pattern has no entry (operator(),
+    // sparse_matrix.h:412-471); a host lookup that reads the row back
+    T operator()(int64_t row, int64_t col) const
+    {
+        if (row < 0 || row >= m_n) throw Error(RXG_ERR_INVALID, "row out of range");
+        int32_t be[2];
+        check_cuda(cudaMemcpy(be, m_row_ptr.data() + row, sizeof(be), cudaMemcpyDeviceToHost),
+                   "cudaMemcpy");
+        const size_t         len = (size_t)(be[1] - be[0]);
+        std::vector<int32_t> c(len);
+        std::vector<T>       v(len);
+        if (len) {
+            check_cuda(cudaMemcpy(c.data(), m_col.data() + be[0], len * 4, cudaMemcpyDeviceToHost),
+                       "cudaMemcpy");
+            check_cuda(cudaMemcpy(v.data(), m_val.data() + be[0], len * sizeof(T),
+                                  cudaMemcpyDeviceToHost),
+                       "cudaMemcpy");
+        }
+        for (size_t k = 0; k < len; ++k)
+            if (c[k] == col) return v[k];
+        return T(0);
+    }
 
    private:
     int64_t              m_n = 0;

@@ -71,6 +71,34 @@ class SparseMatrix:
         check(self._L.rxg_spmm(ctypes.byref(c), nc, _ptr(X), _ptr(Y), _stream(stream)))
         return Y
 
+    def non_zeros(self):
+        return self.col.numel()
+
+    def __call__(self, row, col):
+        """A(row, col), 0 where the pattern has no entry (operator(),
+        sparse_matrix.h:412-471); a host lookup."""
+        lo, hi = (int(v) for v in self.row_ptr[row:row + 2].tolist())
+        cols = self.col[lo:hi].tolist()
+        return float(self.val[lo + cols.index(col)]) if col in cols else 0.0
+
+    def transpose(self):
+        """A^T as a new SparseMatrix on the same device (transpose,
+        sparse_matrix.h; tests/RXMesh_test/test_sparse_matrix.cu:325-367):
+        each row keeps its diagonal entry first, then the rest by column."""
+        n = self.rows()
+        dev = self.row_ptr.device
+        counts = (self.row_ptr[1:] - self.row_ptr[:-1]).to(torch.int64)
+        rows = torch.repeat_interleave(torch.arange(n, device=dev), counts)
+        cols = self.col.to(torch.int64)
+        off_diag = (rows != cols).to(torch.int64)
+        # sort by (new row = old col, diagonal first, new col = old row)
+        key = (cols * 2 + off_diag) * n + rows
+        order = torch.argsort(key)
+        new_ptr = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+        new_ptr[1:] = torch.cumsum(torch.bincount(cols, minlength=n), 0)
+        return SparseMatrix(row_ptr=new_ptr.to(torch.int32), col=rows[order].to(torch.int32),
+                            val=self.val[order])
+
     def to_scipy(self):
         import scipy.sparse as sp
         n = self.rows()

@@ -201,6 +201,7 @@ static int gpu_checks()
     solver.pre_solve(B, X);
     solver.solve(B, X);
     REQUIRE(solver.iter_taken() > 0 && solver.converged());
+    REQUIRE(A(0, 0) > 0.0 && A(0, (int64_t)nv + 5) == 0.0);  // diagonal; no such column
     A.multiply(X, AX);
     const std::vector<double> hb = B.to_host(), hax = AX.to_host();
     double                    num = 0, den = 0;

@@ -264,3 +264,54 @@ def meshgen_edges(fv):
             row.append(ids[key])
         fe.append(row)
     return np.array(ev), np.array(fe)
+
+
+def diag_first_csr(M):
+    """scipy CSR -> (row_ptr, col, val) with each row's diagonal first."""
+    M = M.tocsr()
+    M.sort_indices()
+    rp, col, val = M.indptr.copy(), M.indices.copy(), M.data.copy()
+    for i in range(M.shape[0]):
+        seg = slice(rp[i], rp[i + 1])
+        c, v = col[seg].copy(), val[seg].copy()
+        o = np.argsort(c != i, kind="stable")
+        col[seg], val[seg] = c[o], v[o]
+    return rp, col, val
+
+
+def test_sparse_matrix_user_managed_and_transpose():
+    """SparseMatrix from user CSR arrays and A(i, j) (the reference's
+    SparseMatrixUserManaged test, test_sparse_matrix.cu:244-323), and
+    transpose (SparseMatrixTranspose, :325-367), on CPU tensors."""
+    sp = pytest.importorskip("scipy.sparse")
+    import torch
+    from rxmesh_gb300 import SparseMatrix
+    rng = np.random.default_rng(3)
+    # 10 x 10 from 20 random triplets, duplicates summed (Eigen setFromTriplets)
+    r, c, v = rng.integers(0, 10, 20), rng.integers(0, 10, 20), rng.random(20)
+    E = sp.coo_matrix((v, (r, c)), shape=(10, 10)).tocsr()
+    E.sum_duplicates()
+    rp, col, val = diag_first_csr(E)
+    A = SparseMatrix(row_ptr=torch.tensor(rp, dtype=torch.int32), col=torch.tensor(col, dtype=torch.int32),
+                     val=torch.tensor(val))
+    assert (A.rows(), A.cols(), A.non_zeros()) == (10, 10, E.nnz)
+    D = E.toarray()
+    for i in range(10):
+        for j in range(10):
+            assert abs(A(i, j) - D[i, j]) <= 1e-12
+    # transpose of a symmetric-pattern, diagonal-first matrix (the VV pattern)
+    _, f = meshgen.icosphere(2)
+    nv = int(np.max(f)) + 1
+    P = sp.coo_matrix((np.ones(3 * len(f)), (np.asarray(f)[:, [0, 1, 2]].reshape(-1),
+                                              np.asarray(f)[:, [1, 2, 0]].reshape(-1))),
+                      shape=(nv, nv))
+    P = ((P + P.T) > 0).astype(float) + sp.eye(nv)
+    P.data = rng.random(P.nnz)  # random values on the pattern, not symmetric
+    rp, col, val = diag_first_csr(P)
+    A = SparseMatrix(row_ptr=torch.tensor(rp, dtype=torch.int32), col=torch.tensor(col, dtype=torch.int32),
+                     val=torch.tensor(val))
+    T = A.transpose()
+    assert abs(T.to_scipy() - P.T.tocsr()).max() == 0
+    trp, tcol = T.row_ptr.numpy(), T.col.numpy()
+    assert all(tcol[trp[i]] == i for i in range(nv))  # diagonal first
+    assert abs(T.transpose().to_scipy() - P.tocsr()).max() == 0
