@@ -129,3 +129,35 @@ def test_mcf_step_host_buffer_and_multi_step(oracle):
     mcf_step(rx, xl, 1e-3, 3, "f64", tol=1e-10)
     mcf_step(rx, host, 1e-3, 3, "f64", tol=1e-10)
     assert np.abs(host.numpy() - xl.cpu().numpy()).max() < 1e-12
+
+
+def test_sparse_matrix_edge_length_spmv_and_transpose(oracle):
+    """The reference's SparseMatrixEdgeLen test (test_sparse_matrix.cu:175-242):
+    every off-diagonal entry of the VV pattern set to its edge length, times
+    a vector of ones, gives each vertex's summed edge lengths (FP32, sphere3);
+    and transpose on the device (test_sparse_matrix.cu:325-367)."""
+    from rxmesh_gb300 import RXMeshStatic
+    from rxmesh_gb300._solvers import SparseMatrix, mcf_assemble
+    g = golden("sphere3")
+    rx = RXMeshStatic(g["fv"], len(g["xyz"]), patch_size=256)
+    xl = rx.to_linear(torch.tensor(g["xyz"], device="cuda"))
+    A, _ = mcf_assemble(rx, xl, 0.01, torch.float32)
+    n = A.rows()
+    rows = torch.repeat_interleave(torch.arange(n, device="cuda"),
+                                   (A.row_ptr[1:] - A.row_ptr[:-1]).long())
+    cols = A.col.long()
+    A.val.copy_(torch.linalg.norm(xl[rows] - xl[cols], dim=1).float())
+    y = A.multiply(torch.ones(n, 1, dtype=torch.float32, device="cuda")).cpu().numpy()[:, 0]
+    ev, _ = oracle.edges(g["fv"])
+    want = np.zeros(len(g["xyz"]))
+    lens = np.linalg.norm(g["xyz"][ev[:, 0]] - g["xyz"][ev[:, 1]], axis=1)
+    np.add.at(want, ev[:, 0], lens)
+    np.add.at(want, ev[:, 1], lens)
+    got = y[rx.input_to_linear("v")]
+    assert np.abs(got - want).max() <= 1e-5 * want.max()
+    # transpose: the pattern is symmetric, so A^T = A here, diagonal kept first
+    A.val.copy_(torch.rand(A.non_zeros(), device="cuda"))
+    T = A.transpose()
+    assert T.row_ptr.is_cuda
+    assert abs(T.to_scipy() - A.to_scipy().T.tocsr()).max() == 0
+    assert torch.equal(T.col[T.row_ptr[:-1].long()], torch.arange(n, device="cuda", dtype=torch.int32))
