@@ -167,6 +167,68 @@ def test_patch_layout_encodes_exact_queries(oracle, name, patch):
     fv, x = MESHES[name]()
     nv = len(x)
     rx = RXMeshStatic(fv, nv, patch_size=patch, host_only=True)
+    check_layout(oracle, rx, fv, nv, patch)
+
+
+def random_mesh(rng):
+    """A torus or grid with faces removed (holes, several components),
+    some faces flipped, vertex ids permuted, faces shuffled, and a few
+    vertices in no face."""
+    if rng.random() < 0.5:
+        x, f = meshgen.torus(int(rng.integers(6, 14)), int(rng.integers(5, 12)))
+    else:
+        x, f = meshgen.plane(int(rng.integers(5, 13)), int(rng.integers(4, 12)))
+    f = np.asarray(f)
+    f = f[rng.random(len(f)) > rng.uniform(0.0, 0.35)]
+    flip = rng.random(len(f)) < rng.uniform(0.0, 0.15)
+    f[flip] = f[flip][:, ::-1]
+    f = f[rng.permutation(len(f))]
+    used = np.unique(f)
+    extra = int(rng.integers(0, 4))
+    perm = rng.permutation(len(used) + extra)
+    remap = np.full(int(f.max()) + 1, -1)
+    remap[used] = perm[:len(used)]
+    return np.ascontiguousarray(remap[f], np.int32), len(used) + extra
+
+
+def random_partition(rng, fv, nv):
+    """Face patches in random order (patches need not be connected), and
+    vertex owners picked at random among each vertex's face patches."""
+    nf = len(fv)
+    k = int(rng.integers(1, max(2, nf // 8)))
+    fp = rng.integers(0, k, nf)
+    fp[rng.permutation(nf)[:k]] = np.arange(k)          # no empty patch id
+    vp = np.full(nv, -1, np.int32)
+    for f in rng.permutation(nf):
+        for v in fv[f]:
+            if vp[v] < 0 or rng.random() < 0.3:
+                vp[v] = fp[f]
+    return fp.astype(np.int32), vp
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_meshes_and_partitions_encode_exact_queries(oracle, seed):
+    """Random holes, flips, vertex permutations and isolated vertices, built
+    with the BFS partitioner at three patch sizes and on a random
+    (disconnected) partition with random vertex owners: the arena decodes to
+    exactly the oracle's queries every time."""
+    from rxmesh_gb300 import RXMeshStatic
+    rng = np.random.default_rng(seed)
+    fv, nv = random_mesh(rng)
+    for patch in (16, 64, 512):
+        rx = RXMeshStatic(fv, nv, patch_size=patch, host_only=True)
+        check_layout(oracle, rx, fv, nv, patch)
+    fp, vp = random_partition(rng, fv, nv)
+    rx = RXMeshStatic(fv, nv, host_only=True, face_patch=fp, vertex_patch=vp)
+    got_fp, got_vp, _ = rx.partition()
+    assert np.array_equal(got_fp, fp)
+    infaces = np.zeros(nv, bool)
+    infaces[fv.reshape(-1)] = True
+    assert np.array_equal(got_vp[infaces], vp[infaces])
+    check_layout(oracle, rx, fv, nv, 4096)
+
+
+def check_layout(oracle, rx, fv, nv, patch):
     assert rx.get_num_faces() == len(fv) and rx.get_num_vertices() == nv
     ev_ref, _ = oracle.edges(fv)
     assert np.array_equal(rx.input_edges(), ev_ref)  # reference edge numbering
@@ -207,7 +269,11 @@ def test_patch_layout_encodes_exact_queries(oracle, name, patch):
     assert got_f == sorted_rows(off, val)
     _, fe_ref = oracle.edges(fv)
     assert np.array_equal(el[feq][np.argsort(fl)], fe_ref)          # FE in face-edge order
-    if rx.info["is_edge_manifold"]:  # EVDiamond is defined on edge-manifold meshes
+    directed = {(int(t[k]), int(t[(k + 1) % 3])) for t in np.asarray(fv) for k in range(3)}
+    oriented = len(directed) == 3 * len(fv)
+    # EVDiamond is defined (and the GPU query runs) on edge-manifold,
+    # consistently oriented meshes
+    if rx.info["is_edge_manifold"] and oriented:
         d = np.where(evd >= 0, vl[np.maximum(evd, 0)], -1)[np.argsort(el)]
         assert np.array_equal(d, oracle.ev_diamond(fv))
 
