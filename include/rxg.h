@@ -78,6 +78,12 @@ typedef struct rxg_mesh_info {
     int64_t ribbon_vertices;    /* sum over patches of not-owned local vertices */
     int64_t ribbon_faces;
     int64_t device_bytes;       /* device memory held by the mesh topology */
+    int32_t num_components;     /* face-connected components (get_num_components) */
+    int32_t is_oriented;        /* no edge traversed in one direction by two faces */
+    int32_t max_edge_incident_faces;  /* get_input_max_edge_incident_faces */
+    int32_t max_face_adjacent_faces;  /* get_input_max_face_adjacent_faces */
+    int32_t num_face_patches;   /* patches that own faces (the rest hold vertices in no face) */
+    int32_t lloyd_runs;         /* GPU patcher iterations (0: not used) */
 } rxg_mesh_info;
 
 /* Status name and the last error message of the calling thread. */

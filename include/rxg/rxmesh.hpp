@@ -338,6 +338,10 @@ class RXMeshStatic
     uint32_t get_input_max_valence() const { return (uint32_t)m_info.max_valence; }
     bool     is_closed() const { return m_info.is_closed != 0; }
     bool     is_edge_manifold() const { return m_info.is_edge_manifold != 0; }
+    bool     is_oriented() const { return m_info.is_oriented != 0; }
+    uint32_t get_num_components() const { return (uint32_t)m_info.num_components; }
+    uint32_t get_input_max_edge_incident_faces() const { return (uint32_t)m_info.max_edge_incident_faces; }
+    uint32_t get_input_max_face_adjacent_faces() const { return (uint32_t)m_info.max_face_adjacent_faces; }
     const rxg_mesh_info& info() const { return m_info; }
     const rxg_mesh*      handle() const { return m_mesh.get(); }
 

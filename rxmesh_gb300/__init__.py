@@ -197,6 +197,21 @@ class RXMeshStatic:
     def is_edge_manifold(self):
         return bool(self.info["is_edge_manifold"])
 
+    def is_oriented(self):
+        return bool(self.info["is_oriented"])
+
+    def get_num_components(self):
+        return self.info["num_components"]
+
+    def get_input_max_valence(self):
+        return self.info["max_valence"]
+
+    def get_input_max_edge_incident_faces(self):
+        return self.info["max_edge_incident_faces"]
+
+    def get_input_max_face_adjacent_faces(self):
+        return self.info["max_face_adjacent_faces"]
+
     def _n(self, elem):
         return (self.get_num_vertices(), self.get_num_edges(), self.get_num_faces())[elem]
 

@@ -29,7 +29,11 @@ class MeshInfo(ctypes.Structure):
                 ("is_edge_manifold", ctypes.c_int32), ("patch_faces", ctypes.c_int32),
                 ("max_local_vertices", ctypes.c_int32), ("max_local_edges", ctypes.c_int32),
                 ("max_local_faces", ctypes.c_int32), ("ribbon_vertices", ctypes.c_int64),
-                ("ribbon_faces", ctypes.c_int64), ("device_bytes", ctypes.c_int64)]
+                ("ribbon_faces", ctypes.c_int64), ("device_bytes", ctypes.c_int64),
+                ("num_components", ctypes.c_int32), ("is_oriented", ctypes.c_int32),
+                ("max_edge_incident_faces", ctypes.c_int32),
+                ("max_face_adjacent_faces", ctypes.c_int32), ("num_face_patches", ctypes.c_int32),
+                ("lloyd_runs", ctypes.c_int32)]
 
 
 class CSR(ctypes.Structure):

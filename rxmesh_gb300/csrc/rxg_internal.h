@@ -97,6 +97,7 @@ struct Mesh
     std::vector<int8_t>  vbnd;  // 1 for a boundary vertex, linear order
     int32_t              num_face_patches = 0, num_components = 0;
     int32_t              lloyd_runs = 0;  // GPU patcher iterations (0: not used)
+    int32_t              max_edge_faces = 0, max_face_faces = 0;
 
     DeviceTopo d;
 

@@ -184,6 +184,12 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
         valence[M.ev_in[2 * e + 1]]++;
     }
     for (int64_t v = 0; v < nv; ++v) M.max_valence = std::max<int64_t>(M.max_valence, valence[v]);
+    for (int64_t e = 0; e < ne; ++e) M.max_edge_faces = std::max(M.max_edge_faces, ef_off[e + 1] - ef_off[e]);
+    for (int64_t f = 0; f < nf; ++f) {
+        int32_t n = 0;
+        for (int k = 0; k < 3; ++k) n += ef_off[fe[3 * f + k] + 1] - ef_off[fe[3 * f + k]] - 1;
+        M.max_face_faces = std::max(M.max_face_faces, n);
+    }
 
     // ---- face-connected components (through shared edges) -------------
     const bool           gpu_partitioning = gpu_patcher && !part;
@@ -803,6 +809,12 @@ rxg_status rxg_mesh_get_info(const rxg_mesh* h, rxg_mesh_info* info)
     info->ribbon_vertices    = M.ribbon_v;
     info->ribbon_faces       = M.ribbon_f;
     info->device_bytes       = M.device_bytes;
+    info->num_components     = M.num_components;
+    info->is_oriented        = M.oriented;
+    info->max_edge_incident_faces = M.max_edge_faces;
+    info->max_face_adjacent_faces = M.max_face_faces;
+    info->num_face_patches   = M.num_face_patches;
+    info->lloyd_runs         = M.lloyd_runs;
     return RXG_OK;
 }
 

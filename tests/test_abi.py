@@ -230,6 +230,15 @@ def test_random_meshes_and_partitions_encode_exact_queries(oracle, seed):
 
 def check_layout(oracle, rx, fv, nv, patch):
     assert rx.get_num_faces() == len(fv) and rx.get_num_vertices() == nv
+    # mesh properties (rxmesh.h:134-220) against the oracle's adjacency
+    ef_off, _ = oracle.ef(fv)
+    ff_off, _ = oracle.ff(fv)
+    assert rx.get_input_max_edge_incident_faces() == np.diff(ef_off).max()
+    assert rx.get_input_max_face_adjacent_faces() == np.diff(ff_off).max()
+    from oracle.patcher import face_graph
+    assert rx.get_num_components() == len(np.unique(face_graph(fv)[2]))
+    directed = {(int(t[k]), int(t[(k + 1) % 3])) for t in np.asarray(fv) for k in range(3)}
+    assert rx.is_oriented() == (len(directed) == 3 * len(fv))
     ev_ref, _ = oracle.edges(fv)
     assert np.array_equal(rx.input_edges(), ev_ref)  # reference edge numbering
     vl, el, fl = rx.linear_to_input("v"), rx.linear_to_input("e"), rx.linear_to_input("f")
