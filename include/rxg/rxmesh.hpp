@@ -309,6 +309,26 @@ class RXMeshStatic
     {
         check(rxg_mesh_save_patch_file(m_mesh.get(), filename.c_str()));
     }
+    // export_obj (rxmesh_static.inl:366-397): vertices in linear order from
+    // coords (linear order), faces in linear order over linear vertex ids
+    void export_obj(const std::string& filename, const DenseMatrix<double>& coords) const
+    {
+        const std::vector<double>  x   = coords.to_host();
+        const std::vector<int32_t> fl  = linear_to_input(RXG_ELEM_FACE);
+        const std::vector<int32_t> vl  = linear_to_input(RXG_ELEM_VERTEX);
+        if ((int64_t)x.size() != 3 * m_info.num_vertices)
+            throw Error(RXG_ERR_INVALID, "one position per vertex expected");
+        std::vector<int32_t> vi2l(vl.size());
+        for (size_t l = 0; l < vl.size(); ++l) vi2l[(size_t)vl[l]] = (int32_t)l;
+        std::FILE* fp = std::fopen(filename.c_str(), "w");
+        if (!fp) throw Error(RXG_ERR_INVALID, "cannot create " + filename);
+        for (size_t v = 0; v < vl.size(); ++v)
+            std::fprintf(fp, "v %.17g %.17g %.17g\n", x[3 * v], x[3 * v + 1], x[3 * v + 2]);
+        for (int32_t f : fl)
+            std::fprintf(fp, "f %d %d %d\n", vi2l[(size_t)m_fv[3 * (size_t)f]] + 1,
+                         vi2l[(size_t)m_fv[3 * (size_t)f + 1]] + 1, vi2l[(size_t)m_fv[3 * (size_t)f + 2]] + 1);
+        if (std::fclose(fp) != 0) throw Error(RXG_ERR_INVALID, "write to " + filename + " failed");
+    }
     // get_boundary_vertices (rxmesh_static.inl:281-323): 1 for the ends of
     // edges with fewer than two faces, linear order
     std::vector<int8_t> get_boundary_vertices() const
@@ -412,6 +432,7 @@ class RXMeshStatic
     };
     std::unique_ptr<rxg_mesh, Del> m_mesh;
     std::vector<int64_t>           m_region_faces, m_region_vertices;  // cumulative, per file
+    std::vector<int32_t>           m_fv;  // the input faces (export_obj)
 
     void create(const std::vector<int32_t>& flat, int64_t nv, const std::string& patcher_file,
                 uint32_t patch_size, bool host_only, bool gpu_patcher)
@@ -420,6 +441,7 @@ class RXMeshStatic
         const int32_t flags =
             (host_only ? RXG_MESH_HOST_ONLY : 0) | (gpu_patcher ? RXG_MESH_GPU_PATCHER : 0);
         const int64_t nf = (int64_t)flat.size() / 3;
+        m_fv             = flat;
         if (patcher_file.empty())
             check(rxg_mesh_create_ex(flat.data(), nf, nv, (int32_t)patch_size, flags, &m));
         else

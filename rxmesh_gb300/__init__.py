@@ -162,6 +162,20 @@ class RXMeshStatic:
     def get_num_faces(self):
         return self.info["num_faces"]
 
+    def export_obj(self, path, xyz):
+        """RXMeshStatic::export_obj (rxmesh_static.inl:366-397): vertices in
+        linear order from xyz (linear order, (nv, 3), tensor or array), faces
+        in linear order over linear vertex ids."""
+        x = xyz.detach().cpu().numpy() if hasattr(xyz, "detach") else np.asarray(xyz)
+        x = x.reshape(-1, 3)
+        if len(x) != self.get_num_vertices():
+            raise ValueError("one position per vertex expected")
+        vi2l = self.input_to_linear("v")
+        faces = vi2l[self._fv[self.linear_to_input("f")]] + 1
+        with open(path, "w") as fh:
+            fh.writelines("v %.17g %.17g %.17g\n" % tuple(p) for p in x)
+            fh.writelines("f %d %d %d\n" % tuple(t) for t in faces)
+
     def get_boundary_vertices(self, stream=None):
         """1 for every vertex on an edge with fewer than two faces
         (get_boundary_vertices, rxmesh_static.inl:281-323): int8 in linear

@@ -143,7 +143,7 @@ static int host_checks(const char* dir)
     return 0;
 }
 
-static int gpu_checks()
+static int gpu_checks(const char* dir)
 {
     std::vector<std::vector<uint32_t>> fv;
     std::vector<std::vector<double>>   xyz;
@@ -190,6 +190,15 @@ static int gpu_checks()
         const int32_t* d = &dv[4 * e];
         REQUIRE(d[1] >= 0 && d[3] >= 0 && d[1] != d[3]);
         REQUIRE(d[1] != d[0] && d[1] != d[2] && d[3] != d[0] && d[3] != d[2]);
+    }
+
+    // export_obj, read back: the same mesh in linear numbering
+    if (dir) {
+        const std::string path = std::string(dir) + "/torus_out.obj";
+        rx.export_obj(path, rx.get_input_vertex_coordinates());
+        RXMeshStatic back(path, "", 512, true);
+        REQUIRE(back.get_num_vertices() == nv && back.get_num_faces() == rx.get_num_faces());
+        REQUIRE(back.get_num_edges() == rx.get_num_edges() && back.is_closed());
     }
 
     // MCF system + Jacobi PCG: |A X - B| / |B| small
@@ -351,7 +360,8 @@ int main(int argc, char** argv)
 {
     const bool gpu = argc > 1 && std::strcmp(argv[1], "gpu") == 0;
     try {
-        const int rc = gpu ? gpu_checks() : host_checks(argc > 2 ? argv[2] : nullptr);
+        const char* dir = argc > 2 ? argv[2] : nullptr;
+        const int   rc  = gpu ? gpu_checks(dir) : host_checks(dir);
         if (rc) return rc;
     } catch (const Error& e) {
         std::printf("FAILED: exception %s\n", e.what());

@@ -47,6 +47,7 @@ def test_facade_host(example, tmp_path):
 
 
 @pytest.mark.gpu
-def test_facade_gpu(example):
-    r = subprocess.run([example, "gpu"], capture_output=True, text=True, timeout=600)
+def test_facade_gpu(example, tmp_path):
+    r = subprocess.run([example, "gpu", str(tmp_path)], capture_output=True, text=True,
+                       timeout=600)
     assert r.returncode == 0 and r.stdout.strip().endswith("OK"), r.stdout + r.stderr

@@ -244,3 +244,18 @@ def test_multi_file_regions(tmp_path):
     assert rx.get_region_label("v").tolist() == [0, 0, 0, 0, 1, 1, 1]
     assert sorted(rx.get_region_label("e").tolist()) == [0] * 5 + [1] * 3
     assert rx.input_vertex_coordinates.shape == (7, 3)
+
+
+def test_export_obj_round_trip(tmp_path):
+    """export_obj (rxmesh_static.inl:366-397): linear numbering; reading the
+    file back gives the same mesh under the linear-to-input map."""
+    from rxmesh_gb300 import RXMeshStatic
+    from rxmesh_gb300.meshgen import read_obj
+    g = golden("sphere3")
+    rx = RXMeshStatic(g["fv"], len(g["xyz"]), patch_size=64, host_only=True)
+    vl = rx.linear_to_input("v")
+    path = tmp_path / "out.obj"
+    rx.export_obj(str(path), g["xyz"][vl])
+    x, f = read_obj(str(path))
+    assert np.array_equal(x, g["xyz"][vl])
+    assert np.array_equal(vl[f], g["fv"][rx.linear_to_input("f")])
