@@ -142,6 +142,8 @@ class DeviceArray
     size_t m_n   = 0;
 };
 
+class RXMeshStatic;
+
 // rows x cols dense matrix in device memory, row-major (one row per mesh
 // element, as every rxg call expects).
 template <typename T>
@@ -155,6 +157,12 @@ class DenseMatrix
         (void)where;
         m_d.fill_zero();
         check_cuda(cudaStreamSynchronize(nullptr), "cudaStreamSynchronize");
+    }
+    // the reference's DenseMatrix(rx, rows, cols, location)
+    // (matrix/dense_matrix.h); the mesh is not needed here
+    DenseMatrix(const RXMeshStatic&, int64_t rows, int64_t cols, locationT where = DEVICE)
+        : DenseMatrix(rows, cols, where)
+    {
     }
     int64_t  rows() const { return m_rows; }
     int64_t  cols() const { return m_cols; }

@@ -204,7 +204,7 @@ static int gpu_checks(const char* dir)
     // MCF system + Jacobi PCG: |A X - B| / |B| small
     const double        dt = 1e-3;
     SparseMatrix<double> A(rx);
-    DenseMatrix<double>  B(nv, 3), X(nv, 3), AX(nv, 3);
+    DenseMatrix<double>  B(rx, nv, 3), X(rx, nv, 3), AX(nv, 3);  // both constructor forms
     mcf_assemble(rx, dt, rx.get_input_vertex_coordinates(), A, B);
     PCGSolver<double> solver(A, 3, 2000, 1e-20, 0.0);
     solver.pre_solve(B, X);
