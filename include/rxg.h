@@ -17,7 +17,7 @@
  *   - linear ids: patch-ordered ids, owned elements of patch 0 first, then
  *     patch 1, ... (RXMesh's linear_id, include/rxmesh/context.h:299-331).
  * Queries and per-element arrays passed to kernels use linear ids; the
- * rxg_mesh_*_map calls give the permutations and rxg_permute applies them.
+ * rxg_mesh_linear_to_input gives the permutation and rxg_permute applies it.
  */
 #ifndef RXG_H
 #define RXG_H

@@ -46,6 +46,10 @@ inline void check(rxg_status s)
         throw Error(s, std::string(rxg_status_string(s)) + ": " + rxg_last_error());
 }
 
+// synchronise s and throw if a bounded device-side wait gave up
+// (rxg_device_check)
+inline void device_check(cudaStream_t s = nullptr) { check(rxg_device_check(s)); }
+
 inline void check_cuda(cudaError_t e, const char* what)
 {
     if (e != cudaSuccess)
@@ -311,6 +315,45 @@ class RXMeshStatic
                 for (size_t e = 0; e < out.size(); ++e) out[e] = label_of(m_region_vertices, ev[2 * e]);
         }
         return out;
+    }
+    // a given partition (rxg_mesh_create_partitioned): face_patch, one patch
+    // id per face; vertex and edge owners by RXMesh's lowest-patch rule
+    RXMeshStatic(std::vector<std::vector<uint32_t>>& fv, const std::vector<int32_t>& face_patch,
+                 bool host_only = false)
+    {
+        std::vector<int32_t> flat;
+        int64_t              nv = 0;
+        for (const auto& f : fv) {
+            if (f.size() != 3) throw Error(RXG_ERR_INVALID, "only triangle faces are supported");
+            for (uint32_t v : f) {
+                flat.push_back((int32_t)v);
+                nv = std::max<int64_t>(nv, (int64_t)v + 1);
+            }
+        }
+        if (face_patch.size() != fv.size()) throw Error(RXG_ERR_INVALID, "one patch id per face");
+        rxg_mesh* m = nullptr;
+        check(rxg_mesh_create_partitioned(flat.data(), (int64_t)fv.size(), nv, face_patch.data(),
+                                          nullptr, nullptr, -1, host_only ? RXG_MESH_HOST_ONLY : 0,
+                                          &m));
+        m_mesh.reset(m);
+        m_fv = flat;
+        check(rxg_mesh_get_info(m, &m_info));
+    }
+    // per-element DenseMatrix between input and linear order on the device
+    // (rxg_permute; Attribute::from_matrix / to_matrix)
+    template <typename T>
+    void to_linear(int32_t elem, const DenseMatrix<T>& input_order, DenseMatrix<T>& linear,
+                   cudaStream_t s = nullptr) const
+    {
+        check(rxg_permute(handle(), elem, 1, dtype_of<T>::value, (int32_t)input_order.cols(),
+                          input_order.data(), linear.data(), s));
+    }
+    template <typename T>
+    void to_input(int32_t elem, const DenseMatrix<T>& linear, DenseMatrix<T>& input_order,
+                  cudaStream_t s = nullptr) const
+    {
+        check(rxg_permute(handle(), elem, 0, dtype_of<T>::value, (int32_t)linear.cols(),
+                          linear.data(), input_order.data(), s));
     }
     // RXMesh::save (rxmesh.h:326-329): the partition as a patcher file
     void save(const std::string& filename) const
@@ -920,6 +963,24 @@ class MeshBatch
     }
     int32_t num_meshes() const { return m_n; }
     int64_t num_vertices() const { return m_total_vertices; }
+    // time the launch shapes on a copy of xyz and keep the fastest
+    // (rxg_batch_autotune); returns the chosen threads per CTA
+    int32_t autotune(const DenseMatrix<double>& xyz, double dt, int32_t nsteps = 1,
+                     double tol = 1e-6, int32_t max_iter = 5000, cudaStream_t s = nullptr)
+    {
+        int32_t threads = 0, per_sm = 0;
+        float   ms      = 0.f;
+        check(rxg_batch_autotune(m_b.get(), dt, nsteps, tol, max_iter, xyz.data(), &threads,
+                                 &per_sm, &ms, s));
+        return threads;
+    }
+    // the union mesh of all meshes (queries and numbering); owned by the batch
+    const rxg_mesh* mesh() const
+    {
+        const rxg_mesh* m = nullptr;
+        check(rxg_batch_mesh(m_b.get(), &m));
+        return m;
+    }
 
    private:
     struct Del

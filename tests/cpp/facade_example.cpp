@@ -85,6 +85,15 @@ static int host_checks(const char* dir)
         threw = e.status == RXG_ERR_INVALID;
     }
     REQUIRE(threw);
+    {
+        // a given partition: two halves of the faces by input order
+        std::vector<int32_t> half(fv.size());
+        for (size_t f = 0; f < fv.size(); ++f) half[f] = f < fv.size() / 2 ? 0 : 1;
+        RXMeshStatic         two(fv, half, true);
+        std::vector<int32_t> fp, vp, ep;
+        two.partition(fp, vp, ep);
+        REQUIRE(two.get_num_patches() == 2 && fp == half);
+    }
     if (dir) {
         // save the partition, load it back: the same patches and numbering
         const std::string path = std::string(dir) + "/torus_patches";
@@ -190,6 +199,20 @@ static int gpu_checks(const char* dir)
         const int32_t* d = &dv[4 * e];
         REQUIRE(d[1] >= 0 && d[3] >= 0 && d[1] != d[3]);
         REQUIRE(d[1] != d[0] && d[1] != d[2] && d[3] != d[0] && d[3] != d[2]);
+    }
+
+    // input order -> linear order on the device: the coordinates that
+    // add_vertex_coordinates placed; and back
+    {
+        std::vector<double> hin;
+        for (const auto& p : xyz) hin.insert(hin.end(), p.begin(), p.end());
+        DenseMatrix<double> xin(nv, 3), xlin(nv, 3), xback(nv, 3);
+        xin.from_host(hin);
+        rx.to_linear(RXG_ELEM_VERTEX, xin, xlin);
+        rx.to_input(RXG_ELEM_VERTEX, xlin, xback);
+        device_check();
+        REQUIRE(xlin.to_host() == rx.get_input_vertex_coordinates().to_host());
+        REQUIRE(xback.to_host() == hin);
     }
 
     // export_obj, read back: the same mesh in linear numbering
