@@ -657,14 +657,13 @@ struct CGSolver
     virtual void pre_solve(const DenseMatrix<T>&, DenseMatrix<T>&, cudaStream_t = nullptr) {}
     virtual void solve(const DenseMatrix<T>& B, DenseMatrix<T>& X, cudaStream_t s = nullptr)
     {
-        rxg_solver_opts o;
-        o.max_iter   = m_max_iter;
-        o.abs_tol    = (double)m_abs_tol;
-        o.rel_tol    = (double)m_rel_tol;
-        o.precond    = precond();
-        rxg_csr    c = A->csr();
-        rxg_status st = rxg_cg_solve(&c, m_nc, B.data(), X.data(), &o, &m_stats, s);
-        if (st != RXG_ERR_NOT_CONVERGED) check(st);
+        run(B, X, s, false);
+    }
+    // the same solve with no device allocation (rxg_cg_solve_noalloc: a
+    // static scratch array, at most 131,072 rows; calls must not overlap)
+    void solve_noalloc(const DenseMatrix<T>& B, DenseMatrix<T>& X, cudaStream_t s = nullptr)
+    {
+        run(B, X, s, true);
     }
     virtual std::string name() { return "CG"; }
     int                 iter_taken() const { return m_stats.iters; }
@@ -673,6 +672,19 @@ struct CGSolver
     bool                converged() const { return m_stats.converged != 0; }
 
    protected:
+    void run(const DenseMatrix<T>& B, DenseMatrix<T>& X, cudaStream_t s, bool noalloc)
+    {
+        rxg_solver_opts o;
+        o.max_iter    = m_max_iter;
+        o.abs_tol     = (double)m_abs_tol;
+        o.rel_tol     = (double)m_rel_tol;
+        o.precond     = precond();
+        rxg_csr    c  = A->csr();
+        rxg_status st = noalloc
+                            ? rxg_cg_solve_noalloc(&c, m_nc, B.data(), X.data(), &o, &m_stats, s)
+                            : rxg_cg_solve(&c, m_nc, B.data(), X.data(), &o, &m_stats, s);
+        if (st != RXG_ERR_NOT_CONVERGED) check(st);
+    }
     virtual int32_t  precond() const { return 0; }
     SparseMatrix<T>* A;
     int              m_nc, m_max_iter;
