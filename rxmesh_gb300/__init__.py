@@ -70,6 +70,8 @@ class RXMeshStatic:
         self._fv = f
         h = ctypes.c_void_p()
         flags = 1 if host_only else 0
+        if sum(x is not None and x is not False for x in (patcher_file, face_patch, gpu_patcher)) > 1:
+            raise ValueError("give at most one of patcher_file, face_patch and gpu_patcher")
         if patcher_file is not None:
             check(L.rxg_mesh_create_from_patch_file(f.ctypes.data, f.shape[0], nv,
                                                     os.fsencode(patcher_file), flags,

@@ -190,6 +190,10 @@ def test_bad_partitions_and_files(tmp_path):
         RXMeshStatic(t["fv"], len(t["xyz"]), host_only=True, patcher_file=str(path))
     with pytest.raises(RXGError):
         RXMeshStatic(fv, nv, host_only=True, patcher_file=str(tmp_path / "missing"))
+    with pytest.raises(ValueError):  # two partition sources
+        RXMeshStatic(fv, nv, host_only=True, patcher_file=str(path), face_patch=fp)
+    with pytest.raises(ValueError):
+        RXMeshStatic(fv, nv, host_only=True, face_patch=fp, gpu_patcher=True)
 
 
 @pytest.mark.parametrize("P", [64, 512])
