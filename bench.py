@@ -242,6 +242,17 @@ def cpu_model():
     return "%s (%s)" % (name or "unknown", platform.machine())
 
 
+def max_over_ranks(torch, ms, device):
+    """The job's time: the slowest rank's, on every rank (one all-reduce of
+    one value; 1 rank: unchanged)."""
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     """--impl reference: the CPU implementation of the sweep on all host cores."""
     import multiprocessing as mp
@@ -725,10 +736,7 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     per, ms, clocks, _, _ = run_sweep(args, torch, rx, xl, (V, E, F))
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(torch, ms, "cuda")
     cb = canonical_bytes(V, E, F)
     sweep_bytes = sum(cb.values())
     value = world * sweep_bytes / (ms * 1e-3) / 1e9
