@@ -263,3 +263,26 @@ def test_export_obj_round_trip(tmp_path):
     x, f = read_obj(str(path))
     assert np.array_equal(x, g["xyz"][vl])
     assert np.array_equal(vl[f], g["fv"][rx.linear_to_input("f")])
+
+
+@pytest.mark.parametrize("name", ["sphere3", "torus"])
+def test_reference_partitions_have_the_lloyd_properties(name):
+    """RXMesh's saved Lloyd partitions satisfy what the restatement in
+    oracle/patcher.py guarantees: every region at most patch_size faces and
+    connected through shared edges."""
+    from oracle.patcher import face_graph
+    g = golden(name)
+    ref = decode(g["patcher_file"].tobytes())
+    fp = ref["face_patch"]
+    assert np.bincount(fp).max() <= ref["patch_size"]
+    off, val, _ = face_graph(g["fv"])
+    for p in range(ref["num_patches"]):
+        faces = np.nonzero(fp == p)[0]
+        seen, stack = {int(faces[0])}, [int(faces[0])]
+        while stack:
+            f = stack.pop()
+            for h in val[off[f]:off[f + 1]]:
+                if fp[h] == p and int(h) not in seen:
+                    seen.add(int(h))
+                    stack.append(int(h))
+        assert len(seen) == len(faces), p
