@@ -155,6 +155,31 @@ def ev_diamond(fv):
     return out.reshape(-1, 4)
 
 
+def ee(fv):
+    """EE rows (ne, 4) in input edge ids, restating e_e_manifold
+    (include/rxmesh/kernels/rxmesh_queries.cuh:269-340) on an edge-manifold,
+    consistently oriented mesh: for the face that traverses edge e in
+    direction d (0: from its first vertex, as numbered by edges()), slot
+    2d holds the face's next edge and slot 2d+1 its previous edge; -1 where
+    e has no such face.  (The reference computes the previous edge's index
+    as (cur - 1) % 3, which is -1 for the first edge in C++; the previous
+    edge is (cur + 2) % 3.)  Walks each edge's faces."""
+    f = np.asarray(fv)
+    ev, fe = edges(fv)
+    ne = len(ev)
+    faces_of = [[] for _ in range(ne)]
+    for fi in range(len(f)):
+        for k in range(3):
+            faces_of[fe[fi][k]].append((fi, k))
+    out = np.full((ne, 4), -1, np.int32)
+    for e in range(ne):
+        for fi, k in faces_of[e]:
+            d = 0 if f[fi][k] == ev[e][0] else 1
+            out[e, 2 * d] = fe[fi][(k + 1) % 3]
+            out[e, 2 * d + 1] = fe[fi][(k + 2) % 3]
+    return out
+
+
 def vertex_normals(fv, xyz, weighting=0):
     """weighting 0 = Max weights (vertex_normal_ref.h), 1 = area weights."""
     f = _fv(fv)

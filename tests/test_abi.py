@@ -280,11 +280,18 @@ def check_layout(oracle, rx, fv, nv, patch):
     assert np.array_equal(el[feq][np.argsort(fl)], fe_ref)          # FE in face-edge order
     directed = {(int(t[k]), int(t[(k + 1) % 3])) for t in np.asarray(fv) for k in range(3)}
     oriented = len(directed) == 3 * len(fv)
-    # EVDiamond is defined (and the GPU query runs) on edge-manifold,
+    # EVDiamond and EE are defined (and run on the GPU) on edge-manifold,
     # consistently oriented meshes
     if rx.info["is_edge_manifold"] and oriented:
         d = np.where(evd >= 0, vl[np.maximum(evd, 0)], -1)[np.argsort(el)]
         assert np.array_equal(d, oracle.ev_diamond(fv))
+        # EE composed from the FV / FE / EV rows (the same torch code the GPU runs)
+        import torch
+        from rxmesh_gb300 import edge_edge_slots
+        ee = edge_edge_slots(torch.from_numpy(fvq), torch.from_numpy(feq), torch.from_numpy(evq),
+                             ne).numpy().reshape(-1, 4)
+        got = np.where(ee >= 0, el[np.maximum(ee, 0)], -1)[np.argsort(el)]
+        assert np.array_equal(got, oracle.ee(fv))
 
 
 def test_ev_diamond_needs_consistent_orientation():

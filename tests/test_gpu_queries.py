@@ -298,3 +298,23 @@ def test_boundary_vertices_device():
     b = rx.get_boundary_vertices()
     assert b.is_cuda and int(b.sum().item()) == 98
     assert np.array_equal(b.cpu().numpy(), host.get_boundary_vertices())
+
+
+@pytest.mark.parametrize("name", ["torus64", "icosphere4", "plane", "sphere3", "plane_5"])
+def test_edge_edge_query(oracle, name):
+    """Op.EE (e_e_manifold, rxmesh_queries.cuh:269-340) on the GPU, composed
+    from the FV / FE / EV queries, against the oracle; refused on a mesh
+    whose faces are not consistently oriented."""
+    from rxmesh_gb300 import Op, RXGError, RXMeshStatic
+    x, f = MESHES[name]()
+    rx = RXMeshStatic(f, len(x), patch_size=64)
+    _, ee = rx.query(Op.EE)
+    assert ee.is_cuda
+    el = rx.linear_to_input("e")
+    ee = ee.cpu().numpy().reshape(-1, 4)
+    got = np.where(ee >= 0, el[np.maximum(ee, 0)], -1)[np.argsort(el)]
+    assert np.array_equal(got, oracle.ee(f))
+    g = np.array(f, np.int32).copy()
+    g[3] = g[3][::-1]
+    with pytest.raises(RXGError):
+        RXMeshStatic(g, len(x), patch_size=64).query(Op.EE)
