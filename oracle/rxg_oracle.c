@@ -1,8 +1,8 @@
 /*
  * rxg_oracle.c -- CPU restatement of RXMesh's hot-path arithmetic.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the parity checker for the CUDA
- * library in rxmesh_gb300/csrc.  Only tests/, __graft_entry__.smoke() and the
+ * TEST INFRASTRUCTURE ONLY.  The CUDA library in rxmesh_gb300/csrc is tested
+ * for parity against this file.  Only tests/, __graft_entry__.smoke() and the
  * cpu_baseline / --impl reference legs of bench.py may load it.  The product
  * path never calls it and has no CPU fallback.
  *

@@ -198,9 +198,9 @@ def test_bad_partitions_and_files(tmp_path):
 
 @pytest.mark.parametrize("P", [64, 512])
 def test_lloyd_restatement_gives_valid_partitions(P):
-    """The oracle's restatement of the Lloyd patcher (the GPU patcher's
-    checker): every face in a region of at most P faces, at least one region
-    per component, and the partition builds."""
+    """The oracle's restatement of the Lloyd patcher (which the GPU patcher
+    must equal): every face in a region of at most P faces, at least one
+    region per component, and the partition builds."""
     from conftest import edge_case_meshes
     from oracle.patcher import face_graph, lloyd_partition
     from rxmesh_gb300 import RXMeshStatic
