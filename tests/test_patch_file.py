@@ -286,3 +286,19 @@ def test_reference_partitions_have_the_lloyd_properties(name):
                     seen.add(int(h))
                     stack.append(int(h))
         assert len(seen) == len(faces), p
+
+
+def test_partition_argument_checks():
+    from rxmesh_gb300 import RXGError, RXMeshStatic
+    _, f = meshgen.icosphere(1)
+    f = np.asarray(f)
+    nv = int(f.max()) + 1
+    with pytest.raises(ValueError):  # one id per face
+        RXMeshStatic(f, nv, host_only=True, face_patch=np.zeros(len(f) - 1, np.int32))
+    with pytest.raises(ValueError):  # one owner per vertex
+        RXMeshStatic(f, nv, host_only=True, face_patch=np.zeros(len(f), np.int32),
+                     vertex_patch=np.zeros(nv - 1, np.int32))
+    with pytest.raises(RXGError):    # patch id beyond the face count
+        RXMeshStatic(f, nv, host_only=True, face_patch=np.full(len(f), len(f), np.int32))
+    rx = RXMeshStatic(f, nv, host_only=True, face_patch=np.zeros(len(f), np.int32))
+    assert rx.get_num_patches() == 1 and rx.info["patch_faces"] == len(f)
