@@ -287,7 +287,8 @@ typedef struct rxg_solver_stats {
  * Solve A X = B (nc columns as one long vector), X in/out as the initial
  * guess.  CGSolver / PCGSolver::pre_solve+solve (cg_solver.h:37-125,
  * pcg_solver.h:34-144, iterative_solver.h:52-58).  All scalars stay on the
- * device; the host reads only the final statistics.  Device arrays only.
+ * device; the host reads only the final statistics.  Device arrays only
+ * (A's row_ptr, col and val, B and X; a host array returns RXG_ERR_INVALID).
  */
 rxg_status rxg_cg_solve(const rxg_csr* A, int32_t nc, const void* B, void* X,
                         const rxg_solver_opts* opts, rxg_solver_stats* stats,
@@ -306,9 +307,11 @@ rxg_status rxg_cg_solve(const rxg_csr* A, int32_t nc, const void* B, void* X,
  * RXG_ERR_INVALID with a message (use rxg_cg_solve).
  * The first call on a device looks up the array's device address (once per
  * device, with that device current); make that first call before any stream
- * capture.  All calls share the one array: calls that overlap on the GPU
- * (other streams, other host threads) race and must be serialised by the
- * caller.  Device arrays only.
+ * capture.  Every call reads the solver statistics back to the host, so it
+ * returns only after its work on `stream` has finished.  All calls share the
+ * one array: calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller.  Device arrays only
+ * (A's row_ptr, col and val, B and X; a host array returns RXG_ERR_INVALID).
  */
 rxg_status rxg_cg_solve_noalloc(const rxg_csr* A, int32_t nc, const void* B,
                                 void* X, const rxg_solver_opts* opts,

@@ -116,7 +116,7 @@ __device__ __forceinline__ bool grid_sum_core(GridSum& g, RedSmem& r, Post post)
                     break;
                 }
                 if (it > kWaitLimit) {
-                    atomicOr(g.err, DEVERR_GRID_TIMEOUT);
+                    if (g.err) atomicOr(g.err, DEVERR_GRID_TIMEOUT);
                     atomicExch(g.bar + 1, 1u);
                     ok = 0;
                     break;

@@ -158,8 +158,16 @@ void  lazy_free(Mesh* m);
 rxg_status launch_query(const Mesh* m, int op, int32_t* d_off, int32_t* d_val,
                         cudaStream_t s);
 
-// device error word (bounded waits)
+// Per-device caches are arrays indexed by the CUDA device ordinal.
+constexpr int kMaxDevices = 64;
+
+// device error word (bounded waits) of the current device; NULL when there
+// is no current device
 int* device_error_word();
+// multiprocessor count of the current device (cached per device)
+int device_sm_count();
+// current device ordinal, clamped to [0, kMaxDevices)
+int current_device();
 rxg_status check_device_error(cudaStream_t s);
 
 }  // namespace rxg

@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(kQT2) k_oriented_vv(const PatchHdr* __restrict
             ++pos;
             cur = nxt;
         }
-        if (bad || nvis != k || pos != olen) atomicOr(err, DEVERR_NONMANIFOLD);
+        if ((bad || nvis != k || pos != olen) && err) atomicOr(err, DEVERR_NONMANIFOLD);
         out_bnd[h.v_base + v] = is_b ? 1 : 0;
     }
 }
@@ -648,17 +648,7 @@ __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
 // host side: CG launch
 // ---------------------------------------------------------------------
 
-static int num_sms()
-{
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
-    return sms;
-}
+static int num_sms() { return device_sm_count(); }
 
 // CTA size of the persistent CG kernel: RXG_CG_THREADS=256|512|1024 (default 512)
 static int cg_threads()
@@ -675,8 +665,10 @@ static int cg_threads()
 template <typename T, int NC, bool PC, int BT>
 static int cg_grid_bt(int64_t n)
 {
-    static int per_sm = -1;
-    if (per_sm < 0) {
+    // resident CTAs per SM, per device (0: not looked up yet)
+    static int per_sm_dev[kMaxDevices] = {0};
+    int&       per_sm = per_sm_dev[current_device()];
+    if (per_sm <= 0) {
         // the grid must fit whichever variant runs (cooperative launch)
         int p1 = 0, p4 = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p1, k_cg<T, NC, PC, BT, 1>, BT, 0) !=
@@ -1052,8 +1044,9 @@ static int cgm_threads()
 template <typename T, int BT>
 static int cgm_grid_bt(int64_t n)
 {
-    static int per_sm = -1;
-    if (per_sm < 0) {
+    static int per_sm_dev[kMaxDevices] = {0};
+    int&       per_sm = per_sm_dev[current_device()];
+    if (per_sm <= 0) {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cgm<T, BT>, BT, 0) != cudaSuccess)
             per_sm = 1;
         per_sm = std::max(1, std::min(per_sm, 2048 / BT));
@@ -1332,6 +1325,11 @@ rxg_status rxg_spmm(const rxg_csr* A, int32_t nc, const void* X, void* Y, void* 
         set_error("rxg_spmm: bad argument");
         return RXG_ERR_INVALID;
     }
+    if (!is_device_ptr(X) || !is_device_ptr(Y) || !is_device_ptr(A->val) ||
+        !is_device_ptr(A->row_ptr) || !is_device_ptr(A->col)) {
+        set_error("rxg_spmm: A (row_ptr, col, val), X and Y must be device arrays");
+        return RXG_ERR_INVALID;
+    }
     if (A->dtype == RXG_F64)
         return spmm_launch<double, double, double>(nc, A->n, A->row_ptr, A->col, (const double*)A->val,
                                                    (const double*)X, (const double*)nullptr,
@@ -1348,8 +1346,9 @@ rxg_status rxg_cg_solve(const rxg_csr* A, int32_t nc, const void* B, void* X,
         set_error("rxg_cg_solve: bad argument");
         return RXG_ERR_INVALID;
     }
-    if (!is_device_ptr(B) || !is_device_ptr(X) || !is_device_ptr(A->val)) {
-        set_error("rxg_cg_solve: A, B and X must be device arrays");
+    if (!is_device_ptr(B) || !is_device_ptr(X) || !is_device_ptr(A->val) ||
+        !is_device_ptr(A->row_ptr) || !is_device_ptr(A->col)) {
+        set_error("rxg_cg_solve: A (row_ptr, col, val), B and X must be device arrays");
         return RXG_ERR_INVALID;
     }
     cudaStream_t s  = S_(stream);
@@ -1578,8 +1577,9 @@ extern "C" rxg_status rxg_cg_solve_noalloc(const rxg_csr* A, int32_t nc, const v
                   (long long)A->n, nc, (long long)kNoAllocMaxRows, kNoAllocMaxCols);
         return RXG_ERR_INVALID;
     }
-    if (!is_device_ptr(B) || !is_device_ptr(X) || !is_device_ptr(A->val)) {
-        set_error("rxg_cg_solve_noalloc: A, B and X must be device arrays");
+    if (!is_device_ptr(B) || !is_device_ptr(X) || !is_device_ptr(A->val) ||
+        !is_device_ptr(A->row_ptr) || !is_device_ptr(A->col)) {
+        set_error("rxg_cg_solve_noalloc: A (row_ptr, col, val), B and X must be device arrays");
         return RXG_ERR_INVALID;
     }
     uint8_t*   scratch = nullptr;

@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <mutex>
 
 #include "rxg_device.cuh"
 
@@ -19,17 +20,56 @@ namespace rxg {
 
 __device__ int g_err_word;
 
+// The error word's device address on the current device.  Every GPU that
+// loads the library has its own copy of g_err_word, so the address is looked
+// up once per device ordinal (with that device current) and cached.
 int* device_error_word()
 {
-    static int* p = nullptr;
-    if (!p) cudaGetSymbolAddress((void**)&p, g_err_word);
-    return p;
+    static std::mutex mu;
+    static int*       addr[kMaxDevices] = {nullptr};
+    int               dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+    std::lock_guard<std::mutex> g(mu);
+    if (!addr[dev] && cudaGetSymbolAddress((void**)&addr[dev], g_err_word) != cudaSuccess) {
+        cudaGetLastError();
+        addr[dev] = nullptr;
+    }
+    return addr[dev];
+}
+
+int device_sm_count()
+{
+    static std::mutex mu;
+    static int        sms[kMaxDevices] = {0};
+    int               dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 1;
+    std::lock_guard<std::mutex> g(mu);
+    if (!sms[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            n = 0;
+        }
+        sms[dev] = n > 0 ? n : 1;
+    }
+    return sms[dev];
+}
+
+int current_device()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 0;
+    return dev;
 }
 
 rxg_status check_device_error(cudaStream_t s)
 {
     int* d = device_error_word();
     int  h = 0;
+    if (!d) {
+        set_error("device error word: no current CUDA device (or ordinal beyond %d)", kMaxDevices - 1);
+        return RXG_ERR_NO_DEVICE;
+    }
     RXG_CUDA_TRY(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, s));
     RXG_CUDA_TRY(cudaStreamSynchronize(s));
     if (h) {

@@ -243,6 +243,22 @@ static int gpu_checks(const char* dir)
     }
     REQUIRE(std::sqrt(num / den) < 1e-8);
 
+    // the same solve through the entry point that allocates nothing (6,144
+    // rows, inside its fixed scratch): the same iterations and solution
+    {
+        DenseMatrix<double> Xn(nv, 3);
+        PCGSolver<double>   s2(A, 3, 2000, 1e-20, 0.0);
+        s2.solve_noalloc(B, Xn);
+        REQUIRE(s2.converged() && s2.iter_taken() == solver.iter_taken());
+        const std::vector<double> hx = X.to_host(), hn = Xn.to_host();
+        double                    d = 0, mx = 0;
+        for (size_t i = 0; i < hx.size(); ++i) {
+            d  = std::max(d, std::fabs(hx[i] - hn[i]));
+            mx = std::max(mx, std::fabs(hx[i]));
+        }
+        REQUIRE(d <= 1e-12 * mx);
+    }
+
     // mcf_step: plain FP64 against mixed precision
     DenseMatrix<double> x64(nv, 3), x32(nv, 3);
     const std::vector<double> x0 = rx.get_input_vertex_coordinates().to_host();

@@ -22,6 +22,10 @@ pytestmark = pytest.mark.gpu
 # FP64 and 1e-6 in FP32 (the two entry points run the same kernel, so in
 # practice the results are identical)
 TOL = {torch.float64: 1e-12, torch.float32: 1e-6}
+# relative residual |A X - B| / |B| the stopping rules above reach (delta
+# relative 1e-20 in FP64 -> ~1e-10 in the 2-norm; 1e-10 in FP32 -> ~1e-5,
+# limited by FP32 rounding of the recursive residual)
+RES = {torch.float64: 1e-8, torch.float32: 1e-4}
 
 
 def _system(dtype):
@@ -53,6 +57,9 @@ def test_noalloc_matches_allocating_solver_twice(dtype, precond):
     from rxmesh_gb300 import _lib
     L = _lib.load()
     rx, A, B, X0 = _system(dtype)
+    import scipy.sparse as sp
+    As = sp.csr_matrix((A.val.double().cpu().numpy(), A.col.cpu().numpy(), A.row_ptr.cpu().numpy()),
+                       shape=(A.rows(), A.rows()))
     # two calls in a row with different right-hand sides and initial guesses
     for k, (b, x0) in enumerate([(B, X0), (0.5 * B + 0.01, torch.zeros_like(X0))]):
         rc_a, Xa, sa = _solve(L.rxg_cg_solve, A, b, x0, precond)
@@ -62,6 +69,11 @@ def test_noalloc_matches_allocating_solver_twice(dtype, precond):
         assert abs(sn.final_res - sa.final_res) <= TOL[dtype] * abs(sa.start_res)
         err = (Xn - Xa).abs().max().item() / Xa.abs().max().item()
         assert err <= TOL[dtype], (k, err)
+        # the solution itself, independent of the other entry point: the
+        # residual |A X - B| computed in FP64 by scipy from the same matrix
+        Xh = Xn.double().cpu().numpy()
+        res = np.linalg.norm(As @ Xh - b.double().cpu().numpy()) / np.linalg.norm(b.double().cpu().numpy())
+        assert res <= RES[dtype], (k, res)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():
@@ -80,3 +92,22 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
                                 ctypes.c_void_p(X.data_ptr()), ctypes.byref(o), ctypes.byref(st), None)
     assert rc == 1 and b"exceeds the fixed scratch" in L.rxg_last_error()
     assert X.abs().max().item() == 0.0
+
+
+def test_noalloc_rejects_host_matrix_arrays():
+    """A's row_ptr and col must be device arrays too: host copies are
+    refused before any launch."""
+    from rxmesh_gb300 import _lib
+    L = _lib.load()
+    rx, A, B, X0 = _system(torch.float64)
+    X = X0.clone()
+    o = _lib.SolverOpts(10, 0.0, 1e-10, 1)
+    st = _lib.SolverStats()
+    rp_h, col_h = A.row_ptr.cpu(), A.col.cpu()
+    for rp, col in ((rp_h, A.col), (A.row_ptr, col_h)):
+        c = _lib.CSR(A.rows(), A.col.numel(), rp.data_ptr(), col.data_ptr(), A.val.data_ptr(), 1)
+        for fn in (L.rxg_cg_solve_noalloc, L.rxg_cg_solve):
+            rc = fn(ctypes.byref(c), 3, ctypes.c_void_p(B.data_ptr()), ctypes.c_void_p(X.data_ptr()),
+                    ctypes.byref(o), ctypes.byref(st), None)
+            assert rc == 1 and b"must be device arrays" in L.rxg_last_error()
+    assert torch.equal(X, X0)
