@@ -28,6 +28,10 @@ sys.path.insert(0, ROOT)
 METRIC = "MCF steps/s & query GB/s vs HBM peak; mixed vs FP64 at 1e-6 rel error, 1 GB300"
 WORKLOAD = "query+normal sweep, torus 1024x1024 (V=1,048,576 F=2,097,152), patches<=512 faces"
 OPS = ["VV", "VE", "VF", "FV", "EV", "normals"]
+# the workload, identical in both arms' lines
+CONFIG = {"workload": WORKLOAD, "patch_faces": 512,
+          "l2": "flushed before every timed sweep (256 MB write, then 256 MB read); the sweep's "
+                "outputs (151 MB) exceed L2"}
 
 
 def canonical_bytes(V, E, F):
@@ -120,16 +124,12 @@ def peaks():
 
 
 def profiled_traffic():
-    """dram bytes per launch from the committed ncu summary, if present."""
-    p = os.path.join(ROOT, "profiles", "query_sweep_torus1024.md")
-    out = {}
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
+    of each sweep kernel, from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "query_sweep_torus1024.json")
     if os.path.exists(p):
-        for line in open(p):
-            if line.startswith("traffic_bytes_per_launch:"):
-                for kv in line.split(":", 1)[1].split():
-                    k, v = kv.split("=")
-                    out[k] = float(v)
-    return out
+        return {k: float(v) for k, v in json.load(open(p))["traffic_bytes_per_launch"].items()}
+    return {}
 
 
 class Clocks:
@@ -186,11 +186,17 @@ class Clocks:
 # CPU legs (oracle port): bounded sample of the same sweep
 # ----------------------------------------------------------------------------
 
-def cpu_sweep_once(n=384):
-    """One sweep of the oracle port on an n x n torus; returns (seconds, bytes)."""
+_CPU_MESH = {}
+
+
+def cpu_sweep_once(n=1024):
+    """One sweep of the oracle port on an n x n torus; returns (seconds,
+    bytes, set-up seconds).  The torus is generated once per process."""
     from oracle import oracle as O
     from rxmesh_gb300 import meshgen
-    x, f = meshgen.torus(n, n, jitter=1e-3, seed=0)
+    if n not in _CPU_MESH:
+        _CPU_MESH[n] = meshgen.torus(n, n, jitter=1e-3, seed=0)
+    x, f = _CPU_MESH[n]
     V, F = len(x), len(f)
     t0 = time.perf_counter()
     ev, fe = O.edges(f)  # the static structure the queries are derived from
@@ -263,7 +269,7 @@ def run_reference(args):
     O.build()
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
-    n = 384
+    n = 1024
     with ctx.Pool(cores) as pool:
         for _ in range(max(1, args.warmup)):
             pool.map(_cpu_worker, [(n, 1)] * cores)
@@ -277,11 +283,12 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32/fp64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": WORKLOAD},
+            "config": dict(CONFIG),
             "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port",
                              "cpu": cpu_model(),
-                             "sample": "per step: %d processes, each one sweep of a %dx%d torus (the same "
-                                       "queries and normals; sweep time only, mesh set-up excluded)" % (cores, n, n)},
+                             "sample": "per step: %d processes, each one sweep of the %dx%d torus (the same "
+                                       "queries and normals; sweep time only, mesh generation and edge "
+                                       "numbering excluded)" % (cores, n, n)},
             "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -345,7 +352,59 @@ def run_sweep(args, torch, rx, xl, sizes):
         per[name].append(a.elapsed_time(b))
     total_ms = sum(sum(v) for v in per.values())
     clocks = clk.summary()
-    return per, total_ms / args.steps, clocks, outs, nrm
+    return per, total_ms / args.steps, clocks, outs, nrm, (flush_l2, launch)
+
+
+def run_sweep_back_to_back(args, torch, flush_l2, launch):
+    """The six kernels launched back to back after one L2 flush, one event
+    pair around all six: the whole sweep, including each kernel's output
+    write-back (151 MB of outputs do not fit the 129 MB L2) and the gaps
+    between launches.  The launches are captured once into a CUDA graph
+    when the capture succeeds (else launched directly; the line says which).
+    Returns (ms per sweep, mode, clocks)."""
+    stream = torch.cuda.current_stream()
+    mode = "graph"
+    g = None
+    try:
+        side = torch.cuda.Stream()
+        side.wait_stream(stream)
+        with torch.cuda.stream(side):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
+                for name in OPS:
+                    launch(name)
+        stream.wait_stream(side)
+        torch.cuda.synchronize()
+    except Exception:  # capture refused: time direct launches
+        torch.cuda.synchronize()
+        g, mode = None, "direct"
+
+    def sweep():
+        if g is not None:
+            g.replay()
+        else:
+            for name in OPS:
+                launch(name)
+
+    for _ in range(args.warmup):
+        flush_l2()
+        sweep()
+    torch.cuda.synchronize()
+    evs = []
+    with Clocks() as clk:
+        for _ in range(3):
+            flush_l2()
+        for _ in range(args.steps):
+            flush_l2()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            sweep()
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+    ms = statistics.mean(a.elapsed_time(b) for a, b in evs)
+    return ms, mode, clk.summary()
 
 
 def run_e2e(args, torch, rx, x_in_host, sizes):
@@ -391,31 +450,64 @@ def run_e2e(args, torch, rx, x_in_host, sizes):
     return ms, h2d, d2h
 
 
-def run_mcf(args, torch):
-    """Level-8 icosphere, 10 implicit MCF steps at dt=1e-3: FP64 and mixed."""
+MCF_LEVEL, MCF_STEPS, MCF_DT, MCF_TOL = 8, 10, 1e-3, 1e-6
+
+
+def mcf_oracle_steps(level=MCF_LEVEL, nsteps=MCF_STEPS, dt=MCF_DT):
+    """The FP64 oracle's flow (CPU): each implicit step assembled by the
+    oracle and solved by its Jacobi PCG to 1e-12 relative residual.  Returns
+    the positions after step 1 and after the last step, in input order."""
+    from oracle import oracle as O
+    from rxmesh_gb300 import meshgen
+    O.build()
+    v, f = meshgen.icosphere(level)
+    x = meshgen.radial_noise(v, 0.02, 0)
+    out = {}
+    for k in range(1, nsteps + 1):
+        rp, col, val, B = O.mcf_system(f, x, dt)
+        x = O.cg(rp, col, val, B, x, 20000, 0.0, 1e-24, True)[0]
+        if k == 1:
+            out[1] = x
+    out[nsteps] = x
+    return out
+
+
+def start_mcf_oracle():
+    """Run mcf_oracle_steps in a spawned process (started before any GPU
+    work of this process is needed, so it overlaps the GPU legs)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    ex = cf.ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn"))
+    return ex, ex.submit(mcf_oracle_steps)
+
+
+def run_mcf(args, torch, oracle_future=None):
+    """Level-8 icosphere, 10 implicit MCF steps at dt=1e-3: FP64 and mixed,
+    each with its error against the FP64 oracle after step 1 and after all
+    10 steps."""
     from oracle import oracle as O
     from rxmesh_gb300 import RXMeshStatic, meshgen, mcf_step
-    level, nsteps, dt, tol = 8, 10, 1e-3, 1e-6
+    level, nsteps, dt, tol = MCF_LEVEL, MCF_STEPS, MCF_DT, MCF_TOL
     v, f = meshgen.icosphere(level)
     x0 = meshgen.radial_noise(v, 0.02, 0)
     rx = RXMeshStatic(f, len(x0), patch_size=256)
     x0l = rx.to_linear(torch.tensor(x0, device="cuda"))
-    res = {"workload": "icosphere level 8 (V=%d F=%d), %d steps dt=%g, Jacobi PCG" % (len(x0), len(f), nsteps, dt)}
-    # FP64 oracle for the first step (CPU, solved to 1e-12 relative residual)
-    rp, col, val, B = O.mcf_system(f, x0, dt)
-    Xo, it_o, _, _, _ = O.cg(rp, col, val, B, x0, 20000, 0.0, 1e-24, True)
+    res = {"workload": "icosphere level 8 (V=%d F=%d), %d steps dt=%g, Jacobi PCG, tol %g" % (
+        len(x0), len(f), nsteps, dt, tol)}
     # CPU baseline: one step of the oracle port (assembly + FP64 Jacobi PCG,
     # stopped at the GPU steps' rule: r.D^-1 r fallen by tol^2), 1 thread
     t0 = time.perf_counter()
     rp_c, col_c, val_c, B_c = O.mcf_system(f, x0, dt)
     _, it_c, _, _, _ = O.cg(rp_c, col_c, val_c, B_c, x0, 20000, 0.0, tol * tol, True)
     t_cpu = time.perf_counter() - t0
+    runs = {}
     for prec in ("f64", "mixed"):
+        # untimed: the 10 steps one at a time, keeping step 1 and step 10
         x = x0l.clone()
-        mcf_step(rx, x, dt, 1, prec, tol=tol)  # warm-up + error of step 1
-        got = rx.to_input(x).cpu().numpy()
-        err = float(np.linalg.norm(got - Xo) / np.linalg.norm(Xo))
-        err_upd = float(np.linalg.norm(got - Xo) / np.linalg.norm(Xo - x0))
+        mcf_step(rx, x, dt, 1, prec, tol=tol)
+        x1 = rx.to_input(x).cpu().numpy()
+        mcf_step(rx, x, dt, nsteps - 1, prec, tol=tol)
+        runs[prec] = (x1, rx.to_input(x).cpu().numpy())
         times = []
         for _ in range(max(1, args.steps)):
             x = x0l.clone()
@@ -426,14 +518,19 @@ def run_mcf(args, torch):
             times.append(time.perf_counter() - t0)
         t = statistics.median(times)
         res[prec] = {"steps_per_s": nsteps / t, "ms_per_step": 1e3 * t / nsteps,
-                     "cg_iters_last_step": st["iters"], "rel_err_step1": err,
-                     "rel_err_of_update_step1": err_upd}
+                     "cg_iters_last_step": st["iters"], "converged": bool(st["converged"])}
+    ref = oracle_future.result() if oracle_future is not None else mcf_oracle_steps()
+    for prec, (x1, x10) in runs.items():
+        res[prec]["rel_err_step1"] = float(np.linalg.norm(x1 - ref[1]) / np.linalg.norm(ref[1]))
+        res[prec]["rel_err_after_10_steps"] = float(np.linalg.norm(x10 - ref[nsteps]) /
+                                                    np.linalg.norm(ref[nsteps]))
+    res["error_measure"] = ("|x - x_oracle| / |x_oracle| over all positions; oracle: FP64 assembly "
+                            "and Jacobi PCG to 1e-12 relative residual every step")
     res["mixed_speedup_vs_f64"] = res["mixed"]["steps_per_s"] / res["f64"]["steps_per_s"]
     res["cpu_baseline_f64"] = {"steps_per_s": 1.0 / t_cpu, "ms_per_step": 1e3 * t_cpu, "pcg_iters": it_c,
                                "cores": 1, "kind": "port",
                                "sample": "one implicit step of the same level-8 system: assembly + FP64 "
                                          "Jacobi PCG to the same stopping rule (oracle port, 1 thread)"}
-    res["oracle_pcg_iters_step1"] = it_o
     # per PCG iteration, algorithmic bytes: FP64 packed solver = 16 B per entry
     # + 4 vectors of 32 B read and 4 written per row; on-chip FP32 solver =
     # 8-slot ELL (64 B) + the 16-byte z row written (p, s, z, d stay on chip).
@@ -650,8 +747,24 @@ def run_batch(args, torch):
     torch.cuda.synchronize()
     ms = statistics.median([a.elapsed_time(c) for a, c in evs])
     it, cv = b.stats()
+    # canonical bytes of the FP32 PCG per iteration (CSR values + columns,
+    # row offsets, the SpMM's x read and y written, 9 vector passes of n x 3
+    # and 2 of the diagonal), times each mesh's PCG iterations over the 5 steps
+    peak, peak_kind = peaks()
+    algo = 0
+    for m, (x, f) in enumerate(meshes):
+        nv, nf = len(x), len(f)
+        ne = nv + nf - (2 if m % 2 == 0 else 1)  # Euler: spheres chi = 2, grids (disks) chi = 1
+        nnz = nv + 2 * ne
+        algo += int(it[m]) * (8 * nnz + 4 * (nv + 1) + 24 * nv + 116 * nv)
+    ach = algo / (ms * 1e-3) / 1e9
     return {"workload": "256 meshes (128 icospheres L2-6, 128 grids 16-256), 5 steps dt=1e-3, "
                         "mixed precision, one persistent launch, CUDA graph",
+            "roofline": {"bound": "hbm", "algorithmic_bytes": algo, "achieved": ach, "peak": peak,
+                         "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind,
+                         "bytes": "sum over meshes of PCG iterations x the FP32 CSR PCG bytes per "
+                                  "iteration (8 nnz + 4(n+1) + 140 n); the kernel keeps its vectors "
+                                  "in shared memory, so it moves fewer bytes than this"},
             "vertices": int(sum(len(x) for x, _ in meshes)), "faces": faces,
             "ms_per_batch": ms, "meshes_per_s": 256 / (ms * 1e-3),
             "faces_per_s": faces / (ms * 1e-3), "autotuned": {"threads": thr, "ctas_per_sm": bps},
@@ -676,7 +789,7 @@ def run_patcher(args, torch):
             build_s = time.perf_counter() - t0
             V, E, F = rx.get_num_vertices(), rx.get_num_edges(), rx.get_num_faces()
             xl = rx.to_linear(torch.tensor(x, device="cuda"))
-            _, ms, _, _, _ = run_sweep(args, torch, rx, xl, (V, E, F))
+            _, ms, _, _, _, _ = run_sweep(args, torch, rx, xl, (V, E, F))
             out[name] = {"build_s": build_s, "num_patches": rx.get_num_patches(),
                          "max_local_faces": rx.info["max_local_faces"],
                          "ribbon_vertex_fraction": rx.info["ribbon_vertices"] / V,
@@ -684,6 +797,32 @@ def run_patcher(args, torch):
                          "sweep_ms": ms}
         except Exception as e:  # reported, not fatal to the rest of the line
             out[name] = {"error": str(e)}
+    return out
+
+
+def summary(line, peak_kind):
+    """The headline figures of every workload in a few keys, placed last in
+    the JSON line."""
+    out = {"sweep_gbs": line["value"],
+           "sweep_frac": line["sweep"].get("frac_of_%s_hbm" % peak_kind),
+           "e2e_gbs": line["e2e"]["value"],
+           "dominant_kernel": line["roofline"]["kernel"], "dominant_frac": line["roofline"]["frac"],
+           "per_kernel_frac": {k: v / line["roofline"]["peak"] for k, v in line["per_kernel_gbs"].items()}}
+    m = line.get("mcf")
+    if m:
+        out["mcf_steps_per_s_f64"] = m["f64"]["steps_per_s"]
+        out["mcf_steps_per_s_mixed"] = m["mixed"]["steps_per_s"]
+        out["mcf_mixed_speedup"] = m["mixed_speedup_vs_f64"]
+        out["mcf_rel_err_f64_10_steps"] = m["f64"]["rel_err_after_10_steps"]
+        out["mcf_rel_err_mixed_10_steps"] = m["mixed"]["rel_err_after_10_steps"]
+        out["spmv_frac"] = {k: v["frac_of_measured_hbm"] for k, v in m["spmv"].items()}
+    b = line.get("batch")
+    if b:
+        out["batch_meshes_per_s"] = b["meshes_per_s"]
+        out["batch_frac"] = b["roofline"]["frac"]
+    a = line.get("arap")
+    if a:
+        out["arap_ms_f32"] = a["f32"]["ms_energy_grad_hessian"]
     return out
 
 
@@ -717,6 +856,11 @@ def main():
     if args.only and args.only != "sweep":
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         fn = {"mcf": run_mcf, "arap": run_arap, "batch": run_batch, "patcher": run_patcher}[args.only]
+        if args.only == "mcf":
+            ex, fut = start_mcf_oracle()
+            print(json.dumps({"only": "mcf", "mcf": run_mcf(args, torch, fut)}))
+            ex.shutdown()
+            return
         print(json.dumps({"only": args.only, args.only: fn(args, torch)}))
         return
     if args.only == "sweep":
@@ -724,6 +868,8 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    # the MCF leg's FP64 oracle runs on a host core beside the GPU legs
+    mcf_oracle = start_mcf_oracle() if rank == 0 and not args.no_mcf else None
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
@@ -735,7 +881,8 @@ def main():
     xl = rx.to_linear(torch.tensor(x, device="cuda"))
     if world > 1:
         torch.distributed.barrier()
-    per, ms, clocks, _, _ = run_sweep(args, torch, rx, xl, (V, E, F))
+    per, ms_isolated, clocks_iso, _, _, fns = run_sweep(args, torch, rx, xl, (V, E, F))
+    ms, sweep_mode, clocks = run_sweep_back_to_back(args, torch, *fns)
     ms = max_over_ranks(torch, ms, "cuda")
     cb = canonical_bytes(V, E, F)
     sweep_bytes = sum(cb.values())
@@ -750,10 +897,17 @@ def main():
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "l2": "flushed before every timed sweep (256 MB write, then 256 MB read)",
-                   "patch_faces": 512, "num_patches": rx.get_num_patches(),
-                   "ribbon_vertex_fraction": rx.info["ribbon_vertices"] / V,
-                   "ribbon_face_fraction": rx.info["ribbon_faces"] / F},
+        "config": dict(CONFIG),
+        "sweep": {"timing": "the six kernels back to back after one L2 flush, one CUDA-event pair "
+                            "around the sweep (%s)" % sweep_mode,
+                  "frac_of_%s_hbm" % peak_kind: (sweep_bytes / (ms * 1e-3) / 1e9) / peak,
+                  "isolated_sum_ms": ms_isolated,
+                  "isolated_note": "sum of the six kernels each timed alone after its own L2 flush "
+                                   "(outputs stay dirty in L2 and are written back outside the "
+                                   "timed region)"},
+        "mesh": {"num_patches": rx.get_num_patches(),
+                 "ribbon_vertex_fraction": rx.info["ribbon_vertices"] / V,
+                 "ribbon_face_fraction": rx.info["ribbon_faces"] / F},
         "per_kernel_ms": avg,
         "per_kernel_gbs": {k: cb[k] / (avg[k] * 1e-3) / 1e9 for k in OPS},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
@@ -763,6 +917,7 @@ def main():
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "gpu_launches": len(OPS) * args.steps,
         "clocks": clocks,
+        "clocks_isolated_leg": clocks_iso,
     }
     if rank == 0:
         line["edge_face_queries"] = run_edge_face_queries(args, torch, rx, (V, E, F))
@@ -770,22 +925,26 @@ def main():
         from oracle import oracle as O
         O.build()
         reps, tot, b = 0, 0.0, 0
-        while tot < 8.0 and reps < 40:
-            dt, bb, _ = cpu_sweep_once(384)
+        while tot < 10.0 and reps < 60:
+            dt, bb, _ = cpu_sweep_once(1024)
             tot += dt
             b += bb
             reps += 1
         line["cpu_baseline"] = {"value": b / tot / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
                                 "cpu": cpu_model(),
-                                "sample": "%d sweeps of a 384x384 torus (oracle port, 1 thread)" % reps}
+                                "sample": "%d sweeps of the 1024x1024 torus (oracle port, 1 thread; "
+                                          "sweep time only)" % reps}
     if rank == 0 and not args.no_mcf:
-        line["mcf"] = run_mcf(args, torch)
+        line["mcf"] = run_mcf(args, torch, mcf_oracle[1] if mcf_oracle else None)
+        mcf_oracle[0].shutdown()
     if rank == 0 and not args.no_arap:
         line["arap"] = run_arap(args, torch)
     if rank == 0 and not args.no_batch:
         line["batch"] = run_batch(args, torch)
     if rank == 0 and not args.no_patcher:
         line["patcher"] = run_patcher(args, torch)
+    if rank == 0:
+        line["summary"] = summary(line, peak_kind)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

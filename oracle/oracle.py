@@ -22,9 +22,13 @@ f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 I64 = ctypes.c_int64
 
 
-def build():
-    """Compile the oracle (and oracle/_ref when the reference tree exists)."""
-    subprocess.check_call(["make", "-s", "-C", _HERE], stdout=subprocess.DEVNULL)
+def build(ref_root=None):
+    """Compile the oracle; with ref_root (an RXMesh source tree) also the
+    reference's own routines into oracle/_ref."""
+    cmd = ["make", "-s", "-C", _HERE]
+    if ref_root:
+        cmd.append("REF=" + ref_root)
+    subprocess.check_call(cmd, stdout=subprocess.DEVNULL)
 
 
 def lib():
@@ -87,6 +91,46 @@ def ref_lib():
         R.ref_vertex_normal_f64.argtypes = [I64, I64, i32p, f64p, f64p]
         _REF = R
     return _REF
+
+
+_GEO = None
+
+
+def ref_geometry():
+    """The reference's own geometry_util.cuh cotangent / Voronoi routines
+    compiled from its source into oracle/_ref, or None."""
+    global _GEO
+    if _GEO is None:
+        path = os.path.join(_HERE, "_ref", "libref_geometry.so")
+        if not os.path.exists(path):
+            return None
+        try:
+            R = ctypes.CDLL(path)
+        except OSError:
+            return None
+        for t, p in (("f64", f64p), ("f32", f32p)):
+            getattr(R, "ref_partial_voronoi_area_" + t).argtypes = [I64, p, p, p, p]
+            getattr(R, "ref_edge_cotan_weight_" + t).argtypes = [I64, p, p, p, p, p]
+        R.ref_tri_area_f64.argtypes = [I64, f64p, f64p, f64p, f64p]
+        _GEO = R
+    return _GEO
+
+
+def partial_voronoi_area(P, Q, R):
+    """Oracle restatement of partial_voronoi_area (geometry_util.cuh:117-167),
+    row by row over (n, 3) arrays."""
+    L = lib()
+    P, Q, R = (np.ascontiguousarray(a, np.float64) for a in (P, Q, R))
+    return np.array([L.orc_partial_voronoi_area(P[i], Q[i], R[i]) for i in range(len(P))])
+
+
+def edge_cotan_weight(P, R, Q, S):
+    """Oracle restatement of edge_cotan_weight (geometry_util.cuh:173-206):
+    the two half-cotangents of edge p-r opposite q and s."""
+    L = lib()
+    P, R, Q, S = (np.ascontiguousarray(a, np.float64) for a in (P, R, Q, S))
+    return np.array([L.orc_half_cot(P[i], R[i], Q[i]) + L.orc_half_cot(P[i], R[i], S[i])
+                     for i in range(len(P))])
 
 
 def _fv(fv):

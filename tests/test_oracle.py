@@ -263,3 +263,42 @@ def test_project_pd_matches_eigh(oracle):
             assert np.abs(got - want).max() < 1e-10 * max(1.0, np.abs(h).max())
             assert np.linalg.eigvalsh(got).min() >= eps * (1 - 1e-6) - 1e-12
 
+
+
+def test_cotan_and_voronoi_match_reference_geometry_util(oracle):
+    """The oracle's partial_voronoi_area and edge_cotan_weight against the
+    reference's own geometry_util.cuh compiled from its source (outputs kept
+    in tests/golden/geometry_util.npz by make_golden.py) on every branch:
+    generic, obtuse at each corner, within 1e-9 .. 1e-3 rad of a right angle,
+    clamped cotangents of slivers, and zero-area triangles."""
+    g = golden("geometry_util")
+    vor = oracle.partial_voronoi_area(g["P"], g["Q"], g["R"])
+    cot = oracle.edge_cotan_weight(g["P"], g["Q"], g["R"], g["S"])
+    # scale: the triangle's area for Voronoi areas (|cot| <= 19.1 for weights)
+    area = 0.5 * np.linalg.norm(np.cross(g["Q"] - g["P"], g["R"] - g["P"]), axis=1)
+    assert np.all(np.abs(vor - g["voronoi_f64"]) <= 1e-12 * np.maximum(area, 1e-300) + 1e-300)
+    assert np.all(np.abs(cot - g["cotan_f64"]) <= 1e-12 * np.maximum(np.abs(g["cotan_f64"]), 1.0))
+    # every branch is exercised: degenerate (-1), obtuse at p (A/4), at q or r (A/8), clamped
+    assert (g["voronoi_f64"] == -1).sum() >= 100
+    assert np.isclose(vor, 0.25 * area, rtol=1e-12).sum() >= 100
+    assert np.isclose(vor, 0.125 * area, rtol=1e-12).sum() >= 100
+    assert (np.abs(g["cotan_f64"]) >= 19.1 - 1e-12).sum() >= 50
+
+
+def test_cotan_and_voronoi_against_live_reference_build(oracle):
+    """Same comparison against oracle/_ref built from the reference tree
+    in this checkout (skipped where the tree is absent)."""
+    G = oracle.ref_geometry()
+    if G is None:
+        pytest.skip("oracle/_ref/libref_geometry.so not built (no reference tree)")
+    from rxmesh_gb300 import meshgen
+    v, f = meshgen.icosphere(3)
+    x = meshgen.radial_noise(v, 0.05, 1)
+    P, Q, R = (np.ascontiguousarray(x[f[:, k]]) for k in range(3))
+    S = np.ascontiguousarray(np.roll(R, 1, axis=0))
+    n = len(P)
+    out = np.empty(n)
+    G.ref_partial_voronoi_area_f64(n, P, Q, R, out)
+    assert np.abs(oracle.partial_voronoi_area(P, Q, R) - out).max() <= 1e-15
+    G.ref_edge_cotan_weight_f64(n, P, Q, R, S, out)
+    assert np.abs(oracle.edge_cotan_weight(P, Q, R, S) - out).max() <= 1e-13
