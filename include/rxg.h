@@ -163,6 +163,32 @@ rxg_status rxg_mesh_patches(const rxg_mesh* m, int32_t* hdr, uint32_t* arena,
                             int64_t* words);
 rxg_status rxg_mesh_get_info(const rxg_mesh* m, rxg_mesh_info* info);
 
+/*
+ * Device view of a mesh's patches, for kernels that run queries themselves
+ * (include/rxg/query.cuh: Query<blockThreads>::dispatch, the facade's
+ * for_each / run_kernel).  Counterpart of RXMesh's Context
+ * (include/rxmesh/context.h:15-120), which kernels receive by value.
+ * patch_hdr: num_patches records of 16 int32 in rxg_mesh_patches' layout
+ * {nVo,nVl,nEo,nEl,nFo,nFl, v_base,e_base,f_base, vv_base,vf_base,
+ *  ev_off,fe_off,rv_off,re_off,rf_off}; arena: the patches' EV (u16 pairs),
+ * FE (u16 edge<<1|dir triples) and ribbon -> linear id tables, at those word
+ * offsets, every slice 16-byte aligned.  Both are device pointers owned by
+ * the mesh (valid until rxg_mesh_destroy).  The max_* fields bound every
+ * patch (shared-memory sizing).  RXG_ERR_INVALID for a host-only mesh.
+ */
+typedef struct rxg_device_context {
+    int64_t         num_vertices, num_edges, num_faces;
+    int32_t         num_patches;
+    int32_t         max_local_vertices, max_local_edges, max_local_faces;
+    int32_t         max_owned_vertices, max_owned_edges, max_owned_faces;
+    int32_t         max_valence;
+    int32_t         max_face_adjacent_faces;
+    int32_t         device; /* CUDA ordinal holding the arrays */
+    const int32_t*  patch_hdr;
+    const uint32_t* arena;
+} rxg_device_context;
+rxg_status rxg_mesh_device_context(const rxg_mesh* m, rxg_device_context* ctx);
+
 /* lin_to_input (host, n_elem ints): input id of each linear id
  * (RXMeshStatic::map_to_global, rxmesh_static.h:874-905). */
 rxg_status rxg_mesh_linear_to_input(const rxg_mesh* m, int32_t elem,
@@ -315,6 +341,45 @@ rxg_status rxg_cg_solve(const rxg_csr* A, int32_t nc, const void* B, void* X,
  */
 rxg_status rxg_cg_solve_noalloc(const rxg_csr* A, int32_t nc, const void* B,
                                 void* X, const rxg_solver_opts* opts,
+                                rxg_solver_stats* stats, void* stream);
+
+/*
+ * Matrix-free implicit MCF operator: the weights of A = 2M + dt*L (as
+ * rxg_mcf_assemble builds it) are recomputed from the positions xyz on every
+ * call and nothing is assembled (matvec / precond_matvec / init_B,
+ * apps/MCF/mcf_kernels.cuh:58-299).  flags: RXG_MCF_UNIFORM_LAPLACE (weight
+ * 1 per neighbour, the valence as vertex weight: use_uniform_laplace),
+ * RXG_MCF_JACOBI (rxg_mcf_matvec only: out = D^-1 in, D = diag(A), the
+ * preconditioner's product).  xyz: nv*3 FP64; in, out, B: nv*3 of dtype; all
+ * linear order, device arrays.  With flags 0, out equals rxg_spmm on the
+ * assembled matrix up to rounding.
+ */
+enum { RXG_MCF_UNIFORM_LAPLACE = 1, RXG_MCF_JACOBI = 2 };
+rxg_status rxg_mcf_matvec(const rxg_mesh* m, double dt, int32_t flags, int32_t dtype,
+                          const double* xyz, const void* in, void* out, void* stream);
+/* B = (1 / v_weight) * xyz: 2 * Voronoi area (cotangent mode) or the
+ * valence (uniform mode) times the positions (init_B). */
+rxg_status rxg_mcf_init_b(const rxg_mesh* m, int32_t flags, int32_t dtype, const double* xyz,
+                          void* B, void* stream);
+/*
+ * Solve A(xyz) X = B with the matrix-free operator (CGMatFreeAttrSolver /
+ * PCGMatFreeAttrSolver, matrix/cg_mat_free_attr_solver.h:45-115): one
+ * cooperative launch, the operator's weights recomputed in every product;
+ * opts as rxg_cg_solve (3 columns as one vector, X in/out as the initial
+ * guess).  flags: RXG_MCF_UNIFORM_LAPLACE.
+ */
+rxg_status rxg_mcf_solve_matfree(const rxg_mesh* m, double dt, int32_t flags, int32_t dtype,
+                                 const double* xyz, const void* B, void* X,
+                                 const rxg_solver_opts* opts, rxg_solver_stats* stats,
+                                 void* stream);
+/*
+ * nsteps implicit MCF steps in place on xyz (nv*3 FP64, linear order,
+ * device) with the matrix-free operator in FP64 and Jacobi PCG, stopped by
+ * the rule of rxg_mcf_step (run_cg_mat_free, apps/MCF/mcf_cg_mat_free.h).
+ * flags: RXG_MCF_UNIFORM_LAPLACE.
+ */
+rxg_status rxg_mcf_step_matfree(const rxg_mesh* m, double dt, int32_t nsteps, int32_t flags,
+                                double tol, int32_t max_iter, double* xyz,
                                 rxg_solver_stats* stats, void* stream);
 
 /*

@@ -11,12 +11,22 @@
 //                           matrix/pcg_solver.h:14-213
 //   DiffScalarProblem       include/rxmesh/diff/diff_scalar_problem.h:310-321
 //                           (ARAP term only)
+//   VertexHandle / EdgeHandle / FaceHandle   include/rxmesh/handle.h:19-144
+//   VertexAttribute<T> ...  include/rxmesh/attribute.h (add_*_attribute,
+//                           rxmesh_static.h:608-793)
+//   Context, LaunchBox      include/rxmesh/context.h, launch_box.h
+// Compiled by nvcc, this header also brings in rxg/query.cuh: Query<bt>,
+// Iterator<H>, ShmemAllocator and the kernels behind RXMeshStatic::for_each,
+// run_kernel and the device side of for_each_vertex/edge/face.
 // Every call goes through librxg.so; errors throw rxg::Error carrying the
 // rxg_status and rxg_last_error().  Header only; needs the CUDA runtime.
 #ifndef RXG_RXMESH_HPP
 #define RXG_RXMESH_HPP
 
 #include <cuda_runtime_api.h>
+
+#include <functional>
+#include <typeinfo>
 
 #include <algorithm>
 #include <cmath>
@@ -147,6 +157,153 @@ class DeviceArray
 };
 
 class RXMeshStatic;
+
+#if defined(__CUDACC__)
+#define RXG_HD __host__ __device__
+#else
+#define RXG_HD
+#endif
+// extended-lambda traits (nvcc --extended-lambda): a __device__-only lambda
+// cannot run in the HOST branch of for_each_vertex and the like
+// and a plain host lambda cannot run in the DEVICE branch (without
+// --extended-lambda any functor is taken to be device-callable)
+#if defined(__CUDACC__) && defined(__CUDACC_EXTENDED_LAMBDA__)
+#define RXG_IS_D_LAMBDA(T) __nv_is_extended_device_lambda_closure_type(T)
+#define RXG_DEVICE_CALLABLE(T) \
+    (__nv_is_extended_device_lambda_closure_type(T) || __nv_is_extended_host_device_lambda_closure_type(T))
+#else
+#define RXG_IS_D_LAMBDA(T) false
+#define RXG_DEVICE_CALLABLE(T) true
+#endif
+
+// Handle of a vertex, edge or face (VertexHandle / EdgeHandle / FaceHandle,
+// handle.h:19-144).  RXMesh's handle packs (owner patch, local index); here
+// it holds the element's linear id, which is unique over the mesh (owned
+// elements of patch 0 first, then patch 1, ...) and indexes every
+// per-element array directly.  Default-constructed handles are invalid.
+template <int ELEM>
+struct ElementHandle
+{
+    static constexpr int kElem = ELEM;  // RXG_ELEM_VERTEX, _EDGE or _FACE
+    RXG_HD ElementHandle() {}
+    RXG_HD explicit ElementHandle(int32_t linear_id) : m_id(linear_id) {}
+    RXG_HD bool     is_valid() const { return m_id >= 0; }
+    RXG_HD int32_t  linear_id() const { return m_id; }
+    RXG_HD uint64_t unique_id() const { return (uint64_t)(uint32_t)m_id; }
+    RXG_HD bool     operator==(const ElementHandle& o) const { return m_id == o.m_id; }
+    RXG_HD bool     operator!=(const ElementHandle& o) const { return m_id != o.m_id; }
+    int32_t         m_id = -1;
+};
+using VertexHandle = ElementHandle<RXG_ELEM_VERTEX>;
+using EdgeHandle   = ElementHandle<RXG_ELEM_EDGE>;
+using FaceHandle   = ElementHandle<RXG_ELEM_FACE>;
+
+// Per-element attribute (Attribute<T, HandleT>, attribute.h): num_attributes
+// values per element, row-major in linear order, with a device and/or a host
+// copy.  A shallow view, copied by value into kernels and device lambdas as
+// RXMesh's attributes are; the RXMeshStatic that created it owns the buffers
+// (remove_attribute or the mesh's destruction frees them).
+template <typename T, typename HandleT>
+class Attribute
+{
+   public:
+    Attribute() = default;
+    // attr(handle, i): value i of the element; device copy in device code,
+    // host copy in host code
+    RXG_HD T& operator()(const HandleT& h, uint32_t attr = 0) const
+    {
+#if defined(__CUDA_ARCH__)
+        return m_d[(int64_t)h.linear_id() * m_num_attr + attr];
+#else
+        return m_h[(int64_t)h.linear_id() * m_num_attr + attr];
+#endif
+    }
+    RXG_HD uint32_t get_num_attributes() const { return m_num_attr; }
+    RXG_HD int64_t  size() const { return m_n; }
+    T*              data(locationT where = DEVICE) const { return where == HOST ? m_h : m_d; }
+    locationT       get_allocated() const { return (locationT)m_alloc; }
+    // copy the values from one location to the other (Attribute::move)
+    void move(locationT source, locationT target, cudaStream_t s = nullptr) const
+    {
+        if (source == target) return;
+        if (!m_d || !m_h) throw Error(RXG_ERR_INVALID, "attribute is not allocated on both sides");
+        const size_t bytes = sizeof(T) * (size_t)m_n * m_num_attr;
+        if (source == HOST && target == DEVICE)
+            check_cuda(cudaMemcpyAsync(m_d, m_h, bytes, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
+        else if (source == DEVICE && target == HOST)
+            check_cuda(cudaMemcpyAsync(m_h, m_d, bytes, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+        check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    }
+    // every value to `value` where allocated among `location`
+    void reset(T value, locationT location, cudaStream_t s = nullptr) const
+    {
+        const size_t       n = (size_t)m_n * m_num_attr;
+        std::vector<T>     tmp;
+        const std::vector<T>* src = nullptr;
+        if ((location & HOST) && m_h) std::fill(m_h, m_h + n, value);
+        if ((location & DEVICE) && m_d) {
+            if (m_h && (location & HOST)) {
+                check_cuda(cudaMemcpyAsync(m_d, m_h, sizeof(T) * n, cudaMemcpyHostToDevice, s),
+                           "cudaMemcpyAsync");
+            } else {
+                tmp.assign(n, value);
+                src = &tmp;
+                check_cuda(cudaMemcpyAsync(m_d, src->data(), sizeof(T) * n, cudaMemcpyHostToDevice, s),
+                           "cudaMemcpyAsync");
+            }
+            check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        }
+    }
+
+   private:
+    friend class RXMeshStatic;
+    T*       m_d        = nullptr;
+    T*       m_h        = nullptr;
+    int64_t  m_n        = 0;
+    uint32_t m_num_attr = 1;
+    uint32_t m_alloc    = LOCATION_NONE;
+};
+template <typename T>
+using VertexAttribute = Attribute<T, VertexHandle>;
+template <typename T>
+using EdgeAttribute = Attribute<T, EdgeHandle>;
+template <typename T>
+using FaceAttribute = Attribute<T, FaceHandle>;
+
+// The mesh as kernels see it (Context, context.h:15-120): patch records and
+// the arena on the device, sizes, and per-patch maxima; passed by value.
+struct Context
+{
+    rxg_device_context c{};
+    RXG_HD int64_t get_num_vertices() const { return c.num_vertices; }
+    RXG_HD int64_t get_num_edges() const { return c.num_edges; }
+    RXG_HD int64_t get_num_faces() const { return c.num_faces; }
+    RXG_HD int32_t get_num_patches() const { return c.num_patches; }
+};
+
+// Grid and dynamic shared memory of a query kernel (LaunchBox, launch_box.h)
+template <uint32_t blockThreads>
+struct LaunchBox
+{
+    uint32_t blocks         = 0;
+    uint32_t num_threads    = blockThreads;
+    uint32_t smem_bytes_dyn = 0;
+};
+
+#if defined(__CUDACC__)
+namespace detail {
+template <Op op, uint32_t blockThreads, typename LambdaT>
+void for_each_impl(const RXMeshStatic& rx, const LaunchBox<blockThreads>* lb, const LambdaT& f,
+                   bool oriented, cudaStream_t stream);
+template <uint32_t blockThreads>
+void prepare_launch_box_impl(const RXMeshStatic& rx, const std::vector<Op>& ops,
+                             LaunchBox<blockThreads>& lb, const void* kernel, bool oriented,
+                             bool with_vertex_valence, bool is_concurrent,
+                             const std::function<size_t(uint32_t, uint32_t, uint32_t)>& user_shmem);
+template <typename HandleT, typename LambdaT>
+void for_each_element_device(const RXMeshStatic& rx, const LambdaT& f, cudaStream_t stream);
+}  // namespace detail
+#endif
 
 // rows x cols dense matrix in device memory, row-major (one row per mesh
 // element, as every rxg call expects).
@@ -476,12 +633,248 @@ class RXMeshStatic
         check(rxg_vertex_normals(handle(), weighting, xyz.data(), out.data(), s));
     }
 
+    // ---- device-side queries (Query<bt>::dispatch, for_each, run_kernel) ----
+
+    // the mesh as kernels see it (RXMeshStatic::get_context)
+    Context get_context() const
+    {
+        Context c;
+        check(rxg_mesh_device_context(handle(), &c.c));
+        return c;
+    }
+
+    // ---- attributes (add_vertex_attribute ..., rxmesh_static.h:608-793) ----
+
+    template <typename T>
+    std::shared_ptr<VertexAttribute<T>> add_vertex_attribute(const std::string& name,
+                                                             uint32_t num_attributes,
+                                                             locationT location = LOCATION_ALL)
+    {
+        return add_attribute<T, VertexHandle>(name, num_attributes, location, m_info.num_vertices);
+    }
+    template <typename T>
+    std::shared_ptr<EdgeAttribute<T>> add_edge_attribute(const std::string& name,
+                                                         uint32_t num_attributes,
+                                                         locationT location = LOCATION_ALL)
+    {
+        return add_attribute<T, EdgeHandle>(name, num_attributes, location, m_info.num_edges);
+    }
+    template <typename T>
+    std::shared_ptr<FaceAttribute<T>> add_face_attribute(const std::string& name,
+                                                         uint32_t num_attributes,
+                                                         locationT location = LOCATION_ALL)
+    {
+        return add_attribute<T, FaceHandle>(name, num_attributes, location, m_info.num_faces);
+    }
+    // from per-vertex values in input order (add_vertex_attribute(value,
+    // name), rxmesh_static.h:700-740): host and device, linear order
+    template <typename T>
+    std::shared_ptr<VertexAttribute<T>> add_vertex_attribute(const std::vector<std::vector<T>>& value,
+                                                             const std::string& name)
+    {
+        if ((int64_t)value.size() != m_info.num_vertices || value.empty())
+            throw Error(RXG_ERR_INVALID, "add_vertex_attribute: one row per vertex expected");
+        const uint32_t na = (uint32_t)value[0].size();
+        auto           a  = add_vertex_attribute<T>(name, na, LOCATION_ALL);
+        const std::vector<int32_t> l2i = linear_to_input(RXG_ELEM_VERTEX);
+        for (size_t l = 0; l < l2i.size(); ++l) {
+            const std::vector<T>& row = value[(size_t)l2i[l]];
+            if (row.size() != na) throw Error(RXG_ERR_INVALID, "add_vertex_attribute: ragged rows");
+            for (uint32_t k = 0; k < na; ++k) a->data(HOST)[l * na + k] = row[k];
+        }
+        a->move(HOST, DEVICE);
+        return a;
+    }
+    template <typename T>
+    std::shared_ptr<VertexAttribute<T>> get_vertex_attribute(const std::string& name) const
+    {
+        return get_attribute<T, VertexHandle>(name);
+    }
+    template <typename T>
+    std::shared_ptr<EdgeAttribute<T>> get_edge_attribute(const std::string& name) const
+    {
+        return get_attribute<T, EdgeHandle>(name);
+    }
+    template <typename T>
+    std::shared_ptr<FaceAttribute<T>> get_face_attribute(const std::string& name) const
+    {
+        return get_attribute<T, FaceHandle>(name);
+    }
+    bool does_attribute_exist(const std::string& name) const
+    {
+        for (const auto& a : m_attrs)
+            if (a->name == name) return true;
+        return false;
+    }
+    // frees the attribute's buffers; views of it must not be used afterwards
+    void remove_attribute(const std::string& name)
+    {
+        for (size_t i = 0; i < m_attrs.size(); ++i)
+            if (m_attrs[i]->name == name) {
+                m_attrs.erase(m_attrs.begin() + (long)i);
+                return;
+            }
+    }
+
+    // ---- per-element loops (for_each_vertex / edge / face, rxmesh_static.h:205-379) ----
+    // apply(handle) for every vertex (edge, face).  HOST: a loop on this
+    // thread (apply must be callable on the host); DEVICE: one kernel, one
+    // thread per element (apply a __device__ or __host__ __device__ lambda;
+    // the caller is compiled by nvcc); LOCATION_ALL: both.
+    template <typename LambdaT>
+    void for_each_vertex(locationT location, LambdaT apply, cudaStream_t stream = nullptr) const
+    {
+        for_each_element<VertexHandle>(location, apply, stream, m_info.num_vertices);
+    }
+    template <typename LambdaT>
+    void for_each_edge(locationT location, LambdaT apply, cudaStream_t stream = nullptr) const
+    {
+        for_each_element<EdgeHandle>(location, apply, stream, m_info.num_edges);
+    }
+    template <typename LambdaT>
+    void for_each_face(locationT location, LambdaT apply, cudaStream_t stream = nullptr) const
+    {
+        for_each_element<FaceHandle>(location, apply, stream, m_info.num_faces);
+    }
+
+#if defined(__CUDACC__)
+    // for_each<op, blockThreads>(lambda, oriented, stream) (rxmesh_static.h:
+    // 524-566): one CTA per patch runs Query<blockThreads>::dispatch<op> and
+    // calls lambda(source handle, output iterator) for every owned source
+    // element of its patch.  The iterator's handles carry linear ids.
+    template <Op op, uint32_t blockThreads, typename LambdaT>
+    void for_each(const LambdaT user_lambda, const bool oriented = false,
+                  cudaStream_t stream = nullptr) const
+    {
+        detail::for_each_impl<op, blockThreads>(*this, nullptr, user_lambda, oriented, stream);
+    }
+    template <Op op, uint32_t blockThreads, typename LambdaT>
+    void for_each(LaunchBox<blockThreads> lb, const LambdaT user_lambda, const bool oriented = false,
+                  cudaStream_t stream = nullptr) const
+    {
+        detail::for_each_impl<op, blockThreads>(*this, &lb, user_lambda, oriented, stream);
+    }
+    // grid (one CTA per patch) and dynamic shared memory for a kernel that
+    // runs the queries `op` (prepare_launch_box, rxmesh_static.h:585-594;
+    // shared memory as calc_shared_memory, rxmesh_static.inl:548-741): the
+    // largest op's need (their sum when is_concurrent), plus the valence
+    // array, plus user_shmem(max local vertices, edges, faces).
+    template <uint32_t blockThreads>
+    void prepare_launch_box(const std::vector<Op> op, LaunchBox<blockThreads>& launch_box,
+                            const void* kernel, const bool oriented = false,
+                            const bool with_vertex_valence = false, const bool is_concurrent = false,
+                            std::function<size_t(uint32_t, uint32_t, uint32_t)> user_shmem =
+                                [](uint32_t, uint32_t, uint32_t) { return (size_t)0; }) const
+    {
+        detail::prepare_launch_box_impl<blockThreads>(*this, op, launch_box, kernel, oriented,
+                                                      with_vertex_valence, is_concurrent, user_shmem);
+    }
+    // run_kernel (rxmesh_static.h:450-505): prepare the launch box for `op`
+    // and launch kernel<<<patches, blockThreads, smem>>>(args...)
+    template <uint32_t blockThreads, typename KernelT, typename... ArgsT>
+    void run_kernel(const std::vector<Op> op, KernelT kernel, ArgsT... args) const
+    {
+        LaunchBox<blockThreads> lb;
+        prepare_launch_box(op, lb, (const void*)kernel);
+        run_kernel(lb, kernel, args...);
+    }
+    template <uint32_t blockThreads, typename KernelT, typename... ArgsT>
+    void run_kernel(const LaunchBox<blockThreads>& lb, KernelT kernel, ArgsT... args) const
+    {
+        kernel<<<lb.blocks, lb.num_threads, lb.smem_bytes_dyn>>>(args...);
+        check_cuda(cudaGetLastError(), "run_kernel launch");
+    }
+#endif
+
    private:
     struct Del
     {
         void operator()(rxg_mesh* m) const { rxg_mesh_destroy(m); }
     };
+    // buffers of one attribute (freed with it)
+    struct AttrStore
+    {
+        std::string           name;
+        const std::type_info* type = nullptr;
+        void*                 d    = nullptr;
+        void*                 h    = nullptr;
+        std::shared_ptr<void> view;
+        AttrStore() = default;
+        AttrStore(const AttrStore&) = delete;
+        AttrStore& operator=(const AttrStore&) = delete;
+        ~AttrStore()
+        {
+            if (d) cudaFree(d);
+            std::free(h);
+        }
+    };
+    std::vector<std::unique_ptr<AttrStore>> m_attrs;
+
+    template <typename T, typename HandleT>
+    std::shared_ptr<Attribute<T, HandleT>> add_attribute(const std::string& name, uint32_t na,
+                                                         locationT location, int64_t n)
+    {
+        if (does_attribute_exist(name)) throw Error(RXG_ERR_INVALID, "attribute " + name + " exists");
+        if (na == 0) throw Error(RXG_ERR_INVALID, "attribute needs at least one value per element");
+        std::unique_ptr<AttrStore> st(new AttrStore);
+        st->name           = name;
+        st->type           = &typeid(Attribute<T, HandleT>);
+        const size_t bytes = sizeof(T) * (size_t)n * na;
+        auto         a     = std::make_shared<Attribute<T, HandleT>>();
+        a->m_n             = n;
+        a->m_num_attr      = na;
+        a->m_alloc         = location;
+        if (location & DEVICE) {
+            check_cuda(cudaMalloc(&st->d, bytes ? bytes : 1), "cudaMalloc");
+            check_cuda(cudaMemset(st->d, 0, bytes), "cudaMemset");
+            a->m_d = static_cast<T*>(st->d);
+        }
+        if (location & HOST) {
+            st->h = std::calloc(bytes ? bytes : 1, 1);
+            if (!st->h) throw Error(RXG_ERR_NOMEM, "attribute host allocation");
+            a->m_h = static_cast<T*>(st->h);
+        }
+        st->view = a;
+        m_attrs.push_back(std::move(st));
+        return a;
+    }
+    template <typename T, typename HandleT>
+    std::shared_ptr<Attribute<T, HandleT>> get_attribute(const std::string& name) const
+    {
+        for (const auto& a : m_attrs)
+            if (a->name == name) {
+                if (*a->type != typeid(Attribute<T, HandleT>))
+                    throw Error(RXG_ERR_INVALID, "attribute " + name + " has another type");
+                return std::static_pointer_cast<Attribute<T, HandleT>>(a->view);
+            }
+        throw Error(RXG_ERR_INVALID, "no attribute " + name);
+    }
+    template <typename HandleT, typename LambdaT>
+    void for_each_element(locationT location, LambdaT& apply, cudaStream_t stream, int64_t n) const
+    {
+        if (location & HOST) {
+            if constexpr (!RXG_IS_D_LAMBDA(LambdaT)) {
+                for (int64_t i = 0; i < n; ++i) apply(HandleT((int32_t)i));
+            } else {
+                throw Error(RXG_ERR_INVALID,
+                            "for_each on HOST needs a host-callable lambda (this one is __device__)");
+            }
+        }
+        if (location & DEVICE) {
+#if defined(__CUDACC__)
+            if constexpr (RXG_DEVICE_CALLABLE(LambdaT))
+                detail::for_each_element_device<HandleT>(*this, apply, stream);
+            else
+                throw Error(RXG_ERR_INVALID,
+                            "for_each on DEVICE needs a __device__ or __host__ __device__ lambda");
+#else
+            (void)stream;
+            throw Error(RXG_ERR_UNSUPPORTED, "for_each on DEVICE needs the caller compiled by nvcc");
+#endif
+        }
+    }
     std::unique_ptr<rxg_mesh, Del> m_mesh;
+
     std::vector<int64_t>           m_region_faces, m_region_vertices;  // cumulative, per file
     std::vector<int32_t>           m_fv;  // the input faces (export_obj)
 
@@ -1005,5 +1398,9 @@ class MeshBatch
 };
 
 }  // namespace rxg
+
+#if defined(__CUDACC__)
+#include "query.cuh"
+#endif
 
 #endif  // RXG_RXMESH_HPP

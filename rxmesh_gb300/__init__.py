@@ -374,6 +374,7 @@ class RXMeshStatic:
         return out
 
 
-from ._solvers import SparseMatrix, CGSolver, PCGSolver, mcf_step, MeshBatch  # noqa: E402
+from ._solvers import (SparseMatrix, CGSolver, PCGSolver, mcf_step, MeshBatch, mcf_matvec,  # noqa: E402
+                       mcf_init_b, mcf_solve_matfree, mcf_step_matfree)
 from ._diff import (DiffScalarProblem, BlockSparseMatrix, NewtonSolver, ArapEnergy, MCFFlow,  # noqa: E402
                     arap_energy, mcf_flow, mcf_step_backward)

@@ -105,6 +105,11 @@ SIGNATURES = {
     "rxg_bcsr_apply_bc": [P, P, P, P],
     "rxg_arap_hvp": [P, I32, P, P, I32, P, P, P, P],
     "rxg_arap_cg_matfree": [P, I32, P, P, I32, P, P, P, P, P, P],
+    "rxg_mesh_device_context": [P, P],
+    "rxg_mcf_matvec": [P, D, I32, I32, P, P, P, P],
+    "rxg_mcf_init_b": [P, I32, I32, P, P, P],
+    "rxg_mcf_solve_matfree": [P, D, I32, I32, P, P, P, P, P, P],
+    "rxg_mcf_step_matfree": [P, D, I32, I32, D, I32, P, P, P],
 }
 _RESTYPE = {"rxg_status_string": ctypes.c_char_p, "rxg_last_error": ctypes.c_char_p,
             "rxg_mesh_destroy": None, "rxg_batch_destroy": None}

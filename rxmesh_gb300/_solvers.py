@@ -175,6 +175,65 @@ def mcf_step(rx, xyz_lin, dt, nsteps=1, precision="f64", tol=1e-6, max_iter=5000
             "final_res": st.final_res}
 
 
+def _mf_flags(uniform, jacobi=False):
+    return (1 if uniform else 0) | (2 if jacobi else 0)
+
+
+def mcf_matvec(rx, xyz_lin, v, dt, uniform=False, jacobi=False, out=None, stream=None):
+    """Matrix-free product of the implicit-MCF operator A = 2M + dt L at
+    positions xyz_lin ((nv,3) float64, linear order) with v ((nv,3) float32
+    or float64): A v, or D^-1 v with jacobi (matvec / precond_matvec,
+    apps/MCF/mcf_kernels.cuh:101-299).  uniform: the uniform Laplacian."""
+    L = _lib.load()
+    out = torch.empty_like(v) if out is None else out
+    dtype = 1 if v.dtype == torch.float64 else 0
+    check(L.rxg_mcf_matvec(rx._h, float(dt), _mf_flags(uniform, jacobi), dtype, _ptr(xyz_lin), _ptr(v),
+                           _ptr(out), _stream(stream)))
+    return out
+
+
+def mcf_init_b(rx, xyz_lin, uniform=False, dtype=torch.float64, stream=None):
+    """Right-hand side B = (1 / v_weight) x of the implicit MCF step
+    (init_B, apps/MCF/mcf_kernels.cuh:58-98)."""
+    L = _lib.load()
+    B = torch.empty(xyz_lin.shape, dtype=dtype, device=xyz_lin.device)
+    check(L.rxg_mcf_init_b(rx._h, _mf_flags(uniform), 1 if dtype == torch.float64 else 0, _ptr(xyz_lin),
+                           _ptr(B), _stream(stream)))
+    return B
+
+
+def mcf_solve_matfree(rx, xyz_lin, B, X, dt, max_iter=5000, abs_tol=0.0, rel_tol=1e-12, precond=True,
+                      uniform=False, stream=None):
+    """Solve A(xyz_lin) X = B with the matrix-free operator
+    (CGMatFreeAttrSolver / PCGMatFreeAttrSolver); X is the initial guess and
+    is overwritten.  Returns the solver stats dict."""
+    L = _lib.load()
+    st = _lib.SolverStats()
+    o = _lib.SolverOpts(int(max_iter), float(abs_tol), float(rel_tol), 1 if precond else 0)
+    rc = L.rxg_mcf_solve_matfree(rx._h, float(dt), _mf_flags(uniform), 1 if X.dtype == torch.float64 else 0,
+                                 _ptr(xyz_lin), _ptr(B), _ptr(X), ctypes.byref(o), ctypes.byref(st),
+                                 _stream(stream))
+    if rc not in (0, 6):
+        check(rc)
+    return {"iters": st.iters, "converged": bool(st.converged), "start_res": st.start_res,
+            "final_res": st.final_res}
+
+
+def mcf_step_matfree(rx, xyz_lin, dt, nsteps=1, tol=1e-6, max_iter=5000, uniform=False, stream=None):
+    """Implicit MCF steps in place on xyz_lin with the matrix-free operator
+    (FP64, Jacobi PCG; run_cg_mat_free, apps/MCF/mcf_cg_mat_free.h)."""
+    L = _lib.load()
+    if xyz_lin.dtype != torch.float64 or not xyz_lin.is_cuda or not xyz_lin.is_contiguous():
+        raise ValueError("xyz_lin must be a contiguous float64 CUDA tensor")
+    st = _lib.SolverStats()
+    rc = L.rxg_mcf_step_matfree(rx._h, float(dt), int(nsteps), _mf_flags(uniform), float(tol), int(max_iter),
+                                _ptr(xyz_lin), ctypes.byref(st), _stream(stream))
+    if rc not in (0, 6):
+        check(rc)
+    return {"iters": st.iters, "converged": bool(st.converged), "start_res": st.start_res,
+            "final_res": st.final_res}
+
+
 class MeshBatch:
     """Many meshes packed for one-launch batched MCF (rxg_batch_*).
 

@@ -437,6 +437,12 @@ struct CGArgs
     int            max_iter;
     double         abs_tol, rel_tol;
     int*           err;
+    // matrix-free MCF operator (k_cg with MF = true): the mesh's
+    // [diagonal, oriented ring] pattern, FP64 positions, the time step
+    const int8_t*  mf_bnd;
+    const double*  mf_xyz;
+    double         mf_dt;
+    int            mf_uniform;
 };
 
 // host side of the grid-sum state (rxg_gridsum.cuh): ticket counter and
@@ -500,6 +506,63 @@ __device__ __forceinline__ void row_spmv_group(const int32_t* __restrict__ rp,
     if (diag) *diag = d;
 }
 
+// Row p of the implicit-MCF operator A = 2M + dt L with its weights
+// recomputed from the positions on every call (the matrix-free matvec of
+// apps/MCF/mcf_kernels.cuh:101-193; cotangent mode as mcf_A_setup, uniform
+// mode: weight 1 per neighbour and the valence as the vertex weight):
+// acc += sum_j A_pj x_j over the row, diag (may be null) = A_pp.  rp/col
+// is the [diagonal, oriented ring] pattern; the arithmetic and its order
+// are k_mcf_assemble's, so a product equals the assembled matrix's.
+template <typename T, typename G, int NC>
+__device__ __forceinline__ void mcf_row(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                                        const int8_t* __restrict__ bnd, const double* __restrict__ xyz,
+                                        T dt, bool uniform, int64_t p, const T* x, T* acc, T* diag)
+{
+    const int32_t  rp   = __ldg(row_ptr + p);
+    const int32_t  k    = __ldg(row_ptr + p + 1) - rp - 1;
+    const int32_t* rg   = col + rp + 1;
+    const bool     wrap = __ldg(bnd + p) == 0;
+    T              area = T(0), sumw = T(0);
+    if (uniform) {
+        for (int32_t i = 0; i < k; ++i) {
+            const int32_t r = __ldg(rg + i);
+            sumw += dt;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) acc[c] -= dt * x[(int64_t)r * NC + c];
+        }
+        area = T(0.5) * (T)k;  // 1 / v_weight = valence
+    } else if (k > 0) {
+        const V3<double> P = ld3(xyz, (int32_t)p);
+        int32_t          qi = __ldg(rg + k - 1), ri = __ldg(rg);
+        V3<double>       Q = ld3(xyz, qi), R = ld3(xyz, ri);
+        for (int32_t i = 0; i < k; ++i) {
+            const int32_t    si    = __ldg(rg + (i + 1 < k ? i + 1 : 0));
+            const V3<double> S     = ld3(xyz, si);
+            const bool       has_q = wrap || i > 0, has_s = wrap || i < k - 1;
+            T                w     = T(0);
+            if (has_q) w += G::hc(P, R, Q);
+            if (has_s) w += G::hc(P, R, S);
+            w = (w >= T(0) ? w : T(0)) * dt;
+            sumw += w;
+#pragma unroll
+            for (int c = 0; c < NC; ++c) acc[c] -= w * x[(int64_t)ri * NC + c];
+            if (has_q) {
+                const T a = G::va(P, Q, R);
+                area += a > T(0) ? a : T(0);
+            }
+            Q  = R;
+            R  = S;
+            ri = si;
+        }
+    }
+    const T vw = T(0.5) / area;
+    const T iv = T(1) / vw;
+    const T dg = iv + sumw;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[c] += dg * x[p * NC + c];
+    if (diag) *diag = dg;
+}
+
 // scalar recurrence of k_cgm, in shared memory, touched by thread 0 only
 struct CGMScalars
 {
@@ -521,8 +584,10 @@ __device__ __forceinline__ bool cgm_sum(double v, double* s_part, GridSum& g, Re
     return grid_sum_staged<BT>(v, s_part, g, r, post);
 }
 
-// L: lanes per matrix row in the two SpMV passes (1, or 4 for long rows)
-template <typename T, int NC, bool PC, int kCGT, int L>
+// L: lanes per matrix row in the two SpMV passes (1, or 4 for long rows).
+// MF: the operator is the matrix-free implicit-MCF one (mcf_row; a.rp and
+// a.col are the mesh's pattern, a.val is unused).
+template <typename T, int NC, bool PC, int kCGT, int L, bool MF = false>
 __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
 {
     __shared__ RedSmem    red;
@@ -548,7 +613,10 @@ __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
 #pragma unroll
         for (int k = 0; k < NC; ++k) acc[k] = T(0);
         T diag = T(0);
-        if (L == 1) row_spmv<T, NC>(a.rp, a.col, a.val, i, a.X, acc, &diag);
+        if constexpr (MF)
+            mcf_row<T, Geo<T>, NC>(a.rp, a.col, a.mf_bnd, a.mf_xyz, (T)a.mf_dt, a.mf_uniform != 0, i,
+                                   a.X, acc, &diag);
+        else if (L == 1) row_spmv<T, NC>(a.rp, a.col, a.val, i, a.X, acc, &diag);
         else row_spmv_group<T, NC, (L > 1 ? L : 2)>(a.rp, a.col, a.val, i, a.X, acc, &diag, lane);
         if (lane != 0) continue;
         const T di = T(1) / (diag + (sizeof(T) == 4 ? (T)FLT_EPSILON : (T)DBL_EPSILON));
@@ -588,7 +656,10 @@ __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
             T acc[NC];
 #pragma unroll
             for (int k = 0; k < NC; ++k) acc[k] = T(0);
-            if (L == 1) row_spmv<T, NC>(a.rp, a.col, a.val, i, src, acc, (T*)nullptr);
+            if constexpr (MF)
+                mcf_row<T, Geo<T>, NC>(a.rp, a.col, a.mf_bnd, a.mf_xyz, (T)a.mf_dt, a.mf_uniform != 0,
+                                       i, src, acc, (T*)nullptr);
+            else if (L == 1) row_spmv<T, NC>(a.rp, a.col, a.val, i, src, acc, (T*)nullptr);
             else row_spmv_group<T, NC, (L > 1 ? L : 2)>(a.rp, a.col, a.val, i, src, acc, (T*)nullptr, lane);
             if (lane != 0) continue;
 #pragma unroll
@@ -662,7 +733,7 @@ static int cg_threads()
     return t;
 }
 
-template <typename T, int NC, bool PC, int BT>
+template <typename T, int NC, bool PC, int BT, bool MF = false>
 static int cg_grid_bt(int64_t n)
 {
     // resident CTAs per SM, per device (0: not looked up yet)
@@ -671,11 +742,11 @@ static int cg_grid_bt(int64_t n)
     if (per_sm <= 0) {
         // the grid must fit whichever variant runs (cooperative launch)
         int p1 = 0, p4 = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p1, k_cg<T, NC, PC, BT, 1>, BT, 0) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p1, k_cg<T, NC, PC, BT, 1, MF>, BT, 0) !=
             cudaSuccess)
             p1 = 1;
         p4 = p1;
-        if constexpr (NC == 1)
+        if constexpr (NC == 1 && !MF)
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p4, k_cg<T, NC, PC, BT, 4>, BT, 0) !=
                 cudaSuccess)
                 p4 = 1;
@@ -689,13 +760,13 @@ static int cg_grid_bt(int64_t n)
     return (int)g;
 }
 
-template <typename T, int NC, bool PC>
+template <typename T, int NC, bool PC, bool MF = false>
 static int cg_grid(int64_t n)
 {
     switch (cg_threads()) {
-        case 256: return cg_grid_bt<T, NC, PC, 256>(n);
-        case 1024: return cg_grid_bt<T, NC, PC, 1024>(n);
-        default: return cg_grid_bt<T, NC, PC, 512>(n);
+        case 256: return cg_grid_bt<T, NC, PC, 256, MF>(n);
+        case 1024: return cg_grid_bt<T, NC, PC, 1024, MF>(n);
+        default: return cg_grid_bt<T, NC, PC, 512, MF>(n);
     }
 }
 
@@ -708,13 +779,27 @@ static size_t cg_scratch_bytes(int64_t n, int nc, int G)
            align256(sizeof(double) * 2 * G) + 3 * 256;
 }
 
-template <typename T, int NC, bool PC>
+// matrix-free operator of the MF launches (unused otherwise)
+struct MatFreeOp
+{
+    const int8_t* bnd     = nullptr;
+    const double* xyz     = nullptr;
+    double        dt      = 0.0;
+    int           uniform = 0;
+};
+
+template <typename T, int NC, bool PC, bool MF = false>
 static rxg_status cg_launch(int64_t n, int64_t nnz, const int32_t* rp, const int32_t* col,
                             const T* val, const T* B, T* X, const rxg_solver_opts& o,
-                            rxg_solver_stats* st, uint8_t* scratch, cudaStream_t s)
+                            rxg_solver_stats* st, uint8_t* scratch, cudaStream_t s,
+                            const MatFreeOp& mf = MatFreeOp())
 {
-    const int  G = cg_grid<T, NC, PC>(n);
+    const int  G = cg_grid<T, NC, PC, MF>(n);
     CGArgs<T>  a;
+    a.mf_bnd     = mf.bnd;
+    a.mf_xyz     = mf.xyz;
+    a.mf_dt      = mf.dt;
+    a.mf_uniform = mf.uniform;
     uint8_t*   q  = scratch;
     const size_t vb = align256(sizeof(T) * n * NC);
     a.n   = n;
@@ -744,7 +829,12 @@ static rxg_status cg_launch(int64_t n, int64_t nnz, const int32_t* rp, const int
     const bool  l4 = n > 0 && nnz >= 12 * n;
     const int   bt = cg_threads();
     const void* kern;
-    if constexpr (NC == 1) {
+    if constexpr (MF) {
+        (void)l4;
+        kern = bt == 256    ? (const void*)k_cg<T, NC, PC, 256, 1, true>
+               : bt == 1024 ? (const void*)k_cg<T, NC, PC, 1024, 1, true>
+                            : (const void*)k_cg<T, NC, PC, 512, 1, true>;
+    } else if constexpr (NC == 1) {
         if (l4)
             kern = bt == 256    ? (const void*)k_cg<T, NC, PC, 256, 4>
                    : bt == 1024 ? (const void*)k_cg<T, NC, PC, 1024, 4>
@@ -1505,6 +1595,229 @@ rxg_status rxg_mcf_step(const rxg_mesh* h, double dt, int32_t nsteps, int32_t pr
     if (st) return st;
     if (stats) *stats = last;
     return last.converged ? RXG_OK : RXG_ERR_NOT_CONVERGED;
+}
+
+}  // extern "C"
+
+namespace rxg {
+
+// ---------------------------------------------------------------------
+// Matrix-free implicit MCF (init_B / matvec / precond_matvec of
+// apps/MCF/mcf_kernels.cuh:58-299, CGMatFreeAttrSolver of
+// matrix/cg_mat_free_attr_solver.h:45-115): the operator's weights are
+// recomputed from the positions on every product (mcf_row), nothing is
+// assembled.  The pattern is the mesh's cached [diagonal, oriented ring].
+// ---------------------------------------------------------------------
+
+// out = A in (JACOBI: out = D^-1 in, D = diag(A)), row-major nv x 3
+template <typename T, bool JACOBI>
+__global__ void __launch_bounds__(256) k_mcf_matvec(int64_t nv, const int32_t* __restrict__ rp,
+                                                    const int32_t* __restrict__ col,
+                                                    const int8_t* __restrict__ bnd,
+                                                    const double* __restrict__ xyz, T dt, int uniform,
+                                                    const T* __restrict__ in, T* __restrict__ out)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nv;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        T acc[3] = {T(0), T(0), T(0)};
+        T dg     = T(0);
+        mcf_row<T, Geo<T>, 3>(rp, col, bnd, xyz, dt, uniform != 0, p, in, acc, &dg);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) out[3 * p + c] = JACOBI ? in[3 * p + c] / dg : acc[c];
+    }
+}
+
+// B = (1 / v_weight) x: 2 x (clamped Voronoi area) x in cotangent mode, the
+// valence x in uniform mode (init_B, mcf_kernels.cuh:58-98)
+template <typename T>
+__global__ void __launch_bounds__(256) k_mcf_init_b(int64_t nv, const int32_t* __restrict__ rp,
+                                                    const int32_t* __restrict__ col,
+                                                    const int8_t* __restrict__ bnd,
+                                                    const double* __restrict__ xyz, int uniform,
+                                                    T* __restrict__ B)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nv;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t  r0   = rp[p];
+        const int32_t  k    = rp[p + 1] - r0 - 1;
+        const int32_t* rg   = col + r0 + 1;
+        const bool     wrap = bnd[p] == 0;
+        T              area = T(0);
+        if (uniform) {
+            area = T(0.5) * (T)k;
+        } else if (k > 0) {
+            const V3<double> P = ld3(xyz, (int32_t)p);
+            V3<double>       Q = ld3(xyz, rg[k - 1]);
+            for (int32_t i = 0; i < k; ++i) {
+                const V3<double> R = ld3(xyz, rg[i]);
+                if (wrap || i > 0) {
+                    const T a = Geo<T>::va(P, Q, R);
+                    area += a > T(0) ? a : T(0);
+                }
+                Q = R;
+            }
+        }
+        const T vw = T(0.5) / area;
+        const T iv = T(1) / vw;
+        const V3<double> P = ld3(xyz, (int32_t)p);
+        B[3 * p + 0] = iv * (T)P.x;
+        B[3 * p + 1] = iv * (T)P.y;
+        B[3 * p + 2] = iv * (T)P.z;
+    }
+}
+
+}  // namespace rxg
+
+using namespace rxg;
+
+extern "C" {
+
+rxg_status rxg_mcf_matvec(const rxg_mesh* h, double dt, int32_t flags, int32_t dtype,
+                          const double* xyz, const void* in, void* out, void* stream)
+{
+    if (!h || !xyz || !in || !out || (dtype != RXG_F32 && dtype != RXG_F64) ||
+        (flags & ~(RXG_MCF_UNIFORM_LAPLACE | RXG_MCF_JACOBI))) {
+        set_error("rxg_mcf_matvec: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    if (!is_device_ptr(xyz) || !is_device_ptr(in) || !is_device_ptr(out)) {
+        set_error("rxg_mcf_matvec: xyz, in and out must be device arrays");
+        return RXG_ERR_INVALID;
+    }
+    Lazy*        z;
+    cudaStream_t s  = S_(stream);
+    rxg_status   st = ensure_pattern(&h->m, s, &z);
+    if (st) return st;
+    const int64_t nv = h->m.nv;
+    const int     g  = grid_for(nv);
+    const int     u  = (flags & RXG_MCF_UNIFORM_LAPLACE) ? 1 : 0;
+    const bool    jc = (flags & RXG_MCF_JACOBI) != 0;
+    if (dtype == RXG_F64) {
+        if (jc)
+            k_mcf_matvec<double, true><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, dt, u,
+                                                         (const double*)in, (double*)out);
+        else
+            k_mcf_matvec<double, false><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, dt, u,
+                                                          (const double*)in, (double*)out);
+    } else {
+        if (jc)
+            k_mcf_matvec<float, true><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, (float)dt,
+                                                        u, (const float*)in, (float*)out);
+        else
+            k_mcf_matvec<float, false><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, (float)dt,
+                                                         u, (const float*)in, (float*)out);
+    }
+    RXG_CUDA_TRY(cudaGetLastError());
+    return RXG_OK;
+}
+
+rxg_status rxg_mcf_init_b(const rxg_mesh* h, int32_t flags, int32_t dtype, const double* xyz, void* B,
+                          void* stream)
+{
+    if (!h || !xyz || !B || (dtype != RXG_F32 && dtype != RXG_F64) ||
+        (flags & ~(RXG_MCF_UNIFORM_LAPLACE | RXG_MCF_JACOBI))) {
+        set_error("rxg_mcf_init_b: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    if (!is_device_ptr(xyz) || !is_device_ptr(B)) {
+        set_error("rxg_mcf_init_b: xyz and B must be device arrays");
+        return RXG_ERR_INVALID;
+    }
+    Lazy*        z;
+    cudaStream_t s  = S_(stream);
+    rxg_status   st = ensure_pattern(&h->m, s, &z);
+    if (st) return st;
+    const int64_t nv = h->m.nv;
+    const int     u  = (flags & RXG_MCF_UNIFORM_LAPLACE) ? 1 : 0;
+    if (dtype == RXG_F64)
+        k_mcf_init_b<double><<<grid_for(nv), 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, u, (double*)B);
+    else
+        k_mcf_init_b<float><<<grid_for(nv), 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, u, (float*)B);
+    RXG_CUDA_TRY(cudaGetLastError());
+    return RXG_OK;
+}
+
+rxg_status rxg_mcf_solve_matfree(const rxg_mesh* h, double dt, int32_t flags, int32_t dtype,
+                                 const double* xyz, const void* B, void* X,
+                                 const rxg_solver_opts* opts, rxg_solver_stats* stats, void* stream)
+{
+    if (!h || !xyz || !B || !X || !opts || opts->max_iter < 0 ||
+        (dtype != RXG_F32 && dtype != RXG_F64) || (flags & ~RXG_MCF_UNIFORM_LAPLACE)) {
+        set_error("rxg_mcf_solve_matfree: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    if (!is_device_ptr(xyz) || !is_device_ptr(B) || !is_device_ptr(X)) {
+        set_error("rxg_mcf_solve_matfree: xyz, B and X must be device arrays");
+        return RXG_ERR_INVALID;
+    }
+    Lazy*        z;
+    cudaStream_t s  = S_(stream);
+    rxg_status   st = ensure_pattern(&h->m, s, &z);
+    if (st) return st;
+    const int64_t    n  = h->m.nv;
+    const bool       pc = opts->precond != 0;
+    MatFreeOp        mf;
+    mf.bnd     = z->bnd;
+    mf.xyz     = xyz;
+    mf.dt      = dt;
+    mf.uniform = (flags & RXG_MCF_UNIFORM_LAPLACE) ? 1 : 0;
+    rxg_solver_stats local;
+    uint8_t*         scratch = nullptr;
+    if (dtype == RXG_F64) {
+        const int G = pc ? cg_grid<double, 3, true, true>(n) : cg_grid<double, 3, false, true>(n);
+        RXG_CUDA_TRY(scratch_alloc((void**)&scratch, cg_scratch_bytes<double>(n, 3, G), s));
+        st = pc ? cg_launch<double, 3, true, true>(n, z->nnz, z->row_ptr, z->col, nullptr, (const double*)B,
+                                                   (double*)X, *opts, &local, scratch, s, mf)
+                : cg_launch<double, 3, false, true>(n, z->nnz, z->row_ptr, z->col, nullptr, (const double*)B,
+                                                    (double*)X, *opts, &local, scratch, s, mf);
+    } else {
+        const int G = pc ? cg_grid<float, 3, true, true>(n) : cg_grid<float, 3, false, true>(n);
+        RXG_CUDA_TRY(scratch_alloc((void**)&scratch, cg_scratch_bytes<float>(n, 3, G), s));
+        st = pc ? cg_launch<float, 3, true, true>(n, z->nnz, z->row_ptr, z->col, nullptr, (const float*)B,
+                                                  (float*)X, *opts, &local, scratch, s, mf)
+                : cg_launch<float, 3, false, true>(n, z->nnz, z->row_ptr, z->col, nullptr, (const float*)B,
+                                                   (float*)X, *opts, &local, scratch, s, mf);
+    }
+    cudaFreeAsync(scratch, s);
+    if (st) return st;
+    if (stats) *stats = local;
+    return local.converged ? RXG_OK : RXG_ERR_NOT_CONVERGED;
+}
+
+rxg_status rxg_mcf_step_matfree(const rxg_mesh* h, double dt, int32_t nsteps, int32_t flags, double tol,
+                                int32_t max_iter, double* xyz, rxg_solver_stats* stats, void* stream)
+{
+    if (!h || !xyz || nsteps < 0 || max_iter <= 0 || !(tol > 0) || (flags & ~RXG_MCF_UNIFORM_LAPLACE)) {
+        set_error("rxg_mcf_step_matfree: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    if (!is_device_ptr(xyz)) {
+        set_error("rxg_mcf_step_matfree: xyz must be a device array");
+        return RXG_ERR_INVALID;
+    }
+    cudaStream_t  s  = S_(stream);
+    const int64_t n  = h->m.nv;
+    double*       xb = nullptr;  // positions of the step's operator, then B
+    RXG_CUDA_TRY(scratch_alloc((void**)&xb, 2 * sizeof(double) * 3 * n, s));
+    double*         Bv = xb + 3 * n;
+    rxg_solver_opts o;
+    o.max_iter = max_iter;
+    o.abs_tol  = 0.0;
+    o.rel_tol  = tol * tol;  // on r.D^-1 r, as rxg_mcf_step
+    o.precond  = 1;
+    rxg_status       st = RXG_OK;
+    rxg_solver_stats local{};
+    for (int32_t k = 0; k < nsteps && st == RXG_OK; ++k) {
+        if (cudaMemcpyAsync(xb, xyz, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+            st = cuda_status(cudaGetLastError(), "cudaMemcpyAsync");
+            break;
+        }
+        if ((st = rxg_mcf_init_b(h, flags, RXG_F64, xb, Bv, s))) break;
+        st = rxg_mcf_solve_matfree(h, dt, flags, RXG_F64, xb, Bv, xyz, &o, &local, s);
+    }
+    cudaFreeAsync(xb, s);
+    if (stats) *stats = local;
+    return st;
 }
 
 }  // extern "C"

@@ -818,6 +818,36 @@ rxg_status rxg_mesh_get_info(const rxg_mesh* h, rxg_mesh_info* info)
     return RXG_OK;
 }
 
+rxg_status rxg_mesh_device_context(const rxg_mesh* h, rxg_device_context* ctx)
+{
+    if (!h || !ctx) {
+        set_error("rxg_mesh_device_context: NULL argument");
+        return RXG_ERR_INVALID;
+    }
+    const Mesh& M = h->m;
+    if (!M.d.hdr || !M.d.arena) {
+        set_error("rxg_mesh_device_context: the mesh has no device copy (built host-only)");
+        return RXG_ERR_INVALID;
+    }
+    static_assert(sizeof(PatchHdr) == 16 * sizeof(int32_t), "patch record is 16 int32");
+    ctx->num_vertices       = M.nv;
+    ctx->num_edges          = M.ne;
+    ctx->num_faces          = M.nf;
+    ctx->num_patches        = M.num_patches;
+    ctx->max_local_vertices = M.max_vl;
+    ctx->max_local_edges    = M.max_el;
+    ctx->max_local_faces    = M.max_fl;
+    ctx->max_owned_vertices = M.max_vo;
+    ctx->max_owned_edges    = M.max_eo;
+    ctx->max_owned_faces    = M.max_fo;
+    ctx->max_valence        = (int32_t)M.max_valence;
+    ctx->max_face_adjacent_faces = M.max_face_faces;
+    ctx->patch_hdr          = reinterpret_cast<const int32_t*>(M.d.hdr);
+    ctx->arena              = M.d.arena;
+    ctx->device             = M.device;
+    return RXG_OK;
+}
+
 rxg_status rxg_mesh_linear_to_input(const rxg_mesh* h, int32_t elem, int32_t* out)
 {
     if (!h || !out || elem < 0 || elem > 2) {

@@ -4,7 +4,8 @@ The other GPU tests compare against the oracle on small meshes; these run
 the same comparisons on the meshes the benchmark measures:
   - torus 1024 x 1024 (1,048,576 vertices, 2,097,152 faces, patches of at
     most 512 faces): VV, VE, VF bit-exact as sorted sets, FV and EV
-    bit-exact in order, both normal weightings within 1e-6;
+    bit-exact in order, both normal weightings within 1e-6 of the
+    magnitude of each vertex's summed face contributions;
   - icosphere level 8 (655,362 vertices), 10 implicit MCF steps at dt 1e-3
     in FP64 and in mixed precision, against the FP64 oracle's 10 steps;
   - cloth 512 x 512 (262,144 vertices, 522,242 faces): per-face ARAP energy,
@@ -68,15 +69,43 @@ def test_torus1024_vertex_queries_bit_exact(oracle, torus1024):
     device_check()
 
 
+def normal_contribution_norms(f, x, weighting):
+    """Per vertex, the sum over its faces of |contribution| (the face's
+    unnormalised normal, divided by the two adjacent squared edge lengths for
+    the max weights): the scale of the rounding error of a floating-point sum
+    of those contributions."""
+    f = np.asarray(f)
+    p = [x[f[:, k]] for k in range(3)]
+    nn = np.linalg.norm(np.cross(p[1] - p[0], p[2] - p[0]), axis=1)
+    l = [np.sum((p[i] - p[(i + 1) % 3]) ** 2, axis=1) for i in range(3)]
+    S = np.zeros(len(x))
+    for i in range(3):
+        np.add.at(S, f[:, i], nn / (l[i] + l[(i + 2) % 3]) if weighting == "max" else nn)
+    return S
+
+
 @pytest.mark.parametrize("weighting", ["max", "area"])
 def test_torus1024_normals(oracle, torus1024, weighting):
+    """FP32 normals against the FP64 oracle on the same FP32 positions.  The
+    N(0, 1e-3) jitter folds the surface at a few vertices, where the face
+    contributions nearly cancel (the worst sum's condition number
+    sum|c_f| / |sum c_f| is 275), so the error is bounded relative to the
+    contributions' magnitude, the forward error bound of a floating-point
+    sum: |n - n_ref| <= 1e-6 sum_f |c_f|.  Relative to each vertex's own
+    normal, 99.99% of the vertices are within 1e-6 and the median is ~5e-8
+    (an FP32 emulation of the same sums in numpy gives the same figures)."""
     x, f, rx = torus1024
     x32 = x.astype(np.float32)
     n = rx.to_input(rx.vertex_normals(rx.to_linear(torch.tensor(x32, device="cuda")), weighting))
     n = n.cpu().numpy()
-    ref = oracle.vertex_normals(f, x32.astype(np.float64), 0 if weighting == "max" else 1)
-    err = np.linalg.norm(n - ref, axis=1) / np.linalg.norm(ref, axis=1)
-    assert err.max() < 1e-6, err.max()
+    x64 = x32.astype(np.float64)
+    ref = oracle.vertex_normals(f, x64, 0 if weighting == "max" else 1)
+    S = normal_contribution_norms(f, x64, weighting)
+    absr = np.linalg.norm(n - ref, axis=1)
+    assert (absr <= 1e-6 * S).all(), (absr / S).max()
+    rel = absr / np.linalg.norm(ref, axis=1)
+    assert (rel <= 1e-6).mean() >= 0.9999, (rel <= 1e-6).mean()
+    assert np.median(rel) <= 1e-7, np.median(rel)
 
 
 def test_torus1024_edge_face_queries_bit_exact(oracle, torus1024):
@@ -161,8 +190,9 @@ def test_cloth512_arap_matches_oracle(oracle, dtype, rtol):
     from rxmesh_gb300 import DiffScalarProblem, RXMeshStatic
     x0, x, f = cloth512()
     # a generic interior state as well as the corner handles, so that every
-    # face has a non-trivial rotation and Hessian
-    x = x + 0.01 * np.random.default_rng(1).normal(size=x.shape)
+    # face has a non-trivial rotation and Hessian; rounded to FP32 so that the
+    # oracle and the FP32 evaluation see the same positions
+    x = (x + 0.01 * np.random.default_rng(1).normal(size=x.shape)).astype(np.float32).astype(np.float64)
     rx = RXMeshStatic(f, len(x0), patch_size=512)
     x0l = rx.to_linear(torch.tensor(x0, device="cuda"))
     xl = rx.to_linear(torch.tensor(x, device="cuda")).to(dtype)
@@ -178,15 +208,38 @@ def test_cloth512_arap_matches_oracle(oracle, dtype, rtol):
     assert np.abs(Hg - H).max() <= rtol * np.abs(H).max()
 
 
+def triangle_angles(x, f):
+    """All corner angles (radians) of the faces f at positions x."""
+    f = np.asarray(f)
+    out = []
+    for k in range(3):
+        a, b, c = x[f[:, k]], x[f[:, (k + 1) % 3]], x[f[:, (k + 2) % 3]]
+        u, v = b - a, c - a
+        cos = np.sum(u * v, axis=1) / (np.linalg.norm(u, axis=1) * np.linalg.norm(v, axis=1))
+        out.append(np.arccos(np.clip(cos, -1.0, 1.0)))
+    return np.concatenate(out)
+
+
 def test_cloth512_adjoint_20_steps_fd():
     """ARAP energy after 20 implicit MCF steps (checkpoints every 5) on the
-    full cloth, d/dx0 through autograd, against FP64 central differences
-    (h = 1e-6) on 16 random directions.  The grid is jittered by N(0, 0.1):
-    the reference's Voronoi area (geometry_util.cuh:117-167) jumps when an
-    angle crosses 90 degrees, and an unjittered grid has every quad corner at
-    exactly 90 degrees, where the flow has no derivative."""
+    full 512 x 512 cloth, d/dx0 through autograd, against FP64 central
+    differences (h = 1e-6) on 16 random directions over all vertices.
+
+    The reference's Voronoi area (geometry_util.cuh:117-167) jumps when a
+    triangle angle crosses 90 degrees, so the flow has no derivative there and
+    a difference quotient across a jump is meaningless.  A create_plane grid
+    has every quad corner at exactly 90 degrees, and a jittered one has
+    ~1.5 M angles spread around 90: somewhere on the full mesh a perturbation
+    of 1e-6 then crosses the jump.  The grid is therefore sheared by 0.3 of y
+    (quad corners at 73 and 107 degrees) before the corner handles and a
+    N(0, 0.01) jitter are applied, and the test first checks that every
+    angle stays at least 0.05 rad from 90 degrees."""
     from rxmesh_gb300 import DiffScalarProblem, RXMeshStatic, arap_energy, mcf_flow
-    x0r, x, f = cloth512(jitter=0.1, seed=3)
+    x0r, x, f = cloth512()
+    x = x.copy()
+    x[:, 0] += 0.3 * x[:, 1]
+    x += 0.01 * np.random.default_rng(3).normal(size=x.shape)
+    assert np.abs(triangle_angles(x, f) - np.pi / 2).min() > 0.05
     rx = RXMeshStatic(f, len(x), patch_size=512)
     rest = rx.to_linear(torch.tensor(x0r, device="cuda"))
     prob = DiffScalarProblem(rx, torch.float64, assemble_hessian=False).add_arap_term(rest)
