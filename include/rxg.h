@@ -463,16 +463,18 @@ rxg_status rxg_batch_autotune(rxg_batch* b, double dt, int32_t nsteps, double to
 /* Per-face ARAP energy, gradient, Hessian (DiffScalarProblem path)     */
 /* ------------------------------------------------------------------ */
 
-/* 3x3-block CSR over the [diagonal, one-ring] pattern of rxg_mcf_pattern_size
- * (HessianSparseMatrix<T,3>, diff/hessian_sparse_matrix.h:16-137); val holds
- * nnzb row-major 3x3 blocks. */
+/* D x D-block CSR over the [diagonal, one-ring] pattern of
+ * rxg_mcf_pattern_size (HessianSparseMatrix<T,K>,
+ * diff/hessian_sparse_matrix.h:16-137); val holds nnzb row-major D x D
+ * blocks.  block_dim: 2 or 3 (0 means 3). */
 typedef struct rxg_bcsr {
-    int64_t  n;       /* block rows */
-    int64_t  nnzb;    /* blocks */
-    int32_t* row_ptr; /* device, n+1 */
-    int32_t* col;     /* device, nnzb */
-    void*    val;     /* device, 9*nnzb of dtype */
+    int64_t  n;         /* block rows */
+    int64_t  nnzb;      /* blocks */
+    int32_t* row_ptr;   /* device, n+1 */
+    int32_t* col;       /* device, nnzb */
+    void*    val;       /* device, D*D*nnzb of dtype */
     int32_t  dtype;
+    int32_t  block_dim; /* D: 2 or 3; 0 = 3 */
 } rxg_bcsr;
 
 /*
@@ -510,6 +512,41 @@ enum { RXG_ARAP_PROJECT_HESSIAN = 1 };
 rxg_status rxg_arap_eval_ex(const rxg_mesh* m, int32_t dtype, const void* x,
                             const void* rest, int32_t flags, double* energy,
                             void* face_E, void* grad, rxg_bcsr* hess, void* stream);
+
+/*
+ * Generic per-face energy terms (DiffScalarProblem::add_term<Op::FV,
+ * ProjectHess>(lambda), diff/diff_scalar_problem.h:127-194): an energy of
+ * the D components of each face's three vertices (D = 2, e.g. uv, or 3).
+ * A term is evaluated face by face into records of
+ * 1 + 3D + 3D(3D+1)/2 values of dtype each (E, the gradient in the order
+ * corner 0 components, corner 1, corner 2 -- the face's vertices in input
+ * order -- then the Hessian's upper triangle, row-major), nf records in face
+ * linear order, by the library's built-in terms or by an application's own
+ * kernel (include/rxg/diff.cuh: Scalar<T, K, Hess>, face_term_kernel).
+ * rxg_face_term_gather assembles them: energy (host or device double, may
+ * be NULL) = the sum of the face energies, face_E (nf of dtype, may be
+ * NULL), grad (nv*D, may be NULL) and hess (D x D blocks, D*D*nnzb values,
+ * over the [diagonal, one-ring] pattern of rxg_mcf_pattern_size; may be
+ * NULL).  RXG_TERM_ACCUMULATE adds into grad and hess (the sum of several
+ * terms) instead of overwriting them.  Needs a manifold mesh.
+ */
+enum { RXG_TERM_ACCUMULATE = 1, RXG_TERM_PROJECT_HESSIAN = 2 };
+rxg_status rxg_face_term_gather(const rxg_mesh* m, int32_t dtype, int32_t dim, const void* records,
+                                int32_t flags, double* energy, void* face_E, void* grad,
+                                rxg_bcsr* hess, void* stream);
+/*
+ * The symmetric Dirichlet energy of Param (apps/Param/param.cu:146-183), a
+ * built-in term with D = 2: per face E = A (|J|_F^2 + |J^-1|_F^2), J = M
+ * Mr^-1, M = [b - a, c - a] of the uv positions (uv: nv*2 of dtype, linear
+ * order), rest = Mr^-1 per face (nf*4, rxg_arap_rest), A = det(Mr) / 2; a
+ * face with det(M) <= 0 gets the largest finite value and no derivatives,
+ * as the reference's energy returns.  flags: RXG_TERM_PROJECT_HESSIAN (each
+ * face's 6x6 Hessian made positive definite, project_positive_definite),
+ * RXG_TERM_ACCUMULATE.  Outputs as rxg_face_term_gather (hess: 2x2 blocks).
+ */
+rxg_status rxg_symdir_eval(const rxg_mesh* m, int32_t dtype, const void* uv, const void* rest,
+                           int32_t flags, double* energy, void* face_E, void* grad, rxg_bcsr* hess,
+                           void* stream);
 
 /*
  * Scalar CSR (3n x 3n) of a 3x3-block CSR, the form the reference's

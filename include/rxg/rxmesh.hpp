@@ -40,6 +40,9 @@
 #include <vector>
 
 #include "../rxg.h"
+#if defined(__CUDACC__)
+#include "diff.cuh"  // Scalar and face_term_kernel behind DiffScalarProblem::add_term
+#endif
 
 namespace rxg {
 
@@ -1132,20 +1135,24 @@ template <typename T>
 class BlockSparseMatrix
 {
    public:
-    BlockSparseMatrix(int64_t n, int64_t nnzb) : m_n(n), m_row_ptr(n + 1), m_col(nnzb), m_val(9 * nnzb)
+    // n block rows, nnzb blocks of dim x dim (HessianSparseMatrix<T, dim>)
+    BlockSparseMatrix(int64_t n, int64_t nnzb, int dim = 3)
+        : m_n(n), m_dim(dim), m_row_ptr(n + 1), m_col(nnzb), m_val((size_t)(dim * dim * nnzb))
     {
     }
     rxg_bcsr bcsr()
     {
         rxg_bcsr b;
-        b.n       = m_n;
-        b.nnzb    = (int64_t)m_col.size();
-        b.row_ptr = m_row_ptr.data();
-        b.col     = m_col.data();
-        b.val     = m_val.data();
-        b.dtype   = dtype_of<T>::value;
+        b.n         = m_n;
+        b.nnzb      = (int64_t)m_col.size();
+        b.row_ptr   = m_row_ptr.data();
+        b.col       = m_col.data();
+        b.val       = m_val.data();
+        b.dtype     = dtype_of<T>::value;
+        b.block_dim = m_dim;
         return b;
     }
+    int block_dim() const { return m_dim; }
     int64_t               rows() const { return m_n; }
     int64_t               non_zero_blocks() const { return (int64_t)m_col.size(); }
     // the scalar 3n x 3n form the CG/PCG solvers take (out: 3n rows, 9 nnzb)
@@ -1167,6 +1174,7 @@ class BlockSparseMatrix
 
    private:
     int64_t              m_n;
+    int                  m_dim;
     DeviceArray<int32_t> m_row_ptr, m_col;
     DeviceArray<T>       m_val;
 };
@@ -1175,42 +1183,60 @@ class BlockSparseMatrix
 // (DiffScalarProblem<T, 3, VertexHandle, true>, diff_scalar_problem.h:27-401;
 // the reference takes a user lambda per face, which a C ABI cannot carry, so
 // the term is fixed: add_arap_term(rest positions)).
-template <typename T>
+template <typename T, int VariableDim = 3>
 class DiffScalarProblem
 {
    public:
+    static_assert(VariableDim == 2 || VariableDim == 3, "2 or 3 components per vertex");
     explicit DiffScalarProblem(const RXMeshStatic& rx, bool assemble_hessian = true) : m_rx(&rx)
     {
         int64_t n = 0, nnz = 0;
         check(rxg_mcf_pattern_size(rx.handle(), &n, &nnz));
-        grad = DenseMatrix<T>(n, 3);
+        grad = DenseMatrix<T>(n, VariableDim);
         face_energy.resize(rx.get_num_faces());
-        if (assemble_hessian) hess.reset(new BlockSparseMatrix<T>(n, nnz));
+        if (assemble_hessian) hess.reset(new BlockSparseMatrix<T>(n, nnz, VariableDim));
     }
     // rest: linear-order FP64 positions of the flat rest shape
     // project_hessian: the reference's add_term<Op::FV, ProjectHess = true>
     void add_arap_term(const DenseMatrix<double>& rest, cudaStream_t s = nullptr,
                        bool project_hessian = false)
     {
+        static_assert(VariableDim == 3, "the ARAP term is on 3-D positions");
         m_project = project_hessian;
         m_rest.resize(4 * (size_t)m_rx->get_num_faces());
         check(rxg_arap_rest(m_rx->handle(), rest.data(), dtype_of<T>::value, m_rest.data(), s));
     }
+#if defined(__CUDACC__)
+    // add_term<Op::FV, ProjectHess>(energy) (diff_scalar_problem.h:127-194):
+    // energy(face id, const Scalar<T, 3 * VariableDim, true>* v) -> Scalar,
+    // a __device__ lambda or functor, where v[k * VariableDim + d] is
+    // component d of the face's corner k (its vertices in input order, the
+    // optimisation variable in linear order).  Terms add up.
+    template <Op op, bool ProjectHess = false, typename LambdaT>
+    void add_term(LambdaT energy)
+    {
+        static_assert(op == Op::FV, "terms are per face (Op::FV)");
+        if (m_fv.size() == 0) {
+            QueryResult q = m_rx->query(Op::FV);
+            m_fv          = std::move(q.values);
+        }
+        const int64_t  nf = m_rx->get_num_faces();
+        const int32_t* fv = m_fv.data();
+        m_terms.push_back([=](const T* x, T* rec, cudaStream_t s) {
+            check_cuda(launch_face_term<T, VariableDim, ProjectHess>(nf, fv, x, energy, rec, s),
+                       "face term launch");
+        });
+    }
+#endif
     // evaluate at linear-order positions x (eval_terms, diff_scalar_problem.h:310-321)
     void eval_terms(const DenseMatrix<T>& x, cudaStream_t s = nullptr)
     {
-        if (!m_rest.size()) throw Error(RXG_ERR_INVALID, "add_arap_term() first");
-        rxg_bcsr  b  = hess ? hess->bcsr() : rxg_bcsr{};
-        check(rxg_arap_eval_ex(m_rx->handle(), dtype_of<T>::value, x.data(), m_rest.data(),
-                               m_project ? RXG_ARAP_PROJECT_HESSIAN : 0, &m_loss,
-                               face_energy.data(), grad.data(), hess ? &b : nullptr, s));
+        run(x, true, s);
     }
     // energy alone (eval_terms_passive): gradient and Hessian untouched
     T eval_terms_passive(const DenseMatrix<T>& x, cudaStream_t s = nullptr)
     {
-        if (!m_rest.size()) throw Error(RXG_ERR_INVALID, "add_arap_term() first");
-        check(rxg_arap_eval_ex(m_rx->handle(), dtype_of<T>::value, x.data(), m_rest.data(), 0,
-                               &m_loss, nullptr, nullptr, nullptr, s));
+        run(x, false, s);
         return (T)m_loss;
     }
     // y = H(x) v without an assembled Hessian (eval_matvec); bc may be null
@@ -1239,6 +1265,44 @@ class DiffScalarProblem
     DeviceArray<T>                        face_energy;
     std::unique_ptr<BlockSparseMatrix<T>> hess;
 
+   private:
+    // the ARAP term (if added) first, then the added terms, accumulated
+    void run(const DenseMatrix<T>& x, bool derivatives, cudaStream_t s)
+    {
+        if (!m_rest.size() && m_terms.empty()) throw Error(RXG_ERR_INVALID, "add a term first");
+        rxg_bcsr b    = hess ? hess->bcsr() : rxg_bcsr{};
+        rxg_bcsr* hb  = (derivatives && hess) ? &b : nullptr;
+        T*        g   = derivatives ? grad.data() : nullptr;
+        T*        fe  = derivatives ? face_energy.data() : nullptr;
+        double    sum = 0.0;
+        bool      first = true;
+        if (m_rest.size()) {
+            check(rxg_arap_eval_ex(m_rx->handle(), dtype_of<T>::value, x.data(), m_rest.data(),
+                                   (m_project && derivatives) ? RXG_ARAP_PROJECT_HESSIAN : 0, &m_loss,
+                                   fe, g, hb, s));
+            sum   = m_loss;
+            first = false;
+        }
+        if (!m_terms.empty()) {
+            constexpr int K     = 3 * VariableDim;  // record: E, gradient, packed Hessian
+            const size_t  words = (size_t)(1 + K + K * (K + 1) / 2);
+            if (m_rec.size() != words * (size_t)m_rx->get_num_faces())
+                m_rec.resize(words * (size_t)m_rx->get_num_faces());
+            for (auto& launch : m_terms) {
+                launch(x.data(), m_rec.data(), s);
+                double e = 0.0;
+                check(rxg_face_term_gather(m_rx->handle(), dtype_of<T>::value, VariableDim, m_rec.data(),
+                                           first ? 0 : RXG_TERM_ACCUMULATE, &e, first ? fe : nullptr, g,
+                                           hb, s));
+                sum += e;
+                first = false;
+            }
+        }
+        m_loss = sum;
+    }
+    std::vector<std::function<void(const T*, T*, cudaStream_t)>> m_terms;
+    DeviceArray<int32_t>                                         m_fv;
+    DeviceArray<T>                                               m_rec;
    private:
     const RXMeshStatic* m_rx;
     DeviceArray<T>      m_rest;

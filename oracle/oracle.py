@@ -347,3 +347,21 @@ def arap_assemble(fv, x, minv, area, rp, col, want_hess=True, project=False, eps
                                    np.ascontiguousarray(col, np.int32), fe.ctypes.data, g.ctypes.data,
                                    H.ctypes.data if want_hess else None, int(project), float(eps))
     return E, fe, g.reshape(nv, 3), (H.reshape(nnz, 3, 3) if want_hess else None)
+
+
+def symmetric_dirichlet(fv, uv, rest_minv):
+    """Per-face symmetric Dirichlet energy of apps/Param/param.cu:146-183:
+    M = [b - a, c - a] of the uv positions (nv, 2), J = M Mr^{-1} with the
+    face's rest-frame inverse rest_minv (nf, 4, row-major, as rest_frame
+    returns it), A = det(Mr) / 2, E = A (|J|_F^2 + |J^{-1}|_F^2); +inf-like
+    (the largest double) where det(M) <= 0.  FP64, vectorised over faces."""
+    f = np.asarray(fv, np.int64)
+    a, b, c = uv[f[:, 0]], uv[f[:, 1]], uv[f[:, 2]]
+    M = np.stack([b - a, c - a], axis=2)  # columns: edge vectors
+    mi = np.asarray(rest_minv, np.float64).reshape(-1, 2, 2)
+    A = 0.5 / np.linalg.det(mi)
+    J = M @ mi
+    dM = np.linalg.det(M)
+    Ji = np.linalg.inv(np.where(dM[:, None, None] > 0, J, np.eye(2)))
+    E = A * ((J ** 2).sum((1, 2)) + (Ji ** 2).sum((1, 2)))
+    return np.where(dM > 0, E, np.finfo(np.float64).max)

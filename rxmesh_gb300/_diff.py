@@ -1,10 +1,14 @@
-"""DiffScalarProblem mirror for the per-face ARAP term, and the torch autograd
-bindings of the differentiable path.
+"""DiffScalarProblem mirror and the torch autograd bindings of the
+differentiable path.
 
 DiffScalarProblem (include/rxmesh/diff/diff_scalar_problem.h:27-401) takes
-user lambdas; lambdas cannot cross the C ABI, so the one energy of this path
-(per-face ARAP against a flat rest frame) is a fixed term here:
-`DiffScalarProblem(rx).add_arap_term(rest_xyz)` then `eval_terms(x)`.
+user lambdas over a forward-mode Scalar; lambdas cannot cross the C ABI, so
+from Python the terms are the library's built-in per-face energies:
+`add_arap_term(rest_xyz)` (3 components per vertex) and
+`add_symmetric_dirichlet_term(rest_xyz)` (Param's energy on 2-D uv), each
+evaluated through the forward-mode Scalar type of include/rxg/diff.cuh or
+its closed form, and summed by eval_terms(x).  C++ applications write their
+own terms with include/rxg/diff.cuh and rxg_face_term_gather.
 """
 import ctypes
 
@@ -14,6 +18,8 @@ from . import _lib
 from ._lib import check
 
 _DT = {torch.float32: 0, torch.float64: 1}
+RXG_TERM_ACCUMULATE = 1
+RXG_TERM_PROJECT_HESSIAN = 2
 
 
 def _stream(stream=None):
@@ -27,23 +33,25 @@ def _p(t):
 
 
 class BlockSparseMatrix:
-    """3x3-block CSR over the [diagonal, one-ring] pattern (HessianSparseMatrix)."""
+    """D x D-block CSR over the [diagonal, one-ring] pattern
+    (HessianSparseMatrix<T, D>); D = dim, 3 by default."""
 
-    def __init__(self, n, nnzb, dtype, device):
+    def __init__(self, n, nnzb, dtype, device, dim=3):
+        self.dim = int(dim)
         self.row_ptr = torch.zeros(n + 1, dtype=torch.int32, device=device)
         self.col = torch.zeros(nnzb, dtype=torch.int32, device=device)
-        self.val = torch.zeros(nnzb, 3, 3, dtype=dtype, device=device)
+        self.val = torch.zeros(nnzb, self.dim, self.dim, dtype=dtype, device=device)
 
     def to_csr(self, out=None, stream=None):
-        """Scalar 3n x 3n CSR of this block matrix (rxg_bcsr_to_csr), the form
-        the CG/PCG solvers take; out: a SparseMatrix of the right sizes to reuse."""
+        """Scalar (D n) x (D n) CSR of this block matrix (rxg_bcsr_to_csr), the
+        form the CG/PCG solvers take; out: a SparseMatrix of the right sizes to reuse."""
         from ._solvers import SparseMatrix
-        n, nnzb = self.row_ptr.numel() - 1, self.col.numel()
+        n, nnzb, d = self.row_ptr.numel() - 1, self.col.numel(), self.dim
         if out is None:
             dev = self.val.device
-            out = SparseMatrix(row_ptr=torch.empty(3 * n + 1, dtype=torch.int32, device=dev),
-                               col=torch.empty(9 * nnzb, dtype=torch.int32, device=dev),
-                               val=torch.empty(9 * nnzb, dtype=self.val.dtype, device=dev))
+            out = SparseMatrix(row_ptr=torch.empty(d * n + 1, dtype=torch.int32, device=dev),
+                               col=torch.empty(d * d * nnzb, dtype=torch.int32, device=dev),
+                               val=torch.empty(d * d * nnzb, dtype=self.val.dtype, device=dev))
         b, c = self.bcsr(), out.csr()
         check(_lib.load().rxg_bcsr_to_csr(ctypes.byref(b), ctypes.byref(c), _stream(stream)))
         return out
@@ -64,84 +72,144 @@ class BlockSparseMatrix:
         b.col = self.col.data_ptr()
         b.val = self.val.data_ptr()
         b.dtype = _DT[self.val.dtype]
+        b.block_dim = self.dim
         return b
 
     def to_scipy(self):
         import scipy.sparse as sp
-        n = self.row_ptr.numel() - 1
+        n, d = self.row_ptr.numel() - 1, self.dim
         return sp.bsr_matrix((self.val.cpu().numpy(), self.col.cpu().numpy(),
-                              self.row_ptr.cpu().numpy()), shape=(3 * n, 3 * n))
+                              self.row_ptr.cpu().numpy()), shape=(d * n, d * n))
 
 
 class DiffScalarProblem:
-    """Energy / gradient / Hessian assembly driver (DiffScalarProblem<T,3,VertexHandle,true>)."""
+    """Energy / gradient / Hessian assembly driver
+    (DiffScalarProblem<T, dim, VertexHandle, true>): the sum of its terms.
 
-    def __init__(self, rx, dtype=torch.float64, assemble_hessian=True):
+    dim: components of the optimisation variable per vertex (3 for the ARAP
+    term on positions, 2 for the symmetric Dirichlet term on uv)."""
+
+    def __init__(self, rx, dtype=torch.float64, assemble_hessian=True, dim=3):
         self.rx = rx
         self.dtype = dtype
+        self.dim = int(dim)
         self.assemble_hessian = assemble_hessian
         self._L = _lib.load()
         dev = torch.device("cuda", torch.cuda.current_device())
         n, nnz = ctypes.c_int64(), ctypes.c_int64()
         check(self._L.rxg_mcf_pattern_size(rx._h, ctypes.byref(n), ctypes.byref(nnz)))
-        self.grad = torch.zeros(n.value, 3, dtype=dtype, device=dev)
+        self.grad = torch.zeros(n.value, self.dim, dtype=dtype, device=dev)
         self.face_energy = torch.zeros(rx.get_num_faces(), dtype=dtype, device=dev)
-        self.hess = BlockSparseMatrix(n.value, nnz.value, dtype, dev) if assemble_hessian else None
+        self.hess = (BlockSparseMatrix(n.value, nnz.value, dtype, dev, self.dim)
+                     if assemble_hessian else None)
+        self.terms = []  # (kind, rest frames Mr^-1 (nf, 4), project)
         self.rest = None
         self.project_hessian = False
         self.opt_var = None
         self._loss = None
+        self._tmp_face = None
+
+    def _rest_frames(self, rest_xyz_lin):
+        xr = rest_xyz_lin.to(torch.float64).contiguous()
+        rest = torch.empty(self.rx.get_num_faces(), 4, dtype=self.dtype, device=xr.device)
+        check(self._L.rxg_arap_rest(self.rx._h, _p(xr), _DT[self.dtype], _p(rest), _stream()))
+        return rest
 
     def add_arap_term(self, rest_xyz_lin, project_hessian=False):
         """Per-face ARAP term against the flat rest frame of rest_xyz_lin (nv,3,
         linear order).  project_hessian: each face's 9x9 Hessian made positive
-        definite before assembly (add_term<Op::FV, ProjectHess = true>)."""
+        definite before assembly (add_term<Op::FV, ProjectHess = true>).
+        Needs dim = 3 and comes first among the terms."""
+        if self.dim != 3 or self.terms:
+            raise ValueError("the ARAP term needs dim=3 and is the problem's first term")
         self.project_hessian = bool(project_hessian)
-        xr = rest_xyz_lin.to(torch.float64).contiguous()
-        self.rest = torch.empty(self.rx.get_num_faces(), 4, dtype=self.dtype, device=xr.device)
-        check(self._L.rxg_arap_rest(self.rx._h, _p(xr), _DT[self.dtype], _p(self.rest), _stream()))
+        self.rest = self._rest_frames(rest_xyz_lin)
+        self.terms.append(("arap", self.rest, self.project_hessian))
         return self
 
-    def eval_terms(self, x_lin=None, with_hessian=None, stream=None):
-        """Energy, gradient (and Hessian) at x_lin (nv,3, linear order), which
-        becomes the problem's opt_var (x_lin None: at the current opt_var)."""
+    def add_symmetric_dirichlet_term(self, rest_xyz_lin, project_hessian=False):
+        """Param's symmetric Dirichlet energy (apps/Param/param.cu:146-183) of
+        the uv parameterisation (opt_var (nv,2)): per face A (|J|^2 +
+        |J^-1|^2), J = M Mr^-1 with Mr the face's rest shape in its own plane
+        (rest_xyz_lin (nv,3), linear order).  Needs dim = 2."""
+        if self.dim != 2:
+            raise ValueError("the symmetric Dirichlet term needs dim=2 (uv)")
+        rest = self._rest_frames(rest_xyz_lin)
         if self.rest is None:
-            raise RuntimeError("add_arap_term() first")
+            self.rest = rest
+        self.terms.append(("symdir", rest, bool(project_hessian)))
+        return self
+
+    def _eval(self, x, grad, face_E, hess_b, with_projection=True, stream=None):
+        """Sum of the terms at x; returns the energy (1-element FP64 tensor)."""
+        if not self.terms:
+            raise RuntimeError("add a term first")
+        total = torch.zeros(1, dtype=torch.float64, device=x.device)
+        for i, (kind, rest, proj) in enumerate(self.terms):
+            e = torch.zeros(1, dtype=torch.float64, device=x.device)
+            fe = face_E
+            if fe is not None and i > 0:
+                if self._tmp_face is None:
+                    self._tmp_face = torch.empty_like(self.face_energy)
+                fe = self._tmp_face
+            hb = ctypes.byref(hess_b) if hess_b is not None else None
+            pj = proj and with_projection
+            if kind == "arap":
+                check(self._L.rxg_arap_eval_ex(self.rx._h, _DT[self.dtype], _p(x), _p(rest),
+                                               1 if pj else 0, _p(e), _p(fe), _p(grad), hb,
+                                               _stream(stream)))
+            else:
+                flags = (RXG_TERM_ACCUMULATE if i > 0 else 0) | (RXG_TERM_PROJECT_HESSIAN if pj else 0)
+                check(self._L.rxg_symdir_eval(self.rx._h, _DT[self.dtype], _p(x), _p(rest), flags,
+                                              _p(e), _p(fe), _p(grad), hb, _stream(stream)))
+            if fe is not None and i > 0:
+                face_E.add_(fe)
+            total += e
+        return total
+
+    def eval_terms(self, x_lin=None, with_hessian=None, stream=None):
+        """Energy, gradient (and Hessian) at x_lin (nv, dim, linear order),
+        which becomes the problem's opt_var (x_lin None: at the current opt_var)."""
         if x_lin is not None:
             self.opt_var = x_lin
         x = self.opt_var.to(self.dtype).contiguous()
         h = self.assemble_hessian if with_hessian is None else with_hessian
-        e = torch.zeros(1, dtype=torch.float64, device=x.device)
         b = self.hess.bcsr() if (h and self.hess is not None) else None
-        check(self._L.rxg_arap_eval_ex(self.rx._h, _DT[self.dtype], _p(x), _p(self.rest),
-                                       1 if self.project_hessian else 0, _p(e),
-                                       _p(self.face_energy), _p(self.grad),
-                                       ctypes.byref(b) if b is not None else None, _stream(stream)))
-        self._loss = e
-        return e
+        self._loss = self._eval(x, self.grad, self.face_energy, b, stream=stream)
+        return self._loss
 
     def eval_terms_passive(self, x_lin, stream=None):
         """Energy alone at x_lin (eval_terms_passive, diff_scalar_problem.h):
         gradient, Hessian and opt_var are left untouched."""
         x = x_lin.to(self.dtype).contiguous()
-        e = torch.zeros(1, dtype=torch.float64, device=x.device)
-        check(self._L.rxg_arap_eval_ex(self.rx._h, _DT[self.dtype], _p(x), _p(self.rest), 0,
-                                       _p(e), None, None, None, _stream(stream)))
-        self._loss = e
-        return e
+        self._loss = self._eval(x, None, None, None, with_projection=False, stream=stream)
+        return self._loss
 
     def eval_matvec(self, v, out=None, bc=None, stream=None):
-        """out = H(opt_var) v without an assembled Hessian (eval_matvec,
-        diff/diff_query_kernel.cuh:26-148; rxg_arap_hvp); bc (nv,) int8/bool:
-        identity rows and zero columns for constrained vertices."""
+        """out = H(opt_var) v (eval_matvec, diff/diff_query_kernel.cuh:26-148):
+        for the ARAP term without an assembled Hessian (rxg_arap_hvp); for
+        the other terms through the assembled Hessian's scalar form.  bc
+        (nv,) int8/bool: identity rows and zero columns for constrained
+        vertices."""
         x = self.opt_var.to(self.dtype).contiguous()
         vv = v.to(self.dtype).contiguous()
         if out is None:
             out = torch.empty_like(vv)
         m = bc.to(torch.int8).contiguous() if bc is not None else None
-        check(self._L.rxg_arap_hvp(self.rx._h, _DT[self.dtype], _p(x), _p(self.rest),
-                                   1 if self.project_hessian else 0, _p(m), _p(vv), _p(out),
-                                   _stream(stream)))
+        if len(self.terms) == 1 and self.terms[0][0] == "arap":
+            check(self._L.rxg_arap_hvp(self.rx._h, _DT[self.dtype], _p(x), _p(self.rest),
+                                       1 if self.project_hessian else 0, _p(m), _p(vv), _p(out),
+                                       _stream(stream)))
+            return out
+        H = self.hess
+        if H is None:
+            nn, nz = ctypes.c_int64(), ctypes.c_int64()
+            check(self._L.rxg_mcf_pattern_size(self.rx._h, ctypes.byref(nn), ctypes.byref(nz)))
+            H = BlockSparseMatrix(nn.value, nz.value, self.dtype, x.device, self.dim)
+        self._eval(x, torch.empty_like(self.grad), None, H.bcsr(), stream=stream)
+        if m is not None:
+            H.apply_bc(m, None, stream)
+        H.to_csr(stream=stream).multiply(vv.reshape(-1, 1), out.view(-1, 1), stream)
         return out
 
     def get_current_loss(self):

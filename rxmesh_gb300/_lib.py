@@ -43,7 +43,8 @@ class CSR(ctypes.Structure):
 
 class BCSR(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64), ("nnzb", ctypes.c_int64), ("row_ptr", ctypes.c_void_p),
-                ("col", ctypes.c_void_p), ("val", ctypes.c_void_p), ("dtype", ctypes.c_int32)]
+                ("col", ctypes.c_void_p), ("val", ctypes.c_void_p), ("dtype", ctypes.c_int32),
+                ("block_dim", ctypes.c_int32)]
 
 
 class SolverOpts(ctypes.Structure):
@@ -110,6 +111,8 @@ SIGNATURES = {
     "rxg_mcf_init_b": [P, I32, I32, P, P, P],
     "rxg_mcf_solve_matfree": [P, D, I32, I32, P, P, P, P, P, P],
     "rxg_mcf_step_matfree": [P, D, I32, I32, D, I32, P, P, P],
+    "rxg_face_term_gather": [P, I32, I32, P, I32, P, P, P, P, P],
+    "rxg_symdir_eval": [P, I32, P, P, I32, P, P, P, P, P],
 }
 _RESTYPE = {"rxg_status_string": ctypes.c_char_p, "rxg_last_error": ctypes.c_char_p,
             "rxg_mesh_destroy": None, "rxg_batch_destroy": None}

@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "librxg.so")
 
-SOURCES = ["rxg_mesh.cpp", "rxg_patchfile.cpp", "rxg_patcher.cu", "rxg_query.cu", "rxg_mcf.cu", "rxg_onchip.cu", "rxg_dense.cu", "rxg_arap.cu", "rxg_batch.cu"]
+SOURCES = ["rxg_mesh.cpp", "rxg_patchfile.cpp", "rxg_patcher.cu", "rxg_query.cu", "rxg_mcf.cu", "rxg_onchip.cu", "rxg_dense.cu", "rxg_arap.cu", "rxg_batch.cu", "rxg_term.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + os.path.join(HERE, "..", "include")]
 

@@ -900,28 +900,29 @@ __global__ void __launch_bounds__(BT) k_cg_matfree(MatFreeArgs<T> a)
 // Block-CSR helpers of the Newton step (diff/newton_solver.h)
 // ---------------------------------------------------------------------
 
-// scalar CSR of a 3x3-block CSR: scalar row 3i+a lists, block by block in
-// the block row's order, the three entries (3j+0..2) of each block (i,j)
-template <typename T>
+// scalar CSR of a DxD-block CSR: scalar row Di+a lists, block by block in
+// the block row's order, the D entries (Dj+0..D-1) of each block (i,j)
+template <typename T, int D>
 __global__ void k_bcsr_expand(int64_t n, const int32_t* __restrict__ brp,
                               const int32_t* __restrict__ bcol, const T* __restrict__ bval,
                               int32_t* __restrict__ rp, int32_t* __restrict__ col,
                               T* __restrict__ val)
 {
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < 3 * n;
+    constexpr int DD = D * D;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < D * n;
          r += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i  = r / 3;
-        const int     a  = (int)(r - 3 * i);
+        const int64_t i  = r / D;
+        const int     a  = (int)(r - D * i);
         const int32_t b0 = brp[i], nb = brp[i + 1] - b0;
-        const int64_t o  = 9 * (int64_t)b0 + 3 * (int64_t)a * nb;
+        const int64_t o  = DD * (int64_t)b0 + D * (int64_t)a * nb;
         rp[r]            = (int32_t)o;
-        if (r == 3 * n - 1) rp[3 * n] = 9 * brp[n];
+        if (r == D * n - 1) rp[D * n] = DD * brp[n];
         for (int32_t t = 0; t < nb; ++t) {
             const int32_t j = bcol[b0 + t];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                col[o + 3 * t + c] = 3 * j + c;
-                val[o + 3 * t + c] = bval[9 * (int64_t)(b0 + t) + 3 * a + c];
+            for (int c = 0; c < D; ++c) {
+                col[o + D * t + c] = D * j + c;
+                val[o + D * t + c] = bval[DD * (int64_t)(b0 + t) + D * a + c];
             }
         }
     }
@@ -931,29 +932,30 @@ __global__ void k_bcsr_expand(int64_t n, const int32_t* __restrict__ brp,
 // row gets the identity as its diagonal block and zero off-diagonal blocks,
 // every block (i, j) with j constrained is zeroed (the symmetric entries),
 // and the constrained rows of the gradient are zeroed.
-template <typename T>
+template <typename T, int D>
 __global__ void k_bcsr_apply_bc(int64_t n, const int32_t* __restrict__ brp,
                                 const int32_t* __restrict__ bcol, T* __restrict__ bval,
                                 const int8_t* __restrict__ bc, T* __restrict__ grad)
 {
+    constexpr int DD = D * D;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const bool ci = bc[i] != 0;
         for (int32_t t = brp[i]; t < brp[i + 1]; ++t) {
             const int32_t j = bcol[t];
-            T*            b = bval + 9 * (int64_t)t;
+            T*            b = bval + DD * (int64_t)t;
             if (j == i) {
                 if (ci)
 #pragma unroll
-                    for (int e = 0; e < 9; ++e) b[e] = (e % 4 == 0) ? T(1) : T(0);
+                    for (int e = 0; e < DD; ++e) b[e] = (e % (D + 1) == 0) ? T(1) : T(0);
             } else if (ci || bc[j] != 0) {
 #pragma unroll
-                for (int e = 0; e < 9; ++e) b[e] = T(0);
+                for (int e = 0; e < DD; ++e) b[e] = T(0);
             }
         }
         if (ci && grad)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) grad[3 * i + c] = T(0);
+            for (int c = 0; c < D; ++c) grad[D * i + c] = T(0);
     }
 }
 
@@ -1009,8 +1011,9 @@ rxg_status rxg_arap_eval_ex(const rxg_mesh* h, int32_t dtype, const void* x, con
         set_error("rxg_arap_eval: bad argument");
         return RXG_ERR_INVALID;
     }
-    if (hess && (!hess->row_ptr || !hess->col || !hess->val || hess->dtype != dtype)) {
-        set_error("rxg_arap_eval: hess needs row_ptr, col, val of the same dtype");
+    if (hess && (!hess->row_ptr || !hess->col || !hess->val || hess->dtype != dtype ||
+                 (hess->block_dim != 0 && hess->block_dim != 3))) {
+        set_error("rxg_arap_eval: hess needs row_ptr, col, val of the same dtype and 3x3 blocks");
         return RXG_ERR_INVALID;
     }
     if (!is_device_ptr(x) || !is_device_ptr(rest) || (grad && !is_device_ptr(grad)) ||
@@ -1303,18 +1306,32 @@ rxg_status rxg_bcsr_to_csr(const rxg_bcsr* H, rxg_csr* out, void* stream)
         set_error("rxg_bcsr_to_csr: %lld blocks exceed 32-bit scalar indices", (long long)H->nnzb);
         return RXG_ERR_INVALID;
     }
+    const int D = H->block_dim == 2 ? 2 : 3;
+    if (H->block_dim != 0 && H->block_dim != 2 && H->block_dim != 3) {
+        set_error("rxg_bcsr_to_csr: block_dim must be 2 or 3");
+        return RXG_ERR_INVALID;
+    }
     cudaStream_t s = (cudaStream_t)stream;
-    out->n         = 3 * H->n;
-    out->nnz       = 9 * H->nnzb;
+    out->n         = D * H->n;
+    out->nnz       = (int64_t)D * D * H->nnzb;
     out->dtype     = H->dtype;
     if (H->n == 0) return RXG_OK;
-    const int g = grid_for_items(3 * H->n);
-    if (H->dtype == RXG_F64)
-        k_bcsr_expand<double><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const double*)H->val,
-                                                out->row_ptr, out->col, (double*)out->val);
-    else
-        k_bcsr_expand<float><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const float*)H->val,
-                                               out->row_ptr, out->col, (float*)out->val);
+    const int g = grid_for_items(D * H->n);
+    if (H->dtype == RXG_F64) {
+        if (D == 2)
+            k_bcsr_expand<double, 2><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const double*)H->val,
+                                                       out->row_ptr, out->col, (double*)out->val);
+        else
+            k_bcsr_expand<double, 3><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const double*)H->val,
+                                                       out->row_ptr, out->col, (double*)out->val);
+    } else {
+        if (D == 2)
+            k_bcsr_expand<float, 2><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const float*)H->val,
+                                                      out->row_ptr, out->col, (float*)out->val);
+        else
+            k_bcsr_expand<float, 3><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const float*)H->val,
+                                                      out->row_ptr, out->col, (float*)out->val);
+    }
     RXG_CUDA_TRY(cudaGetLastError());
     return RXG_OK;
 }
@@ -1326,15 +1343,28 @@ rxg_status rxg_bcsr_apply_bc(rxg_bcsr* H, const int8_t* bc, void* grad, void* st
         set_error("rxg_bcsr_apply_bc: bad argument");
         return RXG_ERR_INVALID;
     }
+    if (H->block_dim != 0 && H->block_dim != 2 && H->block_dim != 3) {
+        set_error("rxg_bcsr_apply_bc: block_dim must be 2 or 3");
+        return RXG_ERR_INVALID;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     if (H->n == 0) return RXG_OK;
     const int g = grid_for_items(H->n);
-    if (H->dtype == RXG_F64)
-        k_bcsr_apply_bc<double><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (double*)H->val, bc,
-                                                  (double*)grad);
-    else
-        k_bcsr_apply_bc<float><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (float*)H->val, bc,
-                                                 (float*)grad);
+    if (H->dtype == RXG_F64) {
+        if (H->block_dim == 2)
+            k_bcsr_apply_bc<double, 2><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (double*)H->val, bc,
+                                                         (double*)grad);
+        else
+            k_bcsr_apply_bc<double, 3><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (double*)H->val, bc,
+                                                         (double*)grad);
+    } else {
+        if (H->block_dim == 2)
+            k_bcsr_apply_bc<float, 2><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (float*)H->val, bc,
+                                                        (float*)grad);
+        else
+            k_bcsr_apply_bc<float, 3><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (float*)H->val, bc,
+                                                        (float*)grad);
+    }
     RXG_CUDA_TRY(cudaGetLastError());
     return RXG_OK;
 }

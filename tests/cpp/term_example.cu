@@ -1,0 +1,173 @@
+// Energies written by the application (include/rxg/diff.cuh), the way an
+// RXMesh application writes DiffScalarProblem::add_term<Op::FV>(lambda):
+//   1. Param's symmetric Dirichlet energy as a __device__ lambda over the
+//      forward-mode Scalar (D = 2), against the library's built-in term
+//      (rxg_symdir_eval): energy, gradient and 2x2-block Hessian;
+//   2. a spring energy sum_{edges (i,j) of f} k/2 |x_i - x_j|^2 (D = 3),
+//      a quadratic, so its gradient must equal H x;
+//   3. both summed in one problem (terms accumulate).
+//   term_example <out_dir>: writes the spring gradient, positions and the
+//   numbering for the test, prints "OK" and exits 0, or the failing check.
+#include <cmath>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "rxg/diff.cuh"
+#include "rxg/rxmesh.hpp"
+
+using namespace rxg;
+
+#define REQUIRE(c)                                               \
+    do {                                                         \
+        if (!(c)) {                                              \
+            std::printf("FAILED: %s (line %d)\n", #c, __LINE__); \
+            return 1;                                            \
+        }                                                        \
+    } while (0)
+
+template <typename T>
+static void dump(const std::string& path, const std::vector<T>& v)
+{
+    std::FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) throw Error(RXG_ERR_INVALID, "cannot write " + path);
+    std::fwrite(v.data(), sizeof(T), v.size(), f);
+    std::fclose(f);
+}
+
+static double max_abs_diff(const std::vector<double>& a, const std::vector<double>& b, double* scale)
+{
+    double d = 0, s = 0;
+    for (size_t i = 0; i < a.size(); ++i) {
+        d = std::max(d, std::fabs(a[i] - b[i]));
+        s = std::max(s, std::fabs(b[i]));
+    }
+    *scale = s;
+    return d;
+}
+
+int main(int argc, char** argv)
+{
+    if (argc < 2) {
+        std::printf("usage: term_example <out_dir>\n");
+        return 2;
+    }
+    try {
+        const std::string dir = argv[1];
+        // a 14 x 14 grid bent out of its plane (rest), uv = the flat grid
+        const int                          n = 14;
+        std::vector<std::vector<uint32_t>> fv;
+        std::vector<std::vector<double>>   rest, uv;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                const double u = j / double(n - 1), v = i / double(n - 1);
+                rest.push_back({u, v, 0.25 * std::sin(2.0 * u) * std::cos(1.5 * v)});
+                uv.push_back({1.2 * u + 0.01 * std::sin(37.0 * i + j), 0.9 * v + 0.01 * std::cos(11.0 * j + i)});
+            }
+        for (int i = 0; i + 1 < n; ++i)
+            for (int j = 0; j + 1 < n; ++j) {
+                const uint32_t a = i * n + j, b = a + 1, c = a + n + 1, d = a + n;
+                fv.push_back({a, b, c});
+                fv.push_back({a, c, d});
+            }
+        RXMeshStatic   rx(fv, "", 64);
+        const uint32_t nv = rx.get_num_vertices(), nf = rx.get_num_faces();
+        const std::vector<int32_t> l2i = rx.linear_to_input(RXG_ELEM_VERTEX);
+        std::vector<double>        hr(3 * nv), hu(2 * nv);
+        for (uint32_t l = 0; l < nv; ++l) {
+            for (int c = 0; c < 3; ++c) hr[3 * l + c] = rest[l2i[l]][c];
+            for (int c = 0; c < 2; ++c) hu[2 * l + c] = uv[l2i[l]][c];
+        }
+        DenseMatrix<double> R(nv, 3), U(nv, 2);
+        R.from_host(hr);
+        U.from_host(hu);
+        DeviceArray<double> minv(4 * (size_t)nf);
+        check(rxg_arap_rest(rx.handle(), R.data(), RXG_F64, minv.data(), nullptr));
+
+        // 1. symmetric Dirichlet as the application's own lambda
+        DiffScalarProblem<double, 2> sd(rx);
+        const double*                mi = minv.data();
+        sd.add_term<Op::FV, false>([mi] __device__(int32_t f, const Scalar<double, 6, true>* v) {
+            using S          = Scalar<double, 6, true>;
+            const Vec2<S> a{v[0], v[1]}, b{v[2], v[3]}, c{v[4], v[5]};
+            const Mat2<S> M = col_mat(b - a, c - a);
+            if (det(M).val <= 0.0) return S(DBL_MAX);
+            const Mat2<double> r{mi[4 * f], mi[4 * f + 1], mi[4 * f + 2], mi[4 * f + 3]};
+            const double       A = 0.5 / (r.a * r.d - r.b * r.c);
+            const Mat2<S>      J = mul(M, r);
+            return (squared_norm(J) + squared_norm(inverse(J))) * A;
+        });
+        sd.eval_terms(U);
+        // the built-in term on the same input
+        DenseMatrix<double>       g_ref(nv, 2);
+        BlockSparseMatrix<double> H_ref(sd.hess->rows(), sd.hess->non_zero_blocks(), 2);
+        rxg_bcsr                  hb = H_ref.bcsr();
+        double                    e_ref = 0;
+        check(rxg_symdir_eval(rx.handle(), RXG_F64, U.data(), minv.data(), 0, &e_ref, nullptr,
+                              g_ref.data(), &hb, nullptr));
+        REQUIRE(std::fabs(sd.get_current_loss() - e_ref) <= 1e-12 * e_ref);
+        double sc = 0;
+        REQUIRE(max_abs_diff(sd.grad.to_host(), g_ref.to_host(), &sc) <= 1e-12 * sc);
+        REQUIRE(max_abs_diff(sd.hess->values().to_host(), H_ref.values().to_host(), &sc) <= 1e-12 * sc);
+        // projected variant through the template flag: positive diagonal blocks
+        DiffScalarProblem<double, 2> sdp(rx);
+        sdp.add_term<Op::FV, true>([mi] __device__(int32_t f, const Scalar<double, 6, true>* v) {
+            using S          = Scalar<double, 6, true>;
+            const Vec2<S> a{v[0], v[1]}, b{v[2], v[3]}, c{v[4], v[5]};
+            const Mat2<double> r{mi[4 * f], mi[4 * f + 1], mi[4 * f + 2], mi[4 * f + 3]};
+            const Mat2<S>      J = mul(col_mat(b - a, c - a), r);
+            return (squared_norm(J) + squared_norm(inverse(J))) * (0.5 / (r.a * r.d - r.b * r.c));
+        });
+        sdp.eval_terms(U);
+        REQUIRE(std::fabs(sdp.get_current_loss() - e_ref) <= 1e-12 * e_ref);
+
+        // 2. spring energy on the 3-D rest positions (quadratic: grad = H x)
+        const double                 k = 2.5;
+        DiffScalarProblem<double, 3> sp(rx);
+        sp.add_term<Op::FV>([k] __device__(int32_t, const Scalar<double, 9, true>* v) {
+            Scalar<double, 9, true> e(0.0);
+            for (int i = 0; i < 3; ++i) {
+                const int j = (i + 1) % 3;
+                for (int c = 0; c < 3; ++c) e += sqr(v[3 * i + c] - v[3 * j + c]) * (0.5 * k);
+            }
+            return e;
+        });
+        sp.eval_terms(R);
+        const std::vector<double> g  = sp.grad.to_host();
+        const std::vector<double> hv = sp.hess->values().to_host();
+        const std::vector<int32_t> rp = sp.hess->row_ptr().to_host(), col = sp.hess->col_idx().to_host();
+        std::vector<double>        Hx(3 * nv, 0.0);
+        for (uint32_t i = 0; i < nv; ++i)
+            for (int32_t t = rp[i]; t < rp[i + 1]; ++t)
+                for (int a = 0; a < 3; ++a)
+                    for (int c = 0; c < 3; ++c) Hx[3 * i + a] += hv[9 * t + 3 * a + c] * hr[3 * col[t] + c];
+        REQUIRE(max_abs_diff(Hx, g, &sc) <= 1e-12 * sc);
+        dump(dir + "/spring_grad.bin", g);
+        dump(dir + "/rest.bin", hr);
+        dump(dir + "/l2i.bin", l2i);
+        std::vector<int32_t> fl;
+        for (const auto& f : fv)
+            for (uint32_t v : f) fl.push_back((int32_t)v);
+        dump(dir + "/fv.bin", fl);
+
+        // 3. two terms in one problem add up
+        DiffScalarProblem<double, 3> both(rx);
+        for (int t = 0; t < 2; ++t)
+            both.add_term<Op::FV>([k] __device__(int32_t, const Scalar<double, 9, true>* v) {
+                Scalar<double, 9, true> e(0.0);
+                for (int i = 0; i < 3; ++i)
+                    for (int c = 0; c < 3; ++c) e += sqr(v[3 * i + c] - v[3 * ((i + 1) % 3) + c]) * (0.5 * k);
+                return e;
+            });
+        both.eval_terms(R);
+        REQUIRE(std::fabs(both.get_current_loss() - 2.0 * sp.get_current_loss()) <= 1e-12 * sp.get_current_loss());
+        std::vector<double> g2 = both.grad.to_host();
+        for (double& x : g2) x *= 0.5;
+        REQUIRE(max_abs_diff(g2, g, &sc) <= 1e-12 * sc);
+    } catch (const std::exception& e) {
+        std::printf("FAILED: %s\n", e.what());
+        return 1;
+    }
+    std::printf("OK\n");
+    return 0;
+}

@@ -184,7 +184,11 @@ def cloth512(jitter=0.0, seed=0):
     return x0, x.astype(np.float32).astype(np.float64), f
 
 
-@pytest.mark.parametrize("dtype,rtol", [(torch.float64, 1e-11), (torch.float32, 2e-4)])
+# FP32: 5e-4 of the largest entry.  The cloth's coordinates reach 511 with
+# unit edges, and the displaced corners' faces are strongly deformed; FP32
+# arithmetic there leaves ~3e-4 of the largest gradient entry (1e-4 or less
+# on the small cloths of test_gpu_arap.py).
+@pytest.mark.parametrize("dtype,rtol", [(torch.float64, 1e-11), (torch.float32, 5e-4)])
 def test_cloth512_arap_matches_oracle(oracle, dtype, rtol):
     from test_gpu_arap import oracle_ref
     from rxmesh_gb300 import DiffScalarProblem, RXMeshStatic
@@ -244,18 +248,31 @@ def test_cloth512_adjoint_20_steps_fd():
     rest = rx.to_linear(torch.tensor(x0r, device="cuda"))
     prob = DiffScalarProblem(rx, torch.float64, assemble_hessian=False).add_arap_term(rest)
     xl = rx.to_linear(torch.tensor(x, device="cuda"))
+    # Every solve runs a fixed 80 Jacobi-PCG iterations (far past convergence
+    # at dt = 1e-3; a tolerance of 1e-30 is never met), so the flow is the same
+    # smooth map for every perturbed start: with a tolerance, the two runs of
+    # a central difference could stop at different iteration counts and
+    # differ by the solver's residual.
+    tol, iters = 1e-30, 80
 
-    def loss(x0):
-        return arap_energy(mcf_flow(x0, rx, 1e-3, 20, 5, tol=1e-13), prob)
+    def flow(x0):
+        return mcf_flow(x0, rx, 1e-3, 20, 5, tol=tol, max_iter=iters)
 
     x0 = xl.clone().requires_grad_(True)
-    (g,) = torch.autograd.grad(loss(x0), x0)
+    (g,) = torch.autograd.grad(arap_energy(flow(x0), prob), x0)
+
+    def face_energies(x0):
+        with torch.no_grad():
+            prob.eval_terms(flow(x0), with_hessian=False)
+        return prob.face_energy.clone()
+
     rng = np.random.default_rng(4)
     h = 1e-6
     for _ in range(16):
         d = torch.tensor(rng.normal(size=x.shape), device="cuda")
-        with torch.no_grad():
-            fd = (loss(xl + h * d) - loss(xl - h * d)).item() / (2 * h)
+        # per-face differences first: the total (~5e3) summed over 522k faces
+        # would lose the directional derivative's digits
+        fd = (face_energies(xl + h * d) - face_energies(xl - h * d)).sum().item() / (2 * h)
         an = (g * d).sum().item()
         assert abs(fd - an) <= 1e-5 * max(abs(an), 1e-6), (fd, an)
 

@@ -1,0 +1,176 @@
+"""Generic per-face energy terms: Param's symmetric Dirichlet energy
+(apps/Param/param.cu:146-183) evaluated through the forward-mode Scalar of
+include/rxg/diff.cuh and assembled by rxg_face_term_gather, against the
+oracle's energy, torch float64 autograd (gradient and full Hessian) and
+central differences; a Newton solve on it with 2x2-block Hessians."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+import torch
+
+from rxmesh_gb300 import meshgen
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def bent_grid(n=12, seed=0):
+    """n x n grid bent out of its plane (rest shape) and uv = the flat grid
+    plus a small jitter (no flipped triangle)."""
+    x, f = meshgen.plane(n, n, 1.0 / (n - 1))
+    rng = np.random.default_rng(seed)
+    rest = x.copy()
+    rest[:, 2] = 0.25 * np.sin(2.0 * rest[:, 0]) * np.cos(1.5 * rest[:, 1])
+    uv = x[:, :2] + 0.01 / n * rng.normal(size=(len(x), 2))
+    return rest, uv, np.asarray(f, np.int32)
+
+
+def torch_energy(fv, minv, uv):
+    """The same energy as a torch float64 function of uv (nv, 2)."""
+    f = torch.tensor(np.asarray(fv, np.int64))
+    mi = torch.tensor(np.asarray(minv, np.float64).reshape(-1, 2, 2))
+    a, b, c = uv[f[:, 0]], uv[f[:, 1]], uv[f[:, 2]]
+    M = torch.stack([b - a, c - a], dim=2)
+    A = 0.5 / torch.linalg.det(mi)
+    J = M @ mi
+    return (A * ((J ** 2).sum((1, 2)) + (torch.linalg.inv(J) ** 2).sum((1, 2)))).sum()
+
+
+def setup(dtype, n=12, proj=False):
+    from rxmesh_gb300 import DiffScalarProblem, RXMeshStatic
+    rest, uv, f = bent_grid(n)
+    rx = RXMeshStatic(f, len(rest), patch_size=64)
+    prob = DiffScalarProblem(rx, dtype, dim=2)
+    prob.add_symmetric_dirichlet_term(rx.to_linear(torch.tensor(rest, device="cuda")), project_hessian=proj)
+    uvl = rx.to_linear(torch.tensor(uv, device="cuda")).to(dtype)
+    return rx, prob, rest, uv, f, uvl
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype,rtol", [(torch.float64, 1e-11), (torch.float32, 2e-4)])
+def test_symmetric_dirichlet_matches_oracle_and_autograd(oracle, dtype, rtol):
+    rx, prob, rest, uv, f, uvl = setup(dtype)
+    prob.eval_terms(uvl)
+    minv, _ = oracle.rest_frame(f, rest)
+    fe = oracle.symmetric_dirichlet(f, uv.astype(np.float32).astype(np.float64)
+                                    if dtype == torch.float32 else uv, minv)
+    fl = rx.linear_to_input("f")
+    assert np.abs(prob.face_energy.double().cpu().numpy() - fe[fl]).max() <= rtol * fe.max()
+    assert abs(prob.get_current_loss() - fe.sum()) <= rtol * fe.sum()
+    # gradient and Hessian against torch float64 autograd of the whole energy
+    u = torch.tensor(uv if dtype == torch.float64 else uv.astype(np.float32).astype(np.float64),
+                     requires_grad=True)
+    g_ref = torch.autograd.grad(torch_energy(f, minv, u), u)[0].numpy()
+    gg = rx.to_input(prob.grad).double().cpu().numpy()
+    assert np.abs(gg - g_ref).max() <= rtol * np.abs(g_ref).max()
+    H_ref = torch.autograd.functional.hessian(lambda z: torch_energy(f, minv, z.reshape(-1, 2)),
+                                              u.detach().reshape(-1)).numpy()
+    H = prob.hess.to_scipy().toarray()
+    vl = rx.linear_to_input("v")
+    perm = np.empty(2 * len(vl), np.int64)  # linear (v, c) -> input (vl[v], c)
+    perm[0::2], perm[1::2] = 2 * vl, 2 * vl + 1
+    Hin = np.zeros_like(H)
+    Hin[np.ix_(perm, perm)] = H
+    assert np.abs(Hin - H_ref).max() <= rtol * np.abs(H_ref).max()
+
+
+@pytest.mark.gpu
+def test_symmetric_dirichlet_central_differences():
+    rx, prob, rest, uv, f, uvl = setup(torch.float64)
+    prob.eval_terms(uvl)
+    g = prob.grad.clone()
+    rng = np.random.default_rng(1)
+    h = 1e-6
+    for _ in range(16):
+        d = torch.tensor(rng.normal(size=uvl.shape), device="cuda")
+        fd = (prob.eval_terms_passive(uvl + h * d).item() - prob.eval_terms_passive(uvl - h * d).item()) / (2 * h)
+        an = (g * d).sum().item()
+        assert abs(fd - an) <= 1e-6 * max(abs(an), 1.0), (fd, an)
+
+
+@pytest.mark.gpu
+def test_flipped_face_gets_the_largest_value_and_no_derivative(oracle):
+    rx, prob, rest, uv, f, uvl = setup(torch.float64)
+    uv2 = uv.copy()
+    t = f[7]
+    uv2[t[0]], uv2[t[1]] = uv[t[1]].copy(), uv[t[0]].copy()  # swap two corners: flipped
+    prob.eval_terms(rx.to_linear(torch.tensor(uv2, device="cuda")))
+    fl = rx.linear_to_input("f")
+    fe = prob.face_energy.cpu().numpy()[np.argsort(fl)]
+    assert fe[7] == np.finfo(np.float64).max
+
+
+@pytest.mark.gpu
+def test_projected_hessian_is_positive_semidefinite():
+    rx, prob, rest, uv, f, uvl = setup(torch.float64, proj=True)
+    # a stretched state, where the unprojected Hessian is indefinite
+    prob.eval_terms(uvl * torch.tensor([1.6, 0.5], dtype=torch.float64, device="cuda"))
+    H = prob.hess.to_scipy().toarray()
+    assert np.linalg.eigvalsh(0.5 * (H + H.T)).min() >= -1e-9 * np.abs(H).max()
+
+
+@pytest.mark.gpu
+def test_newton_on_symmetric_dirichlet_decreases_energy():
+    """Param's Newton loop (diff/newton_solver.h) on the 2x2-block Hessian:
+    projected Hessian, PCG on its scalar form, Armijo line search."""
+    from rxmesh_gb300 import NewtonSolver
+    rx, prob, rest, uv, f, uvl = setup(torch.float64, n=16, proj=True)
+    x = uvl * torch.tensor([1.3, 0.8], dtype=torch.float64, device="cuda")
+    prob.eval_terms(x)
+    e = [prob.get_current_loss()]
+    newton = NewtonSolver(prob, "pcg", max_iter=2000, abs_tol=0.0, rel_tol=1e-12)
+    for _ in range(6):
+        prob.eval_terms()
+        newton.compute_direction()
+        assert newton.line_search()
+        prob.eval_terms()
+        e.append(prob.get_current_loss())
+    assert all(b <= a + 1e-12 for a, b in zip(e, e[1:])), e
+    assert e[-1] < 0.9 * e[0], e
+
+
+@pytest.fixture(scope="module")
+def term_example(tmp_path_factory):
+    """tests/cpp/term_example.cu: energies written by the application with
+    include/rxg/diff.cuh, built with nvcc against librxg.so."""
+    from rxmesh_gb300 import _lib
+    _lib.load()
+    libdir = os.path.dirname(_lib.lib_path())
+    exe = str(tmp_path_factory.mktemp("terms") / "term_example")
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    cmd = [nvcc, "-std=c++17", "--extended-lambda", "-O2", "-gencode", "arch=compute_103a,code=sm_103a",
+           os.path.join(ROOT, "tests", "cpp", "term_example.cu"), "-I", os.path.join(ROOT, "include"),
+           "-L", libdir, "-lrxg", "-Xlinker", "-rpath," + libdir, "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_term_example_compiles(term_example):
+    assert os.path.exists(term_example)
+
+
+@pytest.mark.gpu
+def test_application_written_terms(term_example, tmp_path):
+    """The application's symmetric Dirichlet lambda equals the built-in term
+    (checked inside the program), and its spring energy's gradient equals
+    the analytic one: sum over the faces' edges of k (x_i - x_j)."""
+    r = subprocess.run([term_example, str(tmp_path)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout.strip().endswith("OK"), r.stdout + r.stderr
+    ld = lambda n, t: np.fromfile(str(tmp_path / (n + ".bin")), dtype=t)
+    g = ld("spring_grad", np.float64).reshape(-1, 3)
+    x = ld("rest", np.float64).reshape(-1, 3)  # linear order
+    l2i = ld("l2i", np.int32)
+    f = ld("fv", np.int32).reshape(-1, 3)      # input ids
+    il = np.empty_like(l2i)
+    il[l2i] = np.arange(len(l2i))
+    fl = il[f]
+    want = np.zeros_like(x)
+    for i in range(3):
+        a, b = fl[:, i], fl[:, (i + 1) % 3]
+        d = 2.5 * (x[a] - x[b])
+        np.add.at(want, a, d)
+        np.add.at(want, b, -d)
+    assert np.abs(g - want).max() <= 1e-12 * np.abs(want).max()
