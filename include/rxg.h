@@ -549,6 +549,19 @@ rxg_status rxg_symdir_eval(const rxg_mesh* m, int32_t dtype, const void* uv, con
                            void* stream);
 
 /*
+ * Inertia term of a mass-spring system (add_inertia_term of
+ * tests/RXMesh_test/test_hess.cu:13-29, a per-vertex Op::V term): E =
+ * sum_v mass/2 |x_v - x_target_v|^2; gradient mass (x - x_target); Hessian
+ * mass I on every diagonal block.  x, x_target: nv*dim of dtype (dim 2 or
+ * 3), linear order, device.  Without RXG_TERM_ACCUMULATE grad and the whole
+ * Hessian are overwritten; with it, added to.  energy: host or device
+ * double, may be NULL.
+ */
+rxg_status rxg_inertia_eval(const rxg_mesh* m, int32_t dtype, int32_t dim, const void* x,
+                            const void* x_target, double mass, int32_t flags, double* energy,
+                            void* grad, rxg_bcsr* hess, void* stream);
+
+/*
  * Scalar CSR (3n x 3n) of a 3x3-block CSR, the form the reference's
  * CG/PCG solvers work on for a Hessian (HessianSparseMatrix,
  * diff/hessian_sparse_matrix.h:16-137): scalar row 3i+a lists, block by

@@ -1228,6 +1228,17 @@ class DiffScalarProblem
         });
     }
 #endif
+    // inertia of a mass-spring system, mass/2 |x - x_target|^2 per vertex
+    // (add_inertia_term, tests/RXMesh_test/test_hess.cu:13-29); x_target in
+    // linear order, copied
+    void add_inertia_term(const DenseMatrix<T>& x_target, T mass, cudaStream_t s = nullptr)
+    {
+        m_xt.resize((size_t)x_target.size());
+        check_cuda(cudaMemcpyAsync(m_xt.data(), x_target.data(), sizeof(T) * (size_t)x_target.size(),
+                                   cudaMemcpyDeviceToDevice, s),
+                   "cudaMemcpyAsync");
+        m_mass = mass;
+    }
     // evaluate at linear-order positions x (eval_terms, diff_scalar_problem.h:310-321)
     void eval_terms(const DenseMatrix<T>& x, cudaStream_t s = nullptr)
     {
@@ -1269,7 +1280,8 @@ class DiffScalarProblem
     // the ARAP term (if added) first, then the added terms, accumulated
     void run(const DenseMatrix<T>& x, bool derivatives, cudaStream_t s)
     {
-        if (!m_rest.size() && m_terms.empty()) throw Error(RXG_ERR_INVALID, "add a term first");
+        if (!m_rest.size() && m_terms.empty() && !m_xt.size())
+            throw Error(RXG_ERR_INVALID, "add a term first");
         rxg_bcsr b    = hess ? hess->bcsr() : rxg_bcsr{};
         rxg_bcsr* hb  = (derivatives && hess) ? &b : nullptr;
         T*        g   = derivatives ? grad.data() : nullptr;
@@ -1298,8 +1310,16 @@ class DiffScalarProblem
                 first = false;
             }
         }
+        if (m_xt.size()) {
+            double e = 0.0;
+            check(rxg_inertia_eval(m_rx->handle(), dtype_of<T>::value, VariableDim, x.data(), m_xt.data(),
+                                   (double)m_mass, first ? 0 : RXG_TERM_ACCUMULATE, &e, g, hb, s));
+            sum += e;
+        }
         m_loss = sum;
     }
+    DeviceArray<T>                                               m_xt;
+    T                                                            m_mass = T(0);
     std::vector<std::function<void(const T*, T*, cudaStream_t)>> m_terms;
     DeviceArray<int32_t>                                         m_fv;
     DeviceArray<T>                                               m_rec;

@@ -102,7 +102,7 @@ class DiffScalarProblem:
         self.face_energy = torch.zeros(rx.get_num_faces(), dtype=dtype, device=dev)
         self.hess = (BlockSparseMatrix(n.value, nnz.value, dtype, dev, self.dim)
                      if assemble_hessian else None)
-        self.terms = []  # (kind, rest frames Mr^-1 (nf, 4), project)
+        self.terms = []  # (kind, rest frames Mr^-1 (nf, 4) or target positions, project or mass)
         self.rest = None
         self.project_hessian = False
         self.opt_var = None
@@ -140,6 +140,14 @@ class DiffScalarProblem:
         self.terms.append(("symdir", rest, bool(project_hessian)))
         return self
 
+    def add_inertia_term(self, x_target_lin, mass):
+        """Inertia of a mass-spring system (add_inertia_term,
+        tests/RXMesh_test/test_hess.cu:13-29): per vertex mass/2 |x - x_target|^2,
+        Hessian mass I.  x_target_lin (nv, dim), linear order."""
+        xt = x_target_lin.to(self.dtype).contiguous().clone()
+        self.terms.append(("inertia", xt, float(mass)))
+        return self
+
     def _eval(self, x, grad, face_E, hess_b, with_projection=True, stream=None):
         """Sum of the terms at x; returns the energy (1-element FP64 tensor)."""
         if not self.terms:
@@ -154,6 +162,14 @@ class DiffScalarProblem:
                 fe = self._tmp_face
             hb = ctypes.byref(hess_b) if hess_b is not None else None
             pj = proj and with_projection
+            if kind == "inertia":
+                check(self._L.rxg_inertia_eval(self.rx._h, _DT[self.dtype], self.dim, _p(x), _p(rest),
+                                               ctypes.c_double(proj), RXG_TERM_ACCUMULATE if i > 0 else 0,
+                                               _p(e), _p(grad), hb, _stream(stream)))
+                if face_E is not None and i == 0:
+                    face_E.zero_()
+                total += e
+                continue
             if kind == "arap":
                 check(self._L.rxg_arap_eval_ex(self.rx._h, _DT[self.dtype], _p(x), _p(rest),
                                                1 if pj else 0, _p(e), _p(fe), _p(grad), hb,

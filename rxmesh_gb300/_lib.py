@@ -113,6 +113,7 @@ SIGNATURES = {
     "rxg_mcf_step_matfree": [P, D, I32, I32, D, I32, P, P, P],
     "rxg_face_term_gather": [P, I32, I32, P, I32, P, P, P, P, P],
     "rxg_symdir_eval": [P, I32, P, P, I32, P, P, P, P, P],
+    "rxg_inertia_eval": [P, I32, I32, P, P, D, I32, P, P, P, P],
 }
 _RESTYPE = {"rxg_status_string": ctypes.c_char_p, "rxg_last_error": ctypes.c_char_p,
             "rxg_mesh_destroy": None, "rxg_batch_destroy": None}

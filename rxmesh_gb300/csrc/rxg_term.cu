@@ -265,11 +265,114 @@ static void launch_gather(bool acc, int G, int64_t nv, const Lazy* z, const int3
                                                      z->bnd, fv, rec, grad, hval);
 }
 
+// Inertia term of a mass-spring system (the reference's add_inertia_term,
+// tests/RXMesh_test/test_hess.cu:13-29, an Op::V term): per vertex
+// E_v = m/2 |x_v - xt_v|^2, gradient m (x_v - xt_v), Hessian m I on the
+// diagonal block.  Without ACC the whole Hessian row is written (m I and
+// zero off-diagonal blocks); with ACC only the diagonal block is added to.
+template <typename T, int D, bool ACC>
+__global__ void __launch_bounds__(128) k_inertia(int64_t nv, const int32_t* __restrict__ row_ptr,
+                                                 const T* __restrict__ x, const T* __restrict__ xt, T m,
+                                                 T* __restrict__ grad, T* __restrict__ hval,
+                                                 double* __restrict__ part)
+{
+    constexpr int DD = D * D;
+    __shared__ double s_red[128 / 32];
+    double            esum = 0;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv;
+         v += (int64_t)gridDim.x * blockDim.x) {
+        T e = T(0);
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            const T d = x[D * v + c] - xt[D * v + c];
+            e += d * d;
+            if (grad) grad[D * v + c] = ACC ? grad[D * v + c] + m * d : m * d;
+        }
+        esum += 0.5 * (double)m * (double)e;
+        if (hval) {
+            const int32_t r0 = row_ptr[v], r1 = row_ptr[v + 1];
+            T*            dg = hval + DD * (int64_t)r0;  // the row's first block is the diagonal
+#pragma unroll
+            for (int t = 0; t < DD; ++t) {
+                const T mi = (t % (D + 1) == 0) ? m : T(0);
+                dg[t]      = ACC ? dg[t] + mi : mi;
+            }
+            if (!ACC)
+                for (int64_t t = DD * (int64_t)(r0 + 1); t < DD * (int64_t)r1; ++t) hval[t] = T(0);
+        }
+    }
+    const double t = term_block_sum<128>(esum, s_red);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
 }  // namespace rxg
 
 using namespace rxg;
 
 extern "C" {
+
+rxg_status rxg_inertia_eval(const rxg_mesh* h, int32_t dtype, int32_t dim, const void* x,
+                            const void* x_target, double mass, int32_t flags, double* energy,
+                            void* grad, rxg_bcsr* hess, void* stream)
+{
+    if (!h || !x || !x_target || (dtype != RXG_F32 && dtype != RXG_F64) || (dim != 2 && dim != 3) ||
+        (flags & ~RXG_TERM_ACCUMULATE)) {
+        set_error("rxg_inertia_eval: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    if (!is_device_ptr(x) || !is_device_ptr(x_target)) {
+        set_error("rxg_inertia_eval: x and x_target must be device arrays");
+        return RXG_ERR_INVALID;
+    }
+    cudaStream_t s   = (cudaStream_t)stream;
+    const bool   acc = (flags & RXG_TERM_ACCUMULATE) != 0;
+    if (hess && (!hess->row_ptr || !hess->col || !hess->val || hess->dtype != dtype ||
+                 (hess->block_dim == 0 ? 3 : hess->block_dim) != dim)) {
+        set_error("rxg_inertia_eval: hess needs row_ptr, col, val of the term's dtype and %dx%d blocks", dim,
+                  dim);
+        return RXG_ERR_INVALID;
+    }
+    if ((grad && !is_device_ptr(grad)) || (hess && !is_device_ptr(hess->val))) {
+        set_error("rxg_inertia_eval: grad and hess must be device arrays");
+        return RXG_ERR_INVALID;
+    }
+    Lazy*      z;
+    rxg_status st = ensure_pattern(&h->m, s, &z);
+    if (st) return st;
+    const int64_t nv = h->m.nv;
+    if (hess) {
+        hess->n    = nv;
+        hess->nnzb = z->nnz;
+        if (!acc) {
+            RXG_CUDA_TRY(cudaMemcpyAsync(hess->row_ptr, z->row_ptr, 4 * (nv + 1), cudaMemcpyDeviceToDevice, s));
+            RXG_CUDA_TRY(cudaMemcpyAsync(hess->col, z->col, 4 * z->nnz, cudaMemcpyDeviceToDevice, s));
+        }
+    }
+    const int G = std::min<int>(grid_for_items(nv) * 2, 152 * 16);
+    double*   part;
+    RXG_CUDA_TRY(scratch_alloc((void**)&part, sizeof(double) * (G + 1), s));
+    auto run = [&](auto tag, auto dtag) {
+        using T         = decltype(tag);
+        constexpr int D = decltype(dtag)::value;
+        T* hv           = hess ? (T*)hess->val : nullptr;
+        if (acc)
+            k_inertia<T, D, true><<<G, 128, 0, s>>>(nv, z->row_ptr, (const T*)x, (const T*)x_target, (T)mass,
+                                                    (T*)grad, hv, part);
+        else
+            k_inertia<T, D, false><<<G, 128, 0, s>>>(nv, z->row_ptr, (const T*)x, (const T*)x_target,
+                                                     (T)mass, (T*)grad, hv, part);
+    };
+    if (dtype == RXG_F64) {
+        if (dim == 2) run(double{}, std::integral_constant<int, 2>{});
+        else run(double{}, std::integral_constant<int, 3>{});
+    } else {
+        if (dim == 2) run(float{}, std::integral_constant<int, 2>{});
+        else run(float{}, std::integral_constant<int, 3>{});
+    }
+    st = term_energy_out(part, G, energy, s);
+    cudaFreeAsync(part, s);
+    return st;
+}
 
 rxg_status rxg_face_term_gather(const rxg_mesh* h, int32_t dtype, int32_t dim, const void* records,
                                 int32_t flags, double* energy, void* face_E, void* grad,

@@ -194,3 +194,59 @@ def test_matfree_newton_matches_assembled():
         assert a.line_search() and b.line_search()
         assert abs(prob.get_current_loss() - prob2.get_current_loss()) <= 1e-9 * abs(prob.get_current_loss())
     assert torch.allclose(xl, xl2, rtol=0, atol=1e-8)
+
+
+def test_inertia_hessian_is_mass_identity():
+    """The reference's Diff.Hess (tests/RXMesh_test/test_hess.cu:117-153):
+    the inertia term's Hessian on a 16 x 16 plane (dx = 1/15) is mass I on
+    the diagonal and zero elsewhere (the reference checks 1e-3)."""
+    from rxmesh_gb300 import DiffScalarProblem, RXMeshStatic
+    n = 16
+    x, f = meshgen.plane(n, n, 1.0 / (n - 1))
+    rx = RXMeshStatic(f, len(x), patch_size=64)
+    xl = rx.to_linear(torch.tensor(x, device="cuda")).float()
+    mass = 0.01
+    prob = DiffScalarProblem(rx, torch.float32).add_inertia_term(xl, mass)
+    prob.eval_terms(xl)
+    H = prob.hess.to_scipy().toarray()
+    assert np.abs(np.diag(H) - mass).max() <= 1e-6
+    assert np.abs(H - np.diag(np.diag(H))).max() == 0.0
+    assert abs(prob.get_current_loss()) == 0.0 and prob.grad.abs().max().item() == 0.0
+    # away from the target: E = m/2 |d|^2, gradient m d
+    d = torch.randn_like(xl)
+    prob.eval_terms(xl + d)
+    assert abs(prob.get_current_loss() - 0.5 * mass * float((d.double() ** 2).sum())) <= 1e-5 * prob.get_current_loss()
+    assert (prob.grad - mass * d).abs().max().item() <= 1e-6
+
+
+def test_newton_arap_with_inertia_converges_each_solve():
+    """ARAP plus the inertia term (mass 0.01): the Newton system is positive
+    definite, so every PCG solve converges (the ARAP term alone has the
+    near-null space of isometric bending, where PCG runs to max_iter)."""
+    from rxmesh_gb300 import DiffScalarProblem, NewtonSolver, RXMeshStatic
+    n = 32
+    x0, f = meshgen.plane(n, n, 1.0)
+    rng = np.random.default_rng(5)
+    x = x0.copy()
+    corners = [0, n - 1, n * (n - 1), n * n - 1]
+    x[corners] += rng.uniform(-0.2, 0.2, size=(4, 3))
+    rx = RXMeshStatic(f, len(x), patch_size=128)
+    rest = rx.to_linear(torch.tensor(x0, device="cuda"))
+    xl = rx.to_linear(torch.tensor(x, device="cuda"))
+    prob = (DiffScalarProblem(rx, torch.float64).add_arap_term(rest, project_hessian=True)
+            .add_inertia_term(xl, 0.01))
+    bc = torch.zeros(len(x), dtype=torch.int8, device="cuda")
+    bc[torch.tensor(rx.input_to_linear("v")[corners], device="cuda", dtype=torch.long)] = 1
+    newton = NewtonSolver(prob, "pcg", max_iter=2000, abs_tol=0.0, rel_tol=1e-12)
+    xn = xl.clone()
+    prob.eval_terms(xn)
+    e = [prob.get_current_loss()]
+    for _ in range(4):
+        prob.eval_terms()
+        newton.apply_bc(bc)
+        newton.compute_direction()
+        assert newton.solver.converged() and newton.iter_taken() < 2000
+        newton.line_search()
+        prob.eval_terms()
+        e.append(prob.get_current_loss())
+    assert all(b <= a for a, b in zip(e, e[1:])), e

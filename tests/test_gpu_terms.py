@@ -20,6 +20,7 @@ def bent_grid(n=12, seed=0):
     """n x n grid bent out of its plane (rest shape) and uv = the flat grid
     plus a small jitter (no flipped triangle)."""
     x, f = meshgen.plane(n, n, 1.0 / (n - 1))
+    f = np.asarray(f)[:, [0, 2, 1]]  # counter-clockwise in the (x, y) plane: det(M) > 0
     rng = np.random.default_rng(seed)
     rest = x.copy()
     rest[:, 2] = 0.25 * np.sin(2.0 * rest[:, 0]) * np.cos(1.5 * rest[:, 1])
