@@ -355,24 +355,38 @@ def run_sweep(args, torch, rx, xl, sizes):
     return per, total_ms / args.steps, clocks, outs, nrm, (flush_l2, launch)
 
 
-def run_sweep_back_to_back(args, torch, flush_l2, launch):
-    """The six kernels launched back to back after one L2 flush, one event
-    pair around all six: the whole sweep, including each kernel's output
-    write-back (151 MB of outputs do not fit the 129 MB L2) and the gaps
-    between launches.  The launches are captured once into a CUDA graph
-    when the capture succeeds (else launched directly; the line says which).
+def run_sweep_back_to_back(args, torch, flush_l2, launch, concurrent=False):
+    """The six kernels of the sweep after one L2 flush, one event pair around
+    all six: the whole sweep, including each kernel's output write-back (151
+    MB of outputs do not fit the 129 MB L2) and the gaps between launches.
+    The launches are captured once into a CUDA graph when the capture
+    succeeds (else launched directly; the line says which).  concurrent: the
+    six queries are independent, so each is its own branch of the graph
+    (forked from the capture stream and joined at the end) and the kernels
+    overlap on the GPU; otherwise they run one after another.
     Returns (ms per sweep, mode, clocks)."""
     stream = torch.cuda.current_stream()
-    mode = "graph"
+    mode = "graph, concurrent branches" if concurrent else "graph, sequential"
     g = None
     try:
         side = torch.cuda.Stream()
+        branches = [torch.cuda.Stream() for _ in OPS] if concurrent else []
         side.wait_stream(stream)
         with torch.cuda.stream(side):
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
-                for name in OPS:
-                    launch(name)
+                if concurrent:
+                    fork = torch.cuda.Event()
+                    fork.record(side)
+                    for name, br in zip(OPS, branches):
+                        br.wait_event(fork)
+                        with torch.cuda.stream(br):
+                            launch(name)
+                    for br in branches:
+                        side.wait_stream(br)
+                else:
+                    for name in OPS:
+                        launch(name)
         stream.wait_stream(side)
         torch.cuda.synchronize()
     except Exception:  # capture refused: time direct launches
@@ -519,6 +533,26 @@ def run_mcf(args, torch, oracle_future=None):
         t = statistics.median(times)
         res[prec] = {"steps_per_s": nsteps / t, "ms_per_step": 1e3 * t / nsteps,
                      "cg_iters_last_step": st["iters"], "converged": bool(st["converged"])}
+    # matrix-free FP64 steps (the operator's weights recomputed in every
+    # product; rxg_mcf_step_matfree)
+    from rxmesh_gb300 import mcf_step_matfree
+    x = x0l.clone()
+    mcf_step_matfree(rx, x, dt, 1, tol=tol)
+    x1 = rx.to_input(x).cpu().numpy()
+    mcf_step_matfree(rx, x, dt, nsteps - 1, tol=tol)
+    runs["f64_matfree"] = (x1, rx.to_input(x).cpu().numpy())
+    times = []
+    for _ in range(max(1, args.steps // 4)):
+        x = x0l.clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = mcf_step_matfree(rx, x, dt, nsteps, tol=tol)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    res["f64_matfree"] = {"steps_per_s": nsteps / t, "ms_per_step": 1e3 * t / nsteps,
+                          "cg_iters_last_step": st["iters"], "converged": bool(st["converged"])}
+    res["matvec"] = run_matvec(torch, rx, x0l, dt)
     ref = oracle_future.result() if oracle_future is not None else mcf_oracle_steps()
     for prec, (x1, x10) in runs.items():
         res[prec]["rel_err_step1"] = float(np.linalg.norm(x1 - ref[1]) / np.linalg.norm(ref[1]))
@@ -546,6 +580,44 @@ def run_mcf(args, torch, oracle_future=None):
                                         "achieved_gbs": ach, "frac_of_%s_hbm" % peak_kind: ach / peak}
     res["spmv"] = run_spmv(torch, rx, x0l, dt)
     return res
+
+
+def run_matvec(torch, rx, x0l, dt):
+    """The matrix-free MCF product (rxg_mcf_matvec) on the level-8 mesh, FP64
+    and FP32, each launch after an L2 flush.  Algorithmic bytes per product:
+    the [diagonal, ring] pattern's row offsets and columns (4(n+1) + 4 nnz),
+    the positions (24 n), x and y (2 x 3 n x sizeof(T)): the weights are
+    recomputed, not read."""
+    from rxmesh_gb300 import mcf_matvec
+    peak, _ = peaks()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    clean = torch.ones(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    n = x0l.shape[0]
+    nnz = n + 2 * (3 * n - 6)
+    out = {}
+    for name, dtype, sz in (("f64", torch.float64, 8), ("f32", torch.float32, 4)):
+        X = x0l.to(dtype).contiguous()
+        Y = torch.empty_like(X)
+        algo = 4 * (n + 1) + 4 * nnz + 24 * n + 2 * 3 * n * sz
+        for _ in range(3):
+            mcf_matvec(rx, x0l, X, dt, out=Y)
+        torch.cuda.synchronize()
+        evs = []
+        for _ in range(20):
+            flush.fill_(1.0)
+            clean.sum()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            mcf_matvec(rx, x0l, X, dt, out=Y)
+            b.record()
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        ms = statistics.median([a.elapsed_time(b) for a, b in evs])
+        gbs = algo / (ms * 1e-3) / 1e9
+        out[name] = {"ms": ms, "gbs_algorithmic": gbs, "frac_of_measured_hbm": gbs / peak,
+                     "algorithmic_bytes": algo}
+    return out
 
 
 def run_spmv(torch, rx, x0l, dt):
@@ -683,6 +755,59 @@ def run_arap(args, torch):
         "cg_ms_per_iteration": newton.solve_time / 3, "cg_iters": iters,
         "energy_after_3": prob.get_current_loss(),
         "solver": "matrix-free CG (face records, no assembled Hessian), rel. tol 1e-6, max 1000"}
+    # the same Newton loop with the inertia term (mass 0.01 per vertex,
+    # add_inertia_term): the system is positive definite and every PCG
+    # solve converges
+    prob = (DiffScalarProblem(rx, torch.float32).add_arap_term(rest, project_hessian=True)
+            .add_inertia_term(xl.to(torch.float32), 0.01))
+    xn = xl.to(torch.float32).clone()
+    newton = NewtonSolver(prob, "pcg", max_iter=2000, abs_tol=0.0, rel_tol=1e-6)
+    newton_iter(newton, prob, xn.clone())  # untimed warm-up
+    newton.solve_time = 0.0
+    prob.eval_terms(xn)
+    e0 = prob.get_current_loss()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    iters, conv = [], []
+    for _ in range(3):
+        prob.eval_terms(xn)
+        prob.hess.apply_bc(bc, prob.grad)
+        newton.compute_direction()
+        newton.line_search()
+        iters.append(newton.solver.iter_taken())
+        conv.append(bool(newton.solver.converged()))
+    torch.cuda.synchronize()
+    res["newton_f32_projected_inertia"] = {
+        "ms_per_iteration": 1e3 * (time.perf_counter() - t0) / 3,
+        "pcg_ms_per_iteration": newton.solve_time / 3, "pcg_iters": iters, "pcg_converged": conv,
+        "energy_before": e0, "energy_after_3": prob.get_current_loss(),
+        "solver": "ARAP + inertia (mass 0.01), PCG on the scalar Hessian, rel. tol 1e-6"}
+    # Param's symmetric Dirichlet term on the same mesh (dim 2: uv = the flat
+    # grid, rest = the displaced cloth), energy + gradient + 2x2-block Hessian
+    # (the grid's faces wind clockwise in (x, y): mirror y so that no face is flipped)
+    uv = rx.to_linear(torch.tensor(x0[:, :2] * np.array([1.0, -1.0]), device="cuda"))
+    for name, dt_ in (("f32", torch.float32), ("f64", torch.float64)):
+        sd = DiffScalarProblem(rx, dt_, dim=2).add_symmetric_dirichlet_term(xl)
+        u = uv.to(dt_)
+        for _ in range(3):
+            sd.eval_terms(u)
+        torch.cuda.synchronize()
+        evs = []
+        for _ in range(max(3, args.steps)):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            sd.eval_terms(u)
+            b.record()
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        ms = statistics.median([a.elapsed_time(b) for a, b in evs])
+        sz = 4 if dt_ == torch.float32 else 8
+        # uv read, Mr^-1 (4 per face), face energies, gradient, 2x2 blocks + columns
+        algo = 2 * sz * V + 4 * sz * F + sz * F + 2 * sz * V + (4 * sz + 4) * nnzb
+        res["symmetric_dirichlet_" + name] = {"ms_energy_grad_hessian": ms, "algorithmic_bytes": algo,
+                                              "gbs_algorithmic": algo / (ms * 1e-3) / 1e9,
+                                              "energy": sd.get_current_loss()}
     # adjoint through 20 steps
     prob = DiffScalarProblem(rx, torch.float64, assemble_hessian=False).add_arap_term(rest)
     times = []
@@ -820,10 +945,91 @@ def summary(line, peak_kind):
     if b:
         out["batch_meshes_per_s"] = b["meshes_per_s"]
         out["batch_frac"] = b["roofline"]["frac"]
+    if m:
+        out["mcf_steps_per_s_f64_matfree"] = m["f64_matfree"]["steps_per_s"]
+        out["mcf_rel_err_f64_matfree_10_steps"] = m["f64_matfree"]["rel_err_after_10_steps"]
     a = line.get("arap")
     if a:
         out["arap_ms_f32"] = a["f32"]["ms_energy_grad_hessian"]
+        ni = a.get("newton_f32_projected_inertia")
+        if ni:
+            out["newton_inertia_ms_per_iteration"] = ni["ms_per_iteration"]
+            out["newton_inertia_pcg_iters"] = ni["pcg_iters"]
     return out
+
+
+def run_kernels(args, torch):
+    """Every hot kernel launched twice on the benchmark meshes, nothing else
+    (no oracle, no timing): the command the committed ncu launch-list
+    summaries are captured from.  Returns the workloads run."""
+    from rxmesh_gb300 import (DiffScalarProblem, Op, RXMeshStatic, mcf_init_b, mcf_matvec,
+                              mcf_solve_matfree, mcf_step, mcf_step_backward, meshgen)
+    from rxmesh_gb300._solvers import mcf_assemble
+    done = []
+    # queries and normals on the torus
+    x, f = meshgen.torus(1024, 1024, jitter=1e-3, seed=0)
+    rx = RXMeshStatic(f, len(x), patch_size=512)
+    xl = rx.to_linear(torch.tensor(x, device="cuda"))
+    for _ in range(2):
+        for op in ("VV", "VE", "VF", "FV", "EV", "EF", "FE", "FF", "EVD"):
+            rx.query(getattr(Op, op))
+        rx.vertex_normals(xl.float(), "area")
+        rx.vertex_normals(xl.float(), "max")
+    done.append("torus 1024x1024: VV VE VF FV EV EF FE FF EVD, normals (area, max)")
+    del rx, xl
+    torch.cuda.synchronize()
+    # MCF on the level-8 icosphere
+    v, f = meshgen.icosphere(8)
+    x0 = meshgen.radial_noise(v, 0.02, 0)
+    rx = RXMeshStatic(f, len(x0), patch_size=256)
+    xl = rx.to_linear(torch.tensor(x0, device="cuda"))
+    rx.query_oriented_vv()
+    for _ in range(2):
+        for dt_ in (torch.float64, torch.float32):
+            A, B = mcf_assemble(rx, xl, 1e-3, dt_)
+            X = xl.to(dt_).contiguous()
+            A.multiply(X)
+            mcf_matvec(rx, xl, X, 1e-3)
+        y = xl.clone()
+        mcf_step(rx, y, 1e-3, 1, "f64", tol=1e-6)
+        y = xl.clone()
+        mcf_step(rx, y, 1e-3, 1, "mixed", tol=1e-6)
+        Bm = mcf_init_b(rx, xl)
+        Xm = xl.clone()
+        mcf_solve_matfree(rx, xl, Bm, Xm, 1e-3, max_iter=40, rel_tol=1e-30)
+        y1 = xl.clone()
+        mcf_step(rx, y1, 1e-3, 1, "f64", tol=1e-10)
+        mcf_step_backward(rx, xl, y1, torch.ones_like(xl), 1e-3, tol=1e-10)
+    done.append("icosphere level 8: assembly, SpMM, matrix-free matvec (FP64, FP32), MCF step "
+                "(FP64, mixed), matrix-free solve (40 iterations), adjoint step")
+    del rx, xl
+    torch.cuda.synchronize()
+    # per-face terms on the 512 x 512 cloth
+    n = 512
+    x0, f = meshgen.plane(n, n, 1.0)
+    rng = np.random.default_rng(0)
+    x = x0.copy()
+    for c in [0, n - 1, n * (n - 1), n * n - 1]:
+        x[c] += rng.uniform(-0.2, 0.2, size=3)
+    rx = RXMeshStatic(f, len(x), patch_size=512)
+    rest = rx.to_linear(torch.tensor(x0, device="cuda"))
+    xl = rx.to_linear(torch.tensor(x, device="cuda"))
+    uv = rx.to_linear(torch.tensor(x0[:, :2] * np.array([1.0, -1.0]), device="cuda"))
+    for _ in range(2):
+        for dt_ in (torch.float32, torch.float64):
+            for proj in (False, True):
+                p = DiffScalarProblem(rx, dt_).add_arap_term(rest, project_hessian=proj)
+                p.eval_terms(xl.to(dt_))
+            p.hess.to_csr()
+            p.eval_matvec(torch.ones_like(p.grad))
+            sd = DiffScalarProblem(rx, dt_, dim=2).add_symmetric_dirichlet_term(xl)
+            sd.eval_terms(uv.to(dt_))
+            pi = DiffScalarProblem(rx, dt_).add_inertia_term(xl.to(dt_), 0.01)
+            pi.eval_terms(xl.to(dt_))
+    done.append("cloth 512x512: ARAP (FP32, FP64, projected), block-to-scalar CSR, Hessian-vector "
+                "product, symmetric Dirichlet (FP32, FP64), inertia")
+    torch.cuda.synchronize()
+    return done
 
 
 def main():
@@ -837,7 +1043,7 @@ def main():
     ap.add_argument("--no-arap", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-patcher", action="store_true")
-    ap.add_argument("--only", choices=["sweep", "queries", "mcf", "arap", "batch", "patcher"],
+    ap.add_argument("--only", choices=["sweep", "queries", "mcf", "arap", "batch", "patcher", "kernels"],
                     help="run one workload and print only its results (for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -852,6 +1058,10 @@ def main():
         rx = RXMeshStatic(f, len(x), patch_size=512)
         sz = (rx.get_num_vertices(), rx.get_num_edges(), rx.get_num_faces())
         print(json.dumps({"only": "queries", "queries": run_edge_face_queries(args, torch, rx, sz)}))
+        return
+    if args.only == "kernels":
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"only": "kernels", "workloads": run_kernels(args, torch)}))
         return
     if args.only and args.only != "sweep":
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
@@ -882,7 +1092,8 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     per, ms_isolated, clocks_iso, _, _, fns = run_sweep(args, torch, rx, xl, (V, E, F))
-    ms, sweep_mode, clocks = run_sweep_back_to_back(args, torch, *fns)
+    ms_seq, mode_seq, _ = run_sweep_back_to_back(args, torch, *fns)
+    ms, sweep_mode, clocks = run_sweep_back_to_back(args, torch, *fns, concurrent=True)
     ms = max_over_ranks(torch, ms, "cuda")
     cb = canonical_bytes(V, E, F)
     sweep_bytes = sum(cb.values())
@@ -898,9 +1109,11 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
         "config": dict(CONFIG),
-        "sweep": {"timing": "the six kernels back to back after one L2 flush, one CUDA-event pair "
-                            "around the sweep (%s)" % sweep_mode,
+        "sweep": {"timing": "the six kernels after one L2 flush, one CUDA-event pair around the "
+                            "sweep (%s)" % sweep_mode,
                   "frac_of_%s_hbm" % peak_kind: (sweep_bytes / (ms * 1e-3) / 1e9) / peak,
+                  "sequential_ms": ms_seq, "sequential_gbs": sweep_bytes / (ms_seq * 1e-3) / 1e9,
+                  "sequential_timing": mode_seq,
                   "isolated_sum_ms": ms_isolated,
                   "isolated_note": "sum of the six kernels each timed alone after its own L2 flush "
                                    "(outputs stay dirty in L2 and are written back outside the "
@@ -915,7 +1128,7 @@ def main():
                      "algorithmic_bytes": cb[dom]},
         "e2e": {"value": sweep_bytes / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-        "gpu_launches": len(OPS) * args.steps,
+        "gpu_launches": len(OPS) * args.steps,  # the concurrent-graph leg that gives `value`
         "clocks": clocks,
         "clocks_isolated_leg": clocks_iso,
     }

@@ -9,6 +9,10 @@
 // Writes one binary int32 (or float64) file per result into out_dir for the
 // test to compare with the oracle, prints "OK" and exits 0; prints the
 // failing check and exits 1 otherwise.
+//   for_each_example torus <n> <patch_size>
+// Times, on an n x n torus, for_each<Op::VV> with a lambda that writes each
+// vertex's valence and the sum of its neighbours' ids, against rxg_query VV
+// into preallocated device buffers (CUDA events, 20 runs after 3 warm-ups).
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -102,8 +106,60 @@ __global__ void k_face_sum(Context ctx, FaceAttribute<int32_t> out)
     query.epilogue(block, shrd_alloc);
 }
 
+static int time_torus(int n, int patch)
+{
+    std::vector<std::vector<uint32_t>> fv;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            const uint32_t a = i * n + j, b = ((i + 1) % n) * n + j, c = ((i + 1) % n) * n + (j + 1) % n,
+                           d = i * n + (j + 1) % n;
+            fv.push_back({a, b, c});
+            fv.push_back({a, c, d});
+        }
+    RXMeshStatic rx(fv, "", (uint32_t)patch);
+    auto         V = rx.add_vertex_attribute<int32_t>("valence", 1, DEVICE);
+    auto         S = rx.add_vertex_attribute<int32_t>("nsum", 1, DEVICE);
+    VertexAttribute<int32_t> val = *V, sum = *S;
+    auto run = [&]() {
+        rx.for_each<Op::VV, 256>([val, sum] __device__(const VertexHandle& vh, const VertexIterator& it) {
+            int32_t s = 0;
+            for (uint16_t k = 0; k < it.size(); ++k) s += it[k].linear_id();
+            val(vh) = it.size();
+            sum(vh) = s;
+        });
+    };
+    int64_t rows = 0, nval = 0;
+    check(rxg_query_size(rx.handle(), RXG_OP_VV, &rows, &nval));
+    DeviceArray<int32_t> off((size_t)rows + 1), vals((size_t)nval);
+    auto q = [&]() { check(rxg_query(rx.handle(), RXG_OP_VV, off.data(), vals.data(), nullptr)); };
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float t[2];
+    for (int w = 0; w < 2; ++w) {
+        for (int i = 0; i < 3; ++i) w ? q() : run();
+        cudaEventRecord(a);
+        for (int i = 0; i < 20; ++i) w ? q() : run();
+        cudaEventRecord(b);
+        check_cuda(cudaEventSynchronize(b), "timing");
+        cudaEventElapsedTime(&t[w], a, b);
+    }
+    std::printf("torus %d x %d, %u patches: for_each<VV> %.2f us, rxg_query VV %.2f us per call\n", n, n,
+                rx.get_num_patches(), 1e3 * t[0] / 20, 1e3 * t[1] / 20);
+    std::printf("OK\n");
+    return 0;
+}
+
 int main(int argc, char** argv)
 {
+    if (argc >= 4 && std::string(argv[1]) == "torus") {
+        try {
+            return time_torus(std::stoi(argv[2]), std::stoi(argv[3]));
+        } catch (const std::exception& e) {
+            std::printf("FAILED: %s\n", e.what());
+            return 1;
+        }
+    }
     if (argc < 4) {
         std::printf("usage: for_each_example <mesh.obj> <patch_size> <out_dir>\n");
         return 2;
