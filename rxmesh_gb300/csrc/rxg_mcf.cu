@@ -531,6 +531,46 @@ __device__ __forceinline__ void mcf_row(const int32_t* __restrict__ row_ptr, con
             for (int c = 0; c < NC; ++c) acc[c] -= dt * x[(int64_t)r * NC + c];
         }
         area = T(0.5) * (T)k;  // 1 / v_weight = valence
+    } else if (k > 0 && k <= 8) {
+        // rings of up to 8 neighbours (nearly every row of a triangle mesh):
+        // all ids, then all positions and x rows, in flight together; the
+        // arithmetic and its order are the general loop's below
+        const V3<double> P = ld3(xyz, (int32_t)p);
+        int32_t          id[8];
+        V3<double>       X[8];
+        T                xv[8][NC];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) id[i] = i < k ? __ldg(rg + i) : (int32_t)p;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            X[i] = ld3(xyz, id[i]);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) xv[i][c] = x[(int64_t)id[i] * NC + c];
+        }
+        V3<double> Q = X[0];
+#pragma unroll
+        for (int j = 1; j < 8; ++j)
+            if (j == k - 1) Q = X[j];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            if (i < k) {
+                const V3<double> R = X[i];
+                const V3<double> S = (i + 1 < k) ? X[i + 1 < 8 ? i + 1 : 0] : X[0];
+                const bool has_q = wrap || i > 0, has_s = wrap || i < k - 1;
+                T          w     = T(0);
+                if (has_q) w += G::hc(P, R, Q);
+                if (has_s) w += G::hc(P, R, S);
+                w = (w >= T(0) ? w : T(0)) * dt;
+                sumw += w;
+#pragma unroll
+                for (int c = 0; c < NC; ++c) acc[c] -= w * xv[i][c];
+                if (has_q) {
+                    const T a = G::va(P, Q, R);
+                    area += a > T(0) ? a : T(0);
+                }
+                Q = R;
+            }
+        }
     } else if (k > 0) {
         const V3<double> P = ld3(xyz, (int32_t)p);
         int32_t          qi = __ldg(rg + k - 1), ri = __ldg(rg);
