@@ -143,13 +143,15 @@ __device__ __forceinline__ void assemble_row(int64_t p, const BatchArgs& a)
     const V3<double> P    = pos4(a.X, (int32_t)p);
     double           area = 0.0, sumw = 0.0;  // FP64 row sums (see k_mcf_assemble)
     if (k > 0) {
-        V3<double> Q = pos4(a.X, rg[k - 1]), R = pos4(a.X, rg[0]);
+        // FP64 and FP32 copies of each position made once (GeoMixed::Pt)
+        const MixedPt Pp = GeoMixed::make(P);
+        MixedPt       Q = GeoMixed::make(pos4(a.X, rg[k - 1])), R = GeoMixed::make(pos4(a.X, rg[0]));
         for (int32_t i = 0; i < k; ++i) {
-            const V3<double> S     = pos4(a.X, rg[i + 1 < k ? i + 1 : 0]);
-            const bool       has_q = wrap || i > 0, has_s = wrap || i < k - 1;
-            float            w     = 0.f;
-            if (has_q) w += GeoMixed::hc(P, R, Q);
-            if (has_s) w += GeoMixed::hc(P, R, S);
+            const MixedPt S     = GeoMixed::make(pos4(a.X, rg[i + 1 < k ? i + 1 : 0]));
+            const bool    has_q = wrap || i > 0, has_s = wrap || i < k - 1;
+            float         w     = 0.f;
+            if (has_q) w += GeoMixed::hc(Pp, R, Q);
+            if (has_s) w += GeoMixed::hc(Pp, R, S);
             w = (w >= 0.f ? w : 0.f) * a.dt;
             sumw += (double)w;
             Ent<float> e;
@@ -157,7 +159,7 @@ __device__ __forceinline__ void assemble_row(int64_t p, const BatchArgs& a)
             e.val              = -w;
             a.ent[ent_at<W>(a, p, rp, 1 + i)] = e;
             if (has_q) {
-                const float ar = GeoMixed::va(P, Q, R);
+                const float ar = GeoMixed::va(Pp, Q, R);
                 area += ar > 0.f ? (double)ar : 0.0;
             }
             Q = R;

@@ -2,6 +2,7 @@
 // and the implicit mean-curvature-flow step (plain FP64 and mixed FP32 with
 // FP64 iterative refinement).
 #include <algorithm>
+#include <type_traits>
 #include <cfloat>
 #include <cstdio>
 #include <cstdlib>
@@ -337,19 +338,30 @@ __global__ void __launch_bounds__(256) k_mcf_assemble(int64_t nv, const int32_t*
         // 2*area + sum of the T-rounded weights, so the Laplacian part keeps
         // exactly zero row sums when the FP64 residual uses it
         TB area = TB(0), sumw = TB(0);
-        if (k > 0) {
-            V3<double> Q = ld3(xyz, rg[k - 1]), R = ld3(xyz, rg[0]);
+        if (k > 0 && std::is_same<G, Geo<T>>::value) {
+            // each fan triangle evaluated once (bit for bit the values of
+            // the per-call loop below)
+            area = fan_row<T, TB>(
+                P, k, wrap, dt, [&](int32_t i) { return ld3(xyz, rg[i]); },
+                [&](int32_t i, T w) {
+                    sumw += (TB)w;
+                    out.entry(rp + 1 + i, rg[i], -w);
+                });
+        } else if (k > 0) {
+            // points made once per position (G::Pt: FP64 and FP32 copies)
+            const typename G::Pt Pp = G::make(P);
+            typename G::Pt       Q = G::make(ld3(xyz, rg[k - 1])), R = G::make(ld3(xyz, rg[0]));
             for (int32_t i = 0; i < k; ++i) {
-                const V3<double> S = ld3(xyz, rg[i + 1 < k ? i + 1 : 0]);
+                const typename G::Pt S = G::make(ld3(xyz, rg[i + 1 < k ? i + 1 : 0]));
                 const bool has_q = wrap || i > 0, has_s = wrap || i < k - 1;
                 T          w     = T(0);
-                if (has_q) w += G::hc(P, R, Q);
-                if (has_s) w += G::hc(P, R, S);
+                if (has_q) w += G::hc(Pp, R, Q);
+                if (has_s) w += G::hc(Pp, R, S);
                 w = (w >= T(0) ? w : T(0)) * dt;
                 sumw += (TB)w;
                 out.entry(rp + 1 + i, rg[i], -w);
                 if (has_q) {
-                    const T a = G::va(P, Q, R);
+                    const T a = G::va(Pp, Q, R);
                     area += a > T(0) ? (TB)a : TB(0);
                 }
                 Q = R;
@@ -518,6 +530,7 @@ __device__ __forceinline__ void mcf_row(const int32_t* __restrict__ row_ptr, con
                                         const int8_t* __restrict__ bnd, const double* __restrict__ xyz,
                                         T dt, bool uniform, int64_t p, const T* x, T* acc, T* diag)
 {
+    static_assert(std::is_same<G, Geo<T>>::value, "the matrix-free row uses the exact-type geometry");
     const int32_t  rp   = __ldg(row_ptr + p);
     const int32_t  k    = __ldg(row_ptr + p + 1) - rp - 1;
     const int32_t* rg   = col + rp + 1;
@@ -533,8 +546,9 @@ __device__ __forceinline__ void mcf_row(const int32_t* __restrict__ row_ptr, con
         area = T(0.5) * (T)k;  // 1 / v_weight = valence
     } else if (k > 0 && k <= 8) {
         // rings of up to 8 neighbours (nearly every row of a triangle mesh):
-        // all ids, then all positions and x rows, in flight together; the
-        // arithmetic and its order are the general loop's below
+        // all ids, then all positions and x rows, in flight together; each
+        // fan triangle evaluated once (fan_row, bit for bit the per-call
+        // values of the general loop below)
         const V3<double> P = ld3(xyz, (int32_t)p);
         int32_t          id[8];
         V3<double>       X[8];
@@ -547,53 +561,33 @@ __device__ __forceinline__ void mcf_row(const int32_t* __restrict__ row_ptr, con
 #pragma unroll
             for (int c = 0; c < NC; ++c) xv[i][c] = x[(int64_t)id[i] * NC + c];
         }
-        V3<double> Q = X[0];
+        area = fan_row<T, T>(
+            P, k, wrap, dt,
+            [&](int32_t i) {
+                V3<double> r = X[0];
 #pragma unroll
-        for (int j = 1; j < 8; ++j)
-            if (j == k - 1) Q = X[j];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            if (i < k) {
-                const V3<double> R = X[i];
-                const V3<double> S = (i + 1 < k) ? X[i + 1 < 8 ? i + 1 : 0] : X[0];
-                const bool has_q = wrap || i > 0, has_s = wrap || i < k - 1;
-                T          w     = T(0);
-                if (has_q) w += G::hc(P, R, Q);
-                if (has_s) w += G::hc(P, R, S);
-                w = (w >= T(0) ? w : T(0)) * dt;
+                for (int j = 1; j < 8; ++j)
+                    if (j == i) r = X[j];
+                return r;
+            },
+            [&](int32_t i, T w) {
                 sumw += w;
 #pragma unroll
-                for (int c = 0; c < NC; ++c) acc[c] -= w * xv[i][c];
-                if (has_q) {
-                    const T a = G::va(P, Q, R);
-                    area += a > T(0) ? a : T(0);
-                }
-                Q = R;
-            }
-        }
+                for (int j = 0; j < 8; ++j)
+                    if (j == i)
+#pragma unroll
+                        for (int c = 0; c < NC; ++c) acc[c] -= w * xv[j][c];
+            });
     } else if (k > 0) {
         const V3<double> P = ld3(xyz, (int32_t)p);
-        int32_t          qi = __ldg(rg + k - 1), ri = __ldg(rg);
-        V3<double>       Q = ld3(xyz, qi), R = ld3(xyz, ri);
-        for (int32_t i = 0; i < k; ++i) {
-            const int32_t    si    = __ldg(rg + (i + 1 < k ? i + 1 : 0));
-            const V3<double> S     = ld3(xyz, si);
-            const bool       has_q = wrap || i > 0, has_s = wrap || i < k - 1;
-            T                w     = T(0);
-            if (has_q) w += G::hc(P, R, Q);
-            if (has_s) w += G::hc(P, R, S);
-            w = (w >= T(0) ? w : T(0)) * dt;
-            sumw += w;
+        area               = fan_row<T, T>(
+            P, k, wrap, dt, [&](int32_t i) { return ld3(xyz, __ldg(rg + i)); },
+            [&](int32_t i, T w) {
+                sumw += w;
+                const int32_t r = __ldg(rg + i);
 #pragma unroll
-            for (int c = 0; c < NC; ++c) acc[c] -= w * x[(int64_t)ri * NC + c];
-            if (has_q) {
-                const T a = G::va(P, Q, R);
-                area += a > T(0) ? a : T(0);
-            }
-            Q  = R;
-            R  = S;
-            ri = si;
-        }
+                for (int c = 0; c < NC; ++c) acc[c] -= w * x[(int64_t)r * NC + c];
+            });
     }
     const T vw = T(0.5) / area;
     const T iv = T(1) / vw;

@@ -81,6 +81,85 @@ __device__ __forceinline__ T voronoi(V3<T> p, V3<T> q, V3<T> r)
     return T(0.125) * (dot(pr, pr) * clamp_cot(dq / A) + dot(pq, pq) * clamp_cot(dr / A));
 }
 
+// The three geometry terms of fan triangle (p, a, b) (a before b around p)
+// that a row of the MCF system uses, sharing the triangle's area:
+//   ha = half_cot(p, a, b)   (edge p-a, seen from b)
+//   hb = half_cot(p, b, a)   (edge p-b, seen from a)
+//   va = voronoi(p, a, b)
+// Bit for bit the values of the three separate calls: the three areas are
+// one |cross| (a swapped cross product is its exact negation), the
+// half-cotangents' dot products are the Voronoi corner products dr and dq
+// (exact sign changes), and their divisions are the Voronoi branch's.
+template <typename T>
+struct TriTerms
+{
+    T ha, hb, va;
+};
+template <typename T>
+__device__ __forceinline__ TriTerms<T> tri_terms(V3<T> p, V3<T> a, V3<T> b)
+{
+    const V3<T> pq = sub(a, p), qr = sub(b, a), pr = sub(b, p);
+    const V3<T> c  = cross(pq, pr);
+    const T     A  = T(0.5) * sqrt(dot(c, c));
+    if (!(A > tmin<T>())) return {T(0), T(0), T(-1)};
+    const T dp = dot(pq, pr), dq = -dot(qr, pq), dr = dot(qr, pr);
+    const T ha = clamp_cot(dr / A), hb = clamp_cot(dq / A);
+    T       va;
+    if (dp < T(0)) va = T(0.25) * A;
+    else if (dq < T(0) || dr < T(0)) va = T(0.125) * A;
+    else va = T(0.125) * (dot(pr, pr) * hb + dot(pq, pq) * ha);
+    return {ha, hb, va};
+}
+
+template <typename T>
+__device__ __forceinline__ V3<T> to_t(V3<double> a)
+{
+    return {(T)a.x, (T)a.y, (T)a.z};
+}
+
+// Row geometry of vertex p's fan with each triangle evaluated once
+// (tri_terms): calls on_w(i, w_i) for ring entries i = 0..k-1 in order, w_i
+// = max(0, cot-halves) * dt as the per-call loop forms it (Q half first,
+// then S half), and returns the sum of the clamped Voronoi terms in the same
+// order.  pos(i): the position (V3<double>) of ring entry i.  wrap: a closed
+// fan (interior vertex); an open fan has no triangle (p, r_{k-1}, r_0).
+template <typename T, typename TB, typename Pos, typename OnW>
+__device__ __forceinline__ TB fan_row(V3<double> Pd, int32_t k, bool wrap, T dt, Pos pos, OnW on_w)
+{
+    TB area = TB(0);
+    if (k <= 0) return area;
+    const V3<T> P     = to_t<T>(Pd);
+    const V3<T> first = to_t<T>(pos(0));
+    V3<T>       R     = first;
+    TriTerms<T> prev{T(0), T(0), T(-1)}, last{T(0), T(0), T(-1)};
+    if (wrap) {
+        last = tri_terms<T>(P, to_t<T>(pos(k - 1)), first);  // (p, r_{k-1}, r_0)
+        prev = last;
+    }
+    for (int32_t i = 0; i < k; ++i) {
+        const bool  has_q = wrap || i > 0, has_s = wrap || i < k - 1;
+        TriTerms<T> cur{T(0), T(0), T(-1)};
+        V3<T>       S = R;
+        if (has_s) {
+            if (i + 1 < k) {
+                S   = to_t<T>(pos(i + 1));
+                cur = tri_terms<T>(P, R, S);
+            } else {
+                cur = last;  // the closing triangle, evaluated above
+            }
+        }
+        T w = T(0);
+        if (has_q) w += prev.hb;
+        if (has_s) w += cur.ha;
+        w = (w >= T(0) ? w : T(0)) * dt;
+        on_w(i, w);
+        if (has_q) area += prev.va > T(0) ? (TB)prev.va : TB(0);
+        prev = cur;
+        R    = S;
+    }
+    return area;
+}
+
 __device__ __forceinline__ V3<float> tof(V3<double> a)
 {
     return {(float)a.x, (float)a.y, (float)a.z};
@@ -99,11 +178,15 @@ __device__ __forceinline__ bool near_degenerate(V3<float> a, V3<float> b, V3<flo
 }
 
 // weight and area evaluators: exact type T, or FP32 with an FP64 redo of
-// near-degenerate triangles (the mixed path)
+// near-degenerate triangles (the mixed path).  Each takes points of its own
+// type (G::Pt, made once per loaded position by G::make), so that a position
+// is converted once however many triangles it belongs to.
 template <typename T>
 struct Geo
 {
-    __device__ static T hc(V3<double> p, V3<double> r, V3<double> v)
+    using Pt = V3<double>;
+    __device__ static Pt make(V3<double> a) { return a; }
+    __device__ static T  hc(V3<double> p, V3<double> r, V3<double> v)
     {
         return half_cot<T>({(T)p.x, (T)p.y, (T)p.z}, {(T)r.x, (T)r.y, (T)r.z}, {(T)v.x, (T)v.y, (T)v.z});
     }
@@ -124,20 +207,27 @@ __device__ __forceinline__ bool near_right_angle(V3<float> p, V3<float> q, V3<fl
     return dp * dp < t * lpq * lpr || dq * dq < t * lqr * lpq || dr * dr < t * lqr * lpr;
 }
 
+// a position in FP64 and its FP32 rounding
+struct MixedPt
+{
+    V3<double> d;
+    V3<float>  f;
+};
+
 struct GeoMixed
 {
-    __device__ static float hc(V3<double> p, V3<double> r, V3<double> v)
+    using Pt = MixedPt;
+    __device__ static Pt    make(V3<double> a) { return {a, tof(a)}; }
+    __device__ static float hc(const Pt& p, const Pt& r, const Pt& v)
     {
-        const V3<float> pf = tof(p), rf = tof(r), vf = tof(v);
-        if (near_degenerate(pf, rf, vf)) return (float)half_cot<double>(p, r, v);
-        return half_cot<float>(pf, rf, vf);
+        if (near_degenerate(p.f, r.f, v.f)) return (float)half_cot<double>(p.d, r.d, v.d);
+        return half_cot<float>(p.f, r.f, v.f);
     }
-    __device__ static float va(V3<double> p, V3<double> q, V3<double> r)
+    __device__ static float va(const Pt& p, const Pt& q, const Pt& r)
     {
-        const V3<float> pf = tof(p), qf = tof(q), rf = tof(r);
-        if (near_degenerate(pf, qf, rf) || near_right_angle(pf, qf, rf))
-            return (float)voronoi<double>(p, q, r);
-        return voronoi<float>(pf, qf, rf);
+        if (near_degenerate(p.f, q.f, r.f) || near_right_angle(p.f, q.f, r.f))
+            return (float)voronoi<double>(p.d, q.d, r.d);
+        return voronoi<float>(p.f, q.f, r.f);
     }
 };
 

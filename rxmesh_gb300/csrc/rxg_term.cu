@@ -268,9 +268,10 @@ static void launch_gather(bool acc, int G, int64_t nv, const Lazy* z, const int3
 // Inertia term of a mass-spring system (the reference's add_inertia_term,
 // tests/RXMesh_test/test_hess.cu:13-29, an Op::V term): per vertex
 // E_v = m/2 |x_v - xt_v|^2, gradient m (x_v - xt_v), Hessian m I on the
-// diagonal block.  Without ACC the whole Hessian row is written (m I and
-// zero off-diagonal blocks); with ACC only the diagonal block is added to.
-template <typename T, int D, bool ACC>
+// diagonal block.  ACC: add to the gradient (else overwrite it).  HACC: add
+// m I to the diagonal blocks (the host has cleared the Hessian when the term
+// overwrites it); else write the whole row (m I, zero off-diagonal blocks).
+template <typename T, int D, bool ACC, bool HACC>
 __global__ void __launch_bounds__(128) k_inertia(int64_t nv, const int32_t* __restrict__ row_ptr,
                                                  const T* __restrict__ x, const T* __restrict__ xt, T m,
                                                  T* __restrict__ grad, T* __restrict__ hval,
@@ -295,9 +296,9 @@ __global__ void __launch_bounds__(128) k_inertia(int64_t nv, const int32_t* __re
 #pragma unroll
             for (int t = 0; t < DD; ++t) {
                 const T mi = (t % (D + 1) == 0) ? m : T(0);
-                dg[t]      = ACC ? dg[t] + mi : mi;
+                dg[t]      = HACC ? dg[t] + mi : mi;
             }
-            if (!ACC)
+            if (!HACC)
                 for (int64_t t = DD * (int64_t)(r0 + 1); t < DD * (int64_t)r1; ++t) hval[t] = T(0);
         }
     }
@@ -350,17 +351,22 @@ rxg_status rxg_inertia_eval(const rxg_mesh* h, int32_t dtype, int32_t dim, const
     }
     const int G = std::min<int>(grid_for_items(nv) * 2, 152 * 16);
     double*   part;
+    // overwriting: one coalesced clear of the whole Hessian, then the kernel
+    // adds m I to the diagonal blocks as when accumulating
+    if (hess && !acc)
+        RXG_CUDA_TRY(cudaMemsetAsync(hess->val, 0,
+                                     (size_t)dim * dim * z->nnz * (dtype == RXG_F64 ? 8 : 4), s));
     RXG_CUDA_TRY(scratch_alloc((void**)&part, sizeof(double) * (G + 1), s));
     auto run = [&](auto tag, auto dtag) {
         using T         = decltype(tag);
         constexpr int D = decltype(dtag)::value;
         T* hv           = hess ? (T*)hess->val : nullptr;
         if (acc)
-            k_inertia<T, D, true><<<G, 128, 0, s>>>(nv, z->row_ptr, (const T*)x, (const T*)x_target, (T)mass,
-                                                    (T*)grad, hv, part);
+            k_inertia<T, D, true, true><<<G, 128, 0, s>>>(nv, z->row_ptr, (const T*)x, (const T*)x_target,
+                                                          (T)mass, (T*)grad, hv, part);
         else
-            k_inertia<T, D, false><<<G, 128, 0, s>>>(nv, z->row_ptr, (const T*)x, (const T*)x_target,
-                                                     (T)mass, (T*)grad, hv, part);
+            k_inertia<T, D, false, true><<<G, 128, 0, s>>>(nv, z->row_ptr, (const T*)x, (const T*)x_target,
+                                                           (T)mass, (T*)grad, hv, part);
     };
     if (dtype == RXG_F64) {
         if (dim == 2) run(double{}, std::integral_constant<int, 2>{});
