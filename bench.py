@@ -46,7 +46,7 @@ def canonical_bytes(V, E, F):
     }
 
 
-EXTRA_OPS = ["EF", "FE", "FF", "EVD"]
+EXTRA_OPS = ["EF", "FE", "FF", "EVD", "EE"]
 
 
 def extra_canonical_bytes(V, E, F, nff):
@@ -57,11 +57,12 @@ def extra_canonical_bytes(V, E, F, nff):
         "FE": 6 * F + 12 * F,
         "FF": 6 * F + 4 * nff + 4 * (F + 1),
         "EVD": 4 * E + 6 * F + 16 * E,
+        "EE": 6 * F + 16 * E,
     }
 
 
 def run_edge_face_queries(args, torch, rx, sizes):
-    """EF, FE, FF and EVDiamond on the sweep's torus, each timed alone after
+    """EF, FE, FF, EVDiamond and EE on the sweep's torus, each timed alone after
     an L2 flush with CUDA events, as in run_sweep (not part of the headline
     sweep value)."""
     from rxmesh_gb300 import Op
@@ -421,15 +422,25 @@ def run_sweep_back_to_back(args, torch, flush_l2, launch, concurrent=False):
     return ms, mode, clk.summary()
 
 
+E2E_MODES = {"sync": None, "async": 1, "direct": 2}  # rxg_query / rxg_query_ex(RXG_HOST_ASYNC / _DIRECT)
+
+
 def run_e2e(args, torch, rx, x_in_host, sizes):
-    """Same sweep through the C ABI with pinned host buffers (copies inside the call)."""
+    """The sweep through the C ABI with page-locked host buffers, copies (or
+    host-link reads and writes) inside the timed region, each step waited
+    for on the host before the next.  Three ways a caller can run it:
+    "sync" calls rxg_query / rxg_vertex_normals one after another (each
+    returns with its results on the host); "async" and "direct" issue the
+    six rxg_query_ex / rxg_vertex_normals_ex calls on six streams and wait
+    for all of them.  Returns ({mode: ms per step}, h2d, d2h)."""
     import ctypes
     from rxmesh_gb300 import Op, _lib
     L = _lib.load()
-    V, E, F = sizes
+    names = ("VV", "VE", "VF", "FV", "EV")
     host = {}
     d2h = 0
-    for name, op in (("VV", Op.VV), ("VE", Op.VE), ("VF", Op.VF), ("FV", Op.FV), ("EV", Op.EV)):
+    for name in names:
+        op = getattr(Op, name)
         rows, nval = rx.query_size(op)
         off = torch.empty(rows + 1, dtype=torch.int32).pin_memory() if op <= Op.VF else None
         val = torch.empty(nval, dtype=torch.int32).pin_memory()
@@ -440,28 +451,43 @@ def run_e2e(args, torch, rx, x_in_host, sizes):
     nh = torch.empty_like(xh).pin_memory()
     d2h += nh.numel() * 4
     h2d = xh.numel() * 4
+    streams = [torch.cuda.Stream() for _ in range(len(names) + 1)]
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
-    def sweep():
-        for name in ("VV", "VE", "VF", "FV", "EV"):
+    def sweep(flags):
+        cur = torch.cuda.current_stream()
+        if flags is None:
+            for name in names:
+                off, val = host[name]
+                _lib.check(L.rxg_query(rx._h, getattr(Op, name), ptr(off), ptr(val), None))
+            _lib.check(L.rxg_vertex_normals(rx._h, 1, ptr(xh), ptr(nh), None))
+            return
+        for s in streams:
+            s.wait_stream(cur)
+        for name, s in zip(names, streams):
             off, val = host[name]
-            _lib.check(L.rxg_query(rx._h, getattr(Op, name),
-                                   ctypes.c_void_p(off.data_ptr()) if off is not None else None,
-                                   ctypes.c_void_p(val.data_ptr()), None))
-        _lib.check(L.rxg_vertex_normals(rx._h, 1, ctypes.c_void_p(xh.data_ptr()),
-                                        ctypes.c_void_p(nh.data_ptr()), None))
+            _lib.check(L.rxg_query_ex(rx._h, getattr(Op, name), ptr(off), ptr(val), flags,
+                                      ctypes.c_void_p(s.cuda_stream)))
+        _lib.check(L.rxg_vertex_normals_ex(rx._h, 1, ptr(xh), ptr(nh), flags,
+                                           ctypes.c_void_p(streams[-1].cuda_stream)))
+        for s in streams:
+            cur.wait_stream(s)
+        cur.synchronize()  # the step's results are on the host
 
-    for _ in range(args.warmup):
-        sweep()
-    torch.cuda.synchronize()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    t0.record()
-    for _ in range(args.steps):
-        sweep()
-    t1.record()
-    torch.cuda.synchronize()
-    ms = t0.elapsed_time(t1) / args.steps
-    return ms, h2d, d2h
+    out = {}
+    for mode, flags in E2E_MODES.items():
+        for _ in range(args.warmup):
+            sweep(flags)
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(args.steps):
+            sweep(flags)
+        t1.record()
+        torch.cuda.synchronize()
+        out[mode] = t0.elapsed_time(t1) / args.steps
+    return out, h2d, d2h
 
 
 MCF_LEVEL, MCF_STEPS, MCF_DT, MCF_TOL = 8, 10, 1e-3, 1e-6
@@ -1098,7 +1124,9 @@ def main():
     cb = canonical_bytes(V, E, F)
     sweep_bytes = sum(cb.values())
     value = world * sweep_bytes / (ms * 1e-3) / 1e9
-    e2e_ms, h2d, d2h = run_e2e(args, torch, rx, xl.cpu(), (V, E, F))
+    e2e_modes, h2d, d2h = run_e2e(args, torch, rx, xl.cpu(), (V, E, F))
+    e2e_best = min(e2e_modes, key=e2e_modes.get)
+    e2e_ms = e2e_modes[e2e_best]
     avg = {k: statistics.mean(v) for k, v in per.items()}
     dom = max(avg, key=lambda k: avg[k])
     peak, peak_kind = peaks()
@@ -1127,7 +1155,9 @@ def main():
                      "frac": ach / peak, "peak_source": peak_kind, "traffic": traffic,
                      "algorithmic_bytes": cb[dom]},
         "e2e": {"value": sweep_bytes / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+                "mode": e2e_best, "ms_per_step_by_mode": e2e_modes,
+                "host_link_gbs": (h2d + d2h) / (e2e_ms * 1e-3) / 1e9},
         "gpu_launches": len(OPS) * args.steps,  # the concurrent-graph leg that gives `value`
         "clocks": clocks,
         "clocks_isolated_leg": clocks_iso,

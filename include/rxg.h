@@ -56,7 +56,13 @@ enum {
                       v0->v1, v1, vertex opposite in the face traversing v1->v0;
                       -1 where there is no such face (dense ne x 4; Op::EVDiamond,
                       kernels/rxmesh_queries.cuh:197-262; edge-manifold, consistently
-                      oriented meshes, else RXG_ERR_NONMANIFOLD) */
+                      oriented meshes, else RXG_ERR_NONMANIFOLD) */,
+    RXG_OP_EE = 9  /* edge   -> edges of its faces: for the face traversing the edge
+                      from its first vertex (as EV lists it), that face's next and
+                      previous edge, then the same for the face traversing it from
+                      its second vertex; -1 where there is no such face (dense ne x 4;
+                      Op::EE, kernels/rxmesh_queries.cuh:269-340; edge-manifold,
+                      consistently oriented meshes, else RXG_ERR_NONMANIFOLD) */
 };
 
 enum { RXG_ELEM_VERTEX = 0, RXG_ELEM_EDGE = 1, RXG_ELEM_FACE = 2 };
@@ -231,6 +237,28 @@ rxg_status rxg_query_size(const rxg_mesh* m, int32_t op, int64_t* n_rows,
  */
 rxg_status rxg_query(const rxg_mesh* m, int32_t op, int32_t* offsets,
                      int32_t* values, void* stream);
+
+/*
+ * rxg_query and rxg_vertex_normals with flags, for host arrays allocated
+ * page-locked (cudaHostAlloc, or registered with cudaHostRegister); both
+ * flags make the call stream-ordered: it enqueues its work on `stream` and
+ * returns, and the results are in the host arrays once the work `stream`
+ * held at return has completed (synchronise the stream or wait on an event
+ * recorded on it).  Independent calls on different streams then overlap.
+ *   RXG_HOST_ASYNC:  the kernel writes device scratch and a stream-ordered
+ *                    copy takes it to the host array (positions come in the
+ *                    same way).
+ *   RXG_HOST_DIRECT: the kernel reads and writes the page-locked arrays in
+ *                    place over the host link: no scratch, no copy.
+ * flags = 0, a device or pageable output array, or an argument error: the
+ * call is rxg_query / rxg_vertex_normals (synchronous for host arrays).
+ * No reference counterpart (RXMesh's queries write device memory only).
+ */
+enum { RXG_HOST_ASYNC = 1, RXG_HOST_DIRECT = 2 };
+rxg_status rxg_query_ex(const rxg_mesh* m, int32_t op, int32_t* offsets, int32_t* values,
+                        int32_t flags, void* stream);
+rxg_status rxg_vertex_normals_ex(const rxg_mesh* m, int32_t weighting, const float* xyz,
+                                 float* out, int32_t flags, void* stream);
 
 /*
  * Oriented VV (Query::dispatch<Op::VV>(..., oriented=true),

@@ -127,6 +127,8 @@ template <>
 struct OpTraits<Op::EF> { static constexpr int src = RXG_ELEM_EDGE, out = RXG_ELEM_FACE; };
 template <>
 struct OpTraits<Op::EVDiamond> { static constexpr int src = RXG_ELEM_EDGE, out = RXG_ELEM_VERTEX; };
+template <>
+struct OpTraits<Op::EE> { static constexpr int src = RXG_ELEM_EDGE, out = RXG_ELEM_EDGE; };
 
 // Exclusive scan of s[0..n) in place (any n), returns the total.
 template <uint32_t BT>
@@ -360,9 +362,9 @@ struct Query
         m_num_src = (uint32_t)(SRC == RXG_ELEM_VERTEX ? (allow_not_owned ? h.nVl : h.nVo)
                                : SRC == RXG_ELEM_EDGE ? (allow_not_owned ? h.nEl : h.nEo)
                                                       : (allow_not_owned ? h.nFl : h.nFo));
-        // EV slice: every op but FE / EF / FF; FE slice: every op but EV, VE
-        // and (unoriented) VV
-        constexpr bool need_ev = op != Op::FE && op != Op::EF && op != Op::FF;
+        // EV slice: every op but FE / EF / FF / EE; FE slice: every op but
+        // EV, VE and (unoriented) VV
+        constexpr bool need_ev = op != Op::FE && op != Op::EF && op != Op::FF && op != Op::EE;
         constexpr bool need_fe = op != Op::EV && op != Op::VV && op != Op::VE;
         const bool     want_fe = need_fe || (op == Op::VV && oriented);
         uint32_t*      s_ev    = need_ev ? shrd_alloc.alloc<uint32_t>((uint32_t)h.nEl) : nullptr;
@@ -402,6 +404,22 @@ struct Query
                 const uint32_t fe = s_fe[i];
                 const int      f = i / 3, k = i - 3 * (i / 3);
                 m_s_value[4 * (fe >> 1) + 1 + 2 * (fe & 1u)] = face_vertex(s_fe, s_ev, f, (k + 2) % 3);
+            }
+            block.sync();
+            m_stride = 4;
+        } else if constexpr (op == Op::EE) {
+            m_s_value = shrd_alloc.alloc<uint16_t>((uint32_t)(4 * h.nEl));
+            for (int i = threadIdx.x; i < 4 * h.nEl; i += blockThreads) m_s_value[i] = INVALID16;
+            block.sync();
+            // beside edge k of a face lie the face's edges k+1 (next) and k+2
+            // (previous); the face traversing the edge as stored (dir 0)
+            // fills slots 0 and 1, the other one slots 2 and 3
+            for (int i = threadIdx.x; i < 3 * h.nFl; i += blockThreads) {
+                const uint32_t fe = s_fe[i];
+                const int      f = i / 3, k = i - 3 * (i / 3);
+                uint16_t*      q = m_s_value + 4 * (fe >> 1) + 2 * (fe & 1u);
+                q[0]             = (uint16_t)(s_fe[3 * f + (k + 1) % 3] >> 1);
+                q[1]             = (uint16_t)(s_fe[3 * f + (k + 2) % 3] >> 1);
             }
             block.sync();
             m_stride = 4;
@@ -710,6 +728,7 @@ inline size_t query_smem_bytes(Op op, const rxg_device_context& c, bool oriented
             return fe + offE + vals3F + (tail > posE ? tail : posE);
         }
         case Op::EVDiamond: return ev + fe + pad16(8 * E);
+        case Op::EE: return fe + pad16(8 * E);
     }
     return 0;
 }

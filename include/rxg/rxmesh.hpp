@@ -79,7 +79,8 @@ enum class Op : int32_t {
     EF = RXG_OP_EF,
     FE = RXG_OP_FE,
     FF = RXG_OP_FF,
-    EVDiamond = RXG_OP_EVD
+    EVDiamond = RXG_OP_EVD,
+    EE = RXG_OP_EE
 };
 
 // where a buffer lives (RXMesh's locationT)

@@ -207,20 +207,16 @@ def ee(fv):
     2d holds the face's next edge and slot 2d+1 its previous edge; -1 where
     e has no such face.  (The reference computes the previous edge's index
     as (cur - 1) % 3, which is -1 for the first edge in C++; the previous
-    edge is (cur + 2) % 3.)  Walks each edge's faces."""
-    f = np.asarray(fv)
+    edge is (cur + 2) % 3.)  Every face corner k writes the slots of its
+    edge k (vectorised; one writer per slot on such a mesh)."""
+    f = np.asarray(fv, np.int64)
     ev, fe = edges(fv)
-    ne = len(ev)
-    faces_of = [[] for _ in range(ne)]
-    for fi in range(len(f)):
-        for k in range(3):
-            faces_of[fe[fi][k]].append((fi, k))
-    out = np.full((ne, 4), -1, np.int32)
-    for e in range(ne):
-        for fi, k in faces_of[e]:
-            d = 0 if f[fi][k] == ev[e][0] else 1
-            out[e, 2 * d] = fe[fi][(k + 1) % 3]
-            out[e, 2 * d + 1] = fe[fi][(k + 2) % 3]
+    ev, fe = np.asarray(ev, np.int64), np.asarray(fe, np.int64)
+    out = np.full((len(ev), 4), -1, np.int32)
+    d = (f != ev[fe][..., 0]).astype(np.int64)  # (nf, 3): direction of edge k in face
+    slot = 4 * fe + 2 * d
+    out.reshape(-1)[slot.reshape(-1)] = np.roll(fe, -1, axis=1).reshape(-1)
+    out.reshape(-1)[(slot + 1).reshape(-1)] = np.roll(fe, 1, axis=1).reshape(-1)
     return out
 
 

@@ -14,7 +14,7 @@ import torch
 from . import _lib
 from ._lib import RXGError, check
 
-__all__ = ["Op", "edge_edge_slots", "RXMeshStatic", "SparseMatrix", "CGSolver", "PCGSolver", "RXGError",
+__all__ = ["Op", "RXMeshStatic", "SparseMatrix", "CGSolver", "PCGSolver", "RXGError",
            "DiffScalarProblem", "BlockSparseMatrix", "NewtonSolver", "mcf_step", "MeshBatch",
            "device_check"]
 
@@ -23,28 +23,12 @@ class Op:
     """Query operations (RXMesh's Op enum, include/rxmesh/types.h).  EVD is
     Op::EVDiamond.  CSR (offsets + values): VV, VE, VF, EF, FF; fixed rows:
     FV (3), EV (2), FE (3), EVD (4, -1 where the edge has no such face),
-    EE (4, -1 likewise; composed from FV, FE and EV, see edge_edge_slots)."""
+    EE (4, -1 likewise: per direction the next and previous edge of the face
+    traversing the edge that way)."""
     VV, VE, VF, FV, EV, EF, FE, FF, EVD, EE = 0, 1, 2, 3, 4, 5, 6, 7, 8, 9
     NAMES = {"VV": 0, "VE": 1, "VF": 2, "FV": 3, "EV": 4, "EF": 5, "FE": 6, "FF": 7, "EVD": 8,
              "EE": 9}
     CSR = (0, 1, 2, 5, 7)
-
-
-def edge_edge_slots(fv, fe, ev, ne):
-    """RXMesh's Op::EE (e_e_manifold, kernels/rxmesh_queries.cuh:269-340)
-    from the FV, FE and EV rows (linear ids, (nf, 3), (nf, 3), (ne, 2)
-    int32 tensors on any device): four slots per edge; for the face that
-    traverses edge e from its first vertex (direction d = 0) or its second
-    (d = 1), slot 2d holds that face's next edge and slot 2d+1 its previous
-    edge, -1 where e has no such face.  Needs an edge-manifold, consistently
-    oriented mesh (then each slot is written once)."""
-    fv, fe, ev = fv.reshape(-1, 3).long(), fe.reshape(-1, 3).long(), ev.reshape(-1, 2).long()
-    d = (ev[fe][..., 0] != fv).long()          # edge k of a face runs fv[k] -> fv[k+1]
-    slot = 4 * fe + 2 * d
-    out = torch.full((4 * ne,), -1, dtype=torch.int32, device=fe.device)
-    out[slot.reshape(-1)] = fe.roll(-1, dims=1).reshape(-1).to(torch.int32)
-    out[(slot + 1).reshape(-1)] = fe.roll(1, dims=1).reshape(-1).to(torch.int32)
-    return out
 
 
 _ELEM = {"v": 0, "vertex": 0, "e": 1, "edge": 1, "f": 2, "face": 2}
@@ -55,14 +39,6 @@ def _stream(stream=None):
     if stream is None:
         stream = torch.cuda.current_stream()
     return ctypes.c_void_p(stream.cuda_stream)
-
-
-class _nullctx:
-    def __enter__(self):
-        return None
-
-    def __exit__(self, *a):
-        return False
 
 
 def _ptr(t):
@@ -319,20 +295,8 @@ class RXMeshStatic:
         """Materialise query `op` for all owned elements, in linear ids.
 
         Returns (offsets, values) int32 CUDA tensors; offsets is None for the
-        fixed-row ops FV, EV, FE, EVD (3, 2, 3, 4 values per row)."""
+        fixed-row ops FV, EV, FE, EVD, EE (3, 2, 3, 4, 4 values per row)."""
         op = Op.NAMES.get(op, op) if isinstance(op, str) else int(op)
-        if op == Op.EE:
-            if not (self.is_edge_manifold() and self.is_oriented()):
-                raise RXGError(4, "Op.EE needs an edge-manifold, consistently oriented mesh")
-            fv = self.query(Op.FV, stream)[1]
-            fe = self.query(Op.FE, stream)[1]
-            ev = self.query(Op.EV, stream)[1]
-            with torch.cuda.stream(stream) if stream is not None else _nullctx():
-                ee = edge_edge_slots(fv, fe, ev, self.get_num_edges())
-            if values is not None:
-                values.copy_(ee)
-                ee = values
-            return None, ee
         rows, nval = self.query_size(op)
         dev = torch.device("cuda", torch.cuda.current_device())
         csr = int(op) in Op.CSR

@@ -114,6 +114,8 @@ SIGNATURES = {
     "rxg_face_term_gather": [P, I32, I32, P, I32, P, P, P, P, P],
     "rxg_symdir_eval": [P, I32, P, P, I32, P, P, P, P, P],
     "rxg_inertia_eval": [P, I32, I32, P, P, D, I32, P, P, P, P],
+    "rxg_query_ex": [P, I32, P, P, I32, P],
+    "rxg_vertex_normals_ex": [P, I32, P, P, I32, P],
 }
 _RESTYPE = {"rxg_status_string": ctypes.c_char_p, "rxg_last_error": ctypes.c_char_p,
             "rxg_mesh_destroy": None, "rxg_batch_destroy": None}

@@ -105,7 +105,7 @@ struct Mesh
     void* lazy = nullptr;
 
     int64_t device_bytes = 0;
-    size_t  smem_bytes[16] = {};  // per kernel kind (query op; 9, 10: normals), max over patches
+    size_t  smem_bytes[16] = {};  // per kernel kind (query ops 0-9; 11: oriented FF; 12, 13: normals), max over patches
 
     // calls with host arrays: a copy stream and events that overlap the
     // device-to-host copy of each slice of patches with the kernel of the next

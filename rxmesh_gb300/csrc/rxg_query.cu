@@ -308,19 +308,20 @@ __global__ void __launch_bounds__(kQT) k_query_elem(const PatchHdr* __restrict__
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ uint64_t bar;
 
-    constexpr bool FE  = OP == RXG_OP_FE, EVD = OP == RXG_OP_EVD;
+    constexpr bool FE = OP == RXG_OP_FE, EVD = OP == RXG_OP_EVD, EE = OP == RXG_OP_EE;
     const PatchHdr h   = load_hdr(hdrs);
     const int32_t  nVo = h.nVo;
     const int32_t  nVr = h.nVl - h.nVo;
     // FV needs every local edge an owned face uses, i.e. the whole EV slice;
     // EV needs only the owned prefix; FE needs no EV; EVD needs the whole
-    // EV slice and every local face (the faces of the owned edges).
-    const int32_t ev_words = (OP == 3 || EVD) ? h.nEl : (FE ? 0 : h.nEo);
-    const int32_t fe_w     = EVD ? (int32_t)fe_words(h.nFl)
-                                 : ((OP == 3 || FE) ? (int32_t)fe_words(h.nFo) : 0);
-    // ribbon table of the output ids: vertices, or edges for FE
-    const int32_t rib_n   = FE ? h.nEl - h.nEo : nVr;
-    const int32_t rib_off = FE ? h.re_off : h.rv_off;
+    // EV slice and every local face (the faces of the owned edges); EE
+    // needs every local face and no EV.
+    const int32_t ev_words = (OP == 3 || EVD) ? h.nEl : ((FE || EE) ? 0 : h.nEo);
+    const int32_t fe_w     = (EVD || EE) ? (int32_t)fe_words(h.nFl)
+                                         : ((OP == 3 || FE) ? (int32_t)fe_words(h.nFo) : 0);
+    // ribbon table of the output ids: vertices, or edges for FE and EE
+    const int32_t rib_n   = (FE || EE) ? h.nEl - h.nEo : nVr;
+    const int32_t rib_off = (FE || EE) ? h.re_off : h.rv_off;
 
     uint32_t* s_ev = smem;
     uint32_t* s_fe = s_ev + pad4i(ev_words);
@@ -374,6 +375,33 @@ __global__ void __launch_bounds__(kQT) k_query_elem(const PatchHdr* __restrict__
             const uint32_t v = slot[i];
             base[i] = v == 0xffffu ? -1
                                    : ((int32_t)v < nVo ? h.v_base + (int32_t)v : (int32_t)s_rv[v - nVo]);
+        }
+    } else if (EE) {
+        // per owned edge two 32-bit slots of two 16-bit local edge ids: slot
+        // d for the face traversing the edge from its vertex d (FE's
+        // direction bit), holding that face's next and previous edge
+        // (0xffff: no such face).  On an edge-manifold, consistently
+        // oriented mesh each slot has one writer.
+        uint32_t* slot = s_rv + pad4i(rib_n);
+        for (int i = threadIdx.x; i < 2 * h.nEo; i += kQT) slot[i] = 0xffffffffu;
+        __syncthreads();
+        for (int i = threadIdx.x; i < 3 * h.nFl; i += kQT) {
+            const uint32_t fe = fe16[i];
+            const uint32_t e  = fe >> 1;
+            if ((int32_t)e >= h.nEo) continue;
+            const int      f  = i / 3, k = i - 3 * f;
+            const uint32_t nx = (uint32_t)fe16[3 * f + (k == 2 ? 0 : k + 1)] >> 1;
+            const uint32_t pv = (uint32_t)fe16[3 * f + (k == 0 ? 2 : k - 1)] >> 1;
+            slot[2 * e + (fe & 1u)] = nx | (pv << 16);
+        }
+        __syncthreads();
+        const uint16_t* s16  = reinterpret_cast<const uint16_t*>(slot);
+        const int32_t   n    = 4 * h.nEo;
+        int32_t*        base = out_val + 4 * (int64_t)h.e_base;
+        for (int i = threadIdx.x; i < n; i += kQT) {
+            const uint32_t e = s16[i];
+            base[i] = e == 0xffffu ? -1
+                                   : ((int32_t)e < h.nEo ? h.e_base + (int32_t)e : (int32_t)s_rv[e - h.nEo]);
         }
     } else if (OP == 3) {
         const int32_t n    = 3 * h.nFo;
@@ -634,7 +662,7 @@ __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restri
 // ---------------------------------------------------------------------
 
 // shared-memory table kinds of the normal kernels (after the query ops)
-constexpr int kNormalArea = 9, kNormalMax = 10;
+constexpr int kNormalArea = 12, kNormalMax = 13;
 // and of the oriented-mesh FF kernel
 constexpr int kFFOriented = 11;
 
@@ -657,6 +685,7 @@ static size_t smem_words(const PatchHdr& h, int kind)
         case RXG_OP_FF:  // + the patch's FF values, added by compute_smem_table
             return few + pad4i(nFr) + pad4i(h.nEl + 1) + few + pad4i(h.nFo + 1) + 4;
         case RXG_OP_EVD: return pad4i(h.nEl) + few + pad4i(nVr) + 2 * (size_t)h.nEo;
+        case RXG_OP_EE: return few + pad4i(nEr) + 2 * (size_t)h.nEo;
         case kFFOriented:  // + the patch's FF values, added by compute_smem_table
             return few + pad4i(nFr) + pad4i(h.nEl) + pad4i(h.nFo + 1) + 4;
         default:  // normals: positions as float4 behind the incidence block
@@ -666,8 +695,8 @@ static size_t smem_words(const PatchHdr& h, int kind)
 
 void compute_smem_table(Mesh& m)
 {
-    for (int kind = 0; kind <= kFFOriented; ++kind) {
-        if (kind > RXG_OP_EVD && kind < kNormalArea) continue;
+    for (int kind = 0; kind <= kNormalMax; ++kind) {
+        if (kind == 10) continue;  // unused
         size_t w = 0;
         for (size_t p = 0; p < m.hdr.size(); ++p) {
             size_t pw = smem_words(m.hdr[p], kind);
@@ -755,6 +784,7 @@ static rxg_status launch_query_bt(const Mesh* m, int op, int32_t* d_off, int32_t
         case RXG_OP_EV: return launch(k_query_elem<4, BT>, BT, m, smem, s, "EV", r, hd, ar, d_val, err);
         case RXG_OP_FE: return launch(k_query_elem<RXG_OP_FE, BT>, BT, m, smem, s, "FE", r, hd, ar, d_val, err);
         case RXG_OP_EVD: return launch(k_query_elem<RXG_OP_EVD, BT>, BT, m, smem, s, "EVD", r, hd, ar, d_val, err);
+        case RXG_OP_EE: return launch(k_query_elem<RXG_OP_EE, BT>, BT, m, smem, s, "EE", r, hd, ar, d_val, err);
     }
     set_error("rxg_query: unknown op %d", op);
     return RXG_ERR_INVALID;
@@ -825,6 +855,30 @@ static rxg_status stage_out(void* user, size_t bytes, cudaStream_t s, Staged& st
     RXG_CUDA_TRY(scratch_alloc(&st.d, bytes ? bytes : 16, s));
     st.owns = true;
     return RXG_OK;
+}
+
+// page-locked (or registered) host memory: a stream-ordered copy can target it
+static bool is_pinned_host(const void* p)
+{
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// the device address of page-locked host memory (nullptr otherwise)
+static void* host_mapped(void* p)
+{
+    if (!is_pinned_host(p)) return nullptr;
+    void* d = nullptr;
+    if (cudaHostGetDevicePointer(&d, p, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return d;
 }
 
 static rxg_status stage_in(const void* user, size_t bytes, cudaStream_t s, Staged& st)
@@ -916,7 +970,8 @@ rxg_status rxg_query_size(const rxg_mesh* h, int32_t op, int64_t* n_rows, int64_
         case RXG_OP_EF: *n_rows = M.ne; *n_values = 3 * M.nf; return RXG_OK;
         case RXG_OP_FE: *n_rows = M.nf; *n_values = 3 * M.nf; return RXG_OK;
         case RXG_OP_FF: *n_rows = M.nf; *n_values = M.ff_base.empty() ? 0 : M.ff_base.back(); return RXG_OK;
-        case RXG_OP_EVD: *n_rows = M.ne; *n_values = 4 * M.ne; return RXG_OK;
+        case RXG_OP_EVD:
+        case RXG_OP_EE: *n_rows = M.ne; *n_values = 4 * M.ne; return RXG_OK;
     }
     set_error("rxg_query_size: unknown op %d", op);
     return RXG_ERR_INVALID;
@@ -929,9 +984,10 @@ rxg_status rxg_query(const rxg_mesh* h, int32_t op, int32_t* offsets, int32_t* v
     rxg_status st = rxg_query_size(h, op, &rows, &nval);
     if (st) return st;
     const bool csr = op <= RXG_OP_VF || op == RXG_OP_EF || op == RXG_OP_FF;
-    if (op == RXG_OP_EVD && (!h->m.edge_manifold || !h->m.oriented)) {
-        set_error("rxg_query: EVDiamond needs an edge-manifold, consistently oriented mesh "
-                  "(each edge's two faces traverse it in opposite directions)");
+    if ((op == RXG_OP_EVD || op == RXG_OP_EE) && (!h->m.edge_manifold || !h->m.oriented)) {
+        set_error("rxg_query: %s needs an edge-manifold, consistently oriented mesh "
+                  "(each edge's two faces traverse it in opposite directions)",
+                  op == RXG_OP_EE ? "EE" : "EVDiamond");
         return RXG_ERR_NONMANIFOLD;
     }
     if (!values || (csr && !offsets)) {
@@ -968,7 +1024,7 @@ rxg_status rxg_query(const rxg_mesh* h, int32_t op, int32_t* offsets, int32_t* v
             int64_t       e;
             if (op == RXG_OP_FV || op == RXG_OP_FE) e = 3 * f_first(M, p);
             else if (op == RXG_OP_EV) e = 2 * e_first(M, p);
-            else if (op == RXG_OP_EVD) e = 4 * e_first(M, p);
+            else if (op == RXG_OP_EVD || op == RXG_OP_EE) e = 4 * e_first(M, p);
             else if (op == RXG_OP_EF) e = M.ef_base[p];
             else if (op == RXG_OP_FF) e = M.ff_base[p];
             else if (p == M.num_patches) e = nval;
@@ -1014,6 +1070,82 @@ rxg_status rxg_vertex_normals(const rxg_mesh* h, int32_t weighting, const float*
                            return launch_normals(&M, weighting, (const float*)si.d, (float*)so.d, s, r);
                        },
                        pieces);
+}
+
+rxg_status rxg_query_ex(const rxg_mesh* h, int32_t op, int32_t* offsets, int32_t* values, int32_t flags,
+                        void* stream)
+{
+    if (flags & ~(RXG_HOST_ASYNC | RXG_HOST_DIRECT)) {
+        set_error("rxg_query_ex: unknown flags %d", flags);
+        return RXG_ERR_INVALID;
+    }
+    const bool csr = op <= RXG_OP_VF || op == RXG_OP_EF || op == RXG_OP_FF;
+    int64_t    rows, nval;
+    rxg_status st = rxg_query_size(h, op, &rows, &nval);
+    if (st) return st;
+    // argument errors, device outputs and non-manifold EVDiamond: rxg_query
+    if (!flags || !values || (csr && !offsets) || is_device_ptr(values) ||
+        ((op == RXG_OP_EVD || op == RXG_OP_EE) && (!h->m.edge_manifold || !h->m.oriented)))
+        return rxg_query(h, op, offsets, values, stream);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (flags & RXG_HOST_DIRECT) {
+        int32_t* dv = (int32_t*)host_mapped(values);
+        int32_t* dof = !csr ? nullptr : is_device_ptr(offsets) ? offsets : (int32_t*)host_mapped(offsets);
+        if (dv && (!csr || dof)) {
+            if (((uintptr_t)dv & 15u) != 0) {
+                set_error("rxg_query_ex: values must be 16-byte aligned (vectorised row stores)");
+                return RXG_ERR_INVALID;
+            }
+            return launch_query(&h->m, op, dof, dv, s);
+        }
+    }
+    // stream-ordered staging: every host output page-locked, else rxg_query
+    if (!is_pinned_host(values) || (csr && !is_device_ptr(offsets) && !is_pinned_host(offsets)))
+        return rxg_query(h, op, offsets, values, stream);
+    if (((uintptr_t)values & 15u) != 0) {
+        set_error("rxg_query_ex: values must be 16-byte aligned (vectorised row stores)");
+        return RXG_ERR_INVALID;
+    }
+    Staged       so, sv;
+    const size_t off_bytes = csr ? (size_t)(rows + 1) * 4 : 0, val_bytes = (size_t)nval * 4;
+    if ((st = stage_out(csr ? offsets : nullptr, off_bytes, s, so))) return st;
+    if ((st = stage_out(values, val_bytes, s, sv))) return st;
+    // kernel, then the copies, all on `stream`; the scratch is freed in
+    // stream order after the copies (Staged's destructor)
+    if ((st = launch_query(&h->m, op, (int32_t*)so.d, (int32_t*)sv.d, s))) return st;
+    if (so.owns) RXG_CUDA_TRY(cudaMemcpyAsync(offsets, so.d, off_bytes, cudaMemcpyDeviceToHost, s));
+    RXG_CUDA_TRY(cudaMemcpyAsync(values, sv.d, val_bytes, cudaMemcpyDeviceToHost, s));
+    return RXG_OK;
+}
+
+rxg_status rxg_vertex_normals_ex(const rxg_mesh* h, int32_t weighting, const float* xyz, float* out,
+                                 int32_t flags, void* stream)
+{
+    if (flags & ~(RXG_HOST_ASYNC | RXG_HOST_DIRECT)) {
+        set_error("rxg_vertex_normals_ex: unknown flags %d", flags);
+        return RXG_ERR_INVALID;
+    }
+    if (!flags || !h || !xyz || !out || (weighting != RXG_NORMAL_MAX && weighting != RXG_NORMAL_AREA) ||
+        is_device_ptr(out))
+        return rxg_vertex_normals(h, weighting, xyz, out, stream);
+    cudaStream_t s     = (cudaStream_t)stream;
+    const size_t bytes = (size_t)h->m.nv * 12;
+    if (flags & RXG_HOST_DIRECT) {
+        const float* dx = is_device_ptr(xyz) ? xyz : (const float*)host_mapped(const_cast<float*>(xyz));
+        float*       dn = (float*)host_mapped(out);
+        if (dx && dn) return launch_normals(&h->m, weighting, dx, dn, s, PatchRange{0, h->m.num_patches});
+    }
+    if (!is_pinned_host(out) || !(is_device_ptr(xyz) || is_pinned_host(xyz)))
+        return rxg_vertex_normals(h, weighting, xyz, out, stream);
+    Staged     si, so;
+    rxg_status st;
+    if ((st = stage_in(xyz, bytes, s, si))) return st;  // stream-ordered upload
+    if ((st = stage_out(out, bytes, s, so))) return st;
+    if ((st = launch_normals(&h->m, weighting, (const float*)si.d, (float*)so.d, s,
+                             PatchRange{0, h->m.num_patches})))
+        return st;
+    RXG_CUDA_TRY(cudaMemcpyAsync(out, so.d, bytes, cudaMemcpyDeviceToHost, s));
+    return RXG_OK;
 }
 
 // Syncs `stream`, reads and clears the device error word set by bounded waits.

@@ -179,6 +179,7 @@ int main(int argc, char** argv)
         run_op<Op::EV, EdgeHandle, VertexHandle, 2>(rx, dir, "ev");
         run_op<Op::EF, EdgeHandle, FaceHandle, 8>(rx, dir, "ef");
         run_op<Op::EVDiamond, EdgeHandle, VertexHandle, 4>(rx, dir, "evd");
+        run_op<Op::EE, EdgeHandle, EdgeHandle, 4>(rx, dir, "ee");
 
         // attributes through handles: the umbrella operator
         // sum_{u in VV(v)} (x_u - x_v) on the input coordinates

@@ -109,6 +109,7 @@ def decode(rx):
     ff = [None] * nf
     feq = np.full((nf, 3), -1, np.int64)
     evd = np.full((ne, 4), -2, np.int64)
+    ee = np.full((ne, 4), -2, np.int64)
     for h in hdr:
         nVo, nVl, nEo, nEl, nFo, nFl, vb, eb, fb, vvb, vfb, evo, feo, rvo, reo, rfo = h.tolist()
         ev = arena[evo:evo + nEl]
@@ -139,6 +140,13 @@ def decode(rx):
             for f, k in zip(*np.nonzero(fel == e)):
                 d[1 + 2 * int(fe[f, k] & 1)] = int(linv(np.array([fvl[f, (k + 2) % 3]]))[0])
             evd[eb + e] = d
+            # EE: per direction bit of FE, that face's next and previous edge
+            q = [-1, -1, -1, -1]
+            for f, k in zip(*np.nonzero(fel == e)):
+                dd = 2 * int(fe[f, k] & 1)
+                q[dd] = int(line(np.array([fel[f, (k + 1) % 3]]))[0])
+                q[dd + 1] = int(line(np.array([fel[f, (k + 2) % 3]]))[0])
+            ee[eb + e] = q
         for f in range(nFo):
             nb = set()
             for k in range(3):
@@ -146,7 +154,7 @@ def decode(rx):
             nb.discard(f)
             ff[fb + f] = sorted(linf(np.array(sorted(nb), np.int64)).tolist()) if nb else []
             feq[fb + f] = line(fel[f])
-    return vv, ve, vf, fvq, evq, ef, ff, feq, evd
+    return vv, ve, vf, fvq, evq, ef, ff, feq, evd, ee
 
 
 MESHES = {
@@ -246,7 +254,7 @@ def check_layout(oracle, rx, fv, nv, patch):
         assert np.array_equal(np.sort(m), np.arange(n))
     hdr, _ = rx.patches()
     assert (hdr[:, 4] <= patch).all()
-    vv, ve, vf, fvq, evq, ef, ff, feq, evd = decode(rx)
+    vv, ve, vf, fvq, evq, ef, ff, feq, evd, ee = decode(rx)
     off, val = oracle.vv(nv, ev_ref)
     want = sorted_rows(off, val)
     got = [None] * nv
@@ -285,11 +293,7 @@ def check_layout(oracle, rx, fv, nv, patch):
     if rx.info["is_edge_manifold"] and oriented:
         d = np.where(evd >= 0, vl[np.maximum(evd, 0)], -1)[np.argsort(el)]
         assert np.array_equal(d, oracle.ev_diamond(fv))
-        # EE composed from the FV / FE / EV rows (the same torch code the GPU runs)
-        import torch
-        from rxmesh_gb300 import edge_edge_slots
-        ee = edge_edge_slots(torch.from_numpy(fvq), torch.from_numpy(feq), torch.from_numpy(evq),
-                             ne).numpy().reshape(-1, 4)
+        # EE: the GPU kernel's slot rule over the same patch slices
         got = np.where(ee >= 0, el[np.maximum(ee, 0)], -1)[np.argsort(el)]
         assert np.array_equal(got, oracle.ee(fv))
 

@@ -9,7 +9,7 @@ Query<blockThreads> (dispatch with an active-set predicate and
 compute_vertex_valence; prologue / run_compute / epilogue).  It writes its
 results to binary files; this test compares them with the oracle in input
 ids: rows as sorted sets (the form of tests/RXMesh_test/rxmesh_test.h:
-347-440), FV / FE / EV / EVDiamond rows and the oriented ring in order.
+347-440), FV / FE / EV / EVDiamond / EE rows and the oriented ring in order.
 The program compiles here (nvcc cross-compiles without a GPU); it runs on
 the GPU.
 """
@@ -132,6 +132,12 @@ def test_for_each_matches_oracle(oracle, example, tmp_path, name):
         got = np.empty((ne, 4), np.int64)
         got[l2i[1]] = np.where(val >= 0, l2i[0][np.maximum(val, 0)], -1)
         assert np.array_equal(got, oracle.ev_diamond(f))
+        cnt = load(d, "ee_cnt")
+        val = load(d, "ee_val").reshape(-1, 4)
+        assert (cnt == 4).all()
+        got = np.empty((ne, 4), np.int64)
+        got[l2i[1]] = np.where(val >= 0, l2i[1][np.maximum(val, 0)], -1)
+        assert np.array_equal(got, oracle.ee(f))
         # oriented VV: the oracle's rotational order (cyclic for interior vertices)
         o_off, o_ring, o_bnd = oracle.oriented_vv(nv, f)
         cnt = load(d, "vvo_cnt")

@@ -109,7 +109,7 @@ def test_torus1024_normals(oracle, torus1024, weighting):
 
 
 def test_torus1024_edge_face_queries_bit_exact(oracle, torus1024):
-    """EF, FF as sets; FE and EVDiamond in order, on the full torus."""
+    """EF, FF as sets; FE, EVDiamond and EE in order, on the full torus."""
     from rxmesh_gb300 import Op
     x, f, rx = torus1024
     vl, el, fl = rx.linear_to_input("v"), rx.linear_to_input("e"), rx.linear_to_input("f")
@@ -125,6 +125,9 @@ def test_torus1024_edge_face_queries_bit_exact(oracle, torus1024):
     dq = dq.cpu().numpy().reshape(-1, 4)
     din = np.where(dq >= 0, vl[np.maximum(dq, 0)], -1)[np.argsort(el)]
     assert np.array_equal(din, oracle.ev_diamond(f))
+    _, eq = rx.query(Op.EE)
+    eq = eq.cpu().numpy().reshape(-1, 4)
+    assert np.array_equal(np.where(eq >= 0, el[np.maximum(eq, 0)], -1)[np.argsort(el)], oracle.ee(f))
 
 
 # --------------------------------------------------------------------------

@@ -118,6 +118,9 @@ def test_edge_and_face_queries_bit_exact(oracle, name, patch, tmp_path):
     dq = dq.cpu().numpy().reshape(-1, 4)
     din = np.where(dq >= 0, vl[np.maximum(dq, 0)], -1)[np.argsort(el)]
     assert np.array_equal(din, oracle.ev_diamond(f))
+    _, eq = rx.query(Op.EE)
+    eq = eq.cpu().numpy().reshape(-1, 4)
+    assert np.array_equal(np.where(eq >= 0, el[np.maximum(eq, 0)], -1)[np.argsort(el)], oracle.ee(f))
     device_check()
 
 
@@ -150,7 +153,7 @@ def test_query_into_host_buffers(oracle, level, patch):
     from rxmesh_gb300 import Op, RXMeshStatic, _lib
     x, f = meshgen.icosphere(level)
     rx = RXMeshStatic(f, len(x), patch_size=patch)
-    for op in (Op.VV, Op.VE, Op.VF, Op.FV, Op.EV, Op.EF, Op.FE, Op.FF, Op.EVD):
+    for op in (Op.VV, Op.VE, Op.VF, Op.FV, Op.EV, Op.EF, Op.FE, Op.FF, Op.EVD, Op.EE):
         rows, nval = rx.query_size(op)
         csr = op in Op.CSR
         off = np.full(rows + 1, -7, np.int32) if csr else None
@@ -182,7 +185,7 @@ def test_query_into_pinned_host_buffers(oracle, level, patch):
     L = _lib.load()
     x, f = meshgen.icosphere(level)
     rx = RXMeshStatic(f, len(x), patch_size=patch)
-    for op in (Op.VV, Op.VE, Op.VF, Op.FV, Op.EV, Op.EF, Op.FE, Op.FF, Op.EVD):
+    for op in (Op.VV, Op.VE, Op.VF, Op.FV, Op.EV, Op.EF, Op.FE, Op.FF, Op.EVD, Op.EE):
         rows, nval = rx.query_size(op)
         csr = op in Op.CSR
         d_off, d_val = rx.query(op)
@@ -212,6 +215,61 @@ def test_query_into_pinned_host_buffers(oracle, level, patch):
         _lib.check(L.rxg_vertex_normals(rx._h, 0, ctypes.c_void_p(xin.data_ptr()),
                                         ctypes.c_void_p(out.data_ptr()), None))
         assert torch.equal(out, dev), pin_in
+
+
+@pytest.mark.parametrize("flags", [1, 2, 3])
+def test_query_ex_stream_ordered(flags):
+    """rxg_query_ex / rxg_vertex_normals_ex with RXG_HOST_ASYNC (1),
+    RXG_HOST_DIRECT (2) or both: every op issued on its own stream before
+    any of them is waited for, page-locked (and device-offset / pageable)
+    outputs; after the streams complete the host arrays equal the device
+    results (row sets for CSR rows, bit for bit otherwise)."""
+    import ctypes
+    from rxmesh_gb300 import Op, RXGError, RXMeshStatic, _lib
+    L = _lib.load()
+    x, f = meshgen.icosphere(5)
+    rx = RXMeshStatic(f, len(x), patch_size=128)
+    ops = (Op.VV, Op.VE, Op.VF, Op.FV, Op.EV, Op.EF, Op.FE, Op.FF, Op.EVD, Op.EE)
+    cases = []
+    for op in ops:
+        rows, nval = rx.query_size(op)
+        csr = op in Op.CSR
+        for kind in ("pinned", "device_offsets", "pageable"):
+            if kind == "device_offsets" and not csr:
+                continue
+            off = None
+            if csr:
+                off = torch.full((rows + 1,), -7, dtype=torch.int32,
+                                 device="cuda" if kind == "device_offsets" else "cpu")
+                off = off.pin_memory() if kind == "pinned" else off
+            val = torch.full((nval,), -7, dtype=torch.int32)
+            val = val if kind == "pageable" else val.pin_memory()
+            cases.append((op, kind, off, val, torch.cuda.Stream()))
+    x32 = rx.to_linear(torch.tensor(x, device="cuda")).float()
+    xin = x32.cpu().pin_memory()
+    nrm = torch.full_like(xin, float("nan")).pin_memory()
+    ns = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    for op, kind, off, val, s in cases:
+        _lib.check(L.rxg_query_ex(rx._h, int(op), ctypes.c_void_p(off.data_ptr()) if off is not None else None,
+                                  ctypes.c_void_p(val.data_ptr()), flags, ctypes.c_void_p(s.cuda_stream)))
+    _lib.check(L.rxg_vertex_normals_ex(rx._h, 1, ctypes.c_void_p(xin.data_ptr()),
+                                       ctypes.c_void_p(nrm.data_ptr()), flags, ctypes.c_void_p(ns.cuda_stream)))
+    torch.cuda.synchronize()
+    for op, kind, off, val, s in cases:
+        d_off, d_val = rx.query(op)
+        if off is not None:
+            assert torch.equal(off.cpu(), d_off.cpu()), (op, kind)
+            o = off.cpu().numpy()
+            assert sorted_rows(o, val.numpy()) == sorted_rows(o, d_val.cpu().numpy()), (op, kind)
+        else:
+            assert torch.equal(val, d_val.cpu()), (op, kind)
+    assert torch.equal(nrm, rx.vertex_normals(x32, "area").cpu())
+    val = torch.empty(rx.query_size(Op.VV)[1], dtype=torch.int32).pin_memory()
+    off = torch.empty(rx.query_size(Op.VV)[0] + 1, dtype=torch.int32).pin_memory()
+    with pytest.raises(RXGError):
+        _lib.check(L.rxg_query_ex(rx._h, int(Op.VV), ctypes.c_void_p(off.data_ptr()),
+                                  ctypes.c_void_p(val.data_ptr()), 4, None))
 
 
 @pytest.mark.parametrize("name,patch", [(n, 256) for n in ("sphere3", "torus", "cloth", "bunnyhead")]
@@ -302,9 +360,9 @@ def test_boundary_vertices_device():
 
 @pytest.mark.parametrize("name", ["torus64", "icosphere4", "plane", "sphere3", "plane_5"])
 def test_edge_edge_query(oracle, name):
-    """Op.EE (e_e_manifold, rxmesh_queries.cuh:269-340) on the GPU, composed
-    from the FV / FE / EV queries, against the oracle; refused on a mesh
-    whose faces are not consistently oriented."""
+    """Op.EE (e_e_manifold, rxmesh_queries.cuh:269-340) on the GPU
+    (k_query_elem<RXG_OP_EE>) against the oracle, also into host arrays;
+    refused on a mesh whose faces are not consistently oriented."""
     from rxmesh_gb300 import Op, RXGError, RXMeshStatic
     x, f = MESHES[name]()
     rx = RXMeshStatic(f, len(x), patch_size=64)
@@ -314,6 +372,9 @@ def test_edge_edge_query(oracle, name):
     ee = ee.cpu().numpy().reshape(-1, 4)
     got = np.where(ee >= 0, el[np.maximum(ee, 0)], -1)[np.argsort(el)]
     assert np.array_equal(got, oracle.ee(f))
+    host = np.full(4 * rx.get_num_edges(), -7, np.int32)
+    rx.query_host(Op.EE, None, host)
+    assert np.array_equal(host.reshape(-1, 4), ee)
     g = np.array(f, np.int32).copy()
     g[3] = g[3][::-1]
     with pytest.raises(RXGError):
