@@ -453,6 +453,7 @@ struct CGArgs
     // [diagonal, oriented ring] pattern, FP64 positions, the time step
     const int8_t*  mf_bnd;
     const double*  mf_xyz;
+    const float*   mf_xyzf;  // the positions rounded to FP32 (T = float)
     double         mf_dt;
     int            mf_uniform;
 };
@@ -524,13 +525,17 @@ __device__ __forceinline__ void row_spmv_group(const int32_t* __restrict__ rp,
 // mode: weight 1 per neighbour and the valence as the vertex weight):
 // acc += sum_j A_pj x_j over the row, diag (may be null) = A_pp.  rp/col
 // is the [diagonal, oriented ring] pattern; the arithmetic and its order
-// are k_mcf_assemble's, so a product equals the assembled matrix's.
-template <typename T, typename G, int NC>
+// are k_mcf_assemble's, so a product equals the assembled matrix's.  PT:
+// the positions' type, double, or float (the FP64 positions rounded once per
+// call or solve, the same values the FP32 arithmetic would convert them to)
+// when T is float, so that no conversion runs on the FP64 pipe per row.
+template <typename T, typename G, int NC, typename PT>
 __device__ __forceinline__ void mcf_row(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
-                                        const int8_t* __restrict__ bnd, const double* __restrict__ xyz,
+                                        const int8_t* __restrict__ bnd, const PT* __restrict__ xyz,
                                         T dt, bool uniform, int64_t p, const T* x, T* acc, T* diag)
 {
     static_assert(std::is_same<G, Geo<T>>::value, "the matrix-free row uses the exact-type geometry");
+    static_assert(std::is_same<PT, double>::value || std::is_same<PT, T>::value, "positions: FP64 or T");
     const int32_t  rp   = __ldg(row_ptr + p);
     const int32_t  k    = __ldg(row_ptr + p + 1) - rp - 1;
     const int32_t* rg   = col + rp + 1;
@@ -549,10 +554,10 @@ __device__ __forceinline__ void mcf_row(const int32_t* __restrict__ row_ptr, con
         // all ids, then all positions and x rows, in flight together; each
         // fan triangle evaluated once (fan_row, bit for bit the per-call
         // values of the general loop below)
-        const V3<double> P = ld3(xyz, (int32_t)p);
-        int32_t          id[8];
-        V3<double>       X[8];
-        T                xv[8][NC];
+        const V3<PT> P = ld3(xyz, (int32_t)p);
+        int32_t      id[8];
+        V3<PT>       X[8];
+        T            xv[8][NC];
 #pragma unroll
         for (int i = 0; i < 8; ++i) id[i] = i < k ? __ldg(rg + i) : (int32_t)p;
 #pragma unroll
@@ -564,7 +569,7 @@ __device__ __forceinline__ void mcf_row(const int32_t* __restrict__ row_ptr, con
         area = fan_row<T, T>(
             P, k, wrap, dt,
             [&](int32_t i) {
-                V3<double> r = X[0];
+                V3<PT> r = X[0];
 #pragma unroll
                 for (int j = 1; j < 8; ++j)
                     if (j == i) r = X[j];
@@ -579,8 +584,8 @@ __device__ __forceinline__ void mcf_row(const int32_t* __restrict__ row_ptr, con
                         for (int c = 0; c < NC; ++c) acc[c] -= w * xv[j][c];
             });
     } else if (k > 0) {
-        const V3<double> P = ld3(xyz, (int32_t)p);
-        area               = fan_row<T, T>(
+        const V3<PT> P = ld3(xyz, (int32_t)p);
+        area           = fan_row<T, T>(
             P, k, wrap, dt, [&](int32_t i) { return ld3(xyz, __ldg(rg + i)); },
             [&](int32_t i, T w) {
                 sumw += w;
@@ -618,6 +623,18 @@ __device__ __forceinline__ bool cgm_sum(double v, double* s_part, GridSum& g, Re
     return grid_sum_staged<BT>(v, s_part, g, r, post);
 }
 
+// positions of the matrix-free operator: FP64, or their FP32 rounding for T = float
+template <typename T>
+struct MfPos
+{
+    __device__ static const double* get(const CGArgs<T>& a) { return a.mf_xyz; }
+};
+template <>
+struct MfPos<float>
+{
+    __device__ static const float* get(const CGArgs<float>& a) { return a.mf_xyzf; }
+};
+
 // L: lanes per matrix row in the two SpMV passes (1, or 4 for long rows).
 // MF: the operator is the matrix-free implicit-MCF one (mcf_row; a.rp and
 // a.col are the mesh's pattern, a.val is unused).
@@ -648,7 +665,7 @@ __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
         for (int k = 0; k < NC; ++k) acc[k] = T(0);
         T diag = T(0);
         if constexpr (MF)
-            mcf_row<T, Geo<T>, NC>(a.rp, a.col, a.mf_bnd, a.mf_xyz, (T)a.mf_dt, a.mf_uniform != 0, i,
+            mcf_row<T, Geo<T>, NC>(a.rp, a.col, a.mf_bnd, MfPos<T>::get(a), (T)a.mf_dt, a.mf_uniform != 0, i,
                                    a.X, acc, &diag);
         else if (L == 1) row_spmv<T, NC>(a.rp, a.col, a.val, i, a.X, acc, &diag);
         else row_spmv_group<T, NC, (L > 1 ? L : 2)>(a.rp, a.col, a.val, i, a.X, acc, &diag, lane);
@@ -691,7 +708,7 @@ __global__ void __launch_bounds__(kCGT) k_cg(CGArgs<T> a)
 #pragma unroll
             for (int k = 0; k < NC; ++k) acc[k] = T(0);
             if constexpr (MF)
-                mcf_row<T, Geo<T>, NC>(a.rp, a.col, a.mf_bnd, a.mf_xyz, (T)a.mf_dt, a.mf_uniform != 0,
+                mcf_row<T, Geo<T>, NC>(a.rp, a.col, a.mf_bnd, MfPos<T>::get(a), (T)a.mf_dt, a.mf_uniform != 0,
                                        i, src, acc, (T*)nullptr);
             else if (L == 1) row_spmv<T, NC>(a.rp, a.col, a.val, i, src, acc, (T*)nullptr);
             else row_spmv_group<T, NC, (L > 1 ? L : 2)>(a.rp, a.col, a.val, i, src, acc, (T*)nullptr, lane);
@@ -818,6 +835,7 @@ struct MatFreeOp
 {
     const int8_t* bnd     = nullptr;
     const double* xyz     = nullptr;
+    const float*  xyzf    = nullptr;  // FP32 rounding of xyz (T = float)
     double        dt      = 0.0;
     int           uniform = 0;
 };
@@ -832,6 +850,7 @@ static rxg_status cg_launch(int64_t n, int64_t nnz, const int32_t* rp, const int
     CGArgs<T>  a;
     a.mf_bnd     = mf.bnd;
     a.mf_xyz     = mf.xyz;
+    a.mf_xyzf    = mf.xyzf;
     a.mf_dt      = mf.dt;
     a.mf_uniform = mf.uniform;
     uint8_t*   q  = scratch;
@@ -1644,21 +1663,28 @@ namespace rxg {
 // ---------------------------------------------------------------------
 
 // out = A in (JACOBI: out = D^-1 in, D = diag(A)), row-major nv x 3
-template <typename T, bool JACOBI>
+template <typename T, bool JACOBI, typename PT>
 __global__ void __launch_bounds__(256) k_mcf_matvec(int64_t nv, const int32_t* __restrict__ rp,
                                                     const int32_t* __restrict__ col,
                                                     const int8_t* __restrict__ bnd,
-                                                    const double* __restrict__ xyz, T dt, int uniform,
+                                                    const PT* __restrict__ xyz, T dt, int uniform,
                                                     const T* __restrict__ in, T* __restrict__ out)
 {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nv;
          p += (int64_t)gridDim.x * blockDim.x) {
         T acc[3] = {T(0), T(0), T(0)};
         T dg     = T(0);
-        mcf_row<T, Geo<T>, 3>(rp, col, bnd, xyz, dt, uniform != 0, p, in, acc, &dg);
+        mcf_row<T, Geo<T>, 3, PT>(rp, col, bnd, xyz, dt, uniform != 0, p, in, acc, &dg);
 #pragma unroll
         for (int c = 0; c < 3; ++c) out[3 * p + c] = JACOBI ? in[3 * p + c] / dg : acc[c];
     }
+}
+
+// the FP32 rounding of n FP64 position triples
+__global__ void __launch_bounds__(256) k_round_f32(int64_t n3, const double* __restrict__ x, float* __restrict__ y)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n3; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = (float)__ldg(x + i);
 }
 
 // B = (1 / v_weight) x: 2 x (clamped Voronoi area) x in cotangent mode, the
@@ -1728,20 +1754,29 @@ rxg_status rxg_mcf_matvec(const rxg_mesh* h, double dt, int32_t flags, int32_t d
     const bool    jc = (flags & RXG_MCF_JACOBI) != 0;
     if (dtype == RXG_F64) {
         if (jc)
-            k_mcf_matvec<double, true><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, dt, u,
-                                                         (const double*)in, (double*)out);
+            k_mcf_matvec<double, true, double><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, dt, u,
+                                                                 (const double*)in, (double*)out);
         else
-            k_mcf_matvec<double, false><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, dt, u,
-                                                          (const double*)in, (double*)out);
-    } else {
-        if (jc)
-            k_mcf_matvec<float, true><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, (float)dt,
-                                                        u, (const float*)in, (float*)out);
-        else
-            k_mcf_matvec<float, false><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, (float)dt,
-                                                         u, (const float*)in, (float*)out);
+            k_mcf_matvec<double, false, double><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, dt, u,
+                                                                  (const double*)in, (double*)out);
+        RXG_CUDA_TRY(cudaGetLastError());
+        return RXG_OK;
     }
-    RXG_CUDA_TRY(cudaGetLastError());
+    // FP32: the positions rounded once (k_round_f32), not per row
+    float* xf = nullptr;
+    if (!u) {
+        RXG_CUDA_TRY(scratch_alloc((void**)&xf, sizeof(float) * 3 * (size_t)nv, s));
+        k_round_f32<<<grid_for(3 * nv), 256, 0, s>>>(3 * nv, xyz, xf);
+    }
+    if (jc)
+        k_mcf_matvec<float, true, float><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xf, (float)dt, u,
+                                                           (const float*)in, (float*)out);
+    else
+        k_mcf_matvec<float, false, float><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xf, (float)dt, u,
+                                                            (const float*)in, (float*)out);
+    const cudaError_t e = cudaGetLastError();
+    if (xf) cudaFreeAsync(xf, s);
+    RXG_CUDA_TRY(e);
     return RXG_OK;
 }
 
@@ -1805,8 +1840,14 @@ rxg_status rxg_mcf_solve_matfree(const rxg_mesh* h, double dt, int32_t flags, in
                 : cg_launch<double, 3, false, true>(n, z->nnz, z->row_ptr, z->col, nullptr, (const double*)B,
                                                     (double*)X, *opts, &local, scratch, s, mf);
     } else {
-        const int G = pc ? cg_grid<float, 3, true, true>(n) : cg_grid<float, 3, false, true>(n);
-        RXG_CUDA_TRY(scratch_alloc((void**)&scratch, cg_scratch_bytes<float>(n, 3, G), s));
+        const int    G  = pc ? cg_grid<float, 3, true, true>(n) : cg_grid<float, 3, false, true>(n);
+        const size_t sb = cg_scratch_bytes<float>(n, 3, G);
+        // the CG scratch, then the positions rounded to FP32 once per solve
+        RXG_CUDA_TRY(scratch_alloc((void**)&scratch, sb + sizeof(float) * 3 * (size_t)n, s));
+        float* xf = reinterpret_cast<float*>(scratch + sb);
+        k_round_f32<<<grid_for(3 * n), 256, 0, s>>>(3 * n, xyz, xf);
+        RXG_CUDA_TRY(cudaGetLastError());
+        mf.xyzf = xf;
         st = pc ? cg_launch<float, 3, true, true>(n, z->nnz, z->row_ptr, z->col, nullptr, (const float*)B,
                                                   (float*)X, *opts, &local, scratch, s, mf)
                 : cg_launch<float, 3, false, true>(n, z->nnz, z->row_ptr, z->col, nullptr, (const float*)B,

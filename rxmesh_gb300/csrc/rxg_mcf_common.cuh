@@ -111,8 +111,8 @@ __device__ __forceinline__ TriTerms<T> tri_terms(V3<T> p, V3<T> a, V3<T> b)
     return {ha, hb, va};
 }
 
-template <typename T>
-__device__ __forceinline__ V3<T> to_t(V3<double> a)
+template <typename T, typename S>
+__device__ __forceinline__ V3<T> to_t(V3<S> a)
 {
     return {(T)a.x, (T)a.y, (T)a.z};
 }
@@ -121,10 +121,11 @@ __device__ __forceinline__ V3<T> to_t(V3<double> a)
 // (tri_terms): calls on_w(i, w_i) for ring entries i = 0..k-1 in order, w_i
 // = max(0, cot-halves) * dt as the per-call loop forms it (Q half first,
 // then S half), and returns the sum of the clamped Voronoi terms in the same
-// order.  pos(i): the position (V3<double>) of ring entry i.  wrap: a closed
-// fan (interior vertex); an open fan has no triangle (p, r_{k-1}, r_0).
-template <typename T, typename TB, typename Pos, typename OnW>
-__device__ __forceinline__ TB fan_row(V3<double> Pd, int32_t k, bool wrap, T dt, Pos pos, OnW on_w)
+// order.  pos(i): the position (V3<double>, or V3<float> already rounded
+// when T is float) of ring entry i.  wrap: a closed fan (interior vertex);
+// an open fan has no triangle (p, r_{k-1}, r_0).
+template <typename T, typename TB, typename PP, typename Pos, typename OnW>
+__device__ __forceinline__ TB fan_row(V3<PP> Pd, int32_t k, bool wrap, T dt, Pos pos, OnW on_w)
 {
     TB area = TB(0);
     if (k <= 0) return area;
@@ -232,6 +233,10 @@ struct GeoMixed
 };
 
 __device__ __forceinline__ V3<double> ld3(const double* __restrict__ x, int32_t i)
+{
+    return {__ldg(x + 3 * (int64_t)i), __ldg(x + 3 * (int64_t)i + 1), __ldg(x + 3 * (int64_t)i + 2)};
+}
+__device__ __forceinline__ V3<float> ld3(const float* __restrict__ x, int32_t i)
 {
     return {__ldg(x + 3 * (int64_t)i), __ldg(x + 3 * (int64_t)i + 1), __ldg(x + 3 * (int64_t)i + 2)};
 }

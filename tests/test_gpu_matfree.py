@@ -89,6 +89,28 @@ def test_solve_matfree_residual(precond):
     assert np.linalg.norm(r) <= 1e-8 * np.linalg.norm(B.cpu().numpy())
 
 
+def test_solve_matfree_fp32():
+    """The FP32 operator (positions rounded to FP32 once per call or solve):
+    a product with FP64 positions equals the product with the same positions
+    pre-rounded to FP32, bit for bit; the FP32 PCG converges and its solution
+    satisfies the FP64 assembled system to FP32 accuracy."""
+    from rxmesh_gb300 import RXMeshStatic, mcf_init_b, mcf_matvec, mcf_solve_matfree
+    from rxmesh_gb300._solvers import mcf_assemble
+    v, f = meshgen.icosphere(5)
+    x = meshgen.radial_noise(v, 0.02, 4)
+    rx = RXMeshStatic(f, len(x), patch_size=256)
+    xl = rx.to_linear(torch.tensor(x, device="cuda"))
+    u = torch.randn_like(xl).float()
+    assert torch.equal(mcf_matvec(rx, xl, u, 0.01), mcf_matvec(rx, xl.float().double(), u, 0.01))
+    B = mcf_init_b(rx, xl)
+    X = xl.float().clone()
+    st = mcf_solve_matfree(rx, xl, B.float(), X, 0.01, max_iter=2000, rel_tol=1e-8, precond=True)
+    assert st["converged"], st
+    A, _ = mcf_assemble(rx, xl, 0.01, torch.float64)
+    r = A.to_scipy() @ X.double().cpu().numpy() - B.cpu().numpy()
+    assert np.linalg.norm(r) <= 1e-3 * np.linalg.norm(B.cpu().numpy())
+
+
 def test_step_matfree_matches_assembled_step_and_oracle(oracle):
     """Three matrix-free MCF steps equal three assembled FP64 steps (the same
     Jacobi PCG and stopping rule) and the oracle's steps."""
