@@ -91,8 +91,11 @@ __host__ __device__ __forceinline__ int32_t pad4i(int32_t n) { return (n + 3) & 
 // Exclusive scan of s[0..n) in place, returns the total.  256-thread blocks.
 // Each thread scans a contiguous chunk, warps combine chunk totals with
 // shuffles, and warp totals go through shared memory.  Deterministic.
+// out (may be null): also written out[i] = base + the exclusive prefix of
+// element i, in the same pass (CSR row offsets).
 template <int BT>
-__device__ __forceinline__ int32_t block_exclusive_scan(int32_t* s, int32_t n, int32_t* s_warp)
+__device__ __forceinline__ int32_t block_exclusive_scan(int32_t* s, int32_t n, int32_t* s_warp,
+                                                        int32_t* __restrict__ out = nullptr, int32_t base = 0)
 {
     const int tid   = threadIdx.x;
     const int chunk = (n + BT - 1) / BT;
@@ -121,10 +124,19 @@ __device__ __forceinline__ int32_t block_exclusive_scan(int32_t* s, int32_t n, i
     __syncthreads();
     int32_t run   = x - sum + (warp > 0 ? s_warp[warp - 1] : 0);
     int32_t total = s_warp[BT / 32 - 1];
-    for (int i = beg; i < end; ++i) {
-        int32_t v = s[i];
-        s[i]      = run;
-        run += v;
+    if (out) {
+        for (int i = beg; i < end; ++i) {
+            int32_t v = s[i];
+            s[i]      = run;
+            out[i]    = base + run;
+            run += v;
+        }
+    } else {
+        for (int i = beg; i < end; ++i) {
+            int32_t v = s[i];
+            s[i]      = run;
+            run += v;
+        }
     }
     __syncthreads();
     return total;
