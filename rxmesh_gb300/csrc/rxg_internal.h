@@ -82,10 +82,11 @@ struct Mesh
     std::vector<PatchHdr> hdr;
     std::vector<uint32_t> arena;
     // Per patch p, words [nrm_off[p], nrm_off[p+1]) of nrm (16-byte aligned):
-    // local face -> 3 local vertex ids (u16 triples, pad4 words), offsets of
-    // the owned vertices' incident-face lists (u32 x nVo+1, pad4), and the
-    // lists themselves (u16 local face ids, pad4).  Static topology, built
-    // once with the patches.
+    // offsets of the owned vertices' incidence lists (u32 x nVo+1, pad4) and
+    // the lists (pad4): one word per incident face (input VF order), the
+    // face's other two corners after the vertex in the face's cyclic order,
+    // local vertex ids a | b << 16.  Static topology, built once with the
+    // patches.
     std::vector<uint32_t> nrm;
     std::vector<int32_t>  nrm_off;
     // first EF / FF value of each patch's owned rows (np+1 each; the last

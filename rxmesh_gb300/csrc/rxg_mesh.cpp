@@ -399,14 +399,13 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
     for (int64_t i = 0; i < nf; ++i) M.f_i2l[M.f_l2i[i]] = (int32_t)i;
 
     // ---- per-patch local topology ---------------------------------------
-    std::vector<int32_t> vstamp(nv, -1), vloc(nv), estamp(ne, -1), eloc(ne), fstamp(nf, -1),
-        floc(nf);
+    std::vector<int32_t> vstamp(nv, -1), vloc(nv), estamp(ne, -1), eloc(ne), fstamp(nf, -1);
     std::vector<int32_t> lf, lv, le;
     M.hdr.resize(np);
     M.arena.clear();
     M.arena.reserve((size_t)(ne * 1.4 + nf * 2.2 + nv * 0.6) + 64 * (size_t)np);
     M.nrm.clear();
-    M.nrm.reserve((size_t)(nf * 2.0 + nv * 1.6) + 16 * (size_t)np);
+    M.nrm.reserve((size_t)(nf * 3.0 + nv * 1.2) + 16 * (size_t)np);
     M.nrm_off.assign((size_t)np + 1, 0);
     int64_t vv_acc = 0, vf_acc = 0, ef_acc = 0, ff_acc = 0;
     M.ef_base.assign((size_t)np + 1, 0);
@@ -544,27 +543,27 @@ static rxg_status build_host(Mesh& M, const int32_t* fv, int64_t nf, int64_t nv,
                 }
             }
         }
-        // vertex-normal incidence block: local FV, then the owned vertices'
-        // incident local faces (input VF order) behind 32-bit offsets
+        // vertex-normal incidence block: per owned vertex (input VF order)
+        // its incident faces' two other corners in the face's cyclic order
+        // (the corner after it, then the one before), as local vertex ids
+        // packed a | b << 16, behind 32-bit offsets
         {
-            for (int32_t i = 0; i < nFl; ++i) floc[lf[i]] = i;
-            const size_t  b0    = M.nrm.size();
-            const int32_t fvw   = pad4((3 * nFl + 1) / 2);
-            const int32_t offw  = pad4(nVo + 1);
-            int64_t       ninc  = 0;
+            const size_t  b0   = M.nrm.size();
+            const int32_t offw = pad4(nVo + 1);
+            int64_t       ninc = 0;
             for (int32_t i = 0; i < nVo; ++i) ninc += vf_off[lv[i] + 1] - vf_off[lv[i]];
-            const int32_t incw  = pad4((int32_t)((ninc + 1) / 2));
-            M.nrm.resize(b0 + fvw + offw + incw, 0u);
-            uint16_t* fv16 = reinterpret_cast<uint16_t*>(M.nrm.data() + b0);
-            for (int32_t i = 0; i < nFl; ++i)
-                for (int k = 0; k < 3; ++k) fv16[3 * i + k] = (uint16_t)vloc[fv[3 * lf[i] + k]];
-            uint32_t* off   = M.nrm.data() + b0 + fvw;
-            uint16_t* inc16 = reinterpret_cast<uint16_t*>(off + offw);
-            uint32_t  j     = 0;
+            const int32_t incw = pad4((int32_t)ninc);
+            M.nrm.resize(b0 + offw + incw, 0u);
+            uint32_t* off = M.nrm.data() + b0;
+            uint32_t* vis = off + offw;
+            uint32_t  j   = 0;
             for (int32_t i = 0; i < nVo; ++i) {
                 off[i] = j;
-                for (int32_t t = vf_off[lv[i]]; t < vf_off[lv[i] + 1]; ++t)
-                    inc16[j++] = (uint16_t)floc[vf_val[t]];
+                for (int32_t t = vf_off[lv[i]]; t < vf_off[lv[i] + 1]; ++t) {
+                    const int32_t* c = fv + 3 * (int64_t)vf_val[t];
+                    const int      k = c[0] == lv[i] ? 0 : (c[1] == lv[i] ? 1 : 2);
+                    vis[j++] = (uint32_t)vloc[c[(k + 1) % 3]] | ((uint32_t)vloc[c[(k + 2) % 3]] << 16);
+                }
             }
             off[nVo] = j;
             if (M.nrm.size() > (size_t)INT32_MAX) {

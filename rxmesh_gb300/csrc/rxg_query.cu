@@ -582,14 +582,16 @@ __global__ void __launch_bounds__(kQT) k_query_ff(const PatchHdr* __restrict__ h
 }
 
 // ---------------------------------------------------------------------
-// Vertex normals: per patch, each owned vertex sums the normals of
-// its incident faces (owned and ribbon), listed in the patch's incidence
-// block, which the static topology builds once: no shared-memory float
-// atomics, and a fixed summation order (input VF order), so the result is
-// deterministic.  Each face normal is formed from the face's corners in
-// their input order, the arithmetic of a per-face scatter, so every
-// contribution is the same float as in a face-centred kernel.
-// Formula of compute_vertex_normal (apps/VertexNormal/vertex_normal_kernel.cuh:10-43).
+// Vertex normals: per patch, each owned vertex sums the normals of its
+// incident faces (owned and ribbon) in input VF order, reading the patch's
+// incidence block (static topology: per incident face the two other
+// corners, in the face's cyclic order after the vertex): no atomics, a fixed
+// summation order, so the result is deterministic.  Each face normal is
+// formed with the vertex as the first corner, cross(a - v, b - v): the same
+// vector as from the face's input corner order (a cyclic rotation), within
+// FP32 rounding.  Max weights divide it by |v - a|^2 + |b - v|^2, the two
+// edges at the corner.  Formula of compute_vertex_normal
+// (apps/VertexNormal/vertex_normal_kernel.cuh:10-43).
 // ---------------------------------------------------------------------
 
 template <int W, int kQT>
@@ -607,11 +609,9 @@ __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restri
     const int32_t  nVo   = h.nVo, nVr = h.nVl - h.nVo;
     const int32_t  b0    = __ldg(nrm_off + blockIdx.x);
     const int32_t  words = __ldg(nrm_off + blockIdx.x + 1) - b0;  // > 0, multiple of 4
-    uint32_t*       s_blk = smem;
-    const uint16_t* s_fv  = reinterpret_cast<const uint16_t*>(s_blk);
-    const uint32_t* s_off = s_blk + pad4i((int32_t)fe_words(h.nFl));
-    const uint16_t* s_inc = reinterpret_cast<const uint16_t*>(s_off + pad4i(nVo + 1));
-    float4*         s_pos = reinterpret_cast<float4*>(s_blk + words);
+    const uint32_t* s_off = smem;
+    const uint32_t* s_vis = smem + pad4i(nVo + 1);
+    float4*         s_pos = reinterpret_cast<float4*>(smem + words);
 
     if (threadIdx.x == 0) mbar_init(&bar, 1);
     __syncthreads();
@@ -620,7 +620,7 @@ __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restri
     // through the ribbon table read straight from global memory
     if (threadIdx.x == 0) {
         mbar_arrive_expect_tx(&bar, 4u * (uint32_t)words);
-        bulk_g2s(s_blk, nrm + b0, 4u * (uint32_t)words, &bar);
+        bulk_g2s(smem, nrm + b0, 4u * (uint32_t)words, &bar);
     }
     const float* xo = xyz + 3 * (int64_t)h.v_base;
     for (int i = threadIdx.x; i < nVo; i += kQT)
@@ -633,25 +633,18 @@ __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restri
 
     float* o = out + 3 * (int64_t)h.v_base;
     for (int v = threadIdx.x; v < nVo; v += kQT) {
+        const float4   P  = s_pos[v];
         float          a0 = 0.f, a1 = 0.f, a2 = 0.f;
         const uint32_t j1 = s_off[v + 1];
         for (uint32_t j = s_off[v]; j < j1; ++j) {
-            const uint32_t f  = s_inc[j];
-            const uint32_t i0 = s_fv[3 * f], i1 = s_fv[3 * f + 1], i2 = s_fv[3 * f + 2];
-            const float4   c0 = s_pos[i0], c1 = s_pos[i1], c2 = s_pos[i2];
-            const float3   u  = make_float3(c1.x - c0.x, c1.y - c0.y, c1.z - c0.z);
-            const float3   w  = make_float3(c2.x - c0.x, c2.y - c0.y, c2.z - c0.z);
-            const float    n0 = u.y * w.z - w.y * u.z, n1 = u.z * w.x - w.z * u.x,
-                        n2 = u.x * w.y - w.x * u.y;
+            const uint32_t q = s_vis[j];
+            const float4   A = s_pos[q & 0xffffu], B = s_pos[q >> 16];
+            const float3   u = make_float3(A.x - P.x, A.y - P.y, A.z - P.z);
+            const float3   w = make_float3(B.x - P.x, B.y - P.y, B.z - P.z);
+            const float    n0 = u.y * w.z - w.y * u.z, n1 = u.z * w.x - w.z * u.x, n2 = u.x * w.y - w.x * u.y;
             if (W == RXG_NORMAL_MAX) {
-                // corner k's two edges: l[k] = |c_k - c_k+1|^2 and l[k+2]
-                const float3 e0 = make_float3(c0.x - c1.x, c0.y - c1.y, c0.z - c1.z);
-                const float3 e1 = make_float3(c1.x - c2.x, c1.y - c2.y, c1.z - c2.z);
-                const float3 e2 = make_float3(c2.x - c0.x, c2.y - c0.y, c2.z - c0.z);
-                const float  l0 = e0.x * e0.x + e0.y * e0.y + e0.z * e0.z;
-                const float  l1 = e1.x * e1.x + e1.y * e1.y + e1.z * e1.z;
-                const float  l2 = e2.x * e2.x + e2.y * e2.y + e2.z * e2.z;
-                const float  d  = i0 == (uint32_t)v ? l0 + l2 : (i1 == (uint32_t)v ? l1 + l0 : l2 + l1);
+                // |v - a|^2 + |b - v|^2
+                const float d = (u.x * u.x + u.y * u.y + u.z * u.z) + (w.x * w.x + w.y * w.y + w.z * w.z);
                 a0 += n0 / d;
                 a1 += n1 / d;
                 a2 += n2 / d;
