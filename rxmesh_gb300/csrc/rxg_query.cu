@@ -359,32 +359,40 @@ __global__ void __launch_bounds__(kQT) k_query_elem(const PatchHdr* __restrict__
         // traversing v0->v1, v1, opposite vertex in the face traversing
         // v1->v0 (0xffff: no such face).  Local ids fit 16 bits with 0xffff
         // to spare (at most 65,535 local vertices).
-        uint16_t* slot = reinterpret_cast<uint16_t*>(s_rv + pad4i(nVr));
+        uint2* slot = reinterpret_cast<uint2*>(s_rv + pad4i(nVr));  // one per owned edge
         for (int e = threadIdx.x; e < h.nEo; e += kQT) {
             const uint32_t ev = s_ev[e];
-            slot[4 * e + 0]   = (uint16_t)(ev & 0xffffu);
-            slot[4 * e + 1]   = 0xffffu;
-            slot[4 * e + 2]   = (uint16_t)(ev >> 16);
-            slot[4 * e + 3]   = 0xffffu;
+            slot[e]           = make_uint2((ev & 0xffffu) | 0xffff0000u, (ev >> 16) | 0xffff0000u);
         }
         __syncthreads();
         // every local face names the vertex opposite each of its edges
         // (corner k+2 for edge k); on an edge-manifold mesh the two faces of
         // an edge traverse it in opposite directions, so each slot has one writer
-        for (int i = threadIdx.x; i < 3 * h.nFl; i += kQT) {
-            const uint32_t fe = fe16[i];
-            const uint32_t e  = fe >> 1;
-            if ((int32_t)e >= h.nEo) continue;
-            const int f = i / 3, k = i - 3 * f;
-            slot[4 * e + 1 + 2 * (fe & 1u)] = (uint16_t)face_vertex(fe16, s_ev, f, k == 0 ? 2 : k - 1);
+        uint16_t* s16 = reinterpret_cast<uint16_t*>(slot);
+        for (int f = threadIdx.x; f < h.nFl; f += kQT) {
+            const uint32_t c[3] = {fe16[3 * f], fe16[3 * f + 1], fe16[3 * f + 2]};
+            uint32_t       v[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t ev = s_ev[c[k] >> 1];
+                v[k]              = (c[k] & 1u) ? (ev >> 16) : (ev & 0xffffu);
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t e = c[k] >> 1;
+                if ((int32_t)e < h.nEo) s16[4 * e + 1 + 2 * (c[k] & 1u)] = (uint16_t)v[(k + 2) % 3];
+            }
         }
         __syncthreads();
-        const int32_t n    = 4 * h.nEo;
-        int32_t*      base = out_val + 4 * (int64_t)h.e_base;
-        for (int i = threadIdx.x; i < n; i += kQT) {
-            const uint32_t v = slot[i];
-            base[i] = v == 0xffffu ? -1
-                                   : ((int32_t)v < nVo ? h.v_base + (int32_t)v : (int32_t)s_rv[v - nVo]);
+        // one owned edge per thread: its four slots as one 16-byte store
+        const int32_t vb   = h.v_base;
+        auto          lin  = [=](uint32_t l) -> int32_t {
+            return l == 0xffffu ? -1 : ((int32_t)l < nVo ? vb + (int32_t)l : (int32_t)s_rv[l - nVo]);
+        };
+        int4* base = reinterpret_cast<int4*>(out_val + 4 * (int64_t)h.e_base);
+        for (int e = threadIdx.x; e < h.nEo; e += kQT) {
+            const uint2 w = slot[e];
+            base[e]       = make_int4(lin(w.x & 0xffffu), lin(w.x >> 16), lin(w.y & 0xffffu), lin(w.y >> 16));
         }
     } else if (EE) {
         // per owned edge two 32-bit slots of two 16-bit local edge ids: slot
@@ -395,23 +403,25 @@ __global__ void __launch_bounds__(kQT) k_query_elem(const PatchHdr* __restrict__
         uint32_t* slot = s_rv + pad4i(rib_n);
         for (int i = threadIdx.x; i < 2 * h.nEo; i += kQT) slot[i] = 0xffffffffu;
         __syncthreads();
-        for (int i = threadIdx.x; i < 3 * h.nFl; i += kQT) {
-            const uint32_t fe = fe16[i];
-            const uint32_t e  = fe >> 1;
-            if ((int32_t)e >= h.nEo) continue;
-            const int      f  = i / 3, k = i - 3 * f;
-            const uint32_t nx = (uint32_t)fe16[3 * f + (k == 2 ? 0 : k + 1)] >> 1;
-            const uint32_t pv = (uint32_t)fe16[3 * f + (k == 0 ? 2 : k - 1)] >> 1;
-            slot[2 * e + (fe & 1u)] = nx | (pv << 16);
+        for (int f = threadIdx.x; f < h.nFl; f += kQT) {
+            const uint32_t c[3] = {fe16[3 * f], fe16[3 * f + 1], fe16[3 * f + 2]};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t e = c[k] >> 1;
+                if ((int32_t)e < h.nEo) slot[2 * e + (c[k] & 1u)] = (c[(k + 1) % 3] >> 1) | ((c[(k + 2) % 3] >> 1) << 16);
+            }
         }
         __syncthreads();
-        const uint16_t* s16  = reinterpret_cast<const uint16_t*>(slot);
-        const int32_t   n    = 4 * h.nEo;
-        int32_t*        base = out_val + 4 * (int64_t)h.e_base;
-        for (int i = threadIdx.x; i < n; i += kQT) {
-            const uint32_t e = s16[i];
-            base[i] = e == 0xffffu ? -1
-                                   : ((int32_t)e < h.nEo ? h.e_base + (int32_t)e : (int32_t)s_rv[e - h.nEo]);
+        // one owned edge per thread: its four slots as one 16-byte store
+        const int32_t eb  = h.e_base, nEo = h.nEo;
+        auto          lin = [=](uint32_t l) -> int32_t {
+            return l == 0xffffu ? -1 : ((int32_t)l < nEo ? eb + (int32_t)l : (int32_t)s_rv[l - nEo]);
+        };
+        const uint2* s2   = reinterpret_cast<const uint2*>(slot);
+        int4*        base = reinterpret_cast<int4*>(out_val + 4 * (int64_t)h.e_base);
+        for (int e = threadIdx.x; e < h.nEo; e += kQT) {
+            const uint2 w = s2[e];
+            base[e]       = make_int4(lin(w.x & 0xffffu), lin(w.x >> 16), lin(w.y & 0xffffu), lin(w.y >> 16));
         }
     } else if (OP == 3) {
         const int32_t n    = 3 * h.nFo;
@@ -589,8 +599,8 @@ __global__ void __launch_bounds__(kQT) k_query_ff(const PatchHdr* __restrict__ h
 // summation order, so the result is deterministic.  Each face normal is
 // formed with the vertex as the first corner, cross(a - v, b - v): the same
 // vector as from the face's input corner order (a cyclic rotation), within
-// FP32 rounding.  Max weights divide it by |v - a|^2 + |b - v|^2, the two
-// edges at the corner.  Formula of compute_vertex_normal
+// FP32 rounding.  Max weights scale it by 1 / (|v - a|^2 + |b - v|^2), the
+// two edges at the corner.  Formula of compute_vertex_normal
 // (apps/VertexNormal/vertex_normal_kernel.cuh:10-43).
 // ---------------------------------------------------------------------
 
@@ -643,11 +653,12 @@ __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restri
             const float3   w = make_float3(B.x - P.x, B.y - P.y, B.z - P.z);
             const float    n0 = u.y * w.z - w.y * u.z, n1 = u.z * w.x - w.z * u.x, n2 = u.x * w.y - w.x * u.y;
             if (W == RXG_NORMAL_MAX) {
-                // |v - a|^2 + |b - v|^2
-                const float d = (u.x * u.x + u.y * u.y + u.z * u.z) + (w.x * w.x + w.y * w.y + w.z * w.z);
-                a0 += n0 / d;
-                a1 += n1 / d;
-                a2 += n2 / d;
+                // n / (|v - a|^2 + |b - v|^2), one reciprocal for the three
+                // components
+                const float r = 1.f / ((u.x * u.x + u.y * u.y + u.z * u.z) + (w.x * w.x + w.y * w.y + w.z * w.z));
+                a0 += n0 * r;
+                a1 += n1 * r;
+                a2 += n2 * r;
             } else {
                 a0 += n0;
                 a1 += n1;
