@@ -901,31 +901,33 @@ __global__ void __launch_bounds__(BT) k_cg_matfree(MatFreeArgs<T> a)
 // ---------------------------------------------------------------------
 
 // scalar CSR of a DxD-block CSR: scalar row Di+a lists, block by block in
-// the block row's order, the D entries (Dj+0..D-1) of each block (i,j)
+// the block row's order, the D entries (Dj+0..D-1) of each block (i,j).
+// One warp per block row: the block row's D scalar rows are one contiguous
+// run of D*D*nb output entries, written by consecutive lanes.
 template <typename T, int D>
 __global__ void k_bcsr_expand(int64_t n, const int32_t* __restrict__ brp,
                               const int32_t* __restrict__ bcol, const T* __restrict__ bval,
                               int32_t* __restrict__ rp, int32_t* __restrict__ col,
                               T* __restrict__ val)
 {
-    constexpr int DD = D * D;
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < D * n;
-         r += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i  = r / D;
-        const int     a  = (int)(r - D * i);
-        const int32_t b0 = brp[i], nb = brp[i + 1] - b0;
-        const int64_t o  = DD * (int64_t)b0 + D * (int64_t)a * nb;
-        rp[r]            = (int32_t)o;
-        if (r == D * n - 1) rp[D * n] = DD * brp[n];
-        for (int32_t t = 0; t < nb; ++t) {
-            const int32_t j = bcol[b0 + t];
+    constexpr int DD     = D * D;
+    const int     lane   = (int)(threadIdx.x & 31);
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < n; i += nwarps) {
+        const int32_t b0 = __ldg(brp + i), nb = __ldg(brp + i + 1) - b0;
+        const int64_t o0 = DD * (int64_t)b0;  // first entry of scalar row Di
+        if (lane < D) rp[D * i + lane] = (int32_t)(o0 + (int64_t)D * lane * nb);
 #pragma unroll
-            for (int c = 0; c < D; ++c) {
-                col[o + D * t + c] = D * j + c;
-                val[o + D * t + c] = bval[DD * (int64_t)(b0 + t) + D * a + c];
+        for (int a = 0; a < D; ++a) {
+            const int64_t oa = o0 + (int64_t)D * a * nb;
+            for (int32_t r = lane; r < D * nb; r += 32) {
+                const int32_t t = r / D, c = r - t * D;
+                col[oa + r]     = D * __ldg(bcol + b0 + t) + c;
+                val[oa + r]     = bval[DD * (int64_t)(b0 + t) + D * a + c];
             }
         }
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0) rp[D * n] = DD * __ldg(brp + n);
 }
 
 // apply_bc of diff/newton_solver.h on the block form: a constrained block
@@ -1316,7 +1318,7 @@ rxg_status rxg_bcsr_to_csr(const rxg_bcsr* H, rxg_csr* out, void* stream)
     out->nnz       = (int64_t)D * D * H->nnzb;
     out->dtype     = H->dtype;
     if (H->n == 0) return RXG_OK;
-    const int g = grid_for_items(D * H->n);
+    const int g = grid_for_items(32 * H->n);  // one warp per block row
     if (H->dtype == RXG_F64) {
         if (D == 2)
             k_bcsr_expand<double, 2><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const double*)H->val,

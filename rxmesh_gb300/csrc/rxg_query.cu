@@ -236,9 +236,16 @@ __global__ void __launch_bounds__(kQT) k_query_vertex(const PatchHdr* __restrict
             for (int k = 0; k < 3; ++k) atomicAdd(slot((uint32_t)fe16[3 * f + k] >> 1), 1);
         }
     } else if (OP == 2) {
+        // each thread resolves its faces' corners once and leaves them in
+        // place of the faces' FE entries (the local FV the scatter reads)
+        uint16_t* fv16 = reinterpret_cast<uint16_t*>(s_fe);
         for (int f = threadIdx.x; f < h.nFl; f += kQT) {
 #pragma unroll
-            for (int k = 0; k < 3; ++k) atomicAdd(slot(face_vertex(fe16, s_ev, f, k)), 1);
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t v = face_vertex(fe16, s_ev, f, k);
+                fv16[3 * f + k]  = (uint16_t)v;
+                atomicAdd(slot(v), 1);
+            }
         }
     } else {
         for (int e2 = threadIdx.x; e2 < nE2; e2 += kQT) {
@@ -275,7 +282,7 @@ __global__ void __launch_bounds__(kQT) k_query_vertex(const PatchHdr* __restrict
         for (int f = threadIdx.x; f < h.nFl; f += kQT) {
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const uint32_t v = face_vertex(fe16, s_ev, f, k);
+                const uint32_t v = fe16[3 * f + k];  // local FV, written by the count
                 const int32_t  q = atomicAdd(slot(v), 1);
                 if ((int32_t)v < nVo) sbuf[q] = (uint16_t)f;
             }
@@ -485,7 +492,10 @@ __global__ void __launch_bounds__(kQT) k_query_ff_oriented(const PatchHdr* __res
     const uint16_t* fe16 = reinterpret_cast<const uint16_t*>(s_fe);
     uint16_t*       slot = reinterpret_cast<uint16_t*>(s_slot);  // [2e + dir]
 
-    for (int i = threadIdx.x; i < 3 * nFl; i += kQT) slot[fe16[i]] = (uint16_t)(i / 3);
+    for (int f = threadIdx.x; f < nFl; f += kQT) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) slot[fe16[3 * f + k]] = (uint16_t)f;
+    }
     __syncthreads();
     for (int f = threadIdx.x; f < nFo; f += kQT) {
         int32_t c = 0;
@@ -495,9 +505,9 @@ __global__ void __launch_bounds__(kQT) k_query_ff_oriented(const PatchHdr* __res
     }
     if (threadIdx.x == 0) s_fc[nFo] = 0;
     __syncthreads();
-    const int32_t total = block_exclusive_scan<kQT>(s_fc, nFo + 1, s_warp);
+    // row offsets written to the global offsets by the scan's last pass
     const int32_t vbase = __ldg(qb + blockIdx.x);
-    for (int f = threadIdx.x; f <= nFo; f += kQT) out_off[h.f_base + f] = vbase + s_fc[f];
+    const int32_t total = block_exclusive_scan<kQT>(s_fc, nFo + 1, s_warp, out_off + h.f_base, vbase);
     uint16_t* sbuf = s_out + (vbase & 3);
     for (int f = threadIdx.x; f < nFo; f += kQT) {
         int32_t pos = s_fc[f];
@@ -566,9 +576,8 @@ __global__ void __launch_bounds__(kQT) k_query_ff(const PatchHdr* __restrict__ h
     }
     if (threadIdx.x == 0) s_fc[nFo] = 0;
     __syncthreads();
-    const int32_t total = block_exclusive_scan<kQT>(s_fc, nFo + 1, s_warp);
     const int32_t vbase = __ldg(qb + blockIdx.x);
-    for (int f = threadIdx.x; f <= nFo; f += kQT) out_off[h.f_base + f] = vbase + s_fc[f];
+    const int32_t total = block_exclusive_scan<kQT>(s_fc, nFo + 1, s_warp, out_off + h.f_base, vbase);
 
     // 3. rows: each owned face lists the other faces of its three edges
     uint16_t* sbuf = s_out + (vbase & 3);
