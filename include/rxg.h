@@ -359,10 +359,10 @@ rxg_status rxg_cg_solve(const rxg_csr* A, int32_t nc, const void* B, void* X,
  * library holds until the process exits.
  * Limits: A->n <= 131072 rows and nc <= 3 columns; larger problems return
  * RXG_ERR_INVALID with a message (use rxg_cg_solve).
- * The first call on a device looks up the array's device address (once per
- * device, with that device current); make that first call before any stream
- * capture.  Every call reads the solver statistics back to the host, so it
- * returns only after its work on `stream` has finished.  All calls share the
+ * The first call on a device also looks up the array's device address (once
+ * per device, with that device current).  Every call reads the solver
+ * statistics back to the host, so it returns only after its work on `stream`
+ * has finished.  All calls share the
  * one array: calls that overlap on the GPU (other streams, other host
  * threads) race and must be serialised by the caller.  Device arrays only
  * (A's row_ptr, col and val, B and X; a host array returns RXG_ERR_INVALID).
