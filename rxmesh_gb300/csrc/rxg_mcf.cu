@@ -2098,15 +2098,23 @@ __device__ __forceinline__ V3<Dual9> seed3(V3<double> a, int slot)
     return r;
 }
 
-__device__ __forceinline__ void scatter3(double* __restrict__ g, int32_t v, const Dual9& f, int slot,
-                                         double c)
+// add c * (derivative slots 3*slot .. 3*slot+2 of f) to a 3-vector
+__device__ __forceinline__ void axpy3(double* acc, const Dual9& f, int slot, double c)
 {
-    atomicAdd(g + 3 * (int64_t)v + 0, c * f.d[3 * slot + 0]);
-    atomicAdd(g + 3 * (int64_t)v + 1, c * f.d[3 * slot + 1]);
-    atomicAdd(g + 3 * (int64_t)v + 2, c * f.d[3 * slot + 2]);
+    acc[0] += c * f.d[3 * slot + 0];
+    acc[1] += c * f.d[3 * slot + 1];
+    acc[2] += c * f.d[3 * slot + 2];
 }
 
-// g_in must be zero on entry
+// Per vertex p, the derivative of  lam_p . ((A x1 - B)_p)  with respect to
+// the positions x (A, B assembled from x): each fan triangle T_t = (p, r_t,
+// r_t+1) is evaluated once with 9 dual tangents (tri_terms: its two
+// half-cotangents and its Voronoi term, bit for bit the values of the
+// separate per-entry calls), and its three derivative rows are combined with
+// their coefficients -- dt lam_p . (x1_r - x1_p) for the half-cotangent of
+// each edge whose (unclamped) weight is >= 0, 2 lam_p . (x_p - x1_p) for a
+// positive Voronoi term -- before one scatter to r_t and r_t+1; p's own
+// share is summed in registers.  g_in must be zero on entry.
 __global__ void __launch_bounds__(128) k_mcf_backward(int64_t nv, const int32_t* __restrict__ row_ptr,
                                                       const int32_t* __restrict__ col,
                                                       const int8_t* __restrict__ bnd,
@@ -2125,45 +2133,62 @@ __global__ void __launch_bounds__(128) k_mcf_backward(int64_t nv, const int32_t*
         const V3<double> L    = ld3(lam, (int32_t)p);
         const V3<double> Y    = ld3(x1, (int32_t)p);
         const double     ap   = 2.0 * (L.x * (P.x - Y.x) + L.y * (P.y - Y.y) + L.z * (P.z - Y.z));
-        double           area = 0.0;
-        for (int32_t i = 0; i < k; ++i) {
-            const int32_t    r = rg[i], q = rg[(i + k - 1) % k], s = rg[(i + 1) % k];
-            const bool       has_q = wrap || i > 0, has_s = wrap || i < k - 1;
-            const V3<double> R = ld3(x, r), Q = ld3(x, q), S = ld3(x, s);
-            double           w = 0;
-            if (has_q) w += half_cot<double>(P, R, Q);
-            if (has_s) w += half_cot<double>(P, R, S);
-            const V3<double> Yr = ld3(x1, r);
-            const double beta = dt * (L.x * (Yr.x - Y.x) + L.y * (Yr.y - Y.y) + L.z * (Yr.z - Y.z));
-            if (w >= 0.0 && beta != 0.0) {
-                if (has_q) {
-                    const Dual9 h = half_cot<Dual9>(seed3(P, 0), seed3(R, 1), seed3(Q, 2));
-                    scatter3(g_in, (int32_t)p, h, 0, beta);
-                    scatter3(g_in, r, h, 1, beta);
-                    scatter3(g_in, q, h, 2, beta);
+        double           area = 0.0, gp[3] = {0.0, 0.0, 0.0};
+        // fan triangles: t = 0 .. nt-1, T_t = (p, r_t, r_(t+1) mod k); an
+        // open fan has no T_(k-1)
+        const int32_t nt   = k <= 0 ? 0 : (wrap ? k : k - 1);
+        auto          beta = [&](int32_t i) {
+            const V3<double> Yr = ld3(x1, rg[i]);
+            return dt * (L.x * (Yr.x - Y.x) + L.y * (Yr.y - Y.y) + L.z * (Yr.z - Y.z));
+        };
+        auto tv = [&](int32_t t) {  // value-only terms of T_t
+            return tri_terms<double>(P, ld3(x, rg[t]), ld3(x, rg[t + 1 < k ? t + 1 : 0]));
+        };
+        if (nt > 0) {
+            // weight of edge p - r_0: hb of the closing triangle (closed
+            // fans) + ha of T_0
+            const TriTerms<double> t0 = tv(0);
+            double       hb_prev = wrap ? tv(k - 1).hb : 0.0;
+            double       w_cur   = hb_prev + t0.ha;
+            double       b_cur   = beta(0);
+            const double w0 = w_cur, b0 = b_cur;
+            double       ha_next = t0.ha;
+            for (int32_t t = 0; t < nt; ++t) {
+                const int32_t  a = rg[t], bi = t + 1 < k ? t + 1 : 0, b = rg[bi];
+                const TriTerms<Dual9> D =
+                    tri_terms<Dual9>(seed3(P, 0), seed3(ld3(x, a), 1), seed3(ld3(x, b), 2));
+                // the next edge's weight and coefficient
+                double w_next, b_next;
+                if (t + 1 < k) {
+                    ha_next = (t + 1 < nt) ? tv(t + 1).ha : 0.0;
+                    w_next  = D.hb.v + ha_next;
+                    b_next  = beta(t + 1);
+                } else {  // closing triangle: the next edge is p - r_0
+                    w_next = w0;
+                    b_next = b0;
                 }
-                if (has_s) {
-                    const Dual9 h = half_cot<Dual9>(seed3(P, 0), seed3(R, 1), seed3(S, 2));
-                    scatter3(g_in, (int32_t)p, h, 0, beta);
-                    scatter3(g_in, r, h, 1, beta);
-                    scatter3(g_in, s, h, 2, beta);
-                }
-            }
-            if (has_q) {
-                const Dual9 a = voronoi<Dual9>(seed3(P, 0), seed3(Q, 1), seed3(R, 2));
-                if (a.v > 0.0) {
-                    area += a.v;
-                    if (ap != 0.0) {
-                        scatter3(g_in, (int32_t)p, a, 0, ap);
-                        scatter3(g_in, q, a, 1, ap);
-                        scatter3(g_in, r, a, 2, ap);
+                const double c_ha = (w_cur >= 0.0 && b_cur != 0.0) ? b_cur : 0.0;
+                const double c_hb = (w_next >= 0.0 && b_next != 0.0) ? b_next : 0.0;
+                const double c_va = D.va.v > 0.0 ? ap : 0.0;
+                if (D.va.v > 0.0) area += D.va.v;
+                double gr[3] = {0.0, 0.0, 0.0}, gs[3] = {0.0, 0.0, 0.0};
+                axpy3(gp, D.ha, 0, c_ha), axpy3(gp, D.hb, 0, c_hb), axpy3(gp, D.va, 0, c_va);
+                axpy3(gr, D.ha, 1, c_ha), axpy3(gr, D.hb, 1, c_hb), axpy3(gr, D.va, 1, c_va);
+                axpy3(gs, D.ha, 2, c_ha), axpy3(gs, D.hb, 2, c_hb), axpy3(gs, D.va, 2, c_va);
+                if (c_ha != 0.0 || c_hb != 0.0 || c_va != 0.0) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        atomicAdd(g_in + 3 * (int64_t)a + c, gr[c]);
+                        atomicAdd(g_in + 3 * (int64_t)b + c, gs[c]);
                     }
                 }
+                w_cur = w_next;
+                b_cur = b_next;
             }
         }
-        atomicAdd(g_in + 3 * p + 0, 2.0 * area * L.x);
-        atomicAdd(g_in + 3 * p + 1, 2.0 * area * L.y);
-        atomicAdd(g_in + 3 * p + 2, 2.0 * area * L.z);
+        atomicAdd(g_in + 3 * p + 0, gp[0] + 2.0 * area * L.x);
+        atomicAdd(g_in + 3 * p + 1, gp[1] + 2.0 * area * L.y);
+        atomicAdd(g_in + 3 * p + 2, gp[2] + 2.0 * area * L.z);
     }
 }
 
