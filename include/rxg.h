@@ -611,6 +611,13 @@ rxg_status rxg_dense_axpby(int64_t n, int32_t dtype, double a, const void* x, do
                            void* y, void* stream);
 rxg_status rxg_dense_dot(int64_t n, int32_t dtype, const void* x, const void* y,
                          double* out, void* stream);
+/*
+ * Zero the rows i of a row-major n x ncols array x (dtype) whose mask[i]
+ * is non-zero: the gradient half of NewtonSolver::apply_bc when there is no
+ * assembled Hessian (diff/newton_solver.h).  Device arrays; enqueues only.
+ */
+rxg_status rxg_dense_zero_rows(int64_t n, int32_t ncols, int32_t dtype, const int8_t* mask,
+                               void* x, void* stream);
 
 /*
  * apply_bc of NewtonSolver (diff/newton_solver.h): for every vertex i with

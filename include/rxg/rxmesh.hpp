@@ -1353,12 +1353,8 @@ class NewtonSolver
     {
         m_bc = bc.data();
         if (m_kind == CG_MATFREE) {
-            std::vector<int8_t> hb(bc.size());
-            check_cuda(cudaMemcpy(hb.data(), bc.data(), hb.size(), cudaMemcpyDeviceToHost), "cudaMemcpy");
-            std::vector<T> g = problem.grad.to_host(s);
-            for (size_t i = 0; i < hb.size(); ++i)
-                if (hb[i]) g[3 * i] = g[3 * i + 1] = g[3 * i + 2] = T(0);
-            problem.grad.from_host(g, s);
+            // no assembled Hessian: the constrained gradient rows only
+            check(rxg_dense_zero_rows((int64_t)bc.size(), 3, dtype_of<T>::value, bc.data(), problem.grad.data(), s));
         } else {
             problem.hess->apply_bc(bc.data(), &problem.grad, s);
         }

@@ -114,6 +114,7 @@ SIGNATURES = {
     "rxg_face_term_gather": [P, I32, I32, P, I32, P, P, P, P, P],
     "rxg_symdir_eval": [P, I32, P, P, I32, P, P, P, P, P],
     "rxg_inertia_eval": [P, I32, I32, P, P, D, I32, P, P, P, P],
+    "rxg_dense_zero_rows": [I64, I32, I32, P, P, P],
     "rxg_query_ex": [P, I32, P, P, I32, P],
     "rxg_vertex_normals_ex": [P, I32, P, P, I32, P],
 }

@@ -18,6 +18,14 @@ __global__ void k_axpby(int64_t n, T a, const T* __restrict__ x, T b, T* __restr
         y[i] = (b == T(0) ? T(0) : b * y[i]) + (a == T(0) ? T(0) : a * x[i]);
 }
 
+template <typename T>
+__global__ void k_zero_rows(int64_t n, int32_t nc, const int8_t* __restrict__ mask, T* __restrict__ x)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * nc;
+         i += (int64_t)gridDim.x * blockDim.x)
+        if (mask[i / nc]) x[i] = T(0);
+}
+
 constexpr int kDotBlocks = 296, kDotThreads = 256;
 
 template <typename T>
@@ -72,6 +80,28 @@ rxg_status rxg_dense_axpby(int64_t n, int32_t dtype, double a, const void* x, do
         k_axpby<double><<<g, 256, 0, s>>>(n, a, (const double*)x, b, (double*)y);
     else
         k_axpby<float><<<g, 256, 0, s>>>(n, (float)a, (const float*)x, (float)b, (float*)y);
+    RXG_CUDA_TRY(cudaGetLastError());
+    return RXG_OK;
+}
+
+rxg_status rxg_dense_zero_rows(int64_t n, int32_t ncols, int32_t dtype, const int8_t* mask, void* x,
+                               void* stream)
+{
+    if (n < 0 || ncols <= 0 || !mask || !x || (dtype != RXG_F32 && dtype != RXG_F64)) {
+        set_error("rxg_dense_zero_rows: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    if (!is_device_ptr(mask) || !is_device_ptr(x)) {
+        set_error("rxg_dense_zero_rows: mask and x must be device arrays");
+        return RXG_ERR_INVALID;
+    }
+    if (n == 0) return RXG_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int    g = grid_for_items(n * ncols);
+    if (dtype == RXG_F64)
+        k_zero_rows<double><<<g, 256, 0, s>>>(n, ncols, mask, (double*)x);
+    else
+        k_zero_rows<float><<<g, 256, 0, s>>>(n, ncols, mask, (float*)x);
     RXG_CUDA_TRY(cudaGetLastError());
     return RXG_OK;
 }

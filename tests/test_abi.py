@@ -76,6 +76,10 @@ def test_dense_and_partition_entry_points_reject_bad_arguments(tmp_path):
     assert L.rxg_dense_axpby(12, 7, 0.0, None, 1.0, x.ctypes.data, None) == 1  # bad dtype
     assert L.rxg_dense_dot(12, 1, x.ctypes.data, x.ctypes.data, ctypes.byref(out), None) == 1
     assert L.rxg_dense_dot(12, 1, None, x.ctypes.data, ctypes.byref(out), None) == 1
+    mask = np.zeros(4, np.int8)
+    assert L.rxg_dense_zero_rows(4, 3, 1, mask.ctypes.data, x.ctypes.data, None) == 1
+    assert b"device arrays" in L.rxg_last_error()
+    assert L.rxg_dense_zero_rows(4, 0, 1, mask.ctypes.data, x.ctypes.data, None) == 1  # no columns
     assert L.rxg_mesh_partition(None, None, None, None) == 1
     _, f = meshgen.icosphere(1)
     f = np.ascontiguousarray(f, np.int32)

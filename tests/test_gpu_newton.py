@@ -250,3 +250,19 @@ def test_newton_arap_with_inertia_converges_each_solve():
         prob.eval_terms()
         e.append(prob.get_current_loss())
     assert all(b <= a for a, b in zip(e, e[1:])), e
+
+
+def test_dense_zero_rows():
+    """rxg_dense_zero_rows (the gradient half of apply_bc without an assembled
+    Hessian) zeroes exactly the masked rows, FP32 and FP64."""
+    import ctypes
+    from rxmesh_gb300 import _lib
+    L = _lib.load()
+    for dt, code in ((torch.float32, 0), (torch.float64, 1)):
+        x = torch.randn(1000, 3, dtype=dt, device="cuda")
+        mask = (torch.rand(1000, device="cuda") < 0.3).to(torch.int8)
+        want = x.clone()
+        want[mask.bool()] = 0
+        _lib.check(L.rxg_dense_zero_rows(1000, 3, code, ctypes.c_void_p(mask.data_ptr()),
+                                         ctypes.c_void_p(x.data_ptr()), None))
+        assert torch.equal(x, want)
