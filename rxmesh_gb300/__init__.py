@@ -308,11 +308,18 @@ class RXMeshStatic:
                                 _stream(stream)))
         return (offsets if csr else None), values
 
-    def query_host(self, op, offsets, values):
-        """Same as query() into host numpy arrays (copies inside the call)."""
-        check(self._L.rxg_query(self._h, int(op),
-                                offsets.ctypes.data if offsets is not None else None,
-                                values.ctypes.data, None))
+    def query_host(self, op, offsets, values, asynchronous=False, stream=None):
+        """Same as query() into host arrays: numpy arrays, or CPU torch
+        tensors (copies inside the call; returns with the results in place).
+        asynchronous=True with page-locked tensors (tensor.pin_memory()):
+        the work and its copies are enqueued on `stream` (rxg_query_ex with
+        RXG_HOST_ASYNC) and the results are there once the stream has run
+        them; pageable arrays fall back to the synchronous call."""
+        ptr = lambda a: None if a is None else (a.ctypes.data if isinstance(a, np.ndarray) else a.data_ptr())
+        if asynchronous:
+            check(self._L.rxg_query_ex(self._h, int(op), ptr(offsets), ptr(values), 1, _stream(stream)))
+        else:
+            check(self._L.rxg_query(self._h, int(op), ptr(offsets), ptr(values), None))
         return offsets, values
 
     def query_oriented_vv(self, stream=None):

@@ -272,6 +272,28 @@ def test_query_ex_stream_ordered(flags):
                                   ctypes.c_void_p(val.data_ptr()), 4, None))
 
 
+def test_query_host_asynchronous_python():
+    """RXMeshStatic.query_host(..., asynchronous=True) on page-locked tensors
+    and a side stream: after the stream completes, the rows equal query()."""
+    from rxmesh_gb300 import Op, RXMeshStatic
+    x, f = meshgen.icosphere(4)
+    rx = RXMeshStatic(f, len(x), patch_size=128)
+    s = torch.cuda.Stream()
+    for op in (Op.VV, Op.FV, Op.EE):
+        rows, nval = rx.query_size(op)
+        off = torch.full((rows + 1,), -7, dtype=torch.int32).pin_memory() if op in Op.CSR else None
+        val = torch.full((nval,), -7, dtype=torch.int32).pin_memory()
+        rx.query_host(op, off, val, asynchronous=True, stream=s)
+        s.synchronize()
+        d_off, d_val = rx.query(op)
+        if off is not None:
+            assert torch.equal(off, d_off.cpu())
+            o = off.numpy()
+            assert sorted_rows(o, val.numpy()) == sorted_rows(o, d_val.cpu().numpy())
+        else:
+            assert torch.equal(val, d_val.cpu()), op
+
+
 @pytest.mark.parametrize("name,patch", [(n, 256) for n in ("sphere3", "torus", "cloth", "bunnyhead")]
                          + [("sphere3", "patcher"), ("torus", "patcher")])
 def test_normals_against_reference_fixture(oracle, name, patch, tmp_path):
