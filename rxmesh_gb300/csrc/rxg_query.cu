@@ -170,6 +170,14 @@ __device__ __forceinline__ uint32_t face_vertex(const uint16_t* s_fe, const uint
 // never stored; the row offsets are written by the scan's last pass.  This
 // form issued 11% fewer instructions than one with a branch per incidence.
 constexpr int kSpill = 32;
+
+// words of VF's first shared region: the EV slice, later the staged rows
+// (3 u16 per local face + 4 words of alignment slack)
+__host__ __device__ __forceinline__ int32_t vf_ev_words(const PatchHdr& h)
+{
+    const int32_t out_w = (3 * h.nFl + 1) / 2 + 4;
+    return pad4i(h.nEl > out_w ? h.nEl : out_w);
+}
 template <int OP, int kQT>
 __global__ void __launch_bounds__(kQT) k_query_vertex(const PatchHdr* __restrict__ hdrs,
                                                       const uint32_t* __restrict__ arena,
@@ -191,11 +199,17 @@ __global__ void __launch_bounds__(kQT) k_query_vertex(const PatchHdr* __restrict
 
     // shared layout (all 16-byte aligned); the patch's rows are staged as
     // 16-bit local ids and mapped to linear ids on the way out
-    uint32_t* s_ev  = smem;
-    uint32_t* s_fe  = s_ev + (EF ? 0 : pad4i(h.nEl));
-    uint32_t* s_rib = s_fe + (FCE ? pad4i((int32_t)fe_words(h.nFl)) : 0);
-    int32_t*  s_cnt = reinterpret_cast<int32_t*>(s_rib + pad4i(nRib));
-    uint16_t* s_out = reinterpret_cast<uint16_t*>(s_cnt + pad4i(nRows + 1 + kSpill));
+    // VF: the staged rows overlay the EV slice, which only the count pass
+    // reads (it leaves each face's corners in place of its FE entries), so
+    // the region is the larger of the two
+    constexpr bool VF = OP == 2;
+    const int32_t  ev_w  = EF ? 0 : (VF ? vf_ev_words(h) : pad4i(h.nEl));
+    uint32_t*      s_ev  = smem;
+    uint32_t*      s_fe  = s_ev + ev_w;
+    uint32_t*      s_rib = s_fe + (FCE ? pad4i((int32_t)fe_words(h.nFl)) : 0);
+    int32_t*       s_cnt = reinterpret_cast<int32_t*>(s_rib + pad4i(nRib));
+    uint16_t*      s_out = VF ? reinterpret_cast<uint16_t*>(smem)
+                              : reinterpret_cast<uint16_t*>(s_cnt + pad4i(nRows + 1 + kSpill));
     const int32_t spill = nRows + 1 + (int32_t)(threadIdx.x & 31);
     // counter of row r, or this lane's spill counter for r >= nRows
     auto slot = [&](uint32_t r) -> int32_t* { return &s_cnt[(int32_t)r < nRows ? (int32_t)r : spill]; };
@@ -699,8 +713,7 @@ static size_t smem_words(const PatchHdr& h, int kind)
         case RXG_OP_VE:
             return pad4i(h.nEl) + pad4i(kind == RXG_OP_VV ? nVr : nEr) + pad4i(h.nVo + 1 + kSpill) +
                    h.nEl + 4;
-        case RXG_OP_VF:
-            return pad4i(h.nEl) + few + pad4i(nFr) + pad4i(h.nVo + 1 + kSpill) + (3 * h.nFl + 1) / 2 + 4;
+        case RXG_OP_VF: return vf_ev_words(h) + few + pad4i(nFr) + pad4i(h.nVo + 1 + kSpill);
         case RXG_OP_FV: return pad4i(h.nEl) + pad4i((3 * h.nFo + 1) / 2) + pad4i(nVr);
         case RXG_OP_EV: return pad4i(h.nEo) + pad4i(nVr);
         case RXG_OP_EF: return few + pad4i(nFr) + pad4i(h.nEo + 1 + kSpill) + (3 * h.nFl + 1) / 2 + 4;
