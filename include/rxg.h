@@ -288,6 +288,15 @@ rxg_status rxg_vertex_normals(const rxg_mesh* m, int32_t weighting,
  */
 rxg_status rxg_device_check(void* stream);
 
+/*
+ * Exercise the bounded-wait error path without faulting or hanging the GPU:
+ * one CTA waits on an mbarrier that nothing arrives at, gives up after about
+ * 0.1 ms, sets the device error word and returns.  A following
+ * rxg_device_check(stream) returns RXG_ERR_DEVICE_TIMEOUT (and clears the
+ * word); the context stays usable.  Enqueues only.
+ */
+rxg_status rxg_selftest_bounded_wait(void* stream);
+
 /* ------------------------------------------------------------------ */
 /* Cotangent Laplacian, SpMV, CG/PCG, implicit MCF                      */
 /* ------------------------------------------------------------------ */

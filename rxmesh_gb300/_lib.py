@@ -84,6 +84,7 @@ SIGNATURES = {
     "rxg_query_oriented_vv": [P, P, P, P, P],
     "rxg_vertex_normals": [P, I32, P, P, P],
     "rxg_device_check": [P],
+    "rxg_selftest_bounded_wait": [P],
     "rxg_mcf_pattern_size": [P, P, P],
     "rxg_mcf_assemble": [P, D, P, P, P, P],
     "rxg_spmm": [P, I32, P, P, P],

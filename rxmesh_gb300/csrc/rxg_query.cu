@@ -694,6 +694,21 @@ __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restri
     }
 }
 
+// A wait that cannot complete (nothing arrives at the barrier), bounded by
+// `attempts` tries of ~1 us each: it reports through the error word and the
+// CTA returns, the path every bounded wait in the library takes.
+__global__ void k_wait_selftest(int* err, int attempts)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        bool ok = false;
+        for (int i = 0; i < attempts && !ok; ++i) ok = mbar_try_wait_hint(&bar, 0, 1000);
+        if (!ok) atomicOr(err, DEVERR_MBAR_TIMEOUT);
+    }
+}
+
 // ---------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------
@@ -1186,5 +1201,17 @@ rxg_status rxg_vertex_normals_ex(const rxg_mesh* h, int32_t weighting, const flo
 
 // Syncs `stream`, reads and clears the device error word set by bounded waits.
 rxg_status rxg_device_check(void* stream) { return check_device_error((cudaStream_t)stream); }
+
+rxg_status rxg_selftest_bounded_wait(void* stream)
+{
+    int* err = device_error_word();
+    if (!err) {
+        set_error("rxg_selftest_bounded_wait: no current CUDA device");
+        return RXG_ERR_NO_DEVICE;
+    }
+    k_wait_selftest<<<1, 32, 0, (cudaStream_t)stream>>>(err, 100);
+    RXG_CUDA_TRY(cudaGetLastError());
+    return RXG_OK;
+}
 
 }  // extern "C"

@@ -401,3 +401,20 @@ def test_edge_edge_query(oracle, name):
     g[3] = g[3][::-1]
     with pytest.raises(RXGError):
         RXMeshStatic(g, len(x), patch_size=64).query(Op.EE)
+
+
+def test_bounded_wait_reports_and_context_survives():
+    """A device wait that can never complete gives up, sets the error word
+    (rxg_device_check -> RXG_ERR_DEVICE_TIMEOUT, then cleared) and leaves the
+    context usable: no fault, trap or hang is involved."""
+    from rxmesh_gb300 import Op, RXGError, RXMeshStatic, _lib, device_check
+    L = _lib.load()
+    device_check()
+    _lib.check(L.rxg_selftest_bounded_wait(None))
+    with pytest.raises(RXGError) as e:
+        device_check()
+    assert e.value.status == 7 and "timed out" in str(e.value)
+    device_check()  # cleared
+    x, f = meshgen.icosphere(2)
+    off, val = RXMeshStatic(f, len(x), patch_size=64).query(Op.VV)
+    assert int(off[-1].item()) == val.numel()
