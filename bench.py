@@ -425,6 +425,28 @@ def run_sweep_back_to_back(args, torch, flush_l2, launch, concurrent=False, orde
     return ms, mode, clk.summary()
 
 
+def run_fused(args, torch, rx, xl32, flush_l2):
+    """The same six outputs from one rxg_query_sweep launch (topology staged
+    once per patch, VV and VE sharing one counting sort), timed like the
+    other legs: one event pair per sweep after an L2 flush."""
+    out = rx.query_sweep(xyz=xl32, weighting="area")
+    for _ in range(args.warmup):
+        flush_l2()
+        rx.query_sweep(xyz=xl32, weighting="area", out=out)
+    torch.cuda.synchronize()
+    evs = []
+    for _ in range(args.steps):
+        flush_l2()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        rx.query_sweep(xyz=xl32, weighting="area", out=out)
+        b.record()
+        evs.append((a, b))
+    torch.cuda.synchronize()
+    return statistics.mean(a.elapsed_time(b) for a, b in evs)
+
+
 E2E_MODES = {"sync": None, "async": 1, "direct": 2}  # rxg_query / rxg_query_ex(RXG_HOST_ASYNC / _DIRECT)
 
 
@@ -1126,6 +1148,7 @@ def main():
     longest_first = sorted(OPS, key=lambda k: -statistics.mean(per[k]))
     ms, sweep_mode, clocks = run_sweep_back_to_back(args, torch, *fns, concurrent=True, order=longest_first)
     ms = max_over_ranks(torch, ms, "cuda")
+    ms_fused = run_fused(args, torch, rx, xl.float(), fns[0])
     cb = canonical_bytes(V, E, F)
     sweep_bytes = sum(cb.values())
     value = world * sweep_bytes / (ms * 1e-3) / 1e9
@@ -1148,6 +1171,8 @@ def main():
                   "sequential_ms": ms_seq, "sequential_gbs": sweep_bytes / (ms_seq * 1e-3) / 1e9,
                   "sequential_timing": mode_seq,
                   "isolated_sum_ms": ms_isolated,
+                  "fused_ms": ms_fused, "fused_gbs": sweep_bytes / (ms_fused * 1e-3) / 1e9,
+                  "fused_timing": "the same six outputs from one rxg_query_sweep launch after an L2 flush",
                   "isolated_note": "sum of the six kernels each timed alone after its own L2 flush "
                                    "(outputs stay dirty in L2 and are written back outside the "
                                    "timed region)"},

@@ -261,6 +261,32 @@ rxg_status rxg_vertex_normals_ex(const rxg_mesh* m, int32_t weighting, const flo
                                  float* out, int32_t flags, void* stream);
 
 /*
+ * Several of the vertex-centred queries and the vertex normals in one launch
+ * (one CTA per patch): the patch's topology slices are staged once for all
+ * of them, and VV and VE share one counting sort.  Any output left NULL is
+ * not computed; CSR outputs (VV, VE, VF) come as offsets + values pairs.
+ * Each output equals the one rxg_query / rxg_vertex_normals writes (rows of
+ * VV, VE, VF as the same sets; FV, EV and normals bit for bit).  Device
+ * arrays only; value arrays 16-byte aligned.  The reference runs each query
+ * as its own for_each; RXMesh's run_kernel also takes several ops for one
+ * kernel of the application's (rxmesh_static.h:450-505).
+ */
+typedef struct rxg_sweep_out {
+    int32_t* vv_offsets; /* nv + 1 */
+    int32_t* vv_values;  /* 2 ne */
+    int32_t* ve_offsets; /* nv + 1 */
+    int32_t* ve_values;  /* 2 ne */
+    int32_t* vf_offsets; /* nv + 1 */
+    int32_t* vf_values;  /* 3 nf */
+    int32_t* fv_values;  /* 3 nf */
+    int32_t* ev_values;  /* 2 ne */
+    const float* xyz;    /* linear-order positions (nv x 3) for the normals */
+    float*   normals;    /* nv x 3 */
+    int32_t  weighting;  /* RXG_NORMAL_MAX or RXG_NORMAL_AREA */
+} rxg_sweep_out;
+rxg_status rxg_query_sweep(const rxg_mesh* m, const rxg_sweep_out* out, void* stream);
+
+/*
  * Oriented VV (Query::dispatch<Op::VV>(..., oriented=true),
  * rxmesh_queries.cuh:376-499): each row lists the one-ring in the rotational
  * order of the incident faces.  A boundary vertex's row starts and ends at

@@ -322,6 +322,43 @@ class RXMeshStatic:
             check(self._L.rxg_query(self._h, int(op), ptr(offsets), ptr(values), None))
         return offsets, values
 
+    def query_sweep(self, ops=("VV", "VE", "VF", "FV", "EV", "normals"), xyz=None, weighting="area",
+                    stream=None, out=None):
+        """Several queries (VV, VE, VF, FV, EV) and vertex normals in one
+        launch (rxg_query_sweep): a dict op -> (offsets, values) for the CSR
+        ops, values for FV / EV, the (nv, 3) normals for "normals" (which
+        needs linear-order FP32 positions xyz).  out: the same dict of
+        preallocated device tensors, to write into."""
+        dev = torch.device("cuda", torch.cuda.current_device())
+        res = {} if out is None else dict(out)
+        so = _lib.SweepOut()
+        for name in ops:
+            if name == "normals":
+                if xyz is None or xyz.dtype != torch.float32 or not xyz.is_cuda:
+                    raise ValueError("normals need CUDA float32 positions xyz (nv, 3)")
+                xyz = xyz.contiguous()
+                if name not in res:
+                    res[name] = torch.empty_like(xyz)
+                so.xyz, so.normals = xyz.data_ptr(), res[name].data_ptr()
+                so.weighting = {"max": 0, "area": 1}[weighting] if isinstance(weighting, str) else int(weighting)
+                continue
+            op = Op.NAMES[name]
+            rows, nval = self.query_size(op)
+            if name not in res:
+                off = torch.empty(rows + 1, dtype=torch.int32, device=dev) if op in Op.CSR else None
+                res[name] = (off, torch.empty(nval, dtype=torch.int32, device=dev)) if op in Op.CSR else \
+                    torch.empty(nval, dtype=torch.int32, device=dev)
+            r = res[name]
+            if op in Op.CSR:
+                setattr(so, name.lower() + "_offsets", r[0].data_ptr())
+                setattr(so, name.lower() + "_values", r[1].data_ptr())
+            elif name in ("FV", "EV"):
+                setattr(so, name.lower() + "_values", r.data_ptr())
+            else:
+                raise ValueError("query_sweep covers VV, VE, VF, FV, EV and normals, not %s" % name)
+        check(self._L.rxg_query_sweep(self._h, ctypes.byref(so), _stream(stream)))
+        return res
+
     def query_oriented_vv(self, stream=None):
         """Oriented one-ring (rxmesh_queries.cuh:376-499): (offsets, values, boundary)."""
         nv = self.get_num_vertices()

@@ -22,6 +22,15 @@ class RXGError(RuntimeError):
         self.status = status
 
 
+class SweepOut(ctypes.Structure):
+    """rxg_sweep_out (include/rxg.h)."""
+    _fields_ = [("vv_offsets", ctypes.c_void_p), ("vv_values", ctypes.c_void_p),
+                ("ve_offsets", ctypes.c_void_p), ("ve_values", ctypes.c_void_p),
+                ("vf_offsets", ctypes.c_void_p), ("vf_values", ctypes.c_void_p),
+                ("fv_values", ctypes.c_void_p), ("ev_values", ctypes.c_void_p),
+                ("xyz", ctypes.c_void_p), ("normals", ctypes.c_void_p), ("weighting", ctypes.c_int32)]
+
+
 class MeshInfo(ctypes.Structure):
     _fields_ = [("num_vertices", ctypes.c_int64), ("num_edges", ctypes.c_int64),
                 ("num_faces", ctypes.c_int64), ("num_patches", ctypes.c_int64),
@@ -117,6 +126,7 @@ SIGNATURES = {
     "rxg_inertia_eval": [P, I32, I32, P, P, D, I32, P, P, P, P],
     "rxg_dense_zero_rows": [I64, I32, I32, P, P, P],
     "rxg_query_ex": [P, I32, P, P, I32, P],
+    "rxg_query_sweep": [P, P, P],
     "rxg_vertex_normals_ex": [P, I32, P, P, I32, P],
 }
 _RESTYPE = {"rxg_status_string": ctypes.c_char_p, "rxg_last_error": ctypes.c_char_p,

@@ -145,7 +145,7 @@ __device__ __forceinline__ PatchHdr load_hdr(const PatchHdr* __restrict__ hdrs)
     return h;
 }
 
-__device__ __forceinline__ uint32_t fe_words(int32_t nF) { return (uint32_t)((3 * nF + 1) / 2); }
+__host__ __device__ __forceinline__ uint32_t fe_words(int32_t nF) { return (uint32_t)((3 * nF + 1) / 2); }
 
 // vertex k (0..2) of local face f from FE (edge<<1|dir) and EV (a | b<<16)
 __device__ __forceinline__ uint32_t face_vertex(const uint16_t* s_fe, const uint32_t* s_ev, int f,
@@ -694,6 +694,236 @@ __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restri
     }
 }
 
+// ---------------------------------------------------------------------
+// The sweep in one launch (rxg_query_sweep): per patch, any of VV, VE, VF,
+// FV, EV and vertex normals.  The patch's EV / FE slices, its three ribbon
+// tables and (for normals) its incidence block are staged once; VV and VE
+// share one counting sort (a row of VV and the same row of VE list the same
+// incident edges: the offsets are identical, the values are the edge's other
+// end and the edge); VF turns the FE slice into local FV in place.  Each
+// output is the value its own kernel writes (normals, FV, EV, EVD-free
+// rows bit for bit; CSR rows as the same sets, in shared-memory-atomic order).
+// ---------------------------------------------------------------------
+
+struct SweepArgs
+{
+    int32_t *vv_off, *vv_val, *ve_off, *ve_val, *vf_off, *vf_val, *fv_val, *ev_val;
+    const float* xyz;
+    float*       nrm_out;
+    int          weighting;
+};
+
+// words of the sweep's reused region for one patch (normals block + float4
+// positions, VV and VE rows, VF rows: the largest of the requested ones)
+__host__ __device__ __forceinline__ int32_t sweep_big_words(const PatchHdr& h, int32_t nrm_words, bool nrm,
+                                                             bool vvve, bool vf)
+{
+    int32_t w = 0;
+    if (nrm) w = nrm_words + 4 * h.nVl;
+    const int32_t vvw = pad4i(h.nEl + 4) + h.nEl + 4;  // VV rows, then VE rows 16-byte aligned
+    if (vvve) w = w > vvw ? w : vvw;
+    const int32_t vfw = (3 * h.nFl + 1) / 2 + 4;
+    if (vf) w = w > vfw ? w : vfw;
+    return pad4i(w);
+}
+
+template <int kQT>
+__global__ void __launch_bounds__(kQT) k_query_sweep(const PatchHdr* __restrict__ hdrs,
+                                                     const int32_t* __restrict__ nrm_off,
+                                                     const uint32_t* __restrict__ nrm,
+                                                     const uint32_t* __restrict__ arena, SweepArgs o,
+                                                     int* err)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ uint64_t bar;
+    __shared__ int32_t  s_warp[kQT / 32];
+
+    const PatchHdr h   = load_hdr(hdrs);
+    const int32_t  nVo = h.nVo, nEo = h.nEo, nFo = h.nFo;
+    const int32_t  nVr = h.nVl - nVo, nEr = h.nEl - nEo, nFr = h.nFl - nFo;
+    const bool     NRM = o.nrm_out != nullptr, VVVE = o.vv_val || o.ve_val, VF = o.vf_val != nullptr;
+    const int32_t  b0  = NRM ? __ldg(nrm_off + blockIdx.x) : 0;
+    const int32_t  nw  = NRM ? __ldg(nrm_off + blockIdx.x + 1) - b0 : 0;
+
+    // only the slices the requested outputs read are staged (the host sizes
+    // shared memory for all of them)
+    const bool    NEV = VVVE || VF || o.fv_val || o.ev_val, NFE = VF || o.fv_val;
+    const bool    NRV = o.vv_val || o.fv_val || o.ev_val, NRE = o.ve_val != nullptr;
+    const int32_t wev = NEV ? pad4i(h.nEl) : 0, wfe = NFE ? pad4i((int32_t)fe_words(h.nFl)) : 0;
+    const int32_t wrv = NRV ? pad4i(nVr) : 0, wre = NRE ? pad4i(nEr) : 0, wrf = VF ? pad4i(nFr) : 0;
+    uint32_t* s_ev  = smem;
+    uint32_t* s_fe  = s_ev + wev;
+    uint32_t* s_rv  = s_fe + wfe;
+    uint32_t* s_re  = s_rv + wrv;
+    uint32_t* s_rf  = s_re + wre;
+    int32_t*  s_cnt = reinterpret_cast<int32_t*>(s_rf + wrf);
+    uint32_t* s_big = reinterpret_cast<uint32_t*>(s_cnt + pad4i(nVo + 1 + kSpill));
+
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    {
+        uint32_t* const dst[6] = {s_ev, s_fe, s_rv, s_re, s_rf, s_big};
+        const Slice     sl[6]  = {{arena + h.ev_off, 4u * (uint32_t)wev}, {arena + h.fe_off, 4u * (uint32_t)wfe},
+                                  {arena + h.rv_off, 4u * (uint32_t)wrv}, {arena + h.re_off, 4u * (uint32_t)wre},
+                                  {arena + h.rf_off, 4u * (uint32_t)wrf}, {nrm + b0, 4u * (uint32_t)nw}};
+        // positions for the normals come in while the slices do
+        float4* s_pos = reinterpret_cast<float4*>(s_big + nw);
+        if (threadIdx.x == 0) {
+            uint32_t total = 0;
+#pragma unroll
+            for (int i = 0; i < 6; ++i) total += sl[i].bytes;
+            mbar_arrive_expect_tx(&bar, total);
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+                if (sl[i].bytes) bulk_g2s(dst[i], sl[i].src, sl[i].bytes, &bar);
+        }
+        if (NRM) {
+            const float* xo = o.xyz + 3 * (int64_t)h.v_base;
+            for (int i = threadIdx.x; i < nVo; i += kQT)
+                s_pos[i] = make_float4(__ldg(xo + 3 * i), __ldg(xo + 3 * i + 1), __ldg(xo + 3 * i + 2), 0.f);
+            for (int i = threadIdx.x; i < nVr; i += kQT) {
+                const int64_t g = 3 * (int64_t)__ldg(arena + h.rv_off + i);
+                s_pos[nVo + i]  = make_float4(__ldg(o.xyz + g), __ldg(o.xyz + g + 1), __ldg(o.xyz + g + 2), 0.f);
+            }
+        }
+        if (!wait_stage(&bar, err)) return;
+    }
+    const uint16_t* fe16 = reinterpret_cast<const uint16_t*>(s_fe);
+    const int32_t   vb = h.v_base, eb = h.e_base, fb = h.f_base;
+    auto            vlin = [=](uint32_t l) -> int32_t { return (int32_t)l < nVo ? vb + (int32_t)l : (int32_t)s_rv[l - nVo]; };
+
+    // ---- normals (the arithmetic and order of k_vertex_normals)
+    if (NRM) {
+        const uint32_t* s_off = s_big;
+        const uint32_t* s_vis = s_big + pad4i(nVo + 1);
+        const float4*   s_pos = reinterpret_cast<const float4*>(s_big + nw);
+        float*          out   = o.nrm_out + 3 * (int64_t)vb;
+        for (int v = threadIdx.x; v < nVo; v += kQT) {
+            const float4   P  = s_pos[v];
+            float          a0 = 0.f, a1 = 0.f, a2 = 0.f;
+            const uint32_t j1 = s_off[v + 1];
+            for (uint32_t j = s_off[v]; j < j1; ++j) {
+                const uint32_t q = s_vis[j];
+                const float4   A = s_pos[q & 0xffffu], B = s_pos[q >> 16];
+                const float3   u = make_float3(A.x - P.x, A.y - P.y, A.z - P.z);
+                const float3   w = make_float3(B.x - P.x, B.y - P.y, B.z - P.z);
+                const float n0 = u.y * w.z - w.y * u.z, n1 = u.z * w.x - w.z * u.x, n2 = u.x * w.y - w.x * u.y;
+                if (o.weighting == RXG_NORMAL_MAX) {
+                    const float r = 1.f / ((u.x * u.x + u.y * u.y + u.z * u.z) + (w.x * w.x + w.y * w.y + w.z * w.z));
+                    a0 += n0 * r;
+                    a1 += n1 * r;
+                    a2 += n2 * r;
+                } else {
+                    a0 += n0;
+                    a1 += n1;
+                    a2 += n2;
+                }
+            }
+            out[3 * v]     = a0;
+            out[3 * v + 1] = a1;
+            out[3 * v + 2] = a2;
+        }
+    }
+    // ---- EV and FV rows
+    if (o.ev_val) {
+        int32_t* base = o.ev_val + 2 * (int64_t)eb;
+        for (int i = threadIdx.x; i < 2 * nEo; i += kQT) {
+            const uint32_t ev = s_ev[i >> 1];
+            base[i]           = vlin((i & 1) ? (ev >> 16) : (ev & 0xffffu));
+        }
+    }
+    if (o.fv_val) {
+        int32_t* base = o.fv_val + 3 * (int64_t)fb;
+        for (int i = threadIdx.x; i < 3 * nFo; i += kQT) base[i] = vlin(face_vertex(fe16, s_ev, i / 3, i % 3));
+    }
+    if (!VVVE && !VF) return;
+    const int32_t spill = nVo + 1 + (int32_t)(threadIdx.x & 31);
+    auto          slot  = [&](uint32_t r) -> int32_t* { return &s_cnt[(int32_t)r < nVo ? (int32_t)r : spill]; };
+    __syncthreads();  // the normals' use of the reused region is over
+
+    // ---- VV and VE: one counting sort over the EV endpoints
+    if (VVVE) {
+        for (int i = threadIdx.x; i < nVo + 1 + kSpill; i += kQT) s_cnt[i] = 0;
+        __syncthreads();
+        const uint2*  ev2 = reinterpret_cast<const uint2*>(s_ev);
+        const int32_t nE2 = (h.nEl + 1) >> 1;
+        for (int e2 = threadIdx.x; e2 < nE2; e2 += kQT) {
+            const uint2    w  = ev2[e2];
+            const bool     hi = 2 * e2 + 1 < h.nEl;
+            const uint32_t a0 = w.x & 0xffffu, b0 = w.x >> 16;
+            const uint32_t a1 = hi ? w.y & 0xffffu : 0xffffu, b1 = hi ? w.y >> 16 : 0xffffu;
+            atomicAdd(slot(a0), 1);
+            atomicAdd(slot(b0), 1);
+            atomicAdd(slot(a1), 1);
+            atomicAdd(slot(b1), 1);
+        }
+        __syncthreads();
+        const int32_t vbase = h.vv_base;
+        const int32_t total = block_exclusive_scan<kQT>(s_cnt, nVo + 1, s_warp, o.vv_off ? o.vv_off + vb : nullptr, vbase);
+        if (o.ve_off) {  // the same offsets, read before the scatter moves the counters
+            for (int v = threadIdx.x; v <= nVo; v += kQT) o.ve_off[vb + v] = vbase + s_cnt[v];
+            __syncthreads();
+        }
+        // rows of VV at s_big, of VE behind them (element g at [g - (vbase & ~3)])
+        uint16_t* svv = reinterpret_cast<uint16_t*>(s_big);
+        uint16_t* sve = reinterpret_cast<uint16_t*>(s_big + pad4i(h.nEl + 4));
+        uint16_t* bvv = svv + (vbase & 3);
+        uint16_t* bve = sve + (vbase & 3);
+        for (int e2 = threadIdx.x; e2 < nE2; e2 += kQT) {
+            const uint2    w  = ev2[e2];
+            const bool     hi = 2 * e2 + 1 < h.nEl;
+            const uint32_t a0 = w.x & 0xffffu, b0 = w.x >> 16;
+            const uint32_t a1 = hi ? w.y & 0xffffu : 0xffffu, b1 = hi ? w.y >> 16 : 0xffffu;
+            const uint16_t e0 = (uint16_t)(2 * e2), e1 = (uint16_t)(2 * e2 + 1);
+            const int32_t  q0 = atomicAdd(slot(a0), 1), q1 = atomicAdd(slot(b0), 1);
+            const int32_t  q2 = atomicAdd(slot(a1), 1), q3 = atomicAdd(slot(b1), 1);
+            if ((int32_t)a0 < nVo) bvv[q0] = (uint16_t)b0, bve[q0] = e0;
+            if ((int32_t)b0 < nVo) bvv[q1] = (uint16_t)a0, bve[q1] = e0;
+            if ((int32_t)a1 < nVo) bvv[q2] = (uint16_t)b1, bve[q2] = e1;
+            if ((int32_t)b1 < nVo) bvv[q3] = (uint16_t)a1, bve[q3] = e1;
+        }
+        __syncthreads();
+        if (o.vv_val) store_u16_mapped<kQT>(o.vv_val, vbase, svv, total, vlin);
+        if (o.ve_val)
+            store_u16_mapped<kQT>(o.ve_val, vbase, sve, total, [=](uint32_t l) -> int32_t {
+                return (int32_t)l < nEo ? eb + (int32_t)l : (int32_t)s_re[l - nEo];
+            });
+        if (VF) __syncthreads();  // VF reuses the counters and the region
+    }
+
+    // ---- VF: the FE slice becomes local FV in place (FV rows are written)
+    if (VF) {
+        for (int i = threadIdx.x; i < nVo + 1 + kSpill; i += kQT) s_cnt[i] = 0;
+        __syncthreads();
+        uint16_t* fv16 = reinterpret_cast<uint16_t*>(s_fe);
+        for (int f = threadIdx.x; f < h.nFl; f += kQT) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t v = face_vertex(fe16, s_ev, f, k);
+                fv16[3 * f + k]  = (uint16_t)v;
+                atomicAdd(slot(v), 1);
+            }
+        }
+        __syncthreads();
+        const int32_t vbase = h.vf_base;
+        const int32_t total = block_exclusive_scan<kQT>(s_cnt, nVo + 1, s_warp, o.vf_off ? o.vf_off + vb : nullptr, vbase);
+        uint16_t* svf = reinterpret_cast<uint16_t*>(s_big);
+        uint16_t* bvf = svf + (vbase & 3);
+        for (int f = threadIdx.x; f < h.nFl; f += kQT) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t v = fv16[3 * f + k];
+                const int32_t  q = atomicAdd(slot(v), 1);
+                if ((int32_t)v < nVo) bvf[q] = (uint16_t)f;
+            }
+        }
+        __syncthreads();
+        store_u16_mapped<kQT>(o.vf_val, vbase, svf, total, [=](uint32_t l) -> int32_t {
+            return (int32_t)l < nFo ? fb + (int32_t)l : (int32_t)s_rf[l - nFo];
+        });
+    }
+}
+
 // A wait that cannot complete (nothing arrives at the barrier), bounded by
 // `attempts` tries of ~1 us each: it reports through the error word and the
 // CTA returns, the path every bounded wait in the library takes.
@@ -758,6 +988,18 @@ void compute_smem_table(Mesh& m)
             w = std::max(w, pw);
         }
         m.smem_bytes[kind] = w * 4;
+    }
+    for (int c = 0; c < 8; ++c) {
+        size_t w = 0;
+        for (size_t p = 0; p < m.hdr.size(); ++p) {
+            const PatchHdr& h = m.hdr[p];
+            const int32_t   nw = (c & 1) ? m.nrm_off[p + 1] - m.nrm_off[p] : 0;
+            const size_t    pw = (size_t)pad4i(h.nEl) + pad4i((int32_t)fe_words(h.nFl)) + pad4i(h.nVl - h.nVo) +
+                              pad4i(h.nEl - h.nEo) + pad4i(h.nFl - h.nFo) + pad4i(h.nVo + 1 + kSpill) +
+                              sweep_big_words(h, nw, c & 1, (c & 2) != 0, (c & 4) != 0);
+            w = std::max(w, pw);
+        }
+        m.sweep_smem[c] = w * 4;
     }
 }
 
@@ -855,6 +1097,18 @@ static rxg_status launch_query_range(const Mesh* m, int op, int32_t* d_off, int3
 rxg_status launch_query(const Mesh* m, int op, int32_t* d_off, int32_t* d_val, cudaStream_t s)
 {
     return launch_query_range(m, op, d_off, d_val, s, PatchRange{0, m->num_patches});
+}
+
+// threads per CTA of the fused sweep: 128 by default (faster than 256 on
+// the 1024^2 torus), RXG_SWEEP_THREADS=256 to tune
+static int sweep_threads()
+{
+    static int t = 0;
+    if (!t) {
+        const char* e = getenv("RXG_SWEEP_THREADS");
+        t             = (e && atoi(e) == 256) ? 256 : 128;
+    }
+    return t;
 }
 
 template <int BT>
@@ -1200,6 +1454,59 @@ rxg_status rxg_vertex_normals_ex(const rxg_mesh* h, int32_t weighting, const flo
 }
 
 // Syncs `stream`, reads and clears the device error word set by bounded waits.
+rxg_status rxg_query_sweep(const rxg_mesh* h, const rxg_sweep_out* o, void* stream)
+{
+    if (!h || !o) {
+        set_error("rxg_query_sweep: NULL argument");
+        return RXG_ERR_INVALID;
+    }
+    const Mesh& M = h->m;
+    // CSR outputs come as pairs; every array given must be device memory;
+    // value arrays 16-byte aligned (vectorised row stores)
+    const struct { const void* off; const void* val; const char* name; bool csr; } outs[] = {
+        {o->vv_offsets, o->vv_values, "VV", true}, {o->ve_offsets, o->ve_values, "VE", true},
+        {o->vf_offsets, o->vf_values, "VF", true}, {nullptr, o->fv_values, "FV", false},
+        {nullptr, o->ev_values, "EV", false}};
+    for (const auto& q : outs) {
+        if (q.csr && ((q.off == nullptr) != (q.val == nullptr))) {
+            set_error("rxg_query_sweep: %s needs both offsets and values (or neither)", q.name);
+            return RXG_ERR_INVALID;
+        }
+        if ((q.off && !is_device_ptr(q.off)) || (q.val && !is_device_ptr(q.val))) {
+            set_error("rxg_query_sweep: the %s arrays must be device arrays", q.name);
+            return RXG_ERR_INVALID;
+        }
+        if (q.val && ((uintptr_t)q.val & 15u) != 0) {
+            set_error("rxg_query_sweep: the %s values must be 16-byte aligned", q.name);
+            return RXG_ERR_INVALID;
+        }
+    }
+    if (o->normals) {
+        if (!o->xyz || !is_device_ptr(o->xyz) || !is_device_ptr(o->normals) ||
+            (o->weighting != RXG_NORMAL_MAX && o->weighting != RXG_NORMAL_AREA)) {
+            set_error("rxg_query_sweep: normals need device xyz and out arrays and a valid weighting");
+            return RXG_ERR_INVALID;
+        }
+    }
+    SweepArgs a;
+    a.vv_off = o->vv_offsets, a.vv_val = o->vv_values, a.ve_off = o->ve_offsets, a.ve_val = o->ve_values;
+    a.vf_off = o->vf_offsets, a.vf_val = o->vf_values, a.fv_val = o->fv_values, a.ev_val = o->ev_values;
+    a.xyz = o->xyz, a.nrm_out = o->normals, a.weighting = o->weighting;
+    const int c = (o->normals ? 1 : 0) | ((a.vv_val || a.ve_val) ? 2 : 0) | (a.vf_val ? 4 : 0);
+    if (!c && !a.fv_val && !a.ev_val) return RXG_OK;
+    cudaStream_t    s    = (cudaStream_t)stream;
+    const size_t    smem = M.sweep_smem[c];
+    int*            err  = device_error_word();
+    const PatchHdr* hd   = M.d.hdr;
+    const PatchRange r{0, M.num_patches};
+    const uint32_t *nb = (const uint32_t*)M.d.nrm, *ar = (const uint32_t*)M.d.arena;
+    if (sweep_threads() == 128)
+        return launch(k_query_sweep<128>, 128, &M, smem, s, "sweep", r, hd, (const int32_t*)M.d.nrm_off, nb, ar,
+                      a, err);
+    return launch(k_query_sweep<256>, 256, &M, smem, s, "sweep", r, hd, (const int32_t*)M.d.nrm_off, nb, ar, a,
+                  err);
+}
+
 rxg_status rxg_device_check(void* stream) { return check_device_error((cudaStream_t)stream); }
 
 rxg_status rxg_selftest_bounded_wait(void* stream)

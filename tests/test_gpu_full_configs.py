@@ -108,6 +108,25 @@ def test_torus1024_normals(oracle, torus1024, weighting):
     assert np.median(rel) <= 1e-7, np.median(rel)
 
 
+def test_torus1024_fused_sweep_equals_queries(torus1024):
+    """rxg_query_sweep on the full torus: VV, VE, VF offsets equal and rows
+    the same sets as the separate queries; FV, EV and area normals equal."""
+    from rxmesh_gb300 import Op
+    x, f, rx = torus1024
+    xl = rx.to_linear(torch.tensor(np.asarray(x, np.float32), device="cuda"))
+    got = rx.query_sweep(xyz=xl, weighting="area")
+    for name in ("VV", "VE", "VF"):
+        off, val = rx.query(getattr(Op, name))
+        go, gv = got[name]
+        assert torch.equal(go, off), name
+        a = pairs(go.cpu().numpy(), gv.cpu().numpy())
+        b = pairs(off.cpu().numpy(), val.cpu().numpy())
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), name
+    assert torch.equal(got["FV"], rx.query(Op.FV)[1])
+    assert torch.equal(got["EV"], rx.query(Op.EV)[1])
+    assert torch.equal(got["normals"], rx.vertex_normals(xl, "area"))
+
+
 def test_torus1024_edge_face_queries_bit_exact(oracle, torus1024):
     """EF, FF as sets; FE, EVDiamond and EE in order, on the full torus."""
     from rxmesh_gb300 import Op
