@@ -1598,8 +1598,9 @@ rxg_status rxg_mcf_step(const rxg_mesh* h, double dt, int32_t nsteps, int32_t pr
         if (precision == RXG_F64) {
             Ent<double>* ent = (Ent<double>*)p;
             uint8_t*     scr = p + align256(sizeof(Ent<double>) * nnz);
-            k_mcf_assemble<double, Geo<double>, double><<<ga, 256, 0, s>>>(
-                n, z->row_ptr, z->col, z->bnd, X, dt, PackedOut<double, double>{ent, B4, nullptr});
+            const auto ka = k_mcf_assemble<double, Geo<double>, double, PackedOut<double, double>>;
+            ka<<<whole_wave_grid(ka, n, 256), 256, 0, s>>>(n, z->row_ptr, z->col, z->bnd, X, dt,
+                                                         PackedOut<double, double>{ent, B4, nullptr});
             RXG_CUDA_TRY(cudaGetLastError());
             rxg_solver_opts o = {max_iter, 0.0, tol * tol, 1};
             st = cgm_launch<double>(n, z->row_ptr, ent, B4, X4, o, &last, scr, s);
@@ -1615,8 +1616,9 @@ rxg_status rxg_mcf_step(const rxg_mesh* h, double dt, int32_t nsteps, int32_t pr
             double* D64 = (double*)w;
             w += align256(8 * n);
             uint8_t* scr = w;
-            k_mcf_assemble<float, GeoMixed, double><<<ga, 256, 0, s>>>(
-                n, z->row_ptr, z->col, z->bnd, X, (float)dt, PackedOut<float, double>{ent, B4, D64});
+            const auto ka = k_mcf_assemble<float, GeoMixed, double, PackedOut<float, double>>;
+            ka<<<whole_wave_grid(ka, n, 256), 256, 0, s>>>(n, z->row_ptr, z->col, z->bnd, X, (float)dt,
+                                                         PackedOut<float, double>{ent, B4, D64});
             RXG_CUDA_TRY(cudaGetLastError());
             if (onchip) {
                 // whole refinement in one launch; statistics read after the last step
@@ -1770,15 +1772,14 @@ rxg_status rxg_mcf_matvec(const rxg_mesh* h, double dt, int32_t flags, int32_t d
     rxg_status   st = ensure_pattern(&h->m, s, &z);
     if (st) return st;
     const int64_t nv = h->m.nv;
-    const int     g  = grid_for(nv);
     const int     u  = (flags & RXG_MCF_UNIFORM_LAPLACE) ? 1 : 0;
     const bool    jc = (flags & RXG_MCF_JACOBI) != 0;
     if (dtype == RXG_F64) {
         if (jc)
-            k_mcf_matvec<double, true, double><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, dt, u,
+            k_mcf_matvec<double, true, double><<<whole_wave_grid(k_mcf_matvec<double, true, double>, nv, 256), 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, dt, u,
                                                                  (const double*)in, (double*)out);
         else
-            k_mcf_matvec<double, false, double><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, dt, u,
+            k_mcf_matvec<double, false, double><<<whole_wave_grid(k_mcf_matvec<double, false, double>, nv, 256), 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xyz, dt, u,
                                                                   (const double*)in, (double*)out);
         RXG_CUDA_TRY(cudaGetLastError());
         return RXG_OK;
@@ -1790,10 +1791,10 @@ rxg_status rxg_mcf_matvec(const rxg_mesh* h, double dt, int32_t flags, int32_t d
         k_round_f32<<<grid_for(3 * nv), 256, 0, s>>>(3 * nv, xyz, xf);
     }
     if (jc)
-        k_mcf_matvec<float, true, float><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xf, (float)dt, u,
+        k_mcf_matvec<float, true, float><<<whole_wave_grid(k_mcf_matvec<float, true, float>, nv, 256), 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xf, (float)dt, u,
                                                            (const float*)in, (float*)out);
     else
-        k_mcf_matvec<float, false, float><<<g, 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xf, (float)dt, u,
+        k_mcf_matvec<float, false, float><<<whole_wave_grid(k_mcf_matvec<float, false, float>, nv, 256), 256, 0, s>>>(nv, z->row_ptr, z->col, z->bnd, xf, (float)dt, u,
                                                             (const float*)in, (float*)out);
     const cudaError_t e = cudaGetLastError();
     if (xf) cudaFreeAsync(xf, s);
