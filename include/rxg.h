@@ -598,6 +598,26 @@ rxg_status rxg_face_term_gather(const rxg_mesh* m, int32_t dtype, int32_t dim, c
                                 int32_t flags, double* energy, void* face_E, void* grad,
                                 rxg_bcsr* hess, void* stream);
 /*
+ * Generic per-edge and per-vertex terms (add_term<Op::EV> and add_term<Op::V>
+ * of diff/diff_scalar_problem.h:127-194), assembled like
+ * rxg_face_term_gather.  An edge term's records hold 1 + 2D + 2D(2D+1)/2
+ * values (E, the gradient for the edge's two vertices in EV order, the
+ * packed upper Hessian), ne records in edge linear order; a vertex term's
+ * 1 + D + D(D+1)/2 values, nv records in vertex linear order
+ * (include/rxg/diff.cuh: edge_term_kernel, vertex_term_kernel).  edge_E /
+ * vertex_E: the per-element energies (ne or nv of dtype, may be NULL).
+ * Without RXG_TERM_ACCUMULATE the gradient and the whole Hessian are
+ * overwritten (a vertex term's off-diagonal blocks cleared).  Needs a
+ * manifold mesh (the Hessian's one-ring pattern).
+ */
+rxg_status rxg_edge_term_gather(const rxg_mesh* m, int32_t dtype, int32_t dim, const void* records,
+                                int32_t flags, double* energy, void* edge_E, void* grad,
+                                rxg_bcsr* hess, void* stream);
+rxg_status rxg_vertex_term_gather(const rxg_mesh* m, int32_t dtype, int32_t dim, const void* records,
+                                  int32_t flags, double* energy, void* vertex_E, void* grad,
+                                  rxg_bcsr* hess, void* stream);
+
+/*
  * The symmetric Dirichlet energy of Param (apps/Param/param.cu:146-183), a
  * built-in term with D = 2: per face E = A (|J|_F^2 + |J^-1|_F^2), J = M
  * Mr^-1, M = [b - a, c - a] of the uv positions (uv: nv*2 of dtype, linear

@@ -17,9 +17,12 @@
 //   face_term_kernel     runs an energy functor over every face with the
 //                        face's 3 vertices x D components as the K = 3D
 //                        active variables, writing the records
+//   edge_term_kernel,    the same over every edge (K = 2D, the edge's two
+//   vertex_term_kernel   ends in EV order) and every vertex (K = D)
 // An application compiles its energy with this header and hands the records
-// to rxg_face_term_gather (librxg.so), which assembles the gradient and the
-// D x D block Hessian over the mesh's [diagonal, one-ring] pattern.
+// to rxg_face_term_gather / rxg_edge_term_gather / rxg_vertex_term_gather
+// (librxg.so), which assemble the gradient and the D x D block Hessian over
+// the mesh's [diagonal, one-ring] pattern.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -298,6 +301,12 @@ RXG_DIFF_HD constexpr int term_record_words(int D)
 {
     return 1 + 3 * D + (3 * D) * (3 * D + 1) / 2;
 }
+// record words of a term over `corners` vertices of D components (a face
+// term: 3; an edge term: 2; a vertex term: 1)
+RXG_DIFF_HD constexpr int term_record_words_n(int corners, int D)
+{
+    return 1 + corners * D + (corners * D) * (corners * D + 1) / 2;
+}
 
 // write e's value, gradient and Hessian as a record
 template <typename T, int K>
@@ -401,6 +410,72 @@ __global__ void __launch_bounds__(128) face_term_kernel(int64_t nf, const int32_
         if (PROJECT) project_packed<T, K>(e.hess, sizeof(T) == 4 ? T(1e-6) : T(1e-9));
         write_term_record<T, K>(e, records + (int64_t)term_record_words(D) * f);
     }
+}
+
+// Evaluate energy(edge, v) over every edge, v[k * D + d] component d of the
+// edge's end k (its two vertices in EV order) as active variables; records:
+// ne x term_record_words_n(2, D), edge linear order.  ev: ne x 2 linear
+// vertex ids (the EV query).  add_term<Op::EV> of the reference.
+template <typename T, int D, bool PROJECT, typename EnergyT>
+__global__ void __launch_bounds__(128) edge_term_kernel(int64_t ne, const int32_t* __restrict__ ev,
+                                                        const T* __restrict__ x, EnergyT energy,
+                                                        T* __restrict__ records)
+{
+    constexpr int K = 2 * D;
+    using S         = Scalar<T, K, true>;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        S v[K];
+        for (int k = 0; k < 2; ++k) {
+            const int32_t vi = ev[2 * e + k];
+            for (int d = 0; d < D; ++d) v[k * D + d] = S::make_active(x[(int64_t)vi * D + d], k * D + d);
+        }
+        S en = energy((int32_t)e, v);
+        if (PROJECT) project_packed<T, K>(en.hess, sizeof(T) == 4 ? T(1e-6) : T(1e-9));
+        write_term_record<T, K>(en, records + (int64_t)term_record_words_n(2, D) * e);
+    }
+}
+
+// Evaluate energy(vertex, v) over every vertex, v[d] its component d as the
+// active variables; records: nv x term_record_words_n(1, D), vertex linear
+// order.  add_term<Op::V> of the reference.
+template <typename T, int D, bool PROJECT, typename EnergyT>
+__global__ void __launch_bounds__(128) vertex_term_kernel(int64_t nv, const T* __restrict__ x, EnergyT energy,
+                                                          T* __restrict__ records)
+{
+    using S = Scalar<T, D, true>;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nv;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        S v[D];
+        for (int d = 0; d < D; ++d) v[d] = S::make_active(x[i * D + d], d);
+        S en = energy((int32_t)i, v);
+        if (PROJECT) project_packed<T, D>(en.hess, sizeof(T) == 4 ? T(1e-6) : T(1e-9));
+        write_term_record<T, D>(en, records + (int64_t)term_record_words_n(1, D) * i);
+    }
+}
+
+inline unsigned term_grid(int64_t n)
+{
+    const int64_t blocks = (n + 127) / 128;
+    return (unsigned)(blocks < 152 * 16 ? blocks : 152 * 16);
+}
+
+template <typename T, int D, bool PROJECT, typename EnergyT>
+inline cudaError_t launch_edge_term(int64_t ne, const int32_t* ev, const T* x, const EnergyT& energy, T* records,
+                                    cudaStream_t stream)
+{
+    if (ne == 0) return cudaSuccess;
+    edge_term_kernel<T, D, PROJECT, EnergyT><<<term_grid(ne), 128, 0, stream>>>(ne, ev, x, energy, records);
+    return cudaGetLastError();
+}
+
+template <typename T, int D, bool PROJECT, typename EnergyT>
+inline cudaError_t launch_vertex_term(int64_t nv, const T* x, const EnergyT& energy, T* records,
+                                      cudaStream_t stream)
+{
+    if (nv == 0) return cudaSuccess;
+    vertex_term_kernel<T, D, PROJECT, EnergyT><<<term_grid(nv), 128, 0, stream>>>(nv, x, energy, records);
+    return cudaGetLastError();
 }
 
 // launch face_term_kernel over nf faces on `stream`

@@ -80,7 +80,11 @@ enum class Op : int32_t {
     FE = RXG_OP_FE,
     FF = RXG_OP_FF,
     EVDiamond = RXG_OP_EVD,
-    EE = RXG_OP_EE
+    EE = RXG_OP_EE,
+    // the elements themselves (per-element terms, add_term<Op::V>); not queries
+    V = 100,
+    E = 101,
+    F = 102
 };
 
 // where a buffer lives (RXMesh's locationT)
@@ -1188,7 +1192,7 @@ template <typename T, int VariableDim = 3>
 class DiffScalarProblem
 {
    public:
-    static_assert(VariableDim == 2 || VariableDim == 3, "2 or 3 components per vertex");
+    static_assert(VariableDim >= 1 && VariableDim <= 3, "1, 2 or 3 components per vertex");
     explicit DiffScalarProblem(const RXMeshStatic& rx, bool assemble_hessian = true) : m_rx(&rx)
     {
         int64_t n = 0, nnz = 0;
@@ -1208,25 +1212,43 @@ class DiffScalarProblem
         check(rxg_arap_rest(m_rx->handle(), rest.data(), dtype_of<T>::value, m_rest.data(), s));
     }
 #if defined(__CUDACC__)
-    // add_term<Op::FV, ProjectHess>(energy) (diff_scalar_problem.h:127-194):
-    // energy(face id, const Scalar<T, 3 * VariableDim, true>* v) -> Scalar,
-    // a __device__ lambda or functor, where v[k * VariableDim + d] is
-    // component d of the face's corner k (its vertices in input order, the
-    // optimisation variable in linear order).  Terms add up.
+    // add_term<op, ProjectHess>(energy) (diff_scalar_problem.h:127-194), a
+    // __device__ lambda or functor over the optimisation variable (linear
+    // order) of one element's vertices, as Scalar<T, K, true> values, v[k *
+    // VariableDim + d] = component d of the element's vertex k:
+    //   Op::FV  energy(face id, v), K = 3 VariableDim, the face's vertices in
+    //           input order;
+    //   Op::EV  energy(edge id, v), K = 2 VariableDim, the edge's two
+    //           vertices in EV order;
+    //   Op::V   energy(vertex id, v), K = VariableDim.
+    // Terms add up.
     template <Op op, bool ProjectHess = false, typename LambdaT>
     void add_term(LambdaT energy)
     {
-        static_assert(op == Op::FV, "terms are per face (Op::FV)");
-        if (m_fv.size() == 0) {
-            QueryResult q = m_rx->query(Op::FV);
-            m_fv          = std::move(q.values);
+        static_assert(op == Op::FV || op == Op::EV || op == Op::V, "terms are per face, edge or vertex");
+        if constexpr (op == Op::FV) {
+            if (m_fv.size() == 0) m_fv = std::move(m_rx->query(Op::FV).values);
+            const int64_t  nf = m_rx->get_num_faces();
+            const int32_t* fv = m_fv.data();
+            m_terms.push_back({0, [=](const T* x, T* rec, cudaStream_t s) {
+                                   check_cuda(launch_face_term<T, VariableDim, ProjectHess>(nf, fv, x, energy, rec, s),
+                                              "face term launch");
+                               }});
+        } else if constexpr (op == Op::EV) {
+            if (m_ev.size() == 0) m_ev = std::move(m_rx->query(Op::EV).values);
+            const int64_t  ne = m_rx->get_num_edges();
+            const int32_t* ev = m_ev.data();
+            m_terms.push_back({1, [=](const T* x, T* rec, cudaStream_t s) {
+                                   check_cuda(launch_edge_term<T, VariableDim, ProjectHess>(ne, ev, x, energy, rec, s),
+                                              "edge term launch");
+                               }});
+        } else {
+            const int64_t nv = m_rx->get_num_vertices();
+            m_terms.push_back({2, [=](const T* x, T* rec, cudaStream_t s) {
+                                   check_cuda(launch_vertex_term<T, VariableDim, ProjectHess>(nv, x, energy, rec, s),
+                                              "vertex term launch");
+                               }});
         }
-        const int64_t  nf = m_rx->get_num_faces();
-        const int32_t* fv = m_fv.data();
-        m_terms.push_back([=](const T* x, T* rec, cudaStream_t s) {
-            check_cuda(launch_face_term<T, VariableDim, ProjectHess>(nf, fv, x, energy, rec, s),
-                       "face term launch");
-        });
     }
 #endif
     // inertia of a mass-spring system, mass/2 |x - x_target|^2 per vertex
@@ -1297,16 +1319,29 @@ class DiffScalarProblem
             first = false;
         }
         if (!m_terms.empty()) {
-            constexpr int K     = 3 * VariableDim;  // record: E, gradient, packed Hessian
-            const size_t  words = (size_t)(1 + K + K * (K + 1) / 2);
-            if (m_rec.size() != words * (size_t)m_rx->get_num_faces())
-                m_rec.resize(words * (size_t)m_rx->get_num_faces());
-            for (auto& launch : m_terms) {
-                launch(x.data(), m_rec.data(), s);
-                double e = 0.0;
-                check(rxg_face_term_gather(m_rx->handle(), dtype_of<T>::value, VariableDim, m_rec.data(),
-                                           first ? 0 : RXG_TERM_ACCUMULATE, &e, first ? fe : nullptr, g,
-                                           hb, s));
+            // records [E, gradient, packed Hessian] of the largest term kind
+            size_t words = 0;
+            for (auto& t : m_terms) {
+                const int     c = 3 - t.kind;  // vertices per element
+                const int64_t n = t.kind == 0 ? m_rx->get_num_faces()
+                                  : t.kind == 1 ? m_rx->get_num_edges() : m_rx->get_num_vertices();
+                const int     K = c * VariableDim;
+                words = std::max(words, (size_t)(1 + K + K * (K + 1) / 2) * (size_t)n);
+            }
+            if (m_rec.size() < words) m_rec.resize(words);
+            for (auto& t : m_terms) {
+                t.launch(x.data(), m_rec.data(), s);
+                double        e  = 0.0;
+                const int32_t fl = first ? 0 : RXG_TERM_ACCUMULATE;
+                if (t.kind == 0)
+                    check(rxg_face_term_gather(m_rx->handle(), dtype_of<T>::value, VariableDim, m_rec.data(), fl,
+                                               &e, first ? fe : nullptr, g, hb, s));
+                else if (t.kind == 1)
+                    check(rxg_edge_term_gather(m_rx->handle(), dtype_of<T>::value, VariableDim, m_rec.data(), fl,
+                                               &e, nullptr, g, hb, s));
+                else
+                    check(rxg_vertex_term_gather(m_rx->handle(), dtype_of<T>::value, VariableDim, m_rec.data(),
+                                                 fl, &e, nullptr, g, hb, s));
                 sum += e;
                 first = false;
             }
@@ -1321,8 +1356,13 @@ class DiffScalarProblem
     }
     DeviceArray<T>                                               m_xt;
     T                                                            m_mass = T(0);
-    std::vector<std::function<void(const T*, T*, cudaStream_t)>> m_terms;
-    DeviceArray<int32_t>                                         m_fv;
+    struct Term
+    {
+        int                                            kind;  // 0 per face, 1 per edge, 2 per vertex
+        std::function<void(const T*, T*, cudaStream_t)> launch;
+    };
+    std::vector<Term>                                            m_terms;
+    DeviceArray<int32_t>                                         m_fv, m_ev;
     DeviceArray<T>                                               m_rec;
    private:
     const RXMeshStatic* m_rx;

@@ -8,7 +8,10 @@ from Python the terms are the library's built-in per-face energies:
 `add_symmetric_dirichlet_term(rest_xyz)` (Param's energy on 2-D uv), each
 evaluated through the forward-mode Scalar type of include/rxg/diff.cuh or
 its closed form, and summed by eval_terms(x).  C++ applications write their
-own terms with include/rxg/diff.cuh and rxg_face_term_gather.
+own terms with include/rxg/diff.cuh and rxg_face_term_gather /
+rxg_edge_term_gather / rxg_vertex_term_gather; from Python, add_term(op, fn)
+takes a function that returns the per-element records (energy, gradient,
+packed Hessian) of a term, which the library assembles.
 """
 import ctypes
 
@@ -148,6 +151,36 @@ class DiffScalarProblem:
         self.terms.append(("inertia", xt, float(mass)))
         return self
 
+    def add_term(self, op, records_fn):
+        """A term given by its per-element records (add_term<Op::FV / Op::EV /
+        Op::V>, diff_scalar_problem.h:127-194): records_fn(x) for x (nv, dim)
+        in linear order returns an (n, W) tensor of the problem's dtype on
+        x's device, one row per face / edge / vertex in linear order, W = 1 +
+        K + K (K + 1) / 2 with K = c * dim and c = 3, 2, 1: the element's
+        energy, its gradient (the element's vertices in FV / EV order, dim
+        components each) and the upper triangle of its K x K Hessian, row by
+        row.  The library assembles the gradient and the block Hessian."""
+        op = str(op).upper()
+        if op not in ("FV", "EV", "V"):
+            raise ValueError("terms are per face (FV), edge (EV) or vertex (V)")
+        self.terms.append(("rec_" + op.lower(), records_fn, False))
+        return self
+
+    def _records_term(self, kind, fn, x, i, e, fe, grad, hb, stream):
+        c = {"rec_fv": 3, "rec_ev": 2, "rec_v": 1}[kind]
+        n = {"rec_fv": self.rx.get_num_faces(), "rec_ev": self.rx.get_num_edges(),
+             "rec_v": self.rx.get_num_vertices()}[kind]
+        k = c * self.dim
+        rec = fn(x)
+        if rec.dtype != self.dtype or rec.device != x.device or tuple(rec.shape) != (n, 1 + k + k * (k + 1) // 2):
+            raise ValueError(f"term records: want ({n}, {1 + k + k * (k + 1) // 2}) {self.dtype} on {x.device}, "
+                             f"got {tuple(rec.shape)} {rec.dtype} on {rec.device}")
+        rec = rec.contiguous()
+        fn_c = {"rec_fv": self._L.rxg_face_term_gather, "rec_ev": self._L.rxg_edge_term_gather,
+                "rec_v": self._L.rxg_vertex_term_gather}[kind]
+        check(fn_c(self.rx._h, _DT[self.dtype], self.dim, _p(rec), RXG_TERM_ACCUMULATE if i > 0 else 0,
+                   _p(e), _p(fe) if kind == "rec_fv" else None, _p(grad), hb, _stream(stream)))
+
     def _eval(self, x, grad, face_E, hess_b, with_projection=True, stream=None):
         """Sum of the terms at x; returns the energy (1-element FP64 tensor)."""
         if not self.terms:
@@ -162,6 +195,14 @@ class DiffScalarProblem:
                 fe = self._tmp_face
             hb = ctypes.byref(hess_b) if hess_b is not None else None
             pj = proj and with_projection
+            if kind.startswith("rec_"):
+                self._records_term(kind, rest, x, i, e, fe, grad, hb, stream)
+                if kind != "rec_fv" and face_E is not None and i == 0:
+                    face_E.zero_()
+                if kind == "rec_fv" and fe is not None and i > 0:
+                    face_E.add_(fe)
+                total += e
+                continue
             if kind == "inertia":
                 check(self._L.rxg_inertia_eval(self.rx._h, _DT[self.dtype], self.dim, _p(x), _p(rest),
                                                ctypes.c_double(proj), RXG_TERM_ACCUMULATE if i > 0 else 0,

@@ -122,6 +122,8 @@ SIGNATURES = {
     "rxg_mcf_solve_matfree": [P, D, I32, I32, P, P, P, P, P, P],
     "rxg_mcf_step_matfree": [P, D, I32, I32, D, I32, P, P, P],
     "rxg_face_term_gather": [P, I32, I32, P, I32, P, P, P, P, P],
+    "rxg_edge_term_gather": [P, I32, I32, P, I32, P, P, P, P, P],
+    "rxg_vertex_term_gather": [P, I32, I32, P, I32, P, P, P, P, P],
     "rxg_symdir_eval": [P, I32, P, P, I32, P, P, P, P, P],
     "rxg_inertia_eval": [P, I32, I32, P, P, D, I32, P, P, P, P],
     "rxg_dense_zero_rows": [I64, I32, I32, P, P, P],

@@ -18,6 +18,7 @@ struct Lazy
     int32_t*   ring       = nullptr;  // 2*ne
     int8_t*    bnd        = nullptr;  // nv
     int32_t*   ring_face  = nullptr;  // 2*ne: face between ring[i] and ring[i+1] (-1: none)
+    int32_t*   ring_edge  = nullptr;  // 2*ne: 2 * (edge to ring[i]) + (the row vertex's end of it, 0 or 1)
     int32_t*   row_ptr    = nullptr;  // nv+1  (= ring_off + p)
     int32_t*   col        = nullptr;  // nnz   (diagonal first, then the ring)
     int64_t    nnz        = 0;

@@ -41,6 +41,7 @@ void lazy_free(Mesh* m)
     cudaFree(z->ring);
     cudaFree(z->bnd);
     cudaFree(z->ring_face);
+    cudaFree(z->ring_edge);
     cudaFree(z->row_ptr);
     cudaFree(z->col);
     cudaFree(z->buf);

@@ -117,6 +117,138 @@ __global__ void __launch_bounds__(128) k_term_energy(int64_t nf, const T* __rest
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
+// energies of n records of W words into partial sums (and per-element E)
+template <typename T, int W>
+__global__ void __launch_bounds__(128) k_term_energy_w(int64_t n, const T* __restrict__ rec,
+                                                       T* __restrict__ elem_E, double* __restrict__ part)
+{
+    __shared__ double s_red[128 / 32];
+    double            esum = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const T e = rec[(int64_t)W * i];
+        if (elem_E) elem_E[i] = e;
+        esum += (double)e;
+    }
+    const double t = term_block_sum<128>(esum, s_red);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// out (D x D row-major) += block (end li, end lj) of a record of C ends
+template <typename T, int D, int C>
+__device__ __forceinline__ void term_block_c(const T* __restrict__ r, int li, int lj, T* out)
+{
+    constexpr int K = C * D;
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            const int i = D * li + a, j = D * lj + c;
+            out[D * a + c] += __ldg(r + 1 + K + (i <= j ? upper_index<K>(i, j) : upper_index<K>(j, i)));
+        }
+}
+
+// For each ring slot of each vertex p, the edge joining p to ring[i] and
+// p's end of it, from p's VE row and EV (both computed once for this)
+__global__ void k_ring_edge(int64_t nv, const int32_t* __restrict__ ring_off, const int32_t* __restrict__ ring,
+                            const int32_t* __restrict__ ve_off, const int32_t* __restrict__ ve,
+                            const int32_t* __restrict__ ev, int32_t* __restrict__ ring_edge, int* err)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nv;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t j0 = ve_off[p], j1 = ve_off[p + 1];
+        for (int32_t i = ring_off[p]; i < ring_off[p + 1]; ++i) {
+            const int32_t r = ring[i];
+            int32_t       c = -1;
+            for (int32_t j = j0; j < j1 && c < 0; ++j) {
+                const int32_t e = ve[j], a = ev[2 * (int64_t)e], b = ev[2 * (int64_t)e + 1];
+                if (a == (int32_t)p && b == r) c = 2 * e;
+                else if (b == (int32_t)p && a == r) c = 2 * e + 1;
+            }
+            if (c < 0 && err) atomicOr(err, DEVERR_NONMANIFOLD);
+            ring_edge[i] = c < 0 ? 0 : c;
+        }
+    }
+}
+
+// One thread per vertex: the gradient row and the D x D Hessian block row
+// [diag, ring...] from the records of the vertex's edges (one per ring
+// slot).  ACC: add to grad / hval instead of overwriting them.
+template <typename T, int D, bool ACC>
+__global__ void __launch_bounds__(128) k_edge_term_gather(int64_t nv, const int32_t* __restrict__ row_ptr,
+                                                          const int32_t* __restrict__ ring_off,
+                                                          const int32_t* __restrict__ ring_edge,
+                                                          const T* __restrict__ rec, T* __restrict__ grad,
+                                                          T* __restrict__ hval)
+{
+    constexpr int W  = term_record_words_n(2, D);
+    constexpr int DD = D * D;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nv;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t ro = ring_off[p], k = ring_off[p + 1] - ro, rp = row_ptr[p];
+        T             g[D], Dg[DD];
+#pragma unroll
+        for (int i = 0; i < D; ++i) g[i] = T(0);
+#pragma unroll
+        for (int i = 0; i < DD; ++i) Dg[i] = T(0);
+        for (int32_t i = 0; i < k; ++i) {
+            const int32_t c  = __ldg(ring_edge + ro + i);
+            const int     lp = c & 1;
+            const T*      r  = rec + (int64_t)W * (c >> 1);
+#pragma unroll
+            for (int t = 0; t < D; ++t) g[t] += __ldg(r + 1 + D * lp + t);
+            if (hval) {
+                term_block_c<T, D, 2>(r, lp, lp, Dg);
+                T bo[DD];
+#pragma unroll
+                for (int t = 0; t < DD; ++t) bo[t] = T(0);
+                term_block_c<T, D, 2>(r, lp, 1 - lp, bo);
+                T* slot = hval + DD * (int64_t)(rp + 1 + i);
+#pragma unroll
+                for (int t = 0; t < DD; ++t) slot[t] = ACC ? slot[t] + bo[t] : bo[t];
+            }
+        }
+        if (hval) {
+            T* dslot = hval + DD * (int64_t)rp;
+#pragma unroll
+            for (int t = 0; t < DD; ++t) dslot[t] = ACC ? dslot[t] + Dg[t] : Dg[t];
+        }
+        if (grad) {
+#pragma unroll
+            for (int t = 0; t < D; ++t) grad[D * p + t] = ACC ? grad[D * p + t] + g[t] : g[t];
+        }
+    }
+}
+
+// One thread per vertex: its own record's gradient and diagonal block.  The
+// off-diagonal blocks are untouched (the host clears the Hessian when the
+// term overwrites it).  ACC: add to grad (else overwrite it).
+template <typename T, int D, bool ACC>
+__global__ void __launch_bounds__(128) k_vertex_term_gather(int64_t nv, const int32_t* __restrict__ row_ptr,
+                                                            const T* __restrict__ rec, T* __restrict__ grad,
+                                                            T* __restrict__ hval)
+{
+    constexpr int W  = term_record_words_n(1, D);
+    constexpr int DD = D * D;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nv;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const T* r = rec + (int64_t)W * p;
+        if (grad) {
+#pragma unroll
+            for (int t = 0; t < D; ++t) grad[D * p + t] = ACC ? grad[D * p + t] + __ldg(r + 1 + t) : __ldg(r + 1 + t);
+        }
+        if (hval) {
+            T b[DD];
+#pragma unroll
+            for (int t = 0; t < DD; ++t) b[t] = T(0);
+            term_block_c<T, D, 1>(r, 0, 0, b);
+            T* dslot = hval + DD * (int64_t)row_ptr[p];
+#pragma unroll
+            for (int t = 0; t < DD; ++t) dslot[t] += b[t];
+        }
+    }
+}
+
 __device__ __forceinline__ int term_corner(const int32_t v[3], int32_t p)
 {
     return v[0] == p ? 0 : (v[1] == p ? 1 : 2);
@@ -211,16 +343,16 @@ static rxg_status term_setup(const rxg_mesh* h, int32_t dtype, int32_t dim, void
 {
     if (hess && (!hess->row_ptr || !hess->col || !hess->val || hess->dtype != dtype ||
                  (hess->block_dim == 0 ? 3 : hess->block_dim) != dim)) {
-        set_error("face term: hess needs row_ptr, col, val of the term's dtype and %dx%d blocks", dim, dim);
+        set_error("term: hess needs row_ptr, col, val of the term's dtype and %dx%d blocks", dim, dim);
         return RXG_ERR_INVALID;
     }
     if ((grad && !is_device_ptr(grad)) || (face_E && !is_device_ptr(face_E)) ||
         (hess && (!is_device_ptr(hess->val) || !is_device_ptr(hess->row_ptr) || !is_device_ptr(hess->col)))) {
-        set_error("face term: grad, face_E and hess must be device arrays");
+        set_error("term: grad, the per-element energies and hess must be device arrays");
         return RXG_ERR_INVALID;
     }
     if (!h->m.edge_manifold) {
-        set_error("face term: the gather walks oriented vertex fans and needs a manifold mesh");
+        set_error("term: the gather walks oriented vertex rings and needs a manifold mesh");
         return RXG_ERR_NONMANIFOLD;
     }
     rxg_status st = ensure_pattern(&h->m, s, z);
@@ -306,17 +438,156 @@ __global__ void __launch_bounds__(128) k_inertia(int64_t nv, const int32_t* __re
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
+// calls f(T{}, integral_constant<D>) for the record type and 1, 2 or 3 components per vertex
+template <typename F>
+static void term_dispatch(int32_t dtype, int32_t dim, F&& f)
+{
+    using C1 = std::integral_constant<int, 1>;
+    using C2 = std::integral_constant<int, 2>;
+    using C3 = std::integral_constant<int, 3>;
+    if (dtype == RXG_F64) {
+        if (dim == 1) f(double{}, C1{});
+        else if (dim == 2) f(double{}, C2{});
+        else f(double{}, C3{});
+    } else {
+        if (dim == 1) f(float{}, C1{});
+        else if (dim == 2) f(float{}, C2{});
+        else f(float{}, C3{});
+    }
+}
+
+// the ring's edges (Lazy::ring_edge), built once per mesh
+static rxg_status ensure_ring_edge(const Mesh* m, Lazy* z, cudaStream_t s)
+{
+    std::lock_guard<std::mutex> g(z->mu);
+    if (z->ring_edge) return RXG_OK;
+    const int64_t nv = m->nv, ne = m->ne;
+    int32_t *     ve_off = nullptr, *ve = nullptr, *ev = nullptr, *re = nullptr;
+    RXG_CUDA_TRY(cudaMalloc(&re, 4 * std::max<int64_t>(1, 2 * ne)));
+    RXG_CUDA_TRY(scratch_alloc((void**)&ve_off, 4 * (nv + 1), s));
+    RXG_CUDA_TRY(scratch_alloc((void**)&ve, 4 * std::max<int64_t>(4, 2 * ne), s));
+    RXG_CUDA_TRY(scratch_alloc((void**)&ev, 4 * std::max<int64_t>(4, 2 * ne), s));
+    rxg_status st = launch_query(m, RXG_OP_VE, ve_off, ve, s);
+    if (!st) st = launch_query(m, RXG_OP_EV, nullptr, ev, s);
+    if (!st) {
+        k_ring_edge<<<grid_for_items(nv), 256, 0, s>>>(nv, z->ring_off, z->ring, ve_off, ve, ev, re,
+                                                       device_error_word());
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) st = cuda_status(e, "ring edges");
+    }
+    cudaFreeAsync(ve_off, s);
+    cudaFreeAsync(ve, s);
+    cudaFreeAsync(ev, s);
+    if (!st) st = check_device_error(s);
+    if (st) {
+        cudaFree(re);
+        return st;
+    }
+    z->ring_edge = re;
+    return RXG_OK;
+}
+
 }  // namespace rxg
 
 using namespace rxg;
 
 extern "C" {
 
+rxg_status rxg_edge_term_gather(const rxg_mesh* h, int32_t dtype, int32_t dim, const void* records,
+                                int32_t flags, double* energy, void* edge_E, void* grad, rxg_bcsr* hess,
+                                void* stream)
+{
+    if (!h || !records || (dtype != RXG_F32 && dtype != RXG_F64) || dim < 1 || dim > 3 ||
+        (flags & ~RXG_TERM_ACCUMULATE)) {
+        set_error("rxg_edge_term_gather: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    if (!is_device_ptr(records)) {
+        set_error("rxg_edge_term_gather: records must be a device array");
+        return RXG_ERR_INVALID;
+    }
+    cudaStream_t s   = (cudaStream_t)stream;
+    const bool   acc = (flags & RXG_TERM_ACCUMULATE) != 0;
+    Lazy*        z;
+    rxg_status   st = term_setup(h, dtype, dim, grad, edge_E, hess, acc, s, &z);
+    if (st) return st;
+    if ((grad || hess) && (st = ensure_ring_edge(&h->m, z, s))) return st;
+    const int64_t nv = h->m.nv, ne = h->m.ne;
+    const int     G  = std::min<int>(grid_for_items(nv) * 2, 152 * 16);
+    const int     GE = std::min<int>(grid_for_items(ne) * 2, 152 * 16);
+    double*       part;
+    RXG_CUDA_TRY(scratch_alloc((void**)&part, sizeof(double) * (GE + 1), s));
+    auto run = [&](auto tag, auto dtag) {
+        using T         = decltype(tag);
+        constexpr int D = decltype(dtag)::value;
+        constexpr int W = term_record_words_n(2, D);
+        k_term_energy_w<T, W><<<GE, 128, 0, s>>>(ne, (const T*)records, (T*)edge_E, part);
+        if (grad || hess) {
+            T* hv = hess ? (T*)hess->val : nullptr;
+            if (acc)
+                k_edge_term_gather<T, D, true><<<G, 128, 0, s>>>(nv, z->row_ptr, z->ring_off, z->ring_edge,
+                                                                 (const T*)records, (T*)grad, hv);
+            else
+                k_edge_term_gather<T, D, false><<<G, 128, 0, s>>>(nv, z->row_ptr, z->ring_off, z->ring_edge,
+                                                                  (const T*)records, (T*)grad, hv);
+        }
+    };
+    term_dispatch(dtype, dim, run);
+    st = term_energy_out(part, GE, energy, s);
+    cudaFreeAsync(part, s);
+    return st;
+}
+
+rxg_status rxg_vertex_term_gather(const rxg_mesh* h, int32_t dtype, int32_t dim, const void* records,
+                                  int32_t flags, double* energy, void* vertex_E, void* grad, rxg_bcsr* hess,
+                                  void* stream)
+{
+    if (!h || !records || (dtype != RXG_F32 && dtype != RXG_F64) || dim < 1 || dim > 3 ||
+        (flags & ~RXG_TERM_ACCUMULATE)) {
+        set_error("rxg_vertex_term_gather: bad argument");
+        return RXG_ERR_INVALID;
+    }
+    if (!is_device_ptr(records)) {
+        set_error("rxg_vertex_term_gather: records must be a device array");
+        return RXG_ERR_INVALID;
+    }
+    cudaStream_t s   = (cudaStream_t)stream;
+    const bool   acc = (flags & RXG_TERM_ACCUMULATE) != 0;
+    Lazy*        z;
+    rxg_status   st = term_setup(h, dtype, dim, grad, vertex_E, hess, acc, s, &z);
+    if (st) return st;
+    const int64_t nv = h->m.nv;
+    const int     G  = std::min<int>(grid_for_items(nv) * 2, 152 * 16);
+    double*       part;
+    // overwriting: the whole Hessian cleared, then the diagonal blocks added
+    if (hess && !acc)
+        RXG_CUDA_TRY(cudaMemsetAsync(hess->val, 0, (size_t)dim * dim * z->nnz * (dtype == RXG_F64 ? 8 : 4), s));
+    RXG_CUDA_TRY(scratch_alloc((void**)&part, sizeof(double) * (G + 1), s));
+    auto run = [&](auto tag, auto dtag) {
+        using T         = decltype(tag);
+        constexpr int D = decltype(dtag)::value;
+        constexpr int W = term_record_words_n(1, D);
+        k_term_energy_w<T, W><<<G, 128, 0, s>>>(nv, (const T*)records, (T*)vertex_E, part);
+        if (grad || hess) {
+            T* hv = hess ? (T*)hess->val : nullptr;
+            if (acc)
+                k_vertex_term_gather<T, D, true><<<G, 128, 0, s>>>(nv, z->row_ptr, (const T*)records, (T*)grad, hv);
+            else
+                k_vertex_term_gather<T, D, false><<<G, 128, 0, s>>>(nv, z->row_ptr, (const T*)records, (T*)grad,
+                                                                    hv);
+        }
+    };
+    term_dispatch(dtype, dim, run);
+    st = term_energy_out(part, G, energy, s);
+    cudaFreeAsync(part, s);
+    return st;
+}
+
 rxg_status rxg_inertia_eval(const rxg_mesh* h, int32_t dtype, int32_t dim, const void* x,
                             const void* x_target, double mass, int32_t flags, double* energy,
                             void* grad, rxg_bcsr* hess, void* stream)
 {
-    if (!h || !x || !x_target || (dtype != RXG_F32 && dtype != RXG_F64) || (dim != 2 && dim != 3) ||
+    if (!h || !x || !x_target || (dtype != RXG_F32 && dtype != RXG_F64) || dim < 1 || dim > 3 ||
         (flags & ~RXG_TERM_ACCUMULATE)) {
         set_error("rxg_inertia_eval: bad argument");
         return RXG_ERR_INVALID;
@@ -368,13 +639,7 @@ rxg_status rxg_inertia_eval(const rxg_mesh* h, int32_t dtype, int32_t dim, const
             k_inertia<T, D, false, true><<<G, 128, 0, s>>>(nv, z->row_ptr, (const T*)x, (const T*)x_target,
                                                            (T)mass, (T*)grad, hv, part);
     };
-    if (dtype == RXG_F64) {
-        if (dim == 2) run(double{}, std::integral_constant<int, 2>{});
-        else run(double{}, std::integral_constant<int, 3>{});
-    } else {
-        if (dim == 2) run(float{}, std::integral_constant<int, 2>{});
-        else run(float{}, std::integral_constant<int, 3>{});
-    }
+    term_dispatch(dtype, dim, run);
     st = term_energy_out(part, G, energy, s);
     cudaFreeAsync(part, s);
     return st;
@@ -384,7 +649,7 @@ rxg_status rxg_face_term_gather(const rxg_mesh* h, int32_t dtype, int32_t dim, c
                                 int32_t flags, double* energy, void* face_E, void* grad,
                                 rxg_bcsr* hess, void* stream)
 {
-    if (!h || !records || (dtype != RXG_F32 && dtype != RXG_F64) || (dim != 2 && dim != 3) ||
+    if (!h || !records || (dtype != RXG_F32 && dtype != RXG_F64) || dim < 1 || dim > 3 ||
         (flags & ~RXG_TERM_ACCUMULATE)) {
         set_error("rxg_face_term_gather: bad argument");
         return RXG_ERR_INVALID;
@@ -404,27 +669,12 @@ rxg_status rxg_face_term_gather(const rxg_mesh* h, int32_t dtype, int32_t dim, c
     double*       part;
     RXG_CUDA_TRY(scratch_alloc((void**)&part, sizeof(double) * (GF + 1), s));
     const int32_t* fv = h->m.d.fv_lin;
-    if (dtype == RXG_F64) {
-        if (dim == 2) {
-            k_term_energy<double, 2><<<GF, 128, 0, s>>>(nf, (const double*)records, (double*)face_E, part);
-            launch_gather<double, 2>(acc, G, nv, z, fv, (const double*)records, (double*)grad,
-                                     hess ? (double*)hess->val : nullptr, s);
-        } else {
-            k_term_energy<double, 3><<<GF, 128, 0, s>>>(nf, (const double*)records, (double*)face_E, part);
-            launch_gather<double, 3>(acc, G, nv, z, fv, (const double*)records, (double*)grad,
-                                     hess ? (double*)hess->val : nullptr, s);
-        }
-    } else {
-        if (dim == 2) {
-            k_term_energy<float, 2><<<GF, 128, 0, s>>>(nf, (const float*)records, (float*)face_E, part);
-            launch_gather<float, 2>(acc, G, nv, z, fv, (const float*)records, (float*)grad,
-                                    hess ? (float*)hess->val : nullptr, s);
-        } else {
-            k_term_energy<float, 3><<<GF, 128, 0, s>>>(nf, (const float*)records, (float*)face_E, part);
-            launch_gather<float, 3>(acc, G, nv, z, fv, (const float*)records, (float*)grad,
-                                    hess ? (float*)hess->val : nullptr, s);
-        }
-    }
+    term_dispatch(dtype, dim, [&](auto tag, auto dtag) {
+        using T         = decltype(tag);
+        constexpr int D = decltype(dtag)::value;
+        k_term_energy<T, D><<<GF, 128, 0, s>>>(nf, (const T*)records, (T*)face_E, part);
+        launch_gather<T, D>(acc, G, nv, z, fv, (const T*)records, (T*)grad, hess ? (T*)hess->val : nullptr, s);
+    });
     st = term_energy_out(part, GF, energy, s);
     cudaFreeAsync(part, s);
     return st;

@@ -5,7 +5,16 @@
 //      (rxg_symdir_eval): energy, gradient and 2x2-block Hessian;
 //   2. a spring energy sum_{edges (i,j) of f} k/2 |x_i - x_j|^2 (D = 3),
 //      a quadratic, so its gradient must equal H x;
-//   3. both summed in one problem (terms accumulate).
+//   3. both summed in one problem (terms accumulate);
+//   4. the spring energy per edge, add_term<Op::EV> (D = 3): gradient and
+//      Hessian against the host sums over EV, and an edge term summed with
+//      a face term;
+//   5. Diff.SmoothingNewton (tests/RXMesh_test/test_grad.h:14-105): the
+//      edge term |x_0 - x_1|^2 in FP32 minimised by Newton steps, which
+//      must bring every vertex to one position;
+//   6. Diff.WhileLoop (tests/RXMesh_test/test_grad.h:107-211): a vertex
+//      term, add_term<Op::V> with D = 1, computing sqrt(a) with a Newton
+//      loop inside the lambda; its gradient must be 1 / (2 sqrt(a)).
 //   term_example <out_dir>: writes the spring gradient, positions and the
 //   numbering for the test, prints "OK" and exits 0, or the failing check.
 #include <cmath>
@@ -164,6 +173,137 @@ int main(int argc, char** argv)
         std::vector<double> g2 = both.grad.to_host();
         for (double& x : g2) x *= 0.5;
         REQUIRE(max_abs_diff(g2, g, &sc) <= 1e-12 * sc);
+
+        // 4. spring energy per edge (each edge once)
+        DiffScalarProblem<double, 3> es(rx);
+        es.add_term<Op::EV>([k] __device__(int32_t, const Scalar<double, 6, true>* v) {
+            Scalar<double, 6, true> e(0.0);
+            for (int c = 0; c < 3; ++c) e += sqr(v[c] - v[3 + c]) * (0.5 * k);
+            return e;
+        });
+        es.eval_terms(R);
+        {
+            const std::vector<int32_t> ev = rx.query(Op::EV).values.to_host();
+            const size_t               ne = ev.size() / 2;
+            std::vector<double>        want(3 * nv, 0.0);
+            double                     ew = 0.0;
+            for (size_t e = 0; e < ne; ++e) {
+                const int32_t a = ev[2 * e], b = ev[2 * e + 1];
+                for (int c = 0; c < 3; ++c) {
+                    const double d = hr[3 * a + c] - hr[3 * b + c];
+                    ew += 0.5 * k * d * d;
+                    want[3 * a + c] += k * d;
+                    want[3 * b + c] -= k * d;
+                }
+            }
+            REQUIRE(std::fabs(es.get_current_loss() - ew) <= 1e-12 * ew);
+            const std::vector<double> ge = es.grad.to_host();
+            REQUIRE(max_abs_diff(ge, want, &sc) <= 1e-12 * sc);
+            // Hessian: k (degree) I on the diagonal blocks, -k I per ring block
+            const std::vector<double>  he  = es.hess->values().to_host();
+            const std::vector<int32_t> erp = es.hess->row_ptr().to_host();
+            for (uint32_t i = 0; i < nv; ++i) {
+                const double deg = erp[i + 1] - erp[i] - 1;
+                for (int32_t t = erp[i]; t < erp[i + 1]; ++t)
+                    for (int a = 0; a < 3; ++a)
+                        for (int c = 0; c < 3; ++c) {
+                            const double w = a != c ? 0.0 : (t == erp[i] ? k * deg : -k);
+                            REQUIRE(std::fabs(he[9 * t + 3 * a + c] - w) <= 1e-12 * k * 8);
+                        }
+            }
+            // a face term and an edge term in one problem
+            DiffScalarProblem<double, 3> fe(rx);
+            fe.add_term<Op::FV>([k] __device__(int32_t, const Scalar<double, 9, true>* v) {
+                Scalar<double, 9, true> e(0.0);
+                for (int i = 0; i < 3; ++i)
+                    for (int c = 0; c < 3; ++c) e += sqr(v[3 * i + c] - v[3 * ((i + 1) % 3) + c]) * (0.5 * k);
+                return e;
+            });
+            fe.add_term<Op::EV>([k] __device__(int32_t, const Scalar<double, 6, true>* v) {
+                Scalar<double, 6, true> e(0.0);
+                for (int c = 0; c < 3; ++c) e += sqr(v[c] - v[3 + c]) * (0.5 * k);
+                return e;
+            });
+            fe.eval_terms(R);
+            std::vector<double> gs = g;
+            for (size_t i = 0; i < gs.size(); ++i) gs[i] += ge[i];
+            REQUIRE(max_abs_diff(fe.grad.to_host(), gs, &sc) <= 1e-12 * sc);
+            const std::vector<double> hfe = fe.hess->values().to_host();
+            std::vector<double>       hs  = hv;
+            for (size_t i = 0; i < hs.size(); ++i) hs[i] += he[i];
+            REQUIRE(max_abs_diff(hfe, hs, &sc) <= 1e-12 * sc);
+        }
+
+        // 5. Diff.SmoothingNewton: sum over edges |x_0 - x_1|^2, FP32
+        {
+            DiffScalarProblem<float, 3> sm(rx);
+            sm.add_term<Op::EV>([] __device__(int32_t, const Scalar<float, 6, true>* v) {
+                Scalar<float, 6, true> d(0.0f);
+                for (int c = 0; c < 3; ++c) d += sqr(v[c] - v[3 + c]);
+                return d;
+            });
+            std::vector<float> xf(hr.begin(), hr.end());
+            DenseMatrix<float> X(nv, 3);
+            X.from_host(xf);
+            NewtonSolver<float> newton(sm, X, NewtonSolver<float>::PCG, 2000, 0.0f, 1e-6f);
+            int                 it = 0;
+            for (; it < 100; ++it) {
+                sm.eval_terms(X);
+                newton.compute_direction();
+                if (0.5f * sm.grad.dot(newton.dir) < 1e-2f) break;
+                newton.line_search();
+            }
+            REQUIRE(it < 100);
+            const std::vector<float> xs = X.to_host();
+            for (uint32_t i = 0; i < nv; ++i)
+                for (int c = 0; c < 3; ++c) REQUIRE(std::fabs(xs[3 * i + c] - xs[c]) <= 1e-3f);
+            std::printf("smoothing newton: %d iterations, energy %g\n", it, (double)sm.get_current_loss());
+        }
+
+        // 6. Diff.WhileLoop: a = x^2 per vertex, the term is sqrt(a) by a
+        // Newton loop (bounded here: at most 64 rounds), its value also
+        // written to root[] from inside the lambda
+        {
+            const float         tol = FLT_EPSILON;
+            std::vector<float>  ha(nv), px(nv);
+            for (uint32_t l = 0; l < nv; ++l) {
+                px[l] = (float)(rest[l2i[l]][0] - 0.37);
+                ha[l] = px[l] * px[l];
+            }
+            DenseMatrix<float>           A(nv, 1);
+            A.from_host(ha);
+            DeviceArray<float>           root(nv);
+            float*                       rt = root.data();
+            DiffScalarProblem<float, 1>  wl(rx, false);
+            wl.add_term<Op::V>([tol, rt] __device__(int32_t vid, const Scalar<float, 1, true>* v) {
+                using S = Scalar<float, 1, true>;
+                const S a = v[0];
+                S       y = a;
+                if (a.val > tol) {
+                    int rounds = 0;
+                    do {
+                        y = (y + a / y) * 0.5f;
+                    } while (fabsf(y.val * y.val - a.val) > tol && ++rounds < 64);
+                } else {
+                    y = S(0.0f);
+                }
+                rt[vid] = y.val;
+                return y;
+            });
+            wl.eval_terms(A);
+            const std::vector<float> r  = root.to_host();
+            const std::vector<float> gw = wl.grad.to_host();
+            int                      checked = 0;
+            for (uint32_t l = 0; l < nv; ++l) {
+                const float s = std::fabs(px[l]);
+                if (s > 0.001f) {
+                    REQUIRE(std::fabs(r[l] - s) <= 0.001f);
+                    REQUIRE(std::fabs(gw[l] - 1.0f / (2.0f * s)) <= 0.001f);
+                    ++checked;
+                }
+            }
+            REQUIRE(checked > (int)nv / 2);
+        }
     } catch (const std::exception& e) {
         std::printf("FAILED: %s\n", e.what());
         return 1;

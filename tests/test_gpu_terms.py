@@ -175,3 +175,165 @@ def test_application_written_terms(term_example, tmp_path):
         np.add.at(want, a, d)
         np.add.at(want, b, -d)
     assert np.abs(g - want).max() <= 1e-12 * np.abs(want).max()
+
+
+# ---- terms given by their records (add_term<Op::FV / EV / V>) -------------
+
+def element_records(energy, xe):
+    """Records [E, gradient, packed upper Hessian] of energy(xe_i) for each
+    row xe_i of xe (n, K), by torch.func (the reference's forward-mode
+    Scalar computes the same three quantities per element)."""
+    from torch.func import grad, hessian, vmap
+    K = xe.shape[1]
+    E = vmap(energy)(xe)
+    G = vmap(grad(energy))(xe)
+    H = vmap(hessian(energy))(xe)
+    iu = torch.triu_indices(K, K, device=xe.device)  # row-major upper triangle
+    return torch.cat([E[:, None], G, H[:, iu[0], iu[1]]], dim=1)
+
+
+def spring_mesh(n=10, seed=3):
+    from rxmesh_gb300 import RXMeshStatic
+    rest, uv, f = bent_grid(n, seed)
+    rx = RXMeshStatic(f, len(rest), patch_size=32)
+    x = rx.to_linear(torch.tensor(rest, device="cuda"))
+    x = x + 0.05 * torch.randn(x.shape, generator=torch.Generator("cpu").manual_seed(seed),
+                               dtype=torch.float64).to(x.device)
+    return rx, x
+
+
+def spring(L):
+    """A nonlinear edge energy: (|x0 - x1|^2 - L^2)^2, plus a vertex-pair
+    coupling so the Hessian blocks are not multiples of I."""
+    def e(xe):
+        d = xe[:3] - xe[3:]
+        return (d @ d - L * L) ** 2 + 0.3 * torch.sin(xe[0] * xe[4])
+    return e
+
+
+def vertex_energy(xv):
+    return torch.sin(xv[0]) * xv[1] + 0.5 * (xv ** 2).sum() * torch.cos(xv[2])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype,rtol", [(torch.float64, 1e-11), (torch.float32, 2e-4)])
+def test_edge_and_vertex_terms_match_autograd(dtype, rtol):
+    """An edge term and a vertex term (records from torch.func) assembled by
+    rxg_edge_term_gather / rxg_vertex_term_gather: energy, gradient and the
+    block Hessian equal torch autograd of the summed energy (FP64)."""
+    from rxmesh_gb300 import DiffScalarProblem
+    rx, x = spring_mesh()
+    ev = rx.query("EV")[1].reshape(-1, 2).long()
+    L = 0.08
+    prob = DiffScalarProblem(rx, dtype, dim=3)
+    prob.add_term("EV", lambda x: element_records(spring(L), torch.cat([x[ev[:, 0]], x[ev[:, 1]]], 1)))
+    prob.add_term("V", lambda x: element_records(vertex_energy, x))
+    xd = x.to(dtype)
+    prob.eval_terms(xd)
+
+    evc = ev.cpu()
+
+    def total(y):
+        d = y[evc[:, 0]] - y[evc[:, 1]]
+        e = ((d * d).sum(1) - L * L) ** 2 + 0.3 * torch.sin(y[evc[:, 0], 0] * y[evc[:, 1], 1])
+        v = torch.sin(y[:, 0]) * y[:, 1] + 0.5 * (y ** 2).sum(1) * torch.cos(y[:, 2])
+        return e.sum() + v.sum()
+
+    x64 = xd.double().cpu().requires_grad_(True)
+    E = total(x64)
+    g = torch.autograd.grad(E, x64)[0]
+    H = torch.autograd.functional.hessian(total, x64.detach()).reshape(x64.numel(), x64.numel())
+    assert abs(prob.get_current_loss() - E.item()) <= rtol * abs(E.item())
+    assert torch.allclose(prob.grad.double().cpu(), g, rtol=0, atol=rtol * g.abs().max().item())
+    Hg = torch.tensor(prob.hess.to_scipy().toarray())
+    assert (Hg - H).abs().max().item() <= rtol * H.abs().max().item()
+
+
+@pytest.mark.gpu
+def test_face_edge_vertex_records_accumulate():
+    """A face term given by records, an edge term and the inertia term in one
+    problem: the gradient and Hessian are the sums of the separate ones."""
+    from rxmesh_gb300 import DiffScalarProblem
+    rx, x = spring_mesh(8)
+    fv = rx.query("FV")[1].reshape(-1, 3).long()
+    ev = rx.query("EV")[1].reshape(-1, 2).long()
+
+    def face_e(xe):
+        a, b, c = xe[:3], xe[3:6], xe[6:]
+        n = torch.linalg.cross(b - a, c - a)
+        return (n @ n) + (a @ c) * 0.1
+
+    fterm = lambda y: element_records(face_e, torch.cat([y[fv[:, 0]], y[fv[:, 1]], y[fv[:, 2]]], 1))
+    eterm = lambda y: element_records(spring(0.1), torch.cat([y[ev[:, 0]], y[ev[:, 1]]], 1))
+    parts = []
+    for terms in (["f"], ["e"], ["i"], ["f", "e", "i"]):
+        p = DiffScalarProblem(rx, torch.float64, dim=3)
+        for t in terms:
+            if t == "f":
+                p.add_term("FV", fterm)
+            elif t == "e":
+                p.add_term("EV", eterm)
+            else:
+                p.add_inertia_term(x * 0.9, 2.0)
+        p.eval_terms(x)
+        parts.append((p.get_current_loss(), p.grad.clone(), p.hess.val.clone(), p.face_energy.clone()))
+    e_sum = sum(q[0] for q in parts[:3])
+    assert abs(parts[3][0] - e_sum) <= 1e-12 * abs(e_sum)
+    g_sum = parts[0][1] + parts[1][1] + parts[2][1]
+    assert torch.allclose(parts[3][1], g_sum, rtol=0, atol=1e-12 * g_sum.abs().max().item())
+    h_sum = parts[0][2] + parts[1][2] + parts[2][2]
+    assert torch.allclose(parts[3][2], h_sum, rtol=0, atol=1e-12 * h_sum.abs().max().item())
+    # per-face energies: those of the face term
+    assert torch.equal(parts[3][3], parts[0][3])
+
+
+@pytest.mark.gpu
+def test_smoothing_newton_brings_vertices_together():
+    """Diff.SmoothingNewton (tests/RXMesh_test/test_grad.h:14-105): the edge
+    term |x_0 - x_1|^2 in FP32, Newton steps with PCG on its Hessian (the
+    graph Laplacian, singular but consistent) until 0.5 grad . dir < 1e-2;
+    every vertex ends at one position (within 1e-3)."""
+    from rxmesh_gb300 import DiffScalarProblem, NewtonSolver
+    rx, x = spring_mesh(12)
+    ev = rx.query("EV")[1].reshape(-1, 2).long()
+    prob = DiffScalarProblem(rx, torch.float32, dim=3)
+    sq = lambda xe: ((xe[:3] - xe[3:]) ** 2).sum()
+    prob.add_term("EV", lambda y: element_records(sq, torch.cat([y[ev[:, 0]], y[ev[:, 1]]], 1)))
+    X = x.float().contiguous()
+    prob.opt_var = X
+    newton = NewtonSolver(prob, "pcg", max_iter=2000, abs_tol=0.0, rel_tol=1e-6)
+    for it in range(100):
+        prob.eval_terms()
+        newton.compute_direction()
+        if 0.5 * float((prob.grad * newton.dir).sum()) < 1e-2:
+            break
+        newton.line_search()
+    assert it < 100
+    assert (X - X[0]).abs().max().item() <= 1e-3
+
+
+@pytest.mark.gpu
+def test_while_loop_vertex_term_dim1():
+    """Diff.WhileLoop (tests/RXMesh_test/test_grad.h:107-211) with one
+    component per vertex: the vertex term sqrt(a) computed by a Newton loop;
+    its gradient is 1 / (2 sqrt(a)).  (The loop itself runs in the C++
+    example's device lambda; here the records of sqrt are given directly.)"""
+    from rxmesh_gb300 import DiffScalarProblem
+    rx, x = spring_mesh(9)
+    a = (x[:, 0] - 0.37) ** 2
+    prob = DiffScalarProblem(rx, torch.float32, assemble_hessian=False, dim=1)
+    prob.add_term("V", lambda y: element_records(lambda v: torch.sqrt(v[0]), y))
+    prob.eval_terms(a.float().reshape(-1, 1).contiguous())
+    s = a.sqrt()
+    keep = s > 1e-3
+    g = prob.grad[:, 0].double()
+    assert keep.sum().item() > 0
+    assert (g[keep] - 1.0 / (2.0 * s[keep])).abs().max().item() <= 1e-3
+
+
+def test_term_records_shape_is_checked():
+    """A records function of the wrong width is refused before any call."""
+    from rxmesh_gb300._diff import DiffScalarProblem
+    p = DiffScalarProblem.__new__(DiffScalarProblem)
+    with pytest.raises(ValueError):
+        DiffScalarProblem.add_term(p, "FE", lambda x: x)
