@@ -356,6 +356,35 @@ def run_sweep(args, torch, rx, xl, sizes):
     return per, total_ms / args.steps, clocks, outs, nrm, (flush_l2, launch)
 
 
+def run_copy_matched(torch, flush_l2, nbytes, reps=20):
+    """A device-to-device copy moving the same bytes as each workload
+    (nbytes[k] / 2 read, as many written), timed like the kernels: after an
+    L2 flush, one CUDA-event pair each, median of `reps`.  The HBM peak is a
+    copy of hundreds of MB; copies of tens of MB reach less of it (launch
+    and ramp-up latency), so this is the roofline at the kernel's own size."""
+    half = {k: (int(b) // 2 + 15) // 16 * 16 for k, b in nbytes.items()}
+    src = torch.ones(max(half.values()) // 4, dtype=torch.int32, device="cuda")
+    dst = torch.empty_like(src)
+    out = {}
+    for k, h in half.items():
+        a_src, a_dst = src[: h // 4], dst[: h // 4]
+        for _ in range(3):
+            a_dst.copy_(a_src)
+        evs = []
+        for _ in range(reps):
+            flush_l2()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            a_dst.copy_(a_src)
+            b.record()
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        ms = statistics.median([a.elapsed_time(b) for a, b in evs])
+        out[k] = {"bytes": 2 * h, "copy_us": 1e3 * ms, "copy_gbs": 2 * h / (ms * 1e-3) / 1e9}
+    return out
+
+
 def run_sweep_back_to_back(args, torch, flush_l2, launch, concurrent=False, order=None):
     """The six kernels of the sweep after one L2 flush, one event pair around
     all six: the whole sweep, including each kernel's output write-back (151
@@ -640,7 +669,7 @@ def run_matvec(torch, rx, x0l, dt):
     the positions (24 n), x and y (2 x 3 n x sizeof(T)): the weights are
     recomputed, not read."""
     from rxmesh_gb300 import mcf_matvec
-    peak, _ = peaks()
+    peak, peak_kind = peaks()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     clean = torch.ones(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     n = x0l.shape[0]
@@ -666,7 +695,7 @@ def run_matvec(torch, rx, x0l, dt):
         torch.cuda.synchronize()
         ms = statistics.median([a.elapsed_time(b) for a, b in evs])
         gbs = algo / (ms * 1e-3) / 1e9
-        out[name] = {"ms": ms, "gbs_algorithmic": gbs, "frac_of_measured_hbm": gbs / peak,
+        out[name] = {"ms": ms, "gbs_algorithmic": gbs, "frac_of_hbm_peak": gbs / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": algo}
     return out
 
@@ -675,7 +704,7 @@ def run_spmv(torch, rx, x0l, dt):
     """Y = A X (rxg_spmm, SparseMatrix::multiply) on the level-8 MCF matrix,
     3 right-hand sides, FP64 and FP32, each launch after an L2 flush."""
     from rxmesh_gb300._solvers import mcf_assemble
-    peak, _ = peaks()
+    peak, peak_kind = peaks()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     clean = torch.ones(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     out = {}
@@ -701,8 +730,10 @@ def run_spmv(torch, rx, x0l, dt):
         torch.cuda.synchronize()
         ms = statistics.median([a.elapsed_time(b) for a, b in evs])
         gbs = algo / (ms * 1e-3) / 1e9
-        out[name] = {"ms": ms, "gbs_algorithmic": gbs, "frac_of_measured_hbm": gbs / peak,
-                     "algorithmic_bytes": algo}
+        cp = run_copy_matched(torch, lambda: (flush.fill_(1.0), clean.sum()), {"c": algo})["c"]
+        out[name] = {"ms": ms, "gbs_algorithmic": gbs, "frac_of_hbm_peak": gbs / peak, "peak_source": peak_kind,
+                     "algorithmic_bytes": algo, "same_size_copy_us": cp["copy_us"],
+                     "frac_of_same_size_copy": cp["copy_us"] / (1e3 * ms)}
     return out
 
 
@@ -984,6 +1015,9 @@ def summary(line, peak_kind):
            "e2e_gbs": line["e2e"]["value"],
            "dominant_kernel": line["roofline"]["kernel"], "dominant_frac": line["roofline"]["frac"],
            "per_kernel_frac": {k: v / line["roofline"]["peak"] for k, v in line["per_kernel_gbs"].items()}}
+    sm = line.get("size_matched_copy")
+    if sm:
+        out["frac_of_same_size_copy"] = {k: v["kernel_over_copy"] for k, v in sm.items()}
     m = line.get("mcf")
     if m:
         out["mcf_steps_per_s_f64"] = m["f64"]["steps_per_s"]
@@ -991,7 +1025,8 @@ def summary(line, peak_kind):
         out["mcf_mixed_speedup"] = m["mixed_speedup_vs_f64"]
         out["mcf_rel_err_f64_10_steps"] = m["f64"]["rel_err_after_10_steps"]
         out["mcf_rel_err_mixed_10_steps"] = m["mixed"]["rel_err_after_10_steps"]
-        out["spmv_frac"] = {k: v["frac_of_measured_hbm"] for k, v in m["spmv"].items()}
+        out["spmv_frac"] = {k: v["frac_of_hbm_peak"] for k, v in m["spmv"].items()}
+        out["spmv_frac_of_same_size_copy"] = {k: v["frac_of_same_size_copy"] for k, v in m["spmv"].items()}
     b = line.get("batch")
     if b:
         out["batch_meshes_per_s"] = b["meshes_per_s"]
@@ -1194,6 +1229,11 @@ def main():
     }
     if rank == 0:
         line["edge_face_queries"] = run_edge_face_queries(args, torch, rx, (V, E, F))
+        sm = run_copy_matched(torch, fns[0], dict(cb, sweep=sweep_bytes))
+        for k in OPS:
+            sm[k]["kernel_over_copy"] = sm[k]["copy_us"] / (1e3 * avg[k])
+        sm["sweep"]["kernel_over_copy"] = sm["sweep"]["copy_us"] / (1e3 * ms)
+        line["size_matched_copy"] = sm
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
         O.build()

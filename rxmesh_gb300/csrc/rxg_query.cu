@@ -669,6 +669,7 @@ __global__ void __launch_bounds__(kQT) k_vertex_normals(const PatchHdr* __restri
         const float4   P  = s_pos[v];
         float          a0 = 0.f, a1 = 0.f, a2 = 0.f;
         const uint32_t j1 = s_off[v + 1];
+#pragma unroll 2
         for (uint32_t j = s_off[v]; j < j1; ++j) {
             const uint32_t q = s_vis[j];
             const float4   A = s_pos[q & 0xffffu], B = s_pos[q >> 16];
