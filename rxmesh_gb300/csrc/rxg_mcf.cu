@@ -396,19 +396,23 @@ __global__ void __launch_bounds__(256) k_spmm(int64_t n, const int32_t* __restri
 #pragma unroll
         for (int c = 0; c < NC; ++c) acc[c] = TACC(0);
         const int32_t e = __ldg(rp + i + 1);
-        // eight entries per round: all column/value loads, then all gathers,
-        // in flight together (MCF rows have about seven entries)
-        for (int32_t j0 = __ldg(rp + i); j0 < e; j0 += 8) {
-            int32_t cj[8];
-            TACC    v[8];
+        // seven entries per round: all column/value loads, then all gathers,
+        // in flight together.  A vertex of valence 6 (the average of a
+        // closed triangle mesh) has a row of seven entries, so most rows take
+        // one round with no padded entry: no FP64 multiply-add is spent on
+        // padding, which matters where the FP64 pipe is the bound.
+        constexpr int RW = 7;
+        for (int32_t j0 = __ldg(rp + i); j0 < e; j0 += RW) {
+            int32_t cj[RW];
+            TACC    v[RW];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
+            for (int u = 0; u < RW; ++u) {
                 const bool ok = j0 + u < e;
                 cj[u]         = ok ? __ldg(col + j0 + u) : (int32_t)i;
                 v[u]          = ok ? (TACC)__ldg(val + j0 + u) : TACC(0);
             }
 #pragma unroll
-            for (int u = 0; u < 8; ++u)
+            for (int u = 0; u < RW; ++u)
 #pragma unroll
                 for (int c = 0; c < NC; ++c) acc[c] += v[u] * (TACC)__ldg(x + (int64_t)cj[u] * NC + c);
         }
@@ -463,27 +467,29 @@ struct CGArgs
 // abort word to 0 before every launch
 static cudaError_t reset_grid_sum(unsigned* bar, cudaStream_t s) { return cudaMemsetAsync(bar, 0, 16, s); }
 
-// acc = sum_j A_ij x_j over row i, eight non-zeros per round so that all
+// acc = sum_j A_ij x_j over row i, seven non-zeros per round so that all
 // column/value loads and then all gathers of a round are in flight together
-// (rows of the MCF matrix have about seven entries).  Padding lanes read
-// row i itself with weight zero.  diag (may be null) receives A_ii.
+// (a valence-6 vertex's row of the MCF matrix has seven entries: one round,
+// no padding).  Padding lanes read row i itself with weight zero.  diag (may
+// be null) receives A_ii.
 template <typename T, int NC>
 __device__ __forceinline__ void row_spmv(const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
                                          const T* __restrict__ val, int64_t i, const T* x, T* acc,
                                          T* diag)
 {
-    const int32_t b = __ldg(rp + i), e = __ldg(rp + i + 1);
-    for (int32_t j0 = b; j0 < e; j0 += 8) {
-        int32_t cj[8];
-        T       v[8];
+    constexpr int RW = 7;
+    const int32_t b  = __ldg(rp + i), e = __ldg(rp + i + 1);
+    for (int32_t j0 = b; j0 < e; j0 += RW) {
+        int32_t cj[RW];
+        T       v[RW];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
+        for (int u = 0; u < RW; ++u) {
             const bool ok = j0 + u < e;
             cj[u]         = ok ? __ldg(col + j0 + u) : (int32_t)i;
             v[u]          = ok ? __ldg(val + j0 + u) : T(0);
         }
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
+        for (int u = 0; u < RW; ++u) {
             if (diag && j0 + u < e && cj[u] == i) *diag = v[u];
 #pragma unroll
             for (int c = 0; c < NC; ++c) acc[c] += v[u] * x[(int64_t)cj[u] * NC + c];
@@ -1345,10 +1351,12 @@ __global__ void __launch_bounds__(256) k_resid_mixed4(int64_t n, const int32_t* 
         const double     d  = diag[i];
         double           a0 = d * xi.x, a1 = d * xi.y, a2 = d * xi.z;
         const int32_t    e  = rp[i + 1];
-        for (int32_t j0 = rp[i] + 1; j0 < e; j0 += 8) {
-            Ent<float> q[8];
+        // the off-diagonal entries, six per round (a valence-6 row in one
+        // round with no padded FP64 multiply-add)
+        for (int32_t j0 = rp[i] + 1; j0 < e; j0 += 6) {
+            Ent<float> q[6];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
+            for (int u = 0; u < 6; ++u) {
                 if (j0 + u < e) {
                     q[u] = ent[j0 + u];
                 } else {
@@ -1357,7 +1365,7 @@ __global__ void __launch_bounds__(256) k_resid_mixed4(int64_t n, const int32_t* 
                 }
             }
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
+            for (int u = 0; u < 6; ++u) {
                 const double     v  = (double)q[u].val;
                 const R4<double> xv = x[q[u].col];
                 a0 += v * xv.x, a1 += v * xv.y, a2 += v * xv.z;

@@ -283,10 +283,13 @@ __device__ __forceinline__ void row_spmv4(const int32_t* __restrict__ rp, const 
                                           int64_t i, const R4<T>* x, T& ax, T& ay, T& az, T* diag)
 {
     const int32_t b = __ldg(rp + i), e = __ldg(rp + i + 1);
-    for (int32_t j0 = b; j0 < e; j0 += 8) {
-        Ent<T> q[8];
+    // seven entries per round: a valence-6 vertex's row in one round with no
+    // padded entry (no FP64 multiply-add spent on padding)
+    constexpr int RW = 7;
+    for (int32_t j0 = b; j0 < e; j0 += RW) {
+        Ent<T> q[RW];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
+        for (int u = 0; u < RW; ++u) {
             if (j0 + u < e) {
                 q[u] = ent[j0 + u];
             } else {
@@ -295,7 +298,7 @@ __device__ __forceinline__ void row_spmv4(const int32_t* __restrict__ rp, const 
             }
         }
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
+        for (int u = 0; u < RW; ++u) {
             if (diag && j0 + u < e && q[u].col == i) *diag = q[u].val;
             const R4<T> xv = x[q[u].col];
             ax += q[u].val * xv.x;
