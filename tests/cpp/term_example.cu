@@ -14,7 +14,11 @@
 //      must bring every vertex to one position;
 //   6. Diff.WhileLoop (tests/RXMesh_test/test_grad.h:107-211): a vertex
 //      term, add_term<Op::V> with D = 1, computing sqrt(a) with a Newton
-//      loop inside the lambda; its gradient must be 1 / (2 sqrt(a)).
+//      loop inside the lambda; its gradient must be 1 / (2 sqrt(a));
+//   7. NeoHookean's per-face cloth energy (apps/NeoHookean/
+//      neo_hookean_energy.h:25-69): zero with zero gradient at rest, the
+//      host's value when deformed, gradient and Hessian against central
+//      differences, unchanged by a rigid motion.
 //   term_example <out_dir>: writes the spring gradient, positions and the
 //   numbering for the test, prints "OK" and exits 0, or the failing check.
 #include <cmath>
@@ -42,6 +46,40 @@ static void dump(const std::string& path, const std::vector<T>& v)
     if (!f) throw Error(RXG_ERR_INVALID, "cannot write " + path);
     std::fwrite(v.data(), sizeof(T), v.size(), f);
     std::fclose(f);
+}
+
+// NeoHookean energy density of one face (apps/NeoHookean/
+// neo_hookean_energy.h:25-69) for T a Scalar or double: with e0 = x2 - x0,
+// e1 = x1 - x0, n their unit normal, F = [e0 e1 n] ib (ib the inverse of the
+// same matrix at rest), J = det F,
+//   E = vol h^2 (mu/2 (tr(F^T F) - 3) - mu ln J + lam/2 (ln J)^2).
+struct NeoHookeanParams
+{
+    double mu, lam, h2;
+};
+template <typename S>
+__host__ __device__ S neo_hookean(const S* v, const double* ib, double vol, NeoHookeanParams q)
+{
+    S e0[3], e1[3], n[3];
+    for (int c = 0; c < 3; ++c) {
+        e0[c] = v[6 + c] - v[c];
+        e1[c] = v[3 + c] - v[c];
+    }
+    n[0]       = e0[1] * e1[2] - e0[2] * e1[1];
+    n[1]       = e0[2] * e1[0] - e0[0] * e1[2];
+    n[2]       = e0[0] * e1[1] - e0[1] * e1[0];
+    const S nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int c = 0; c < 3; ++c) n[c] = n[c] / nn;
+    S F[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) F[3 * r + c] = e0[r] * ib[c] + e1[r] * ib[3 + c] + n[r] * ib[6 + c];
+    const S J   = F[0] * (F[4] * F[8] - F[5] * F[7]) - F[1] * (F[3] * F[8] - F[5] * F[6]) +
+                F[2] * (F[3] * F[7] - F[4] * F[6]);
+    const S lnJ = log(J);
+    S       tr  = F[0] * F[0];
+    for (int i = 1; i < 9; ++i) tr = tr + F[i] * F[i];
+    const S psi = (tr - 3.0) * (0.5 * q.mu) - lnJ * q.mu + lnJ * lnJ * (0.5 * q.lam);
+    return psi * (vol * q.h2);
 }
 
 static double max_abs_diff(const std::vector<double>& a, const std::vector<double>& b, double* scale)
@@ -303,6 +341,127 @@ int main(int argc, char** argv)
                 }
             }
             REQUIRE(checked > (int)nv / 2);
+        }
+
+        // 7. NeoHookean: rest = the bent grid R, rest frames on the host
+        {
+            const NeoHookeanParams q{2.0, 5.0, 1e-2};
+            const std::vector<int32_t> fvl = rx.query(Op::FV).values.to_host();
+            std::vector<double>        ib(9 * (size_t)nf), vol(nf);
+            for (uint32_t f = 0; f < nf; ++f) {
+                const double* x0 = &hr[3 * fvl[3 * f]];
+                const double* x1 = &hr[3 * fvl[3 * f + 1]];
+                const double* x2 = &hr[3 * fvl[3 * f + 2]];
+                double        e0[3], e1[3], n[3];
+                for (int c = 0; c < 3; ++c) {
+                    e0[c] = x2[c] - x0[c];
+                    e1[c] = x1[c] - x0[c];
+                }
+                n[0]            = e0[1] * e1[2] - e0[2] * e1[1];
+                n[1]            = e0[2] * e1[0] - e0[0] * e1[2];
+                n[2]            = e0[0] * e1[1] - e0[1] * e1[0];
+                const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+                vol[f]          = 0.5 * nn;
+                const double B[9] = {e0[0], e1[0], n[0] / nn, e0[1], e1[1], n[1] / nn, e0[2], e1[2], n[2] / nn};
+                const double d    = B[0] * (B[4] * B[8] - B[5] * B[7]) - B[1] * (B[3] * B[8] - B[5] * B[6]) +
+                                 B[2] * (B[3] * B[7] - B[4] * B[6]);
+                double* o = &ib[9 * (size_t)f];  // the inverse: adjugate / det
+                o[0]      = (B[4] * B[8] - B[5] * B[7]) / d;
+                o[1]      = (B[2] * B[7] - B[1] * B[8]) / d;
+                o[2]      = (B[1] * B[5] - B[2] * B[4]) / d;
+                o[3]      = (B[5] * B[6] - B[3] * B[8]) / d;
+                o[4]      = (B[0] * B[8] - B[2] * B[6]) / d;
+                o[5]      = (B[2] * B[3] - B[0] * B[5]) / d;
+                o[6]      = (B[3] * B[7] - B[4] * B[6]) / d;
+                o[7]      = (B[1] * B[6] - B[0] * B[7]) / d;
+                o[8]      = (B[0] * B[4] - B[1] * B[3]) / d;
+            }
+            DenseMatrix<double> IB(nf, 9), VOL(nf, 1);
+            IB.from_host(ib);
+            VOL.from_host(vol);
+            const double* ibd = IB.data();
+            const double* vd  = VOL.data();
+            DiffScalarProblem<double, 3> nh(rx);
+            nh.add_term<Op::FV>([ibd, vd, q] __device__(int32_t f, const Scalar<double, 9, true>* v) {
+                return neo_hookean(v, ibd + 9 * f, vd[f], q);
+            });
+            // at rest: zero energy and gradient
+            nh.eval_terms(R);
+            REQUIRE(std::fabs(nh.get_current_loss()) <= 1e-12);
+            const std::vector<double> g0 = nh.grad.to_host();
+            double                    gm = 0;
+            for (double x : g0) gm = std::max(gm, std::fabs(x));
+            REQUIRE(gm <= 1e-10);
+            // deformed: stretched, sheared and jittered
+            std::vector<double> xd(3 * nv);
+            for (uint32_t l = 0; l < nv; ++l) {
+                const double* X = &hr[3 * l];
+                xd[3 * l]       = 1.15 * X[0] + 0.1 * X[1] + 0.01 * std::sin(7.0 * l);
+                xd[3 * l + 1]   = 0.92 * X[1] + 0.01 * std::cos(5.0 * l);
+                xd[3 * l + 2]   = X[2] + 0.05 * X[0] * X[1];
+            }
+            auto host_energy = [&](const std::vector<double>& x) {
+                double E = 0;
+                for (uint32_t f = 0; f < nf; ++f) {
+                    double v[9];
+                    for (int k = 0; k < 3; ++k)
+                        for (int c = 0; c < 3; ++c) v[3 * k + c] = x[3 * fvl[3 * f + k] + c];
+                    E += neo_hookean<double>(v, &ib[9 * (size_t)f], vol[f], q);
+                }
+                return E;
+            };
+            DenseMatrix<double> XD(nv, 3);
+            XD.from_host(xd);
+            nh.eval_terms(XD);
+            const double Ed = nh.get_current_loss(), Eh = host_energy(xd);
+            std::printf("neo-hookean: E = %.12g (host %.12g)\n", Ed, Eh);
+            REQUIRE(Ed > 0 && std::fabs(Ed - Eh) <= 1e-10 * Eh);
+            const std::vector<double>  g   = nh.grad.to_host();
+            const std::vector<double>  hv  = nh.hess->values().to_host();
+            const std::vector<int32_t> rp  = nh.hess->row_ptr().to_host();
+            const std::vector<int32_t> col = nh.hess->col_idx().to_host();
+            // central differences along three directions
+            for (int t = 0; t < 3; ++t) {
+                std::vector<double> d(3 * nv), xp(xd), xm(xd);
+                for (size_t i = 0; i < d.size(); ++i) d[i] = std::sin(1.7 * i + 3.1 * t);
+                const double h = 1e-6;
+                for (size_t i = 0; i < d.size(); ++i) {
+                    xp[i] += h * d[i];
+                    xm[i] -= h * d[i];
+                }
+                DenseMatrix<double> XP(nv, 3), XM(nv, 3);
+                XP.from_host(xp);
+                XM.from_host(xm);
+                const double fd = (nh.eval_terms_passive(XP) - nh.eval_terms_passive(XM)) / (2 * h);
+                double       gd = 0;
+                for (size_t i = 0; i < d.size(); ++i) gd += g[i] * d[i];
+                REQUIRE(std::fabs(fd - gd) <= 1e-6 * std::fabs(gd) + 1e-12);
+                // H d against the difference of gradients
+                nh.eval_terms(XP);
+                const std::vector<double> gp = nh.grad.to_host();
+                nh.eval_terms(XM);
+                const std::vector<double> gmn = nh.grad.to_host();
+                std::vector<double>       Hd(3 * nv, 0.0), dg(3 * nv);
+                for (uint32_t i = 0; i < nv; ++i)
+                    for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
+                        for (int a = 0; a < 3; ++a)
+                            for (int c = 0; c < 3; ++c) Hd[3 * i + a] += hv[9 * k + 3 * a + c] * d[3 * col[k] + c];
+                for (size_t i = 0; i < dg.size(); ++i) dg[i] = (gp[i] - gmn[i]) / (2 * h);
+                double scale = 0;
+                REQUIRE(max_abs_diff(Hd, dg, &scale) <= 1e-5 * scale);
+            }
+            // a rigid motion leaves the energy unchanged
+            std::vector<double> xr(3 * nv);
+            const double        ca = std::cos(0.7), sa = std::sin(0.7);
+            for (uint32_t l = 0; l < nv; ++l) {
+                const double* X = &xd[3 * l];
+                xr[3 * l]       = ca * X[0] - sa * X[2] + 0.3;
+                xr[3 * l + 1]   = X[1] - 1.0;
+                xr[3 * l + 2]   = sa * X[0] + ca * X[2] + 2.0;
+            }
+            DenseMatrix<double> XR(nv, 3);
+            XR.from_host(xr);
+            REQUIRE(std::fabs(nh.eval_terms_passive(XR) - Ed) <= 1e-9 * Ed);
         }
     } catch (const std::exception& e) {
         std::printf("FAILED: %s\n", e.what());
