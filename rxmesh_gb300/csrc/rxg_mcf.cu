@@ -573,15 +573,8 @@ __device__ __forceinline__ void mcf_row(const int32_t* __restrict__ row_ptr, con
 #pragma unroll
             for (int c = 0; c < NC; ++c) xv[i][c] = x[(int64_t)id[i] * NC + c];
         }
-        area = fan_row<T, T>(
-            P, k, wrap, dt,
-            [&](int32_t i) {
-                V3<PT> r = X[0];
-#pragma unroll
-                for (int j = 1; j < 8; ++j)
-                    if (j == i) r = X[j];
-                return r;
-            },
+        area = fan_row8<T, T>(
+            P, k, wrap, dt, X,
             [&](int32_t i, T w) {
                 sumw += w;
 #pragma unroll
@@ -1694,9 +1687,18 @@ namespace rxg {
 // assembled.  The pattern is the mesh's cached [diagonal, oriented ring].
 // ---------------------------------------------------------------------
 
+// CTAs per SM the FP32 product is compiled for: its rows hold eight ring
+// positions and x rows in registers, and at one CTA-pair per SM (116
+// registers) too few warps hide the latency of its divisions and square roots
+template <typename T>
+constexpr int matvec_min_ctas()
+{
+    return sizeof(T) == 4 ? 3 : 1;
+}
+
 // out = A in (JACOBI: out = D^-1 in, D = diag(A)), row-major nv x 3
 template <typename T, bool JACOBI, typename PT>
-__global__ void __launch_bounds__(256) k_mcf_matvec(int64_t nv, const int32_t* __restrict__ rp,
+__global__ void __launch_bounds__(256, matvec_min_ctas<T>()) k_mcf_matvec(int64_t nv, const int32_t* __restrict__ rp,
                                                     const int32_t* __restrict__ col,
                                                     const int8_t* __restrict__ bnd,
                                                     const PT* __restrict__ xyz, T dt, int uniform,

@@ -161,6 +161,50 @@ __device__ __forceinline__ TB fan_row(V3<PP> Pd, int32_t k, bool wrap, T dt, Pos
     return area;
 }
 
+// fan_row for rings of at most eight neighbours whose positions are already
+// in registers (X[0..k)): the same triangles, arithmetic and order, with the
+// ring loop unrolled over the eight slots so that every X[i] and every
+// on_w(i, .) index is a compile-time constant (no run-time selection among
+// registers); only the closing triangle's r_{k-1} is selected at run time.
+template <typename T, typename TB, typename PP, typename OnW>
+__device__ __forceinline__ TB fan_row8(V3<PP> Pd, int32_t k, bool wrap, T dt, const V3<PP> (&X)[8], OnW on_w)
+{
+    TB area = TB(0);
+    if (k <= 0) return area;
+    const V3<T> P = to_t<T>(Pd);
+    V3<T>       Xt[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) Xt[i] = to_t<T>(X[i]);
+    TriTerms<T> prev{T(0), T(0), T(-1)}, last{T(0), T(0), T(-1)};
+    if (wrap) {
+        V3<T> rl = Xt[0];
+#pragma unroll
+        for (int j = 1; j < 8; ++j)
+            if (j == k - 1) rl = Xt[j];
+        last = tri_terms<T>(P, rl, Xt[0]);  // (p, r_{k-1}, r_0)
+        prev = last;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        if (i < k) {
+            const bool  has_q = wrap || i > 0, has_s = wrap || i < k - 1;
+            TriTerms<T> cur{T(0), T(0), T(-1)};
+            if (has_s) {
+                if (i + 1 < k) cur = tri_terms<T>(P, Xt[i], Xt[i < 7 ? i + 1 : 7]);
+                else cur = last;  // the closing triangle, evaluated above
+            }
+            T w = T(0);
+            if (has_q) w += prev.hb;
+            if (has_s) w += cur.ha;
+            w = (w >= T(0) ? w : T(0)) * dt;
+            on_w(i, w);
+            if (has_q) area += prev.va > T(0) ? (TB)prev.va : TB(0);
+            prev = cur;
+        }
+    }
+    return area;
+}
+
 __device__ __forceinline__ V3<float> tof(V3<double> a)
 {
     return {(float)a.x, (float)a.y, (float)a.z};
