@@ -476,7 +476,8 @@ def run_fused(args, torch, rx, xl32, flush_l2):
     return statistics.mean(a.elapsed_time(b) for a, b in evs)
 
 
-E2E_MODES = {"sync": None, "async": 1, "direct": 2}  # rxg_query / rxg_query_ex(RXG_HOST_ASYNC / _DIRECT)
+# rxg_query / rxg_query_ex(RXG_HOST_ASYNC / _DIRECT) / one rxg_query_sweep_ex(RXG_HOST_ASYNC) call
+E2E_MODES = {"sync": None, "async": 1, "direct": 2, "sweep_ex": "sweep_ex"}
 
 
 def run_e2e(args, torch, rx, x_in_host, sizes):
@@ -486,7 +487,9 @@ def run_e2e(args, torch, rx, x_in_host, sizes):
     "sync" calls rxg_query / rxg_vertex_normals one after another (each
     returns with its results on the host); "async" and "direct" issue the
     six rxg_query_ex / rxg_vertex_normals_ex calls on six streams and wait
-    for all of them.  Returns ({mode: ms per step}, h2d, d2h)."""
+    for all of them; "sweep_ex" makes one rxg_query_sweep_ex call (the six
+    kernels on the mesh's streams, each result copied out as soon as its
+    kernel ends) and waits for it.  Returns ({mode: ms per step}, h2d, d2h)."""
     import ctypes
     from rxmesh_gb300 import Op, _lib
     L = _lib.load()
@@ -508,8 +511,20 @@ def run_e2e(args, torch, rx, x_in_host, sizes):
     streams = [torch.cuda.Stream() for _ in range(len(names) + 1)]
     ptr = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
+    so = _lib.SweepOut()
+    for name in names:
+        off, val = host[name]
+        if off is not None:
+            setattr(so, name.lower() + "_offsets", off.data_ptr())
+        setattr(so, name.lower() + "_values", val.data_ptr())
+    so.xyz, so.normals, so.weighting = xh.data_ptr(), nh.data_ptr(), 1
+
     def sweep(flags):
         cur = torch.cuda.current_stream()
+        if flags == "sweep_ex":
+            _lib.check(L.rxg_query_sweep_ex(rx._h, ctypes.byref(so), 1, ctypes.c_void_p(cur.cuda_stream)))
+            cur.synchronize()  # the step's results are on the host
+            return
         if flags is None:
             for name in names:
                 off, val = host[name]

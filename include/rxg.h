@@ -285,6 +285,16 @@ typedef struct rxg_sweep_out {
     int32_t  weighting;  /* RXG_NORMAL_MAX or RXG_NORMAL_AREA */
 } rxg_sweep_out;
 rxg_status rxg_query_sweep(const rxg_mesh* m, const rxg_sweep_out* out, void* stream);
+/*
+ * The same outputs with flags = RXG_HOST_ASYNC: every array (and xyz) may
+ * be device memory or page-locked host memory, and the call is stream
+ * ordered (it returns at once; the host arrays hold the results when
+ * `stream` reaches that point).  The queries then run as separate kernels
+ * on the mesh's own streams, quickest first and at the highest priority,
+ * and each host result is copied out as soon as its kernel ends, so the
+ * host link starts early and stays busy.  flags = 0: rxg_query_sweep.
+ */
+rxg_status rxg_query_sweep_ex(const rxg_mesh* m, const rxg_sweep_out* out, int32_t flags, void* stream);
 
 /*
  * Oriented VV (Query::dispatch<Op::VV>(..., oriented=true),

@@ -323,31 +323,38 @@ class RXMeshStatic:
         return offsets, values
 
     def query_sweep(self, ops=("VV", "VE", "VF", "FV", "EV", "normals"), xyz=None, weighting="area",
-                    stream=None, out=None):
+                    stream=None, out=None, host=False):
         """Several queries (VV, VE, VF, FV, EV) and vertex normals in one
         launch (rxg_query_sweep): a dict op -> (offsets, values) for the CSR
         ops, values for FV / EV, the (nv, 3) normals for "normals" (which
         needs linear-order FP32 positions xyz).  out: the same dict of
-        preallocated device tensors, to write into."""
-        dev = torch.device("cuda", torch.cuda.current_device())
+        preallocated tensors, to write into.  host=True: the results go to
+        page-locked host tensors (allocated here unless given in out; xyz may
+        be a page-locked host tensor too) through rxg_query_sweep_ex, stream
+        ordered: they hold the results once `stream` has run up to this call."""
+        dev = torch.device("cuda", torch.cuda.current_device()) if not host else None
+
+        def empty(n, dtype):
+            return torch.empty(n, dtype=dtype, device=dev) if not host else \
+                torch.empty(n, dtype=dtype).pin_memory()
         res = {} if out is None else dict(out)
         so = _lib.SweepOut()
         for name in ops:
             if name == "normals":
-                if xyz is None or xyz.dtype != torch.float32 or not xyz.is_cuda:
-                    raise ValueError("normals need CUDA float32 positions xyz (nv, 3)")
+                if xyz is None or xyz.dtype != torch.float32 or (not xyz.is_cuda and not host):
+                    raise ValueError("normals need float32 positions xyz (nv, 3), on the GPU (or "
+                                     "page-locked with host=True)")
                 xyz = xyz.contiguous()
                 if name not in res:
-                    res[name] = torch.empty_like(xyz)
+                    res[name] = empty(xyz.numel(), torch.float32).view(-1, 3)
                 so.xyz, so.normals = xyz.data_ptr(), res[name].data_ptr()
                 so.weighting = {"max": 0, "area": 1}[weighting] if isinstance(weighting, str) else int(weighting)
                 continue
             op = Op.NAMES[name]
             rows, nval = self.query_size(op)
             if name not in res:
-                off = torch.empty(rows + 1, dtype=torch.int32, device=dev) if op in Op.CSR else None
-                res[name] = (off, torch.empty(nval, dtype=torch.int32, device=dev)) if op in Op.CSR else \
-                    torch.empty(nval, dtype=torch.int32, device=dev)
+                res[name] = (empty(rows + 1, torch.int32), empty(nval, torch.int32)) if op in Op.CSR else \
+                    empty(nval, torch.int32)
             r = res[name]
             if op in Op.CSR:
                 setattr(so, name.lower() + "_offsets", r[0].data_ptr())
@@ -356,7 +363,10 @@ class RXMeshStatic:
                 setattr(so, name.lower() + "_values", r.data_ptr())
             else:
                 raise ValueError("query_sweep covers VV, VE, VF, FV, EV and normals, not %s" % name)
-        check(self._L.rxg_query_sweep(self._h, ctypes.byref(so), _stream(stream)))
+        if host:
+            check(self._L.rxg_query_sweep_ex(self._h, ctypes.byref(so), 1, _stream(stream)))
+        else:
+            check(self._L.rxg_query_sweep(self._h, ctypes.byref(so), _stream(stream)))
         return res
 
     def query_oriented_vv(self, stream=None):

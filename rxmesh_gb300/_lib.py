@@ -129,6 +129,7 @@ SIGNATURES = {
     "rxg_dense_zero_rows": [I64, I32, I32, P, P, P],
     "rxg_query_ex": [P, I32, P, P, I32, P],
     "rxg_query_sweep": [P, P, P],
+    "rxg_query_sweep_ex": [P, P, I32, P],
     "rxg_vertex_normals_ex": [P, I32, P, P, I32, P],
 }
 _RESTYPE = {"rxg_status_string": ctypes.c_char_p, "rxg_last_error": ctypes.c_char_p,

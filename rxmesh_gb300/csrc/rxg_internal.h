@@ -114,6 +114,11 @@ struct Mesh
     mutable std::mutex   stage_mu;
     mutable cudaStream_t copy_stream = nullptr;
     mutable cudaEvent_t  copy_ev[4]  = {nullptr, nullptr, nullptr, nullptr};
+    // rxg_query_sweep_ex with host outputs: one stream per query kernel
+    // (highest priority first) and their completion events, plus the
+    // fork and join events (also under stage_mu)
+    mutable cudaStream_t sweep_streams[6] = {};
+    mutable cudaEvent_t  sweep_ev[8]      = {};
 };
 
 void compute_smem_table(Mesh& m);

@@ -649,6 +649,14 @@ static void free_device(Mesh& M)
         if (e) cudaEventDestroy(e);
         e = nullptr;
     }
+    for (cudaStream_t& q : M.sweep_streams) {
+        if (q) cudaStreamDestroy(q);
+        q = nullptr;
+    }
+    for (cudaEvent_t& e : M.sweep_ev) {
+        if (e) cudaEventDestroy(e);
+        e = nullptr;
+    }
 }
 
 }  // namespace rxg

@@ -1508,6 +1508,149 @@ rxg_status rxg_query_sweep(const rxg_mesh* h, const rxg_sweep_out* o, void* stre
                   err);
 }
 
+// The sweep's outputs in page-locked host memory (or device memory), stream
+// ordered: the six kernels run concurrently on the mesh's sweep streams,
+// the fastest first and at the highest priority, each writing into one
+// device scratch block; the mesh's copy stream moves each result to the
+// host as soon as its kernel is done, in that order, so the host link (the
+// bound of a sweep to host memory) starts early and stays busy.  Host
+// positions for the normals come in on their kernel's stream.  `stream`
+// waits for all of it; the call itself returns at once.
+rxg_status rxg_query_sweep_ex(const rxg_mesh* h, const rxg_sweep_out* o, int32_t flags, void* stream)
+{
+    if (!h || !o) {
+        set_error("rxg_query_sweep_ex: NULL argument");
+        return RXG_ERR_INVALID;
+    }
+    if (flags & ~RXG_HOST_ASYNC) {
+        set_error("rxg_query_sweep_ex: unknown flags %d", flags);
+        return RXG_ERR_INVALID;
+    }
+    if (!flags) return rxg_query_sweep(h, o, stream);
+    const Mesh& M = h->m;
+    // the outputs in launch order: the quickest kernels first
+    struct Out
+    {
+        int         op;
+        void*       off;
+        void*       val;
+        const char* name;
+    };
+    const Out outs[5] = {{RXG_OP_EV, nullptr, o->ev_values, "EV"},
+                         {RXG_OP_FV, nullptr, o->fv_values, "FV"},
+                         {RXG_OP_VV, o->vv_offsets, o->vv_values, "VV"},
+                         {RXG_OP_VE, o->ve_offsets, o->ve_values, "VE"},
+                         {RXG_OP_VF, o->vf_offsets, o->vf_values, "VF"}};
+    // every array device or page-locked host memory; CSR outputs as pairs;
+    // device value arrays 16-byte aligned (the kernels' vectorised stores)
+    auto kind_ok = [](const void* p) { return p == nullptr || is_device_ptr(p) || is_pinned_host(p); };
+    size_t off_b[5] = {}, val_b[5] = {};
+    for (int k = 0; k < 5; ++k) {
+        const Out& q   = outs[k];
+        const bool csr = q.op <= RXG_OP_VF;
+        if (csr && ((q.off == nullptr) != (q.val == nullptr))) {
+            set_error("rxg_query_sweep_ex: %s needs both offsets and values (or neither)", q.name);
+            return RXG_ERR_INVALID;
+        }
+        if (!kind_ok(q.off) || !kind_ok(q.val)) {
+            set_error("rxg_query_sweep_ex: the %s arrays must be device or page-locked host memory", q.name);
+            return RXG_ERR_INVALID;
+        }
+        if (q.val && is_device_ptr(q.val) && ((uintptr_t)q.val & 15u) != 0) {
+            set_error("rxg_query_sweep_ex: the %s values must be 16-byte aligned", q.name);
+            return RXG_ERR_INVALID;
+        }
+        int64_t rows = 0, nval = 0;
+        rxg_status st = rxg_query_size(h, q.op, &rows, &nval);
+        if (st) return st;
+        off_b[k] = csr ? (size_t)(rows + 1) * 4 : 0;
+        val_b[k] = (size_t)nval * 4;
+    }
+    if (o->normals && (!o->xyz || !kind_ok(o->xyz) || !kind_ok(o->normals) ||
+                       (o->weighting != RXG_NORMAL_MAX && o->weighting != RXG_NORMAL_AREA))) {
+        set_error("rxg_query_sweep_ex: normals need xyz and out arrays (device or page-locked host) and a "
+                  "valid weighting");
+        return RXG_ERR_INVALID;
+    }
+    // scratch: every host output and host xyz, 256-byte aligned pieces
+    auto   up     = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    auto   host   = [](const void* p) { return p != nullptr && !is_device_ptr(p); };
+    size_t scr    = 0;
+    size_t so[5], sv[5];
+    for (int k = 0; k < 5; ++k) {
+        so[k] = scr, scr += host(outs[k].off) ? up(off_b[k]) : 0;
+        sv[k] = scr, scr += host(outs[k].val) ? up(val_b[k]) : 0;
+    }
+    const size_t nb = (size_t)M.nv * 3 * sizeof(float);
+    const size_t sx = scr;
+    scr += (o->normals && host(o->xyz)) ? up(nb) : 0;
+    const size_t sn = scr;
+    scr += (o->normals && host(o->normals)) ? up(nb) : 0;
+
+    cudaStream_t                s = (cudaStream_t)stream;
+    std::lock_guard<std::mutex> lk(M.stage_mu);
+    if (!M.sweep_streams[0]) {
+        int least = 0, greatest = 0;
+        RXG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        for (int k = 0; k < 6; ++k) {
+            // greatest is the numerically lowest; step towards least
+            const int pr = greatest + k < least ? greatest + k : least;
+            RXG_CUDA_TRY(cudaStreamCreateWithPriority(&M.sweep_streams[k], cudaStreamNonBlocking, pr));
+        }
+        for (cudaEvent_t& e : M.sweep_ev) RXG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    if (!M.copy_stream) {
+        RXG_CUDA_TRY(cudaStreamCreateWithFlags(&M.copy_stream, cudaStreamNonBlocking));
+        for (cudaEvent_t& e : M.copy_ev) RXG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    char* base = nullptr;
+    if (scr) RXG_CUDA_TRY(scratch_alloc((void**)&base, scr, s));
+    cudaEvent_t fork = M.sweep_ev[6], join = M.sweep_ev[7];
+    RXG_CUDA_TRY(cudaEventRecord(fork, s));
+    RXG_CUDA_TRY(cudaStreamWaitEvent(M.copy_stream, fork, 0));
+    rxg_status st = RXG_OK;
+    for (int k = 0; k < 5 && !st; ++k) {
+        const Out& q = outs[k];
+        if (!q.val) continue;
+        cudaStream_t ks = M.sweep_streams[k];
+        RXG_CUDA_TRY(cudaStreamWaitEvent(ks, fork, 0));
+        int32_t* dof = !q.off ? nullptr : host(q.off) ? (int32_t*)(base + so[k]) : (int32_t*)q.off;
+        int32_t* dv  = host(q.val) ? (int32_t*)(base + sv[k]) : (int32_t*)q.val;
+        st           = launch_query(&M, q.op, dof, dv, ks);
+        if (st) break;
+        RXG_CUDA_TRY(cudaEventRecord(M.sweep_ev[k], ks));
+        RXG_CUDA_TRY(cudaStreamWaitEvent(s, M.sweep_ev[k], 0));
+        RXG_CUDA_TRY(cudaStreamWaitEvent(M.copy_stream, M.sweep_ev[k], 0));
+        if (host(q.off))
+            RXG_CUDA_TRY(cudaMemcpyAsync(q.off, dof, off_b[k], cudaMemcpyDeviceToHost, M.copy_stream));
+        if (host(q.val))
+            RXG_CUDA_TRY(cudaMemcpyAsync(q.val, dv, val_b[k], cudaMemcpyDeviceToHost, M.copy_stream));
+    }
+    if (!st && o->normals) {
+        cudaStream_t ks = M.sweep_streams[5];
+        RXG_CUDA_TRY(cudaStreamWaitEvent(ks, fork, 0));
+        const float* dx = o->xyz;
+        if (host(o->xyz)) {
+            RXG_CUDA_TRY(cudaMemcpyAsync(base + sx, o->xyz, nb, cudaMemcpyHostToDevice, ks));
+            dx = (const float*)(base + sx);
+        }
+        float* dn = host(o->normals) ? (float*)(base + sn) : o->normals;
+        st        = launch_normals(&M, o->weighting, dx, dn, ks, PatchRange{0, M.num_patches});
+        if (!st) {
+            RXG_CUDA_TRY(cudaEventRecord(M.sweep_ev[5], ks));
+            RXG_CUDA_TRY(cudaStreamWaitEvent(s, M.sweep_ev[5], 0));
+            RXG_CUDA_TRY(cudaStreamWaitEvent(M.copy_stream, M.sweep_ev[5], 0));
+            if (host(o->normals))
+                RXG_CUDA_TRY(cudaMemcpyAsync(o->normals, dn, nb, cudaMemcpyDeviceToHost, M.copy_stream));
+        }
+    }
+    // `stream` waits for the copies; the scratch is freed in its order
+    RXG_CUDA_TRY(cudaEventRecord(join, M.copy_stream));
+    RXG_CUDA_TRY(cudaStreamWaitEvent(s, join, 0));
+    if (base) RXG_CUDA_TRY(cudaFreeAsync(base, s));
+    return st;
+}
+
 rxg_status rxg_device_check(void* stream) { return check_device_error((cudaStream_t)stream); }
 
 rxg_status rxg_selftest_bounded_wait(void* stream)

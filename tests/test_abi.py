@@ -80,6 +80,7 @@ def test_dense_and_partition_entry_points_reject_bad_arguments(tmp_path):
     assert L.rxg_dense_zero_rows(4, 3, 1, mask.ctypes.data, x.ctypes.data, None) == 1
     assert b"device arrays" in L.rxg_last_error()
     assert L.rxg_dense_zero_rows(4, 0, 1, mask.ctypes.data, x.ctypes.data, None) == 1  # no columns
+    assert L.rxg_query_sweep_ex(None, None, 1, None) == 1
     for fn in (L.rxg_edge_term_gather, L.rxg_vertex_term_gather, L.rxg_face_term_gather):
         assert fn(None, 1, 3, x.ctypes.data, 0, None, None, None, None, None) == 1      # no mesh
     assert L.rxg_edge_term_gather(None, 1, 4, x.ctypes.data, 0, None, None, None, None, None) == 1

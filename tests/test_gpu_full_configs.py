@@ -127,6 +127,27 @@ def test_torus1024_fused_sweep_equals_queries(torus1024):
     assert torch.equal(got["normals"], rx.vertex_normals(xl, "area"))
 
 
+def test_torus1024_host_sweep_equals_queries(torus1024):
+    """rxg_query_sweep_ex into page-locked host memory on the full torus:
+    the separate queries' offsets and rows (as sets), FV, EV and normals
+    bit for bit."""
+    from rxmesh_gb300 import Op
+    x, f, rx = torus1024
+    xl = rx.to_linear(torch.tensor(np.asarray(x, np.float32), device="cuda"))
+    s = torch.cuda.Stream()
+    got = rx.query_sweep(xyz=xl.cpu().pin_memory(), weighting="area", stream=s, host=True)
+    s.synchronize()
+    for name in ("VV", "VE", "VF"):
+        off, val = rx.query(getattr(Op, name))
+        go, gv = got[name]
+        assert torch.equal(go, off.cpu()), name
+        a, b = pairs(go.numpy(), gv.numpy()), pairs(off.cpu().numpy(), val.cpu().numpy())
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), name
+    assert torch.equal(got["FV"], rx.query(Op.FV)[1].cpu())
+    assert torch.equal(got["EV"], rx.query(Op.EV)[1].cpu())
+    assert torch.equal(got["normals"], rx.vertex_normals(xl, "area").cpu())
+
+
 def test_torus1024_edge_face_queries_bit_exact(oracle, torus1024):
     """EF, FF as sets; FE, EVDiamond and EE in order, on the full torus."""
     from rxmesh_gb300 import Op
