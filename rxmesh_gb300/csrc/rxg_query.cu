@@ -1606,49 +1606,54 @@ rxg_status rxg_query_sweep_ex(const rxg_mesh* h, const rxg_sweep_out* o, int32_t
     char* base = nullptr;
     if (scr) RXG_CUDA_TRY(scratch_alloc((void**)&base, scr, s));
     cudaEvent_t fork = M.sweep_ev[6], join = M.sweep_ev[7];
-    RXG_CUDA_TRY(cudaEventRecord(fork, s));
-    RXG_CUDA_TRY(cudaStreamWaitEvent(M.copy_stream, fork, 0));
-    rxg_status st = RXG_OK;
-    for (int k = 0; k < 5 && !st; ++k) {
-        const Out& q = outs[k];
-        if (!q.val) continue;
-        cudaStream_t ks = M.sweep_streams[k];
-        RXG_CUDA_TRY(cudaStreamWaitEvent(ks, fork, 0));
-        int32_t* dof = !q.off ? nullptr : host(q.off) ? (int32_t*)(base + so[k]) : (int32_t*)q.off;
-        int32_t* dv  = host(q.val) ? (int32_t*)(base + sv[k]) : (int32_t*)q.val;
-        st           = launch_query(&M, q.op, dof, dv, ks);
-        if (st) break;
-        RXG_CUDA_TRY(cudaEventRecord(M.sweep_ev[k], ks));
-        RXG_CUDA_TRY(cudaStreamWaitEvent(s, M.sweep_ev[k], 0));
-        RXG_CUDA_TRY(cudaStreamWaitEvent(M.copy_stream, M.sweep_ev[k], 0));
-        if (host(q.off))
-            RXG_CUDA_TRY(cudaMemcpyAsync(q.off, dof, off_b[k], cudaMemcpyDeviceToHost, M.copy_stream));
-        if (host(q.val))
-            RXG_CUDA_TRY(cudaMemcpyAsync(q.val, dv, val_b[k], cudaMemcpyDeviceToHost, M.copy_stream));
-    }
-    if (!st && o->normals) {
-        cudaStream_t ks = M.sweep_streams[5];
-        RXG_CUDA_TRY(cudaStreamWaitEvent(ks, fork, 0));
-        const float* dx = o->xyz;
-        if (host(o->xyz)) {
-            RXG_CUDA_TRY(cudaMemcpyAsync(base + sx, o->xyz, nb, cudaMemcpyHostToDevice, ks));
-            dx = (const float*)(base + sx);
+    // the enqueue; whatever it returns, `stream` then joins the copy stream
+    // and frees the scratch in its order (nothing leaks on an error)
+    auto enqueue = [&]() -> rxg_status {
+        RXG_CUDA_TRY(cudaEventRecord(fork, s));
+        RXG_CUDA_TRY(cudaStreamWaitEvent(M.copy_stream, fork, 0));
+        for (int k = 0; k < 5; ++k) {
+            const Out& q = outs[k];
+            if (!q.val) continue;
+            cudaStream_t ks = M.sweep_streams[k];
+            RXG_CUDA_TRY(cudaStreamWaitEvent(ks, fork, 0));
+            int32_t*   dof = !q.off ? nullptr : host(q.off) ? (int32_t*)(base + so[k]) : (int32_t*)q.off;
+            int32_t*   dv  = host(q.val) ? (int32_t*)(base + sv[k]) : (int32_t*)q.val;
+            rxg_status st  = launch_query(&M, q.op, dof, dv, ks);
+            if (st) return st;
+            RXG_CUDA_TRY(cudaEventRecord(M.sweep_ev[k], ks));
+            RXG_CUDA_TRY(cudaStreamWaitEvent(s, M.sweep_ev[k], 0));
+            RXG_CUDA_TRY(cudaStreamWaitEvent(M.copy_stream, M.sweep_ev[k], 0));
+            if (host(q.off))
+                RXG_CUDA_TRY(cudaMemcpyAsync(q.off, dof, off_b[k], cudaMemcpyDeviceToHost, M.copy_stream));
+            if (host(q.val))
+                RXG_CUDA_TRY(cudaMemcpyAsync(q.val, dv, val_b[k], cudaMemcpyDeviceToHost, M.copy_stream));
         }
-        float* dn = host(o->normals) ? (float*)(base + sn) : o->normals;
-        st        = launch_normals(&M, o->weighting, dx, dn, ks, PatchRange{0, M.num_patches});
-        if (!st) {
+        if (o->normals) {
+            cudaStream_t ks = M.sweep_streams[5];
+            RXG_CUDA_TRY(cudaStreamWaitEvent(ks, fork, 0));
+            const float* dx = o->xyz;
+            if (host(o->xyz)) {
+                RXG_CUDA_TRY(cudaMemcpyAsync(base + sx, o->xyz, nb, cudaMemcpyHostToDevice, ks));
+                dx = (const float*)(base + sx);
+            }
+            float*     dn = host(o->normals) ? (float*)(base + sn) : o->normals;
+            rxg_status st = launch_normals(&M, o->weighting, dx, dn, ks, PatchRange{0, M.num_patches});
+            if (st) return st;
             RXG_CUDA_TRY(cudaEventRecord(M.sweep_ev[5], ks));
             RXG_CUDA_TRY(cudaStreamWaitEvent(s, M.sweep_ev[5], 0));
             RXG_CUDA_TRY(cudaStreamWaitEvent(M.copy_stream, M.sweep_ev[5], 0));
             if (host(o->normals))
                 RXG_CUDA_TRY(cudaMemcpyAsync(o->normals, dn, nb, cudaMemcpyDeviceToHost, M.copy_stream));
         }
-    }
+        return RXG_OK;
+    };
+    const rxg_status st = enqueue();
     // `stream` waits for the copies; the scratch is freed in its order
-    RXG_CUDA_TRY(cudaEventRecord(join, M.copy_stream));
-    RXG_CUDA_TRY(cudaStreamWaitEvent(s, join, 0));
-    if (base) RXG_CUDA_TRY(cudaFreeAsync(base, s));
-    return st;
+    cudaError_t e = cudaEventRecord(join, M.copy_stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, join, 0);
+    if (base && e == cudaSuccess) e = cudaFreeAsync(base, s);
+    if (st) return st;
+    return e == cudaSuccess ? RXG_OK : cuda_status(e, "rxg_query_sweep_ex join");
 }
 
 rxg_status rxg_device_check(void* stream) { return check_device_error((cudaStream_t)stream); }
