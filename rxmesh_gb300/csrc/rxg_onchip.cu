@@ -186,11 +186,29 @@ __global__ void __launch_bounds__(BT, 1) k_mcf_onchip(OnchipArgs a)
         const bool  first = sh.first != 0;
         // ---- s = A z + beta s, p = z + beta p, s . p
         float tp = 0.f;
-        for (int l = threadIdx.x; l < m; l += BT) {
-            const int64_t i = r0 + l;
-            Ent<float>    q[W];
+        // W <= 8: the next row's ELL entries are loaded before this row's
+        // gathers and arithmetic, so two rows' L2 round trips are in flight
+        // per thread (one CTA of BT threads per SM leaves few warps to hide
+        // them); the 16-slot form has no registers to spare for it
+        constexpr bool PF = W <= 8;
+        Ent<float>     qn[PF ? W : 1];
+        if (PF && (int)threadIdx.x < m) {
 #pragma unroll
-            for (int u = 0; u < W; ++u) q[u] = a.ell[u * a.n + i];
+            for (int u = 0; u < (PF ? W : 1); ++u) qn[u] = a.ell[u * a.n + r0 + threadIdx.x];
+        }
+        for (int l = threadIdx.x; l < m; l += BT) {
+            Ent<float> q[W];
+            if constexpr (PF) {
+#pragma unroll
+                for (int u = 0; u < W; ++u) q[u] = qn[u];
+                if (l + BT < m) {
+#pragma unroll
+                    for (int u = 0; u < W; ++u) qn[u] = a.ell[u * a.n + r0 + l + BT];
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < W; ++u) q[u] = a.ell[u * a.n + r0 + l];
+            }
             float ax = 0.f, ay = 0.f, az = 0.f;
 #pragma unroll
             for (int u = 0; u < W; ++u) {
