@@ -2246,26 +2246,34 @@ extern "C" rxg_status rxg_mcf_step_backward(const rxg_mesh* h, double dt, const 
     rxg_status   st = ensure_pattern(&h->m, s, &z);
     if (st) return st;
     const int64_t n = h->m.nv, nnz = z->nnz;
-    const int     Gd = cg_grid_any<double>(3, true, n);
-    const size_t  need = align256(8 * nnz) + 2 * align256(24 * n) + cg_scratch_bytes<double>(n, 3, Gd);
+    // the adjoint system is the forward step's (A symmetric): the same packed
+    // assembly and persistent FP64 Jacobi-PCG (k_cgm) as rxg_mcf_step
+    const size_t x4b  = align256(sizeof(R4<double>) * n);
+    const size_t entb = align256(sizeof(Ent<double>) * nnz);
+    const size_t need = entb + 2 * x4b + align256(24 * n) + cgm_scratch_bytes<double>(n, cgm_grid<double>(n));
     {
         std::lock_guard<std::mutex> g(z->mu);
         if ((st = mcf_buffers(z, need, s))) return st;
     }
-    uint8_t* q   = (uint8_t*)z->buf;
-    double*  val = (double*)q;
-    double*  B   = (double*)(q + align256(8 * nnz));
-    double*  lam = (double*)(q + align256(8 * nnz) + align256(24 * n));
-    uint8_t* scr = q + align256(8 * nnz) + 2 * align256(24 * n);
-    const int ga = grid_for(n);
-    k_mcf_assemble<double, Geo<double>, double><<<ga, 256, 0, s>>>(n, z->row_ptr, z->col, z->bnd,
-                                                                  x_in, dt, CsrOut<double, double>{val, B});
+    uint8_t*     q   = (uint8_t*)z->buf;
+    Ent<double>* ent = (Ent<double>*)q;
+    R4<double>*  B4  = (R4<double>*)(q + entb);
+    R4<double>*  L4  = (R4<double>*)(q + entb + x4b);
+    double*      lam = (double*)(q + entb + 2 * x4b);
+    uint8_t*     scr = q + entb + 2 * x4b + align256(24 * n);
+    const int    ga  = grid_for(n);
+    const auto   ka  = k_mcf_assemble<double, Geo<double>, double, PackedOut<double, double>>;
+    // (the assembly's right-hand side lands in B4 and is replaced by g_out)
+    ka<<<whole_wave_grid(ka, n, 256), 256, 0, s>>>(n, z->row_ptr, z->col, z->bnd, x_in, dt,
+                                                 PackedOut<double, double>{ent, B4, nullptr});
     RXG_CUDA_TRY(cudaGetLastError());
-    RXG_CUDA_TRY(cudaMemsetAsync(lam, 0, 24 * n, s));
+    k_pack3<<<ga, 256, 0, s>>>(n, g_out, B4);
+    RXG_CUDA_TRY(cudaMemsetAsync(L4, 0, sizeof(R4<double>) * n, s));
     rxg_solver_opts  o = {max_iter, 0.0, tol * tol, 1};
     rxg_solver_stats local;
-    st = cg_dispatch<double>(3, n, z->nnz, z->row_ptr, z->col, val, g_out, lam, o, &local, scr, s);
+    st = cgm_launch<double>(n, z->row_ptr, ent, B4, L4, o, &local, scr, s);
     if (st) return st;
+    k_unpack3<<<ga, 256, 0, s>>>(n, L4, lam);
     RXG_CUDA_TRY(cudaMemsetAsync(g_in, 0, 24 * n, s));
     k_mcf_backward<<<grid_for(n, 128), 128, 0, s>>>(n, z->row_ptr, z->col, z->bnd, x_in, x_out, lam,
                                                      dt, g_in);
