@@ -2111,6 +2111,16 @@ __device__ __forceinline__ Dual9 sqrt(const Dual9& a)
     for (int i = 0; i < 9; ++i) r.d[i] = a.d[i] * h;
     return r;
 }
+// x^(-1/2), derivative -x^(-3/2) / 2
+__device__ __forceinline__ Dual9 inv_sqrt(const Dual9& a)
+{
+    const double s = ::rsqrt(a.v);
+    Dual9        r(s);
+    const double h = -0.5 * s * s * s;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) r.d[i] = a.d[i] * h;
+    return r;
+}
 __device__ __forceinline__ bool operator<(const Dual9& a, const Dual9& b) { return a.v < b.v; }
 __device__ __forceinline__ bool operator>(const Dual9& a, const Dual9& b) { return a.v > b.v; }
 __device__ __forceinline__ bool operator<=(const Dual9& a, const Dual9& b) { return a.v <= b.v; }

@@ -81,15 +81,24 @@ __device__ __forceinline__ T voronoi(V3<T> p, V3<T> q, V3<T> r)
     return T(0.125) * (dot(pr, pr) * clamp_cot(dq / A) + dot(pq, pq) * clamp_cot(dr / A));
 }
 
+// 1 / sqrt(x) in one call (FP64 and FP32 reciprocal square roots)
+__device__ __forceinline__ double inv_sqrt(double x) { return ::rsqrt(x); }
+__device__ __forceinline__ float  inv_sqrt(float x) { return ::rsqrtf(x); }
+
 // The three geometry terms of fan triangle (p, a, b) (a before b around p)
 // that a row of the MCF system uses, sharing the triangle's area:
 //   ha = half_cot(p, a, b)   (edge p-a, seen from b)
 //   hb = half_cot(p, b, a)   (edge p-b, seen from a)
 //   va = voronoi(p, a, b)
-// Bit for bit the values of the three separate calls: the three areas are
-// one |cross| (a swapped cross product is its exact negation), the
-// half-cotangents' dot products are the Voronoi corner products dr and dq
-// (exact sign changes), and their divisions are the Voronoi branch's.
+// The same formulas as the three separate calls with the area's square root
+// and the two cotangent divisions replaced by one reciprocal square root of
+// |cross|^2: with il = 1 / |cross|, A = |cross|^2 il / 2 and dot / A =
+// 2 dot il (within a unit or two in the last place of the separate calls'
+// values; on GB300 each FP64 square root or division is a long sequence on
+// the FP64 pipe).  The three areas are one |cross| (a swapped cross product
+// is its exact negation) and the half-cotangents' dot products are the
+// Voronoi corner products dr and dq.  A > DBL_MIN (FLT_MIN) of the
+// separate calls holds exactly when |cross|^2 > 0.
 template <typename T>
 struct TriTerms
 {
@@ -100,10 +109,12 @@ __device__ __forceinline__ TriTerms<T> tri_terms(V3<T> p, V3<T> a, V3<T> b)
 {
     const V3<T> pq = sub(a, p), qr = sub(b, a), pr = sub(b, p);
     const V3<T> c  = cross(pq, pr);
-    const T     A  = T(0.5) * sqrt(dot(c, c));
-    if (!(A > tmin<T>())) return {T(0), T(0), T(-1)};
+    const T     cc = dot(c, c);
+    if (!(cc > T(0))) return {T(0), T(0), T(-1)};
+    const T il = inv_sqrt(cc);
+    const T A  = T(0.5) * (cc * il);
     const T dp = dot(pq, pr), dq = -dot(qr, pq), dr = dot(qr, pr);
-    const T ha = clamp_cot(dr / A), hb = clamp_cot(dq / A);
+    const T ha = clamp_cot(T(2) * (dr * il)), hb = clamp_cot(T(2) * (dq * il));
     T       va;
     if (dp < T(0)) va = T(0.25) * A;
     else if (dq < T(0) || dr < T(0)) va = T(0.125) * A;
