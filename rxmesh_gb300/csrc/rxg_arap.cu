@@ -44,6 +44,10 @@ __device__ __forceinline__ void cross3(const T* a, const T* b, T* c)
     c[2] = a[0] * b[1] - a[1] * b[0];
 }
 
+// 1 / sqrt(x), FP64 and FP32
+__device__ __forceinline__ double arap_rsqrt(double x) { return ::rsqrt(x); }
+__device__ __forceinline__ float  arap_rsqrt(float x) { return ::rsqrtf(x); }
+
 template <typename T, bool HESS>
 __device__ __forceinline__ void arap_face(const T* x9, const T* mi, T A, FaceDeriv<T>& o)
 {
@@ -65,9 +69,15 @@ __device__ __forceinline__ void arap_face(const T* x9, const T* mi, T A, FaceDer
                j2[2] * j2[2];
     T w[3];
     cross3(j1, j2, w);
-    const T d  = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-    const T q  = s + T(2) * d;
-    const T sq = sqrt(q);
+    // |w| and |q|^(1/2) with their reciprocals from one reciprocal square
+    // root each (FP64 square roots and divisions are long sequences on
+    // GB300's FP64 pipe): d = ww / sqrt(ww), sq = q / sqrt(q)
+    const T ww  = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+    const T id  = ww > T(0) ? arap_rsqrt(ww) : T(0);  // 1 / d (0 for a degenerate J)
+    const T d   = ww * id;
+    const T q   = s + T(2) * d;
+    const T isq = arap_rsqrt(q);
+    const T sq  = q * isq;
     {
         // Energy without cancellation near the rest state: with M = J^T J - I
         // and mu its eigenvalues (sigma^2 - 1), (sigma - 1)^2 equals
@@ -107,24 +117,18 @@ __device__ __forceinline__ void arap_face(const T* x9, const T* mi, T A, FaceDer
                 W[i][j + 3] = cj1[i][j];
             }
     }
-    T wh[3] = {0, 0, 0};
-    if (d > T(0)) {
-        wh[0] = w[0] / d;
-        wh[1] = w[1] / d;
-        wh[2] = w[2] / d;
-    }
-    T gq[6];
+    const T wh[3] = {w[0] * id, w[1] * id, w[2] * id};  // 0 when d = 0
+    T       gq[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
         const T gd = W[0][i] * wh[0] + W[1][i] * wh[1] + W[2][i] * wh[2];
         gq[i]      = T(2) * u[i] + T(2) * gd;
-        o.gE[i]    = A * (T(2) * u[i] - gq[i] / sq);
+        o.gE[i]    = A * (T(2) * u[i] - gq[i] * isq);
     }
     if (!HESS) return;
     // Hd = W^T P W + [[0, -[wh]x], [[wh]x, 0]],  P = (I - wh wh^T) / d
     T PW[3][6];
     if (d > T(0)) {
-        const T id = T(1) / d;
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -139,7 +143,7 @@ __device__ __forceinline__ void arap_face(const T* x9, const T* mi, T A, FaceDer
             for (int b = 0; b < 6; ++b) PW[i][b] = T(0);
     }
     const T cw[3][3] = {{0, -wh[2], wh[1]}, {wh[2], 0, -wh[0]}, {-wh[1], wh[0], 0}};
-    const T isq = T(1) / sq, c3 = T(1) / (T(2) * q * sq);
+    const T c3 = T(0.5) * isq * isq * isq;  // 1 / (2 q sq)
 #pragma unroll
     for (int a = 0; a < 6; ++a)
 #pragma unroll
