@@ -318,8 +318,14 @@ RXG_DIFF_HD void write_term_record(const Scalar<T, K, true>& e, T* rec)
 }
 
 #if defined(__CUDACC__)
+__device__ __forceinline__ double term_rsqrt(double x) { return ::rsqrt(x); }
+__device__ __forceinline__ float  term_rsqrt(float x) { return ::rsqrtf(x); }
+
 // cyclic Jacobi eigen-decomposition of the symmetric K x K matrix A (row
-// major, overwritten by its eigenvalues on the diagonal), V the eigenvectors
+// major, overwritten by its eigenvalues on the diagonal), V the eigenvectors.
+// A rotation's t = sgn(th) / (|th| + sqrt(th^2 + 1)), th = (a_qq - a_pp) /
+// (2 a_pq), is formed as sgn(th) |2 a_pq| / (|a_qq - a_pp| + hypot) (one
+// division) and c = 1 / sqrt(t^2 + 1) as one reciprocal square root.
 template <typename T, int K>
 __device__ inline void term_jacobi(T* A, T* V)
 {
@@ -336,9 +342,10 @@ __device__ inline void term_jacobi(T* A, T* V)
             for (int q = p + 1; q < K; ++q) {
                 const T apq = A[p * K + q];
                 if (apq == T(0)) continue;
-                const T th = (A[q * K + q] - A[p * K + p]) / (T(2) * apq);
-                const T t  = (th >= T(0) ? T(1) : T(-1)) / (::fabs(th) + ::sqrt(th * th + T(1)));
-                const T c = T(1) / ::sqrt(t * t + T(1)), sn = t * c;
+                const T    dl  = A[q * K + q] - A[p * K + p], tw = T(2) * apq;
+                const bool pos = dl == T(0) || ((dl > T(0)) == (tw > T(0)));  // th >= 0
+                const T    t   = (pos ? ::fabs(tw) : -::fabs(tw)) / (::fabs(dl) + ::sqrt(dl * dl + tw * tw));
+                const T    c = term_rsqrt(t * t + T(1)), sn = t * c;
                 for (int r = 0; r < K; ++r) {
                     const T arp = A[r * K + p], arq = A[r * K + q];
                     A[r * K + p] = c * arp - sn * arq;

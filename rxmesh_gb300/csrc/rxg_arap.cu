@@ -488,7 +488,9 @@ __global__ void __launch_bounds__(128) k_arap_gather(
 // Van Loan, Matrix Computations, sec. 8.5): A (row-major) is rotated until
 // its off-diagonal part vanishes, leaving the eigenvalues on its diagonal;
 // V receives the eigenvectors as columns.  Each rotation zeroes A[p][q] with
-// t = sgn(th) / (|th| + sqrt(th^2 + 1)), th = (A[q][q] - A[p][p]) / (2 A[p][q]).
+// t = sgn(th) / (|th| + sqrt(th^2 + 1)), th = (A[q][q] - A[p][p]) / (2 A[p][q]),
+// formed as sgn(th) |2 A[p][q]| / (|A[q][q] - A[p][p]| + hypot) (the same t
+// with one division) and c = 1 / sqrt(t^2 + 1) as one reciprocal square root.
 template <typename T, int K>
 __device__ void jacobi_eigen(T* A, T* V)
 {
@@ -507,9 +509,10 @@ __device__ void jacobi_eigen(T* A, T* V)
             for (int q = p + 1; q < K; ++q) {
                 const T apq = A[p * K + q];
                 if (apq == T(0)) continue;
-                const T th = (A[q * K + q] - A[p * K + p]) / (T(2) * apq);
-                const T t  = (th >= T(0) ? T(1) : T(-1)) / (fabs(th) + sqrt(th * th + T(1)));
-                const T c = T(1) / sqrt(t * t + T(1)), sn = t * c;
+                const T    dl  = A[q * K + q] - A[p * K + p], tw = T(2) * apq;
+                const bool pos = dl == T(0) || ((dl > T(0)) == (tw > T(0)));  // th >= 0
+                const T    t   = (pos ? fabs(tw) : -fabs(tw)) / (fabs(dl) + sqrt(dl * dl + tw * tw));
+                const T    c = arap_rsqrt(t * t + T(1)), sn = t * c;
                 for (int r = 0; r < K; ++r) {
                     const T arp = A[r * K + p], arq = A[r * K + q];
                     A[r * K + p] = c * arp - sn * arq;
@@ -556,12 +559,12 @@ __device__ void project_face_hessian(const FaceDeriv<T>& o, T eps, T* H)
         a[v] = o.d[v][0];
         b[v] = o.d[v][1];
     }
-    const T r11 = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
-    for (int v = 0; v < 3; ++v) q[v][0] = a[v] / r11;
+    const T a2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2], i11 = arap_rsqrt(a2), r11 = a2 * i11;
+    for (int v = 0; v < 3; ++v) q[v][0] = a[v] * i11;
     const T r12 = q[0][0] * b[0] + q[1][0] * b[1] + q[2][0] * b[2];
     for (int v = 0; v < 3; ++v) b[v] -= r12 * q[v][0];
-    const T r22 = sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
-    for (int v = 0; v < 3; ++v) q[v][1] = b[v] / r22;
+    const T b2 = b[0] * b[0] + b[1] * b[1] + b[2] * b[2], i22 = arap_rsqrt(b2), r22 = b2 * i22;
+    for (int v = 0; v < 3; ++v) q[v][1] = b[v] * i22;
     const T R[2][2] = {{r11, r12}, {T(0), r22}};
     // M[(m,c),(n,e)] = sum_kl R[m][k] Hu[(k,c),(l,e)] R[n][l]
     T M[36], W[36];
