@@ -74,7 +74,8 @@ def test_sweep_on_random_partitions(seed):
     check_against_queries(rx, rng.normal(size=(nv, 3)))
 
 
-@pytest.mark.parametrize("ops", [("VE",), ("VV",), ("VF", "normals"), ("FV", "EV"), ("VE", "VF"), ("normals",)])
+@pytest.mark.parametrize("ops", [("VE",), ("VV",), ("VF", "normals"), ("FV", "EV"), ("VE", "VF"), ("normals",),
+                                 ("VF", "FV"), ("VV", "VE", "EV")])
 def test_sweep_subsets(ops):
     from rxmesh_gb300 import RXMeshStatic
     x, f = meshgen.icosphere(4)
