@@ -18,7 +18,10 @@
 //   7. NeoHookean's per-face cloth energy (apps/NeoHookean/
 //      neo_hookean_energy.h:25-69): zero with zero gradient at rest, the
 //      host's value when deformed, gradient and Hessian against central
-//      differences, unchanged by a rigid motion.
+//      differences, unchanged by a rigid motion;
+//   8. the per-face ARAP energy written with the forward-mode Scalar
+//      (E = A (s - 2 sqrt(s + 2 |j1 x j2|) + 2), the DiffScalar way) against
+//      the library's analytic ARAP term: energy, gradient and Hessian.
 //   term_example <out_dir>: writes the spring gradient, positions and the
 //   numbering for the test, prints "OK" and exits 0, or the failing check.
 #include <cmath>
@@ -462,6 +465,46 @@ int main(int argc, char** argv)
             DenseMatrix<double> XR(nv, 3);
             XR.from_host(xr);
             REQUIRE(std::fabs(nh.eval_terms_passive(XR) - Ed) <= 1e-9 * Ed);
+        }
+
+        // 8. ARAP through the forward-mode Scalar against the analytic term
+        {
+            std::vector<double> xd(3 * nv);
+            for (uint32_t l = 0; l < nv; ++l) {
+                const double* X = &hr[3 * l];
+                xd[3 * l]       = 1.12 * X[0] + 0.08 * X[1] + 0.02 * std::sin(5.0 * l);
+                xd[3 * l + 1]   = 0.93 * X[1] + 0.02 * std::cos(3.0 * l);
+                xd[3 * l + 2]   = X[2] + 0.1 * X[0] * X[1];
+            }
+            DenseMatrix<double> XD(nv, 3);
+            XD.from_host(xd);
+            DiffScalarProblem<double, 3> an(rx);
+            an.add_arap_term(R);
+            an.eval_terms(XD);
+            DiffScalarProblem<double, 3> ad(rx);
+            ad.add_term<Op::FV>([mi] __device__(int32_t f, const Scalar<double, 9, true>* v) {
+                using S         = Scalar<double, 9, true>;
+                const double* m = mi + 4 * f;  // the rest frame's inverse, row-major 2x2
+                S             j1[3], j2[3];
+                for (int c = 0; c < 3; ++c) {
+                    const S e1 = v[3 + c] - v[c], e2 = v[6 + c] - v[c];
+                    j1[c]      = e1 * m[0] + e2 * m[2];
+                    j2[c]      = e1 * m[1] + e2 * m[3];
+                }
+                S sn(0.0);
+                for (int c = 0; c < 3; ++c) sn += sqr(j1[c]) + sqr(j2[c]);
+                const S w0 = j1[1] * j2[2] - j1[2] * j2[1], w1 = j1[2] * j2[0] - j1[0] * j2[2],
+                        w2 = j1[0] * j2[1] - j1[1] * j2[0];
+                const S      d = sqrt(sqr(w0) + sqr(w1) + sqr(w2));
+                const double A = 0.5 / (m[0] * m[3] - m[1] * m[2]);
+                return (sn - 2.0 * sqrt(sn + 2.0 * d) + 2.0) * A;
+            });
+            ad.eval_terms(XD);
+            const double ea = an.get_current_loss(), eb = ad.get_current_loss();
+            std::printf("arap: analytic %.15g, forward-mode %.15g\n", ea, eb);
+            REQUIRE(ea > 0 && std::fabs(ea - eb) <= 1e-10 * ea);
+            REQUIRE(max_abs_diff(ad.grad.to_host(), an.grad.to_host(), &sc) <= 1e-9 * sc);
+            REQUIRE(max_abs_diff(ad.hess->values().to_host(), an.hess->values().to_host(), &sc) <= 1e-8 * sc);
         }
     } catch (const std::exception& e) {
         std::printf("FAILED: %s\n", e.what());

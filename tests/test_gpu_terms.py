@@ -159,6 +159,7 @@ def test_application_written_terms(term_example, tmp_path):
     (checked inside the program), and its spring energy's gradient equals
     the analytic one: sum over the faces' edges of k (x_i - x_j)."""
     r = subprocess.run([term_example, str(tmp_path)], capture_output=True, text=True, timeout=300)
+    print(r.stdout)
     assert r.returncode == 0 and r.stdout.strip().endswith("OK"), r.stdout + r.stderr
     ld = lambda n, t: np.fromfile(str(tmp_path / (n + ".bin")), dtype=t)
     g = ld("spring_grad", np.float64).reshape(-1, 3)
