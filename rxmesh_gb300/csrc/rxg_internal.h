@@ -107,7 +107,9 @@ struct Mesh
 
     int64_t device_bytes = 0;
     size_t  smem_bytes[16] = {};  // per kernel kind (query ops 0-9; 11: oriented FF; 12, 13: normals), max over patches
-    size_t  sweep_smem[8]  = {};  // rxg_query_sweep: by outputs (1 normals, 2 VV/VE, 4 VF), max over patches
+    // rxg_query_sweep: by requested outputs (bit 0 normals, 1 VV, 2 VE, 3 VF,
+    // 4 FV, 5 EV; only the slices those outputs read are counted), max over patches
+    size_t  sweep_smem[64] = {};
 
     // calls with host arrays: a copy stream and events that overlap the
     // device-to-host copy of each slice of patches with the kernel of the next

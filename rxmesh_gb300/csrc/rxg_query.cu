@@ -990,14 +990,20 @@ void compute_smem_table(Mesh& m)
         }
         m.smem_bytes[kind] = w * 4;
     }
-    for (int c = 0; c < 8; ++c) {
-        size_t w = 0;
+    // the fused sweep: the slices each set of outputs stages (as
+    // k_query_sweep lays them out) plus its counters and reused region
+    for (int c = 0; c < 64; ++c) {
+        const bool NRM = c & 1, VV = c & 2, VE = c & 4, VF = c & 8, FV = c & 16, EV = c & 32;
+        const bool VVVE = VV || VE, NEV = VVVE || VF || FV || EV, NFE = VF || FV;
+        const bool NRV = VV || FV || EV, NRE = VE;
+        size_t     w = 0;
         for (size_t p = 0; p < m.hdr.size(); ++p) {
-            const PatchHdr& h = m.hdr[p];
-            const int32_t   nw = (c & 1) ? m.nrm_off[p + 1] - m.nrm_off[p] : 0;
-            const size_t    pw = (size_t)pad4i(h.nEl) + pad4i((int32_t)fe_words(h.nFl)) + pad4i(h.nVl - h.nVo) +
-                              pad4i(h.nEl - h.nEo) + pad4i(h.nFl - h.nFo) + pad4i(h.nVo + 1 + kSpill) +
-                              sweep_big_words(h, nw, c & 1, (c & 2) != 0, (c & 4) != 0);
+            const PatchHdr& h  = m.hdr[p];
+            const int32_t   nw = NRM ? m.nrm_off[p + 1] - m.nrm_off[p] : 0;
+            const size_t    pw = (size_t)(NEV ? pad4i(h.nEl) : 0) + (NFE ? pad4i((int32_t)fe_words(h.nFl)) : 0) +
+                              (NRV ? pad4i(h.nVl - h.nVo) : 0) + (NRE ? pad4i(h.nEl - h.nEo) : 0) +
+                              (VF ? pad4i(h.nFl - h.nFo) : 0) + pad4i(h.nVo + 1 + kSpill) +
+                              sweep_big_words(h, nw, NRM, VVVE, VF);
             w = std::max(w, pw);
         }
         m.sweep_smem[c] = w * 4;
@@ -1493,8 +1499,9 @@ rxg_status rxg_query_sweep(const rxg_mesh* h, const rxg_sweep_out* o, void* stre
     a.vv_off = o->vv_offsets, a.vv_val = o->vv_values, a.ve_off = o->ve_offsets, a.ve_val = o->ve_values;
     a.vf_off = o->vf_offsets, a.vf_val = o->vf_values, a.fv_val = o->fv_values, a.ev_val = o->ev_values;
     a.xyz = o->xyz, a.nrm_out = o->normals, a.weighting = o->weighting;
-    const int c = (o->normals ? 1 : 0) | ((a.vv_val || a.ve_val) ? 2 : 0) | (a.vf_val ? 4 : 0);
-    if (!c && !a.fv_val && !a.ev_val) return RXG_OK;
+    const int c = (o->normals ? 1 : 0) | (a.vv_val ? 2 : 0) | (a.ve_val ? 4 : 0) | (a.vf_val ? 8 : 0) |
+                  (a.fv_val ? 16 : 0) | (a.ev_val ? 32 : 0);
+    if (!c) return RXG_OK;
     cudaStream_t    s    = (cudaStream_t)stream;
     const size_t    smem = M.sweep_smem[c];
     int*            err  = device_error_word();
