@@ -539,7 +539,7 @@ rxg_status rxg_batch_autotune(rxg_batch* b, double dt, int32_t nsteps, double to
 /* D x D-block CSR over the [diagonal, one-ring] pattern of
  * rxg_mcf_pattern_size (HessianSparseMatrix<T,K>,
  * diff/hessian_sparse_matrix.h:16-137); val holds nnzb row-major D x D
- * blocks.  block_dim: 2 or 3 (0 means 3). */
+ * blocks.  block_dim: 1, 2 or 3 (0 means 3). */
 typedef struct rxg_bcsr {
     int64_t  n;         /* block rows */
     int64_t  nnzb;      /* blocks */
@@ -547,7 +547,7 @@ typedef struct rxg_bcsr {
     int32_t* col;       /* device, nnzb */
     void*    val;       /* device, D*D*nnzb of dtype */
     int32_t  dtype;
-    int32_t  block_dim; /* D: 2 or 3; 0 = 3 */
+    int32_t  block_dim; /* D: 1, 2 or 3; 0 = 3 */
 } rxg_bcsr;
 
 /*

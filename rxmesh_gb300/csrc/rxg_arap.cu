@@ -1315,31 +1315,34 @@ rxg_status rxg_bcsr_to_csr(const rxg_bcsr* H, rxg_csr* out, void* stream)
         set_error("rxg_bcsr_to_csr: %lld blocks exceed 32-bit scalar indices", (long long)H->nnzb);
         return RXG_ERR_INVALID;
     }
-    const int D = H->block_dim == 2 ? 2 : 3;
-    if (H->block_dim != 0 && H->block_dim != 2 && H->block_dim != 3) {
-        set_error("rxg_bcsr_to_csr: block_dim must be 2 or 3");
+    if (H->block_dim < 0 || H->block_dim > 3) {
+        set_error("rxg_bcsr_to_csr: block_dim must be 1, 2 or 3");
         return RXG_ERR_INVALID;
     }
+    const int    D = H->block_dim == 0 ? 3 : H->block_dim;
     cudaStream_t s = (cudaStream_t)stream;
     out->n         = D * H->n;
     out->nnz       = (int64_t)D * D * H->nnzb;
     out->dtype     = H->dtype;
     if (H->n == 0) return RXG_OK;
-    const int g = grid_for_items(32 * H->n);  // one warp per block row
+    const int g   = grid_for_items(32 * H->n);  // one warp per block row
+    auto      run = [&](auto tag, auto dtag) {
+        using T         = decltype(tag);
+        constexpr int B = decltype(dtag)::value;
+        k_bcsr_expand<T, B><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const T*)H->val, out->row_ptr,
+                                                   out->col, (T*)out->val);
+    };
+    using C1 = std::integral_constant<int, 1>;
+    using C2 = std::integral_constant<int, 2>;
+    using C3 = std::integral_constant<int, 3>;
     if (H->dtype == RXG_F64) {
-        if (D == 2)
-            k_bcsr_expand<double, 2><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const double*)H->val,
-                                                       out->row_ptr, out->col, (double*)out->val);
-        else
-            k_bcsr_expand<double, 3><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const double*)H->val,
-                                                       out->row_ptr, out->col, (double*)out->val);
+        if (D == 1) run(double{}, C1{});
+        else if (D == 2) run(double{}, C2{});
+        else run(double{}, C3{});
     } else {
-        if (D == 2)
-            k_bcsr_expand<float, 2><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const float*)H->val,
-                                                      out->row_ptr, out->col, (float*)out->val);
-        else
-            k_bcsr_expand<float, 3><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (const float*)H->val,
-                                                      out->row_ptr, out->col, (float*)out->val);
+        if (D == 1) run(float{}, C1{});
+        else if (D == 2) run(float{}, C2{});
+        else run(float{}, C3{});
     }
     RXG_CUDA_TRY(cudaGetLastError());
     return RXG_OK;
@@ -1352,27 +1355,30 @@ rxg_status rxg_bcsr_apply_bc(rxg_bcsr* H, const int8_t* bc, void* grad, void* st
         set_error("rxg_bcsr_apply_bc: bad argument");
         return RXG_ERR_INVALID;
     }
-    if (H->block_dim != 0 && H->block_dim != 2 && H->block_dim != 3) {
-        set_error("rxg_bcsr_apply_bc: block_dim must be 2 or 3");
+    if (H->block_dim < 0 || H->block_dim > 3) {
+        set_error("rxg_bcsr_apply_bc: block_dim must be 1, 2 or 3");
         return RXG_ERR_INVALID;
     }
     cudaStream_t s = (cudaStream_t)stream;
     if (H->n == 0) return RXG_OK;
-    const int g = grid_for_items(H->n);
+    const int D   = H->block_dim == 0 ? 3 : H->block_dim;
+    const int g   = grid_for_items(H->n);
+    auto      run = [&](auto tag, auto dtag) {
+        using T         = decltype(tag);
+        constexpr int B = decltype(dtag)::value;
+        k_bcsr_apply_bc<T, B><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (T*)H->val, bc, (T*)grad);
+    };
+    using C1 = std::integral_constant<int, 1>;
+    using C2 = std::integral_constant<int, 2>;
+    using C3 = std::integral_constant<int, 3>;
     if (H->dtype == RXG_F64) {
-        if (H->block_dim == 2)
-            k_bcsr_apply_bc<double, 2><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (double*)H->val, bc,
-                                                         (double*)grad);
-        else
-            k_bcsr_apply_bc<double, 3><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (double*)H->val, bc,
-                                                         (double*)grad);
+        if (D == 1) run(double{}, C1{});
+        else if (D == 2) run(double{}, C2{});
+        else run(double{}, C3{});
     } else {
-        if (H->block_dim == 2)
-            k_bcsr_apply_bc<float, 2><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (float*)H->val, bc,
-                                                        (float*)grad);
-        else
-            k_bcsr_apply_bc<float, 3><<<g, 256, 0, s>>>(H->n, H->row_ptr, H->col, (float*)H->val, bc,
-                                                        (float*)grad);
+        if (D == 1) run(float{}, C1{});
+        else if (D == 2) run(float{}, C2{});
+        else run(float{}, C3{});
     }
     RXG_CUDA_TRY(cudaGetLastError());
     return RXG_OK;

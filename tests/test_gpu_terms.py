@@ -372,3 +372,40 @@ def test_diff_arap_application(diff_arap_example):
     r = subprocess.run([diff_arap_example], capture_output=True, text=True, timeout=300)
     print(r.stdout)
     assert r.returncode == 0 and r.stdout.strip().endswith("OK"), r.stdout + r.stderr
+
+
+@pytest.mark.gpu
+def test_newton_on_one_component_variable():
+    """Newton with 1x1 blocks (dim=1): the vertex term (a - t)^2 per vertex
+    plus the edge term (a0 - a1)^2 (a graph Laplacian) is quadratic, so one
+    Newton step (PCG on the scalar form of the 1x1-block Hessian) reaches
+    its minimiser: H a = t, checked against scipy; a constrained vertex
+    keeps its value (apply_bc)."""
+    import scipy.sparse.linalg as spl
+    from rxmesh_gb300 import DiffScalarProblem, NewtonSolver
+    rx, x = spring_mesh(10)
+    ev = rx.query("EV")[1].reshape(-1, 2).long()
+    t = torch.sin(3.0 * x[:, 0]) + x[:, 1]
+    prob = DiffScalarProblem(rx, torch.float64, dim=1)
+    tt = t.reshape(-1, 1)
+    prob.add_term("V", lambda y: torch.cat([((y - tt) ** 2), 2 * (y - tt), torch.full_like(y, 2.0)], 1))
+    prob.add_term("EV", lambda y: element_records(lambda e: (e[0] - e[1]) ** 2,
+                                                  torch.cat([y[ev[:, 0]], y[ev[:, 1]]], 1)))
+    a = torch.zeros(rx.get_num_vertices(), 1, dtype=torch.float64, device="cuda")
+    prob.opt_var = a
+    newton = NewtonSolver(prob, "pcg", max_iter=5000, abs_tol=0.0, rel_tol=1e-24)
+    bc = torch.zeros(rx.get_num_vertices(), dtype=torch.int8, device="cuda")
+    bc[0] = 1
+    prob.eval_terms()
+    newton.apply_bc(bc)
+    newton.compute_direction()
+    newton.line_search()
+    prob.eval_terms()
+    H = prob.hess.to_scipy().tocsr()
+    free = np.arange(1, rx.get_num_vertices())
+    want = np.zeros(rx.get_num_vertices())
+    Hf = H[free][:, free]
+    want[free] = spl.spsolve(Hf.tocsc(), 2.0 * t.cpu().numpy()[free])
+    got = a[:, 0].cpu().numpy()
+    assert got[0] == 0.0
+    assert np.abs(got - want).max() <= 1e-8 * np.abs(want).max()
