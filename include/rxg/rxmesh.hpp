@@ -1377,24 +1377,29 @@ class DiffScalarProblem
 // the scalar Hessian, or with the matrix-free CG; line_search() backtracks
 // with the Armijo test of diff/armijo_condition.h.  As in the reference,
 // compute_direction leaves grad negated and the Armijo test uses dir . grad.
-template <typename T>
+// VariableDim: the problem's components per vertex (1, 2 or 3); the
+// matrix-free CG (CG_MATFREE) is the ARAP term's, on 3 components.
+template <typename T, int VariableDim = 3>
 class NewtonSolver
 {
    public:
     enum Kind { PCG, CG, CG_MATFREE };
-    NewtonSolver(DiffScalarProblem<T>& p, DenseMatrix<T>& x, Kind kind = PCG, int max_iter = 1000,
+    NewtonSolver(DiffScalarProblem<T, VariableDim>& p, DenseMatrix<T>& x, Kind kind = PCG, int max_iter = 1000,
                  T abs_tol = T(0), T rel_tol = T(1e-6))
-        : problem(p), opt_var(x), dir(x.rows(), 3), m_tmp(x.rows(), 3), m_kind(kind),
+        : problem(p), opt_var(x), dir(x.rows(), VariableDim), m_tmp(x.rows(), VariableDim), m_kind(kind),
           m_max_iter(max_iter), m_abs_tol(abs_tol), m_rel_tol(rel_tol)
     {
         if (kind != CG_MATFREE && !p.hess) throw Error(RXG_ERR_INVALID, "the problem has no Hessian");
+        if (kind == CG_MATFREE && VariableDim != 3)
+            throw Error(RXG_ERR_INVALID, "the matrix-free CG is the ARAP term's (3 components per vertex)");
     }
     void apply_bc(const DeviceArray<int8_t>& bc, cudaStream_t s = nullptr)
     {
         m_bc = bc.data();
         if (m_kind == CG_MATFREE) {
             // no assembled Hessian: the constrained gradient rows only
-            check(rxg_dense_zero_rows((int64_t)bc.size(), 3, dtype_of<T>::value, bc.data(), problem.grad.data(), s));
+            check(rxg_dense_zero_rows((int64_t)bc.size(), VariableDim, dtype_of<T>::value, bc.data(),
+                                      problem.grad.data(), s));
         } else {
             problem.hess->apply_bc(bc.data(), &problem.grad, s);
         }
@@ -1409,7 +1414,8 @@ class NewtonSolver
             return;
         }
         if (!m_A)
-            m_A.reset(new SparseMatrix<T>(3 * problem.hess->rows(), 9 * problem.hess->non_zero_blocks()));
+            m_A.reset(new SparseMatrix<T>(VariableDim * problem.hess->rows(),
+                                          VariableDim * VariableDim * problem.hess->non_zero_blocks()));
         problem.hess->to_csr(*m_A, s);
         rxg_solver_opts o{m_max_iter, (double)m_abs_tol, (double)m_rel_tol, m_kind == PCG ? 1 : 0};
         rxg_csr         c = m_A->csr();
@@ -1438,9 +1444,9 @@ class NewtonSolver
     }
     int iter_taken() const { return m_stats.iters; }
 
-    DiffScalarProblem<T>& problem;
-    DenseMatrix<T>&       opt_var;
-    DenseMatrix<T>        dir;
+    DiffScalarProblem<T, VariableDim>& problem;
+    DenseMatrix<T>&                    opt_var;
+    DenseMatrix<T>                     dir;
 
    private:
     DenseMatrix<T>                   m_tmp;

@@ -170,6 +170,31 @@ int main(int argc, char** argv)
         });
         sdp.eval_terms(U);
         REQUIRE(std::fabs(sdp.get_current_loss() - e_ref) <= 1e-12 * e_ref);
+        // Newton on it with 2x2 blocks (NewtonSolver<double, 2>): a stretched
+        // uv relaxes, the energy falling at every step
+        {
+            std::vector<double> hs = hu;
+            for (uint32_t l = 0; l < nv; ++l) {
+                hs[2 * l] *= 1.3;
+                hs[2 * l + 1] *= 0.8;
+            }
+            DenseMatrix<double> Us(nv, 2);
+            Us.from_host(hs);
+            NewtonSolver<double, 2> nt(sdp, Us, NewtonSolver<double, 2>::PCG, 2000, 0.0, 1e-12);
+            sdp.eval_terms(Us);
+            const double e0 = sdp.get_current_loss();
+            double       ep = e0;
+            for (int it = 0; it < 4; ++it) {
+                sdp.eval_terms(Us);
+                nt.compute_direction();
+                REQUIRE(nt.line_search());
+                sdp.eval_terms(Us);
+                REQUIRE(sdp.get_current_loss() <= ep * (1 + 1e-12));
+                ep = sdp.get_current_loss();
+            }
+            std::printf("symmetric Dirichlet Newton (2x2 blocks): %.6g -> %.6g\n", e0, ep);
+            REQUIRE(ep < 0.9 * e0);
+        }
 
         // 2. spring energy on the 3-D rest positions (quadratic: grad = H x)
         const double                 k = 2.5;
